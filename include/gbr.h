@@ -1,0 +1,474 @@
+/*
+ * gbr.h — C ABI of the GB300 render-pass path (drop-in for wgpu-cpu's render-pass hot path).
+ *
+ * Every entry point below replaces one method of the wgpu 28 "custom backend" traits that
+ * wgpu-cpu implements in Rust.  The reference method is cited beside each declaration as
+ * `file:line` relative to the wgpu-cpu repository.  A Rust `wgpu::custom` shim would bind these
+ * symbols with `extern "C"` declarations (see INTEGRATION.md for the binding stubs).
+ *
+ * Conventions
+ *  - Objects are opaque 64-bit handles owned by the library; 0 is never a valid handle.
+ *  - Every call returns a gbr_status (0 = GBR_OK).  Nothing unwinds across the ABI: where the
+ *    reference panics (`todo!`, `unwrap`, `expect`), the call returns an error status and
+ *    gbr_last_error() gives the thread-local message.
+ *  - Host memory passed in is copied before the call returns; the caller keeps ownership.
+ *  - All structs are plain C, little-endian, with explicit padding so that ctypes/cgo/Rust
+ *    `#[repr(C)]` mirrors have identical layouts.
+ *  - Enum values follow the numbering of the corresponding wgpu-types enums where one exists.
+ */
+#ifndef GBR_H
+#define GBR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define GBR_API __declspec(dllexport)
+#else
+#define GBR_API __attribute__((visibility("default")))
+#endif
+
+#define GBR_ABI_VERSION 1u
+
+typedef int32_t gbr_status;
+enum {
+    GBR_OK = 0,
+    GBR_ERR_INVALID_ARGUMENT = -1, /* bad handle / null pointer / malformed descriptor        */
+    GBR_ERR_OUT_OF_MEMORY = -2,    /* device allocation failed or HBM budget exceeded        */
+    GBR_ERR_UNSUPPORTED = -3,      /* the reference has `todo!()`/panics for this feature    */
+    GBR_ERR_VALIDATION = -4,       /* the reference would panic (assert/expect/out of range) */
+    GBR_ERR_DEVICE_LOST = -5,      /* a kernel reported a fault; the device must be recreated */
+    GBR_ERR_TIMEOUT = -6,          /* gbr_device_poll ran out of time                          */
+    GBR_ERR_SHADER = -7,           /* shader parse / translate / NVRTC compile error           */
+    GBR_ERR_CUDA = -8              /* a CUDA runtime call failed                               */
+};
+
+typedef uint64_t gbr_device;
+typedef uint64_t gbr_buffer;
+typedef uint64_t gbr_texture;
+typedef uint64_t gbr_sampler;
+typedef uint64_t gbr_shader_module;
+typedef uint64_t gbr_render_pipeline;
+typedef uint64_t gbr_bind_group;
+
+/* ---------------------------------------------------------------- enums (wgpu-types numbering) */
+
+enum gbr_texture_format {
+    GBR_TEXTURE_FORMAT_UNDEFINED = 0,
+    GBR_TEXTURE_FORMAT_R8_UNORM = 1,
+    GBR_TEXTURE_FORMAT_RG8_UNORM = 2,
+    GBR_TEXTURE_FORMAT_RGBA8_UNORM = 3,
+    GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB = 4,
+    GBR_TEXTURE_FORMAT_BGRA8_UNORM = 5,
+    GBR_TEXTURE_FORMAT_BGRA8_UNORM_SRGB = 6,
+    GBR_TEXTURE_FORMAT_RGBA16_FLOAT = 7,
+    GBR_TEXTURE_FORMAT_RGBA32_FLOAT = 8,
+    GBR_TEXTURE_FORMAT_DEPTH32_FLOAT = 9
+};
+
+enum gbr_vertex_format {
+    GBR_VERTEX_FORMAT_FLOAT32 = 1,
+    GBR_VERTEX_FORMAT_FLOAT32X2 = 2,
+    GBR_VERTEX_FORMAT_FLOAT32X3 = 3,
+    GBR_VERTEX_FORMAT_FLOAT32X4 = 4,
+    GBR_VERTEX_FORMAT_UINT32 = 5,
+    GBR_VERTEX_FORMAT_SINT32 = 6,
+    GBR_VERTEX_FORMAT_FLOAT16X2 = 7,
+    GBR_VERTEX_FORMAT_FLOAT16X4 = 8,
+    GBR_VERTEX_FORMAT_UNORM8X4 = 9
+};
+
+enum gbr_vertex_step_mode { GBR_STEP_VERTEX = 0, GBR_STEP_INSTANCE = 1 };
+enum gbr_index_format { GBR_INDEX_NONE = 0, GBR_INDEX_UINT16 = 1, GBR_INDEX_UINT32 = 2 };
+
+enum gbr_primitive_topology {
+    GBR_TOPOLOGY_POINT_LIST = 0,
+    GBR_TOPOLOGY_LINE_LIST = 1,
+    GBR_TOPOLOGY_LINE_STRIP = 2,
+    GBR_TOPOLOGY_TRIANGLE_LIST = 3,
+    GBR_TOPOLOGY_TRIANGLE_STRIP = 4
+};
+enum gbr_front_face { GBR_FRONT_FACE_CCW = 0, GBR_FRONT_FACE_CW = 1 };
+enum gbr_cull_mode { GBR_CULL_NONE = 0, GBR_CULL_FRONT = 1, GBR_CULL_BACK = 2 };
+enum gbr_polygon_mode { GBR_POLYGON_FILL = 0, GBR_POLYGON_LINE = 1, GBR_POLYGON_POINT = 2 };
+
+enum gbr_compare_function {
+    GBR_COMPARE_UNDEFINED = 0,
+    GBR_COMPARE_NEVER = 1,
+    GBR_COMPARE_LESS = 2,
+    GBR_COMPARE_EQUAL = 3,
+    GBR_COMPARE_LESS_EQUAL = 4,
+    GBR_COMPARE_GREATER = 5,
+    GBR_COMPARE_NOT_EQUAL = 6,
+    GBR_COMPARE_GREATER_EQUAL = 7,
+    GBR_COMPARE_ALWAYS = 8
+};
+
+enum gbr_blend_factor {
+    GBR_BLEND_ZERO = 0,
+    GBR_BLEND_ONE = 1,
+    GBR_BLEND_SRC = 2,
+    GBR_BLEND_ONE_MINUS_SRC = 3,
+    GBR_BLEND_SRC_ALPHA = 4,
+    GBR_BLEND_ONE_MINUS_SRC_ALPHA = 5,
+    GBR_BLEND_DST = 6,
+    GBR_BLEND_ONE_MINUS_DST = 7,
+    GBR_BLEND_DST_ALPHA = 8,
+    GBR_BLEND_ONE_MINUS_DST_ALPHA = 9,
+    GBR_BLEND_CONSTANT = 11,
+    GBR_BLEND_ONE_MINUS_CONSTANT = 12
+};
+enum gbr_blend_operation {
+    GBR_BLEND_OP_ADD = 0,
+    GBR_BLEND_OP_SUBTRACT = 1,
+    GBR_BLEND_OP_REVERSE_SUBTRACT = 2,
+    GBR_BLEND_OP_MIN = 3,
+    GBR_BLEND_OP_MAX = 4
+};
+
+enum gbr_address_mode {
+    GBR_ADDRESS_CLAMP_TO_EDGE = 0,
+    GBR_ADDRESS_REPEAT = 1,
+    GBR_ADDRESS_MIRROR_REPEAT = 2,
+    GBR_ADDRESS_CLAMP_TO_BORDER = 3
+};
+enum gbr_filter_mode { GBR_FILTER_NEAREST = 0, GBR_FILTER_LINEAR = 1 };
+
+enum gbr_load_op { GBR_LOAD_OP_LOAD = 0, GBR_LOAD_OP_CLEAR = 1 };
+enum gbr_store_op { GBR_STORE_OP_STORE = 0, GBR_STORE_OP_DISCARD = 1 };
+
+/* Semantics profile of a device.
+ *  PARITY    — exactly the reference's behaviour: blend state ignored (overwrite), sRGB formats
+ *              read/written as linear, sampler filters ignored (nearest), perspective
+ *              interpolation and f16/f32 colour targets rejected with GBR_ERR_UNSUPPORTED.
+ *  EXTENSION — the same coverage and depth rule, plus WebGPU-spec blending, Rgba16Float /
+ *              Rgba32Float targets, sRGB encode/decode, linear/mip filtering and
+ *              perspective-correct interpolation (features the reference leaves `todo!`). */
+enum gbr_profile { GBR_PROFILE_PARITY = 0, GBR_PROFILE_EXTENSION = 1 };
+
+/* ---------------------------------------------------------------- descriptors */
+
+typedef struct gbr_device_config {
+    uint32_t abi_version;       /* must be GBR_ABI_VERSION                                   */
+    uint32_t profile;           /* gbr_profile                                               */
+    uint32_t device_ordinal;    /* CUDA device                                               */
+    uint32_t tile_size;         /* raster tile side: 8, 16 or 32 (0 = default 16)            */
+    uint32_t bin_capacity;      /* max primitives sorted per tile in one window (0 = auto)   */
+    uint32_t warps_per_tile;    /* 1..8 (0 = default)                                        */
+    uint32_t batch_submissions; /* 1 = the worker merges queued submissions into one launch  */
+    uint32_t use_graphs;        /* 1 = replay per-shape CUDA graphs                          */
+    uint64_t hbm_budget_bytes;  /* transient (per-submission) memory budget; 0 = 80 GB       */
+    uint64_t reserved[4];
+} gbr_device_config;
+
+typedef struct gbr_limits {
+    uint32_t max_texture_dimension_2d;
+    uint32_t max_bind_groups;
+    uint32_t max_vertex_buffers;
+    uint32_t max_vertex_attributes;
+    uint32_t max_color_attachments;
+    uint32_t max_inter_stage_components;
+    uint64_t max_buffer_size;
+} gbr_limits;
+
+typedef struct gbr_extent3d {
+    uint32_t width, height, depth_or_array_layers;
+} gbr_extent3d;
+
+typedef struct gbr_texture_desc {
+    gbr_extent3d size;
+    uint32_t mip_level_count;
+    uint32_t sample_count;
+    uint32_t dimension; /* 2 = D2 (only D2 is used on the path) */
+    uint32_t format;    /* gbr_texture_format */
+    uint32_t usage;     /* wgpu::TextureUsages bits (informational) */
+    uint32_t _pad;
+} gbr_texture_desc;
+
+/* wgpu::TexelCopyBufferLayout */
+typedef struct gbr_texel_copy_buffer_layout {
+    uint64_t offset;
+    uint32_t bytes_per_row; /* 0 = None */
+    uint32_t rows_per_image; /* 0 = None */
+} gbr_texel_copy_buffer_layout;
+
+typedef struct gbr_sampler_desc {
+    uint32_t address_mode_u, address_mode_v, address_mode_w; /* gbr_address_mode */
+    uint32_t mag_filter, min_filter, mipmap_filter;          /* gbr_filter_mode  */
+    float lod_min_clamp, lod_max_clamp;
+    uint32_t compare; /* gbr_compare_function, 0 = none */
+    uint32_t anisotropy_clamp;
+} gbr_sampler_desc;
+
+typedef struct gbr_vertex_attribute {
+    uint32_t format; /* gbr_vertex_format */
+    uint32_t shader_location;
+    uint64_t offset;
+} gbr_vertex_attribute;
+
+#define GBR_MAX_VERTEX_BUFFERS 8
+#define GBR_MAX_VERTEX_ATTRIBUTES 16
+#define GBR_MAX_COLOR_TARGETS 4
+#define GBR_MAX_BIND_GROUPS 4
+#define GBR_MAX_BIND_GROUP_ENTRIES 8
+#define GBR_MAX_ENTRY_POINT_NAME 64
+
+typedef struct gbr_vertex_buffer_layout {
+    uint64_t array_stride;
+    uint32_t step_mode; /* gbr_vertex_step_mode */
+    uint32_t attribute_count;
+    gbr_vertex_attribute attributes[GBR_MAX_VERTEX_ATTRIBUTES];
+} gbr_vertex_buffer_layout;
+
+typedef struct gbr_blend_component {
+    uint32_t src_factor, dst_factor, operation;
+} gbr_blend_component;
+
+typedef struct gbr_color_target_state {
+    uint32_t format;     /* gbr_texture_format */
+    uint32_t has_blend;  /* 0 = blend: None */
+    gbr_blend_component color, alpha;
+    uint32_t write_mask; /* wgpu::ColorWrites bits: R=1 G=2 B=4 A=8 */
+} gbr_color_target_state;
+
+typedef struct gbr_primitive_state {
+    uint32_t topology;           /* gbr_primitive_topology */
+    uint32_t strip_index_format; /* gbr_index_format, NONE = no primitive restart */
+    uint32_t front_face;         /* gbr_front_face */
+    uint32_t cull_mode;          /* gbr_cull_mode */
+    uint32_t polygon_mode;       /* gbr_polygon_mode */
+    uint32_t unclipped_depth;
+} gbr_primitive_state;
+
+typedef struct gbr_depth_stencil_state {
+    uint32_t format;              /* GBR_TEXTURE_FORMAT_DEPTH32_FLOAT */
+    uint32_t depth_write_enabled;
+    uint32_t depth_compare;       /* gbr_compare_function */
+    uint32_t _pad;
+} gbr_depth_stencil_state;
+
+typedef struct gbr_render_pipeline_desc {
+    gbr_shader_module vertex_module;
+    char vertex_entry_point[GBR_MAX_ENTRY_POINT_NAME];
+    uint32_t vertex_buffer_count;
+    uint32_t _pad0;
+    gbr_vertex_buffer_layout vertex_buffers[GBR_MAX_VERTEX_BUFFERS];
+    gbr_primitive_state primitive;
+    uint32_t has_depth_stencil;
+    uint32_t _pad1;
+    gbr_depth_stencil_state depth_stencil;
+    uint32_t multisample_count;
+    uint32_t has_fragment;
+    gbr_shader_module fragment_module;
+    char fragment_entry_point[GBR_MAX_ENTRY_POINT_NAME];
+    uint32_t color_target_count;
+    uint32_t _pad2;
+    gbr_color_target_state color_targets[GBR_MAX_COLOR_TARGETS];
+} gbr_render_pipeline_desc;
+
+enum gbr_binding_kind { GBR_BINDING_BUFFER = 0, GBR_BINDING_SAMPLER = 1, GBR_BINDING_TEXTURE_VIEW = 2 };
+
+typedef struct gbr_bind_group_entry {
+    uint32_t binding;
+    uint32_t kind;     /* gbr_binding_kind */
+    uint64_t resource; /* gbr_buffer / gbr_sampler / gbr_texture handle */
+    uint64_t offset;   /* buffer bindings */
+    uint64_t size;     /* buffer bindings, 0 = rest of buffer */
+} gbr_bind_group_entry;
+
+typedef struct gbr_bind_group_desc {
+    uint32_t entry_count;
+    uint32_t _pad;
+    gbr_bind_group_entry entries[GBR_MAX_BIND_GROUP_ENTRIES];
+} gbr_bind_group_desc;
+
+/* Per-submission record kept for metrics (the reference logs these with `tracing` only:
+ * render_pass/mod.rs:392-393, render_pass/state.rs:516-517,592). */
+typedef struct gbr_submission_stats {
+    uint64_t submission_index;
+    uint64_t draws;
+    uint64_t primitives_in;        /* primitives assembled (incl. culled) */
+    uint64_t fragments_shaded;     /* fragment-shader invocations, counted as the reference */
+    uint64_t kernel_launches;
+    double queue_wait_ms;          /* submit -> start of device work  */
+    double gpu_ms;                 /* device time of the submission   */
+    double submit_to_fence_ms;     /* submit -> fence signalled       */
+    uint32_t batched_with;         /* number of submissions merged into the same launch */
+    uint32_t _pad;
+} gbr_submission_stats;
+
+/* ---------------------------------------------------------------- command stream
+ *
+ * A command buffer is a flat little-endian byte stream of records
+ *     [u32 opcode][u32 payload_bytes][payload ... padded to 8 bytes]
+ * mirroring `RenderPassSubCommand` (render_pass/mod.rs:397-423) wrapped in begin/end pass
+ * records (`Command::RenderPass`, command.rs:188-190).  Streams are consumed at submit.
+ */
+enum gbr_opcode {
+    GBR_OP_BEGIN_RENDER_PASS = 1,  /* payload: gbr_cmd_begin_render_pass */
+    GBR_OP_END_RENDER_PASS = 2,    /* payload: none */
+    GBR_OP_SET_PIPELINE = 3,       /* payload: gbr_cmd_set_pipeline */
+    GBR_OP_SET_BIND_GROUP = 4,     /* payload: gbr_cmd_set_bind_group */
+    GBR_OP_SET_INDEX_BUFFER = 5,   /* payload: gbr_cmd_set_index_buffer */
+    GBR_OP_SET_VERTEX_BUFFER = 6,  /* payload: gbr_cmd_set_vertex_buffer */
+    GBR_OP_SET_VIEWPORT = 7,       /* payload: gbr_cmd_set_viewport */
+    GBR_OP_SET_SCISSOR_RECT = 8,   /* payload: gbr_cmd_set_scissor_rect */
+    GBR_OP_SET_BLEND_CONSTANT = 9, /* payload: gbr_cmd_set_blend_constant */
+    GBR_OP_SET_STENCIL_REFERENCE = 10, /* payload: u32 + pad */
+    GBR_OP_DRAW = 11,              /* payload: gbr_cmd_draw */
+    GBR_OP_DRAW_INDEXED = 12       /* payload: gbr_cmd_draw_indexed */
+};
+
+typedef struct gbr_cmd_header {
+    uint32_t opcode;
+    uint32_t payload_bytes;
+} gbr_cmd_header;
+
+typedef struct gbr_color_attachment {
+    gbr_texture view;      /* texture (mip 0, layer `depth_slice`) */
+    uint32_t load_op;      /* gbr_load_op */
+    uint32_t store_op;     /* gbr_store_op */
+    double clear_value[4]; /* wgpu::Color (f64) */
+    uint32_t depth_slice;
+    uint32_t _pad;
+} gbr_color_attachment;
+
+typedef struct gbr_depth_attachment {
+    gbr_texture view;
+    uint32_t has_depth_ops;
+    uint32_t depth_load_op;
+    uint32_t depth_store_op;
+    float depth_clear_value;
+} gbr_depth_attachment;
+
+typedef struct gbr_cmd_begin_render_pass {
+    uint32_t color_attachment_count;
+    uint32_t has_depth_attachment;
+    gbr_color_attachment color_attachments[GBR_MAX_COLOR_TARGETS]; /* view 0 = None */
+    gbr_depth_attachment depth_attachment;
+} gbr_cmd_begin_render_pass;
+
+typedef struct gbr_cmd_set_pipeline { gbr_render_pipeline pipeline; } gbr_cmd_set_pipeline;
+typedef struct gbr_cmd_set_bind_group {
+    uint32_t index;
+    uint32_t dynamic_offset_count; /* dynamic offsets are ignored, as in state.rs:194-205 */
+    gbr_bind_group bind_group;     /* 0 = unset */
+} gbr_cmd_set_bind_group;
+typedef struct gbr_cmd_set_index_buffer {
+    gbr_buffer buffer;
+    uint32_t index_format;
+    uint32_t _pad;
+    uint64_t offset;
+    uint64_t size; /* 0 = rest of buffer */
+} gbr_cmd_set_index_buffer;
+typedef struct gbr_cmd_set_vertex_buffer {
+    uint32_t slot;
+    uint32_t _pad;
+    gbr_buffer buffer;
+    uint64_t offset;
+    uint64_t size; /* 0 = rest of buffer */
+} gbr_cmd_set_vertex_buffer;
+typedef struct gbr_cmd_set_viewport { float x, y, width, height, min_depth, max_depth; } gbr_cmd_set_viewport;
+typedef struct gbr_cmd_set_scissor_rect { uint32_t x, y, width, height; } gbr_cmd_set_scissor_rect;
+typedef struct gbr_cmd_set_blend_constant { double color[4]; } gbr_cmd_set_blend_constant;
+typedef struct gbr_cmd_draw {
+    uint32_t vertex_start, vertex_end;     /* Range<u32> */
+    uint32_t instance_start, instance_end; /* Range<u32> */
+} gbr_cmd_draw;
+typedef struct gbr_cmd_draw_indexed {
+    uint32_t index_start, index_end;
+    int32_t base_vertex;
+    uint32_t instance_start, instance_end;
+    uint32_t _pad;
+} gbr_cmd_draw_indexed;
+
+/* ---------------------------------------------------------------- entry points */
+
+/* Thread-local text of the last error on this thread; returns the full message length. */
+GBR_API size_t gbr_last_error(char* buf, size_t buf_len);
+GBR_API uint32_t gbr_abi_version(void);
+
+/* wgpu_cpu::instance (lib.rs:25-27) -> Instance::request_adapter (instance.rs:72-102) ->
+ * Adapter::request_device (adapter.rs:24-42) -> create_device_and_queue (device.rs:40-74),
+ * which spawns the engine thread (engine.rs:12-24).  One call creates device + queue + worker. */
+GBR_API gbr_status gbr_device_create(const gbr_device_config* config, gbr_device* out_device);
+/* Drop of Queue / QueueReceiver (device.rs:480-487, 543-549): stops the worker, frees all objects. */
+GBR_API gbr_status gbr_device_destroy(gbr_device device);
+/* AdapterInterface::limits (adapter.rs:60-62). */
+GBR_API gbr_status gbr_device_limits(gbr_device device, gbr_limits* out_limits);
+
+/* DeviceInterface::create_buffer (device.rs:157-159 -> buffer.rs:40-52). */
+GBR_API gbr_status gbr_buffer_create(gbr_device device, uint64_t size, uint32_t usage, gbr_buffer* out_buffer);
+GBR_API gbr_status gbr_buffer_destroy(gbr_device device, gbr_buffer buffer);
+/* QueueInterface::write_buffer (device.rs:332-344).  Ordered with later submissions. */
+GBR_API gbr_status gbr_queue_write_buffer(gbr_device device, gbr_buffer buffer, uint64_t offset,
+                                          const void* data, uint64_t size);
+/* BufferInterface::map_async + get_mapped_range for reads (buffer.rs:112-136): waits for all
+ * prior submissions, then copies `size` bytes at `offset` into `dst`. */
+GBR_API gbr_status gbr_buffer_read(gbr_device device, gbr_buffer buffer, uint64_t offset, void* dst, uint64_t size);
+
+/* DeviceInterface::create_texture (device.rs:161-163 -> texture.rs:34-43). */
+GBR_API gbr_status gbr_texture_create(gbr_device device, const gbr_texture_desc* desc, gbr_texture* out_texture);
+GBR_API gbr_status gbr_texture_destroy(gbr_device device, gbr_texture texture);
+/* QueueInterface::write_texture (device.rs:371-434).  As in the reference, the copy extent
+ * is the whole texture and whole rows are copied; `mip_level` > 0 is accepted only by the
+ * extension profile (the reference has `todo!` at device.rs:378-380). */
+GBR_API gbr_status gbr_queue_write_texture(gbr_device device, gbr_texture texture, uint32_t mip_level,
+                                           const void* data, uint64_t data_size,
+                                           const gbr_texel_copy_buffer_layout* layout, gbr_extent3d size);
+/* wgpu_cpu::image::rgba_texture_image (lib.rs:158-173): waits for prior submissions and
+ * copies the whole mip level (tightly packed rows) into `dst`. */
+GBR_API gbr_status gbr_texture_read(gbr_device device, gbr_texture texture, uint32_t mip_level, void* dst, uint64_t size);
+
+/* DeviceInterface::create_sampler (device.rs:185-187 -> sampler.rs:4-29). */
+GBR_API gbr_status gbr_sampler_create(gbr_device device, const gbr_sampler_desc* desc, gbr_sampler* out_sampler);
+GBR_API gbr_status gbr_sampler_destroy(gbr_device device, gbr_sampler sampler);
+
+/* DeviceInterface::create_shader_module (device.rs:91-100 -> shader.rs:31-50): parses and
+ * validates WGSL.  Entry points are translated to CUDA C and compiled with NVRTC when a
+ * pipeline that uses them is created (shader.rs:52-74 `for_pipeline`). */
+GBR_API gbr_status gbr_shader_module_create(gbr_device device, const char* wgsl, uint64_t wgsl_len,
+                                            gbr_shader_module* out_module);
+/* No reference counterpart: selects one of the library's precompiled CUDA shader programs by
+ * name (e.g. "colored_triangle", "mesh_color", "mesh_tex_lambert", "quad_color").  Used to pin
+ * the WGSL translator against hand-written programs and by callers without NVRTC. */
+GBR_API gbr_status gbr_shader_module_create_native(gbr_device device, const char* name,
+                                                   gbr_shader_module* out_module);
+GBR_API gbr_status gbr_shader_module_destroy(gbr_device device, gbr_shader_module module);
+
+/* DeviceInterface::create_render_pipeline (device.rs:129-134 -> pipeline.rs:57-76). */
+GBR_API gbr_status gbr_render_pipeline_create(gbr_device device, const gbr_render_pipeline_desc* desc,
+                                              gbr_render_pipeline* out_pipeline);
+GBR_API gbr_status gbr_render_pipeline_destroy(gbr_device device, gbr_render_pipeline pipeline);
+
+/* DeviceInterface::create_bind_group (device.rs:115-120 -> bind_group.rs:58-72,91-117). */
+GBR_API gbr_status gbr_bind_group_create(gbr_device device, const gbr_bind_group_desc* desc,
+                                         gbr_bind_group* out_bind_group);
+GBR_API gbr_status gbr_bind_group_destroy(gbr_device device, gbr_bind_group bind_group);
+
+/* QueueInterface::submit (device.rs:436-462): validates and enqueues one command buffer
+ * (the flat stream above) for the worker; returns its submission index.  Never blocks on
+ * device work (it may block on HBM admission when the transient budget is exhausted). */
+GBR_API gbr_status gbr_queue_submit(gbr_device device, const void* commands, uint64_t commands_len,
+                                    uint64_t* out_submission_index);
+
+enum gbr_poll_status { GBR_POLL_WAIT_SUCCEEDED = 0, GBR_POLL_QUEUE_EMPTY = 1, GBR_POLL_POLL = 2 };
+/* DeviceInterface::poll (device.rs:237-295).  wait = 0 is PollType::Poll.  With wait = 1 and
+ * has_index = 1, waits until `submission_index` is done; with has_index = 0 waits for one
+ * more submission to finish, as the reference does.  timeout_ns = UINT64_MAX waits forever.
+ * Returns GBR_ERR_TIMEOUT when the wait runs out (PollError::Timeout). */
+GBR_API gbr_status gbr_device_poll(gbr_device device, uint32_t wait, uint32_t has_index,
+                                   uint64_t submission_index, uint64_t timeout_ns, uint32_t* out_status);
+
+/* Metrics of a finished submission (tracing events in the reference, see struct comment). */
+GBR_API gbr_status gbr_submission_stats_get(gbr_device device, uint64_t submission_index,
+                                            gbr_submission_stats* out_stats);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GBR_H */

@@ -1,0 +1,1324 @@
+// TEST INFRASTRUCTURE — the oracle (see orc_core.hpp).  Only tests/, __graft_entry__.smoke()
+// and bench.py's cpu_baseline leg load liborc.so, as the checker.
+//
+// orc_device.cpp — a CPU device behind the same C ABI as the GPU library (include/gbr.h), with
+// every symbol prefixed `orc_` instead of `gbr_`.  It restates wgpu-cpu's engine: resources are
+// host byte vectors (buffer.rs:22-52, texture.rs:34-43), a submission executes its render
+// passes immediately and in order (engine.rs:26-46), and each pass replays its sub-commands
+// through the reference's draw loop (render_pass/mod.rs:345-395, render_pass/state.rs:239-593)
+// and fragment processing (render_pass/fragment.rs:127-214, 427-489).
+//
+// Threading: with orc_set_threads(n > 1) a pass is executed by n threads, each owning a band of
+// framebuffer rows.  Every thread runs the whole draw loop but emits only fragments of its
+// rows, so the per-pixel fragment order — and therefore every output bit — is the same as
+// with one thread.
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "gbr.h"
+#include "orc_core.hpp"
+#include "orc_programs.hpp"
+
+#define ORC_API extern "C" __attribute__((visibility("default")))
+
+namespace orc {
+
+static thread_local std::string g_last_error;
+static int g_threads = 1;
+
+struct Error {
+    gbr_status status;
+    std::string msg;
+};
+[[noreturn]] static void fail(gbr_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    throw Error{st, buf};
+}
+
+// ---------------------------------------------------------------- texture formats
+// bytes_per_texel (texture.rs:456-505) for the formats this ABI exposes.
+static uint32_t bytes_per_texel(uint32_t f) {
+    switch (f) {
+        case GBR_TEXTURE_FORMAT_R8_UNORM: return 1;
+        case GBR_TEXTURE_FORMAT_RG8_UNORM: return 2;
+        case GBR_TEXTURE_FORMAT_RGBA8_UNORM:
+        case GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB:
+        case GBR_TEXTURE_FORMAT_BGRA8_UNORM:
+        case GBR_TEXTURE_FORMAT_BGRA8_UNORM_SRGB:
+        case GBR_TEXTURE_FORMAT_DEPTH32_FLOAT: return 4;
+        case GBR_TEXTURE_FORMAT_RGBA16_FLOAT: return 8;
+        case GBR_TEXTURE_FORMAT_RGBA32_FLOAT: return 16;
+        default: return 0;
+    }
+}
+
+// ---------------------------------------------------------------- objects
+struct Object {
+    virtual ~Object() {}
+};
+struct Buffer : Object {
+    std::vector<uint8_t> data;
+};
+struct Texture : Object {
+    gbr_texture_desc desc;
+    uint32_t bpp;
+    uint32_t mips_stored;
+    std::vector<std::vector<uint8_t>> mips;  // mip level -> bytes (layer-major, row-major)
+    uint32_t mip_w(uint32_t m) const { return std::max(1u, desc.size.width >> m); }
+    uint32_t mip_h(uint32_t m) const { return std::max(1u, desc.size.height >> m); }
+};
+struct TextureView {
+    const Texture* tex;
+};
+struct SamplerState {
+    gbr_sampler_desc desc;
+};
+struct Sampler : Object {
+    SamplerState s;
+};
+struct ShaderModule : Object {
+    const Program* prog;
+};
+struct Pipeline : Object {
+    gbr_render_pipeline_desc desc;
+    const Program* vs;
+    const Program* fs;
+    // shader input location -> (buffer index, offset, format)
+    struct Loc {
+        bool present;
+        uint32_t buffer;
+        uint64_t offset;
+        uint32_t format;
+    } loc[16];
+};
+struct BindGroup : Object {
+    gbr_bind_group_desc desc;
+};
+
+struct Device {
+    uint32_t profile = GBR_PROFILE_PARITY;
+    std::mutex mu;
+    uint64_t next_handle = 1;
+    std::unordered_map<uint64_t, std::unique_ptr<Object>> objects;
+    uint64_t next_submission = 0;
+    std::unordered_map<uint64_t, gbr_submission_stats> stats;
+
+    template <class T>
+    T* get(uint64_t h, const char* what) {
+        auto it = objects.find(h);
+        if (it == objects.end()) fail(GBR_ERR_INVALID_ARGUMENT, "invalid %s handle %llu", what, (unsigned long long)h);
+        T* p = dynamic_cast<T*>(it->second.get());
+        if (!p) fail(GBR_ERR_INVALID_ARGUMENT, "handle %llu is not a %s", (unsigned long long)h, what);
+        return p;
+    }
+    uint64_t add(Object* o) {
+        uint64_t h = next_handle++;
+        objects[h].reset(o);
+        return h;
+    }
+};
+
+static std::mutex g_devices_mu;
+static std::unordered_map<uint64_t, std::unique_ptr<Device>> g_devices;
+static uint64_t g_next_device = 1;
+
+static Device* get_device(gbr_device d) {
+    std::lock_guard<std::mutex> lk(g_devices_mu);
+    auto it = g_devices.find(d);
+    if (it == g_devices.end()) fail(GBR_ERR_INVALID_ARGUMENT, "invalid device handle");
+    return it->second.get();
+}
+
+// ---------------------------------------------------------------- sampling
+// texel_coordinate (render_pass/binding.rs:150-164)
+static uint32_t texel_coordinate(float x, uint32_t mode, uint32_t size) {
+    switch (mode) {
+        case GBR_ADDRESS_CLAMP_TO_EDGE:
+            if (x < 0.0f) x = 0.0f;
+            if (x > 1.0f) x = 1.0f;
+            break;
+        case GBR_ADDRESS_REPEAT: {
+            float r = std::fmod(x, 1.0f);
+            x = (r < 0.0f) ? r + 1.0f : r;  // f32::rem_euclid(1.0)
+            break;
+        }
+        case GBR_ADDRESS_MIRROR_REPEAT: {
+            float r = std::fmod(x, 2.0f);
+            r = (r < 0.0f) ? r + 2.0f : r;  // f32::rem_euclid(2.0)
+            x = (r <= 1.0f) ? r : 2.0f - r;
+            break;
+        }
+        default: fail(GBR_ERR_UNSUPPORTED, "ClampToBorder is not implemented (binding.rs:160)");
+    }
+    float scaled = x * (float)(size - 1u);
+    return rust_f32_to_u32(std::round(scaled));
+}
+
+// TextureReadGuard::get_pixel (texture.rs:170-188): Rgba8Unorm / Rgba8UnormSrgb only.
+static V4 get_pixel_rgba8(const Texture* t, uint32_t mip, uint32_t x, uint32_t y) {
+    uint32_t w = t->mip_w(mip);
+    const uint8_t* p = t->mips[mip].data() + ((size_t)y * w + x) * 4;
+    return {(float)p[0] / 255.0f, (float)p[1] / 255.0f, (float)p[2] / 255.0f, (float)p[3] / 255.0f};
+}
+
+struct SampleCtx {
+    uint32_t profile;
+};
+
+// image_sample (render_pass/binding.rs:93-140).  Nearest, mip 0, layer 0; filters ignored.
+static V4 sample_parity(const TextureView* tv, const SamplerState* s, float u, float v) {
+    const Texture* t = tv->tex;
+    if (t->desc.format != GBR_TEXTURE_FORMAT_RGBA8_UNORM && t->desc.format != GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB)
+        fail(GBR_ERR_UNSUPPORTED, "sampling format %u is not implemented (texture.rs:186)", t->desc.format);
+    uint32_t x = texel_coordinate(u, s->desc.address_mode_u, t->desc.size.width);
+    uint32_t y = texel_coordinate(v, s->desc.address_mode_v, t->desc.size.height);
+    return get_pixel_rgba8(t, 0, x, y);
+}
+
+static V4 sample_cb(const TextureView* tv, const SamplerState* s, float u, float v, const void* ctx) {
+    (void)ctx;
+    if (!tv || !s) fail(GBR_ERR_VALIDATION, "No such binding resource");
+    return sample_parity(tv, s, u, v);
+}
+
+// ---------------------------------------------------------------- texel writers
+// f32_to_u8 (texture.rs:378-381): (v * 255).clamp(0, 255) as u8, i.e. truncation.
+static inline uint8_t unorm8_trunc(float v) {
+    float s = v * 255.0f;
+    if (s < 0.0f) s = 0.0f;
+    if (s > 255.0f) s = 255.0f;
+    return rust_f32_to_u8(s);
+}
+
+// TexelWriter::from_color (texture.rs:373-411) + put_pixel (texture.rs:213-218).
+static void write_color(Texture* t, uint32_t x, uint32_t y, uint32_t slice, V4 c, uint32_t profile) {
+    uint32_t w = t->desc.size.width, h = t->desc.size.height;
+    uint8_t* p = t->mips[0].data() + (((size_t)slice * h + y) * w + x) * t->bpp;
+    switch (t->desc.format) {
+        case GBR_TEXTURE_FORMAT_R8_UNORM: p[0] = unorm8_trunc(c.x); break;
+        case GBR_TEXTURE_FORMAT_RG8_UNORM:
+            p[0] = unorm8_trunc(c.x);
+            p[1] = unorm8_trunc(c.y);
+            break;
+        case GBR_TEXTURE_FORMAT_RGBA8_UNORM:
+        case GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB:
+            p[0] = unorm8_trunc(c.x);
+            p[1] = unorm8_trunc(c.y);
+            p[2] = unorm8_trunc(c.z);
+            p[3] = unorm8_trunc(c.w);
+            break;
+        case GBR_TEXTURE_FORMAT_BGRA8_UNORM:
+        case GBR_TEXTURE_FORMAT_BGRA8_UNORM_SRGB:
+            p[0] = unorm8_trunc(c.z);
+            p[1] = unorm8_trunc(c.y);
+            p[2] = unorm8_trunc(c.x);
+            p[3] = unorm8_trunc(c.w);
+            break;
+        case GBR_TEXTURE_FORMAT_RGBA16_FLOAT:
+            if (profile != GBR_PROFILE_EXTENSION)
+                fail(GBR_ERR_UNSUPPORTED, "Unsupported texture format: Rgba16Float (texture.rs:407)");
+            {
+                uint16_t hv[4] = {f32_to_f16_rne(c.x), f32_to_f16_rne(c.y), f32_to_f16_rne(c.z), f32_to_f16_rne(c.w)};
+                std::memcpy(p, hv, 8);
+            }
+            break;
+        case GBR_TEXTURE_FORMAT_RGBA32_FLOAT:
+            if (profile != GBR_PROFILE_EXTENSION)
+                fail(GBR_ERR_UNSUPPORTED, "Unsupported texture format: Rgba32Float (texture.rs:407)");
+            {
+                float fv[4] = {c.x, c.y, c.z, c.w};
+                std::memcpy(p, fv, 16);
+            }
+            break;
+        default: fail(GBR_ERR_UNSUPPORTED, "Unsupported colour target format %u", t->desc.format);
+    }
+}
+
+// Decoded read of a colour target texel (extension-profile blending only).
+static V4 read_color(const Texture* t, uint32_t x, uint32_t y, uint32_t slice) {
+    uint32_t w = t->desc.size.width, h = t->desc.size.height;
+    const uint8_t* p = t->mips[0].data() + (((size_t)slice * h + y) * w + x) * t->bpp;
+    switch (t->desc.format) {
+        case GBR_TEXTURE_FORMAT_RGBA16_FLOAT: {
+            uint16_t hv[4];
+            std::memcpy(hv, p, 8);
+            return {f16_to_f32(hv[0]), f16_to_f32(hv[1]), f16_to_f32(hv[2]), f16_to_f32(hv[3])};
+        }
+        case GBR_TEXTURE_FORMAT_RGBA32_FLOAT: {
+            float fv[4];
+            std::memcpy(fv, p, 16);
+            return {fv[0], fv[1], fv[2], fv[3]};
+        }
+        case GBR_TEXTURE_FORMAT_RGBA8_UNORM:
+        case GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB:
+            return {p[0] / 255.0f, p[1] / 255.0f, p[2] / 255.0f, p[3] / 255.0f};
+        case GBR_TEXTURE_FORMAT_BGRA8_UNORM:
+        case GBR_TEXTURE_FORMAT_BGRA8_UNORM_SRGB:
+            return {p[2] / 255.0f, p[1] / 255.0f, p[0] / 255.0f, p[3] / 255.0f};
+        default: fail(GBR_ERR_UNSUPPORTED, "blend: unsupported target format %u", t->desc.format);
+    }
+}
+
+// WebGPU blend factor (extension profile; the reference never reads the blend state).
+static float blend_factor(uint32_t f, float src, float src_a, float dst, float dst_a, float konst) {
+    switch (f) {
+        case GBR_BLEND_ZERO: return 0.0f;
+        case GBR_BLEND_ONE: return 1.0f;
+        case GBR_BLEND_SRC: return src;
+        case GBR_BLEND_ONE_MINUS_SRC: return 1.0f - src;
+        case GBR_BLEND_SRC_ALPHA: return src_a;
+        case GBR_BLEND_ONE_MINUS_SRC_ALPHA: return 1.0f - src_a;
+        case GBR_BLEND_DST: return dst;
+        case GBR_BLEND_ONE_MINUS_DST: return 1.0f - dst;
+        case GBR_BLEND_DST_ALPHA: return dst_a;
+        case GBR_BLEND_ONE_MINUS_DST_ALPHA: return 1.0f - dst_a;
+        case GBR_BLEND_CONSTANT: return konst;
+        case GBR_BLEND_ONE_MINUS_CONSTANT: return 1.0f - konst;
+        default: fail(GBR_ERR_UNSUPPORTED, "blend factor %u", f);
+    }
+}
+static float blend_op(uint32_t op, float s, float d) {
+    switch (op) {
+        case GBR_BLEND_OP_ADD: return s + d;
+        case GBR_BLEND_OP_SUBTRACT: return s - d;
+        case GBR_BLEND_OP_REVERSE_SUBTRACT: return d - s;
+        case GBR_BLEND_OP_MIN: return std::fmin(s, d);
+        case GBR_BLEND_OP_MAX: return std::fmax(s, d);
+        default: fail(GBR_ERR_UNSUPPORTED, "blend op %u", op);
+    }
+}
+// One channel: (src * srcFactor) op (dst * dstFactor); MIN/MAX ignore the factors.
+static float blend_channel(const gbr_blend_component& bc, float s, float sa, float d, float da, float k) {
+    if (bc.operation == GBR_BLEND_OP_MIN || bc.operation == GBR_BLEND_OP_MAX) return blend_op(bc.operation, s, d);
+    float fs = blend_factor(bc.src_factor, s, sa, d, da, k);
+    float fd = blend_factor(bc.dst_factor, s, sa, d, da, k);
+    return blend_op(bc.operation, s * fs, d * fd);
+}
+static V4 blend_colors(const gbr_color_target_state& ct, V4 s, V4 d, const double konst[4]) {
+    V4 r;
+    r.x = blend_channel(ct.color, s.x, s.w, d.x, d.w, (float)konst[0]);
+    r.y = blend_channel(ct.color, s.y, s.w, d.y, d.w, (float)konst[1]);
+    r.z = blend_channel(ct.color, s.z, s.w, d.z, d.w, (float)konst[2]);
+    r.w = blend_channel(ct.alpha, s.w, s.w, d.w, d.w, (float)konst[3]);
+    return r;
+}
+
+// ---------------------------------------------------------------- pass state
+struct BoundSlice {
+    const Buffer* buf = nullptr;
+    uint64_t offset = 0, size = 0;
+};
+
+struct PassState {  // render_pass/state.rs:57-74
+    const Pipeline* pipeline = nullptr;
+    BoundSlice index;
+    uint32_t index_format = 0;
+    BoundSlice vb[GBR_MAX_VERTEX_BUFFERS];
+    const BindGroup* groups[GBR_MAX_BIND_GROUPS] = {};
+    float viewport[6];
+    uint32_t scissor[4];
+    double blend_constant[4] = {0, 0, 0, 0};
+};
+
+struct PassTargets {
+    Texture* color[GBR_MAX_COLOR_TARGETS] = {};
+    uint32_t color_slice[GBR_MAX_COLOR_TARGETS] = {};
+    Texture* depth = nullptr;
+    uint32_t width = 0, height = 0;
+};
+
+struct Counters {
+    uint64_t fragments = 0;
+    uint64_t primitives = 0;
+};
+
+struct Exec {
+    Device* dev;
+    uint32_t profile;
+    PassTargets* tg;
+    uint32_t band_y0, band_y1;  // rows [y0, y1) this thread owns
+    Counters cnt;
+};
+
+// Per-draw resolved bindings for the program callbacks.
+static void resolve_bindings(Device* dev, const PassState& st, ProgramBindings& pb) {
+    std::memset(&pb, 0, sizeof pb);
+    for (int g = 0; g < GBR_MAX_BIND_GROUPS; ++g) {
+        const BindGroup* bg = st.groups[g];
+        if (!bg) continue;
+        for (uint32_t e = 0; e < bg->desc.entry_count; ++e) {
+            const gbr_bind_group_entry& en = bg->desc.entries[e];
+            if (en.binding >= 8) continue;
+            if (en.kind == GBR_BINDING_BUFFER) {
+                Buffer* b = dev->get<Buffer>(en.resource, "buffer");
+                uint64_t size = en.size ? en.size : b->data.size() - en.offset;
+                if (en.offset + size > b->data.size()) fail(GBR_ERR_VALIDATION, "bind group buffer range out of bounds");
+                pb.uniform[g][en.binding] = b->data.data() + en.offset;
+                pb.uniform_size[g][en.binding] = size;
+            } else if (en.kind == GBR_BINDING_TEXTURE_VIEW) {
+                Texture* t = dev->get<Texture>(en.resource, "texture");
+                pb.texture[g][en.binding] = new TextureView{t};  // freed in free_bindings
+            } else if (en.kind == GBR_BINDING_SAMPLER) {
+                Sampler* s = dev->get<Sampler>(en.resource, "sampler");
+                pb.sampler[g][en.binding] = &s->s;
+            }
+        }
+    }
+    pb.sample = sample_cb;
+}
+static void free_bindings(ProgramBindings& pb) {
+    for (int g = 0; g < 4; ++g)
+        for (int b = 0; b < 8; ++b) delete pb.texture[g][b];
+}
+
+// Vertex attribute fetch (render_pass/vertex.rs:128-156, 191-195).
+static void fetch_vertex(const PassState& st, const Pipeline* pl, uint32_t profile, uint32_t vertex, uint32_t instance,
+                         VsIn& in) {
+    std::memset(in.attr, 0, sizeof in.attr);
+    in.vertex_index = vertex;
+    in.instance_index = instance;
+    const Program* prog = pl->vs;
+    for (int i = 0; i < prog->num_inputs; ++i) {
+        int loc = prog->inputs[i].location;
+        const Pipeline::Loc& L = pl->loc[loc];
+        if (!L.present) fail(GBR_ERR_VALIDATION, "No vertex attribute at location %d", loc);
+        const gbr_vertex_buffer_layout& lay = pl->desc.vertex_buffers[L.buffer];
+        const BoundSlice& bs = st.vb[L.buffer];
+        if (!bs.buf) fail(GBR_ERR_VALIDATION, "Buffer %u not bound", L.buffer);
+        uint64_t stride_v = lay.step_mode == GBR_STEP_VERTEX ? lay.array_stride : 0;
+        uint64_t stride_i = lay.step_mode == GBR_STEP_INSTANCE ? lay.array_stride : 0;
+        uint64_t start = (uint64_t)instance * stride_i + (uint64_t)vertex * stride_v + L.offset;
+        uint32_t fsize = 0;
+        switch (L.format) {
+            case GBR_VERTEX_FORMAT_FLOAT32:
+            case GBR_VERTEX_FORMAT_UINT32:
+            case GBR_VERTEX_FORMAT_SINT32:
+            case GBR_VERTEX_FORMAT_UNORM8X4:
+            case GBR_VERTEX_FORMAT_FLOAT16X2: fsize = 4; break;
+            case GBR_VERTEX_FORMAT_FLOAT32X2:
+            case GBR_VERTEX_FORMAT_FLOAT16X4: fsize = 8; break;
+            case GBR_VERTEX_FORMAT_FLOAT32X3: fsize = 12; break;
+            case GBR_VERTEX_FORMAT_FLOAT32X4: fsize = 16; break;
+            default: fail(GBR_ERR_UNSUPPORTED, "vertex format %u", L.format);
+        }
+        if (start + fsize > bs.size) fail(GBR_ERR_VALIDATION, "vertex attribute read out of bounds (vertex %u)", vertex);
+        const uint8_t* src = bs.buf->data.data() + bs.offset + start;
+        int comps = prog->inputs[i].components;
+        if (profile == GBR_PROFILE_EXTENSION && L.format == GBR_VERTEX_FORMAT_FLOAT16X4 && comps == 4) {
+            uint16_t h[4];
+            std::memcpy(h, src, 8);
+            for (int k = 0; k < 4; ++k) in.attr[loc][k] = f16_to_f32(h[k]);
+        } else if (profile == GBR_PROFILE_EXTENSION && L.format == GBR_VERTEX_FORMAT_UNORM8X4 && comps == 4) {
+            for (int k = 0; k < 4; ++k) in.attr[loc][k] = (float)src[k] / 255.0f;
+        } else {
+            // The reference copies exactly `format.size()` bytes into the shader input, so the
+            // shader type must have the same size (vertex.rs:150-154).
+            if ((uint32_t)comps * 4u != fsize)
+                fail(GBR_ERR_VALIDATION, "vertex format %u does not match a %d-component shader input", L.format, comps);
+            std::memcpy(in.attr[loc], src, fsize);
+        }
+    }
+}
+
+// evaluate_compare_function (render_pass/mod.rs:434-452)
+static bool compare(uint32_t f, float v, float r) {
+    switch (f) {
+        case GBR_COMPARE_NEVER: return false;
+        case GBR_COMPARE_LESS: return v < r;
+        case GBR_COMPARE_EQUAL: return v == r;
+        case GBR_COMPARE_LESS_EQUAL: return v <= r;
+        case GBR_COMPARE_GREATER: return v > r;
+        case GBR_COMPARE_NOT_EQUAL: return v != r;
+        case GBR_COMPARE_GREATER_EQUAL: return v >= r;
+        case GBR_COMPARE_ALWAYS: return true;
+        default: fail(GBR_ERR_VALIDATION, "invalid compare function %u", f);
+    }
+}
+
+// The per-fragment work of FragmentProcessingState::process (fragment.rs:127-214),
+// FragmentOutput::depth_test (fragment.rs:427-453) and ::read_from (fragment.rs:456-489).
+// `coeff` are the interpolation coefficients for the FS inputs (N = 1, 2 or 3 vertices),
+// `vars` the inter-stage variables of the primitive's unclipped vertices.
+struct FragCtx {
+    Exec* ex;
+    const PassState* st;
+    const Pipeline* pl;
+    const ProgramBindings* pb;
+};
+
+static void process_fragment(FragCtx& fc, uint32_t fx, uint32_t fy, V4 fragment, bool front_facing,
+                             uint32_t primitive_index, int nverts, const float coeff[3], const VsOut* const verts[3],
+                             const float inv_w[3]) {
+    Exec* ex = fc.ex;
+    const Pipeline* pl = fc.pl;
+    const Program* fs = pl->fs;
+    ex->cnt.fragments++;
+    FsIn in;
+    in.position = fragment;
+    in.front_facing = front_facing;
+    in.primitive_index = primitive_index;
+    in.sample_index = 0;
+    in.sample_mask = ~0u;
+    for (int v = 0; v < fs->num_varyings; ++v) {
+        const ProgramVarying& pv = fs->varyings[v];
+        for (int c = 0; c < pv.components; ++c) {
+            float x;
+            if (pv.interp == INTERP_FLAT) {
+                x = verts[0]->var[pv.location][c];  // FlatSampling: inputs[0] (fragment.rs:395-405)
+            } else if (pv.interp == INTERP_LINEAR) {
+                // Interpolate::interpolate on the inter-stage values (fragment.rs:346-366)
+                float accu = verts[0]->var[pv.location][c] * coeff[0];
+                for (int k = 1; k < nverts; ++k) accu = accu + verts[k]->var[pv.location][c] * coeff[k];
+                x = accu;
+            } else {
+                if (ex->profile != GBR_PROFILE_EXTENSION)
+                    fail(GBR_ERR_UNSUPPORTED, "perspective interpolation is todo!() (fragment.rs:343-345)");
+                // Extension: perspective-correct, (sum v_k c_k / w_k) / (sum c_k / w_k).
+                float num = (verts[0]->var[pv.location][c] * coeff[0]) * inv_w[0];
+                float den = coeff[0] * inv_w[0];
+                for (int k = 1; k < nverts; ++k) {
+                    num = num + (verts[k]->var[pv.location][c] * coeff[k]) * inv_w[k];
+                    den = den + coeff[k] * inv_w[k];
+                }
+                x = num / den;
+            }
+            in.var[pv.location][c] = x;
+        }
+    }
+    FsOut out;
+    out.killed = false;
+    fs->fs(in, *fc.pb, out);
+    if (out.killed) return;  // EntryPointError::Killed (fragment.rs:204-208)
+    if (fs->num_outputs == 0) return;
+    // Late depth test at the first @location output (fragment.rs:470-479).
+    bool pass = true;
+    PassTargets* tg = ex->tg;
+    if (tg->depth && pl->desc.has_depth_stencil) {
+        Texture* d = tg->depth;
+        float* dp = reinterpret_cast<float*>(d->mips[0].data()) + (size_t)fy * d->desc.size.width + fx;
+        float stored = *dp;
+        if (compare(pl->desc.depth_stencil.depth_compare, fragment.z, stored)) {
+            if (pl->desc.depth_stencil.depth_write_enabled) *dp = fragment.z;
+        } else {
+            pass = false;
+        }
+    }
+    if (!pass) return;
+    for (int o = 0; o < fs->num_outputs; ++o) {
+        Texture* t = tg->color[o];
+        if (!t) fail(GBR_ERR_VALIDATION, "no colour attachment at location %d (fragment.rs:482-483)", o);
+        V4 c = out.color[o];
+        if (ex->profile == GBR_PROFILE_EXTENSION && o < (int)pl->desc.color_target_count) {
+            const gbr_color_target_state& ct = pl->desc.color_targets[o];
+            if (ct.has_blend) c = blend_colors(ct, c, read_color(t, fx, fy, tg->color_slice[o]), fc.st->blend_constant);
+            uint32_t wm = ct.write_mask;
+            if (wm != 0xF) {
+                V4 d = read_color(t, fx, fy, tg->color_slice[o]);
+                if (!(wm & 1)) c.x = d.x;
+                if (!(wm & 2)) c.y = d.y;
+                if (!(wm & 4)) c.z = d.z;
+                if (!(wm & 8)) c.w = d.w;
+            }
+        }
+        write_color(t, fx, fy, tg->color_slice[o], c, ex->profile);
+    }
+}
+
+// ------------------------------------------------------------------ the draw loop
+// DrawCall::execute + draw (render_pass/state.rs:239-593)
+static void execute_draw(Exec* ex, const PassState& st, bool indexed, uint32_t start, uint32_t end, int32_t base_vertex,
+                         uint32_t inst_start, uint32_t inst_end) {
+    Device* dev = ex->dev;
+    const Pipeline* pl = st.pipeline;
+    if (!pl) fail(GBR_ERR_VALIDATION, "No pipeline bound");
+    const gbr_primitive_state& ps = pl->desc.primitive;
+    if (ps.polygon_mode != GBR_POLYGON_FILL) fail(GBR_ERR_UNSUPPORTED, "Unsupported polygon mode %u", ps.polygon_mode);
+    bool is_strip = ps.topology == GBR_TOPOLOGY_LINE_STRIP || ps.topology == GBR_TOPOLOGY_TRIANGLE_STRIP;
+    bool separated = false;
+    if (indexed) {
+        if (!st.index.buf) fail(GBR_ERR_VALIDATION, "No index buffer bound");
+        if (ps.strip_index_format != GBR_INDEX_NONE) {
+            if (!is_strip) fail(GBR_ERR_VALIDATION, "List can't be separated");
+            if (ps.strip_index_format != st.index_format) fail(GBR_ERR_VALIDATION, "strip_index_format mismatch");
+            separated = true;
+        }
+    }
+    ProgramBindings pb;
+    resolve_bindings(dev, st, pb);
+    struct Guard {
+        ProgramBindings* p;
+        ~Guard() { free_bindings(*p); }
+    } guard{&pb};
+
+    ToRaster tr = make_to_raster(st.viewport, st.scissor);
+    FragCtx fc{ex, &st, pl, &pb};
+    bool has_fs = pl->desc.has_fragment && pl->fs;
+    uint32_t n = end > start ? end - start : 0;
+
+    for (uint32_t instance = inst_start; instance < inst_end; ++instance) {
+        // index resolution + vertex processing, once per index (state.rs:521-535)
+        std::vector<VsOut> vout(n);
+        std::vector<uint8_t> is_sep(n, 0);
+        for (uint32_t k = 0; k < n; ++k) {
+            uint32_t vertex;
+            if (indexed) {
+                uint32_t pos = start + k;
+                uint64_t isz = st.index_format == GBR_INDEX_UINT16 ? 2 : 4;
+                if ((uint64_t)(pos + 1) * isz > st.index.size) fail(GBR_ERR_VALIDATION, "index %u out of range", pos);
+                const uint8_t* ip = st.index.buf->data.data() + st.index.offset + (uint64_t)pos * isz;
+                uint32_t raw;
+                if (isz == 2) {
+                    uint16_t h;
+                    std::memcpy(&h, ip, 2);
+                    raw = h;
+                    if (separated && h == 0xFFFFu) {
+                        is_sep[k] = 1;
+                        continue;
+                    }
+                } else {
+                    std::memcpy(&raw, ip, 4);
+                    if (separated && raw == 0xFFFFFFFFu) {
+                        is_sep[k] = 1;
+                        continue;
+                    }
+                }
+                int64_t v = (int64_t)raw + (int64_t)base_vertex;  // u32::strict_add_signed (index.rs:55-57)
+                if (v < 0 || v > 0xFFFFFFFFll) fail(GBR_ERR_VALIDATION, "index + base_vertex overflows u32");
+                vertex = (uint32_t)v;
+            } else {
+                vertex = start + k;
+            }
+            VsIn in;
+            fetch_vertex(st, pl, ex->profile, vertex, instance, in);
+            std::memset(vout[k].var, 0, sizeof vout[k].var);
+            if (!pl->vs->vs(in, pb, vout[k])) fail(GBR_ERR_VALIDATION, "vertex processing failed");
+        }
+        if (!has_fs) continue;  // vertex shaders still ran (state.rs:584-589)
+
+        // primitive assembly (primitive.rs:206-487) -> list of vertex positions per primitive
+        int nv = (ps.topology == GBR_TOPOLOGY_POINT_LIST) ? 1
+                 : (ps.topology == GBR_TOPOLOGY_LINE_LIST || ps.topology == GBR_TOPOLOGY_LINE_STRIP) ? 2
+                                                                                                    : 3;
+        std::vector<std::array<uint32_t, 3>> prims;
+        if (ps.topology == GBR_TOPOLOGY_POINT_LIST || ps.topology == GBR_TOPOLOGY_LINE_LIST ||
+            ps.topology == GBR_TOPOLOGY_TRIANGLE_LIST) {
+            for (uint32_t k = 0; k + nv <= n; k += nv) {  // array_chunks_ drops a partial chunk
+                std::array<uint32_t, 3> p = {k, nv > 1 ? k + 1 : 0, nv > 2 ? k + 2 : 0};
+                prims.push_back(p);
+            }
+        } else if (ps.topology == GBR_TOPOLOGY_LINE_STRIP) {
+            if (!separated) {
+                for (uint32_t k = 0; k + 1 < n; ++k) prims.push_back({k, k + 1, 0});  // tuple_windows
+            } else {  // Strip<2> with separators (primitive.rs:287-322)
+                int cnt = 0;
+                uint32_t last = 0;
+                for (uint32_t k = 0; k < n; ++k) {
+                    if (is_sep[k]) {
+                        cnt = 0;
+                        continue;
+                    }
+                    if (cnt == 1) prims.push_back({last, k, 0});
+                    last = k;
+                    cnt = 1;
+                }
+            }
+        } else {  // triangle strip
+            if (!separated) {  // TriStripIter (primitive.rs:394-426)
+                for (uint32_t p = 0; p + 2 < n; ++p) {
+                    uint32_t t[3];
+                    strip_tri(p, t);
+                    prims.push_back({t[0], t[1], t[2]});
+                }
+            } else {  // ResetTriStripIter (primitive.rs:428-487)
+                uint32_t seg[3];
+                int fill = 0;
+                bool odd = false;
+                uint32_t buf[2];
+                for (uint32_t k = 0; k < n; ++k) {
+                    if (is_sep[k]) {
+                        fill = 0;
+                        continue;
+                    }
+                    if (fill < 2) {
+                        seg[fill] = k;
+                        ++fill;
+                        if (fill == 2) {
+                            buf[0] = seg[0];
+                            buf[1] = seg[1];
+                            odd = false;
+                        }
+                        continue;
+                    }
+                    prims.push_back({buf[0], buf[1], k});  // TriStripGenerator::push
+                    buf[odd ? 1 : 0] = k;
+                    odd = !odd;
+                }
+            }
+        }
+
+        for (size_t prim_index = 0; prim_index < prims.size(); ++prim_index) {
+            const auto& pr = prims[prim_index];
+            ex->cnt.primitives++;
+            if (nv == 3) {
+                const VsOut* verts[3] = {&vout[pr[0]], &vout[pr[1]], &vout[pr[2]]};
+                V4 pos[3] = {verts[0]->position, verts[1]->position, verts[2]->position};
+                bool ccw;
+                if (!tri_face_ccw(pos, &ccw)) fail(GBR_ERR_VALIDATION, "clip position w=0 (primitive.rs:177)");
+                bool front_facing = (ccw ? GBR_FRONT_FACE_CCW : GBR_FRONT_FACE_CW) == ps.front_face;
+                bool cull = ps.cull_mode == GBR_CULL_FRONT ? front_facing
+                            : ps.cull_mode == GBR_CULL_BACK ? !front_facing
+                                                            : false;
+                if (cull) continue;
+                float inv_w[3] = {1.0f / pos[0].w, 1.0f / pos[1].w, 1.0f / pos[2].w};
+                std::vector<ClipTri> subs;
+                clip_tri(pos, subs);
+                for (const ClipTri& sub : subs) {
+                    // TriRasterizer::rasterize (raster.rs:280-363)
+                    RasterPoint rp[3];
+                    for (int i = 0; i < 3; ++i)
+                        if (!to_raster(tr, sub.v[i].position, &rp[i])) fail(GBR_ERR_VALIDATION, "w=0 (raster.rs:146)");
+                    P2 va = {rp[0].frag.x, rp[0].frag.y}, vb = {rp[1].frag.x, rp[1].frag.y},
+                       vc = {rp[2].frag.x, rp[2].frag.y};
+                    float total = shoelace(va, vb, vc);
+                    if (total == 0.0f) continue;
+                    Bary3 clipb[3] = {sub.v[0].bary, sub.v[1].bary, sub.v[2].bary};
+                    V4 frags[3] = {rp[0].frag, rp[1].frag, rp[2].frag};
+                    uint32_t fxs[3] = {rp[0].fbx, rp[1].fbx, rp[2].fbx}, fys[3] = {rp[0].fby, rp[1].fby, rp[2].fby};
+                    bool ok = scanlines(fxs, fys, [&](const Scanline& sl) {
+                        if (sl.y < (int64_t)ex->band_y0 || sl.y >= (int64_t)ex->band_y1) return;
+                        for (int64_t x = sl.x1; x <= sl.x2; ++x) {
+                            uint32_t px = (uint32_t)x, py = (uint32_t)sl.y;
+                            if (!in_scissor(tr, px, py)) continue;
+                            P2 p = {(float)px, (float)py};
+                            Bary3 lam = {{shoelace(p, vb, vc) / total, shoelace(va, p, vc) / total,
+                                          shoelace(va, vb, p) / total}};
+                            Bary3 comp = compose_bary(clipb, lam);
+                            V4 fragment = interp3_v4(frags, comp);
+                            process_fragment(fc, px, py, fragment, front_facing, (uint32_t)prim_index, 3, comp.c,
+                                             verts, inv_w);
+                        }
+                    });
+                    if (!ok) fail(GBR_ERR_VALIDATION, "scanlines generated points that don't fit u32");
+                }
+            } else if (nv == 2) {
+                const VsOut* verts[3] = {&vout[pr[0]], &vout[pr[1]], nullptr};
+                V4 pts[2] = {verts[0]->position, verts[1]->position};
+                float alphas[2];
+                if (!clip_line(pts, alphas)) continue;
+                RasterPoint s, e;
+                if (!to_raster(tr, pts[0], &s) || !to_raster(tr, pts[1], &e)) fail(GBR_ERR_VALIDATION, "w=0");
+                float inv_w[3] = {1.0f / verts[0]->position.w, 1.0f / verts[1]->position.w, 0.0f};
+                bresenham(s.fbx, s.fby, e.fbx, e.fby, [&](uint32_t px, uint32_t py, float t) {
+                    if (py < ex->band_y0 || py >= ex->band_y1) return;
+                    if (!in_scissor(tr, px, py)) return;
+                    // Lerp(t).interpolate([Lerp(a0), Lerp(a1)]) (raster.rs:248-254)
+                    float T = alphas[0] * (1.0f - t) + alphas[1] * t;
+                    V4 fragment = v4_add(v4_mul(s.frag, 1.0f - T), v4_mul(e.frag, T));
+                    float coeff[3] = {1.0f - T, T, 0.0f};
+                    // Lerp::interpolate for the inter-stage values: v0*(1-T) + v1*T
+                    process_fragment(fc, px, py, fragment, true, (uint32_t)prim_index, 2, coeff, verts, inv_w);
+                });
+            } else {
+                const VsOut* verts[3] = {&vout[pr[0]], nullptr, nullptr};
+                RasterPoint r;
+                if (!to_raster(tr, verts[0]->position, &r)) fail(GBR_ERR_VALIDATION, "w=0");
+                if (r.fby < ex->band_y0 || r.fby >= ex->band_y1) continue;
+                if (!in_scissor(tr, r.fbx, r.fby)) continue;
+                float coeff[3] = {1.0f, 0.0f, 0.0f};
+                float inv_w[3] = {1.0f / verts[0]->position.w, 0.0f, 0.0f};
+                process_fragment(fc, r.fbx, r.fby, r.frag, true, (uint32_t)prim_index, 1, coeff, verts, inv_w);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------ command stream
+struct Cursor {
+    const uint8_t* p;
+    const uint8_t* end;
+};
+
+template <class T>
+static const T* payload(const gbr_cmd_header* h, const uint8_t* body) {
+    if (h->payload_bytes < sizeof(T)) fail(GBR_ERR_INVALID_ARGUMENT, "command %u payload too short", h->opcode);
+    return reinterpret_cast<const T*>(body);
+}
+
+struct DecodedPass {
+    gbr_cmd_begin_render_pass begin;
+    std::vector<std::pair<gbr_cmd_header, std::vector<uint8_t>>> cmds;
+};
+
+static std::vector<DecodedPass> decode_stream(const uint8_t* data, uint64_t len) {
+    std::vector<DecodedPass> passes;
+    uint64_t off = 0;
+    DecodedPass* cur = nullptr;
+    while (off < len) {
+        if (len - off < sizeof(gbr_cmd_header)) fail(GBR_ERR_INVALID_ARGUMENT, "truncated command header");
+        gbr_cmd_header h;
+        std::memcpy(&h, data + off, sizeof h);
+        off += sizeof h;
+        uint64_t padded = (h.payload_bytes + 7ull) & ~7ull;
+        if (len - off < padded) fail(GBR_ERR_INVALID_ARGUMENT, "truncated command payload");
+        const uint8_t* body = data + off;
+        off += padded;
+        if (h.opcode == GBR_OP_BEGIN_RENDER_PASS) {
+            if (cur) fail(GBR_ERR_INVALID_ARGUMENT, "nested render pass");
+            passes.emplace_back();
+            cur = &passes.back();
+            std::memcpy(&cur->begin, payload<gbr_cmd_begin_render_pass>(&h, body), sizeof cur->begin);
+        } else if (h.opcode == GBR_OP_END_RENDER_PASS) {
+            if (!cur) fail(GBR_ERR_INVALID_ARGUMENT, "end without begin");
+            cur = nullptr;
+        } else {
+            if (!cur) fail(GBR_ERR_INVALID_ARGUMENT, "command %u outside a render pass", h.opcode);
+            cur->cmds.emplace_back(h, std::vector<uint8_t>(body, body + h.payload_bytes));
+        }
+    }
+    if (cur) fail(GBR_ERR_INVALID_ARGUMENT, "render pass not ended");
+    return passes;
+}
+
+// texture.rs:199-211 (clear_color / clear_depth) for rows [y0, y1).
+static void clear_targets(Exec* ex, const DecodedPass& dp) {
+    PassTargets* tg = ex->tg;
+    for (uint32_t a = 0; a < dp.begin.color_attachment_count && a < GBR_MAX_COLOR_TARGETS; ++a) {
+        const gbr_color_attachment& ca = dp.begin.color_attachments[a];
+        Texture* t = tg->color[a];
+        if (!t || ca.load_op != GBR_LOAD_OP_CLEAR) continue;
+        V4 c = {(float)ca.clear_value[0], (float)ca.clear_value[1], (float)ca.clear_value[2], (float)ca.clear_value[3]};
+        for (uint32_t y = ex->band_y0; y < ex->band_y1; ++y)
+            for (uint32_t x = 0; x < t->desc.size.width; ++x) write_color(t, x, y, tg->color_slice[a], c, ex->profile);
+    }
+    if (tg->depth && dp.begin.depth_attachment.has_depth_ops &&
+        dp.begin.depth_attachment.depth_load_op == GBR_LOAD_OP_CLEAR) {
+        float* d = reinterpret_cast<float*>(tg->depth->mips[0].data());
+        uint32_t w = tg->depth->desc.size.width;
+        for (uint32_t y = ex->band_y0; y < ex->band_y1; ++y)
+            std::fill(d + (size_t)y * w, d + (size_t)(y + 1) * w, dp.begin.depth_attachment.depth_clear_value);
+    }
+}
+
+static void run_pass_band(Exec* ex, const DecodedPass& dp) {
+    Device* dev = ex->dev;
+    clear_targets(ex, dp);
+    PassState st;
+    st.viewport[0] = 0.0f;
+    st.viewport[1] = 0.0f;
+    st.viewport[2] = (float)ex->tg->width;
+    st.viewport[3] = (float)ex->tg->height;
+    st.viewport[4] = 0.0f;
+    st.viewport[5] = 1.0f;
+    st.scissor[0] = 0;
+    st.scissor[1] = 0;
+    st.scissor[2] = ex->tg->width;
+    st.scissor[3] = ex->tg->height;
+    for (const auto& c : dp.cmds) {
+        const gbr_cmd_header& h = c.first;
+        const uint8_t* b = c.second.data();
+        switch (h.opcode) {
+            case GBR_OP_SET_PIPELINE:
+                st.pipeline = dev->get<Pipeline>(payload<gbr_cmd_set_pipeline>(&h, b)->pipeline, "pipeline");
+                break;
+            case GBR_OP_SET_BIND_GROUP: {
+                auto* p = payload<gbr_cmd_set_bind_group>(&h, b);
+                if (p->index >= GBR_MAX_BIND_GROUPS) fail(GBR_ERR_VALIDATION, "bind group index");
+                st.groups[p->index] = p->bind_group ? dev->get<BindGroup>(p->bind_group, "bind group") : nullptr;
+                break;
+            }
+            case GBR_OP_SET_INDEX_BUFFER: {
+                auto* p = payload<gbr_cmd_set_index_buffer>(&h, b);
+                Buffer* buf = dev->get<Buffer>(p->buffer, "buffer");
+                uint64_t size = p->size ? p->size : buf->data.size() - p->offset;
+                if (p->offset + size > buf->data.size()) fail(GBR_ERR_VALIDATION, "index buffer slice out of range");
+                st.index = {buf, p->offset, size};
+                st.index_format = p->index_format;
+                break;
+            }
+            case GBR_OP_SET_VERTEX_BUFFER: {
+                auto* p = payload<gbr_cmd_set_vertex_buffer>(&h, b);
+                if (p->slot >= GBR_MAX_VERTEX_BUFFERS) fail(GBR_ERR_VALIDATION, "vertex buffer slot");
+                Buffer* buf = dev->get<Buffer>(p->buffer, "buffer");
+                uint64_t size = p->size ? p->size : buf->data.size() - p->offset;
+                if (p->offset + size > buf->data.size()) fail(GBR_ERR_VALIDATION, "vertex buffer slice out of range");
+                st.vb[p->slot] = {buf, p->offset, size};
+                break;
+            }
+            case GBR_OP_SET_VIEWPORT: {
+                auto* p = payload<gbr_cmd_set_viewport>(&h, b);
+                st.viewport[0] = p->x;
+                st.viewport[1] = p->y;
+                st.viewport[2] = p->width;
+                st.viewport[3] = p->height;
+                st.viewport[4] = p->min_depth;
+                st.viewport[5] = p->max_depth;
+                break;
+            }
+            case GBR_OP_SET_SCISSOR_RECT: {
+                auto* p = payload<gbr_cmd_set_scissor_rect>(&h, b);
+                st.scissor[0] = p->x;
+                st.scissor[1] = p->y;
+                st.scissor[2] = p->width;
+                st.scissor[3] = p->height;
+                break;
+            }
+            case GBR_OP_SET_BLEND_CONSTANT: {
+                auto* p = payload<gbr_cmd_set_blend_constant>(&h, b);
+                for (int k = 0; k < 4; ++k) st.blend_constant[k] = p->color[k];
+                break;
+            }
+            case GBR_OP_SET_STENCIL_REFERENCE: break;
+            case GBR_OP_DRAW: {
+                auto* p = payload<gbr_cmd_draw>(&h, b);
+                execute_draw(ex, st, false, p->vertex_start, p->vertex_end, 0, p->instance_start, p->instance_end);
+                break;
+            }
+            case GBR_OP_DRAW_INDEXED: {
+                auto* p = payload<gbr_cmd_draw_indexed>(&h, b);
+                execute_draw(ex, st, true, p->index_start, p->index_end, p->base_vertex, p->instance_start,
+                             p->instance_end);
+                break;
+            }
+            default: fail(GBR_ERR_INVALID_ARGUMENT, "unknown opcode %u", h.opcode);
+        }
+    }
+}
+
+static void execute_pass(Device* dev, const DecodedPass& dp, Counters& total) {
+    // State::new (render_pass/state.rs:77-133): all attachments must have the same size.
+    PassTargets tg;
+    bool have = false;
+    auto size_of = [&](Texture* t) {
+        if (!have) {
+            tg.width = t->desc.size.width;
+            tg.height = t->desc.size.height;
+            have = true;
+        } else if (tg.width != t->desc.size.width || tg.height != t->desc.size.height) {
+            fail(GBR_ERR_VALIDATION, "All render attachments must be the same size");
+        }
+    };
+    for (uint32_t a = 0; a < dp.begin.color_attachment_count && a < GBR_MAX_COLOR_TARGETS; ++a) {
+        const gbr_color_attachment& ca = dp.begin.color_attachments[a];
+        if (!ca.view) continue;
+        Texture* t = dev->get<Texture>(ca.view, "texture");
+        tg.color[a] = t;
+        tg.color_slice[a] = ca.depth_slice;
+        size_of(t);
+    }
+    if (dp.begin.has_depth_attachment && dp.begin.depth_attachment.view) {
+        Texture* t = dev->get<Texture>(dp.begin.depth_attachment.view, "texture");
+        if (t->desc.format != GBR_TEXTURE_FORMAT_DEPTH32_FLOAT) fail(GBR_ERR_UNSUPPORTED, "depth format");
+        tg.depth = t;
+        size_of(t);
+    }
+    int nt = std::max(1, g_threads);
+    if ((uint32_t)nt > tg.height) nt = std::max(1u, tg.height);
+    std::vector<Exec> ex(nt);
+    std::vector<std::string> errs(nt);
+    std::vector<gbr_status> sts(nt, GBR_OK);
+    auto work = [&](int i) {
+        ex[i].dev = dev;
+        ex[i].profile = dev->profile;
+        ex[i].tg = &tg;
+        ex[i].band_y0 = (uint32_t)((uint64_t)tg.height * i / nt);
+        ex[i].band_y1 = (uint32_t)((uint64_t)tg.height * (i + 1) / nt);
+        try {
+            run_pass_band(&ex[i], dp);
+        } catch (const Error& e) {
+            sts[i] = e.status;
+            errs[i] = e.msg;
+        }
+    };
+    if (nt == 1) {
+        work(0);
+    } else {
+        std::vector<std::thread> th;
+        for (int i = 0; i < nt; ++i) th.emplace_back(work, i);
+        for (auto& t : th) t.join();
+    }
+    for (int i = 0; i < nt; ++i)
+        if (sts[i] != GBR_OK) throw Error{sts[i], errs[i]};
+    total.fragments += ex[0].cnt.fragments;
+    for (int i = 1; i < nt; ++i) total.fragments += ex[i].cnt.fragments;
+    total.primitives += ex[0].cnt.primitives;  // every thread assembles all primitives
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+#define ORC_TRY(...)                               \
+    try {                                          \
+        __VA_ARGS__;                                   \
+        return GBR_OK;                             \
+    } catch (const Error& e) {                     \
+        g_last_error = e.msg;                      \
+        return e.status;                           \
+    } catch (const std::exception& e) {            \
+        g_last_error = e.what();                   \
+        return GBR_ERR_OUT_OF_MEMORY;              \
+    }
+
+ORC_API size_t orc_last_error(char* buf, size_t len) {
+    if (buf && len) {
+        size_t n = std::min(len - 1, g_last_error.size());
+        std::memcpy(buf, g_last_error.data(), n);
+        buf[n] = 0;
+    }
+    return g_last_error.size();
+}
+ORC_API uint32_t orc_abi_version(void) { return GBR_ABI_VERSION; }
+ORC_API void orc_set_threads(int n) { g_threads = n < 1 ? 1 : n; }
+
+ORC_API gbr_status orc_device_create(const gbr_device_config* cfg, gbr_device* out) {
+    ORC_TRY({
+        if (!cfg || !out) fail(GBR_ERR_INVALID_ARGUMENT, "null argument");
+        if (cfg->abi_version != GBR_ABI_VERSION) fail(GBR_ERR_INVALID_ARGUMENT, "ABI version mismatch");
+        auto d = std::make_unique<Device>();
+        d->profile = cfg->profile;
+        std::lock_guard<std::mutex> lk(g_devices_mu);
+        uint64_t h = g_next_device++;
+        g_devices[h] = std::move(d);
+        *out = h;
+    })
+}
+ORC_API gbr_status orc_device_destroy(gbr_device d) {
+    ORC_TRY({
+        std::lock_guard<std::mutex> lk(g_devices_mu);
+        if (!g_devices.erase(d)) fail(GBR_ERR_INVALID_ARGUMENT, "invalid device handle");
+    })
+}
+ORC_API gbr_status orc_device_limits(gbr_device d, gbr_limits* out) {
+    ORC_TRY({
+        get_device(d);
+        out->max_texture_dimension_2d = 16384;
+        out->max_bind_groups = GBR_MAX_BIND_GROUPS;
+        out->max_vertex_buffers = GBR_MAX_VERTEX_BUFFERS;
+        out->max_vertex_attributes = GBR_MAX_VERTEX_ATTRIBUTES;
+        out->max_color_attachments = GBR_MAX_COLOR_TARGETS;
+        out->max_inter_stage_components = 32;
+        out->max_buffer_size = 1ull << 36;
+    })
+}
+ORC_API gbr_status orc_buffer_create(gbr_device d, uint64_t size, uint32_t usage, gbr_buffer* out) {
+    ORC_TRY({
+        (void)usage;
+        Device* dev = get_device(d);
+        auto* b = new Buffer;
+        b->data.assign(size, 0);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        *out = dev->add(b);
+    })
+}
+ORC_API gbr_status orc_buffer_destroy(gbr_device d, gbr_buffer b) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        dev->get<Buffer>(b, "buffer");
+        dev->objects.erase(b);
+    })
+}
+ORC_API gbr_status orc_queue_write_buffer(gbr_device d, gbr_buffer b, uint64_t offset, const void* data, uint64_t size) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        Buffer* buf = dev->get<Buffer>(b, "buffer");
+        if (offset + size > buf->data.size()) fail(GBR_ERR_VALIDATION, "write_buffer out of range");
+        std::memcpy(buf->data.data() + offset, data, size);
+    })
+}
+ORC_API gbr_status orc_buffer_read(gbr_device d, gbr_buffer b, uint64_t offset, void* dst, uint64_t size) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        Buffer* buf = dev->get<Buffer>(b, "buffer");
+        if (offset + size > buf->data.size()) fail(GBR_ERR_VALIDATION, "buffer read out of range");
+        std::memcpy(dst, buf->data.data() + offset, size);
+    })
+}
+ORC_API gbr_status orc_texture_create(gbr_device d, const gbr_texture_desc* desc, gbr_texture* out) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        uint32_t bpp = bytes_per_texel(desc->format);
+        if (!bpp) fail(GBR_ERR_UNSUPPORTED, "Unsupported texture format: %u", desc->format);
+        auto* t = new Texture;
+        t->desc = *desc;
+        if (t->desc.size.depth_or_array_layers == 0) t->desc.size.depth_or_array_layers = 1;
+        t->bpp = bpp;
+        // The reference stores mip 0 only (texture.rs:34-43); the extension profile keeps the chain.
+        uint32_t mips = desc->mip_level_count ? desc->mip_level_count : 1;
+        t->mips_stored = dev->profile == GBR_PROFILE_EXTENSION ? mips : 1;
+        t->mips.resize(t->mips_stored);
+        for (uint32_t m = 0; m < t->mips_stored; ++m)
+            t->mips[m].assign((size_t)t->mip_w(m) * t->mip_h(m) * t->desc.size.depth_or_array_layers * bpp, 0);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        *out = dev->add(t);
+    })
+}
+ORC_API gbr_status orc_texture_destroy(gbr_device d, gbr_texture t) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        dev->get<Texture>(t, "texture");
+        dev->objects.erase(t);
+    })
+}
+// QueueInterface::write_texture (device.rs:371-434): whole texture, whole rows.
+ORC_API gbr_status orc_queue_write_texture(gbr_device d, gbr_texture tex, uint32_t mip, const void* data,
+                                           uint64_t data_size, const gbr_texel_copy_buffer_layout* layout,
+                                           gbr_extent3d size) {
+    ORC_TRY({
+        (void)size;  // shadowed by the texture size in the reference (device.rs:388)
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        Texture* t = dev->get<Texture>(tex, "texture");
+        if (mip >= t->mips_stored) fail(GBR_ERR_UNSUPPORTED, "write to mip_level %u (device.rs:378-380)", mip);
+        uint32_t w = t->mip_w(mip), h = t->mip_h(mip), layers = t->desc.size.depth_or_array_layers;
+        uint64_t row = layout->bytes_per_row ? layout->bytes_per_row : data_size;
+        uint64_t rows_per_image = layout->rows_per_image ? layout->rows_per_image : h;
+        uint64_t dst_row = (uint64_t)w * t->bpp;
+        if (row < dst_row) fail(GBR_ERR_VALIDATION, "bytes_per_row too small");
+        const uint8_t* src = static_cast<const uint8_t*>(data);
+        uint8_t* dst = t->mips[mip].data();
+        for (uint32_t z = 0; z < layers; ++z)
+            for (uint32_t y = 0; y < h; ++y) {
+                uint64_t so = layout->offset + (z * rows_per_image + y) * row;
+                if (so + dst_row > data_size) fail(GBR_ERR_VALIDATION, "write_texture source out of range");
+                std::memcpy(dst + ((uint64_t)z * h + y) * dst_row, src + so, dst_row);
+            }
+    })
+}
+ORC_API gbr_status orc_texture_read(gbr_device d, gbr_texture tex, uint32_t mip, void* dst, uint64_t size) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        Texture* t = dev->get<Texture>(tex, "texture");
+        if (mip >= t->mips_stored) fail(GBR_ERR_VALIDATION, "mip level not stored");
+        if (size < t->mips[mip].size()) fail(GBR_ERR_VALIDATION, "destination too small");
+        std::memcpy(dst, t->mips[mip].data(), t->mips[mip].size());
+    })
+}
+ORC_API gbr_status orc_sampler_create(gbr_device d, const gbr_sampler_desc* desc, gbr_sampler* out) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        auto* s = new Sampler;
+        s->s.desc = *desc;
+        std::lock_guard<std::mutex> lk(dev->mu);
+        *out = dev->add(s);
+    })
+}
+ORC_API gbr_status orc_sampler_destroy(gbr_device d, gbr_sampler s) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        dev->get<Sampler>(s, "sampler");
+        dev->objects.erase(s);
+    })
+}
+ORC_API gbr_status orc_shader_module_create_native(gbr_device d, const char* name, gbr_shader_module* out) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        const Program* p = find_program(name);
+        if (!p) fail(GBR_ERR_SHADER, "unknown native program '%s'", name);
+        auto* m = new ShaderModule;
+        m->prog = p;
+        std::lock_guard<std::mutex> lk(dev->mu);
+        *out = dev->add(m);
+    })
+}
+ORC_API gbr_status orc_shader_module_destroy(gbr_device d, gbr_shader_module m) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        dev->get<ShaderModule>(m, "shader module");
+        dev->objects.erase(m);
+    })
+}
+ORC_API gbr_status orc_render_pipeline_create(gbr_device d, const gbr_render_pipeline_desc* desc,
+                                              gbr_render_pipeline* out) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        auto pl = std::make_unique<Pipeline>();
+        pl->desc = *desc;
+        pl->vs = dev->get<ShaderModule>(desc->vertex_module, "shader module")->prog;
+        pl->fs = desc->has_fragment ? dev->get<ShaderModule>(desc->fragment_module, "shader module")->prog : nullptr;
+        std::memset(pl->loc, 0, sizeof pl->loc);
+        if (desc->vertex_buffer_count > GBR_MAX_VERTEX_BUFFERS) fail(GBR_ERR_VALIDATION, "too many vertex buffers");
+        // VertexState::new (vertex.rs:50-94): location -> (buffer, offset, size); duplicates panic.
+        for (uint32_t b = 0; b < desc->vertex_buffer_count; ++b) {
+            const gbr_vertex_buffer_layout& L = desc->vertex_buffers[b];
+            for (uint32_t a = 0; a < L.attribute_count && a < GBR_MAX_VERTEX_ATTRIBUTES; ++a) {
+                const gbr_vertex_attribute& at = L.attributes[a];
+                if (at.shader_location >= 16) fail(GBR_ERR_VALIDATION, "shader location out of range");
+                if (pl->loc[at.shader_location].present)
+                    fail(GBR_ERR_VALIDATION, "Duplicate vertex attribute at location %u", at.shader_location);
+                pl->loc[at.shader_location] = {true, b, at.offset, at.format};
+            }
+        }
+        *out = dev->add(pl.release());
+    })
+}
+ORC_API gbr_status orc_render_pipeline_destroy(gbr_device d, gbr_render_pipeline p) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        dev->get<Pipeline>(p, "pipeline");
+        dev->objects.erase(p);
+    })
+}
+ORC_API gbr_status orc_bind_group_create(gbr_device d, const gbr_bind_group_desc* desc, gbr_bind_group* out) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        auto* g = new BindGroup;
+        g->desc = *desc;
+        std::lock_guard<std::mutex> lk(dev->mu);
+        *out = dev->add(g);
+    })
+}
+ORC_API gbr_status orc_bind_group_destroy(gbr_device d, gbr_bind_group g) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        dev->get<BindGroup>(g, "bind group");
+        dev->objects.erase(g);
+    })
+}
+// Submission executes immediately on the calling thread (the engine loop of engine.rs:26-46
+// without the thread hop).
+ORC_API gbr_status orc_queue_submit(gbr_device d, const void* cmds, uint64_t len, uint64_t* out_index) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        auto passes = decode_stream(static_cast<const uint8_t*>(cmds), len);
+        uint64_t idx = dev->next_submission++;
+        Counters total;
+        uint64_t draws = 0;
+        for (const auto& p : passes) {
+            for (const auto& c : p.cmds)
+                if (c.first.opcode == GBR_OP_DRAW || c.first.opcode == GBR_OP_DRAW_INDEXED) ++draws;
+            execute_pass(dev, p, total);
+        }
+        gbr_submission_stats s;
+        std::memset(&s, 0, sizeof s);
+        s.submission_index = idx;
+        s.draws = draws;
+        s.primitives_in = total.primitives;
+        s.fragments_shaded = total.fragments;
+        s.batched_with = 1;
+        dev->stats[idx] = s;
+        if (out_index) *out_index = idx;
+    })
+}
+ORC_API gbr_status orc_device_poll(gbr_device d, uint32_t wait, uint32_t has_index, uint64_t index, uint64_t timeout_ns,
+                                   uint32_t* out_status) {
+    ORC_TRY({
+        (void)has_index;
+        (void)index;
+        (void)timeout_ns;
+        get_device(d);
+        if (out_status) *out_status = wait ? GBR_POLL_QUEUE_EMPTY : GBR_POLL_POLL;
+    })
+}
+ORC_API gbr_status orc_submission_stats_get(gbr_device d, uint64_t index, gbr_submission_stats* out) {
+    ORC_TRY({
+        Device* dev = get_device(d);
+        std::lock_guard<std::mutex> lk(dev->mu);
+        auto it = dev->stats.find(index);
+        if (it == dev->stats.end()) fail(GBR_ERR_INVALID_ARGUMENT, "unknown submission");
+        *out = it->second;
+    })
+}
+
+// ------------------------------------------------------------------ stage-level entry points
+// used by the known-answer tests that replay the reference's unit tests.
+
+// TriClipper::clip_tri; out: per triangle 3 x (x, y, z, w, b0, b1, b2).  Returns the count.
+ORC_API int orc_kat_clip_tri(const float* pos12, float* out, int max_tris) {
+    V4 pos[3];
+    for (int i = 0; i < 3; ++i) pos[i] = {pos12[4 * i], pos12[4 * i + 1], pos12[4 * i + 2], pos12[4 * i + 3]};
+    std::vector<ClipTri> r;
+    clip_tri(pos, r);
+    int n = (int)r.size();
+    for (int t = 0; t < n && t < max_tris; ++t)
+        for (int i = 0; i < 3; ++i) {
+            float* o = out + (t * 3 + i) * 7;
+            const ClipVertex& v = r[t].v[i];
+            o[0] = v.position.x;
+            o[1] = v.position.y;
+            o[2] = v.position.z;
+            o[3] = v.position.w;
+            o[4] = v.bary.c[0];
+            o[5] = v.bary.c[1];
+            o[6] = v.bary.c[2];
+        }
+    return n;
+}
+// cohen_sutherland::clip; returns 1 with out8/alphas2 filled, 0 for None.
+ORC_API int orc_kat_clip_line(const float* pos8, float* out8, float* alphas2) {
+    V4 p[2] = {{pos8[0], pos8[1], pos8[2], pos8[3]}, {pos8[4], pos8[5], pos8[6], pos8[7]}};
+    if (!clip_line(p, alphas2)) return 0;
+    float v[8] = {p[0].x, p[0].y, p[0].z, p[0].w, p[1].x, p[1].y, p[1].z, p[1].w};
+    std::memcpy(out8, v, sizeof v);
+    return 1;
+}
+// scanlines; out rows of (y, x1, x2).  Returns the row count or -1 when the reference panics.
+ORC_API int orc_kat_scanlines(const uint32_t* xy6, int64_t* out, int max_rows) {
+    uint32_t fx[3] = {xy6[0], xy6[2], xy6[4]}, fy[3] = {xy6[1], xy6[3], xy6[5]};
+    int n = 0;
+    bool ok = scanlines(fx, fy, [&](const Scanline& s) {
+        if (n < max_rows) {
+            out[3 * n] = s.y;
+            out[3 * n + 1] = s.x1;
+            out[3 * n + 2] = s.x2;
+        }
+        ++n;
+    });
+    return ok ? n : -1;
+}
+ORC_API void orc_kat_bubblesort3(int64_t* v) {
+    bubblesort3(v, [](int64_t x) { return x; });
+}
+ORC_API int orc_kat_bresenham(uint32_t sx, uint32_t sy, uint32_t ex, uint32_t ey, uint32_t* out_xy, float* out_t,
+                              int max_pts) {
+    int n = 0;
+    bresenham(sx, sy, ex, ey, [&](uint32_t x, uint32_t y, float t) {
+        if (n < max_pts) {
+            out_xy[2 * n] = x;
+            out_xy[2 * n + 1] = y;
+            out_t[n] = t;
+        }
+        ++n;
+    });
+    return n;
+}
+// TriFace::front_face: 1 = Ccw, 0 = Cw, -1 = w == 0.
+ORC_API int orc_kat_tri_face(const float* pos12) {
+    V4 pos[3];
+    for (int i = 0; i < 3; ++i) pos[i] = {pos12[4 * i], pos12[4 * i + 1], pos12[4 * i + 2], pos12[4 * i + 3]};
+    bool ccw;
+    if (!tri_face_ccw(pos, &ccw)) return -1;
+    return ccw ? 1 : 0;
+}
+ORC_API void orc_kat_strip_tri(uint32_t p, uint32_t* out3) { strip_tri(p, out3); }
+ORC_API uint16_t orc_kat_f32_to_f16(float f) { return f32_to_f16_rne(f); }
+ORC_API float orc_kat_f16_to_f32(uint16_t h) { return f16_to_f32(h); }
+// TextureDataLayout::byte_size (texture.rs:251-302)
+ORC_API uint64_t orc_kat_texture_byte_size(uint32_t w, uint32_t h, uint32_t layers, uint32_t format) {
+    return (uint64_t)w * h * layers * bytes_per_texel(format);
+}

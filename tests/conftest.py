@@ -1,0 +1,14 @@
+"""Test configuration: registers the `gpu` marker and puts the package on sys.path."""
+
+import os
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+PKG_DIR = os.path.join(ROOT, "wgpu-cpu_gb300")
+for p in (ROOT, PKG_DIR, os.path.join(ROOT, "tests")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
