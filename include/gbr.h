@@ -159,11 +159,18 @@ typedef struct gbr_device_config {
     uint32_t tile_size;         /* raster tile side: 8, 16 or 32 (0 = default 16)            */
     uint32_t bin_capacity;      /* max primitives sorted per tile in one window (0 = auto)   */
     uint32_t warps_per_tile;    /* 1..8 (0 = default)                                        */
+    uint32_t launch_mode;       /* gbr_launch_mode                                           */
     uint32_t batch_submissions; /* 1 = the worker merges queued submissions into one launch  */
     uint32_t use_graphs;        /* 1 = replay per-shape CUDA graphs                          */
+    uint32_t time_kernels;      /* 1 = CUDA events around the raster kernels (stats.raster_ms) */
     uint64_t hbm_budget_bytes;  /* transient (per-submission) memory budget; 0 = 80 GB       */
     uint64_t reserved[4];
 } gbr_device_config;
+
+/* How draws map to kernel launches.
+ *  PER_PASS — all draws of a render pass go through one setup/bin/raster launch sequence.
+ *  PER_DRAW — the plain drop-in: one launch sequence per draw, each over the whole target. */
+enum gbr_launch_mode { GBR_LAUNCH_PER_PASS = 0, GBR_LAUNCH_PER_DRAW = 1 };
 
 typedef struct gbr_limits {
     uint32_t max_texture_dimension_2d;
@@ -299,6 +306,7 @@ typedef struct gbr_submission_stats {
     double submit_to_fence_ms;     /* submit -> fence signalled       */
     uint32_t batched_with;         /* number of submissions merged into the same launch */
     uint32_t _pad;
+    double raster_ms;              /* device time of the raster kernels (config.time_kernels) */
 } gbr_submission_stats;
 
 /* ---------------------------------------------------------------- command stream
@@ -467,6 +475,13 @@ GBR_API gbr_status gbr_device_poll(gbr_device device, uint32_t wait, uint32_t ha
 /* Metrics of a finished submission (tracing events in the reference, see struct comment). */
 GBR_API gbr_status gbr_submission_stats_get(gbr_device device, uint64_t submission_index,
                                             gbr_submission_stats* out_stats);
+/* No reference counterpart (measurement): device time in milliseconds from the start of
+ * submission `first` to the end of submission `last`, from CUDA events on the device stream. */
+GBR_API gbr_status gbr_device_elapsed_ms(gbr_device device, uint64_t first_submission, uint64_t last_submission,
+                                         double* out_ms);
+/* No reference counterpart (measurement): enqueues a write of a 256 MiB scratch buffer on the
+ * device stream, evicting the L2 cache between timed submissions. */
+GBR_API gbr_status gbr_device_flush_caches(gbr_device device);
 
 #ifdef __cplusplus
 }

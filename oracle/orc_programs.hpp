@@ -163,6 +163,13 @@ static bool vs_quad_color(const VsIn& in, const ProgramBindings&, VsOut& out) {
     return true;
 }
 
+// ---- clip_passthrough: clip-space position (vec4f) and an RGBA colour straight through.
+static bool vs_clip_passthrough(const VsIn& in, const ProgramBindings&, VsOut& out) {
+    out.position = {in.attr[0][0], in.attr[0][1], in.attr[0][2], in.attr[0][3]};
+    for (int k = 0; k < 4; ++k) out.var[0][k] = in.attr[1][k];
+    return true;
+}
+
 // ---- mesh_color_discard: mesh_color that discards fragments whose red channel is below 0.5
 // (exercises `discard` = EntryPointError::Killed, fragment.rs:202-208).
 static void fs_mesh_color_discard(const FsIn& in, const ProgramBindings&, FsOut& out) {
@@ -187,6 +194,8 @@ static const Program kPrograms[] = {
      vs_mesh_tex_lambert, fs_mesh_tex_lambert},
     {"quad_color", 2, {{0, 3, SK_F32}, {1, 4, SK_F32}}, 1, {{0, 4, INTERP_LINEAR}}, 1, 0, {}, vs_quad_color,
      fs_passthrough_vec4},
+    {"clip_passthrough", 2, {{0, 4, SK_F32}, {1, 4, SK_F32}}, 1, {{0, 4, INTERP_LINEAR}}, 1, 0, {},
+     vs_clip_passthrough, fs_passthrough_vec4},
 };
 
 static inline const Program* find_program(const char* name) {

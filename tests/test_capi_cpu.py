@@ -1,0 +1,93 @@
+"""CPU-only checks of the drop-in boundary: libgbr.so loads, exports every entry point that
+include/gbr.h declares, and the ctypes mirror has the C header's struct layouts."""
+
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "gbr.h")
+
+
+def declared_symbols():
+    text = open(HEADER).read()
+    return sorted(set(re.findall(r"GBR_API\s+[\w\s\*]+?\b(gbr_\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def libgbr():
+    import build_lib
+
+    path = build_lib.build()
+    return ctypes.CDLL(path)
+
+
+def test_header_declares_entry_points():
+    syms = declared_symbols()
+    assert "gbr_device_create" in syms and "gbr_queue_submit" in syms and len(syms) >= 25
+
+
+def test_library_exports_every_declared_symbol(libgbr):
+    missing = [s for s in declared_symbols() if not hasattr(libgbr, s)]
+    assert not missing, missing
+
+
+def test_abi_version(libgbr):
+    libgbr.gbr_abi_version.restype = ctypes.c_uint32
+    assert libgbr.gbr_abi_version() == 1
+
+
+def test_device_create_without_gpu_fails_cleanly(libgbr):
+    """With no CUDA device the call returns an error status instead of crashing."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from wgpu_gb300 import _abi as A
+
+    cfg = A.DeviceConfig()
+    cfg.abi_version = 1
+    out = ctypes.c_uint64()
+    lib = A.Lib(libgbr, "gbr_")
+    st = lib.device_create(ctypes.byref(cfg), ctypes.byref(out))
+    assert st != 0
+    assert lib.error_text()
+
+
+STRUCTS = ["gbr_device_config", "gbr_limits", "gbr_texture_desc", "gbr_texel_copy_buffer_layout", "gbr_sampler_desc",
+           "gbr_vertex_attribute", "gbr_vertex_buffer_layout", "gbr_color_target_state", "gbr_primitive_state",
+           "gbr_depth_stencil_state", "gbr_render_pipeline_desc", "gbr_bind_group_entry", "gbr_bind_group_desc",
+           "gbr_submission_stats", "gbr_color_attachment", "gbr_depth_attachment", "gbr_cmd_begin_render_pass",
+           "gbr_cmd_set_bind_group", "gbr_cmd_set_index_buffer", "gbr_cmd_set_vertex_buffer", "gbr_cmd_set_viewport",
+           "gbr_cmd_draw", "gbr_cmd_draw_indexed"]
+PY = ["DeviceConfig", "Limits", "TextureDesc", "TexelCopyBufferLayout", "SamplerDesc", "VertexAttribute",
+      "VertexBufferLayout", "ColorTargetState", "PrimitiveState", "DepthStencilState", "RenderPipelineDesc",
+      "BindGroupEntry", "BindGroupDesc", "SubmissionStats", "ColorAttachment", "DepthAttachment",
+      "CmdBeginRenderPass", "CmdSetBindGroup", "CmdSetIndexBuffer", "CmdSetVertexBuffer", "CmdSetViewport",
+      "CmdDraw", "CmdDrawIndexed"]
+
+
+def test_ctypes_layouts_match_header(tmp_path):
+    from wgpu_gb300 import _abi as A
+
+    src = tmp_path / "sizes.c"
+    src.write_text('#include "gbr.h"\n#include <stdio.h>\nint main(void){\n' +
+                   "".join(f'printf("%zu\\n", sizeof({s}));\n' for s in STRUCTS) + "return 0;}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    sizes = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    for c_name, py_name, n in zip(STRUCTS, PY, sizes):
+        assert ctypes.sizeof(getattr(A, py_name)) == n, (c_name, ctypes.sizeof(getattr(A, py_name)), n)
+
+
+def test_gpu_path_has_no_fallback(monkeypatch, tmp_path):
+    """The product raises when libgbr.so is absent instead of routing anywhere else."""
+    from wgpu_gb300 import api
+
+    monkeypatch.setattr(api, "LIB_PATH", str(tmp_path / "missing.so"))
+    monkeypatch.setattr(api, "_gpu_lib", None)
+    with pytest.raises(RuntimeError):
+        api.gpu_lib()

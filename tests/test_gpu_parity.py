@@ -1,0 +1,201 @@
+"""GPU parity: the CUDA path (libgbr.so through the C ABI) against the oracle on the same seeded
+inputs.  Colour and depth must be bit-exact and the fragment-shader invocation count equal; the
+f16 blend target (extension profile) is compared to within 1 f16 ULP, though it is expected to
+match exactly as well."""
+
+import numpy as np
+import pytest
+
+import oracle_device
+import scenes
+from wgpu_gb300 import api as W
+from wgpu_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def gpu():
+    d = W.Device()
+    yield d
+    d.close()
+
+
+@pytest.fixture(scope="module")
+def gpu_ext():
+    d = W.Device(profile=W.Profile.EXTENSION)
+    yield d
+    d.close()
+
+
+@pytest.fixture(scope="module")
+def orc():
+    return oracle_device.device(threads=8)
+
+
+@pytest.fixture(scope="module")
+def orc_ext():
+    return oracle_device.device(profile=W.Profile.EXTENSION, threads=8)
+
+
+def assert_same(a, b, what=""):
+    (ca, da, na), (cb, db, nb) = a, b
+    diff = (ca != cb).any(-1)
+    assert not diff.any(), f"{what}: {int(diff.sum())} colour pixels differ, first at {np.argwhere(diff)[:3].tolist()}"
+    if da is not None or db is not None:
+        dd = da.view(np.uint32) != db.view(np.uint32)
+        assert not dd.any(), f"{what}: {int(dd.sum())} depth values differ"
+    assert na == nb, f"{what}: fragments {na} vs {nb}"
+
+
+@pytest.mark.parametrize("ff,cull", [(W.FrontFace.CW, W.Face.BACK), (W.FrontFace.CW, W.Face.FRONT),
+                                     (W.FrontFace.CCW, W.Face.BACK), (W.FrontFace.CCW, W.Face.NONE)])
+def test_reference_triangle(gpu, orc, ff, cull):
+    res = [scenes.render_scene(d, wl.scene_reference_triangle, front_face=ff, cull_mode=cull) for d in (gpu, orc)]
+    assert_same(*res, "colored_triangle")
+
+
+def test_colored_sphere_512(gpu, orc):
+    res = [scenes.render_scene(d, wl.scene_colored_sphere) for d in (gpu, orc)]
+    assert_same(*res, "colored sphere 512x512")
+    assert res[0][2] > 50000
+
+
+@pytest.mark.parametrize("cull", [W.Face.NONE, W.Face.FRONT])
+def test_colored_sphere_cull_modes(gpu, orc, cull):
+    res = [scenes.render_scene(d, wl.scene_colored_sphere, width=300, height=200, cull=cull) for d in (gpu, orc)]
+    assert_same(*res, f"cull {cull}")
+
+
+def test_textured_icosphere_small(gpu, orc):
+    kw = dict(width=480, height=270, level=4, tex_size=256)
+    res = [scenes.render_scene(d, wl.scene_textured_icosphere, **kw) for d in (gpu, orc)]
+    assert_same(*res, "textured icosphere level 4")
+
+
+def test_textured_icosphere_full(gpu, orc):
+    """The textured-mesh workload at full size: 81,920 triangles, 1920x1080 + Depth32Float."""
+    res = [scenes.render_scene(d, wl.scene_textured_icosphere) for d in (gpu, orc)]
+    assert_same(*res, "textured icosphere level 6 1080p")
+    assert res[0][2] > 500000
+
+
+@pytest.mark.parametrize("address", [W.AddressMode.CLAMP_TO_EDGE, W.AddressMode.MIRROR_REPEAT])
+def test_textured_address_modes(gpu, orc, address):
+    kw = dict(width=256, height=160, level=3, tex_size=64, address=address)
+    res = [scenes.render_scene(d, wl.scene_textured_icosphere, **kw) for d in (gpu, orc)]
+    assert_same(*res, f"address mode {address}")
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_random_clip_triangles(gpu, orc, seed):
+    """Triangles crossing every clip plane: sub-triangle order, the clipped-depth composition and
+    degenerate spans."""
+    kw = dict(n_tris=400, width=160, height=120, seed=seed)
+    res = [scenes.random_clip_triangles(d, **kw) for d in (gpu, orc)]
+    assert_same(*res, f"random clip seed {seed}")
+
+
+@pytest.mark.parametrize("compare", [W.CompareFunction.LESS, W.CompareFunction.LESS_EQUAL, W.CompareFunction.GREATER,
+                                     W.CompareFunction.GREATER_EQUAL, W.CompareFunction.EQUAL,
+                                     W.CompareFunction.NOT_EQUAL, W.CompareFunction.ALWAYS, W.CompareFunction.NEVER])
+def test_depth_compare_functions(gpu, orc, compare):
+    kw = dict(n_tris=300, width=128, height=96, seed=11, depth=compare, z_range=(0.0, 1.0), spread=0.9)
+    res = [scenes.random_clip_triangles(d, **kw) for d in (gpu, orc)]
+    assert_same(*res, f"depth compare {compare}")
+
+
+def test_depth_write_disabled(gpu, orc):
+    kw = dict(n_tris=300, width=128, height=96, seed=12, depth=W.CompareFunction.LESS, depth_write=False,
+              z_range=(0.0, 1.0), spread=0.9)
+    res = [scenes.random_clip_triangles(d, **kw) for d in (gpu, orc)]
+    assert_same(*res, "depth write disabled")
+
+
+def test_strip_u16_instances_base_vertex(gpu, orc):
+    kw = dict(n_tris=120, width=128, height=96, seed=5, topology=W.PrimitiveTopology.TRIANGLE_STRIP,
+              index_format=W.IndexFormat.UINT16, instances=3, base_vertex=7, cull=W.Face.BACK,
+              depth=W.CompareFunction.LESS_EQUAL, z_range=(0.0, 1.0))
+    res = [scenes.random_clip_triangles(d, **kw) for d in (gpu, orc)]
+    assert_same(*res, "strip/u16/instances/base_vertex")
+
+
+def test_direct_draw_scissor_viewport(gpu, orc):
+    kw = dict(n_tris=200, width=200, height=150, seed=8, scissor=(17, 9, 150, 101),
+              viewport=(-30.0, 12.5, 260.0, 120.0, 0.0, 1.0))
+    res = [scenes.random_clip_triangles(d, **kw) for d in (gpu, orc)]
+    assert_same(*res, "scissor + viewport")
+
+
+def test_bgra_target(gpu, orc):
+    kw = dict(n_tris=100, width=96, height=64, seed=9, color_format=W.TextureFormat.BGRA8_UNORM)
+    res = [scenes.random_clip_triangles(d, **kw) for d in (gpu, orc)]
+    assert_same(*res, "bgra8")
+
+
+@pytest.mark.parametrize("tile,warps", [(8, 1), (8, 2), (16, 2), (16, 4), (32, 4), (32, 8)])
+def test_tile_configurations(orc, tile, warps):
+    dev = W.Device(tile_size=tile, warps_per_tile=warps)
+    try:
+        kw = dict(n_tris=300, width=150, height=110, seed=21, depth=W.CompareFunction.LESS, z_range=(0.0, 1.0))
+        res = [scenes.random_clip_triangles(d, **kw) for d in (dev, orc)]
+        assert_same(*res, f"tile {tile} warps {warps}")
+    finally:
+        dev.close()
+
+
+def test_per_draw_launch_mode_matches(orc):
+    dev = W.Device(launch_mode=W.LaunchMode.PER_DRAW)
+    try:
+        res = [scenes.render_scene(d, wl.scene_textured_icosphere, width=320, height=180, level=3, tex_size=64)
+               for d in (dev, orc)]
+        assert_same(*res, "per-draw mode")
+    finally:
+        dev.close()
+
+
+def test_tiny_bins_force_retry(orc):
+    """A bin capacity far too small makes the first launch run out of scratch; the worker
+    grows it and re-runs, with the same result."""
+    dev = W.Device(bin_capacity=64)
+    try:
+        res = [scenes.render_scene(d, wl.scene_colored_sphere, width=200, height=200) for d in (dev, orc)]
+        assert_same(*res, "bin retry")
+    finally:
+        dev.close()
+
+
+def test_blended_quads_f16(gpu_ext, orc_ext):
+    """Extension profile: Rgba16Float + ALPHA_BLENDING in painter order."""
+    kw = dict(width=320, height=192, n_quads=300, size_lo=8, size_hi=160)
+    (cg, _, ng), (co, _, no) = [scenes.render_scene(d, wl.scene_blended_quads, **kw) for d in (gpu_ext, orc_ext)]
+    assert ng == no
+    hg = cg.view(np.uint16).astype(np.int32)
+    ho = co.view(np.uint16).astype(np.int32)
+    assert np.abs(hg - ho).max() <= 1  # within 1 f16 ULP (same-sign finite values)
+    assert (hg == ho).mean() > 0.999
+
+
+def test_discard_program(gpu, orc):
+    def build(dev):
+        s = wl.scene_colored_sphere(dev, 200, 160)
+        sm = dev.create_shader_module(native="mesh_color_discard")
+        pl = dev.create_render_pipeline(
+            sm, [W.VertexBufferLayout(24, [W.VertexAttribute(3, 0, 0), W.VertexAttribute(3, 12, 1)])],
+            W.PrimitiveState(cull_mode=W.Face.BACK), None, sm, [W.ColorTargetState(W.TextureFormat.RGBA8_UNORM)])
+        s.draws[0] = (pl,) + s.draws[0][1:]
+        return s
+    res = [scenes.render_scene(d, build) for d in (gpu, orc)]
+    assert_same(*res, "discard")
+
+
+def test_errors_are_reported(gpu):
+    s = wl.scene_colored_sphere(gpu, 64, 64)
+    pl, groups, vbs, ib, rng, bv = s.draws[0]
+    s.draws[0] = (pl, groups, vbs, ib, range(0, rng.stop + 3), bv)
+    with pytest.raises(W.GbrError) as e:
+        s.render()
+    assert e.value.status == -4
+    # the device stays usable after a failed submission
+    s2 = wl.scene_colored_sphere(gpu, 64, 64)
+    s2.render()

@@ -1,0 +1,68 @@
+// exact.cuh — IEEE binary32 building blocks that reproduce wgpu-cpu's scalar arithmetic bit for
+// bit on the GPU.  Every operation is an explicitly rounded intrinsic (__fadd_rn, __fmul_rn,
+// ...), which the compiler never contracts into FMA, and the library is also built with
+// --fmad=false.  The order of operations in each helper is the reference's order.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "gbr_types.h"
+
+namespace gbr {
+
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+struct V4 {
+    float x, y, z, w;
+};
+
+__device__ __forceinline__ V4 v4_mul(V4 a, float s) { return {fmul(a.x, s), fmul(a.y, s), fmul(a.z, s), fmul(a.w, s)}; }
+__device__ __forceinline__ V4 v4_add(V4 a, V4 b) { return {fadd(a.x, b.x), fadd(a.y, b.y), fadd(a.z, b.z), fadd(a.w, b.w)}; }
+
+// nalgebra 0.34 `Matrix::dot` for 4-vectors (blas.rs `dotx`): (p0 + p2) + (p1 + p3).
+__device__ __forceinline__ float dot4(V4 a, V4 b) {
+    float p0 = fmul(a.x, b.x), p1 = fmul(a.y, b.y), p2 = fmul(a.z, b.z), p3 = fmul(a.w, b.w);
+    return fadd(fadd(p0, p2), fadd(p1, p3));
+}
+
+// Rust f32::max(v, 0.0) as used by to_raster (raster.rs:150-151); NaN -> 0, -0 -> +0.
+__device__ __forceinline__ float rust_max0(float v) { return v > 0.0f ? v : 0.0f; }
+
+// Rust `v as u32` (saturating, NaN -> 0).
+__device__ __forceinline__ uint32_t rust_f2u32(float v) {
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 4294967296.0f) return 0xFFFFFFFFu;
+    return __float2uint_rz(v);
+}
+
+// f32_to_u8 of TexelWriter::from_color (texture.rs:378-381): (v*255).clamp(0,255) as u8.
+__device__ __forceinline__ uint32_t unorm8_trunc(float v) {
+    float s = fmul(v, 255.0f);
+    if (s < 0.0f) s = 0.0f;
+    if (s > 255.0f) s = 255.0f;
+    if (!(s > 0.0f)) return 0u;  // NaN and zero
+    return __float2uint_rz(s);
+}
+
+// shoelace (raster.rs:294-298), left to right.
+__device__ __forceinline__ float shoelace(float ax, float ay, float bx, float by, float cx, float cy) {
+    float t1 = fmul(fsub(by, ay), fadd(bx, ax));
+    float t2 = fmul(fsub(cy, by), fadd(cx, bx));
+    float t3 = fmul(fsub(ay, cy), fadd(ax, cx));
+    return fadd(fadd(t1, t2), t3);
+}
+
+// Integer division truncating toward zero for d > 0 (Rust isize `/`), 32-bit fast path.
+__device__ __forceinline__ int64_t div_trunc(int64_t n, int64_t d) {
+    if (n >= -2147483647ll && n <= 2147483647ll && d <= 2147483647ll) return (int64_t)((int32_t)n / (int32_t)d);
+    return n / d;
+}
+
+__device__ __forceinline__ uint16_t f32_to_f16_bits(float f) { return __half_as_ushort(__float2half_rn(f)); }
+__device__ __forceinline__ float f16_bits_to_f32(uint16_t h) { return __half2float(__ushort_as_half(h)); }
+
+}  // namespace gbr

@@ -1,0 +1,193 @@
+// gbr_types.h — plain-old-data structures shared by the host runtime and the CUDA kernels of
+// the render-pass path.  Everything here is device-resident per launch batch.
+#pragma once
+
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define GBR_HD __host__ __device__
+#else
+#define GBR_HD
+#endif
+
+namespace gbr {
+
+enum : uint32_t {
+    MAX_VARYING_LOCATIONS = 4,  // inter-stage @location slots carried per vertex
+    MAX_VARYING_FLOATS = 16,    // 4 locations x vec4
+    SUBTRI_BITS = 6,            // a clipped triangle yields at most 2^6 sub-triangles
+};
+
+// Native shader programs compiled into the library (the same WGSL programs as
+// shaders/*.wgsl, written by hand in CUDA).
+enum Program : uint32_t {
+    PROG_COLORED_TRIANGLE = 0,
+    PROG_MESH_COLOR = 1,
+    PROG_MESH_COLOR_PERSPECTIVE = 2,
+    PROG_MESH_COLOR_DISCARD = 3,
+    PROG_MESH_TEX_LAMBERT = 4,
+    PROG_QUAD_COLOR = 5,
+    PROG_CLIP_PASSTHROUGH = 6,
+    PROG_COUNT = 7
+};
+
+enum Interp : uint8_t { INTERP_LINEAR = 0, INTERP_PERSPECTIVE = 1, INTERP_FLAT = 2 };
+
+enum ErrorCode : uint32_t {
+    ERR_NONE = 0,
+    ERR_W_ZERO = 1,            // clip position w == 0 (primitive.rs:177, raster.rs:146)
+    ERR_INDEX_OOB = 2,         // index buffer read out of range
+    ERR_VERTEX_OOB = 3,        // vertex attribute read out of range
+    ERR_BASE_VERTEX = 4,       // index + base_vertex overflows u32 (index.rs:55-57)
+    ERR_OVERFLOW_RECORDS = 5,  // more clipped sub-triangles than scratch slots (retried)
+    ERR_OVERFLOW_BINS = 6,     // more tile entries than scratch slots (retried)
+    ERR_SPAN_RANGE = 7,        // scanline coordinate outside u32 (scanline.rs:156-170)
+    ERR_UNSUPPORTED = 8,
+};
+
+// One texture binding as seen by the kernels.
+struct TexDesc {
+    const uint8_t* data;  // mip 0 .. mip n-1 back to back
+    uint32_t width, height;
+    uint32_t format;      // gbr_texture_format
+    uint32_t mip_count;
+    uint64_t mip_offset[16];
+};
+
+struct SamplerDescDev {
+    uint32_t address_u, address_v;
+    uint32_t mag_filter, min_filter, mip_filter;
+    float lod_min, lod_max;
+    uint32_t _pad;
+};
+
+// Where one vertex-shader input location comes from.
+struct AttrDesc {
+    int32_t buffer;   // -1 = absent
+    uint32_t format;  // gbr_vertex_format
+    uint32_t offset;
+    uint32_t _pad;
+};
+
+// A colour/depth target of a batch.
+struct TargetDesc {
+    uint8_t* color;        // null = no colour attachment
+    float* depth;          // null = no depth attachment
+    uint32_t width, height;
+    uint32_t color_format; // gbr_texture_format
+    uint32_t color_bpp;
+    uint32_t color_load;   // 1 = clear
+    uint32_t depth_load;   // 1 = clear, 0 = load, 2 = no depth ops (load)
+    float clear[4];        // colour clear value (f32, from wgpu::Color f64)
+    float depth_clear;
+    uint32_t tiles_x, tiles_y;
+    uint32_t tile_base;    // first global tile id of this target
+    uint32_t slice_offset; // byte offset of the depth_slice layer
+    uint32_t _pad[3];
+};
+
+// One draw call of a batch, fully resolved on the host.
+struct DrawDesc {
+    // primitive stream
+    uint32_t topology;       // gbr_primitive_topology
+    uint32_t index_format;   // 0 = direct draw, 1 = u16, 2 = u32
+    uint32_t first;          // first vertex (direct) or first index
+    uint32_t count;          // vertex / index count
+    int32_t base_vertex;
+    uint32_t instance_start;
+    uint32_t instance_count;
+    uint32_t prims_per_instance;
+    uint32_t prim_base;      // first global primitive id of this draw in the batch
+    uint32_t target;         // index into the batch's TargetDesc array
+    const uint8_t* index_data;
+    uint64_t index_bytes;
+    // vertex buffers
+    const uint8_t* vb_data[8];
+    uint64_t vb_size[8];
+    uint32_t vb_stride_vertex[8];
+    uint32_t vb_stride_instance[8];
+    AttrDesc attr[16];
+    // bindings
+    const uint8_t* uniform[4][8];
+    uint64_t uniform_size[4][8];
+    TexDesc tex;             // the one texture binding native programs use (group 1, binding 0)
+    SamplerDescDev samp;     // group 1, binding 1
+    // programs
+    uint32_t program;        // Program (VS and FS come from the same native module)
+    uint32_t has_fragment;
+    uint32_t num_varyings;   // floats per vertex carried to the FS
+    uint32_t profile;        // gbr_profile
+    // raster state
+    uint32_t cull_mode, front_face;
+    float vp_tx, vp_ty, vp_sx, vp_sy;
+    uint32_t sc_x0, sc_y0, sc_x1, sc_y1;  // scissor [x0, x1) x [y0, y1)
+    uint32_t depth_test;                  // pipeline has depth state AND target has depth
+    uint32_t depth_compare, depth_write;
+    uint32_t blend_enabled;
+    uint32_t blend_color[3], blend_alpha[3];  // src, dst, op
+    uint32_t write_mask;
+    float blend_constant[4];
+};
+
+// Per-sub-triangle record written by the setup kernel and read by binning and raster.
+// Fixed header followed by 3 x num_varyings floats (stride set per batch).
+struct TriRecord {
+    uint32_t key;        // global order key: prim << SUBTRI_BITS | sub
+    uint32_t draw;
+    uint32_t prim_index; // per-instance primitive index (the @builtin(primitive_index))
+    uint32_t flags;      // bit 0 front_facing, bit 1 empty, bits 2-3 span mode
+    int32_t row0, row1;  // rows emitted by the scanline state machine (inclusive)
+    int32_t xmin, xmax;  // min / max framebuffer x of the three vertices
+    int32_t sx[3], sy[3];// framebuffer vertices sorted by y (bubblesort3 order)
+    float vpx[3], vpy[3];// viewport coordinates of rasterize()'s a, b, c
+    float area;          // total_area (shoelace of a, b, c)
+    float fz[3], fw[3];  // fragment z and 1/w of a, b, c
+    float cb[9];         // clip barycentrics of a, b, c (3 x 3)
+    float inv_w0[3];     // 1/w of the unclipped vertices (perspective interpolation)
+    uint32_t ovf;        // primary record: first overflow slot of sub-triangles 1..nsub-1
+    uint32_t nsub;       // primary record: number of sub-triangles
+    uint32_t _pad[2];
+    // float var[3][num_varyings] follows
+};
+
+enum : uint32_t {
+    TRI_RECORD_HEADER_BYTES = sizeof(TriRecord),
+    SPAN_DEGENERATE = 1,  // all three vertices on one row: single span xmin..xmax
+};
+
+// Device-side status of a batch (zeroed before launch).
+struct BatchStatus {
+    uint32_t error;
+    uint32_t error_detail;
+    uint32_t ovf_used;        // overflow record slots used (may exceed capacity -> retry)
+    uint32_t _pad;
+    unsigned long long bin_entries;   // tile entries needed
+    unsigned long long fragments;     // fragment-shader invocations
+    unsigned long long primitives;    // primitives assembled
+};
+
+struct BatchParams {
+    const DrawDesc* draws;
+    const TargetDesc* targets;
+    uint32_t num_draws;
+    uint32_t num_targets;
+    uint32_t total_prims;     // sum over draws of prims_per_instance * instance_count
+    uint32_t total_tiles;
+    uint32_t tile_size;       // T
+    uint32_t tile_shift;      // log2(T)
+    uint32_t record_stride;   // bytes per record
+    uint32_t num_varyings;    // max floats per vertex over the batch's programs
+    uint8_t* records;         // total_prims primary records
+    uint8_t* ovf_records;     // overflow records
+    uint32_t ovf_capacity;
+    uint32_t bin_capacity;    // entries in `bins`
+    uint32_t* tile_count;     // [total_tiles + 1]
+    uint32_t* tile_offset;    // [total_tiles + 1]
+    uint32_t* tile_cursor;    // [total_tiles]
+    uint32_t* bins;           // keys
+    uint32_t* work_counter;   // persistent raster work queue
+    BatchStatus* status;
+    uint32_t* abort_flag;        // set by a failed batch; later batches of the submission skip
+};
+
+}  // namespace gbr

@@ -1,0 +1,209 @@
+// programs.cuh — the library's native shader programs: hand-written CUDA versions of the WGSL
+// programs in shaders/*.wgsl, evaluated with naga-cranelift's arithmetic (one rounded IEEE op
+// per WGSL operator, left to right; mat4x4f * vec4f as the column sum
+// ((v0*c0 + v1*c1) + v2*c2) + v3*c3, naga-cranelift/src/expression/binary.rs:273-325).
+//
+// Also here: vertex attribute fetch (render_pass/vertex.rs:128-156, 191-195) and the nearest
+// texture sampler of render_pass/binding.rs:93-164.
+#pragma once
+
+#include "exact.cuh"
+#include "gbr_types.h"
+
+namespace gbr {
+
+// gbr_vertex_format sizes (wgpu VertexFormat::size)
+__device__ __forceinline__ uint32_t vertex_format_size(uint32_t f) {
+    switch (f) {
+        case 1: case 5: case 6: case 7: case 9: return 4;  // f32, u32, i32, f16x2, unorm8x4
+        case 2: case 8: return 8;                          // f32x2, f16x4
+        case 3: return 12;
+        case 4: return 16;
+        default: return 0;
+    }
+}
+
+// Fetch `comps` f32 lanes of the attribute at `loc`.  In the parity profile the bytes are copied
+// as they are (the reference copies `format.size()` bytes into the shader input; the host
+// rejects pipelines whose format size differs from the input's); the extension profile
+// converts Float16x4 / Unorm8x4 to f32 as WebGPU does.
+__device__ __forceinline__ bool fetch_attr(const DrawDesc& d, int loc, int comps, uint32_t vertex, uint32_t instance,
+                                           float out[4], uint32_t* err) {
+    const AttrDesc a = d.attr[loc];
+    if (a.buffer < 0) {
+        *err = ERR_UNSUPPORTED;
+        return false;
+    }
+    const int b = a.buffer;
+    const uint64_t start = (uint64_t)instance * d.vb_stride_instance[b] + (uint64_t)vertex * d.vb_stride_vertex[b] +
+                           a.offset;
+    const uint32_t fsize = vertex_format_size(a.format);
+    if (start + fsize > d.vb_size[b]) {
+        *err = ERR_VERTEX_OOB;
+        return false;
+    }
+    const uint8_t* p = d.vb_data[b] + start;
+    if (a.format == 8 /* f16x4 */ && comps == 4) {
+        const uint16_t* h = reinterpret_cast<const uint16_t*>(p);
+        for (int k = 0; k < 4; ++k) out[k] = f16_bits_to_f32(__ldg(h + k));
+    } else if (a.format == 9 /* unorm8x4 */ && comps == 4) {
+        for (int k = 0; k < 4; ++k) out[k] = fdiv((float)__ldg(p + k), 255.0f);
+    } else {
+        const float* f = reinterpret_cast<const float*>(p);
+        for (int k = 0; k < comps; ++k) out[k] = __ldg(f + k);
+    }
+    return true;
+}
+
+__device__ __forceinline__ float ld_uniform(const DrawDesc& d, int group, int binding, uint32_t byte_off) {
+    return __ldg(reinterpret_cast<const float*>(d.uniform[group][binding] + byte_off));
+}
+
+// mat4x4f (column-major at group/binding/offset) * vec4f, column-sum order.
+__device__ __forceinline__ V4 mat4_mul_vec4(const DrawDesc& d, int group, int binding, V4 v) {
+    const float* m = reinterpret_cast<const float*>(d.uniform[group][binding]);
+    float r[4];
+#pragma unroll
+    for (int lane = 0; lane < 4; ++lane) {
+        float s = fmul(v.x, __ldg(m + 0 * 4 + lane));
+        s = fadd(s, fmul(v.y, __ldg(m + 1 * 4 + lane)));
+        s = fadd(s, fmul(v.z, __ldg(m + 2 * 4 + lane)));
+        s = fadd(s, fmul(v.w, __ldg(m + 3 * 4 + lane)));
+        r[lane] = s;
+    }
+    return {r[0], r[1], r[2], r[3]};
+}
+
+// texel_coordinate (render_pass/binding.rs:150-164)
+__device__ __forceinline__ uint32_t texel_coordinate(float x, uint32_t mode, uint32_t size) {
+    if (mode == 0) {  // ClampToEdge: f32::clamp keeps NaN
+        if (x < 0.0f) x = 0.0f;
+        if (x > 1.0f) x = 1.0f;
+    } else if (mode == 1) {  // Repeat: rem_euclid(1.0)
+        float r = fmodf(x, 1.0f);
+        x = (r < 0.0f) ? fadd(r, 1.0f) : r;
+    } else {  // MirrorRepeat: rem_euclid(2.0), fold
+        float r = fmodf(x, 2.0f);
+        r = (r < 0.0f) ? fadd(r, 2.0f) : r;
+        x = (r <= 1.0f) ? r : fsub(2.0f, r);
+    }
+    return rust_f2u32(roundf(fmul(x, (float)(size - 1u))));
+}
+
+// image_sample, nearest, mip 0 of an Rgba8 texture, `x as f32 / 255.0` per channel
+// (render_pass/binding.rs:93-140, texture.rs:170-188).
+__device__ __forceinline__ V4 sample_nearest_rgba8(const TexDesc& t, const SamplerDescDev& s, float u, float v) {
+    uint32_t x = texel_coordinate(u, s.address_u, t.width);
+    uint32_t y = texel_coordinate(v, s.address_v, t.height);
+    uint32_t px = __ldg(reinterpret_cast<const uint32_t*>(t.data) + (size_t)y * t.width + x);
+    return {fdiv((float)(px & 0xFFu), 255.0f), fdiv((float)((px >> 8) & 0xFFu), 255.0f),
+            fdiv((float)((px >> 16) & 0xFFu), 255.0f), fdiv((float)(px >> 24), 255.0f)};
+}
+
+// ---------------------------------------------------------------------------- programs
+// Number of f32 inter-stage values per vertex and their interpolation, by program.
+__host__ __device__ __forceinline__ uint32_t program_num_varyings(uint32_t prog) {
+    switch (prog) {
+        case PROG_COLORED_TRIANGLE: return 4;
+        case PROG_MESH_COLOR:
+        case PROG_MESH_COLOR_PERSPECTIVE:
+        case PROG_MESH_COLOR_DISCARD: return 3;
+        case PROG_MESH_TEX_LAMBERT: return 5;
+        case PROG_QUAD_COLOR:
+        case PROG_CLIP_PASSTHROUGH: return 4;
+        default: return 0;
+    }
+}
+__host__ __device__ __forceinline__ uint32_t program_interp(uint32_t prog) {
+    return prog == PROG_MESH_COLOR_PERSPECTIVE ? INTERP_PERSPECTIVE : INTERP_LINEAR;
+}
+
+// Vertex stage: position + varyings.  Returns false with *err set on a fetch error.
+__device__ __forceinline__ bool run_vs(const DrawDesc& d, uint32_t vertex, uint32_t instance, V4& pos, float* var,
+                                       uint32_t* err) {
+    float a0[4], a1[4], a2[4];
+    switch (d.program) {
+        case PROG_COLORED_TRIANGLE: {
+            uint32_t vi = vertex % 3u;
+            float x = (float)((int32_t)vi - 1);
+            float y = (float)((int32_t)(vi & 1u) * 2 - 1);
+            pos = {x, y, 0.0f, 1.0f};
+            var[0] = (float)(vi == 0u);
+            var[1] = (float)(vi == 1u);
+            var[2] = (float)(vi == 2u);
+            var[3] = 1.0f;
+            return true;
+        }
+        case PROG_MESH_COLOR:
+        case PROG_MESH_COLOR_PERSPECTIVE:
+        case PROG_MESH_COLOR_DISCARD: {
+            if (!fetch_attr(d, 0, 3, vertex, instance, a0, err)) return false;
+            if (!fetch_attr(d, 1, 3, vertex, instance, a1, err)) return false;
+            pos = mat4_mul_vec4(d, 0, 0, V4{a0[0], a0[1], a0[2], 1.0f});
+            var[0] = a1[0];
+            var[1] = a1[1];
+            var[2] = a1[2];
+            return true;
+        }
+        case PROG_MESH_TEX_LAMBERT: {
+            if (!fetch_attr(d, 0, 3, vertex, instance, a0, err)) return false;
+            if (!fetch_attr(d, 1, 3, vertex, instance, a1, err)) return false;
+            if (!fetch_attr(d, 2, 2, vertex, instance, a2, err)) return false;
+            pos = mat4_mul_vec4(d, 0, 0, V4{a0[0], a0[1], a0[2], 1.0f});
+            var[0] = a1[0];
+            var[1] = a1[1];
+            var[2] = a1[2];
+            var[3] = a2[0];
+            var[4] = a2[1];
+            return true;
+        }
+        case PROG_QUAD_COLOR: {
+            if (!fetch_attr(d, 0, 3, vertex, instance, a0, err)) return false;
+            if (!fetch_attr(d, 1, 4, vertex, instance, a1, err)) return false;
+            pos = {a0[0], a0[1], a0[2], 1.0f};
+            var[0] = a1[0];
+            var[1] = a1[1];
+            var[2] = a1[2];
+            var[3] = a1[3];
+            return true;
+        }
+        case PROG_CLIP_PASSTHROUGH: {
+            if (!fetch_attr(d, 0, 4, vertex, instance, a0, err)) return false;
+            if (!fetch_attr(d, 1, 4, vertex, instance, a1, err)) return false;
+            pos = {a0[0], a0[1], a0[2], a0[3]};
+            var[0] = a1[0];
+            var[1] = a1[1];
+            var[2] = a1[2];
+            var[3] = a1[3];
+            return true;
+        }
+        default: *err = ERR_UNSUPPORTED; return false;
+    }
+}
+
+// Fragment stage.  Returns false when the fragment is discarded.
+__device__ __forceinline__ bool run_fs(const DrawDesc& d, const float* var, V4& color) {
+    switch (d.program) {
+        case PROG_COLORED_TRIANGLE:
+        case PROG_QUAD_COLOR:
+        case PROG_CLIP_PASSTHROUGH: color = {var[0], var[1], var[2], var[3]}; return true;
+        case PROG_MESH_COLOR:
+        case PROG_MESH_COLOR_PERSPECTIVE: color = {var[0], var[1], var[2], 1.0f}; return true;
+        case PROG_MESH_COLOR_DISCARD:
+            if (var[0] < 0.5f) return false;
+            color = {var[0], var[1], var[2], 1.0f};
+            return true;
+        case PROG_MESH_TEX_LAMBERT: {
+            V4 t = sample_nearest_rgba8(d.tex, d.samp, var[3], var[4]);
+            float lx = ld_uniform(d, 0, 0, 64), ly = ld_uniform(d, 0, 0, 68), lz = ld_uniform(d, 0, 0, 72);
+            float dd = fadd(fmul(var[0], lx), fmul(var[1], ly));
+            dd = fadd(dd, fmul(var[2], lz));
+            float k = (dd > 0.0f) ? dd : 0.0f;  // select(0.0, d, d > 0.0)
+            color = {fmul(t.x, k), fmul(t.y, k), fmul(t.z, k), fmul(t.w, k)};
+            return true;
+        }
+        default: return false;
+    }
+}
+
+}  // namespace gbr

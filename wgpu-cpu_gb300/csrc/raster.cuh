@@ -1,0 +1,833 @@
+// raster.cuh — the render-pass kernels.
+//
+//   k_setup   one thread per primitive: index resolution, vertex fetch + vertex stage for the
+//             three corners, TriFace / cull, homogeneous clipping, viewport transform and the
+//             per-sub-triangle raster record; counts the screen tiles each record covers.
+//   k_scan    exclusive scan of the per-tile counts (bin offsets).
+//   k_fill    writes each record's order key into the bins of the tiles it covers.
+//   k_raster  persistent: one CTA per (target, tile) work item.  Sorts the tile's keys (the
+//             reference order: draw, instance, primitive, sub-triangle), then walks them in
+//             order; every thread owns pixels of the tile and keeps their colour and depth in
+//             registers, so per-pixel fragment order — and with it depth test, blending and
+//             last-writer-wins — is exactly the reference's sequential order.  The pass's
+//             LoadOp::Clear is fused into the register initialisation.
+//
+// Coverage, barycentrics, interpolation, depth and colour encoding restate render_pass/
+// raster.rs:129-363, util/scanline.rs:14-198, render_pass/fragment.rs:127-214,427-489 and
+// texture.rs:213-239,373-411, operation for operation.
+#pragma once
+
+#include "exact.cuh"
+#include "gbr_types.h"
+#include "programs.cuh"
+
+namespace gbr {
+
+__device__ __forceinline__ TriRecord* rec_at(uint8_t* base, uint32_t stride, uint32_t i) {
+    return reinterpret_cast<TriRecord*>(base + (size_t)i * stride);
+}
+__device__ __forceinline__ float* rec_var(TriRecord* r) { return reinterpret_cast<float*>(r + 1); }
+__device__ __forceinline__ const float* rec_var(const TriRecord* r) { return reinterpret_cast<const float*>(r + 1); }
+
+__device__ __forceinline__ void raise_error(BatchStatus* st, uint32_t code, uint32_t detail) {
+    if (atomicCAS(&st->error, 0u, code) == 0u) st->error_detail = detail;
+}
+
+__device__ __forceinline__ uint32_t find_draw(const DrawDesc* draws, uint32_t n, uint32_t prim) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&draws[mid].prim_base) <= prim) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+__device__ __forceinline__ uint32_t find_target(const TargetDesc* t, uint32_t n, uint32_t tile) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(&t[mid].tile_base) <= tile) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// ------------------------------------------------------------------------- clipping
+// tri_clip::Vertex (clipper.rs:590-613): clip position + barycentric w.r.t. the input triangle.
+struct CV {
+    V4 p;
+    float b[3];
+};
+
+__device__ __forceinline__ CV cv_lerp(const CV& a, const CV& c, float t) {
+    float omt = fsub(1.0f, t);
+    CV r;
+    r.p = v4_add(v4_mul(a.p, omt), v4_mul(c.p, t));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) r.b[k] = fadd(fmul(a.b[k], omt), fmul(c.b[k], t));
+    return r;
+}
+
+__device__ __forceinline__ V4 clip_plane(int i) {
+    switch (i) {
+        case 0: return {1.0f, 0.0f, 0.0f, 1.0f};
+        case 1: return {-1.0f, 0.0f, 0.0f, 1.0f};
+        case 2: return {0.0f, 1.0f, 0.0f, 1.0f};
+        case 3: return {0.0f, -1.0f, 0.0f, 1.0f};
+        case 4: return {0.0f, 0.0f, 1.0f, 0.0f};
+        default: return {0.0f, 0.0f, -1.0f, 1.0f};
+    }
+}
+
+// clip_tri_against_plane (clipper.rs:625-728): same case table, same output vertex orders.
+__device__ __forceinline__ int clip_against(const CV v[3], int plane, CV out[2][3]) {
+    V4 n = clip_plane(plane);
+    float d[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) d[i] = dot4(v[i].p, n);
+    bool o0 = d[0] < 0.0f, o1 = d[1] < 0.0f, o2 = d[2] < 0.0f;
+    auto clip = [&](int i, int j) { return cv_lerp(v[i], v[j], fdiv(d[i], fsub(d[i], d[j]))); };
+    if (o0 && o1 && o2) return 0;
+    if (!o0 && !o1 && !o2) {
+        out[0][0] = v[0]; out[0][1] = v[1]; out[0][2] = v[2];
+        return 1;
+    }
+    if (o0 && o1 && !o2) {
+        CV an = clip(2, 0), bn = clip(1, 2);
+        out[0][0] = an; out[0][1] = bn; out[0][2] = v[2];
+        return 1;
+    }
+    if (!o0 && o1 && o2) {
+        CV bn = clip(0, 1), cn = clip(2, 0);
+        out[0][0] = v[0]; out[0][1] = bn; out[0][2] = cn;
+        return 1;
+    }
+    if (o0 && !o1 && o2) {
+        CV an = clip(0, 1), cn = clip(1, 2);
+        out[0][0] = an; out[0][1] = v[1]; out[0][2] = cn;
+        return 1;
+    }
+    if (o0 && !o1 && !o2) {
+        CV bn = clip(0, 1), cn = clip(0, 2);
+        out[0][0] = bn; out[0][1] = v[1]; out[0][2] = cn;
+        out[1][0] = v[1]; out[1][1] = v[2]; out[1][2] = cn;
+        return 2;
+    }
+    if (!o0 && o1 && !o2) {
+        CV an = clip(0, 1), cn = clip(1, 2);
+        out[0][0] = v[0]; out[0][1] = an; out[0][2] = cn;
+        out[1][0] = v[0]; out[1][1] = cn; out[1][2] = v[2];
+        return 2;
+    }
+    CV bn = clip(1, 2), an = clip(0, 2);
+    out[0][0] = v[0]; out[0][1] = v[1]; out[0][2] = bn;
+    out[1][0] = v[0]; out[1][1] = bn; out[1][2] = an;
+    return 2;
+}
+
+// TriClipper::clip_tri (clipper.rs:756-776) processes the planes breadth first through a FIFO;
+// its output order is the lexicographic order of the split paths, which is what this
+// depth-first walk (first child first, second child parked on a stack) produces.
+template <class Emit>
+__device__ __noinline__ void clip_tri_ordered(const V4 pos[3], Emit& emit) {
+    struct Entry {
+        CV v[3];
+        int plane;
+    };
+    Entry stack[7];
+    int sp = 0;
+    Entry cur;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        cur.v[i].p = pos[i];
+        cur.v[i].b[0] = i == 0 ? 1.0f : 0.0f;
+        cur.v[i].b[1] = i == 1 ? 1.0f : 0.0f;
+        cur.v[i].b[2] = i == 2 ? 1.0f : 0.0f;
+    }
+    cur.plane = 0;
+    for (;;) {
+        bool dropped = false;
+        while (cur.plane < 6) {
+            CV out[2][3];
+            int m = clip_against(cur.v, cur.plane, out);
+            if (m == 0) {
+                dropped = true;
+                break;
+            }
+            if (m == 2 && sp < 7) {
+                stack[sp].v[0] = out[1][0];
+                stack[sp].v[1] = out[1][1];
+                stack[sp].v[2] = out[1][2];
+                stack[sp].plane = cur.plane + 1;
+                ++sp;
+            }
+            cur.v[0] = out[0][0];
+            cur.v[1] = out[0][1];
+            cur.v[2] = out[0][2];
+            cur.plane += 1;
+        }
+        if (!dropped) emit(cur.v);
+        if (sp == 0) break;
+        cur = stack[--sp];
+    }
+}
+
+__device__ __forceinline__ bool inside_all_planes(const V4 pos[3]) {
+#pragma unroll
+    for (int p = 0; p < 6; ++p) {
+        V4 n = clip_plane(p);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            if (dot4(pos[i], n) < 0.0f) return false;
+    }
+    return true;
+}
+
+// ------------------------------------------------------------------------- spans
+// The row's inclusive span [x1, x2] of the scanline state machine, in closed form
+// (util/scanline.rs:14-146): x1 on edge AC, x2 on AB before row b.y and on BC from row b.y.
+__device__ __forceinline__ void span_at(const TriRecord& r, int y, int& x1, int& x2) {
+    if (r.flags & (SPAN_DEGENERATE << 2)) {
+        x1 = r.xmin;
+        x2 = r.xmax;
+        return;
+    }
+    const int ax = r.sx[0], ay = r.sy[0], bx = r.sx[1], by = r.sy[1], cx = r.sx[2], cy = r.sy[2];
+    int64_t i = y - ay;
+    int64_t a = ax + div_trunc((int64_t)(cx - ax) * i, (int64_t)(cy - ay));
+    int64_t b;
+    if (y < by) b = ax + div_trunc((int64_t)(bx - ax) * i, (int64_t)(by - ay));
+    else b = bx + div_trunc((int64_t)(cx - bx) * (int64_t)(y - by), (int64_t)(cy - by));
+    x1 = (int)(a < b ? a : b);
+    x2 = (int)(a < b ? b : a);
+}
+
+// Calls f(tile_index_in_target) for every tile whose pixels the record can emit.
+template <class F>
+__device__ __forceinline__ void for_each_tile(const TriRecord& r, const DrawDesc& d, const TargetDesc& t, uint32_t shift,
+                                              F&& f) {
+    int lo = max(r.row0, (int)d.sc_y0);
+    int hi = min(r.row1, min((int)d.sc_y1 - 1, (int)t.height - 1));
+    if (lo > hi) return;
+    const int T = 1 << shift;
+    const int sx_hi = min((int)d.sc_x1 - 1, (int)t.width - 1);
+    const int sx_lo = (int)d.sc_x0;
+    for (int ty = lo >> shift; ty <= (hi >> shift); ++ty) {
+        int y0 = max(lo, ty << shift), y1 = min(hi, (ty << shift) + T - 1);
+        int xa, xb, mn, mx;
+        span_at(r, y0, xa, xb);
+        mn = xa; mx = xb;
+        span_at(r, y1, xa, xb);
+        mn = min(mn, xa); mx = max(mx, xb);
+        const int by = r.sy[1];
+        if (by - 1 >= y0 && by - 1 <= y1) {
+            span_at(r, by - 1, xa, xb);
+            mn = min(mn, xa); mx = max(mx, xb);
+        }
+        if (by >= y0 && by <= y1) {
+            span_at(r, by, xa, xb);
+            mn = min(mn, xa); mx = max(mx, xb);
+        }
+        mn = max(mn, sx_lo);
+        mx = min(mx, sx_hi);
+        if (mn > mx) continue;
+        for (int tx = mn >> shift; tx <= (mx >> shift); ++tx) f((uint32_t)ty * t.tiles_x + (uint32_t)tx);
+    }
+}
+
+// ------------------------------------------------------------------------- setup
+// to_raster (raster.rs:145-160)
+__device__ __forceinline__ bool to_raster(const DrawDesc& d, V4 c, uint32_t& fbx, uint32_t& fby, V4& frag) {
+    if (c.w == 0.0f) return false;
+    float nx = fdiv(c.x, c.w), ny = fdiv(c.y, c.w), nz = fdiv(c.z, c.w);
+    float pd = fdiv(1.0f, c.w);
+    float vx = rust_max0(fadd(fmul(nx, d.vp_sx), d.vp_tx));
+    float vy = rust_max0(fadd(fmul(ny, d.vp_sy), d.vp_ty));
+    fbx = rust_f2u32(vx);
+    fby = rust_f2u32(vy);
+    frag = {vx, vy, nz, pd};
+    return true;
+}
+
+// Index resolution (render_pass/index.rs:45-88) for stream position k of a draw.
+__device__ __forceinline__ bool resolve_vertex(const DrawDesc& d, uint32_t k, uint32_t& vertex, uint32_t* err) {
+    uint32_t pos = d.first + k;
+    if (d.index_format == 0) {
+        vertex = pos;
+        return true;
+    }
+    uint32_t raw;
+    if (d.index_format == 1) {
+        if ((uint64_t)(pos + 1) * 2 > d.index_bytes) { *err = ERR_INDEX_OOB; return false; }
+        raw = __ldg(reinterpret_cast<const uint16_t*>(d.index_data) + pos);
+    } else {
+        if ((uint64_t)(pos + 1) * 4 > d.index_bytes) { *err = ERR_INDEX_OOB; return false; }
+        raw = __ldg(reinterpret_cast<const uint32_t*>(d.index_data) + pos);
+    }
+    int64_t v = (int64_t)raw + (int64_t)d.base_vertex;  // u32::strict_add_signed
+    if (v < 0 || v > 0xFFFFFFFFll) { *err = ERR_BASE_VERTEX; return false; }
+    vertex = (uint32_t)v;
+    return true;
+}
+
+// Fills one sub-triangle record; returns false for a w == 0 vertex.
+__device__ __forceinline__ bool build_record(const BatchParams& bp, const DrawDesc& d, TriRecord* r, uint32_t key,
+                                             uint32_t draw, uint32_t prim_index, bool front_facing, const CV v[3],
+                                             const float inv_w0[3], const float var[3][MAX_VARYING_FLOATS],
+                                             uint32_t nvar) {
+    uint32_t fbx[3], fby[3];
+    V4 frag[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        if (!to_raster(d, v[i].p, fbx[i], fby[i], frag[i])) return false;
+    float area = shoelace(frag[0].x, frag[0].y, frag[1].x, frag[1].y, frag[2].x, frag[2].y);
+    // scanlines(): sort the framebuffer vertices by y with bubblesort3 (util/sort.rs:3-8)
+    int64_t px[3] = {fbx[0], fbx[1], fbx[2]}, py[3] = {fby[0], fby[1], fby[2]};
+    auto cas = [&](int l, int rr) {
+        if (py[l] > py[rr]) {
+            int64_t tx = px[l], tyy = py[l];
+            px[l] = px[rr]; py[l] = py[rr];
+            px[rr] = tx; py[rr] = tyy;
+        }
+    };
+    cas(0, 1);
+    cas(0, 2);
+    cas(1, 2);
+    uint32_t flags = front_facing ? 1u : 0u;
+    int64_t lim = 1ll << 30;
+    if (px[0] >= lim || px[1] >= lim || px[2] >= lim || py[2] >= lim) {
+        raise_error(bp.status, ERR_SPAN_RANGE, key);
+        flags |= 2u;
+    }
+    if (area == 0.0f) flags |= 2u;  // raster.rs:308-311: no fragments
+    int row0 = (int)py[0], row1;
+    if (py[2] == py[0]) {
+        flags |= SPAN_DEGENERATE << 2;
+        row1 = row0;
+    } else if (py[1] == py[0]) {
+        row1 = (int)py[2];
+    } else if (py[2] == py[1]) {
+        row1 = (int)py[1] - 1;  // the state machine stops before row c.y (scanline.rs:114-121)
+    } else {
+        row1 = (int)py[2];
+    }
+    r->key = key;
+    r->draw = draw;
+    r->prim_index = prim_index;
+    r->flags = flags;
+    r->row0 = row0;
+    r->row1 = row1;
+    r->xmin = (int)min(px[0], min(px[1], px[2]));
+    r->xmax = (int)max(px[0], max(px[1], px[2]));
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        r->sx[i] = (int)px[i];
+        r->sy[i] = (int)py[i];
+        r->vpx[i] = frag[i].x;
+        r->vpy[i] = frag[i].y;
+        r->fz[i] = frag[i].z;
+        r->fw[i] = frag[i].w;
+        r->inv_w0[i] = inv_w0[i];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) r->cb[i * 3 + j] = v[i].b[j];
+    }
+    r->area = area;
+    float* rv = rec_var(r);
+    for (uint32_t i = 0; i < 3; ++i)
+        for (uint32_t k = 0; k < nvar; ++k) rv[i * nvar + k] = var[i][k];
+    return true;
+}
+
+__device__ __forceinline__ void count_tiles(const BatchParams& bp, const TriRecord* r, const DrawDesc& d) {
+    if (r->flags & 2u) return;
+    const TargetDesc& t = bp.targets[d.target];
+    uint32_t base = t.tile_base;
+    for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) { atomicAdd(&bp.tile_count[base + lt], 1u); });
+}
+
+__global__ void __launch_bounds__(128) k_setup(BatchParams bp) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t gp = blockIdx.x * blockDim.x + threadIdx.x; gp < bp.total_prims; gp += stride) {
+        TriRecord* prim_rec = rec_at(bp.records, bp.record_stride, gp);
+        if (*bp.abort_flag) return;
+        const uint32_t di = find_draw(bp.draws, bp.num_draws, gp);
+        const DrawDesc& d = bp.draws[di];
+        const uint32_t local = gp - d.prim_base;
+        const uint32_t inst = local / d.prims_per_instance;
+        const uint32_t p = local - inst * d.prims_per_instance;
+        const uint32_t instance = d.instance_start + inst;
+        prim_rec->key = gp << SUBTRI_BITS;
+        prim_rec->flags = 2u;
+        prim_rec->nsub = 0;
+        prim_rec->draw = di;
+        uint32_t sp[3];
+        if (d.topology == 4) {  // triangle strip (primitive.rs:360-392)
+            sp[0] = (p & 1u) ? p + 1 : p;
+            sp[1] = (p & 1u) ? p : p + 1;
+            sp[2] = p + 2;
+        } else {
+            sp[0] = 3 * p;
+            sp[1] = 3 * p + 1;
+            sp[2] = 3 * p + 2;
+        }
+        V4 pos[3];
+        float var[3][MAX_VARYING_FLOATS];
+        uint32_t err = 0;
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            uint32_t vertex = 0;
+            ok = ok && resolve_vertex(d, sp[k], vertex, &err) && run_vs(d, vertex, instance, pos[k], var[k], &err);
+        }
+        if (!ok) {
+            raise_error(bp.status, err, gp);
+            continue;
+        }
+        if (!d.has_fragment) continue;
+        // TriFace (primitive.rs:169-197) and the cull decision (state.rs:542-561)
+        if (pos[0].w == 0.0f || pos[1].w == 0.0f || pos[2].w == 0.0f) {
+            raise_error(bp.status, ERR_W_ZERO, gp);
+            continue;
+        }
+        float n[3][2];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            n[i][0] = fdiv(pos[i].x, pos[i].w);
+            n[i][1] = fdiv(pos[i].y, pos[i].w);
+        }
+        float abx = fsub(n[1][0], n[0][0]), aby = fsub(n[1][1], n[0][1]);
+        float acx = fsub(n[2][0], n[0][0]), acy = fsub(n[2][1], n[0][1]);
+        bool ccw = fsub(fmul(abx, acy), fmul(aby, acx)) > 0.0f;
+        bool front_facing = (ccw ? 0u : 1u) == d.front_face;
+        bool cull = d.cull_mode == 1 ? front_facing : d.cull_mode == 2 ? !front_facing : false;
+        if (cull) continue;
+        const float inv_w0[3] = {fdiv(1.0f, pos[0].w), fdiv(1.0f, pos[1].w), fdiv(1.0f, pos[2].w)};
+        const uint32_t nvar = d.num_varyings;
+        if (inside_all_planes(pos)) {
+            CV v[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) {
+                v[i].p = pos[i];
+                v[i].b[0] = i == 0 ? 1.0f : 0.0f;
+                v[i].b[1] = i == 1 ? 1.0f : 0.0f;
+                v[i].b[2] = i == 2 ? 1.0f : 0.0f;
+            }
+            if (!build_record(bp, d, prim_rec, gp << SUBTRI_BITS, di, p, front_facing, v, inv_w0, var, nvar)) {
+                raise_error(bp.status, ERR_W_ZERO, gp);
+                prim_rec->flags = 2u;
+                continue;
+            }
+            prim_rec->nsub = 1;
+            prim_rec->ovf = 0;
+            count_tiles(bp, prim_rec, d);
+            continue;
+        }
+        // clipped: count the sub-triangles, reserve overflow slots, then emit in order
+        struct Counter {
+            uint32_t n;
+            __device__ void operator()(const CV*) { ++n; }
+        } counter{0};
+        clip_tri_ordered(pos, counter);
+        const uint32_t nsub = counter.n;
+        uint32_t ovf = 0;
+        if (nsub > 1) {
+            ovf = atomicAdd(&bp.status->ovf_used, nsub - 1);
+            if (ovf + nsub - 1 > bp.ovf_capacity) {
+                raise_error(bp.status, ERR_OVERFLOW_RECORDS, gp);
+                continue;
+            }
+        }
+        struct Emitter {
+            const BatchParams* bp;
+            const DrawDesc* d;
+            TriRecord* prim_rec;
+            uint32_t gp, di, p, ovf, s;
+            bool ff;
+            const float* inv_w0;
+            const float (*var)[MAX_VARYING_FLOATS];
+            uint32_t nvar;
+            __device__ void operator()(const CV* v) {
+                TriRecord* r = s == 0 ? prim_rec : rec_at(bp->ovf_records, bp->record_stride, ovf + s - 1);
+                if (!build_record(*bp, *d, r, (gp << SUBTRI_BITS) | s, di, p, ff, v, inv_w0, var, nvar)) {
+                    raise_error(bp->status, ERR_W_ZERO, gp);
+                    r->flags = 2u;
+                } else {
+                    count_tiles(*bp, r, *d);
+                }
+                ++s;
+            }
+        } emitter{&bp, &d, prim_rec, gp, di, p, ovf, 0, front_facing, inv_w0, var, nvar};
+        clip_tri_ordered(pos, emitter);
+        if (nsub == 0) prim_rec->flags = 2u;
+        prim_rec->nsub = nsub;
+        prim_rec->ovf = ovf;
+    }
+}
+
+// Single-CTA exclusive scan of tile counts -> tile_offset; zeroes tile_cursor.
+__global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
+    __shared__ uint32_t part[1024];
+    const uint32_t n = bp.total_tiles;
+    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t b = threadIdx.x * per, e = min(n, b + per);
+    uint32_t s = 0;
+    for (uint32_t i = b; i < e; ++i) s += bp.tile_count[i];
+    part[threadIdx.x] = s;
+    __syncthreads();
+    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
+        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - s;
+    for (uint32_t i = b; i < e; ++i) {
+        uint32_t c = bp.tile_count[i];
+        bp.tile_offset[i] = run;
+        bp.tile_cursor[i] = 0;
+        run += c;
+    }
+    if (threadIdx.x == blockDim.x - 1) {
+        bp.tile_offset[n] = part[blockDim.x - 1];
+        bp.status->bin_entries = part[blockDim.x - 1];
+        if (part[blockDim.x - 1] > bp.bin_capacity) raise_error(bp.status, ERR_OVERFLOW_BINS, part[blockDim.x - 1]);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
+    if (bp.status->error) return;
+    const uint32_t n_ovf = min(bp.status->ovf_used, bp.ovf_capacity);
+    const uint32_t total = bp.total_prims + n_ovf;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        const TriRecord* r = i < bp.total_prims ? rec_at(bp.records, bp.record_stride, i)
+                                                : rec_at(bp.ovf_records, bp.record_stride, i - bp.total_prims);
+        if (r->flags & 2u) continue;
+        const DrawDesc& d = bp.draws[r->draw];
+        const TargetDesc& t = bp.targets[d.target];
+        const uint32_t base = t.tile_base;
+        const uint32_t key = r->key;
+        for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) {
+            uint32_t tile = base + lt;
+            uint32_t pos = atomicAdd(&bp.tile_cursor[tile], 1u);
+            bp.bins[bp.tile_offset[tile] + pos] = key;
+        });
+    }
+}
+
+// ------------------------------------------------------------------------- raster
+// Ascending bitonic sort of n keys (n need not be a power of two: the comparators whose upper
+// index is >= n are skipped, as if those slots held +infinity).  All threads of the CTA call it.
+__device__ __forceinline__ void block_sort(uint32_t* a, uint32_t n) {
+    uint32_t N = 1;
+    while (N < n) N <<= 1;
+    const uint32_t half = N >> 1;
+    for (uint32_t k = 2; k <= N; k <<= 1) {
+        const uint32_t hk = k >> 1;
+        for (uint32_t i = threadIdx.x; i < half; i += blockDim.x) {
+            uint32_t blk = i / hk, off = i - blk * hk;
+            uint32_t lo = blk * k + off, hi = blk * k + k - 1 - off;
+            if (hi < n) {
+                uint32_t x = a[lo], y = a[hi];
+                if (x > y) { a[lo] = y; a[hi] = x; }
+            }
+        }
+        __syncthreads();
+        for (uint32_t j = k >> 2; j >= 1; j >>= 1) {
+            for (uint32_t i = threadIdx.x; i < half; i += blockDim.x) {
+                uint32_t blk = i / j, off = i - blk * j;
+                uint32_t lo = blk * 2 * j + off, hi = lo + j;
+                if (hi < n) {
+                    uint32_t x = a[lo], y = a[hi];
+                    if (x > y) { a[lo] = y; a[hi] = x; }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__device__ __forceinline__ bool depth_compare(uint32_t f, float v, float r) {  // render_pass/mod.rs:434-452
+    switch (f) {
+        case 1: return false;
+        case 2: return v < r;
+        case 3: return v == r;
+        case 4: return v <= r;
+        case 5: return v > r;
+        case 6: return v != r;
+        case 7: return v >= r;
+        default: return true;
+    }
+}
+
+// Encodes a colour into the target format (texture.rs:373-411); c[] holds the texel bytes.
+__device__ __forceinline__ void encode_color(uint32_t fmt, V4 col, uint32_t c[4]) {
+    switch (fmt) {
+        case 1: c[0] = unorm8_trunc(col.x); break;
+        case 2: c[0] = unorm8_trunc(col.x) | (unorm8_trunc(col.y) << 8); break;
+        case 3: case 4:
+            c[0] = unorm8_trunc(col.x) | (unorm8_trunc(col.y) << 8) | (unorm8_trunc(col.z) << 16) |
+                   (unorm8_trunc(col.w) << 24);
+            break;
+        case 5: case 6:
+            c[0] = unorm8_trunc(col.z) | (unorm8_trunc(col.y) << 8) | (unorm8_trunc(col.x) << 16) |
+                   (unorm8_trunc(col.w) << 24);
+            break;
+        case 7:
+            c[0] = (uint32_t)f32_to_f16_bits(col.x) | ((uint32_t)f32_to_f16_bits(col.y) << 16);
+            c[1] = (uint32_t)f32_to_f16_bits(col.z) | ((uint32_t)f32_to_f16_bits(col.w) << 16);
+            break;
+        case 8:
+            c[0] = __float_as_uint(col.x); c[1] = __float_as_uint(col.y);
+            c[2] = __float_as_uint(col.z); c[3] = __float_as_uint(col.w);
+            break;
+        default: break;
+    }
+}
+__device__ __forceinline__ V4 decode_color(uint32_t fmt, const uint32_t c[4]) {
+    switch (fmt) {
+        case 3: case 4:
+            return {fdiv((float)(c[0] & 0xFF), 255.0f), fdiv((float)((c[0] >> 8) & 0xFF), 255.0f),
+                    fdiv((float)((c[0] >> 16) & 0xFF), 255.0f), fdiv((float)(c[0] >> 24), 255.0f)};
+        case 5: case 6:
+            return {fdiv((float)((c[0] >> 16) & 0xFF), 255.0f), fdiv((float)((c[0] >> 8) & 0xFF), 255.0f),
+                    fdiv((float)(c[0] & 0xFF), 255.0f), fdiv((float)(c[0] >> 24), 255.0f)};
+        case 7:
+            return {f16_bits_to_f32(c[0] & 0xFFFF), f16_bits_to_f32(c[0] >> 16), f16_bits_to_f32(c[1] & 0xFFFF),
+                    f16_bits_to_f32(c[1] >> 16)};
+        case 8: return {__uint_as_float(c[0]), __uint_as_float(c[1]), __uint_as_float(c[2]), __uint_as_float(c[3])};
+        default: return {0.0f, 0.0f, 0.0f, 0.0f};
+    }
+}
+
+__device__ __forceinline__ float blend_factor(uint32_t f, float s, float sa, float dd, float da, float k) {
+    switch (f) {
+        case 0: return 0.0f;
+        case 1: return 1.0f;
+        case 2: return s;
+        case 3: return fsub(1.0f, s);
+        case 4: return sa;
+        case 5: return fsub(1.0f, sa);
+        case 6: return dd;
+        case 7: return fsub(1.0f, dd);
+        case 8: return da;
+        case 9: return fsub(1.0f, da);
+        case 11: return k;
+        case 12: return fsub(1.0f, k);
+        default: return 0.0f;
+    }
+}
+__device__ __forceinline__ float blend_channel(const uint32_t bc[3], float s, float sa, float dd, float da, float k) {
+    if (bc[2] == 3) return fminf(s, dd);
+    if (bc[2] == 4) return fmaxf(s, dd);
+    float fs = blend_factor(bc[0], s, sa, dd, da, k);
+    float fd = blend_factor(bc[1], s, sa, dd, da, k);
+    float a = fmul(s, fs), b = fmul(dd, fd);
+    switch (bc[2]) {
+        case 1: return fsub(a, b);
+        case 2: return fsub(b, a);
+        default: return fadd(a, b);
+    }
+}
+
+struct PixelState {
+    uint32_t c[4];
+    float depth;
+};
+
+template <int T, int WARPS, int CAP, int RB>
+__global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
+    constexpr int NT = WARPS * 32;
+    constexpr int BLK_X = T / 8, BLK_Y = T / 4, NBLK = BLK_X * BLK_Y;
+    constexpr int PPT = (NBLK + WARPS - 1) / WARPS;  // 8x4 blocks per warp
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    uint32_t* s_keys = reinterpret_cast<uint32_t*>(smem_raw);                  // CAP keys
+    uint8_t* s_recs = smem_raw + CAP * sizeof(uint32_t);                       // RB records
+    __shared__ uint32_t s_tile;
+    __shared__ const uint8_t* s_rec_ptr[RB];
+    __shared__ unsigned long long s_frag;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const bool failed = bp.status->error != 0 || *bp.abort_flag != 0;
+    if (threadIdx.x == 0) s_frag = 0;
+    if (failed && blockIdx.x == 0 && threadIdx.x == 0) *bp.abort_flag = 1u;
+
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(bp.work_counter, 1u);
+        __syncthreads();
+        const uint32_t tile = s_tile;
+        if (tile >= bp.total_tiles || failed) break;
+        const uint32_t ti = find_target(bp.targets, bp.num_targets, tile);
+        const TargetDesc& tg = bp.targets[ti];
+        const uint32_t lt = tile - tg.tile_base;
+        const int tx = (int)(lt % tg.tiles_x), ty = (int)(lt / tg.tiles_x);
+        const uint32_t n = bp.tile_count[tile];
+        const uint32_t off = bp.tile_offset[tile];
+
+        // pixel state init: LoadOp::Clear from the clear value, else the target's texels
+        PixelState px[PPT];
+        int pxx[PPT], pxy[PPT];
+        bool pvalid[PPT];
+        uint32_t clear_c[4] = {0, 0, 0, 0};
+        if (tg.color) encode_color(tg.color_format, V4{tg.clear[0], tg.clear[1], tg.clear[2], tg.clear[3]}, clear_c);
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+            const int blk = warp + k * WARPS;
+            const int bx = blk % BLK_X, byy = blk / BLK_X;
+            pxx[k] = tx * T + bx * 8 + (lane & 7);
+            pxy[k] = ty * T + byy * 4 + (lane >> 3);
+            pvalid[k] = blk < NBLK && pxx[k] < (int)tg.width && pxy[k] < (int)tg.height;
+            const size_t pix = (size_t)pxy[k] * tg.width + pxx[k];
+            px[k].c[0] = clear_c[0]; px[k].c[1] = clear_c[1]; px[k].c[2] = clear_c[2]; px[k].c[3] = clear_c[3];
+            px[k].depth = tg.depth_clear;
+            if (pvalid[k]) {
+                if (tg.color && tg.color_load != 1) {
+                    const uint8_t* src = tg.color + tg.slice_offset + pix * tg.color_bpp;
+                    if (tg.color_bpp == 4) px[k].c[0] = *reinterpret_cast<const uint32_t*>(src);
+                    else if (tg.color_bpp == 8) { px[k].c[0] = reinterpret_cast<const uint32_t*>(src)[0]; px[k].c[1] = reinterpret_cast<const uint32_t*>(src)[1]; }
+                    else if (tg.color_bpp == 16) { for (int q = 0; q < 4; ++q) px[k].c[q] = reinterpret_cast<const uint32_t*>(src)[q]; }
+                    else if (tg.color_bpp == 2) px[k].c[0] = *reinterpret_cast<const uint16_t*>(src);
+                    else px[k].c[0] = *src;
+                }
+                if (tg.depth && tg.depth_load != 1) px[k].depth = tg.depth[pix];
+            }
+        }
+
+        // order the tile's keys
+        const uint32_t* keys;
+        if (n <= (uint32_t)CAP) {
+            for (uint32_t i = threadIdx.x; i < n; i += NT) s_keys[i] = bp.bins[off + i];
+            __syncthreads();
+            block_sort(s_keys, n);
+            keys = s_keys;
+        } else {
+            block_sort(bp.bins + off, n);
+            __threadfence_block();
+            keys = bp.bins + off;
+        }
+        __syncthreads();
+
+        uint32_t frag_count = 0;
+        for (uint32_t b0 = 0; b0 < n; b0 += RB) {
+            const uint32_t nb = min((uint32_t)RB, n - b0);
+            // resolve keys -> record addresses
+            if (threadIdx.x < nb) {
+                const uint32_t key = keys[b0 + threadIdx.x];
+                const uint32_t prim = key >> SUBTRI_BITS, sub = key & ((1u << SUBTRI_BITS) - 1u);
+                const TriRecord* pr = rec_at(bp.records, bp.record_stride, prim);
+                s_rec_ptr[threadIdx.x] = sub == 0 ? reinterpret_cast<const uint8_t*>(pr)
+                                                  : reinterpret_cast<const uint8_t*>(
+                                                        rec_at(bp.ovf_records, bp.record_stride, pr->ovf + sub - 1));
+            }
+            __syncthreads();
+            // stage records into shared memory (16-byte copies)
+            const uint32_t words = bp.record_stride >> 4;
+            for (uint32_t w = threadIdx.x; w < nb * words; w += NT) {
+                const uint32_t ri = w / words, wi = w - ri * words;
+                reinterpret_cast<uint4*>(s_recs + (size_t)ri * bp.record_stride)[wi] =
+                    __ldg(reinterpret_cast<const uint4*>(s_rec_ptr[ri]) + wi);
+            }
+            __syncthreads();
+            for (uint32_t ri = 0; ri < nb; ++ri) {
+                const TriRecord& r = *reinterpret_cast<const TriRecord*>(s_recs + (size_t)ri * bp.record_stride);
+                const DrawDesc& d = bp.draws[r.draw];
+                const float* rv = rec_var(&r);
+                const uint32_t nvar = d.num_varyings;
+#pragma unroll
+                for (int k = 0; k < PPT; ++k) {
+                    // warp-uniform reject of the whole 8x4 block
+                    const int blk = warp + k * WARPS;
+                    if (blk >= NBLK) continue;
+                    const int bx0 = tx * T + (blk % BLK_X) * 8, by0 = ty * T + (blk / BLK_X) * 4;
+                    if (by0 > r.row1 || by0 + 3 < r.row0 || bx0 > r.xmax || bx0 + 7 < r.xmin) continue;
+                    const int x = pxx[k], y = pxy[k];
+                    if (!pvalid[k] || y < r.row0 || y > r.row1) continue;
+                    int x1, x2;
+                    span_at(r, y, x1, x2);
+                    if (x < x1 || x > x2) continue;
+                    if ((uint32_t)x < d.sc_x0 || (uint32_t)x >= d.sc_x1 || (uint32_t)y < d.sc_y0 ||
+                        (uint32_t)y >= d.sc_y1)
+                        continue;
+                    // barycentrics at the integer pixel corner (raster.rs:313-321, 334-335)
+                    const float fx = (float)x, fy = (float)y;
+                    const float l0 = fdiv(shoelace(fx, fy, r.vpx[1], r.vpy[1], r.vpx[2], r.vpy[2]), r.area);
+                    const float l1 = fdiv(shoelace(r.vpx[0], r.vpy[0], fx, fy, r.vpx[2], r.vpy[2]), r.area);
+                    const float l2 = fdiv(shoelace(r.vpx[0], r.vpy[0], r.vpx[1], r.vpy[1], fx, fy), r.area);
+                    // composed with the clip barycentrics (raster.rs:338-343)
+                    float cmp[3];
+#pragma unroll
+                    for (int j = 0; j < 3; ++j)
+                        cmp[j] = fadd(fadd(fmul(r.cb[j], l0), fmul(r.cb[3 + j], l1)), fmul(r.cb[6 + j], l2));
+                    // fragment.z (raster.rs:345-346)
+                    const float z = fadd(fadd(fmul(r.fz[0], cmp[0]), fmul(r.fz[1], cmp[1])), fmul(r.fz[2], cmp[2]));
+                    ++frag_count;
+                    // inter-stage values (fragment.rs:319-378)
+                    float var[MAX_VARYING_FLOATS];
+                    const uint32_t im = program_interp(d.program);
+                    if (im == INTERP_PERSPECTIVE) {
+                        const float den = fadd(fadd(fmul(cmp[0], r.inv_w0[0]), fmul(cmp[1], r.inv_w0[1])),
+                                               fmul(cmp[2], r.inv_w0[2]));
+                        for (uint32_t q = 0; q < nvar; ++q) {
+                            float num = fmul(fmul(rv[q], cmp[0]), r.inv_w0[0]);
+                            num = fadd(num, fmul(fmul(rv[nvar + q], cmp[1]), r.inv_w0[1]));
+                            num = fadd(num, fmul(fmul(rv[2 * nvar + q], cmp[2]), r.inv_w0[2]));
+                            var[q] = fdiv(num, den);
+                        }
+                    } else {
+                        for (uint32_t q = 0; q < nvar; ++q)
+                            var[q] = fadd(fadd(fmul(rv[q], cmp[0]), fmul(rv[nvar + q], cmp[1])),
+                                          fmul(rv[2 * nvar + q], cmp[2]));
+                    }
+                    V4 col;
+                    if (!run_fs(d, var, col)) continue;  // discard: no depth test, no write
+                    // late depth test at the first colour output (fragment.rs:427-453, 470-479)
+                    if (d.depth_test) {
+                        if (!depth_compare(d.depth_compare, z, px[k].depth)) continue;
+                        if (d.depth_write) px[k].depth = z;
+                    }
+                    if (!tg.color) continue;
+                    if (d.blend_enabled) {
+                        const V4 dst = decode_color(tg.color_format, px[k].c);
+                        V4 o;
+                        o.x = blend_channel(d.blend_color, col.x, col.w, dst.x, dst.w, d.blend_constant[0]);
+                        o.y = blend_channel(d.blend_color, col.y, col.w, dst.y, dst.w, d.blend_constant[1]);
+                        o.z = blend_channel(d.blend_color, col.z, col.w, dst.z, dst.w, d.blend_constant[2]);
+                        o.w = blend_channel(d.blend_alpha, col.w, col.w, dst.w, dst.w, d.blend_constant[3]);
+                        col = o;
+                    }
+                    if (d.write_mask != 0xF) {
+                        const V4 dst = decode_color(tg.color_format, px[k].c);
+                        if (!(d.write_mask & 1)) col.x = dst.x;
+                        if (!(d.write_mask & 2)) col.y = dst.y;
+                        if (!(d.write_mask & 4)) col.z = dst.z;
+                        if (!(d.write_mask & 8)) col.w = dst.w;
+                    }
+                    encode_color(tg.color_format, col, px[k].c);
+                }
+            }
+            __syncthreads();
+        }
+
+        // write the tile back
+#pragma unroll
+        for (int k = 0; k < PPT; ++k) {
+            if (!pvalid[k]) continue;
+            const size_t pix = (size_t)pxy[k] * tg.width + pxx[k];
+            if (tg.color) {
+                uint8_t* dst = tg.color + tg.slice_offset + pix * tg.color_bpp;
+                if (tg.color_bpp == 4) *reinterpret_cast<uint32_t*>(dst) = px[k].c[0];
+                else if (tg.color_bpp == 8) { reinterpret_cast<uint2*>(dst)[0] = make_uint2(px[k].c[0], px[k].c[1]); }
+                else if (tg.color_bpp == 16) { reinterpret_cast<uint4*>(dst)[0] = make_uint4(px[k].c[0], px[k].c[1], px[k].c[2], px[k].c[3]); }
+                else if (tg.color_bpp == 2) *reinterpret_cast<uint16_t*>(dst) = (uint16_t)px[k].c[0];
+                else *dst = (uint8_t)px[k].c[0];
+            }
+            if (tg.depth) tg.depth[pix] = px[k].depth;
+        }
+        // fragment count
+        for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
+        if (lane == 0 && frag_count) atomicAdd(&s_frag, (unsigned long long)frag_count);
+        __syncthreads();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_frag) atomicAdd(&bp.status->fragments, s_frag);
+}
+
+}  // namespace gbr

@@ -1,0 +1,1348 @@
+// runtime.cu — the C ABI of include/gbr.h: objects, the queue worker, command-stream decoding,
+// batch planning and the launch of the render-pass kernels.
+//
+// Threading mirrors wgpu-cpu (device.rs:40-74, 436-549; engine.rs:11-47): any thread may call
+// the ABI; gbr_queue_submit decodes and validates on the caller's thread and enqueues; one worker
+// thread per device owns the CUDA stream and executes queue items in order (buffer/texture
+// writes, submissions, reads), so writes are ordered with submissions as wgpu's queue orders
+// them.  A submission's render passes become launch batches (one per draw in the per-draw
+// mode, one per pass otherwise); the worker waits for the submission's last kernel, checks
+// each batch's device status and re-runs from a batch that ran out of scratch space.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <future>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "gbr.h"
+#include "gbr_types.h"
+#include "kernels.h"
+
+namespace gbr {
+namespace {
+
+thread_local std::string g_last_error;
+
+struct Failure {
+    gbr_status status;
+    std::string msg;
+};
+[[noreturn]] void fail(gbr_status st, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    throw Failure{st, buf};
+}
+void cuda_check(cudaError_t e, const char* what) {
+    if (e != cudaSuccess) fail(GBR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+using Clock = std::chrono::steady_clock;
+double ms_between(Clock::time_point a, Clock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+// ---------------------------------------------------------------- formats and programs
+uint32_t bytes_per_texel(uint32_t f) {
+    switch (f) {
+        case GBR_TEXTURE_FORMAT_R8_UNORM: return 1;
+        case GBR_TEXTURE_FORMAT_RG8_UNORM: return 2;
+        case GBR_TEXTURE_FORMAT_RGBA8_UNORM:
+        case GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB:
+        case GBR_TEXTURE_FORMAT_BGRA8_UNORM:
+        case GBR_TEXTURE_FORMAT_BGRA8_UNORM_SRGB:
+        case GBR_TEXTURE_FORMAT_DEPTH32_FLOAT: return 4;
+        case GBR_TEXTURE_FORMAT_RGBA16_FLOAT: return 8;
+        case GBR_TEXTURE_FORMAT_RGBA32_FLOAT: return 16;
+        default: return 0;
+    }
+}
+uint32_t vertex_format_bytes(uint32_t f) {
+    switch (f) {
+        case GBR_VERTEX_FORMAT_FLOAT32:
+        case GBR_VERTEX_FORMAT_UINT32:
+        case GBR_VERTEX_FORMAT_SINT32:
+        case GBR_VERTEX_FORMAT_FLOAT16X2:
+        case GBR_VERTEX_FORMAT_UNORM8X4: return 4;
+        case GBR_VERTEX_FORMAT_FLOAT32X2:
+        case GBR_VERTEX_FORMAT_FLOAT16X4: return 8;
+        case GBR_VERTEX_FORMAT_FLOAT32X3: return 12;
+        case GBR_VERTEX_FORMAT_FLOAT32X4: return 16;
+        default: return 0;
+    }
+}
+
+// Interface of the native programs (their code is in programs.cuh).
+struct ProgramInfo {
+    const char* name;
+    uint32_t id;
+    int num_inputs;
+    int input_loc[3], input_comps[3];
+    uint32_t num_varyings;
+    bool perspective;
+    uint32_t uniform_min;  // bytes required at @group(0) @binding(0), 0 = none
+    bool uses_texture;     // @group(1) @binding(0) texture_2d + @binding(1) sampler
+};
+const ProgramInfo kPrograms[] = {
+    {"colored_triangle", PROG_COLORED_TRIANGLE, 0, {0, 0, 0}, {0, 0, 0}, 4, false, 0, false},
+    {"mesh_color", PROG_MESH_COLOR, 2, {0, 1, 0}, {3, 3, 0}, 3, false, 64, false},
+    {"mesh_color_perspective", PROG_MESH_COLOR_PERSPECTIVE, 2, {0, 1, 0}, {3, 3, 0}, 3, true, 64, false},
+    {"mesh_color_discard", PROG_MESH_COLOR_DISCARD, 2, {0, 1, 0}, {3, 3, 0}, 3, false, 64, false},
+    {"mesh_tex_lambert", PROG_MESH_TEX_LAMBERT, 3, {0, 1, 2}, {3, 3, 2}, 5, false, 80, true},
+    {"quad_color", PROG_QUAD_COLOR, 2, {0, 1, 0}, {3, 4, 0}, 4, false, 0, false},
+    {"clip_passthrough", PROG_CLIP_PASSTHROUGH, 2, {0, 1, 0}, {4, 4, 0}, 4, false, 0, false},
+};
+const ProgramInfo* find_program(const char* name) {
+    for (const auto& p : kPrograms)
+        if (std::strcmp(p.name, name) == 0) return &p;
+    return nullptr;
+}
+
+// ---------------------------------------------------------------- objects
+struct Object {
+    virtual ~Object() {}
+};
+struct Buffer : Object {
+    uint8_t* ptr = nullptr;
+    uint64_t size = 0;
+    ~Buffer() override {
+        if (ptr) cudaFree(ptr);
+    }
+};
+struct Texture : Object {
+    gbr_texture_desc desc{};
+    uint32_t bpp = 0;
+    uint32_t mips_stored = 1;
+    uint64_t mip_offset[16] = {};
+    uint64_t bytes = 0;
+    uint8_t* ptr = nullptr;
+    uint32_t layers() const { return desc.size.depth_or_array_layers ? desc.size.depth_or_array_layers : 1; }
+    uint32_t mip_w(uint32_t m) const { return std::max(1u, desc.size.width >> m); }
+    uint32_t mip_h(uint32_t m) const { return std::max(1u, desc.size.height >> m); }
+    uint64_t mip_bytes(uint32_t m) const { return (uint64_t)mip_w(m) * mip_h(m) * layers() * bpp; }
+    ~Texture() override {
+        if (ptr) cudaFree(ptr);
+    }
+};
+struct Sampler : Object {
+    gbr_sampler_desc desc{};
+};
+struct ShaderModule : Object {
+    const ProgramInfo* prog = nullptr;
+};
+struct Pipeline : Object {
+    gbr_render_pipeline_desc desc{};
+    const ProgramInfo* prog = nullptr;
+    AttrDesc attr[16];
+};
+struct BindGroup : Object {
+    gbr_bind_group_desc desc{};
+    std::vector<std::shared_ptr<Object>> refs;  // the resources, kept alive with the group
+};
+
+// ---------------------------------------------------------------- decoded commands
+struct Slice {
+    std::shared_ptr<Buffer> buf;
+    uint64_t offset = 0, size = 0;
+};
+struct DrawCmd {
+    bool indexed = false;
+    uint32_t start = 0, end = 0;
+    int32_t base_vertex = 0;
+    uint32_t inst_start = 0, inst_end = 1;
+    std::shared_ptr<Pipeline> pipeline;  // state snapshot at the draw (state.rs:57-74)
+    Slice index;
+    uint32_t index_format = 0;
+    Slice vb[GBR_MAX_VERTEX_BUFFERS];
+    std::shared_ptr<BindGroup> groups[GBR_MAX_BIND_GROUPS];
+    float viewport[6] = {};
+    uint32_t scissor[4] = {};
+    double blend_constant[4] = {};
+};
+struct PassCmd {
+    gbr_cmd_begin_render_pass begin{};
+    std::shared_ptr<Texture> color;
+    std::shared_ptr<Texture> depth;
+    uint32_t width = 0, height = 0;
+    std::vector<DrawCmd> draws;
+};
+
+// ---------------------------------------------------------------- queue items
+struct Item {
+    enum Kind { SUBMIT, WRITE_BUFFER, WRITE_TEXTURE, READ_BUFFER, READ_TEXTURE, FLUSH } kind = SUBMIT;
+    uint64_t index = 0;
+    std::vector<PassCmd> passes;
+    std::shared_ptr<Buffer> buffer;
+    std::shared_ptr<Texture> texture;
+    uint32_t mip = 0;
+    uint64_t offset = 0;
+    std::vector<uint8_t> data;
+    gbr_texel_copy_buffer_layout layout{};
+    void* dst = nullptr;
+    uint64_t size = 0;
+    std::promise<Failure>* done = nullptr;  // reads: completion for the blocked caller
+    Clock::time_point t_submit;
+};
+
+struct SubmissionRecord {
+    gbr_submission_stats stats{};
+    gbr_status status = GBR_OK;
+    std::string error;
+    cudaEvent_t ev_start = nullptr, ev_end = nullptr;
+};
+
+// ---------------------------------------------------------------- scratch (grow-only)
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t size = 0;
+    void ensure(size_t need, uint64_t* total) {
+        if (need <= size) return;
+        size_t n = std::max(need, size + size / 2);
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        *total -= size;
+        size = 0;
+        cuda_check(cudaMalloc(&ptr, n), "cudaMalloc(scratch)");
+        size = n;
+        *total += n;
+    }
+    void release() {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        size = 0;
+    }
+};
+
+struct Device {
+    gbr_device_config cfg{};
+    int ordinal = 0;
+    int num_sms = 0;
+    int tile = 16, warps = 8;
+    cudaStream_t stream = nullptr;
+
+    std::mutex obj_mu;
+    uint64_t next_handle = 1;
+    std::unordered_map<uint64_t, std::shared_ptr<Object>> objects;
+
+    std::mutex q_mu;
+    std::condition_variable q_cv, done_cv;
+    std::deque<Item> queue;
+    bool stopping = false;
+    uint64_t next_submission = 0;
+    uint64_t completed_submissions = 0;  // submissions with index < this are done
+    std::map<uint64_t, SubmissionRecord> records;
+    bool lost = false;
+    std::string lost_msg;
+    std::thread worker;
+
+    // worker-owned scratch
+    uint64_t scratch_bytes = 0;
+    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf;
+    uint32_t ovf_capacity = 4096;
+    uint64_t bin_capacity = 1u << 22;
+
+    template <class T>
+    std::shared_ptr<T> get(uint64_t h, const char* what) {
+        std::lock_guard<std::mutex> lk(obj_mu);
+        auto it = objects.find(h);
+        if (it == objects.end()) fail(GBR_ERR_INVALID_ARGUMENT, "invalid %s handle %llu", what, (unsigned long long)h);
+        auto p = std::dynamic_pointer_cast<T>(it->second);
+        if (!p) fail(GBR_ERR_INVALID_ARGUMENT, "handle %llu is not a %s", (unsigned long long)h, what);
+        return p;
+    }
+    uint64_t add(std::shared_ptr<Object> o) {
+        std::lock_guard<std::mutex> lk(obj_mu);
+        uint64_t h = next_handle++;
+        objects[h] = std::move(o);
+        return h;
+    }
+    void remove(uint64_t h) {
+        std::lock_guard<std::mutex> lk(obj_mu);
+        objects.erase(h);
+    }
+    void enqueue(Item&& it) {
+        std::lock_guard<std::mutex> lk(q_mu);
+        if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
+        queue.push_back(std::move(it));
+        q_cv.notify_all();
+    }
+    void worker_main();
+    void execute(Item& it);
+    void execute_submission(Item& it, SubmissionRecord& rec);
+};
+
+std::mutex g_dev_mu;
+std::unordered_map<uint64_t, std::shared_ptr<Device>> g_devices;
+uint64_t g_next_device = 1;
+
+std::shared_ptr<Device> get_device(gbr_device d) {
+    std::lock_guard<std::mutex> lk(g_dev_mu);
+    auto it = g_devices.find(d);
+    if (it == g_devices.end()) fail(GBR_ERR_INVALID_ARGUMENT, "invalid device handle");
+    return it->second;
+}
+
+// ---------------------------------------------------------------- batch planning
+struct Batch {
+    std::vector<DrawDesc> draws;
+    std::vector<TargetDesc> targets;
+    uint32_t total_prims = 0, total_tiles = 0, nvar = 0;
+};
+
+uint32_t ilog2(uint32_t v) {
+    uint32_t r = 0;
+    while ((1u << r) < v) ++r;
+    return r;
+}
+
+TargetDesc make_target(const PassCmd& p, bool first_in_pass, uint32_t tile, uint32_t profile) {
+    TargetDesc t{};
+    t.width = p.width;
+    t.height = p.height;
+    if (p.color) {
+        const gbr_color_attachment& ca = p.begin.color_attachments[0];
+        t.color = p.color->ptr;
+        t.color_format = p.color->desc.format;
+        t.color_bpp = p.color->bpp;
+        t.slice_offset = (uint32_t)((uint64_t)ca.depth_slice * p.width * p.height * p.color->bpp);
+        t.color_load = first_in_pass && ca.load_op == GBR_LOAD_OP_CLEAR ? 1u : 0u;
+        for (int k = 0; k < 4; ++k) t.clear[k] = (float)ca.clear_value[k];  // wgpu_color_to_vec4
+        uint32_t f = t.color_format;
+        if (profile == GBR_PROFILE_PARITY && (f == GBR_TEXTURE_FORMAT_RGBA16_FLOAT || f == GBR_TEXTURE_FORMAT_RGBA32_FLOAT))
+            fail(GBR_ERR_UNSUPPORTED, "Unsupported texture format for colour writes (texture.rs:407)");
+    }
+    if (p.depth) {
+        const gbr_depth_attachment& da = p.begin.depth_attachment;
+        t.depth = reinterpret_cast<float*>(p.depth->ptr);
+        t.depth_load = !da.has_depth_ops ? 2u : (first_in_pass && da.depth_load_op == GBR_LOAD_OP_CLEAR ? 1u : 0u);
+        t.depth_clear = da.depth_clear_value;
+    }
+    t.tiles_x = (p.width + tile - 1) / tile;
+    t.tiles_y = (p.height + tile - 1) / tile;
+    return t;
+}
+
+DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachment) {
+    DrawDesc d{};
+    const Pipeline& pl = *dc.pipeline;
+    const gbr_render_pipeline_desc& pd = pl.desc;
+    const ProgramInfo& prog = *pl.prog;
+    const gbr_primitive_state& ps = pd.primitive;
+    if (ps.polygon_mode != GBR_POLYGON_FILL) fail(GBR_ERR_UNSUPPORTED, "Unsupported polygon mode (state.rs:475-477)");
+    if (ps.topology != GBR_TOPOLOGY_TRIANGLE_LIST && ps.topology != GBR_TOPOLOGY_TRIANGLE_STRIP)
+        fail(GBR_ERR_UNSUPPORTED, "point and line topologies run on the oracle path only");
+    if (dc.indexed && ps.strip_index_format != GBR_INDEX_NONE) {
+        if (ps.topology != GBR_TOPOLOGY_TRIANGLE_STRIP) fail(GBR_ERR_VALIDATION, "List can't be separated");
+        fail(GBR_ERR_UNSUPPORTED, "primitive restart is not implemented on the GPU path");
+    }
+    if (prog.perspective && profile != GBR_PROFILE_EXTENSION)
+        fail(GBR_ERR_UNSUPPORTED, "perspective interpolation is todo!() in the reference (fragment.rs:343-345)");
+    d.topology = ps.topology;
+    d.index_format = dc.indexed ? dc.index_format : 0;
+    d.first = dc.start;
+    d.count = dc.end > dc.start ? dc.end - dc.start : 0;
+    d.base_vertex = dc.base_vertex;
+    d.instance_start = dc.inst_start;
+    d.instance_count = dc.inst_end > dc.inst_start ? dc.inst_end - dc.inst_start : 0;
+    d.prims_per_instance = ps.topology == GBR_TOPOLOGY_TRIANGLE_LIST ? d.count / 3 : (d.count >= 3 ? d.count - 2 : 0);
+    if (dc.indexed) {
+        if (!dc.index.buf) fail(GBR_ERR_VALIDATION, "No index buffer bound");
+        d.index_data = dc.index.buf->ptr + dc.index.offset;
+        d.index_bytes = dc.index.size;
+        uint32_t isz = dc.index_format == GBR_INDEX_UINT16 ? 2 : 4;
+        if (dc.index.offset % isz) fail(GBR_ERR_VALIDATION, "index buffer offset is not aligned");
+    }
+    for (uint32_t b = 0; b < pd.vertex_buffer_count; ++b) {
+        const gbr_vertex_buffer_layout& L = pd.vertex_buffers[b];
+        const Slice& s = dc.vb[b];
+        if (!s.buf) fail(GBR_ERR_VALIDATION, "Buffer %u not bound (vertex.rs:268-272)", b);
+        d.vb_data[b] = s.buf->ptr + s.offset;
+        d.vb_size[b] = s.size;
+        d.vb_stride_vertex[b] = L.step_mode == GBR_STEP_VERTEX ? (uint32_t)L.array_stride : 0;
+        d.vb_stride_instance[b] = L.step_mode == GBR_STEP_INSTANCE ? (uint32_t)L.array_stride : 0;
+    }
+    for (int l = 0; l < 16; ++l) d.attr[l] = pl.attr[l];
+    for (int g = 0; g < GBR_MAX_BIND_GROUPS; ++g) {
+        const BindGroup* bg = dc.groups[g].get();
+        if (!bg) continue;
+        for (uint32_t e = 0; e < bg->desc.entry_count; ++e) {
+            const gbr_bind_group_entry& en = bg->desc.entries[e];
+            if (en.binding >= 8) continue;
+            auto* obj = bg->refs[e].get();
+            if (en.kind == GBR_BINDING_BUFFER) {
+                auto* b = static_cast<Buffer*>(obj);
+                uint64_t size = en.size ? en.size : b->size - en.offset;
+                d.uniform[g][en.binding] = b->ptr + en.offset;
+                d.uniform_size[g][en.binding] = size;
+            } else if (en.kind == GBR_BINDING_TEXTURE_VIEW && g == 1 && en.binding == 0) {
+                auto* t = static_cast<Texture*>(obj);
+                d.tex.data = t->ptr;
+                d.tex.width = t->desc.size.width;
+                d.tex.height = t->desc.size.height;
+                d.tex.format = t->desc.format;
+                d.tex.mip_count = t->mips_stored;
+                for (uint32_t m = 0; m < t->mips_stored && m < 16; ++m) d.tex.mip_offset[m] = t->mip_offset[m];
+            } else if (en.kind == GBR_BINDING_SAMPLER && g == 1 && en.binding == 1) {
+                auto* s = static_cast<Sampler*>(obj);
+                d.samp.address_u = s->desc.address_mode_u;
+                d.samp.address_v = s->desc.address_mode_v;
+                d.samp.mag_filter = s->desc.mag_filter;
+                d.samp.min_filter = s->desc.min_filter;
+                d.samp.mip_filter = s->desc.mipmap_filter;
+                d.samp.lod_min = s->desc.lod_min_clamp;
+                d.samp.lod_max = s->desc.lod_max_clamp;
+            }
+        }
+    }
+    if (prog.uniform_min && (!d.uniform[0][0] || d.uniform_size[0][0] < prog.uniform_min))
+        fail(GBR_ERR_VALIDATION, "No such binding resource: uniform @group(0) @binding(0)");
+    if (prog.uses_texture) {
+        if (!d.tex.data) fail(GBR_ERR_VALIDATION, "No such binding resource: texture @group(1) @binding(0)");
+        if (d.tex.format != GBR_TEXTURE_FORMAT_RGBA8_UNORM && d.tex.format != GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB)
+            fail(GBR_ERR_UNSUPPORTED, "sampling this texture format is todo!() (texture.rs:186)");
+        if (d.samp.address_u == GBR_ADDRESS_CLAMP_TO_BORDER || d.samp.address_v == GBR_ADDRESS_CLAMP_TO_BORDER)
+            fail(GBR_ERR_UNSUPPORTED, "ClampToBorder is todo!() (binding.rs:160)");
+        bool have_sampler = false;
+        for (int gi = 1; gi < 2; ++gi)
+            if (dc.groups[gi])
+                for (uint32_t e = 0; e < dc.groups[gi]->desc.entry_count; ++e)
+                    if (dc.groups[gi]->desc.entries[e].kind == GBR_BINDING_SAMPLER &&
+                        dc.groups[gi]->desc.entries[e].binding == 1)
+                        have_sampler = true;
+        if (!have_sampler) fail(GBR_ERR_VALIDATION, "No such binding resource: sampler @group(1) @binding(1)");
+    }
+    d.program = prog.id;
+    d.has_fragment = pd.has_fragment;
+    d.num_varyings = prog.num_varyings;
+    d.profile = profile;
+    d.cull_mode = ps.cull_mode;
+    d.front_face = ps.front_face;
+    // ToRaster::new (raster.rs:130-143): translation = offset + 0.5 size, scaling = 0.5 size, y *= -1
+    volatile float vx = dc.viewport[0], vy = dc.viewport[1], vw = dc.viewport[2], vh = dc.viewport[3];
+    d.vp_tx = vx + 0.5f * vw;
+    d.vp_ty = vy + 0.5f * vh;
+    d.vp_sx = 0.5f * vw;
+    d.vp_sy = (0.5f * vh) * -1.0f;
+    d.sc_x0 = dc.scissor[0];
+    d.sc_y0 = dc.scissor[1];
+    d.sc_x1 = dc.scissor[0] + dc.scissor[2];
+    d.sc_y1 = dc.scissor[1] + dc.scissor[3];
+    d.depth_test = (pd.has_depth_stencil && has_depth_attachment) ? 1u : 0u;
+    d.depth_compare = pd.depth_stencil.depth_compare;
+    d.depth_write = pd.depth_stencil.depth_write_enabled;
+    d.write_mask = 0xF;
+    if (profile == GBR_PROFILE_EXTENSION && pd.has_fragment && pd.color_target_count > 0) {
+        const gbr_color_target_state& ct = pd.color_targets[0];
+        d.blend_enabled = ct.has_blend;
+        d.blend_color[0] = ct.color.src_factor;
+        d.blend_color[1] = ct.color.dst_factor;
+        d.blend_color[2] = ct.color.operation;
+        d.blend_alpha[0] = ct.alpha.src_factor;
+        d.blend_alpha[1] = ct.alpha.dst_factor;
+        d.blend_alpha[2] = ct.alpha.operation;
+        d.write_mask = ct.write_mask & 0xF;
+    }
+    for (int k = 0; k < 4; ++k) d.blend_constant[k] = (float)dc.blend_constant[k];
+    return d;
+}
+
+// ---------------------------------------------------------------- worker
+void Device::worker_main() {
+    cudaSetDevice(ordinal);
+    for (;;) {
+        Item it;
+        {
+            std::unique_lock<std::mutex> lk(q_mu);
+            q_cv.wait(lk, [&] { return stopping || !queue.empty(); });
+            if (queue.empty() && stopping) return;
+            it = std::move(queue.front());
+            queue.pop_front();
+        }
+        execute(it);
+    }
+}
+
+void Device::execute(Item& it) {
+    Failure err{GBR_OK, ""};
+    SubmissionRecord rec;
+    bool is_submit = it.kind == Item::SUBMIT;
+    try {
+        if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
+        switch (it.kind) {
+            case Item::WRITE_BUFFER:
+                cuda_check(cudaMemcpyAsync(it.buffer->ptr + it.offset, it.data.data(), it.data.size(),
+                                           cudaMemcpyHostToDevice, stream),
+                           "write_buffer");
+                break;
+            case Item::WRITE_TEXTURE: {
+                Texture& t = *it.texture;
+                uint32_t w = t.mip_w(it.mip), h = t.mip_h(it.mip), layers = t.layers();
+                uint64_t row = (uint64_t)w * t.bpp;
+                uint64_t src_row = it.layout.bytes_per_row ? it.layout.bytes_per_row : it.data.size();
+                uint64_t rows_per_image = it.layout.rows_per_image ? it.layout.rows_per_image : h;
+                uint8_t* dst = t.ptr + t.mip_offset[it.mip];
+                for (uint32_t z = 0; z < layers; ++z)
+                    cuda_check(cudaMemcpy2DAsync(dst + (uint64_t)z * h * row, row,
+                                                 it.data.data() + it.layout.offset + z * rows_per_image * src_row,
+                                                 src_row, row, h, cudaMemcpyHostToDevice, stream),
+                               "write_texture");
+                break;
+            }
+            case Item::READ_BUFFER:
+                cuda_check(cudaMemcpyAsync(it.dst, it.buffer->ptr + it.offset, it.size, cudaMemcpyDeviceToHost, stream),
+                           "buffer_read");
+                cuda_check(cudaStreamSynchronize(stream), "buffer_read sync");
+                break;
+            case Item::READ_TEXTURE:
+                cuda_check(cudaMemcpyAsync(it.dst, it.texture->ptr + it.texture->mip_offset[it.mip],
+                                           it.texture->mip_bytes(it.mip), cudaMemcpyDeviceToHost, stream),
+                           "texture_read");
+                cuda_check(cudaStreamSynchronize(stream), "texture_read sync");
+                break;
+            case Item::FLUSH:
+                flush_buf.ensure(256ull << 20, &scratch_bytes);
+                cuda_check(cudaMemsetAsync(flush_buf.ptr, (int)(it.offset & 0xFF), flush_buf.size, stream), "flush");
+                break;
+            case Item::SUBMIT: execute_submission(it, rec); break;
+        }
+    } catch (const Failure& f) {
+        err = f;
+        cudaError_t ce = cudaGetLastError();
+        if (f.status == GBR_ERR_CUDA || ce != cudaSuccess) {
+            std::lock_guard<std::mutex> lk(q_mu);
+            lost = true;
+            lost_msg = f.msg;
+        }
+    }
+    if (it.done) it.done->set_value(err);
+    if (is_submit) {
+        std::lock_guard<std::mutex> lk(q_mu);
+        rec.stats.submission_index = it.index;
+        rec.stats.submit_to_fence_ms = ms_between(it.t_submit, Clock::now());
+        if (err.status != GBR_OK) {
+            rec.status = err.status;
+            rec.error = err.msg;
+        }
+        auto& slot = records[it.index];
+        if (slot.ev_start) cudaEventDestroy(slot.ev_start);
+        if (slot.ev_end) cudaEventDestroy(slot.ev_end);
+        slot = rec;
+        completed_submissions = it.index + 1;
+        // keep the last 4096 records
+        while (records.size() > 4096) {
+            auto f = records.begin();
+            if (f->second.ev_start) cudaEventDestroy(f->second.ev_start);
+            if (f->second.ev_end) cudaEventDestroy(f->second.ev_end);
+            records.erase(f);
+        }
+        done_cv.notify_all();
+    }
+}
+
+void Device::execute_submission(Item& it, SubmissionRecord& rec) {
+    const auto t_start = Clock::now();
+    rec.stats.queue_wait_ms = ms_between(it.t_submit, t_start);
+    const uint32_t profile = cfg.profile;
+    const bool per_draw = cfg.launch_mode == GBR_LAUNCH_PER_DRAW;  // the plain one-launch-per-draw path
+    // plan batches
+    std::vector<Batch> batches;
+    uint64_t draws = 0, prims_in = 0;
+    for (const PassCmd& p : it.passes) {
+        if (p.width == 0 || p.height == 0) continue;
+        if (p.draws.empty() || !per_draw) {
+            Batch b;
+            b.targets.push_back(make_target(p, true, tile, profile));
+            for (const DrawCmd& dc : p.draws) {
+                ++draws;
+                DrawDesc d = make_draw(dc, profile, (bool)p.depth);
+                d.prim_base = b.total_prims;
+                d.target = 0;
+                uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
+                prims_in += np;
+                if ((uint64_t)b.total_prims + np >= (1ull << (32 - SUBTRI_BITS)))
+                    fail(GBR_ERR_UNSUPPORTED, "too many primitives in one pass");
+                b.total_prims += (uint32_t)np;
+                b.nvar = std::max(b.nvar, d.num_varyings);
+                if (np) b.draws.push_back(d);
+            }
+            batches.push_back(std::move(b));
+        } else {
+            bool first = true;
+            for (const DrawCmd& dc : p.draws) {
+                ++draws;
+                Batch b;
+                b.targets.push_back(make_target(p, first, tile, profile));
+                first = false;
+                DrawDesc d = make_draw(dc, profile, (bool)p.depth);
+                d.prim_base = 0;
+                d.target = 0;
+                uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
+                prims_in += np;
+                if (np >= (1ull << (32 - SUBTRI_BITS))) fail(GBR_ERR_UNSUPPORTED, "too many primitives in one draw");
+                b.total_prims = (uint32_t)np;
+                b.nvar = d.num_varyings;
+                if (np) b.draws.push_back(d);
+                batches.push_back(std::move(b));
+            }
+        }
+    }
+    for (Batch& b : batches) {
+        uint32_t base = 0;
+        for (TargetDesc& t : b.targets) {
+            t.tile_base = base;
+            base += t.tiles_x * t.tiles_y;
+        }
+        b.total_tiles = base;
+    }
+    rec.stats.draws = draws;
+    rec.stats.primitives_in = prims_in;
+    rec.stats.batched_with = 1;
+    if (batches.empty()) return;
+
+    // metadata layout: [abort flag][statuses][work counters][draw/target descriptors per batch]
+    const size_t nb = batches.size();
+    auto align = [](size_t v) { return (v + 255) & ~size_t(255); };
+    size_t off_status = 256, off_work = align(off_status + nb * sizeof(BatchStatus));
+    size_t off_desc = align(off_work + nb * sizeof(uint32_t) * 4);
+    std::vector<size_t> desc_off(nb);
+    size_t cur = off_desc;
+    for (size_t i = 0; i < nb; ++i) {
+        desc_off[i] = cur;
+        cur = align(cur + batches[i].draws.size() * sizeof(DrawDesc) + batches[i].targets.size() * sizeof(TargetDesc));
+    }
+    std::vector<uint8_t> host_meta(cur, 0);
+    for (size_t i = 0; i < nb; ++i) {
+        uint8_t* p = host_meta.data() + desc_off[i];
+        std::memcpy(p, batches[i].draws.data(), batches[i].draws.size() * sizeof(DrawDesc));
+        std::memcpy(p + batches[i].draws.size() * sizeof(DrawDesc), batches[i].targets.data(),
+                    batches[i].targets.size() * sizeof(TargetDesc));
+    }
+    uint64_t budget = cfg.hbm_budget_bytes ? cfg.hbm_budget_bytes : (80ull << 30);
+    meta_buf.ensure(cur, &scratch_bytes);
+    cuda_check(cudaMemcpyAsync(meta_buf.ptr, host_meta.data(), cur, cudaMemcpyHostToDevice, stream), "upload descriptors");
+
+    cudaEvent_t ev0, ev1;
+    cuda_check(cudaEventCreate(&ev0), "event");
+    cuda_check(cudaEventCreate(&ev1), "event");
+    rec.ev_start = ev0;
+    rec.ev_end = ev1;
+    uint32_t launches = 0;
+    uint64_t fragments = 0;
+    size_t first_batch = 0;
+    std::vector<BatchStatus> st(nb);
+    std::vector<cudaEvent_t> rev;  // raster kernel events (time_kernels)
+    struct EventGuard {
+        std::vector<cudaEvent_t>* v;
+        ~EventGuard() {
+            for (cudaEvent_t e : *v) cudaEventDestroy(e);
+        }
+    } rev_guard{&rev};
+    if (cfg.time_kernels) {
+        rev.resize(2 * nb);
+        for (auto& e : rev) cuda_check(cudaEventCreate(&e), "event");
+    }
+    double raster_ms = 0.0;
+    for (int attempt = 0; attempt < 12; ++attempt) {
+        // scratch for the remaining batches
+        uint32_t max_prims = 0, max_tiles = 0, max_stride = 0;
+        for (size_t i = first_batch; i < nb; ++i) {
+            uint32_t stride = (uint32_t)((sizeof(TriRecord) + 3 * batches[i].nvar * sizeof(float) + 15) & ~size_t(15));
+            max_stride = std::max(max_stride, stride);
+            max_prims = std::max(max_prims, batches[i].total_prims);
+            max_tiles = std::max(max_tiles, batches[i].total_tiles);
+        }
+        records_buf.ensure((size_t)std::max(1u, max_prims) * max_stride, &scratch_bytes);
+        ovf_buf.ensure((size_t)ovf_capacity * max_stride, &scratch_bytes);
+        tiles_buf.ensure((size_t)(max_tiles + 1) * 3 * sizeof(uint32_t) + 64, &scratch_bytes);
+        bins_buf.ensure((size_t)bin_capacity * sizeof(uint32_t), &scratch_bytes);
+        if (scratch_bytes > budget) fail(GBR_ERR_OUT_OF_MEMORY, "transient memory exceeds the HBM budget");
+        uint8_t* meta = static_cast<uint8_t*>(meta_buf.ptr);
+        cuda_check(cudaMemsetAsync(meta, 0, 4, stream), "abort flag");
+        if (attempt == 0) cuda_check(cudaEventRecord(ev0, stream), "event");
+        for (size_t i = first_batch; i < nb; ++i) {
+            const Batch& b = batches[i];
+            BatchParams bp{};
+            bp.draws = reinterpret_cast<const DrawDesc*>(meta + desc_off[i]);
+            bp.targets = reinterpret_cast<const TargetDesc*>(meta + desc_off[i] + b.draws.size() * sizeof(DrawDesc));
+            bp.num_draws = (uint32_t)b.draws.size();
+            bp.num_targets = (uint32_t)b.targets.size();
+            bp.total_prims = b.total_prims;
+            bp.total_tiles = b.total_tiles;
+            bp.tile_size = tile;
+            bp.tile_shift = ilog2(tile);
+            bp.record_stride = (uint32_t)((sizeof(TriRecord) + 3 * b.nvar * sizeof(float) + 15) & ~size_t(15));
+            bp.num_varyings = b.nvar;
+            bp.records = static_cast<uint8_t*>(records_buf.ptr);
+            bp.ovf_records = static_cast<uint8_t*>(ovf_buf.ptr);
+            bp.ovf_capacity = ovf_capacity;
+            bp.bin_capacity = (uint32_t)std::min<uint64_t>(bin_capacity, 0xFFFFFFFFull);
+            uint32_t* tiles = static_cast<uint32_t*>(tiles_buf.ptr);
+            bp.tile_count = tiles;
+            bp.tile_offset = tiles + (max_tiles + 1);
+            bp.tile_cursor = tiles + 2 * (max_tiles + 1);
+            bp.bins = static_cast<uint32_t*>(bins_buf.ptr);
+            bp.work_counter = reinterpret_cast<uint32_t*>(meta + off_work) + i * 4;
+            bp.status = reinterpret_cast<BatchStatus*>(meta + off_status) + i;
+            bp.abort_flag = reinterpret_cast<uint32_t*>(meta);
+            cuda_check(launch_batch(bp, tile, warps, num_sms, stream, &launches, rev.empty() ? nullptr : &rev[2 * i]),
+                       "launch");
+        }
+        cuda_check(cudaEventRecord(ev1, stream), "event");
+        cuda_check(cudaMemcpyAsync(st.data(), meta + off_status, nb * sizeof(BatchStatus), cudaMemcpyDeviceToHost,
+                                   stream),
+                   "status readback");
+        cuda_check(cudaStreamSynchronize(stream), "submission");
+        // first failing batch
+        size_t bad = nb;
+        for (size_t i = first_batch; i < nb; ++i)
+            if (st[i].error) {
+                bad = i;
+                break;
+            }
+        for (size_t i = first_batch; i < (bad == nb ? nb : bad); ++i) {
+            fragments += st[i].fragments;
+            if (!rev.empty()) {
+                float ms = 0.0f;
+                if (cudaEventElapsedTime(&ms, rev[2 * i], rev[2 * i + 1]) == cudaSuccess) raster_ms += ms;
+            }
+        }
+        if (bad == nb) break;
+        const BatchStatus& s = st[bad];
+        if (s.error == ERR_OVERFLOW_RECORDS) {
+            ovf_capacity = std::max<uint32_t>(ovf_capacity * 2, s.ovf_used + 1024);
+        } else if (s.error == ERR_OVERFLOW_BINS) {
+            bin_capacity = std::max<uint64_t>(bin_capacity * 2, s.bin_entries + (s.bin_entries >> 2));
+        } else {
+            static const char* names[] = {"none", "clip position w=0 (primitive.rs:177 / raster.rs:146)",
+                                          "index out of range of the index buffer",
+                                          "vertex attribute read out of range of the vertex buffer",
+                                          "index + base_vertex overflows u32 (index.rs:55-57)", "", "",
+                                          "scanline coordinate does not fit u32 (scanline.rs:156-170)",
+                                          "unsupported"};
+            fail(GBR_ERR_VALIDATION, "%s (primitive %u)", s.error < 9 ? names[s.error] : "device error",
+                 s.error_detail);
+        }
+        first_batch = bad;
+        if (attempt == 11) fail(GBR_ERR_OUT_OF_MEMORY, "scratch growth did not converge");
+    }
+    float gms = 0.0f;
+    cudaEventElapsedTime(&gms, ev0, ev1);
+    rec.stats.gpu_ms = gms;
+    rec.stats.fragments_shaded = fragments;
+    rec.stats.kernel_launches = launches;
+    rec.stats.raster_ms = raster_ms;
+}
+
+// ---------------------------------------------------------------- command decoding
+template <class T>
+const T* payload(const gbr_cmd_header& h, const uint8_t* body) {
+    if (h.payload_bytes < sizeof(T)) fail(GBR_ERR_INVALID_ARGUMENT, "command %u payload too short", h.opcode);
+    return reinterpret_cast<const T*>(body);
+}
+
+std::vector<PassCmd> decode(Device& dev, const uint8_t* data, uint64_t len) {
+    std::vector<PassCmd> passes;
+    uint64_t off = 0;
+    PassCmd* cur = nullptr;
+    DrawCmd st;  // current render-pass state (state.rs:57-74)
+    while (off < len) {
+        if (len - off < sizeof(gbr_cmd_header)) fail(GBR_ERR_INVALID_ARGUMENT, "truncated command header");
+        gbr_cmd_header h;
+        std::memcpy(&h, data + off, sizeof h);
+        off += sizeof h;
+        uint64_t padded = (h.payload_bytes + 7ull) & ~7ull;
+        if (len - off < padded) fail(GBR_ERR_INVALID_ARGUMENT, "truncated command payload");
+        std::vector<uint8_t> tmp(data + off, data + off + h.payload_bytes);
+        const uint8_t* b = tmp.data();
+        off += padded;
+        if (h.opcode == GBR_OP_BEGIN_RENDER_PASS) {
+            if (cur) fail(GBR_ERR_INVALID_ARGUMENT, "nested render pass");
+            passes.emplace_back();
+            cur = &passes.back();
+            std::memcpy(&cur->begin, payload<gbr_cmd_begin_render_pass>(h, b), sizeof cur->begin);
+            // State::new (state.rs:77-133): all attachments must have the same size
+            bool have = false;
+            auto size_of = [&](const Texture& t) {
+                if (!have) {
+                    cur->width = t.desc.size.width;
+                    cur->height = t.desc.size.height;
+                    have = true;
+                } else if (cur->width != t.desc.size.width || cur->height != t.desc.size.height) {
+                    fail(GBR_ERR_VALIDATION, "All render attachments must be the same size");
+                }
+            };
+            if (cur->begin.color_attachment_count > GBR_MAX_COLOR_TARGETS) fail(GBR_ERR_VALIDATION, "too many attachments");
+            for (uint32_t a = 0; a < cur->begin.color_attachment_count; ++a) {
+                uint64_t v = cur->begin.color_attachments[a].view;
+                if (!v) continue;
+                if (a > 0) fail(GBR_ERR_UNSUPPORTED, "more than one colour attachment");
+                cur->color = dev.get<Texture>(v, "texture");
+                size_of(*cur->color);
+                if (cur->begin.color_attachments[a].depth_slice >= cur->color->layers())
+                    fail(GBR_ERR_VALIDATION, "depth_slice out of range");
+            }
+            if (cur->begin.has_depth_attachment && cur->begin.depth_attachment.view) {
+                cur->depth = dev.get<Texture>(cur->begin.depth_attachment.view, "texture");
+                if (cur->depth->desc.format != GBR_TEXTURE_FORMAT_DEPTH32_FLOAT)
+                    fail(GBR_ERR_UNSUPPORTED, "depth attachment format");
+                size_of(*cur->depth);
+            }
+            st = DrawCmd();
+            st.viewport[2] = (float)cur->width;
+            st.viewport[3] = (float)cur->height;
+            st.viewport[5] = 1.0f;
+            st.scissor[2] = cur->width;
+            st.scissor[3] = cur->height;
+            continue;
+        }
+        if (h.opcode == GBR_OP_END_RENDER_PASS) {
+            if (!cur) fail(GBR_ERR_INVALID_ARGUMENT, "end without begin");
+            cur = nullptr;
+            continue;
+        }
+        if (!cur) fail(GBR_ERR_INVALID_ARGUMENT, "command %u outside a render pass", h.opcode);
+        switch (h.opcode) {
+            case GBR_OP_SET_PIPELINE:
+                st.pipeline = dev.get<Pipeline>(payload<gbr_cmd_set_pipeline>(h, b)->pipeline, "pipeline");
+                break;
+            case GBR_OP_SET_BIND_GROUP: {
+                auto* p = payload<gbr_cmd_set_bind_group>(h, b);
+                if (p->index >= GBR_MAX_BIND_GROUPS) fail(GBR_ERR_VALIDATION, "bind group index");
+                st.groups[p->index] = p->bind_group ? dev.get<BindGroup>(p->bind_group, "bind group") : nullptr;
+                break;
+            }
+            case GBR_OP_SET_INDEX_BUFFER: {
+                auto* p = payload<gbr_cmd_set_index_buffer>(h, b);
+                auto buf = dev.get<Buffer>(p->buffer, "buffer");
+                uint64_t size = p->size ? p->size : buf->size - std::min(p->offset, buf->size);
+                if (p->offset + size > buf->size) fail(GBR_ERR_VALIDATION, "index buffer slice out of range");
+                st.index = {buf, p->offset, size};
+                st.index_format = p->index_format;
+                break;
+            }
+            case GBR_OP_SET_VERTEX_BUFFER: {
+                auto* p = payload<gbr_cmd_set_vertex_buffer>(h, b);
+                if (p->slot >= GBR_MAX_VERTEX_BUFFERS) fail(GBR_ERR_VALIDATION, "vertex buffer slot");
+                if (p->offset % 4) fail(GBR_ERR_VALIDATION, "vertex buffer offset must be a multiple of 4");
+                auto buf = dev.get<Buffer>(p->buffer, "buffer");
+                uint64_t size = p->size ? p->size : buf->size - std::min(p->offset, buf->size);
+                if (p->offset + size > buf->size) fail(GBR_ERR_VALIDATION, "vertex buffer slice out of range");
+                st.vb[p->slot] = {buf, p->offset, size};
+                break;
+            }
+            case GBR_OP_SET_VIEWPORT: {
+                auto* p = payload<gbr_cmd_set_viewport>(h, b);
+                st.viewport[0] = p->x;
+                st.viewport[1] = p->y;
+                st.viewport[2] = p->width;
+                st.viewport[3] = p->height;
+                st.viewport[4] = p->min_depth;
+                st.viewport[5] = p->max_depth;
+                break;
+            }
+            case GBR_OP_SET_SCISSOR_RECT: {
+                auto* p = payload<gbr_cmd_set_scissor_rect>(h, b);
+                if ((uint64_t)p->x + p->width > cur->width || (uint64_t)p->y + p->height > cur->height)
+                    fail(GBR_ERR_VALIDATION, "scissor rect exceeds the render target");
+                st.scissor[0] = p->x;
+                st.scissor[1] = p->y;
+                st.scissor[2] = p->width;
+                st.scissor[3] = p->height;
+                break;
+            }
+            case GBR_OP_SET_BLEND_CONSTANT: {
+                auto* p = payload<gbr_cmd_set_blend_constant>(h, b);
+                for (int k = 0; k < 4; ++k) st.blend_constant[k] = p->color[k];
+                break;
+            }
+            case GBR_OP_SET_STENCIL_REFERENCE: break;
+            case GBR_OP_DRAW:
+            case GBR_OP_DRAW_INDEXED: {
+                if (!st.pipeline) fail(GBR_ERR_VALIDATION, "No pipeline bound");
+                DrawCmd dc = st;
+                if (h.opcode == GBR_OP_DRAW) {
+                    auto* p = payload<gbr_cmd_draw>(h, b);
+                    dc.indexed = false;
+                    dc.start = p->vertex_start;
+                    dc.end = p->vertex_end;
+                    dc.base_vertex = 0;
+                    dc.inst_start = p->instance_start;
+                    dc.inst_end = p->instance_end;
+                } else {
+                    auto* p = payload<gbr_cmd_draw_indexed>(h, b);
+                    if (!st.index.buf) fail(GBR_ERR_VALIDATION, "No index buffer bound");
+                    dc.indexed = true;
+                    dc.start = p->index_start;
+                    dc.end = p->index_end;
+                    dc.base_vertex = p->base_vertex;
+                    dc.inst_start = p->instance_start;
+                    dc.inst_end = p->instance_end;
+                }
+                cur->draws.push_back(dc);
+                break;
+            }
+            default: fail(GBR_ERR_INVALID_ARGUMENT, "unknown opcode %u", h.opcode);
+        }
+    }
+    if (cur) fail(GBR_ERR_INVALID_ARGUMENT, "render pass not ended");
+    return passes;
+}
+
+}  // namespace
+}  // namespace gbr
+
+using namespace gbr;
+
+#define GBR_TRY(...)                      \
+    try {                                 \
+        __VA_ARGS__;                      \
+        return GBR_OK;                    \
+    } catch (const Failure& f) {          \
+        g_last_error = f.msg;             \
+        return f.status;                  \
+    } catch (const std::exception& e) {   \
+        g_last_error = e.what();          \
+        return GBR_ERR_OUT_OF_MEMORY;     \
+    }
+
+extern "C" {
+
+GBR_API size_t gbr_last_error(char* buf, size_t len) {
+    if (buf && len) {
+        size_t n = std::min(len - 1, g_last_error.size());
+        std::memcpy(buf, g_last_error.data(), n);
+        buf[n] = 0;
+    }
+    return g_last_error.size();
+}
+GBR_API uint32_t gbr_abi_version(void) { return GBR_ABI_VERSION; }
+
+GBR_API gbr_status gbr_device_create(const gbr_device_config* cfg, gbr_device* out) {
+    GBR_TRY({
+        if (!cfg || !out) fail(GBR_ERR_INVALID_ARGUMENT, "null argument");
+        if (cfg->abi_version != GBR_ABI_VERSION) fail(GBR_ERR_INVALID_ARGUMENT, "ABI version mismatch");
+        auto d = std::make_shared<Device>();
+        d->cfg = *cfg;
+        d->ordinal = (int)cfg->device_ordinal;
+        int n = 0;
+        cuda_check(cudaGetDeviceCount(&n), "cudaGetDeviceCount");
+        if (d->ordinal >= n) fail(GBR_ERR_INVALID_ARGUMENT, "no CUDA device %d", d->ordinal);
+        cuda_check(cudaSetDevice(d->ordinal), "cudaSetDevice");
+        cuda_check(cudaDeviceGetAttribute(&d->num_sms, cudaDevAttrMultiProcessorCount, d->ordinal), "attribute");
+        d->tile = cfg->tile_size ? (int)cfg->tile_size : 16;
+        d->warps = cfg->warps_per_tile ? (int)cfg->warps_per_tile : (d->tile == 8 ? 2 : 8);
+        if (!raster_config_supported(d->tile, d->warps))
+            fail(GBR_ERR_INVALID_ARGUMENT, "unsupported tile size / warps per tile %d/%d", d->tile, d->warps);
+        if (cfg->bin_capacity) d->bin_capacity = cfg->bin_capacity;
+        cuda_check(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        Device* raw = d.get();
+        d->worker = std::thread([raw] { raw->worker_main(); });
+        std::lock_guard<std::mutex> lk(g_dev_mu);
+        uint64_t h = g_next_device++;
+        g_devices[h] = d;
+        *out = h;
+    })
+}
+
+GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
+    GBR_TRY({
+        std::shared_ptr<Device> d;
+        {
+            std::lock_guard<std::mutex> lk(g_dev_mu);
+            auto it = g_devices.find(dh);
+            if (it == g_devices.end()) fail(GBR_ERR_INVALID_ARGUMENT, "invalid device handle");
+            d = it->second;
+            g_devices.erase(it);
+        }
+        {
+            std::lock_guard<std::mutex> lk(d->q_mu);
+            d->stopping = true;
+            d->q_cv.notify_all();
+        }
+        if (d->worker.joinable()) d->worker.join();
+        cudaSetDevice(d->ordinal);
+        cudaStreamSynchronize(d->stream);
+        for (auto& r : d->records) {
+            if (r.second.ev_start) cudaEventDestroy(r.second.ev_start);
+            if (r.second.ev_end) cudaEventDestroy(r.second.ev_end);
+        }
+        d->objects.clear();
+        d->records_buf.release();
+        d->ovf_buf.release();
+        d->tiles_buf.release();
+        d->bins_buf.release();
+        d->meta_buf.release();
+        d->flush_buf.release();
+        cudaStreamDestroy(d->stream);
+    })
+}
+
+GBR_API gbr_status gbr_device_limits(gbr_device dh, gbr_limits* out) {
+    GBR_TRY({
+        get_device(dh);
+        out->max_texture_dimension_2d = 16384;
+        out->max_bind_groups = GBR_MAX_BIND_GROUPS;
+        out->max_vertex_buffers = GBR_MAX_VERTEX_BUFFERS;
+        out->max_vertex_attributes = GBR_MAX_VERTEX_ATTRIBUTES;
+        out->max_color_attachments = 1;
+        out->max_inter_stage_components = MAX_VARYING_FLOATS;
+        out->max_buffer_size = 1ull << 36;
+    })
+}
+
+GBR_API gbr_status gbr_buffer_create(gbr_device dh, uint64_t size, uint32_t usage, gbr_buffer* out) {
+    GBR_TRY({
+        (void)usage;
+        auto d = get_device(dh);
+        cuda_check(cudaSetDevice(d->ordinal), "cudaSetDevice");
+        auto b = std::make_shared<Buffer>();
+        b->size = size;
+        cuda_check(cudaMalloc(&b->ptr, std::max<uint64_t>(size, 16)), "cudaMalloc(buffer)");
+        cuda_check(cudaMemset(b->ptr, 0, std::max<uint64_t>(size, 16)), "cudaMemset(buffer)");
+        *out = d->add(b);
+    })
+}
+GBR_API gbr_status gbr_buffer_destroy(gbr_device dh, gbr_buffer b) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        d->get<Buffer>(b, "buffer");
+        d->remove(b);
+    })
+}
+GBR_API gbr_status gbr_queue_write_buffer(gbr_device dh, gbr_buffer b, uint64_t offset, const void* data, uint64_t size) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        Item it;
+        it.kind = Item::WRITE_BUFFER;
+        it.buffer = d->get<Buffer>(b, "buffer");
+        if (offset + size > it.buffer->size) fail(GBR_ERR_VALIDATION, "write_buffer out of range");
+        if (!size) return GBR_OK;
+        it.offset = offset;
+        it.data.assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + size);
+        d->enqueue(std::move(it));
+    })
+}
+GBR_API gbr_status gbr_buffer_read(gbr_device dh, gbr_buffer b, uint64_t offset, void* dst, uint64_t size) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        Item it;
+        it.kind = Item::READ_BUFFER;
+        it.buffer = d->get<Buffer>(b, "buffer");
+        if (offset + size > it.buffer->size) fail(GBR_ERR_VALIDATION, "buffer read out of range");
+        it.offset = offset;
+        it.dst = dst;
+        it.size = size;
+        std::promise<Failure> done;
+        auto fut = done.get_future();
+        it.done = &done;
+        d->enqueue(std::move(it));
+        Failure f = fut.get();
+        if (f.status != GBR_OK) throw f;
+    })
+}
+
+GBR_API gbr_status gbr_texture_create(gbr_device dh, const gbr_texture_desc* desc, gbr_texture* out) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        if (!desc) fail(GBR_ERR_INVALID_ARGUMENT, "null descriptor");
+        uint32_t bpp = bytes_per_texel(desc->format);
+        if (!bpp) fail(GBR_ERR_UNSUPPORTED, "Unsupported texture format: %u", desc->format);
+        if (!desc->size.width || !desc->size.height) fail(GBR_ERR_VALIDATION, "zero-sized texture");
+        cuda_check(cudaSetDevice(d->ordinal), "cudaSetDevice");
+        auto t = std::make_shared<Texture>();
+        t->desc = *desc;
+        t->bpp = bpp;
+        uint32_t mips = desc->mip_level_count ? desc->mip_level_count : 1;
+        // the reference stores mip 0 only (texture.rs:34-43); the extension profile keeps the chain
+        t->mips_stored = d->cfg.profile == GBR_PROFILE_EXTENSION ? std::min(mips, 16u) : 1;
+        uint64_t off = 0;
+        for (uint32_t m = 0; m < t->mips_stored; ++m) {
+            t->mip_offset[m] = off;
+            off += (t->mip_bytes(m) + 255) & ~uint64_t(255);
+        }
+        t->bytes = off;
+        cuda_check(cudaMalloc(&t->ptr, off), "cudaMalloc(texture)");
+        cuda_check(cudaMemset(t->ptr, 0, off), "cudaMemset(texture)");
+        *out = d->add(t);
+    })
+}
+GBR_API gbr_status gbr_texture_destroy(gbr_device dh, gbr_texture t) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        d->get<Texture>(t, "texture");
+        d->remove(t);
+    })
+}
+GBR_API gbr_status gbr_queue_write_texture(gbr_device dh, gbr_texture th, uint32_t mip, const void* data,
+                                           uint64_t data_size, const gbr_texel_copy_buffer_layout* layout,
+                                           gbr_extent3d size) {
+    GBR_TRY({
+        (void)size;  // the reference copies the whole texture (the extent is shadowed, device.rs:388)
+        auto d = get_device(dh);
+        Item it;
+        it.kind = Item::WRITE_TEXTURE;
+        it.texture = d->get<Texture>(th, "texture");
+        const Texture& t = *it.texture;
+        if (mip >= t.mips_stored) fail(GBR_ERR_UNSUPPORTED, "write_texture to mip_level %u (device.rs:378-380)", mip);
+        it.mip = mip;
+        it.layout = *layout;
+        uint64_t row = (uint64_t)t.mip_w(mip) * t.bpp;
+        uint64_t src_row = layout->bytes_per_row ? layout->bytes_per_row : data_size;
+        uint64_t rows_per_image = layout->rows_per_image ? layout->rows_per_image : t.mip_h(mip);
+        if (src_row < row) fail(GBR_ERR_VALIDATION, "bytes_per_row smaller than a texel row");
+        uint64_t need = layout->offset + ((uint64_t)(t.layers() - 1) * rows_per_image + (t.mip_h(mip) - 1)) * src_row + row;
+        if (need > data_size) fail(GBR_ERR_VALIDATION, "write_texture source out of range");
+        it.data.assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + data_size);
+        d->enqueue(std::move(it));
+    })
+}
+GBR_API gbr_status gbr_texture_read(gbr_device dh, gbr_texture th, uint32_t mip, void* dst, uint64_t size) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        Item it;
+        it.kind = Item::READ_TEXTURE;
+        it.texture = d->get<Texture>(th, "texture");
+        if (mip >= it.texture->mips_stored) fail(GBR_ERR_VALIDATION, "mip level not stored");
+        if (size < it.texture->mip_bytes(mip)) fail(GBR_ERR_VALIDATION, "destination too small");
+        it.mip = mip;
+        it.dst = dst;
+        std::promise<Failure> done;
+        auto fut = done.get_future();
+        it.done = &done;
+        d->enqueue(std::move(it));
+        Failure f = fut.get();
+        if (f.status != GBR_OK) throw f;
+    })
+}
+
+GBR_API gbr_status gbr_sampler_create(gbr_device dh, const gbr_sampler_desc* desc, gbr_sampler* out) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        auto s = std::make_shared<Sampler>();
+        s->desc = *desc;
+        *out = d->add(s);
+    })
+}
+GBR_API gbr_status gbr_sampler_destroy(gbr_device dh, gbr_sampler s) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        d->get<Sampler>(s, "sampler");
+        d->remove(s);
+    })
+}
+
+GBR_API gbr_status gbr_shader_module_create_native(gbr_device dh, const char* name, gbr_shader_module* out) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        const ProgramInfo* p = name ? find_program(name) : nullptr;
+        if (!p) fail(GBR_ERR_SHADER, "unknown native program '%s'", name ? name : "(null)");
+        auto m = std::make_shared<ShaderModule>();
+        m->prog = p;
+        *out = d->add(m);
+    })
+}
+GBR_API gbr_status gbr_shader_module_create(gbr_device dh, const char* wgsl, uint64_t len, gbr_shader_module* out) {
+    GBR_TRY({
+        (void)wgsl;
+        (void)len;
+        (void)out;
+        get_device(dh);
+        fail(GBR_ERR_UNSUPPORTED, "WGSL translation is not available in this build; use a native program");
+    })
+}
+GBR_API gbr_status gbr_shader_module_destroy(gbr_device dh, gbr_shader_module m) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        d->get<ShaderModule>(m, "shader module");
+        d->remove(m);
+    })
+}
+
+GBR_API gbr_status gbr_render_pipeline_create(gbr_device dh, const gbr_render_pipeline_desc* desc,
+                                              gbr_render_pipeline* out) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        if (!desc) fail(GBR_ERR_INVALID_ARGUMENT, "null descriptor");
+        auto pl = std::make_shared<Pipeline>();
+        pl->desc = *desc;
+        auto vs = d->get<ShaderModule>(desc->vertex_module, "shader module");
+        pl->prog = vs->prog;
+        if (desc->has_fragment) {
+            auto fs = d->get<ShaderModule>(desc->fragment_module, "shader module");
+            if (fs->prog != vs->prog)
+                fail(GBR_ERR_UNSUPPORTED, "native programs pair their own vertex and fragment stages");
+        }
+        if (desc->vertex_buffer_count > GBR_MAX_VERTEX_BUFFERS) fail(GBR_ERR_VALIDATION, "too many vertex buffers");
+        for (auto& a : pl->attr) a = AttrDesc{-1, 0, 0, 0};
+        // VertexState::new (vertex.rs:50-94): location -> (buffer, offset, format); duplicates panic
+        for (uint32_t b = 0; b < desc->vertex_buffer_count; ++b) {
+            const gbr_vertex_buffer_layout& L = desc->vertex_buffers[b];
+            if (L.array_stride % 4) fail(GBR_ERR_VALIDATION, "array_stride must be a multiple of 4");
+            for (uint32_t a = 0; a < L.attribute_count && a < GBR_MAX_VERTEX_ATTRIBUTES; ++a) {
+                const gbr_vertex_attribute& at = L.attributes[a];
+                if (at.shader_location >= 16) fail(GBR_ERR_VALIDATION, "shader location out of range");
+                if (pl->attr[at.shader_location].buffer >= 0)
+                    fail(GBR_ERR_VALIDATION, "Duplicate vertex attribute at location %u", at.shader_location);
+                uint32_t align = at.format == GBR_VERTEX_FORMAT_UNORM8X4 ? 1u
+                                 : (at.format == GBR_VERTEX_FORMAT_FLOAT16X2 || at.format == GBR_VERTEX_FORMAT_FLOAT16X4) ? 2u
+                                                                                                                       : 4u;
+                if (at.offset % align) fail(GBR_ERR_VALIDATION, "attribute offset must be a multiple of %u", align);
+                pl->attr[at.shader_location] = AttrDesc{(int32_t)b, at.format, (uint32_t)at.offset, 0};
+            }
+        }
+        const ProgramInfo& p = *pl->prog;
+        for (int i = 0; i < p.num_inputs; ++i) {
+            const AttrDesc& a = pl->attr[p.input_loc[i]];
+            if (a.buffer < 0) fail(GBR_ERR_VALIDATION, "No vertex attribute at location %d", p.input_loc[i]);
+            uint32_t fsz = vertex_format_bytes(a.format);
+            bool ext_conv = d->cfg.profile == GBR_PROFILE_EXTENSION && p.input_comps[i] == 4 &&
+                            (a.format == GBR_VERTEX_FORMAT_FLOAT16X4 || a.format == GBR_VERTEX_FORMAT_UNORM8X4);
+            if (!ext_conv && fsz != (uint32_t)p.input_comps[i] * 4u)
+                fail(GBR_ERR_VALIDATION, "vertex format size %u does not match the shader input (vertex.rs:150-154)", fsz);
+        }
+        if (desc->has_depth_stencil && desc->depth_stencil.format != GBR_TEXTURE_FORMAT_DEPTH32_FLOAT)
+            fail(GBR_ERR_UNSUPPORTED, "depth format");
+        *out = d->add(pl);
+    })
+}
+GBR_API gbr_status gbr_render_pipeline_destroy(gbr_device dh, gbr_render_pipeline p) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        d->get<Pipeline>(p, "pipeline");
+        d->remove(p);
+    })
+}
+
+GBR_API gbr_status gbr_bind_group_create(gbr_device dh, const gbr_bind_group_desc* desc, gbr_bind_group* out) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        if (!desc || desc->entry_count > GBR_MAX_BIND_GROUP_ENTRIES) fail(GBR_ERR_INVALID_ARGUMENT, "bad descriptor");
+        auto g = std::make_shared<BindGroup>();
+        g->desc = *desc;
+        for (uint32_t e = 0; e < desc->entry_count; ++e) {
+            const gbr_bind_group_entry& en = desc->entries[e];
+            if (en.kind == GBR_BINDING_BUFFER) {
+                auto b = d->get<Buffer>(en.resource, "buffer");
+                if (en.offset > b->size || (en.size && en.offset + en.size > b->size))
+                    fail(GBR_ERR_VALIDATION, "bind group buffer range out of bounds");
+                if (en.offset % 16) fail(GBR_ERR_VALIDATION, "uniform binding offset must be a multiple of 16");
+                g->refs.push_back(b);
+            } else if (en.kind == GBR_BINDING_SAMPLER) {
+                g->refs.push_back(d->get<Sampler>(en.resource, "sampler"));
+            } else if (en.kind == GBR_BINDING_TEXTURE_VIEW) {
+                g->refs.push_back(d->get<Texture>(en.resource, "texture"));
+            } else {
+                fail(GBR_ERR_INVALID_ARGUMENT, "binding kind");
+            }
+        }
+        *out = d->add(g);
+    })
+}
+GBR_API gbr_status gbr_bind_group_destroy(gbr_device dh, gbr_bind_group g) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        d->get<BindGroup>(g, "bind group");
+        d->remove(g);
+    })
+}
+
+GBR_API gbr_status gbr_queue_submit(gbr_device dh, const void* cmds, uint64_t len, uint64_t* out_index) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        Item it;
+        it.kind = Item::SUBMIT;
+        it.t_submit = Clock::now();
+        it.passes = decode(*d, static_cast<const uint8_t*>(cmds), cmds ? len : 0);
+        {
+            std::lock_guard<std::mutex> lk(d->q_mu);
+            if (d->lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", d->lost_msg.c_str());
+            it.index = d->next_submission++;
+            if (out_index) *out_index = it.index;
+            d->queue.push_back(std::move(it));
+            d->q_cv.notify_all();
+        }
+    })
+}
+
+GBR_API gbr_status gbr_device_poll(gbr_device dh, uint32_t wait, uint32_t has_index, uint64_t index,
+                                   uint64_t timeout_ns, uint32_t* out_status) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        std::unique_lock<std::mutex> lk(d->q_mu);
+        if (!wait) {
+            if (out_status) *out_status = GBR_POLL_POLL;
+            return GBR_OK;
+        }
+        auto deadline = timeout_ns == UINT64_MAX ? Clock::time_point::max()
+                                                 : Clock::now() + std::chrono::nanoseconds(timeout_ns);
+        if (d->completed_submissions == d->next_submission) {
+            if (out_status) *out_status = GBR_POLL_QUEUE_EMPTY;
+            return GBR_OK;
+        }
+        uint64_t target = has_index ? index + 1 : d->completed_submissions + 1;
+        if (has_index && index >= d->next_submission) fail(GBR_ERR_INVALID_ARGUMENT, "unknown submission index");
+        while (d->completed_submissions < target) {
+            if (deadline == Clock::time_point::max()) {
+                d->done_cv.wait(lk);
+            } else if (d->done_cv.wait_until(lk, deadline) == std::cv_status::timeout &&
+                       d->completed_submissions < target) {
+                fail(GBR_ERR_TIMEOUT, "poll timed out");
+            }
+        }
+        if (out_status) *out_status = GBR_POLL_WAIT_SUCCEEDED;
+        if (has_index) {
+            auto it = d->records.find(index);
+            if (it != d->records.end() && it->second.status != GBR_OK) fail(it->second.status, "%s", it->second.error.c_str());
+        }
+    })
+}
+
+GBR_API gbr_status gbr_submission_stats_get(gbr_device dh, uint64_t index, gbr_submission_stats* out) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        std::lock_guard<std::mutex> lk(d->q_mu);
+        auto it = d->records.find(index);
+        if (it == d->records.end()) fail(GBR_ERR_INVALID_ARGUMENT, "unknown or unfinished submission");
+        *out = it->second.stats;
+    })
+}
+
+GBR_API gbr_status gbr_device_elapsed_ms(gbr_device dh, uint64_t first, uint64_t last, double* out_ms) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        std::lock_guard<std::mutex> lk(d->q_mu);
+        auto a = d->records.find(first), b = d->records.find(last);
+        if (a == d->records.end() || b == d->records.end() || !a->second.ev_start || !b->second.ev_end)
+            fail(GBR_ERR_INVALID_ARGUMENT, "no device timing for these submissions");
+        float ms = 0.0f;
+        cuda_check(cudaEventElapsedTime(&ms, a->second.ev_start, b->second.ev_end), "cudaEventElapsedTime");
+        *out_ms = ms;
+    })
+}
+
+GBR_API gbr_status gbr_device_flush_caches(gbr_device dh) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        Item it;
+        it.kind = Item::FLUSH;
+        static uint64_t salt = 0;
+        it.offset = ++salt;
+        d->enqueue(std::move(it));
+    })
+}
+
+}  // extern "C"

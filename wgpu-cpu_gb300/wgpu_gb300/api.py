@@ -132,6 +132,11 @@ class Profile:
     EXTENSION = 1
 
 
+class LaunchMode:
+    PER_PASS = 0
+    PER_DRAW = 1
+
+
 class BindingKind:
     BUFFER = 0
     SAMPLER = 1
@@ -436,8 +441,9 @@ class Device:
     """One device + queue + worker (wgpu_cpu::instance -> request_adapter -> request_device)."""
 
     def __init__(self, lib: Optional[A.Lib] = None, profile: int = Profile.PARITY, tile_size: int = 0,
-                 warps_per_tile: int = 0, bin_capacity: int = 0, batch_submissions: bool = False,
-                 use_graphs: bool = False, hbm_budget_bytes: int = 0, device_ordinal: int = 0):
+                 warps_per_tile: int = 0, bin_capacity: int = 0, launch_mode: int = LaunchMode.PER_PASS,
+                 batch_submissions: bool = False, use_graphs: bool = False, hbm_budget_bytes: int = 0,
+                 device_ordinal: int = 0, time_kernels: bool = False):
         self.lib = lib if lib is not None else gpu_lib()
         cfg = A.DeviceConfig()
         cfg.abi_version = A.GBR_ABI_VERSION
@@ -446,8 +452,10 @@ class Device:
         cfg.tile_size = tile_size
         cfg.warps_per_tile = warps_per_tile
         cfg.bin_capacity = bin_capacity
+        cfg.launch_mode = launch_mode
         cfg.batch_submissions = int(batch_submissions)
         cfg.use_graphs = int(use_graphs)
+        cfg.time_kernels = int(time_kernels)
         cfg.hbm_budget_bytes = hbm_budget_bytes
         h = C.c_uint64()
         self.handle = 0
@@ -596,6 +604,18 @@ class Device:
         s = A.SubmissionStats()
         _check(self.lib, self.lib.submission_stats_get(self.handle, index, C.byref(s)))
         return s
+
+    def elapsed_ms(self, first: int, last: int) -> float:
+        """Device time from the start of submission `first` to the end of `last` (CUDA events)."""
+        if self.lib.device_elapsed_ms is None:
+            raise GbrError(A.ERR_UNSUPPORTED, "no device timing in this library")
+        out = C.c_double()
+        _check(self.lib, self.lib.device_elapsed_ms(self.handle, first, last, C.byref(out)))
+        return out.value
+
+    def flush_caches(self) -> None:
+        if self.lib.device_flush_caches is not None:
+            _check(self.lib, self.lib.device_flush_caches(self.handle))
 
     def read_texture(self, texture: Texture, mip_level: int = 0) -> np.ndarray:
         w, h = texture.mip_size(mip_level)
