@@ -903,6 +903,7 @@ std::vector<PassCmd> decode(Device& dev, const uint8_t* data, uint64_t len) {
 }
 
 }  // namespace
+
 }  // namespace gbr
 
 using namespace gbr;
