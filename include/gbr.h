@@ -483,6 +483,63 @@ GBR_API gbr_status gbr_device_elapsed_ms(gbr_device device, uint64_t first_submi
  * device stream, evicting the L2 cache between timed submissions. */
 GBR_API gbr_status gbr_device_flush_caches(gbr_device device);
 
+/* ---------------------------------------------------------------- allocation-free rendering
+ *
+ * No counterpart in the reference: wgpu-cpu has no entry point of this kind.
+ *
+ * gbr_render_triangles_noalloc draws a non-indexed triangle list whose vertices are already in
+ * clip space into caller-owned device memory, and allocates no memory at all: no cudaMalloc,
+ * no cudaFree, no allocating library routine.  It is meant for callers that cannot allocate
+ * device memory themselves or let a library do it: a plugin running inside a host application
+ * that owns every byte of the device, or a frame loop that must not take the implicit device
+ * synchronisation that cudaMalloc/cudaFree perform.
+ *
+ * The rasterisation is the same as the device/queue path's (same kernels, same bit-exact
+ * coverage, interpolation, depth test and Rgba8Unorm encoding, parity profile): the per-vertex
+ * colour is interpolated linearly and written as the fragment colour.  Its scratch space
+ * (triangle records, tile bins, counters) is one fixed array in the library's device memory,
+ * GBR_NOALLOC_SCRATCH_BYTES large, which every GPU that loads the library keeps until the
+ * process exits.  Limits: at most GBR_NOALLOC_MAX_TRIANGLES triangles, targets of at most
+ * GBR_NOALLOC_MAX_DIM x GBR_NOALLOC_MAX_DIM pixels, and at most GBR_NOALLOC_MAX_CLIPPED extra
+ * sub-triangles from clipping and GBR_NOALLOC_MAX_BIN_ENTRIES triangle/tile pairs; beyond
+ * them the call returns GBR_ERR_OUT_OF_MEMORY with a message saying which limit was hit, and
+ * the targets are left unchanged.
+ *
+ * Every call shares that one scratch array and overwrites what the previous call left there,
+ * so calls whose GPU work overlaps (two host threads, or two streams) race with each other:
+ * serialise them.  The first call on a device looks up the array's device address (once per
+ * device, with that device current); make that first call before any stream capture.  The
+ * call returns after the work on `stream` has finished.
+ *
+ *   clip_positions  device pointer, 3 * triangle_count float4 (x, y, z, w), 16-byte aligned
+ *   colors          device pointer, 3 * triangle_count float4 (r, g, b, a), 16-byte aligned
+ *   color_target    device pointer, width * height Rgba8Unorm texels, 4-byte aligned
+ *   depth_target    device pointer to width * height f32 (Depth32Float), or NULL for none
+ *   stream          a cudaStream_t, or NULL for the default stream
+ */
+#define GBR_NOALLOC_SCRATCH_BYTES (24u << 20)
+#define GBR_NOALLOC_MAX_TRIANGLES 32768u
+#define GBR_NOALLOC_MAX_CLIPPED 8192u
+#define GBR_NOALLOC_MAX_DIM 2048u
+#define GBR_NOALLOC_MAX_BIN_ENTRIES 3800000u
+
+typedef struct gbr_noalloc_state {
+    uint32_t cull_mode;           /* gbr_cull_mode */
+    uint32_t front_face;          /* gbr_front_face */
+    uint32_t depth_compare;       /* gbr_compare_function, used when depth_target != NULL */
+    uint32_t depth_write_enabled;
+    uint32_t color_load_op;       /* gbr_load_op */
+    uint32_t depth_load_op;       /* gbr_load_op */
+    float clear_color[4];
+    float clear_depth;
+    uint32_t _pad;
+} gbr_noalloc_state;
+
+GBR_API gbr_status gbr_render_triangles_noalloc(const float* clip_positions, const float* colors,
+                                                uint32_t triangle_count, uint8_t* color_target, float* depth_target,
+                                                uint32_t width, uint32_t height, const gbr_noalloc_state* state,
+                                                void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -89,3 +89,195 @@ cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms
 }
 
 }  // namespace gbr
+
+// ============================================================================================
+// gbr_render_triangles_noalloc: the render-pass kernels above, with every byte of scratch taken
+// from one file-scope device array instead of allocated memory (see include/gbr.h).
+#include <cstdio>
+#include <cstring>
+
+#include "gbr.h"
+
+namespace gbr {
+void set_thread_error(const char* msg);  // runtime.cu: the text gbr_last_error() returns
+}
+
+namespace {
+
+using namespace gbr;
+
+// The whole scratch of the allocation-free entry point.  It lives in the library's device
+// memory on every GPU that loads the library, until the process exits.
+static __device__ __align__(256) uint8_t g_noalloc_scratch[GBR_NOALLOC_SCRATCH_BYTES];
+
+// Layout of g_noalloc_scratch (byte offsets).
+constexpr size_t kNaAbort = 0, kNaStatus = 256, kNaWork = 512, kNaDraw = 1024, kNaTarget = 4096;
+constexpr size_t kNaTiles = 8192, kNaRecords = 262144;
+constexpr uint32_t kNaVaryings = 4;  // clip_passthrough carries one vec4f colour
+constexpr uint32_t kNaStride = (uint32_t)((sizeof(TriRecord) + 3 * kNaVaryings * sizeof(float) + 15) & ~size_t(15));
+constexpr size_t kNaOvf = kNaRecords + (size_t)GBR_NOALLOC_MAX_TRIANGLES * kNaStride;
+constexpr size_t kNaBins = kNaOvf + (size_t)GBR_NOALLOC_MAX_CLIPPED * kNaStride;
+constexpr uint32_t kNaTile = 16, kNaWarps = 8;
+constexpr uint32_t kNaMaxTiles = (GBR_NOALLOC_MAX_DIM / kNaTile) * (GBR_NOALLOC_MAX_DIM / kNaTile);
+static_assert(sizeof(DrawDesc) <= kNaTarget - kNaDraw, "DrawDesc does not fit its slot");
+static_assert(sizeof(TargetDesc) <= kNaTiles - kNaTarget, "TargetDesc does not fit its slot");
+static_assert(kNaTiles + 3 * (kNaMaxTiles + 1) * sizeof(uint32_t) <= kNaRecords, "tile arrays do not fit");
+static_assert(kNaBins + (size_t)GBR_NOALLOC_MAX_BIN_ENTRIES * sizeof(uint32_t) <= GBR_NOALLOC_SCRATCH_BYTES,
+              "bins do not fit the scratch array");
+
+std::mutex g_na_mu;
+constexpr int kNaMaxDevices = 64;
+uint8_t* g_na_scratch[kNaMaxDevices] = {};  // device address of g_noalloc_scratch, per device
+
+gbr_status na_fail(gbr_status st, const char* msg) {
+    set_thread_error(msg);
+    return st;
+}
+
+}  // namespace
+
+extern "C" GBR_API gbr_status gbr_render_triangles_noalloc(const float* clip_positions, const float* colors,
+                                                           uint32_t triangle_count, uint8_t* color_target,
+                                                           float* depth_target, uint32_t width, uint32_t height,
+                                                           const gbr_noalloc_state* state, void* stream) {
+    char msg[256];
+    if (!state || !color_target || (triangle_count && (!clip_positions || !colors)))
+        return na_fail(GBR_ERR_INVALID_ARGUMENT, "null argument");
+    if (width == 0 || height == 0) return na_fail(GBR_ERR_INVALID_ARGUMENT, "zero-sized target");
+    if (triangle_count > GBR_NOALLOC_MAX_TRIANGLES) {
+        snprintf(msg, sizeof msg, "triangle_count %u exceeds GBR_NOALLOC_MAX_TRIANGLES (%u)", triangle_count,
+                 GBR_NOALLOC_MAX_TRIANGLES);
+        return na_fail(GBR_ERR_OUT_OF_MEMORY, msg);
+    }
+    if (width > GBR_NOALLOC_MAX_DIM || height > GBR_NOALLOC_MAX_DIM) {
+        snprintf(msg, sizeof msg, "target %ux%u exceeds GBR_NOALLOC_MAX_DIM (%u)", width, height, GBR_NOALLOC_MAX_DIM);
+        return na_fail(GBR_ERR_OUT_OF_MEMORY, msg);
+    }
+    if (((uintptr_t)clip_positions | (uintptr_t)colors) % 16 || (uintptr_t)color_target % 4 ||
+        (uintptr_t)depth_target % 4)
+        return na_fail(GBR_ERR_INVALID_ARGUMENT, "misaligned device pointer");
+    if (state->depth_compare > GBR_COMPARE_ALWAYS || state->cull_mode > GBR_CULL_BACK || state->front_face > 1)
+        return na_fail(GBR_ERR_INVALID_ARGUMENT, "invalid raster state");
+
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return na_fail(GBR_ERR_CUDA, cudaGetErrorString(e));
+    if (dev < 0 || dev >= kNaMaxDevices) return na_fail(GBR_ERR_INVALID_ARGUMENT, "device ordinal out of range");
+    uint8_t* scratch = nullptr;
+    {
+        // Set-up, once per device with that device current: the host-side name of the array is
+        // only a stand-in, so its device address is looked up and passed to the kernels.
+        std::lock_guard<std::mutex> lk(g_na_mu);
+        if (!g_na_scratch[dev]) {
+            void* p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p) return na_fail(GBR_ERR_CUDA, "cudaGetSymbolAddress(g_noalloc_scratch) failed");
+            g_na_scratch[dev] = static_cast<uint8_t*>(p);
+        }
+        scratch = g_na_scratch[dev];
+    }
+    int num_sms = 0;
+    e = cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return na_fail(GBR_ERR_CUDA, cudaGetErrorString(e));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+    // The draw and its target, resolved as the queue path resolves a clip_passthrough draw.
+    DrawDesc d;
+    std::memset(&d, 0, sizeof d);
+    d.topology = GBR_TOPOLOGY_TRIANGLE_LIST;
+    d.count = 3 * triangle_count;
+    d.instance_count = 1;
+    d.prims_per_instance = triangle_count;
+    d.vb_data[0] = reinterpret_cast<const uint8_t*>(clip_positions);
+    d.vb_data[1] = reinterpret_cast<const uint8_t*>(colors);
+    d.vb_size[0] = d.vb_size[1] = (uint64_t)d.count * 16;
+    d.vb_stride_vertex[0] = d.vb_stride_vertex[1] = 16;
+    for (auto& a : d.attr) a = AttrDesc{-1, 0, 0, 0};
+    d.attr[0] = AttrDesc{0, GBR_VERTEX_FORMAT_FLOAT32X4, 0, 0};
+    d.attr[1] = AttrDesc{1, GBR_VERTEX_FORMAT_FLOAT32X4, 0, 0};
+    d.program = PROG_CLIP_PASSTHROUGH;
+    d.has_fragment = 1;
+    d.num_varyings = kNaVaryings;
+    d.profile = GBR_PROFILE_PARITY;
+    d.cull_mode = state->cull_mode;
+    d.front_face = state->front_face;
+    volatile float vw = (float)width, vh = (float)height;  // ToRaster::new with the default viewport
+    d.vp_tx = 0.0f + 0.5f * vw;
+    d.vp_ty = 0.0f + 0.5f * vh;
+    d.vp_sx = 0.5f * vw;
+    d.vp_sy = (0.5f * vh) * -1.0f;
+    d.sc_x1 = width;
+    d.sc_y1 = height;
+    d.depth_test = depth_target ? 1u : 0u;
+    d.depth_compare = state->depth_compare;
+    d.depth_write = state->depth_write_enabled;
+    d.write_mask = 0xF;
+    TargetDesc t;
+    std::memset(&t, 0, sizeof t);
+    t.color = color_target;
+    t.depth = depth_target;
+    t.width = width;
+    t.height = height;
+    t.color_format = GBR_TEXTURE_FORMAT_RGBA8_UNORM;
+    t.color_bpp = 4;
+    t.color_load = state->color_load_op == GBR_LOAD_OP_CLEAR ? 1u : 0u;
+    t.depth_load = state->depth_load_op == GBR_LOAD_OP_CLEAR ? 1u : 0u;
+    for (int k = 0; k < 4; ++k) t.clear[k] = state->clear_color[k];
+    t.depth_clear = state->clear_depth;
+    t.tiles_x = (width + kNaTile - 1) / kNaTile;
+    t.tiles_y = (height + kNaTile - 1) / kNaTile;
+
+    BatchParams bp;
+    std::memset(&bp, 0, sizeof bp);
+    bp.draws = reinterpret_cast<const DrawDesc*>(scratch + kNaDraw);
+    bp.targets = reinterpret_cast<const TargetDesc*>(scratch + kNaTarget);
+    bp.num_draws = triangle_count ? 1 : 0;
+    bp.num_targets = 1;
+    bp.total_prims = triangle_count;
+    bp.total_tiles = t.tiles_x * t.tiles_y;
+    bp.tile_size = kNaTile;
+    bp.tile_shift = 4;
+    bp.record_stride = kNaStride;
+    bp.num_varyings = kNaVaryings;
+    bp.records = scratch + kNaRecords;
+    bp.ovf_records = scratch + kNaOvf;
+    bp.ovf_capacity = GBR_NOALLOC_MAX_CLIPPED;
+    bp.bin_capacity = GBR_NOALLOC_MAX_BIN_ENTRIES;
+    uint32_t* tiles = reinterpret_cast<uint32_t*>(scratch + kNaTiles);
+    bp.tile_count = tiles;
+    bp.tile_offset = tiles + (kNaMaxTiles + 1);
+    bp.tile_cursor = tiles + 2 * (kNaMaxTiles + 1);
+    bp.bins = reinterpret_cast<uint32_t*>(scratch + kNaBins);
+    bp.work_counter = reinterpret_cast<uint32_t*>(scratch + kNaWork);
+    bp.status = reinterpret_cast<BatchStatus*>(scratch + kNaStatus);
+    bp.abort_flag = reinterpret_cast<uint32_t*>(scratch + kNaAbort);
+
+    // The array keeps whatever the previous call left: clear the flag the kernels read first
+    // (launch_batch zeroes the tile counts, the status and the work counter itself).
+    if ((e = cudaMemsetAsync(scratch + kNaAbort, 0, sizeof(uint32_t), s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(scratch + kNaDraw, &d, sizeof d, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(scratch + kNaTarget, &t, sizeof t, cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        return na_fail(GBR_ERR_CUDA, cudaGetErrorString(e));
+    uint32_t launches = 0;
+    if ((e = launch_batch(bp, kNaTile, kNaWarps, num_sms, s, &launches)) != cudaSuccess)
+        return na_fail(GBR_ERR_CUDA, cudaGetErrorString(e));
+    BatchStatus st;
+    if ((e = cudaMemcpyAsync(&st, scratch + kNaStatus, sizeof st, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return na_fail(GBR_ERR_CUDA, cudaGetErrorString(e));
+    switch (st.error) {
+        case ERR_NONE: return GBR_OK;
+        case ERR_OVERFLOW_RECORDS:
+            snprintf(msg, sizeof msg, "clipping produced more than GBR_NOALLOC_MAX_CLIPPED (%u) extra sub-triangles",
+                     GBR_NOALLOC_MAX_CLIPPED);
+            return na_fail(GBR_ERR_OUT_OF_MEMORY, msg);
+        case ERR_OVERFLOW_BINS:
+            snprintf(msg, sizeof msg, "%llu triangle/tile pairs exceed GBR_NOALLOC_MAX_BIN_ENTRIES (%u)",
+                     (unsigned long long)st.bin_entries, GBR_NOALLOC_MAX_BIN_ENTRIES);
+            return na_fail(GBR_ERR_OUT_OF_MEMORY, msg);
+        case ERR_W_ZERO: return na_fail(GBR_ERR_VALIDATION, "clip position w=0 (primitive.rs:177 / raster.rs:146)");
+        default:
+            snprintf(msg, sizeof msg, "device error %u (primitive %u)", st.error, st.error_detail);
+            return na_fail(GBR_ERR_VALIDATION, msg);
+    }
+}

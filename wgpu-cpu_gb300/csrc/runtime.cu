@@ -904,6 +904,10 @@ std::vector<PassCmd> decode(Device& dev, const uint8_t* data, uint64_t len) {
 
 }  // namespace
 
+// Sets the text that gbr_last_error() returns on this thread (used by entry points defined in
+// other translation units).
+void set_thread_error(const char* msg) { g_last_error = msg ? msg : ""; }
+
 }  // namespace gbr
 
 using namespace gbr;
