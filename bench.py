@@ -1,21 +1,30 @@
-"""Benchmark of the render-pass path on the textured-mesh workload.
+"""Benchmark of the render-pass path.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
-Workload (one step = one render pass = one frame): displaced icosphere subdivided 6 times
-(81,920 triangles, f32x3 position + f32x3 normal + f32x2 UV), a 1024x1024 Rgba8UnormSrgb
-checker x value-noise texture, texture x Lambert fragment shader, 1920x1080 Rgba8UnormSrgb +
-Depth32Float (Less), cleared every frame.  Parity profile: nearest sampling with sRGB formats
-read and written as linear, exactly as wgpu-cpu does (its sampler ignores filter modes and it
-stores mip 0 only).  Inputs are seeded synthetic data.
+One step = one render pass (one frame) of the workload, submitted through the library's queue.
 
-`value` is shaded fragments per second with every input resident in HBM, timed with CUDA events
-on the library's stream (each step's device time; an L2 flush between steps keeps every step
-cold because the working set is smaller than the 129 MB L2).  `e2e` is the same metric through the
-C ABI with host buffers: each step uploads vertices, indices, uniforms and the texture from pinned
-host memory, renders, and reads the colour target back.  `--impl reference` times the CPU
-restatement of wgpu-cpu's rasteriser (the oracle; the Rust reference cannot be built here) on all
-host cores.  One GPU per process: with N > 1 every rank renders its own replica.
+Workloads (seeded synthetic inputs with the configurations' shapes; no dataset exists):
+  textured (default)  displaced icosphere subdivided 6 times (81,920 triangles; f32x3 position,
+                      f32x3 normal, f32x2 UV), 1024x1024 Rgba8UnormSrgb checker x value-noise
+                      texture, texture x Lambert shading, 1920x1080 Rgba8UnormSrgb + Depth32Float
+                      (Less).  Parity profile: nearest sampling, sRGB formats read and written as
+                      linear, exactly as wgpu-cpu does (its sampler ignores filter modes).
+  blend               10,000 screen-aligned quads (20,000 triangles), sides U[16,1024] px, RGBA f16
+                      colours with alpha U[0.1,0.9], painter order, SrcAlpha/OneMinusSrcAlpha into
+                      3840x2160 Rgba16Float (extension profile: the reference has neither blending
+                      nor f16 targets).  The fill-rate-bound configuration.
+  colored             UV sphere 32x16 (992 triangles), per-vertex colours, back-face cull,
+                      512x512 Rgba8Unorm (the reference's CPU-runnable configuration).
+
+`value` is shaded fragments per second (fragment-shader invocations, counted as the reference
+counts them) with every input resident in HBM, over the device time of the K steps (CUDA events on
+the library's stream; a 256 MiB L2 flush is enqueued between steps, so each step starts cold).
+`e2e` is the same metric through the C ABI with host buffers: each step uploads the pass's inputs
+from pinned host memory, renders, and reads the colour target back.  `roofline` covers the
+dominant kernel (k_raster).  `--impl reference` times the CPU restatement of wgpu-cpu's rasteriser
+(the oracle; the Rust reference cannot be built here) on all host cores.  One GPU per process;
+with N > 1 each rank renders its own replica and `value` sums them.
 """
 
 from __future__ import annotations
@@ -35,16 +44,51 @@ import numpy as np  # noqa: E402
 
 METRIC = "shaded fragments/s, batched vs per-draw GPU at bit-exact coverage; p99 submit ms"
 UNIT = "fragments/s"
-WORKLOAD = dict(width=1920, height=1080, level=6, tex_size=1024)
 
 
-def config_block(flush: bool = True) -> dict:
-    return {"workload": "textured icosphere: 81,920 tris, 1920x1080 Rgba8UnormSrgb + Depth32Float Less, "
-                        "1024^2 texture, texture x Lambert, parity profile (nearest, sRGB as linear)",
-            "triangles": 81920, "target": "1920x1080", "texture": "1024x1024 rgba8", "profile": "parity",
-            "launch_mode": "per_pass", "tile": 16, "warps_per_tile": 8,
-            "l2": "flushed between timed steps (256 MiB write)" if flush else "inputs resident",
-            "seed": 2}
+class Workload:
+    def __init__(self, name, profile, builder, kwargs, bytes_per_fragment, pixel_bytes, description, extra_cfg,
+                 cpu_kwargs=None, dtype="f32"):
+        self.name, self.profile, self.builder, self.kwargs = name, profile, builder, kwargs
+        self.bytes_per_fragment, self.pixel_bytes = bytes_per_fragment, pixel_bytes
+        self.description, self.extra_cfg = description, extra_cfg
+        self.cpu_kwargs = cpu_kwargs if cpu_kwargs is not None else kwargs
+        self.dtype = dtype
+
+    def build(self, dev, **over):
+        from wgpu_gb300 import workloads as wl
+
+        return getattr(wl, self.builder)(dev, **{**self.kwargs, **over})
+
+    def config(self, flush=True):
+        return {"workload": self.description, **self.extra_cfg, "launch_mode": "per_pass",
+                "l2": "flushed between timed steps (256 MiB write)" if flush else "n/a (CPU)"}
+
+
+def workloads():
+    from wgpu_gb300 import api as W
+
+    return {
+        "textured": Workload(
+            "textured", W.Profile.PARITY, "scene_textured_icosphere",
+            dict(width=1920, height=1080, level=6, tex_size=1024),
+            4 + 4 + 4 + 4, 1920 * 1080 * (4 + 4),
+            "textured icosphere: 81,920 tris, 1920x1080 Rgba8UnormSrgb + Depth32Float Less, 1024^2 texture, "
+            "texture x Lambert, parity profile (nearest, sRGB as linear)",
+            {"triangles": 81920, "target": "1920x1080", "texture": "1024x1024 rgba8", "profile": "parity", "seed": 2}),
+        "blend": Workload(
+            "blend", W.Profile.EXTENSION, "scene_blended_quads", dict(width=3840, height=2160, n_quads=10000),
+            8 + 8, 3840 * 2160 * 8,
+            "blended quads: 10,000 quads (20,000 tris) sides U[16,1024], painter order, SrcAlpha/OneMinusSrcAlpha "
+            "into 3840x2160 Rgba16Float, extension profile",
+            {"triangles": 20000, "target": "3840x2160 rgba16float", "profile": "extension", "seed": 4},
+            cpu_kwargs=dict(width=3840, height=2160, n_quads=60), dtype="f32 (f16 storage)"),
+        "colored": Workload(
+            "colored", W.Profile.PARITY, "scene_colored_sphere", dict(width=512, height=512),
+            4, 512 * 512 * 4,
+            "colored UV sphere: 992 tris, 512x512 Rgba8Unorm, back-face cull, no depth",
+            {"triangles": 992, "target": "512x512", "profile": "parity", "seed": 1}),
+    }
 
 
 def dist_env():
@@ -59,17 +103,14 @@ class ClockSampler:
               "clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index: int):
-        self.gpu = gpu_index
-        self.proc = None
-        self.lines = []
+        self.gpu, self.proc, self.lines = gpu_index, None, []
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-            self._t = threading.Thread(target=self._read, daemon=True)
-            self._t.start()
+            threading.Thread(target=self._read, daemon=True).start()
         except OSError:
             self.proc = None
         return self
@@ -113,9 +154,9 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def raster_traffic():
-    """DRAM bytes per raster launch from the committed ncu summary, if one exists."""
-    p = os.path.join(ROOT, "profiles", "raster_textured_icosphere_1080p.json")
+def raster_traffic(name):
+    """DRAM bytes per raster launch from the committed ncu summary of this workload, if any."""
+    p = os.path.join(ROOT, "profiles", f"raster_{name}.json")
     if os.path.exists(p):
         try:
             return json.load(open(p)).get("dram_bytes_per_launch")
@@ -124,15 +165,15 @@ def raster_traffic():
     return None
 
 
-def cpu_baseline(target_seconds: float = 12.0):
-    """The oracle (CPU restatement of wgpu-cpu's rasteriser) on all host cores."""
+def cpu_baseline(wk: Workload, target_seconds: float = 12.0):
+    """The oracle (CPU restatement of wgpu-cpu's rasteriser) on all host cores, bounded sample."""
     import oracle_device
-    from wgpu_gb300 import workloads as wl
 
     cores = os.cpu_count() or 1
-    dev = oracle_device.device(threads=cores)
-    scene = wl.scene_textured_icosphere(dev, **WORKLOAD)
-    frags, t0, frames = 0, time.perf_counter(), 0
+    dev = oracle_device.device(profile=wk.profile, threads=cores)
+    scene = getattr(__import__("wgpu_gb300.workloads", fromlist=["x"]), wk.builder)(dev, **wk.cpu_kwargs)
+    frags, frames = 0, 0
+    t0 = time.perf_counter()
     while True:
         idx = scene.render()
         frags += dev.submission_stats(idx).fragments_shaded
@@ -141,37 +182,37 @@ def cpu_baseline(target_seconds: float = 12.0):
             break
     dt = time.perf_counter() - t0
     oracle_device.oracle_lib.load().orc_set_threads(1)
+    what = "full frames of the workload" if wk.cpu_kwargs == wk.kwargs else f"frames of the workload cut to {wk.cpu_kwargs}"
     return {"value": frags / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{frames} full frames of the workload ({frags // frames} fragments each) in {dt:.1f} s"}
+            "sample": f"{frames} {what} ({frags // frames} fragments each) in {dt:.1f} s, row bands per thread"}
 
 
-def run_reference(args):
+def run_reference(args, wk: Workload):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    base = cpu_baseline(target_seconds=max(5.0, 2.0 * args.steps))
+    base = cpu_baseline(wk, target_seconds=max(5.0, min(60.0, 2.0 * args.steps)))
     line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config_block(False),
+            "vs_baseline": None, "dtype": wk.dtype, "data": "synthetic (seeded)", "config": wk.config(False),
             "cpu_baseline": base,
             "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args):
+def run_ours(args, wk: Workload):
     import torch
 
     from wgpu_gb300 import api as W
-    from wgpu_gb300 import workloads as wl
 
     rank, world, local = dist_env()
     if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    dev = W.Device(device_ordinal=local, time_kernels=True)
-    scene = wl.scene_textured_icosphere(dev, **WORKLOAD)
+    dev = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True, tile_size=args.tile,
+                   warps_per_tile=args.warps)
+    over = {"n_quads": args.quads} if args.quads and wk.name == "blend" else {}
+    scene = wk.build(dev, **over)
     enc = dev.create_command_encoder()
     scene.record(enc)
     cmd = enc.finish()
@@ -190,83 +231,73 @@ def run_ours(args):
     barrier()
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
-        first = None
         subs = []
         for _ in range(args.steps):
             dev.flush_caches()
-            i = dev.queue.submit([cmd])
-            subs.append(i)
+            subs.append(dev.queue.submit([cmd]))
         dev.poll(True, subs[-1])
         wall = time.perf_counter() - t0
     barrier()
     stats = [dev.submission_stats(i) for i in subs]
     gpu_ms = [s.gpu_ms for s in stats]
-    raster_ms = [getattr(s, "raster_ms", 0.0) for s in stats]
+    raster_ms = [s.raster_ms for s in stats]
     device_s = sum(gpu_ms) / 1e3
     if world > 1:
         t = torch.tensor([device_s], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         device_s = float(t.item())
-    total_frags = frags_per_step * args.steps * world
-    value = total_frags / device_s
+    value = frags_per_step * args.steps * world / device_s
     launches = int(sum(s.kernel_launches for s in stats))
 
-    # roofline of the dominant kernel (raster/shade/ROP): algorithmic bytes per launch
-    w, h = WORKLOAD["width"], WORKLOAD["height"]
-    pix_bytes = w * h * (4 + 4)                       # colour + depth written once per pixel
-    frag_bytes = frags_per_step * (4 + 4 + 4 + 4)     # depth read + depth write + colour write + texel
-    alg_bytes = pix_bytes + frag_bytes
+    # roofline of the dominant kernel: algorithmic bytes per launch / its event-timed duration
+    alg_bytes = wk.pixel_bytes + frags_per_step * wk.bytes_per_fragment
     peak, peak_src = measured_peak_hbm()
-    r_ms = float(np.mean(raster_ms)) if any(raster_ms) else float(np.mean(gpu_ms))
+    r_ms = float(np.mean(raster_ms))
     achieved = alg_bytes / (r_ms / 1e3) / 1e9
-    traffic = raster_traffic()
 
-    # end to end through the C ABI with host buffers (pinned), host<->device copies timed
-    pos, nrm, uv, faces = wl.displaced_icosphere(WORKLOAD["level"], 2)
-    vdata = torch.from_numpy(np.concatenate([pos, nrm, uv], 1).astype(np.float32).ravel().view(np.uint8)).pin_memory()
-    idata = torch.from_numpy(faces.ravel().view(np.uint8)).pin_memory()
-    tdata = torch.from_numpy(wl.checker_noise_texture(WORKLOAD["tex_size"], 102).ravel()).pin_memory()
-    udata = torch.from_numpy(np.frombuffer(
-        wl.mvp_bytes(wl.camera_mvp(w, h)) + np.array([0.3, 0.5, 0.8, 0.0], np.float32).tobytes(), np.uint8).copy()
-    ).pin_memory()
-    out = torch.empty(w * h * 4, dtype=torch.uint8).pin_memory()
-    vb, ib = scene.draws[0][2][0], scene.draws[0][3]
-    ub, tex = scene._keep[2], scene._keep[3]
+    # end to end through the C ABI: inputs from pinned host memory, colour target read back
+    pinned = [(obj, torch.from_numpy(np.ascontiguousarray(arr).reshape(-1).view(np.uint8)).pin_memory())
+              for obj, arr in scene.uploads]
+    out_bytes = scene.color.width * scene.color.height * W.BYTES_PER_TEXEL[scene.color.format]
+    out = torch.empty(out_bytes, dtype=torch.uint8).pin_memory()
 
     def e2e_step():
-        dev.queue.write_buffer(vb, 0, vdata.numpy())
-        dev.queue.write_buffer(ib, 0, idata.numpy())
-        dev.queue.write_buffer(ub, 0, udata.numpy())
-        dev.queue.write_texture(tex, tdata.numpy())
+        for obj, host in pinned:
+            if isinstance(obj, W.Texture):
+                dev.queue.write_texture(obj, host.numpy())
+            else:
+                dev.queue.write_buffer(obj, 0, host.numpy())
         i = dev.queue.submit([cmd])
         dev.poll(True, i)
-        dev.lib.texture_read(dev.handle, scene.color.handle, 0, out.data_ptr(), out.numel())
-        return i
+        st = dev.lib.texture_read(dev.handle, scene.color.handle, 0, out.data_ptr(), out.numel())
+        if st != 0:
+            raise W.GbrError(st, dev.lib.error_text())
 
-    for _ in range(max(1, args.warmup)):
+    for _ in range(max(1, min(args.warmup, 3))):
         e2e_step()
     e_steps = max(3, min(args.steps, 20))
     t0 = time.perf_counter()
     for _ in range(e_steps):
         e2e_step()
     e2e_s = (time.perf_counter() - t0) / e_steps
-    h2d = vdata.numel() + idata.numel() + udata.numel() + tdata.numel()
+    h2d = sum(h.numel() for _, h in pinned)
 
     if rank == 0:
-        base = cpu_baseline() if world == 1 and not args.no_cpu_baseline else None
+        base = cpu_baseline(wk) if world == 1 and not args.no_cpu_baseline else None
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": sum(gpu_ms) / len(gpu_ms), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": config_block(), "fragments_per_step": frags_per_step,
-            "wall_ms_per_step": wall * 1e3 / args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.mean(gpu_ms)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": wk.dtype, "data": "synthetic (seeded)",
+            "config": {**wk.config(), "tile": dev_tile(args), "warps_per_tile": dev_warps(args),
+                       **({"n_quads": args.quads} if over else {})},
+            "fragments_per_step": frags_per_step, "wall_ms_per_step": wall * 1e3 / args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
-                         "kernel": "k_raster (tile sort + raster + shade + depth + ROP)",
+                         "frac": achieved / peak, "traffic": raster_traffic(wk.name) if not over else None,
+                         "peak_source": peak_src, "kernel": "k_raster (tile sort + raster + shade + depth/blend + ROP)",
                          "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": r_ms},
             "cpu_baseline": base,
             "e2e": {"value": frags_per_step / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-                    "d2h_bytes_per_step": int(out.numel()), "ms_per_step": e2e_s * 1e3},
+                    "d2h_bytes_per_step": int(out_bytes), "ms_per_step": e2e_s * 1e3},
             "gpu_launches": launches,
             "clocks": clocks.summary(),
         }
@@ -276,20 +307,32 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def dev_tile(args):
+    return args.tile or 16
+
+
+def dev_warps(args):
+    return args.warps or (2 if dev_tile(args) == 8 else 8)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="textured", choices=["textured", "blend", "colored"])
+    ap.add_argument("--quads", type=int, default=0, help="blend workload: number of quads (profiling runs)")
+    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
-    if args.warmup < 3:
-        args.warmup = 3
+    args.warmup = max(3, args.warmup)
+    wk = workloads()[args.workload]
     if args.impl == "reference":
-        run_reference(args)
+        run_reference(args, wk)
     else:
-        run_ours(args)
+        run_ours(args, wk)
 
 
 if __name__ == "__main__":

@@ -482,6 +482,12 @@ GBR_API gbr_status gbr_device_elapsed_ms(gbr_device device, uint64_t first_submi
 /* No reference counterpart (measurement): enqueues a write of a 256 MiB scratch buffer on the
  * device stream, evicting the L2 cache between timed submissions. */
 GBR_API gbr_status gbr_device_flush_caches(gbr_device device);
+/* No reference counterpart (verification): runs `samples` seeded quotients through the
+ * raster kernels' division by a precomputed reciprocal (exact.cuh, div_by_recip) on the current
+ * CUDA device and counts results whose bits differ from CUDA's __fdiv_rn.  `first_mismatch`
+ * receives (a, b) of the first difference found, if any. */
+GBR_API gbr_status gbr_selftest_division(uint64_t samples, uint64_t seed, uint64_t* out_mismatches,
+                                         float* first_mismatch);
 
 /* ---------------------------------------------------------------- allocation-free rendering
  *

@@ -189,6 +189,21 @@ def test_discard_program(gpu, orc):
     assert_same(*res, "discard")
 
 
+def test_division_by_reciprocal_matches_cuda(gpu):
+    """The raster kernels divide by a per-record reciprocal with Markstein's correction steps;
+    every quotient must carry exactly the bits of CUDA's correctly rounded __fdiv_rn."""
+    import ctypes
+
+    fn = gpu.lib.cdll.gbr_selftest_division
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_float)]
+    mism = ctypes.c_uint64()
+    first = (ctypes.c_float * 2)()
+    for seed in (1, 2):
+        assert fn(1 << 32, seed, ctypes.byref(mism), first) == 0, gpu.lib.error_text()
+        assert mism.value == 0, f"{mism.value} mismatches, first a={first[0]!r} b={first[1]!r}"
+
+
 def test_errors_are_reported(gpu):
     s = wl.scene_colored_sphere(gpu, 64, 64)
     pl, groups, vbs, ib, rng, bv = s.draws[0]

@@ -62,6 +62,30 @@ __device__ __forceinline__ int64_t div_trunc(int64_t n, int64_t d) {
     return n / d;
 }
 
+// a / b correctly rounded (round to nearest even), given y = RN(1/b) from __frcp_rn.
+//
+// Method: P. Markstein, "Computation of elementary functions on the IBM RISC System/6000
+// processor" (IBM J. Res. Dev. 34(1), 1990), Theorem: if y is within half an ulp of 1/b and q is
+// within one ulp of a/b, then with r = a - b*q computed exactly by one fused multiply-add,
+// RN(q + r*y) is the correctly rounded quotient (see also Muller et al., Handbook of Floating-Point
+// Arithmetic, §4.7).  q0 = RN(a*y) can be up to ~1.5 ulp away, so one correction step first makes
+// it faithful; the second step then rounds correctly.  The theorem assumes no underflow or
+// overflow: the fast path is taken only for 2^-60 <= |a|, |b| <= 2^60 (quotients, remainders and
+// products then stay far inside the normal range); zeros, NaNs, infinities and everything outside
+// go to __fdiv_rn.  tests/test_gpu_parity.py checks the result against __fdiv_rn bit for bit.
+__device__ __forceinline__ bool div_fast_ok(float v) {
+    const float m = fabsf(v);
+    return m >= 0x1p-60f && m <= 0x1p60f;
+}
+__device__ __forceinline__ float div_by_recip(float a, float b, float y, bool b_ok) {
+    if (!(b_ok && div_fast_ok(a))) return __fdiv_rn(a, b);
+    const float q0 = __fmul_rn(a, y);
+    const float r0 = __fmaf_rn(-b, q0, a);
+    const float q1 = __fmaf_rn(r0, y, q0);
+    const float r1 = __fmaf_rn(-b, q1, a);
+    return __fmaf_rn(r1, y, q1);
+}
+
 __device__ __forceinline__ uint16_t f32_to_f16_bits(float f) { return __half_as_ushort(__float2half_rn(f)); }
 __device__ __forceinline__ float f16_bits_to_f32(uint16_t h) { return __half2float(__ushort_as_half(h)); }
 

@@ -12,12 +12,12 @@ namespace gbr {
 namespace {
 
 constexpr int kCap = 4096;  // keys per tile sorted in shared memory; larger bins sort in place
-constexpr int kRB = 32;     // records staged in shared memory per step
+constexpr int kRW = 64;     // records staged in shared memory per window
 
-template <int T, int W>
+template <int T, int W, int KIND = 0>
 cudaError_t launch_raster(const BatchParams& bp, int num_sms, cudaStream_t s) {
-    auto kern = k_raster<T, W, kCap, kRB>;
-    const size_t smem = kCap * sizeof(uint32_t) + (size_t)kRB * bp.record_stride;
+    auto kern = k_raster<T, W, kCap, kRW, KIND>;
+    const size_t smem = (kCap + 2 * W * 32) * sizeof(uint32_t) + (size_t)kRW * bp.record_stride;
     static std::mutex mu;
     static size_t configured = 0;
     static int blocks_per_sm = 0;
@@ -39,6 +39,41 @@ cudaError_t launch_raster(const BatchParams& bp, int num_sms, cudaStream_t s) {
 
 }  // namespace
 
+// Seeded inputs for the division self-test: random bit patterns, raster-like magnitudes,
+// exact multiples and neighbours of powers of two, in rotation.
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+}
+__device__ __forceinline__ float selftest_value(uint64_t r, uint32_t kind) {
+    const uint32_t lo = (uint32_t)r, hi = (uint32_t)(r >> 32);
+    switch (kind & 3u) {
+        case 0: return __uint_as_float(lo);                                      // any bit pattern
+        case 1: return (float)((int32_t)(lo & 0x3FFFFFF) - 0x2000000) * 0.013f;  // pixel-scale values
+        case 2: return __uint_as_float((lo & 0x807FFFFFu) | ((100u + (hi & 63u)) << 23));
+        default: return ldexpf(1.0f + (float)(lo & 7u) * 0x1p-23f * (hi & 1u ? -1.0f : 1.0f), (int)(hi % 80u) - 40);
+    }
+}
+__global__ void k_selftest_division(uint64_t n, uint64_t seed, unsigned long long* mismatches, float* first) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const uint64_t r0 = splitmix64(seed ^ (i * 2 + 0)), r1 = splitmix64(seed ^ (i * 2 + 1));
+        const float a = selftest_value(r0, (uint32_t)(i & 3u));
+        float b = selftest_value(r1, (uint32_t)((i >> 2) & 3u));
+        if ((i >> 4) % 5u == 0) b = __fmul_rn(a, (float)(1 + (r1 & 15)));  // quotients 1/k
+        const float y = __frcp_rn(b);
+        const float q = div_by_recip(a, b, y, div_fast_ok(b));
+        const float ref = __fdiv_rn(a, b);
+        const bool same = __float_as_uint(q) == __float_as_uint(ref) || (q != q && ref != ref);
+        if (!same && atomicAdd(mismatches, 1ull) == 0ull) {
+            first[0] = a;
+            first[1] = b;
+        }
+    }
+}
+
 bool raster_config_supported(int tile, int warps) {
     switch (tile) {
         case 8: return warps == 1 || warps == 2;
@@ -49,7 +84,7 @@ bool raster_config_supported(int tile, int warps) {
 }
 
 cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms, cudaStream_t s,
-                         uint32_t* launches, cudaEvent_t* ev_raster) {
+                         uint32_t* launches, cudaEvent_t* ev_raster, int kind) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(bp.tile_count, 0, (bp.total_tiles + 1) * sizeof(uint32_t), s)) != cudaSuccess) return e;
     if ((e = cudaMemsetAsync(bp.status, 0, sizeof(BatchStatus), s)) != cudaSuccess) return e;
@@ -72,15 +107,27 @@ cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms
         ++*launches;
     }
     if (ev_raster && (e = cudaEventRecord(ev_raster[0], s)) != cudaSuccess) return e;
-    switch (tile * 16 + warps) {
-        case 8 * 16 + 1: e = launch_raster<8, 1>(bp, num_sms, s); break;
-        case 8 * 16 + 2: e = launch_raster<8, 2>(bp, num_sms, s); break;
-        case 16 * 16 + 2: e = launch_raster<16, 2>(bp, num_sms, s); break;
-        case 16 * 16 + 4: e = launch_raster<16, 4>(bp, num_sms, s); break;
-        case 16 * 16 + 8: e = launch_raster<16, 8>(bp, num_sms, s); break;
-        case 32 * 16 + 4: e = launch_raster<32, 4>(bp, num_sms, s); break;
-        case 32 * 16 + 8: e = launch_raster<32, 8>(bp, num_sms, s); break;
-        default: return cudaErrorInvalidValue;
+    for (;;) {
+    switch ((tile * 16 + warps) * 4 + (kind & 3)) {
+        case (8 * 16 + 1) * 4: e = launch_raster<8, 1>(bp, num_sms, s); break;
+        case (8 * 16 + 2) * 4: e = launch_raster<8, 2>(bp, num_sms, s); break;
+        case (8 * 16 + 2) * 4 + 1: e = launch_raster<8, 2, 1>(bp, num_sms, s); break;
+        case (8 * 16 + 2) * 4 + 2: e = launch_raster<8, 2, 2>(bp, num_sms, s); break;
+        case (16 * 16 + 2) * 4: e = launch_raster<16, 2>(bp, num_sms, s); break;
+        case (16 * 16 + 4) * 4: e = launch_raster<16, 4>(bp, num_sms, s); break;
+        case (16 * 16 + 8) * 4: e = launch_raster<16, 8>(bp, num_sms, s); break;
+        case (16 * 16 + 8) * 4 + 1: e = launch_raster<16, 8, 1>(bp, num_sms, s); break;
+        case (16 * 16 + 8) * 4 + 2: e = launch_raster<16, 8, 2>(bp, num_sms, s); break;
+        case (32 * 16 + 4) * 4: e = launch_raster<32, 4>(bp, num_sms, s); break;
+        case (32 * 16 + 8) * 4: e = launch_raster<32, 8>(bp, num_sms, s); break;
+        case (32 * 16 + 8) * 4 + 1: e = launch_raster<32, 8, 1>(bp, num_sms, s); break;
+        case (32 * 16 + 8) * 4 + 2: e = launch_raster<32, 8, 2>(bp, num_sms, s); break;
+        default:
+            if (kind == 0) return cudaErrorInvalidValue;
+            kind = 0;  // no specialised instantiation for this tile shape: the generic kernel
+            continue;
+    }
+    break;
     }
     if (e != cudaSuccess) return e;
     ++*launches;
@@ -280,4 +327,33 @@ extern "C" GBR_API gbr_status gbr_render_triangles_noalloc(const float* clip_pos
             snprintf(msg, sizeof msg, "device error %u (primitive %u)", st.error, st.error_detail);
             return na_fail(GBR_ERR_VALIDATION, msg);
     }
+}
+
+extern "C" GBR_API gbr_status gbr_selftest_division(uint64_t samples, uint64_t seed, uint64_t* out_mismatches,
+                                                    float* first_mismatch) {
+    if (!out_mismatches) return na_fail(GBR_ERR_INVALID_ARGUMENT, "null argument");
+    unsigned long long* d_count = nullptr;
+    float* d_first = nullptr;
+    cudaError_t e = cudaMalloc(&d_count, sizeof(unsigned long long) + 2 * sizeof(float));
+    if (e != cudaSuccess) return na_fail(GBR_ERR_CUDA, cudaGetErrorString(e));
+    d_first = reinterpret_cast<float*>(d_count + 1);
+    unsigned long long h_count = 0;
+    float h_first[2] = {0.0f, 0.0f};
+    int dev = 0, sms = 0;
+    if ((e = cudaMemset(d_count, 0, sizeof(unsigned long long) + 2 * sizeof(float))) == cudaSuccess &&
+        (e = cudaGetDevice(&dev)) == cudaSuccess &&
+        (e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) == cudaSuccess) {
+        gbr::k_selftest_division<<<sms * 8, 256>>>(samples, seed, d_count, d_first);
+        if ((e = cudaGetLastError()) == cudaSuccess &&
+            (e = cudaMemcpy(&h_count, d_count, sizeof h_count, cudaMemcpyDeviceToHost)) == cudaSuccess)
+            e = cudaMemcpy(h_first, d_first, sizeof h_first, cudaMemcpyDeviceToHost);
+    }
+    cudaFree(d_count);
+    if (e != cudaSuccess) return na_fail(GBR_ERR_CUDA, cudaGetErrorString(e));
+    *out_mismatches = h_count;
+    if (first_mismatch) {
+        first_mismatch[0] = h_first[0];
+        first_mismatch[1] = h_first[1];
+    }
+    return GBR_OK;
 }

@@ -181,6 +181,102 @@ __device__ __forceinline__ bool run_vs(const DrawDesc& d, uint32_t vertex, uint3
     }
 }
 
+// What the fragment stage and the output merger need of a draw, cached per warp in shared
+// memory by the raster kernel (built from the DrawDesc in global memory).
+struct RasterState {
+    uint32_t draw;  // DrawDesc index this copy was built from
+    uint32_t program, nvar, interp;
+    uint32_t sc_x0, sc_y0, sc_x1, sc_y1;
+    uint32_t depth_test, depth_compare, depth_write;
+    uint32_t blend_enabled, write_mask;
+    uint32_t blend_over;  // colour SrcAlpha/OneMinusSrcAlpha/Add, alpha One/OneMinusSrcAlpha/Add
+    uint32_t blend_color[3], blend_alpha[3];
+    float blend_constant[4];
+    const uint8_t* tex_data;
+    uint32_t tex_w, tex_h, addr_u, addr_v;
+    float uconst[4];  // program constants read from the uniform block (light direction)
+};
+
+__device__ __forceinline__ void build_raster_state(const DrawDesc& d, uint32_t di, RasterState& rs) {
+    rs.draw = di;
+    rs.program = d.program;
+    rs.nvar = d.num_varyings;
+    rs.interp = program_interp(d.program);
+    rs.sc_x0 = d.sc_x0;
+    rs.sc_y0 = d.sc_y0;
+    rs.sc_x1 = d.sc_x1;
+    rs.sc_y1 = d.sc_y1;
+    rs.depth_test = d.depth_test;
+    rs.depth_compare = d.depth_compare;
+    rs.depth_write = d.depth_write;
+    rs.blend_enabled = d.blend_enabled;
+    rs.write_mask = d.write_mask;
+    for (int k = 0; k < 3; ++k) {
+        rs.blend_color[k] = d.blend_color[k];
+        rs.blend_alpha[k] = d.blend_alpha[k];
+    }
+    for (int k = 0; k < 4; ++k) rs.blend_constant[k] = d.blend_constant[k];
+    rs.blend_over = d.blend_color[0] == 4 && d.blend_color[1] == 5 && d.blend_color[2] == 0 && d.blend_alpha[0] == 1 &&
+                    d.blend_alpha[1] == 5 && d.blend_alpha[2] == 0;
+    rs.tex_data = d.tex.data;
+    rs.tex_w = d.tex.width;
+    rs.tex_h = d.tex.height;
+    rs.addr_u = d.samp.address_u;
+    rs.addr_v = d.samp.address_v;
+    for (int k = 0; k < 4; ++k) rs.uconst[k] = 0.0f;
+    if (d.program == PROG_MESH_TEX_LAMBERT) {
+        rs.uconst[0] = ld_uniform(d, 0, 0, 64);
+        rs.uconst[1] = ld_uniform(d, 0, 0, 68);
+        rs.uconst[2] = ld_uniform(d, 0, 0, 72);
+    }
+}
+
+// texel_coordinate with Repeat computed as x - trunc(x): for finite x this is exactly
+// fmodf(x, 1.0) (the fractional part of a binary32 value is representable and the subtraction
+// is exact); the two can differ only in the sign of a zero result, which the following
+// `< 0`, multiply, round and saturating cast map to the same texel 0.  Infinite/NaN x give NaN
+// either way.
+__device__ __forceinline__ uint32_t texel_coordinate_fast(float x, uint32_t mode, uint32_t size) {
+    if (mode == 1) {
+        float r = fsub(x, truncf(x));
+        x = (r < 0.0f) ? fadd(r, 1.0f) : r;
+        return rust_f2u32(roundf(fmul(x, (float)(size - 1u))));
+    }
+    return texel_coordinate(x, mode, size);
+}
+
+// Nearest Rgba8 sample with `x as f32 / 255.0` from a table of exactly those 256 quotients.
+__device__ __forceinline__ V4 sample_nearest_rgba8_lut(const RasterState& rs, float u, float v, const float* lut) {
+    uint32_t x = texel_coordinate_fast(u, rs.addr_u, rs.tex_w);
+    uint32_t y = texel_coordinate_fast(v, rs.addr_v, rs.tex_h);
+    uint32_t px = __ldg(reinterpret_cast<const uint32_t*>(rs.tex_data) + (size_t)y * rs.tex_w + x);
+    return {lut[px & 0xFFu], lut[(px >> 8) & 0xFFu], lut[(px >> 16) & 0xFFu], lut[px >> 24]};
+}
+
+// Fragment stage on the cached state.  Returns false when the fragment is discarded.
+__device__ __forceinline__ bool run_fs_rs(const RasterState& rs, const float* var, const float* lut, V4& color) {
+    switch (rs.program) {
+        case PROG_COLORED_TRIANGLE:
+        case PROG_QUAD_COLOR:
+        case PROG_CLIP_PASSTHROUGH: color = {var[0], var[1], var[2], var[3]}; return true;
+        case PROG_MESH_COLOR:
+        case PROG_MESH_COLOR_PERSPECTIVE: color = {var[0], var[1], var[2], 1.0f}; return true;
+        case PROG_MESH_COLOR_DISCARD:
+            if (var[0] < 0.5f) return false;
+            color = {var[0], var[1], var[2], 1.0f};
+            return true;
+        case PROG_MESH_TEX_LAMBERT: {
+            V4 t = sample_nearest_rgba8_lut(rs, var[3], var[4], lut);
+            float dd = fadd(fmul(var[0], rs.uconst[0]), fmul(var[1], rs.uconst[1]));
+            dd = fadd(dd, fmul(var[2], rs.uconst[2]));
+            float k = (dd > 0.0f) ? dd : 0.0f;  // select(0.0, d, d > 0.0)
+            color = {fmul(t.x, k), fmul(t.y, k), fmul(t.z, k), fmul(t.w, k)};
+            return true;
+        }
+        default: return false;
+    }
+}
+
 // Fragment stage.  Returns false when the fragment is discarded.
 __device__ __forceinline__ bool run_fs(const DrawDesc& d, const float* var, V4& color) {
     switch (d.program) {

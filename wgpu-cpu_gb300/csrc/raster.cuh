@@ -201,16 +201,17 @@ __device__ __forceinline__ void span_at(const TriRecord& r, int y, int& x1, int&
 }
 
 // Calls f(tile_index_in_target) for every tile whose pixels the record can emit.
+// Tile rows are visited from `first` in steps of `step` (1, or 32 when a warp shares a record).
 template <class F>
 __device__ __forceinline__ void for_each_tile(const TriRecord& r, const DrawDesc& d, const TargetDesc& t, uint32_t shift,
-                                              F&& f) {
+                                              F&& f, int first = 0, int step = 1) {
     int lo = max(r.row0, (int)d.sc_y0);
     int hi = min(r.row1, min((int)d.sc_y1 - 1, (int)t.height - 1));
     if (lo > hi) return;
     const int T = 1 << shift;
     const int sx_hi = min((int)d.sc_x1 - 1, (int)t.width - 1);
     const int sx_lo = (int)d.sc_x0;
-    for (int ty = lo >> shift; ty <= (hi >> shift); ++ty) {
+    for (int ty = (lo >> shift) + first; ty <= (hi >> shift); ty += step) {
         int y0 = max(lo, ty << shift), y1 = min(hi, (ty << shift) + T - 1);
         int xa, xb, mn, mx;
         span_at(r, y0, xa, xb);
@@ -298,6 +299,10 @@ __device__ __forceinline__ bool build_record(const BatchParams& bp, const DrawDe
         flags |= 2u;
     }
     if (area == 0.0f) flags |= 2u;  // raster.rs:308-311: no fragments
+    // bit 4: the clip barycentrics are exactly the unit vectors (an unclipped triangle)
+    if (v[0].b[0] == 1.0f && v[0].b[1] == 0.0f && v[0].b[2] == 0.0f && v[1].b[0] == 0.0f && v[1].b[1] == 1.0f &&
+        v[1].b[2] == 0.0f && v[2].b[0] == 0.0f && v[2].b[1] == 0.0f && v[2].b[2] == 1.0f)
+        flags |= 16u;
     int row0 = (int)py[0], row1;
     if (py[2] == py[0]) {
         flags |= SPAN_DEGENERATE << 2;
@@ -331,8 +336,11 @@ __device__ __forceinline__ bool build_record(const BatchParams& bp, const DrawDe
     }
     r->area = area;
     float* rv = rec_var(r);
+#pragma unroll
     for (uint32_t i = 0; i < 3; ++i)
-        for (uint32_t k = 0; k < nvar; ++k) rv[i * nvar + k] = var[i][k];
+#pragma unroll
+        for (uint32_t k = 0; k < MAX_VARYING_FLOATS; ++k)
+            if (k < nvar) rv[i * nvar + k] = var[i][k];
     return true;
 }
 
@@ -343,11 +351,37 @@ __device__ __forceinline__ void count_tiles(const BatchParams& bp, const TriReco
     for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) { atomicAdd(&bp.tile_count[base + lt], 1u); });
 }
 
+// A record spanning more than two tile rows is handed to the whole warp, whose lanes take its
+// tile rows in turn, so a large triangle does not serialise its thousands of tiles on one lane.
+__device__ __forceinline__ bool tiles_are_many(const TriRecord& r, uint32_t shift) {
+    return (r.row1 >> shift) - (r.row0 >> shift) >= 2;
+}
+template <class F>
+__device__ __forceinline__ void coop_tiles(const BatchParams& bp, const TriRecord* mine, uint32_t lane, F&& f) {
+    uint32_t todo = __ballot_sync(0xFFFFFFFFu, mine != nullptr);
+    while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        __syncwarp();  // the record was written by lane `src`
+        const TriRecord* r = reinterpret_cast<const TriRecord*>(
+            __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(mine), src));
+        const DrawDesc& d = bp.draws[r->draw];
+        const TargetDesc& t = bp.targets[d.target];
+        const uint32_t key = r->key;
+        for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) { f(t.tile_base + lt, key); }, (int)lane, 32);
+    }
+}
+
 __global__ void __launch_bounds__(128) k_setup(BatchParams bp) {
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t gp = blockIdx.x * blockDim.x + threadIdx.x; gp < bp.total_prims; gp += stride) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < bp.total_prims; base += stride) {
+        if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the warp
+        const uint32_t gp = base + lane;
+        const TriRecord* coop = nullptr;  // primary record whose tiles the warp counts together
+        do {
+        if (gp >= bp.total_prims) break;
         TriRecord* prim_rec = rec_at(bp.records, bp.record_stride, gp);
-        if (*bp.abort_flag) return;
         const uint32_t di = find_draw(bp.draws, bp.num_draws, gp);
         const DrawDesc& d = bp.draws[di];
         const uint32_t local = gp - d.prim_base;
@@ -417,7 +451,8 @@ __global__ void __launch_bounds__(128) k_setup(BatchParams bp) {
             }
             prim_rec->nsub = 1;
             prim_rec->ovf = 0;
-            count_tiles(bp, prim_rec, d);
+            if (!(prim_rec->flags & 2u) && tiles_are_many(*prim_rec, bp.tile_shift)) coop = prim_rec;
+            else count_tiles(bp, prim_rec, d);
             continue;
         }
         // clipped: count the sub-triangles, reserve overflow slots, then emit in order
@@ -454,41 +489,84 @@ __global__ void __launch_bounds__(128) k_setup(BatchParams bp) {
                 }
                 ++s;
             }
-        } emitter{&bp, &d, prim_rec, gp, di, p, ovf, 0, front_facing, inv_w0, var, nvar};
+        };
+        // a copy for the emitter, so that only this rare path keeps the varyings in local memory
+        float var_copy[3][MAX_VARYING_FLOATS];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int k = 0; k < (int)MAX_VARYING_FLOATS; ++k) var_copy[i][k] = var[i][k];
+        Emitter emitter{&bp, &d, prim_rec, gp, di, p, ovf, 0, front_facing, inv_w0, var_copy, nvar};
         clip_tri_ordered(pos, emitter);
         if (nsub == 0) prim_rec->flags = 2u;
         prim_rec->nsub = nsub;
         prim_rec->ovf = ovf;
+        } while (false);
+        coop_tiles(bp, coop, lane, [&](uint32_t tile, uint32_t) { atomicAdd(&bp.tile_count[tile], 1u); });
     }
 }
 
 // Single-CTA exclusive scan of tile counts -> tile_offset; zeroes tile_cursor.
+// Chunks of 4096 counts are loaded coalesced into shared memory, each thread scans four
+// consecutive counts, and warps combine through shuffles; a carry links the chunks.
 __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
-    __shared__ uint32_t part[1024];
+    __shared__ uint32_t buf[4096];
+    __shared__ uint32_t warp_sum[32];
+    __shared__ unsigned long long s_carry;
     const uint32_t n = bp.total_tiles;
-    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
-    const uint32_t b = threadIdx.x * per, e = min(n, b + per);
-    uint32_t s = 0;
-    for (uint32_t i = b; i < e; ++i) s += bp.tile_count[i];
-    part[threadIdx.x] = s;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) s_carry = 0;
     __syncthreads();
-    for (uint32_t off = 1; off < blockDim.x; off <<= 1) {
-        uint32_t v = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+    for (uint32_t base = 0; base < n; base += 4096) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t i = base + tid + j * 1024;
+            buf[tid + j * 1024] = i < n ? bp.tile_count[i] : 0u;
+        }
         __syncthreads();
-        part[threadIdx.x] += v;
+        const uint32_t a0 = buf[4 * tid], a1 = buf[4 * tid + 1], a2 = buf[4 * tid + 2], a3 = buf[4 * tid + 3];
+        const uint32_t s = a0 + a1 + a2 + a3;
+        uint32_t x = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) warp_sum[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t w = warp_sum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+                if (lane >= o) w += y;
+            }
+            warp_sum[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t excl = (uint32_t)s_carry + (wid ? warp_sum[wid - 1] : 0u) + x - s;
+        buf[4 * tid] = excl;
+        buf[4 * tid + 1] = excl + a0;
+        buf[4 * tid + 2] = excl + a0 + a1;
+        buf[4 * tid + 3] = excl + a0 + a1 + a2;
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            const uint32_t i = base + tid + j * 1024;
+            if (i < n) {
+                bp.tile_offset[i] = buf[tid + j * 1024];
+                bp.tile_cursor[i] = 0;
+            }
+        }
+        __syncthreads();
+        if (tid == 0) s_carry += warp_sum[31];
         __syncthreads();
     }
-    uint32_t run = part[threadIdx.x] - s;
-    for (uint32_t i = b; i < e; ++i) {
-        uint32_t c = bp.tile_count[i];
-        bp.tile_offset[i] = run;
-        bp.tile_cursor[i] = 0;
-        run += c;
-    }
-    if (threadIdx.x == blockDim.x - 1) {
-        bp.tile_offset[n] = part[blockDim.x - 1];
-        bp.status->bin_entries = part[blockDim.x - 1];
-        if (part[blockDim.x - 1] > bp.bin_capacity) raise_error(bp.status, ERR_OVERFLOW_BINS, part[blockDim.x - 1]);
+    if (tid == 0) {
+        const unsigned long long total = s_carry;
+        bp.tile_offset[n] = (uint32_t)total;
+        bp.status->bin_entries = total;
+        if (total > bp.bin_capacity) raise_error(bp.status, ERR_OVERFLOW_BINS, (uint32_t)min(total, 0xFFFFFFFFull));
     }
 }
 
@@ -497,19 +575,29 @@ __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
     const uint32_t n_ovf = min(bp.status->ovf_used, bp.ovf_capacity);
     const uint32_t total = bp.total_prims + n_ovf;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
-        const TriRecord* r = i < bp.total_prims ? rec_at(bp.records, bp.record_stride, i)
-                                                : rec_at(bp.ovf_records, bp.record_stride, i - bp.total_prims);
-        if (r->flags & 2u) continue;
-        const DrawDesc& d = bp.draws[r->draw];
-        const TargetDesc& t = bp.targets[d.target];
-        const uint32_t base = t.tile_base;
-        const uint32_t key = r->key;
-        for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) {
-            uint32_t tile = base + lt;
-            uint32_t pos = atomicAdd(&bp.tile_cursor[tile], 1u);
-            bp.bins[bp.tile_offset[tile] + pos] = key;
-        });
+    const uint32_t lane = threadIdx.x & 31;
+    auto put = [&](uint32_t tile, uint32_t key) {
+        const uint32_t pos = atomicAdd(&bp.tile_cursor[tile], 1u);
+        bp.bins[bp.tile_offset[tile] + pos] = key;
+    };
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total; base += stride) {
+        const uint32_t i = base + lane;
+        const TriRecord* coop = nullptr;
+        if (i < total) {
+            const TriRecord* r = i < bp.total_prims ? rec_at(bp.records, bp.record_stride, i)
+                                                    : rec_at(bp.ovf_records, bp.record_stride, i - bp.total_prims);
+            if (!(r->flags & 2u)) {
+                if (tiles_are_many(*r, bp.tile_shift)) {
+                    coop = r;
+                } else {
+                    const DrawDesc& d = bp.draws[r->draw];
+                    const TargetDesc& t = bp.targets[d.target];
+                    const uint32_t key = r->key;
+                    for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) { put(t.tile_base + lt, key); });
+                }
+            }
+        }
+        coop_tiles(bp, coop, lane, put);
     }
 }
 
@@ -633,22 +721,70 @@ struct PixelState {
     float depth;
 };
 
-template <int T, int WARPS, int CAP, int RB>
+// Rank sort for small bins: every key counts the keys below it (keys are unique per tile) and
+// goes straight to its place; two barriers instead of a sorting network's log^2 stages.
+__device__ __forceinline__ void rank_sort(const uint32_t* in, uint32_t* out, uint32_t n) {
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+        const uint32_t k = in[i];
+        uint32_t rank = 0;
+        for (uint32_t j = 0; j < n; ++j) rank += in[j] < k ? 1u : 0u;
+        out[rank] = k;
+    }
+}
+
+// x-range of the pixels a record emits on rows [y0, y1] (already inside [row0, row1]).
+__device__ __forceinline__ void band_xrange(const TriRecord& r, int y0, int y1, int& mn, int& mx) {
+    int xa, xb;
+    span_at(r, y0, xa, xb);
+    mn = xa;
+    mx = xb;
+    span_at(r, y1, xa, xb);
+    mn = min(mn, xa);
+    mx = max(mx, xb);
+    const int by = r.sy[1];
+    if (by - 1 >= y0 && by - 1 <= y1) {
+        span_at(r, by - 1, xa, xb);
+        mn = min(mn, xa);
+        mx = max(mx, xb);
+    }
+    if (by >= y0 && by <= y1) {
+        span_at(r, by, xa, xb);
+        mn = min(mn, xa);
+        mx = max(mx, xb);
+    }
+}
+
+// One tile per CTA iteration.  Pixels are owned by threads in 8x4 blocks (one block per warp
+// per PPT slot); their colour and depth stay in registers for the whole tile.  Records are
+// staged RW at a time; for each staged record the CTA computes which 8x4 blocks it can touch
+// (exact per-block-row x ranges of its spans), and every warp walks only the records whose bit
+// is set for its block, in key order (ballot + find-first-set), without further barriers.
+template <int T, int WARPS, int CAP, int RW, int KIND>
 __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
     constexpr int NT = WARPS * 32;
     constexpr int BLK_X = T / 8, BLK_Y = T / 4, NBLK = BLK_X * BLK_Y;
     constexpr int PPT = (NBLK + WARPS - 1) / WARPS;  // 8x4 blocks per warp
+    constexpr int SMALL = 2 * NT;                    // bins up to this size use rank_sort
+    static_assert(NBLK <= 32, "block mask is 32 bits");
     extern __shared__ __align__(16) uint8_t smem_raw[];
-    uint32_t* s_keys = reinterpret_cast<uint32_t*>(smem_raw);                  // CAP keys
-    uint8_t* s_recs = smem_raw + CAP * sizeof(uint32_t);                       // RB records
+    uint32_t* s_keys = reinterpret_cast<uint32_t*>(smem_raw);  // CAP
+    uint32_t* s_sorted = s_keys + CAP;                         // SMALL
+    uint8_t* s_recs = reinterpret_cast<uint8_t*>(s_sorted + SMALL);
+    __shared__ uint32_t s_mask[RW];
+    __shared__ float s_kc[RW][4];  // p-independent shoelace terms of the three barycentrics, RN(1/area)
+    __shared__ int2 s_span[RW * T];  // per staged record and tile row: emitted [x1, x2] within scissor and tile
+    __shared__ const uint8_t* s_rec_ptr[RW];
+    __shared__ RasterState s_rs[WARPS];
+    __shared__ float s_lut[256];
     __shared__ uint32_t s_tile;
-    __shared__ const uint8_t* s_rec_ptr[RB];
     __shared__ unsigned long long s_frag;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const bool failed = bp.status->error != 0 || *bp.abort_flag != 0;
-    if (threadIdx.x == 0) s_frag = 0;
     if (failed && blockIdx.x == 0 && threadIdx.x == 0) *bp.abort_flag = 1u;
+    for (int i = threadIdx.x; i < 256; i += NT) s_lut[i] = fdiv((float)i, 255.0f);  // `x as f32 / 255.0`
+    if (lane == 0) s_rs[warp].draw = 0xFFFFFFFFu;
+    if (threadIdx.x == 0) s_frag = 0;
 
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(bp.work_counter, 1u);
@@ -662,7 +798,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
         const uint32_t n = bp.tile_count[tile];
         const uint32_t off = bp.tile_offset[tile];
 
-        // pixel state init: LoadOp::Clear from the clear value, else the target's texels
+        // pixel state: LoadOp::Clear from the clear value, otherwise the stored texels
         PixelState px[PPT];
         int pxx[PPT], pxy[PPT];
         bool pvalid[PPT];
@@ -691,9 +827,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
             }
         }
 
-        // order the tile's keys
+        // the tile's keys in reference order
         const uint32_t* keys;
-        if (n <= (uint32_t)CAP) {
+        if (n <= (uint32_t)SMALL) {
+            for (uint32_t i = threadIdx.x; i < n; i += NT) s_keys[i] = bp.bins[off + i];
+            __syncthreads();
+            rank_sort(s_keys, s_sorted, n);
+            keys = s_sorted;
+        } else if (n <= (uint32_t)CAP) {
             for (uint32_t i = threadIdx.x; i < n; i += NT) s_keys[i] = bp.bins[off + i];
             __syncthreads();
             block_sort(s_keys, n);
@@ -706,101 +847,218 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
         __syncthreads();
 
         uint32_t frag_count = 0;
-        for (uint32_t b0 = 0; b0 < n; b0 += RB) {
-            const uint32_t nb = min((uint32_t)RB, n - b0);
-            // resolve keys -> record addresses
-            if (threadIdx.x < nb) {
-                const uint32_t key = keys[b0 + threadIdx.x];
+        const uint32_t stride = bp.record_stride;
+        for (uint32_t w0 = 0; w0 < n; w0 += RW) {
+            const uint32_t nb = min((uint32_t)RW, n - w0);
+            for (uint32_t i = threadIdx.x; i < nb; i += NT) {
+                const uint32_t key = keys[w0 + i];
                 const uint32_t prim = key >> SUBTRI_BITS, sub = key & ((1u << SUBTRI_BITS) - 1u);
-                const TriRecord* pr = rec_at(bp.records, bp.record_stride, prim);
-                s_rec_ptr[threadIdx.x] = sub == 0 ? reinterpret_cast<const uint8_t*>(pr)
-                                                  : reinterpret_cast<const uint8_t*>(
-                                                        rec_at(bp.ovf_records, bp.record_stride, pr->ovf + sub - 1));
+                const TriRecord* pr = rec_at(bp.records, stride, prim);
+                s_rec_ptr[i] = sub == 0 ? reinterpret_cast<const uint8_t*>(pr)
+                                        : reinterpret_cast<const uint8_t*>(
+                                              rec_at(bp.ovf_records, stride, pr->ovf + sub - 1));
+                s_mask[i] = 0;
             }
             __syncthreads();
-            // stage records into shared memory (16-byte copies)
-            const uint32_t words = bp.record_stride >> 4;
+            const uint32_t words = stride >> 4;
             for (uint32_t w = threadIdx.x; w < nb * words; w += NT) {
                 const uint32_t ri = w / words, wi = w - ri * words;
-                reinterpret_cast<uint4*>(s_recs + (size_t)ri * bp.record_stride)[wi] =
+                reinterpret_cast<uint4*>(s_recs + (size_t)ri * stride)[wi] =
                     __ldg(reinterpret_cast<const uint4*>(s_rec_ptr[ri]) + wi);
             }
             __syncthreads();
-            for (uint32_t ri = 0; ri < nb; ++ri) {
-                const TriRecord& r = *reinterpret_cast<const TriRecord*>(s_recs + (size_t)ri * bp.record_stride);
-                const DrawDesc& d = bp.draws[r.draw];
-                const float* rv = rec_var(&r);
-                const uint32_t nvar = d.num_varyings;
+            // per (record, tile row): the span the scanline rule emits on that row, cut to the
+            // draw's scissor and to the tile (empty = x1 > x2)
+            for (uint32_t q = threadIdx.x; q < nb * T; q += NT) {
+                const uint32_t ri = q / T, row = q - ri * T;
+                const TriRecord& r = *reinterpret_cast<const TriRecord*>(s_recs + (size_t)ri * stride);
+                if (row == 0) {
+                    s_kc[ri][0] = fmul(fsub(r.vpy[2], r.vpy[1]), fadd(r.vpx[2], r.vpx[1]));
+                    s_kc[ri][1] = fmul(fsub(r.vpy[0], r.vpy[2]), fadd(r.vpx[0], r.vpx[2]));
+                    s_kc[ri][2] = fmul(fsub(r.vpy[1], r.vpy[0]), fadd(r.vpx[1], r.vpx[0]));
+                    s_kc[ri][3] = __frcp_rn(r.area);
+                }
+                const int y = ty * T + (int)row;
+                int2 sp = make_int2(1, 0);
+                if (y >= r.row0 && y <= r.row1) {
+                    const DrawDesc& d = bp.draws[r.draw];
+                    if ((uint32_t)y >= d.sc_y0 && (uint32_t)y < d.sc_y1) {
+                        int x1, x2;
+                        span_at(r, y, x1, x2);
+                        sp.x = max(max(x1, (int)d.sc_x0), tx * T);
+                        sp.y = min(min(x2, (int)d.sc_x1 - 1), tx * T + T - 1);
+                    }
+                }
+                s_span[q] = sp;
+            }
+            __syncthreads();
+            // which 8x4 blocks of the tile each staged record can emit into
+            for (uint32_t ri = threadIdx.x; ri < nb; ri += NT) {
+                uint32_t bits = 0;
 #pragma unroll
-                for (int k = 0; k < PPT; ++k) {
-                    // warp-uniform reject of the whole 8x4 block
-                    const int blk = warp + k * WARPS;
-                    if (blk >= NBLK) continue;
-                    const int bx0 = tx * T + (blk % BLK_X) * 8, by0 = ty * T + (blk / BLK_X) * 4;
-                    if (by0 > r.row1 || by0 + 3 < r.row0 || bx0 > r.xmax || bx0 + 7 < r.xmin) continue;
-                    const int x = pxx[k], y = pxy[k];
-                    if (!pvalid[k] || y < r.row0 || y > r.row1) continue;
-                    int x1, x2;
-                    span_at(r, y, x1, x2);
-                    if (x < x1 || x > x2) continue;
-                    if ((uint32_t)x < d.sc_x0 || (uint32_t)x >= d.sc_x1 || (uint32_t)y < d.sc_y0 ||
-                        (uint32_t)y >= d.sc_y1)
-                        continue;
-                    // barycentrics at the integer pixel corner (raster.rs:313-321, 334-335)
-                    const float fx = (float)x, fy = (float)y;
-                    const float l0 = fdiv(shoelace(fx, fy, r.vpx[1], r.vpy[1], r.vpx[2], r.vpy[2]), r.area);
-                    const float l1 = fdiv(shoelace(r.vpx[0], r.vpy[0], fx, fy, r.vpx[2], r.vpy[2]), r.area);
-                    const float l2 = fdiv(shoelace(r.vpx[0], r.vpy[0], r.vpx[1], r.vpy[1], fx, fy), r.area);
-                    // composed with the clip barycentrics (raster.rs:338-343)
-                    float cmp[3];
+                for (int band = 0; band < BLK_Y; ++band) {
+                    int mn = T, mx = -1;
 #pragma unroll
-                    for (int j = 0; j < 3; ++j)
-                        cmp[j] = fadd(fadd(fmul(r.cb[j], l0), fmul(r.cb[3 + j], l1)), fmul(r.cb[6 + j], l2));
-                    // fragment.z (raster.rs:345-346)
-                    const float z = fadd(fadd(fmul(r.fz[0], cmp[0]), fmul(r.fz[1], cmp[1])), fmul(r.fz[2], cmp[2]));
-                    ++frag_count;
-                    // inter-stage values (fragment.rs:319-378)
-                    float var[MAX_VARYING_FLOATS];
-                    const uint32_t im = program_interp(d.program);
-                    if (im == INTERP_PERSPECTIVE) {
-                        const float den = fadd(fadd(fmul(cmp[0], r.inv_w0[0]), fmul(cmp[1], r.inv_w0[1])),
-                                               fmul(cmp[2], r.inv_w0[2]));
-                        for (uint32_t q = 0; q < nvar; ++q) {
-                            float num = fmul(fmul(rv[q], cmp[0]), r.inv_w0[0]);
-                            num = fadd(num, fmul(fmul(rv[nvar + q], cmp[1]), r.inv_w0[1]));
-                            num = fadd(num, fmul(fmul(rv[2 * nvar + q], cmp[2]), r.inv_w0[2]));
-                            var[q] = fdiv(num, den);
+                    for (int rr = 0; rr < 4; ++rr) {
+                        const int2 sp = s_span[ri * T + band * 4 + rr];
+                        if (sp.x <= sp.y) {
+                            mn = min(mn, sp.x - tx * T);
+                            mx = max(mx, sp.y - tx * T);
                         }
-                    } else {
-                        for (uint32_t q = 0; q < nvar; ++q)
-                            var[q] = fadd(fadd(fmul(rv[q], cmp[0]), fmul(rv[nvar + q], cmp[1])),
-                                          fmul(rv[2 * nvar + q], cmp[2]));
                     }
-                    V4 col;
-                    if (!run_fs(d, var, col)) continue;  // discard: no depth test, no write
-                    // late depth test at the first colour output (fragment.rs:427-453, 470-479)
-                    if (d.depth_test) {
-                        if (!depth_compare(d.depth_compare, z, px[k].depth)) continue;
-                        if (d.depth_write) px[k].depth = z;
+                    if (mn <= mx)
+                        for (int bx = mn >> 3; bx <= (mx >> 3); ++bx) bits |= 1u << (band * BLK_X + bx);
+                }
+                s_mask[ri] = bits;
+            }
+            __syncthreads();
+            // the warp's 8x4 blocks, as bits of the record masks
+            uint32_t wbits = 0;
+#pragma unroll
+            for (int k = 0; k < PPT; ++k)
+                if (warp + k * WARPS < NBLK) wbits |= 1u << (warp + k * WARPS);
+            for (uint32_t c0 = 0; c0 < nb; c0 += 32) {
+                uint32_t todo = __ballot_sync(0xFFFFFFFFu, c0 + lane < nb && (s_mask[c0 + lane] & wbits));
+                while (todo) {
+                    const uint32_t ri = c0 + __ffs(todo) - 1;
+                    todo &= todo - 1;
+                    const TriRecord& r = *reinterpret_cast<const TriRecord*>(s_recs + (size_t)ri * stride);
+                    RasterState& rs = s_rs[warp];
+                    if (rs.draw != r.draw) {  // warp-uniform
+                        __syncwarp();
+                        if (lane == 0) build_raster_state(bp.draws[r.draw], r.draw, rs);
+                        __syncwarp();
                     }
-                    if (!tg.color) continue;
-                    if (d.blend_enabled) {
-                        const V4 dst = decode_color(tg.color_format, px[k].c);
-                        V4 o;
-                        o.x = blend_channel(d.blend_color, col.x, col.w, dst.x, dst.w, d.blend_constant[0]);
-                        o.y = blend_channel(d.blend_color, col.y, col.w, dst.y, dst.w, d.blend_constant[1]);
-                        o.z = blend_channel(d.blend_color, col.z, col.w, dst.z, dst.w, d.blend_constant[2]);
-                        o.w = blend_channel(d.blend_alpha, col.w, col.w, dst.w, dst.w, d.blend_constant[3]);
-                        col = o;
+                    // per-record constants, held in registers across this lane's pixels
+                    const uint32_t rmask = s_mask[ri];
+                    const float ax = r.vpx[0], ay = r.vpy[0], bx = r.vpx[1], by = r.vpy[1], cx = r.vpx[2], cy = r.vpy[2];
+                    const float kc0 = s_kc[ri][0], kc1 = s_kc[ri][1], kc2 = s_kc[ri][2], rcp = s_kc[ri][3];
+                    const float area = r.area;
+                    const bool area_ok = div_fast_ok(area);
+                    const bool ident = (r.flags & 16u) != 0;
+                    const float* rv = rec_var(&r);
+                    constexpr uint32_t KNV = KIND == 1 ? 4 : KIND == 2 ? 5 : 0;
+                    float rvv[3 * (KNV ? KNV : 1)];
+                    if constexpr (KNV != 0) {
+#pragma unroll
+                        for (uint32_t q = 0; q < 3 * KNV; ++q) rvv[q] = rv[q];
                     }
-                    if (d.write_mask != 0xF) {
-                        const V4 dst = decode_color(tg.color_format, px[k].c);
-                        if (!(d.write_mask & 1)) col.x = dst.x;
-                        if (!(d.write_mask & 2)) col.y = dst.y;
-                        if (!(d.write_mask & 4)) col.z = dst.z;
-                        if (!(d.write_mask & 8)) col.w = dst.w;
+#pragma unroll
+                    for (int k = 0; k < PPT; ++k) {
+                        const int blk = warp + k * WARPS;
+                        if (blk >= NBLK || !((rmask >> blk) & 1u)) continue;  // warp-uniform
+                        const int x = pxx[k], y = pxy[k];
+                        {
+                            // coverage: the row's span (already cut to scissor and tile)
+                            const int2 sp = s_span[ri * T + (y - ty * T)];
+                            if (!pvalid[k] || x < sp.x || x > sp.y) continue;
+                        }
+                        // barycentrics at the integer pixel corner (raster.rs:313-321, 334-335)
+                        const float fx = (float)x, fy = (float)y;
+                        const float s0 = fadd(fadd(fmul(fsub(by, fy), fadd(bx, fx)), kc0), fmul(fsub(fy, cy), fadd(fx, cx)));
+                        const float s1 = fadd(fadd(fmul(fsub(fy, ay), fadd(fx, ax)), fmul(fsub(cy, fy), fadd(cx, fx))), kc1);
+                        const float s2 = fadd(fadd(kc2, fmul(fsub(fy, by), fadd(fx, bx))), fmul(fsub(ay, fy), fadd(ax, fx)));
+                        const float l0 = div_by_recip(s0, area, rcp, area_ok);
+                        const float l1 = div_by_recip(s1, area, rcp, area_ok);
+                        const float l2 = div_by_recip(s2, area, rcp, area_ok);
+                        // composed with the clip barycentrics (raster.rs:338-343).  For an unclipped
+                        // record the composition is ((1*l0 + 0*l1) + 0*l2, ...), which equals
+                        // (l0, l1, l2) exactly when every l is finite and non-zero — guaranteed when
+                        // all three quotients took div_by_recip's in-range path.
+                        float cmp[3];
+                        if (ident && area_ok && div_fast_ok(s0) && div_fast_ok(s1) && div_fast_ok(s2)) {
+                            cmp[0] = l0;
+                            cmp[1] = l1;
+                            cmp[2] = l2;
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 3; ++j)
+                                cmp[j] = fadd(fadd(fmul(r.cb[j], l0), fmul(r.cb[3 + j], l1)), fmul(r.cb[6 + j], l2));
+                        }
+                        ++frag_count;
+                        // inter-stage values (fragment.rs:319-378) and the fragment stage
+                        V4 col;
+                        if constexpr (KIND == 1) {
+                            // linear vec4f colour straight to the output (quad_color / clip_passthrough)
+                            float v[4];
+#pragma unroll
+                            for (int q = 0; q < 4; ++q)
+                                v[q] = fadd(fadd(fmul(rvv[q], cmp[0]), fmul(rvv[4 + q], cmp[1])), fmul(rvv[8 + q], cmp[2]));
+                            col = V4{v[0], v[1], v[2], v[3]};
+                        } else if constexpr (KIND == 2) {
+                            float v[5];
+#pragma unroll
+                            for (int q = 0; q < 5; ++q)
+                                v[q] = fadd(fadd(fmul(rvv[q], cmp[0]), fmul(rvv[5 + q], cmp[1])), fmul(rvv[10 + q], cmp[2]));
+                            run_fs_rs(rs, v, s_lut, col);
+                        } else {
+                            const uint32_t nvar = rs.nvar;
+                            float var[MAX_VARYING_FLOATS];
+                            if (rs.interp == INTERP_PERSPECTIVE) {
+                                const float den = fadd(fadd(fmul(cmp[0], r.inv_w0[0]), fmul(cmp[1], r.inv_w0[1])),
+                                                       fmul(cmp[2], r.inv_w0[2]));
+#pragma unroll
+                                for (uint32_t qv = 0; qv < MAX_VARYING_FLOATS; ++qv) {
+                                    if (qv >= nvar) break;
+                                    float num = fmul(fmul(rv[qv], cmp[0]), r.inv_w0[0]);
+                                    num = fadd(num, fmul(fmul(rv[nvar + qv], cmp[1]), r.inv_w0[1]));
+                                    num = fadd(num, fmul(fmul(rv[2 * nvar + qv], cmp[2]), r.inv_w0[2]));
+                                    var[qv] = fdiv(num, den);
+                                }
+                            } else {
+#pragma unroll
+                                for (uint32_t qv = 0; qv < MAX_VARYING_FLOATS; ++qv) {
+                                    if (qv >= nvar) break;
+                                    var[qv] = fadd(fadd(fmul(rv[qv], cmp[0]), fmul(rv[nvar + qv], cmp[1])),
+                                                   fmul(rv[2 * nvar + qv], cmp[2]));
+                                }
+                            }
+                            if (!run_fs_rs(rs, var, s_lut, col)) continue;  // discard: no depth test, no write
+                        }
+                        // late depth test at the first colour output (fragment.rs:427-453, 470-479)
+                        if (KIND == 2 || (KIND == 0 && rs.depth_test)) {
+                            // fragment.z (raster.rs:345-346); only the depth test reads it here
+                            const float z =
+                                fadd(fadd(fmul(r.fz[0], cmp[0]), fmul(r.fz[1], cmp[1])), fmul(r.fz[2], cmp[2]));
+                            if (!depth_compare(rs.depth_compare, z, px[k].depth)) continue;
+                            if (rs.depth_write) px[k].depth = z;
+                        }
+                        if constexpr (KIND == 1) {
+                            // Rgba16Float, colour SrcAlpha/OneMinusSrcAlpha/Add, alpha One/OneMinusSrcAlpha/Add
+                            const V4 dst = decode_color(7, px[k].c);
+                            const float oma = fsub(1.0f, col.w);
+                            col = V4{fadd(fmul(col.x, col.w), fmul(dst.x, oma)), fadd(fmul(col.y, col.w), fmul(dst.y, oma)),
+                                     fadd(fmul(col.z, col.w), fmul(dst.z, oma)), fadd(fmul(col.w, 1.0f), fmul(dst.w, oma))};
+                            encode_color(7, col, px[k].c);
+                        } else if constexpr (KIND == 2) {
+                            encode_color(3, col, px[k].c);  // Rgba8Unorm / Rgba8UnormSrgb: same bytes here
+                        } else {
+                            if (!tg.color) continue;
+                            if (rs.blend_enabled && rs.blend_over) {
+                                // the generic formula below with its factors resolved: s*sa + d*(1-sa), alpha s*1 + d*(1-sa)
+                                const V4 dst = decode_color(tg.color_format, px[k].c);
+                                const float oma = fsub(1.0f, col.w);
+                                col = V4{fadd(fmul(col.x, col.w), fmul(dst.x, oma)), fadd(fmul(col.y, col.w), fmul(dst.y, oma)),
+                                         fadd(fmul(col.z, col.w), fmul(dst.z, oma)), fadd(fmul(col.w, 1.0f), fmul(dst.w, oma))};
+                            } else if (rs.blend_enabled) {
+                                const V4 dst = decode_color(tg.color_format, px[k].c);
+                                V4 o;
+                                o.x = blend_channel(rs.blend_color, col.x, col.w, dst.x, dst.w, rs.blend_constant[0]);
+                                o.y = blend_channel(rs.blend_color, col.y, col.w, dst.y, dst.w, rs.blend_constant[1]);
+                                o.z = blend_channel(rs.blend_color, col.z, col.w, dst.z, dst.w, rs.blend_constant[2]);
+                                o.w = blend_channel(rs.blend_alpha, col.w, col.w, dst.w, dst.w, rs.blend_constant[3]);
+                                col = o;
+                            }
+                            if (rs.write_mask != 0xF) {
+                                const V4 dst = decode_color(tg.color_format, px[k].c);
+                                if (!(rs.write_mask & 1)) col.x = dst.x;
+                                if (!(rs.write_mask & 2)) col.y = dst.y;
+                                if (!(rs.write_mask & 4)) col.z = dst.z;
+                                if (!(rs.write_mask & 8)) col.w = dst.w;
+                            }
+                            encode_color(tg.color_format, col, px[k].c);
+                        }
                     }
-                    encode_color(tg.color_format, col, px[k].c);
                 }
             }
             __syncthreads();
@@ -821,7 +1079,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
             }
             if (tg.depth) tg.depth[pix] = px[k].depth;
         }
-        // fragment count
         for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
         if (lane == 0 && frag_count) atomicAdd(&s_frag, (unsigned long long)frag_count);
         __syncthreads();

@@ -303,6 +303,28 @@ struct Batch {
     uint32_t total_prims = 0, total_tiles = 0, nvar = 0;
 };
 
+// Which specialised raster kernel can run a batch (kernels.h): 1 = a vec4f colour passed straight
+// to an Rgba16Float target with SrcAlpha/OneMinusSrcAlpha (alpha One/OneMinusSrcAlpha) blending and
+// no depth test; 2 = the textured Lambert program into Rgba8 with a depth test, no blending, parity
+// profile.  Every draw of the batch must qualify; otherwise 0, the generic kernel.
+int fragment_kind(const Batch& b) {
+    if (b.draws.empty() || b.targets.size() != 1 || !b.targets[0].color) return 0;
+    const uint32_t fmt = b.targets[0].color_format;
+    bool k1 = fmt == GBR_TEXTURE_FORMAT_RGBA16_FLOAT, k2 = fmt == GBR_TEXTURE_FORMAT_RGBA8_UNORM ||
+                                                          fmt == GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB;
+    for (const DrawDesc& d : b.draws) {
+        const bool over = d.blend_enabled && d.blend_color[0] == GBR_BLEND_SRC_ALPHA &&
+                          d.blend_color[1] == GBR_BLEND_ONE_MINUS_SRC_ALPHA && d.blend_color[2] == GBR_BLEND_OP_ADD &&
+                          d.blend_alpha[0] == GBR_BLEND_ONE && d.blend_alpha[1] == GBR_BLEND_ONE_MINUS_SRC_ALPHA &&
+                          d.blend_alpha[2] == GBR_BLEND_OP_ADD;
+        k1 = k1 && over && d.write_mask == 0xF && !d.depth_test && d.has_fragment &&
+             (d.program == PROG_QUAD_COLOR || d.program == PROG_CLIP_PASSTHROUGH || d.program == PROG_COLORED_TRIANGLE);
+        k2 = k2 && !d.blend_enabled && d.write_mask == 0xF && d.depth_test && d.has_fragment &&
+             d.program == PROG_MESH_TEX_LAMBERT && d.profile == GBR_PROFILE_PARITY;
+    }
+    return k1 ? 1 : k2 ? 2 : 0;
+}
+
 uint32_t ilog2(uint32_t v) {
     uint32_t r = 0;
     while ((1u << r) < v) ++r;
@@ -698,7 +720,8 @@ void Device::execute_submission(Item& it, SubmissionRecord& rec) {
             bp.work_counter = reinterpret_cast<uint32_t*>(meta + off_work) + i * 4;
             bp.status = reinterpret_cast<BatchStatus*>(meta + off_status) + i;
             bp.abort_flag = reinterpret_cast<uint32_t*>(meta);
-            cuda_check(launch_batch(bp, tile, warps, num_sms, stream, &launches, rev.empty() ? nullptr : &rev[2 * i]),
+            cuda_check(launch_batch(bp, tile, warps, num_sms, stream, &launches, rev.empty() ? nullptr : &rev[2 * i],
+                                    fragment_kind(b)),
                        "launch");
         }
         cuda_check(cudaEventRecord(ev1, stream), "event");

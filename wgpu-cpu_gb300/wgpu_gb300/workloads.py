@@ -171,6 +171,7 @@ class Scene:
     color: W.Texture
     depth: Optional[W.Texture]
     draws: list = field(default_factory=list)  # (pipeline, bind_groups, vbufs, ibuf, index_range)
+    uploads: list = field(default_factory=list)  # (buffer or texture, host array) inputs of the pass
     clear_color: tuple = (0.0, 0.0, 0.0, 1.0)
     depth_clear: float = 1.0
     triangles: int = 0
@@ -227,6 +228,7 @@ def scene_colored_sphere(dev: W.Device, width: int = 512, height: int = 512, see
     s = Scene(dev, color, None, clear_color=(0.0, 0.0, 0.0, 1.0), triangles=len(idx), label="colored_sphere")
     s.draws.append((pl, [bg], [vb], ib, range(0, idx.size), 0))
     s._keep = [vb, ib, ub, sm, bg]
+    s.uploads = [(vb, vdata), (ib, idx.ravel()), (ub, np.frombuffer(mvp_bytes(camera_mvp(width, height)), np.uint8))]
     return s
 
 
@@ -266,6 +268,7 @@ def scene_textured_icosphere(dev: W.Device, width: int = 1920, height: int = 108
     s = Scene(dev, color, depth, clear_color=(0.0, 0.0, 0.0, 1.0), triangles=len(f), label="textured_icosphere")
     s.draws.append((pl, [g0, g1], [vb], ib, range(0, f.size), 0))
     s._keep = [vb, ib, ub, tex, samp, sm, g0, g1]
+    s.uploads = [(vb, vdata), (ib, f.ravel()), (ub, np.frombuffer(ubytes, np.uint8)), (tex, img)]
     return s
 
 
@@ -312,6 +315,7 @@ def scene_blended_quads(dev: W.Device, width: int = 3840, height: int = 2160, n_
     s = Scene(dev, color, None, clear_color=(0.0, 0.0, 0.0, 0.0), triangles=n_quads * 2, label="blended_quads")
     s.draws.append((pl, [], [vb_pos, vb_col], ib, range(0, idx.size), 0))
     s._keep = [vb_pos, vb_col, ib, sm]
+    s.uploads = [(vb_pos, pos), (vb_col, col), (ib, idx)]
     return s
 
 
