@@ -16,6 +16,11 @@ Workloads (seeded synthetic inputs with the configurations' shapes; no dataset e
                       nor f16 targets).  The fill-rate-bound configuration.
   colored             UV sphere 32x16 (992 triangles), per-vertex colours, back-face cull,
                       512x512 Rgba8Unorm (the reference's CPU-runnable configuration).
+  batched             256 draws into 64 render targets (sides log-uniform in [128, 2048], triangle
+                      counts log-uniform in [100, 200k], random model rotations, half textured x
+                      Lambert and half vertex-colour programs), Rgba8Unorm + Depth32Float (Less),
+                      one command buffer.  Besides the batched launch sequence the line reports
+                      the same command buffer launched per draw, the plain path it replaces.
 
 `value` is shaded fragments per second (fragment-shader invocations, counted as the reference
 counts them) with every input resident in HBM, over the device time of the K steps (CUDA events on
@@ -60,8 +65,8 @@ class Workload:
 
         return getattr(wl, self.builder)(dev, **{**self.kwargs, **over})
 
-    def config(self, flush=True):
-        return {"workload": self.description, **self.extra_cfg, "launch_mode": "per_pass",
+    def config(self, flush=True, launch_mode="batched", graphs=False):
+        return {"workload": self.description, **self.extra_cfg, "launch_mode": launch_mode, "cuda_graphs": graphs,
                 "l2": "flushed between timed steps (256 MiB write)" if flush else "n/a (CPU)"}
 
 
@@ -88,7 +93,33 @@ def workloads():
             4, 512 * 512 * 4,
             "colored UV sphere: 992 tris, 512x512 Rgba8Unorm, back-face cull, no depth",
             {"triangles": 992, "target": "512x512", "profile": "parity", "seed": 1}),
+        "batched": Workload(
+            "batched", W.Profile.PARITY, "scene_batched", dict(n_targets=64, n_draws=256, seed=3),
+            4 + 4 + 4 + 4, None,
+            "batched draws: 256 draws into 64 targets (sides log-uniform [128,2048], tris log-uniform [100,200k]), "
+            "Rgba8Unorm + Depth32Float Less, half texture x Lambert / half vertex colour, one command buffer",
+            {"draws": 256, "targets": 64, "profile": "parity", "seed": 3},
+            cpu_kwargs=dict(n_targets=16, n_draws=64, seed=3)),
     }
+
+
+def pixel_bytes(wk: Workload, scene) -> int:
+    """Target bytes written per step: colour plus depth of every target."""
+    from wgpu_gb300 import api as W
+
+    if wk.pixel_bytes is not None:
+        return wk.pixel_bytes
+    total = 0
+    for color, depth, _ in scene.passes:
+        total += color.width * color.height * (W.BYTES_PER_TEXEL[color.format] + (4 if depth is not None else 0))
+    return total
+
+
+def color_targets(scene):
+    return [p[0] for p in scene.passes] if hasattr(scene, "passes") else [scene.color]
+
+
+LAUNCH_MODES = {"batched": 0, "per_pass": 2, "per_draw": 1}
 
 
 def dist_env():
@@ -210,7 +241,7 @@ def run_ours(args, wk: Workload):
         torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
     dev = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True, tile_size=args.tile,
-                   warps_per_tile=args.warps)
+                   warps_per_tile=args.warps, launch_mode=LAUNCH_MODES[args.launch_mode], use_graphs=args.graphs)
     over = {"n_quads": args.quads} if args.quads and wk.name == "blend" else {}
     scene = wk.build(dev, **over)
     enc = dev.create_command_encoder()
@@ -228,17 +259,39 @@ def run_ours(args, wk: Workload):
             torch.distributed.barrier()
         torch.cuda.synchronize()
 
+    def timed_steps(d, c, steps):
+        subs = []
+        for _ in range(steps):
+            d.flush_caches()
+            subs.append(d.queue.submit([c]))
+        d.poll(True, subs[-1])
+        return [d.submission_stats(i) for i in subs]
+
     barrier()
     with ClockSampler(local) as clocks:
         t0 = time.perf_counter()
-        subs = []
-        for _ in range(args.steps):
-            dev.flush_caches()
-            subs.append(dev.queue.submit([cmd]))
-        dev.poll(True, subs[-1])
+        stats = timed_steps(dev, cmd, args.steps)
         wall = time.perf_counter() - t0
     barrier()
-    stats = [dev.submission_stats(i) for i in subs]
+
+    # the same command buffer on the plain per-draw path (one launch sequence per draw)
+    per_draw = None
+    if wk.name == "batched" and args.launch_mode != "per_draw":
+        d2 = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True, tile_size=dev_tile(args),
+                      warps_per_tile=dev_warps(args), launch_mode=W.LaunchMode.PER_DRAW)
+        scene2 = wk.build(d2)
+        enc2 = d2.create_command_encoder()
+        scene2.record(enc2)
+        cmd2 = enc2.finish()
+        timed_steps(d2, cmd2, 3)
+        st2 = timed_steps(d2, cmd2, max(3, min(args.steps, 10)))
+        ms2 = float(np.mean([s.gpu_ms for s in st2]))
+        if st2[-1].fragments_shaded != frags_per_step:
+            raise RuntimeError("per-draw launches shaded a different number of fragments")
+        per_draw = {"value": st2[-1].fragments_shaded / (ms2 / 1e3), "unit": UNIT, "ms_per_step": ms2,
+                    "gpu_launches_per_step": int(st2[-1].kernel_launches)}
+        del scene2, cmd2
+        d2.close()
     gpu_ms = [s.gpu_ms for s in stats]
     raster_ms = [s.raster_ms for s in stats]
     device_s = sum(gpu_ms) / 1e3
@@ -250,16 +303,19 @@ def run_ours(args, wk: Workload):
     launches = int(sum(s.kernel_launches for s in stats))
 
     # roofline of the dominant kernel: algorithmic bytes per launch / its event-timed duration
-    alg_bytes = wk.pixel_bytes + frags_per_step * wk.bytes_per_fragment
+    alg_bytes = pixel_bytes(wk, scene) + frags_per_step * wk.bytes_per_fragment
     peak, peak_src = measured_peak_hbm()
     r_ms = float(np.mean(raster_ms))
-    achieved = alg_bytes / (r_ms / 1e3) / 1e9
+    achieved = alg_bytes / (r_ms / 1e3) / 1e9 if r_ms > 0 else None
 
     # end to end through the C ABI: inputs from pinned host memory, colour target read back
-    pinned = [(obj, torch.from_numpy(np.ascontiguousarray(arr).reshape(-1).view(np.uint8)).pin_memory())
+    pinned = [(obj, torch.from_numpy(np.array(arr).reshape(-1).view(np.uint8)).pin_memory())
               for obj, arr in scene.uploads]
-    out_bytes = scene.color.width * scene.color.height * W.BYTES_PER_TEXEL[scene.color.format]
-    out = torch.empty(out_bytes, dtype=torch.uint8).pin_memory()
+    reads = []
+    for t in color_targets(scene):
+        n = t.width * t.height * W.BYTES_PER_TEXEL[t.format]
+        reads.append((t, torch.empty(n, dtype=torch.uint8).pin_memory()))
+    out_bytes = sum(o.numel() for _, o in reads)
 
     def e2e_step():
         for obj, host in pinned:
@@ -269,9 +325,10 @@ def run_ours(args, wk: Workload):
                 dev.queue.write_buffer(obj, 0, host.numpy())
         i = dev.queue.submit([cmd])
         dev.poll(True, i)
-        st = dev.lib.texture_read(dev.handle, scene.color.handle, 0, out.data_ptr(), out.numel())
-        if st != 0:
-            raise W.GbrError(st, dev.lib.error_text())
+        for t, o in reads:
+            st = dev.lib.texture_read(dev.handle, t.handle, 0, o.data_ptr(), o.numel())
+            if st != 0:
+                raise W.GbrError(st, dev.lib.error_text())
 
     for _ in range(max(1, min(args.warmup, 3))):
         e2e_step()
@@ -288,11 +345,13 @@ def run_ours(args, wk: Workload):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": float(np.mean(gpu_ms)), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": wk.dtype, "data": "synthetic (seeded)",
-            "config": {**wk.config(), "tile": dev_tile(args), "warps_per_tile": dev_warps(args),
+            "config": {**wk.config(launch_mode=args.launch_mode, graphs=args.graphs),
+                       "tile": dev_tile(args) if not args.autotune else "autotuned",
+                       "warps_per_tile": dev_warps(args) if not args.autotune else "autotuned",
                        **({"n_quads": args.quads} if over else {})},
             "fragments_per_step": frags_per_step, "wall_ms_per_step": wall * 1e3 / args.steps,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": raster_traffic(wk.name) if not over else None,
+                         "frac": achieved / peak if achieved else None, "traffic": raster_traffic(wk.name) if not over else None,
                          "peak_source": peak_src, "kernel": "k_raster (tile sort + raster + shade + depth/blend + ROP)",
                          "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": r_ms},
             "cpu_baseline": base,
@@ -301,6 +360,8 @@ def run_ours(args, wk: Workload):
             "gpu_launches": launches,
             "clocks": clocks.summary(),
         }
+        if per_draw is not None:
+            line["per_draw_path"] = per_draw
         print(json.dumps(line), flush=True)
     dev.close()
     if world > 1:
@@ -321,13 +382,20 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="textured", choices=["textured", "blend", "colored"])
+    ap.add_argument("--workload", default="textured", choices=["textured", "blend", "colored", "batched"])
+    ap.add_argument("--launch-mode", default="batched", choices=list(LAUNCH_MODES))
+    ap.add_argument("--graphs", action="store_true", help="replay each submission's launches from a CUDA graph")
+    ap.add_argument("--autotune", action="store_true", help="let the device time tile shapes (tile/warps ignored)")
     ap.add_argument("--quads", type=int, default=0, help="blend workload: number of quads (profiling runs)")
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--warps", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.autotune:
+        args.tile = args.warps = 0
+    elif not args.tile:
+        args.tile, args.warps = dev_tile(args), dev_warps(args)
     wk = workloads()[args.workload]
     if args.impl == "reference":
         run_reference(args, wk)

@@ -168,9 +168,12 @@ typedef struct gbr_device_config {
 } gbr_device_config;
 
 /* How draws map to kernel launches.
- *  PER_PASS — all draws of a render pass go through one setup/bin/raster launch sequence.
- *  PER_DRAW — the plain drop-in: one launch sequence per draw, each over the whole target. */
-enum gbr_launch_mode { GBR_LAUNCH_PER_PASS = 0, GBR_LAUNCH_PER_DRAW = 1 };
+ *  BATCHED  — consecutive render passes without dependencies between them (no pass writes or
+ *             samples a texture another pass of the group writes) share one setup/bin/raster
+ *             launch sequence over all their targets and draws.  The default.
+ *  PER_DRAW — the plain drop-in: one launch sequence per draw, each over the whole target.
+ *  PER_PASS — one launch sequence per render pass. */
+enum gbr_launch_mode { GBR_LAUNCH_BATCHED = 0, GBR_LAUNCH_PER_DRAW = 1, GBR_LAUNCH_PER_PASS = 2 };
 
 typedef struct gbr_limits {
     uint32_t max_texture_dimension_2d;

@@ -106,7 +106,7 @@ cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         ++*launches;
     }
-    if (ev_raster && (e = cudaEventRecord(ev_raster[0], s)) != cudaSuccess) return e;
+    if (ev_raster && (e = cudaEventRecordWithFlags(ev_raster[0], s, cudaEventRecordExternal)) != cudaSuccess) return e;
     for (;;) {
     switch ((tile * 16 + warps) * 4 + (kind & 3)) {
         case (8 * 16 + 1) * 4: e = launch_raster<8, 1>(bp, num_sms, s); break;
@@ -131,7 +131,7 @@ cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms
     }
     if (e != cudaSuccess) return e;
     ++*launches;
-    if (ev_raster) e = cudaEventRecord(ev_raster[1], s);
+    if (ev_raster) e = cudaEventRecordWithFlags(ev_raster[1], s, cudaEventRecordExternal);
     return e;
 }
 

@@ -196,6 +196,7 @@ struct Item {
     uint64_t size = 0;
     std::promise<Failure>* done = nullptr;  // reads: completion for the blocked caller
     Clock::time_point t_submit;
+    uint32_t merged = 0;  // submissions executed together with this one (serving mode)
 };
 
 struct SubmissionRecord {
@@ -227,6 +228,8 @@ struct DevBuf {
     }
 };
 
+struct Batch;
+
 struct Device {
     gbr_device_config cfg{};
     int ordinal = 0;
@@ -254,6 +257,30 @@ struct Device {
     DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf;
     uint32_t ovf_capacity = 4096;
     uint64_t bin_capacity = 1u << 22;
+
+    // autotuner: per batch signature, each candidate tile shape is timed once, then the fastest
+    // is kept (all shapes give bit-identical results, only the time differs)
+    bool autotune = false;
+    struct TuneEntry {
+        int tried = 0, best = 0;
+        float ms[8] = {};
+    };
+    std::map<uint64_t, TuneEntry> tuner;
+    uint64_t tuner_signature(const Batch& b) const;
+    int tuner_pick(const Batch& b, int* t, int* w);
+    void tuner_record(const Batch& b, int cand, float ms);
+
+    // CUDA graphs of whole launch sequences, keyed by their launch parameters
+    struct GraphEntry {
+        cudaGraphExec_t exec = nullptr;
+        std::vector<cudaEvent_t> events;
+        uint64_t last_use = 0;
+    };
+    std::map<std::string, GraphEntry> graphs;
+    uint64_t graph_clock = 0;
+
+    std::vector<Batch> plan_batches(const std::vector<PassCmd>& passes, uint64_t* draws, uint64_t* prims_in);
+    void launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec);
 
     template <class T>
     std::shared_ptr<T> get(uint64_t h, const char* what) {
@@ -323,6 +350,50 @@ int fragment_kind(const Batch& b) {
              d.program == PROG_MESH_TEX_LAMBERT && d.profile == GBR_PROFILE_PARITY;
     }
     return k1 ? 1 : k2 ? 2 : 0;
+}
+
+// Tile shapes the autotuner tries (all compiled into kernels.cu).
+const int kTuneCands[][2] = {{16, 8}, {32, 8}, {8, 2}};
+constexpr int kNumTuneCands = 3;
+
+uint64_t log2_bucket(uint64_t v) {
+    uint64_t r = 0;
+    while (v > 1) {
+        v >>= 1;
+        ++r;
+    }
+    return r;
+}
+
+// Batches with the same fragment kernel, order of magnitude of primitives, of pixels and of
+// targets share a tuning decision.
+uint64_t Device::tuner_signature(const Batch& b) const {
+    uint64_t pixels = 0;
+    for (const TargetDesc& t : b.targets) pixels += (uint64_t)t.width * t.height;
+    return ((uint64_t)fragment_kind(b) << 48) | (log2_bucket(b.total_prims + 1) << 32) |
+           (log2_bucket(pixels + 1) << 16) | log2_bucket(b.targets.size());
+}
+int Device::tuner_pick(const Batch& b, int* t, int* w) {
+    TuneEntry& e = tuner[tuner_signature(b)];
+    if (e.tried < kNumTuneCands) {
+        *t = kTuneCands[e.tried][0];
+        *w = kTuneCands[e.tried][1];
+        return e.tried;
+    }
+    *t = kTuneCands[e.best][0];
+    *w = kTuneCands[e.best][1];
+    return -1;
+}
+void Device::tuner_record(const Batch& b, int cand, float ms) {
+    TuneEntry& e = tuner[tuner_signature(b)];
+    if (cand != e.tried || cand >= kNumTuneCands) return;  // a second batch of the same signature
+    e.ms[cand] = ms;
+    e.tried = cand + 1;
+    if (e.tried == kNumTuneCands) {
+        e.best = 0;
+        for (int c = 1; c < kNumTuneCands; ++c)
+            if (e.ms[c] < e.ms[e.best]) e.best = c;
+    }
 }
 
 uint32_t ilog2(uint32_t v) {
@@ -578,62 +649,120 @@ void Device::execute(Item& it) {
 void Device::execute_submission(Item& it, SubmissionRecord& rec) {
     const auto t_start = Clock::now();
     rec.stats.queue_wait_ms = ms_between(it.t_submit, t_start);
-    const uint32_t profile = cfg.profile;
-    const bool per_draw = cfg.launch_mode == GBR_LAUNCH_PER_DRAW;  // the plain one-launch-per-draw path
-    // plan batches
-    std::vector<Batch> batches;
     uint64_t draws = 0, prims_in = 0;
-    for (const PassCmd& p : it.passes) {
+    std::vector<Batch> batches = plan_batches(it.passes, &draws, &prims_in);
+    rec.stats.draws = draws;
+    rec.stats.primitives_in = prims_in;
+    rec.stats.batched_with = it.merged ? it.merged : 1;
+    if (batches.empty()) return;
+    launch_batches(batches, rec);
+}
+
+// Splits a list of render passes into launch batches.
+//  PER_DRAW  one batch per draw (the pass's load ops apply to its first draw);
+//  PER_PASS  one batch per pass;
+//  BATCHED   consecutive passes share a batch until one would touch a texture an earlier pass of
+//            the batch writes (as an attachment) or reads (as a bound texture), or write one it
+//            reads — so no batch contains a dependency between its passes.
+std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint64_t* draws, uint64_t* prims_in) {
+    const uint32_t profile = cfg.profile;
+    std::vector<Batch> batches;
+    std::vector<const Texture*> written, read;
+    bool open = false;
+    auto close = [&] {
+        open = false;
+        written.clear();
+        read.clear();
+    };
+    auto has = [](const std::vector<const Texture*>& v, const Texture* t) {
+        return t && std::find(v.begin(), v.end(), t) != v.end();
+    };
+    for (const PassCmd& p : passes) {
         if (p.width == 0 || p.height == 0) continue;
-        if (p.draws.empty() || !per_draw) {
-            Batch b;
-            b.targets.push_back(make_target(p, true, tile, profile));
-            for (const DrawCmd& dc : p.draws) {
-                ++draws;
-                DrawDesc d = make_draw(dc, profile, (bool)p.depth);
-                d.prim_base = b.total_prims;
-                d.target = 0;
-                uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
-                prims_in += np;
-                if ((uint64_t)b.total_prims + np >= (1ull << (32 - SUBTRI_BITS)))
-                    fail(GBR_ERR_UNSUPPORTED, "too many primitives in one pass");
-                b.total_prims += (uint32_t)np;
-                b.nvar = std::max(b.nvar, d.num_varyings);
-                if (np) b.draws.push_back(d);
-            }
-            batches.push_back(std::move(b));
-        } else {
+        std::vector<const Texture*> p_write = {p.color.get(), p.depth.get()};
+        std::vector<const Texture*> p_read;
+        for (const DrawCmd& dc : p.draws)
+            for (const auto& g : dc.groups)
+                if (g)
+                    for (const auto& ref : g->refs)
+                        if (auto* t = dynamic_cast<const Texture*>(ref.get())) p_read.push_back(t);
+        uint64_t p_prims = 0;
+        for (const DrawCmd& dc : p.draws) {
+            const auto& ps = dc.pipeline->desc.primitive;
+            uint32_t cnt = dc.end > dc.start ? dc.end - dc.start : 0;
+            uint32_t ppi = ps.topology == GBR_TOPOLOGY_TRIANGLE_STRIP ? (cnt >= 3 ? cnt - 2 : 0) : cnt / 3;
+            p_prims += (uint64_t)ppi * (dc.inst_end > dc.inst_start ? dc.inst_end - dc.inst_start : 0);
+        }
+        const uint64_t kMaxPrims = (1ull << (32 - SUBTRI_BITS)) - 1;
+        if (cfg.launch_mode == GBR_LAUNCH_PER_DRAW && !p.draws.empty()) {
+            close();
             bool first = true;
             for (const DrawCmd& dc : p.draws) {
-                ++draws;
+                ++*draws;
                 Batch b;
                 b.targets.push_back(make_target(p, first, tile, profile));
                 first = false;
                 DrawDesc d = make_draw(dc, profile, (bool)p.depth);
-                d.prim_base = 0;
-                d.target = 0;
                 uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
-                prims_in += np;
-                if (np >= (1ull << (32 - SUBTRI_BITS))) fail(GBR_ERR_UNSUPPORTED, "too many primitives in one draw");
+                *prims_in += np;
+                if (np > kMaxPrims) fail(GBR_ERR_UNSUPPORTED, "too many primitives in one draw");
                 b.total_prims = (uint32_t)np;
                 b.nvar = d.num_varyings;
                 if (np) b.draws.push_back(d);
                 batches.push_back(std::move(b));
             }
+            continue;
         }
+        bool conflict = !open || cfg.launch_mode == GBR_LAUNCH_PER_PASS;
+        for (const Texture* t : p_write) conflict = conflict || has(written, t) || has(read, t);
+        for (const Texture* t : p_read) conflict = conflict || has(written, t);
+        if (!conflict && (uint64_t)batches.back().total_prims + p_prims > kMaxPrims) conflict = true;
+        if (conflict) {
+            close();
+            batches.emplace_back();
+            open = true;
+        }
+        Batch& b = batches.back();
+        const uint32_t ti = (uint32_t)b.targets.size();
+        b.targets.push_back(make_target(p, true, tile, profile));
+        for (const DrawCmd& dc : p.draws) {
+            ++*draws;
+            DrawDesc d = make_draw(dc, profile, (bool)p.depth);
+            d.prim_base = b.total_prims;
+            d.target = ti;
+            uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
+            *prims_in += np;
+            if ((uint64_t)b.total_prims + np > kMaxPrims) fail(GBR_ERR_UNSUPPORTED, "too many primitives in one pass");
+            b.total_prims += (uint32_t)np;
+            b.nvar = std::max(b.nvar, d.num_varyings);
+            if (np) b.draws.push_back(d);
+        }
+        for (const Texture* t : p_write)
+            if (t) written.push_back(t);
+        for (const Texture* t : p_read) read.push_back(t);
     }
-    for (Batch& b : batches) {
+    return batches;
+}
+
+// Chooses each batch's tile shape (fixed by the config, or by the autotuner), lays out its
+// tiles and launches all batches; re-runs from a batch that ran out of scratch space.
+void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) {
+    std::vector<int> btile(batches.size()), bwarps(batches.size()), tuning(batches.size(), -1);
+    for (size_t i = 0; i < batches.size(); ++i) {
+        Batch& b = batches[i];
+        int t = tile, w = warps;
+        if (autotune) tuning[i] = tuner_pick(b, &t, &w);
+        btile[i] = t;
+        bwarps[i] = w;
         uint32_t base = 0;
-        for (TargetDesc& t : b.targets) {
-            t.tile_base = base;
-            base += t.tiles_x * t.tiles_y;
+        for (TargetDesc& td : b.targets) {
+            td.tiles_x = (td.width + t - 1) / t;
+            td.tiles_y = (td.height + t - 1) / t;
+            td.tile_base = base;
+            base += td.tiles_x * td.tiles_y;
         }
         b.total_tiles = base;
     }
-    rec.stats.draws = draws;
-    rec.stats.primitives_in = prims_in;
-    rec.stats.batched_with = 1;
-    if (batches.empty()) return;
 
     // metadata layout: [abort flag][statuses][work counters][draw/target descriptors per batch]
     const size_t nb = batches.size();
@@ -673,7 +802,8 @@ void Device::execute_submission(Item& it, SubmissionRecord& rec) {
             for (cudaEvent_t e : *v) cudaEventDestroy(e);
         }
     } rev_guard{&rev};
-    if (cfg.time_kernels) {
+    const bool any_tuning = std::any_of(tuning.begin(), tuning.end(), [](int v) { return v >= 0; });
+    if (cfg.time_kernels || any_tuning) {
         rev.resize(2 * nb);
         for (auto& e : rev) cuda_check(cudaEventCreate(&e), "event");
     }
@@ -693,19 +823,25 @@ void Device::execute_submission(Item& it, SubmissionRecord& rec) {
         bins_buf.ensure((size_t)bin_capacity * sizeof(uint32_t), &scratch_bytes);
         if (scratch_bytes > budget) fail(GBR_ERR_OUT_OF_MEMORY, "transient memory exceeds the HBM budget");
         uint8_t* meta = static_cast<uint8_t*>(meta_buf.ptr);
-        cuda_check(cudaMemsetAsync(meta, 0, 4, stream), "abort flag");
         if (attempt == 0) cuda_check(cudaEventRecord(ev0, stream), "event");
+        // The launch sequence of the remaining batches; replayed from a CUDA graph when the
+        // config asks for graphs and the same parameters were launched before.
+        std::vector<BatchParams> params(nb);
+        std::vector<cudaEvent_t>* revp = &rev;
+        auto enqueue = [&]() {
+        cuda_check(cudaMemsetAsync(meta, 0, 4, stream), "abort flag");
         for (size_t i = first_batch; i < nb; ++i) {
             const Batch& b = batches[i];
-            BatchParams bp{};
+            BatchParams& bp = params[i];
+            bp = BatchParams{};
             bp.draws = reinterpret_cast<const DrawDesc*>(meta + desc_off[i]);
             bp.targets = reinterpret_cast<const TargetDesc*>(meta + desc_off[i] + b.draws.size() * sizeof(DrawDesc));
             bp.num_draws = (uint32_t)b.draws.size();
             bp.num_targets = (uint32_t)b.targets.size();
             bp.total_prims = b.total_prims;
             bp.total_tiles = b.total_tiles;
-            bp.tile_size = tile;
-            bp.tile_shift = ilog2(tile);
+            bp.tile_size = btile[i];
+            bp.tile_shift = ilog2(btile[i]);
             bp.record_stride = (uint32_t)((sizeof(TriRecord) + 3 * b.nvar * sizeof(float) + 15) & ~size_t(15));
             bp.num_varyings = b.nvar;
             bp.records = static_cast<uint8_t*>(records_buf.ptr);
@@ -720,9 +856,68 @@ void Device::execute_submission(Item& it, SubmissionRecord& rec) {
             bp.work_counter = reinterpret_cast<uint32_t*>(meta + off_work) + i * 4;
             bp.status = reinterpret_cast<BatchStatus*>(meta + off_status) + i;
             bp.abort_flag = reinterpret_cast<uint32_t*>(meta);
-            cuda_check(launch_batch(bp, tile, warps, num_sms, stream, &launches, rev.empty() ? nullptr : &rev[2 * i],
-                                    fragment_kind(b)),
+            cuda_check(launch_batch(bp, btile[i], bwarps[i], num_sms, stream, &launches,
+                                    revp->empty() ? nullptr : &(*revp)[2 * i], fragment_kind(b)),
                        "launch");
+        }
+        };
+        if (cfg.use_graphs && attempt == 0 && !any_tuning) {
+            // key: every launch parameter of the sequence (descriptors are re-uploaded each time)
+            std::string key;
+            for (size_t i = 0; i < nb; ++i) {
+                key.append(reinterpret_cast<const char*>(&btile[i]), sizeof(int));
+                key.append(reinterpret_cast<const char*>(&bwarps[i]), sizeof(int));
+                const int kind = fragment_kind(batches[i]);
+                key.append(reinterpret_cast<const char*>(&kind), sizeof(int));
+                key.append(reinterpret_cast<const char*>(&batches[i].total_prims), sizeof(uint32_t));
+                key.append(reinterpret_cast<const char*>(&batches[i].total_tiles), sizeof(uint32_t));
+                key.append(reinterpret_cast<const char*>(&batches[i].nvar), sizeof(uint32_t));
+                const size_t nd = batches[i].draws.size(), nt = batches[i].targets.size();
+                key.append(reinterpret_cast<const char*>(&nd), sizeof nd);
+                key.append(reinterpret_cast<const char*>(&nt), sizeof nt);
+            }
+            const void* ptrs[6] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, nullptr};
+            key.append(reinterpret_cast<const char*>(ptrs), sizeof ptrs);
+            key.append(reinterpret_cast<const char*>(&ovf_capacity), sizeof ovf_capacity);
+            key.append(reinterpret_cast<const char*>(&bin_capacity), sizeof bin_capacity);
+            key.push_back(rev.empty() ? 0 : 1);
+            GraphEntry& g = graphs[key];
+            g.last_use = ++graph_clock;
+            if (!g.exec) {
+                if (!rev.empty() && g.events.empty()) {
+                    g.events.resize(rev.size());
+                    for (auto& e : g.events) cuda_check(cudaEventCreate(&e), "event");
+                }
+                revp = &g.events;
+                cudaGraph_t graph = nullptr;
+                cuda_check(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+                try {
+                    enqueue();
+                } catch (...) {
+                    cudaStreamEndCapture(stream, &graph);
+                    if (graph) cudaGraphDestroy(graph);
+                    throw;
+                }
+                cuda_check(cudaStreamEndCapture(stream, &graph), "end capture");
+                cudaError_t ie = cudaGraphInstantiate(&g.exec, graph, 0);
+                cudaGraphDestroy(graph);
+                cuda_check(ie, "cudaGraphInstantiate");
+                // keep the 32 most recently used graphs
+                while (graphs.size() > 32) {
+                    auto victim = graphs.begin();
+                    for (auto gi = graphs.begin(); gi != graphs.end(); ++gi)
+                        if (gi->second.last_use < victim->second.last_use) victim = gi;
+                    if (victim->second.exec) cudaGraphExecDestroy(victim->second.exec);
+                    for (cudaEvent_t e : victim->second.events) cudaEventDestroy(e);
+                    graphs.erase(victim);
+                }
+            } else {
+                revp = &g.events;
+                for (size_t i = first_batch; i < nb; ++i) launches += 2 + (batches[i].total_prims ? 2 : 0);
+            }
+            cuda_check(cudaGraphLaunch(graphs[key].exec, stream), "cudaGraphLaunch");
+        } else {
+            enqueue();
         }
         cuda_check(cudaEventRecord(ev1, stream), "event");
         cuda_check(cudaMemcpyAsync(st.data(), meta + off_status, nb * sizeof(BatchStatus), cudaMemcpyDeviceToHost,
@@ -738,9 +933,12 @@ void Device::execute_submission(Item& it, SubmissionRecord& rec) {
             }
         for (size_t i = first_batch; i < (bad == nb ? nb : bad); ++i) {
             fragments += st[i].fragments;
-            if (!rev.empty()) {
+            if (!revp->empty()) {
                 float ms = 0.0f;
-                if (cudaEventElapsedTime(&ms, rev[2 * i], rev[2 * i + 1]) == cudaSuccess) raster_ms += ms;
+                if (cudaEventElapsedTime(&ms, (*revp)[2 * i], (*revp)[2 * i + 1]) == cudaSuccess) {
+                    raster_ms += ms;
+                    if (tuning[i] >= 0) tuner_record(batches[i], tuning[i], ms);
+                }
             }
         }
         if (bad == nb) break;
@@ -976,6 +1174,8 @@ GBR_API gbr_status gbr_device_create(const gbr_device_config* cfg, gbr_device* o
         if (!raster_config_supported(d->tile, d->warps))
             fail(GBR_ERR_INVALID_ARGUMENT, "unsupported tile size / warps per tile %d/%d", d->tile, d->warps);
         if (cfg->bin_capacity) d->bin_capacity = cfg->bin_capacity;
+        d->autotune = cfg->tile_size == 0 && cfg->warps_per_tile == 0;
+        if (cfg->launch_mode > GBR_LAUNCH_PER_PASS) fail(GBR_ERR_INVALID_ARGUMENT, "launch_mode");
         cuda_check(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         Device* raw = d.get();
         d->worker = std::thread([raw] { raw->worker_main(); });
@@ -1008,6 +1208,11 @@ GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
             if (r.second.ev_start) cudaEventDestroy(r.second.ev_start);
             if (r.second.ev_end) cudaEventDestroy(r.second.ev_end);
         }
+        for (auto& g : d->graphs) {
+            if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+            for (cudaEvent_t e : g.second.events) cudaEventDestroy(e);
+        }
+        d->graphs.clear();
         d->objects.clear();
         d->records_buf.release();
         d->ovf_buf.release();

@@ -133,8 +133,9 @@ class Profile:
 
 
 class LaunchMode:
-    PER_PASS = 0
+    BATCHED = 0
     PER_DRAW = 1
+    PER_PASS = 2
 
 
 class BindingKind:
@@ -441,7 +442,7 @@ class Device:
     """One device + queue + worker (wgpu_cpu::instance -> request_adapter -> request_device)."""
 
     def __init__(self, lib: Optional[A.Lib] = None, profile: int = Profile.PARITY, tile_size: int = 0,
-                 warps_per_tile: int = 0, bin_capacity: int = 0, launch_mode: int = LaunchMode.PER_PASS,
+                 warps_per_tile: int = 0, bin_capacity: int = 0, launch_mode: int = LaunchMode.BATCHED,
                  batch_submissions: bool = False, use_graphs: bool = False, hbm_budget_bytes: int = 0,
                  device_ordinal: int = 0, time_kernels: bool = False):
         self.lib = lib if lib is not None else gpu_lib()

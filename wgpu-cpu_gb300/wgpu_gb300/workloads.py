@@ -335,3 +335,122 @@ def scene_reference_triangle(dev: W.Device, front_face: int, cull_mode: int,
     s.draws.append((pl, [], [], None, vertices, 0))
     s._keep = [sm]
     return s
+
+
+def random_rotation(rng) -> np.ndarray:
+    """Uniform random rotation (from a random unit quaternion) as a 4x4 matrix."""
+    q = rng.normal(size=4)
+    q /= np.linalg.norm(q)
+    w, x, y, z = q
+    r = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                  [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                  [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+    m = np.eye(4)
+    m[:3, :3] = r
+    return m
+
+
+@dataclass
+class MultiScene:
+    """Several render passes (one per target) recorded into one command buffer."""
+    device: W.Device
+    passes: list = field(default_factory=list)  # (color, depth, [(pipeline, groups, vbufs, ibuf, range)])
+    uploads: list = field(default_factory=list)
+    triangles: int = 0
+    label: str = ""
+
+    @property
+    def color(self):
+        return self.passes[0][0]
+
+    def record(self, enc: W.CommandEncoder) -> None:
+        for color, depth, draws in self.passes:
+            rp = enc.begin_render_pass([W.RenderPassColorAttachment(color, (0.0, 0.0, 0.0, 1.0))],
+                                       W.RenderPassDepthStencilAttachment(depth, 1.0))
+            for pipeline, groups, vbufs, ibuf, rng in draws:
+                rp.set_pipeline(pipeline)
+                for gi, g in enumerate(groups):
+                    rp.set_bind_group(gi, g)
+                for slot, vb in enumerate(vbufs):
+                    rp.set_vertex_buffer(slot, vb)
+                rp.set_index_buffer(ibuf, W.IndexFormat.UINT32)
+                rp.draw_indexed(rng)
+            rp.end()
+
+    def render(self) -> int:
+        enc = self.device.create_command_encoder()
+        self.record(enc)
+        idx = self.device.queue.submit([enc.finish()])
+        self.device.poll(True, idx)
+        return idx
+
+
+def scene_batched(dev: W.Device, n_targets: int = 64, n_draws: int = 256, seed: int = 3, tri_lo: int = 100,
+                  tri_hi: int = 200000, side_lo: int = 128, side_hi: int = 2048, tex_size: int = 256) -> MultiScene:
+    """Batching workload: n_draws draws into n_targets targets (Rgba8Unorm + Depth32Float Less),
+    target sides log-uniform in [side_lo, side_hi], triangle counts log-uniform in [tri_lo, tri_hi]
+    taken from the front of a displaced icosphere of the smallest sufficient level, random model
+    rotations seen from a random distance (every vertex in front of the camera, so w > 0), half
+    vertex-colour and half textured programs, draw d into target d mod n_targets."""
+    rng = np.random.default_rng(seed)
+    tw = np.exp(rng.uniform(math.log(side_lo), math.log(side_hi), n_targets)).astype(int)
+    th = np.exp(rng.uniform(math.log(side_lo), math.log(side_hi), n_targets)).astype(int)
+    counts = np.exp(rng.uniform(math.log(tri_lo), math.log(tri_hi), n_draws)).astype(int)
+    levels = [max(0, math.ceil(math.log(max(c, 20) / 20.0, 4))) for c in counts]
+    s = MultiScene(dev, label="batched")
+    meshes = {}
+    for lvl in sorted(set(levels)):
+        pos, nrm, uv, f = displaced_icosphere(lvl, seed + lvl)
+        col = rng.random((len(pos), 3)).astype(np.float32)
+        vt = np.concatenate([pos, nrm, uv], 1).astype(np.float32)
+        vc = np.concatenate([pos, col], 1).astype(np.float32)
+        vbt, vbc, ib = dev.create_buffer_init(vt), dev.create_buffer_init(vc), dev.create_buffer_init(f.ravel())
+        s.uploads += [(vbt, vt), (vbc, vc), (ib, f.ravel())]
+        meshes[lvl] = (vbt, vbc, ib)
+    img = checker_noise_texture(tex_size, seed + 7)
+    tex = dev.create_texture(tex_size, tex_size, W.TextureFormat.RGBA8_UNORM)
+    dev.queue.write_texture(tex, img)
+    s.uploads.append((tex, img))
+    samp = dev.create_sampler(W.AddressMode.REPEAT, W.AddressMode.REPEAT)
+    sm_t = dev.create_shader_module(native="mesh_tex_lambert")
+    sm_c = dev.create_shader_module(native="mesh_color")
+    fmt = W.TextureFormat.RGBA8_UNORM
+    prim = W.PrimitiveState(W.PrimitiveTopology.TRIANGLE_LIST, cull_mode=W.Face.NONE)
+    depth = W.DepthStencilState(True, W.CompareFunction.LESS)
+    pl_t = dev.create_render_pipeline(
+        sm_t, [W.VertexBufferLayout(32, [_f32x3_layout(0, 0), _f32x3_layout(1, 12),
+                                         W.VertexAttribute(W.VertexFormat.FLOAT32X2, 24, 2)])],
+        prim, depth, sm_t, [W.ColorTargetState(fmt)])
+    pl_c = dev.create_render_pipeline(
+        sm_c, [W.VertexBufferLayout(24, [_f32x3_layout(0, 0), _f32x3_layout(1, 12)])], prim, depth, sm_c,
+        [W.ColorTargetState(fmt)])
+    g_tex = dev.create_bind_group([W.BindGroupEntry(0, tex), W.BindGroupEntry(1, samp)])
+    targets = []
+    for t in range(n_targets):
+        color = dev.create_texture(int(tw[t]), int(th[t]), fmt)
+        dtex = dev.create_texture(int(tw[t]), int(th[t]), W.TextureFormat.DEPTH32_FLOAT)
+        targets.append((color, dtex, []))
+    keep = [tex, samp, sm_t, sm_c, g_tex]
+    for d in range(n_draws):
+        t = d % n_targets
+        color, dtex, draws = targets[t]
+        dist = rng.uniform(2.6, 4.5)
+        model = random_rotation(rng)
+        mvp = camera_mvp(color.width, color.height, eye=(0.0, 0.0, dist), model=model)
+        L = rng.normal(size=3)
+        L /= np.linalg.norm(L)
+        ubytes = mvp_bytes(mvp) + np.array([*L, 0.0], dtype=np.float32).tobytes()
+        ub = dev.create_buffer_init(ubytes)
+        s.uploads.append((ub, np.frombuffer(ubytes, np.uint8)))
+        g0 = dev.create_bind_group([W.BindGroupEntry(0, ub)])
+        keep += [ub, g0]
+        vbt, vbc, ib = meshes[levels[d]]
+        n = int(counts[d])
+        if d % 2 == 0:
+            draws.append((pl_t, [g0, g_tex], [vbt], ib, range(0, 3 * n)))
+        else:
+            draws.append((pl_c, [g0], [vbc], ib, range(0, 3 * n)))
+        s.triangles += n
+    s.passes = targets
+    s._keep = keep + [pl_t, pl_c] + [m for v in meshes.values() for m in v]
+    return s
