@@ -243,6 +243,8 @@ def run_ours(args, wk: Workload):
     dev = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True, tile_size=args.tile,
                    warps_per_tile=args.warps, launch_mode=LAUNCH_MODES[args.launch_mode], use_graphs=args.graphs)
     over = {"n_quads": args.quads} if args.quads and wk.name == "blend" else {}
+    if wk.name == "batched" and (args.draws or args.targets):
+        over = {"n_draws": args.draws or wk.kwargs["n_draws"], "n_targets": args.targets or wk.kwargs["n_targets"]}
     scene = wk.build(dev, **over)
     enc = dev.create_command_encoder()
     scene.record(enc)
@@ -276,10 +278,10 @@ def run_ours(args, wk: Workload):
 
     # the same command buffer on the plain per-draw path (one launch sequence per draw)
     per_draw = None
-    if wk.name == "batched" and args.launch_mode != "per_draw":
+    if wk.name == "batched" and args.launch_mode != "per_draw" and not args.no_per_draw:
         d2 = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True, tile_size=dev_tile(args),
                       warps_per_tile=dev_warps(args), launch_mode=W.LaunchMode.PER_DRAW)
-        scene2 = wk.build(d2)
+        scene2 = wk.build(d2, **over)
         enc2 = d2.create_command_encoder()
         scene2.record(enc2)
         cmd2 = enc2.finish()
@@ -348,8 +350,9 @@ def run_ours(args, wk: Workload):
             "config": {**wk.config(launch_mode=args.launch_mode, graphs=args.graphs),
                        "tile": dev_tile(args) if not args.autotune else "autotuned",
                        "warps_per_tile": dev_warps(args) if not args.autotune else "autotuned",
-                       **({"n_quads": args.quads} if over else {})},
+                       **over},
             "fragments_per_step": frags_per_step, "wall_ms_per_step": wall * 1e3 / args.steps,
+            "generic_setup_prims_per_step": int(stats[-1].generic_setup_prims),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None, "traffic": raster_traffic(wk.name) if not over else None,
                          "peak_source": peak_src, "kernel": "k_raster (tile sort + raster + shade + depth/blend + ROP)",
@@ -389,7 +392,10 @@ def main():
     ap.add_argument("--quads", type=int, default=0, help="blend workload: number of quads (profiling runs)")
     ap.add_argument("--tile", type=int, default=0)
     ap.add_argument("--warps", type=int, default=0)
+    ap.add_argument("--draws", type=int, default=0, help="batched workload: number of draws (profiling runs)")
+    ap.add_argument("--targets", type=int, default=0, help="batched workload: number of targets (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-per-draw", action="store_true", help="batched workload: skip the per-draw comparison")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.autotune:

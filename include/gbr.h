@@ -164,7 +164,9 @@ typedef struct gbr_device_config {
     uint32_t use_graphs;        /* 1 = replay per-shape CUDA graphs                          */
     uint32_t time_kernels;      /* 1 = CUDA events around the raster kernels (stats.raster_ms) */
     uint64_t hbm_budget_bytes;  /* transient (per-submission) memory budget; 0 = 80 GB       */
-    uint64_t reserved[4];
+    uint32_t raster_order;      /* gbr_raster_order                                          */
+    uint32_t _pad0;
+    uint64_t reserved[3];
 } gbr_device_config;
 
 /* How draws map to kernel launches.
@@ -174,6 +176,14 @@ typedef struct gbr_device_config {
  *  PER_DRAW — the plain drop-in: one launch sequence per draw, each over the whole target.
  *  PER_PASS — one launch sequence per render pass. */
 enum gbr_launch_mode { GBR_LAUNCH_BATCHED = 0, GBR_LAUNCH_PER_DRAW = 1, GBR_LAUNCH_PER_PASS = 2 };
+
+/* How a tile's fragments are resolved.
+ *  AUTO     — batches whose draws all write depth with Less/LessEqual/Greater/GreaterEqual, do
+ *             not blend and never discard resolve each pixel's surviving fragment by an atomic
+ *             (depth, order) minimum and shade only that one (same colour, depth and fragment
+ *             count as the ordered walk); every other batch walks its fragments in order.
+ *  ORDERED  — always walk fragments in primitive order. */
+enum gbr_raster_order { GBR_RASTER_AUTO = 0, GBR_RASTER_ORDERED = 1 };
 
 typedef struct gbr_limits {
     uint32_t max_texture_dimension_2d;
@@ -308,7 +318,7 @@ typedef struct gbr_submission_stats {
     double gpu_ms;                 /* device time of the submission   */
     double submit_to_fence_ms;     /* submit -> fence signalled       */
     uint32_t batched_with;         /* number of submissions merged into the same launch */
-    uint32_t _pad;
+    uint32_t generic_setup_prims;  /* primitives set up by the generic (clipping) setup kernel */
     double raster_ms;              /* device time of the raster kernels (config.time_kernels) */
 } gbr_submission_stats;
 

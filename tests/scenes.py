@@ -10,7 +10,7 @@ def random_clip_triangles(dev, n_tris, width, height, seed, topology=W.Primitive
                           index_format=None, depth=None, cull=W.Face.NONE, front_face=W.FrontFace.CCW,
                           depth_write=True, spread=1.6, w_range=(0.3, 2.0), z_range=(-0.3, 1.3),
                           clear=(0.1, 0.2, 0.3, 1.0), color_format=W.TextureFormat.RGBA8_UNORM,
-                          instances=1, base_vertex=0, scissor=None, viewport=None, blend=None):
+                          instances=1, base_vertex=0, scissor=None, viewport=None, blend=None, depth_clear=0.75):
     """Random triangles given directly in clip space (clip_passthrough program): they cross
     every clip plane, so the clipper, the sub-triangle order and degenerate spans all get hit."""
     rng = np.random.default_rng(seed)
@@ -40,7 +40,7 @@ def random_clip_triangles(dev, n_tris, width, height, seed, topology=W.Primitive
     dtex = dev.create_texture(width, height, W.TextureFormat.DEPTH32_FLOAT) if depth is not None else None
     enc = dev.create_command_encoder()
     rp = enc.begin_render_pass([W.RenderPassColorAttachment(color, clear)],
-                               W.RenderPassDepthStencilAttachment(dtex, 0.75) if dtex is not None else None)
+                               W.RenderPassDepthStencilAttachment(dtex, depth_clear) if dtex is not None else None)
     rp.set_pipeline(pl)
     rp.set_vertex_buffer(0, vb_pos)
     rp.set_vertex_buffer(1, vb_col)

@@ -41,14 +41,15 @@ def oracle_result():
     return out, n
 
 
+@pytest.mark.parametrize("order", [W.RasterOrder.AUTO, W.RasterOrder.ORDERED])
 @pytest.mark.parametrize("mode", [W.LaunchMode.BATCHED, W.LaunchMode.PER_PASS, W.LaunchMode.PER_DRAW])
-def test_launch_modes_match_oracle(oracle_result, mode):
-    dev = W.Device(launch_mode=mode, tile_size=16, warps_per_tile=8)
+def test_launch_modes_match_oracle(oracle_result, mode, order):
+    dev = W.Device(launch_mode=mode, tile_size=16, warps_per_tile=8, raster_order=order)
     try:
         out, n, st, _ = render_all(dev, **SMALL)
         assert_targets_same((out, n), oracle_result, f"mode {mode}")
         if mode == W.LaunchMode.BATCHED:
-            assert st.kernel_launches <= 8, st.kernel_launches
+            assert st.kernel_launches <= 6, st.kernel_launches
         if mode == W.LaunchMode.PER_DRAW:
             assert st.kernel_launches >= 4 * SMALL["n_draws"]
     finally:

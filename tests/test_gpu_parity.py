@@ -22,6 +22,14 @@ def gpu():
 
 
 @pytest.fixture(scope="module")
+def gpu_ordered():
+    """Every batch walks its fragments in primitive order (no visibility raster)."""
+    d = W.Device(raster_order=W.RasterOrder.ORDERED)
+    yield d
+    d.close()
+
+
+@pytest.fixture(scope="module")
 def gpu_ext():
     d = W.Device(profile=W.Profile.EXTENSION)
     yield d
@@ -73,10 +81,11 @@ def test_textured_icosphere_small(gpu, orc):
     assert_same(*res, "textured icosphere level 4")
 
 
-def test_textured_icosphere_full(gpu, orc):
+def test_textured_icosphere_full(gpu, gpu_ordered, orc):
     """The textured-mesh workload at full size: 81,920 triangles, 1920x1080 + Depth32Float."""
-    res = [scenes.render_scene(d, wl.scene_textured_icosphere) for d in (gpu, orc)]
-    assert_same(*res, "textured icosphere level 6 1080p")
+    res = [scenes.render_scene(d, wl.scene_textured_icosphere) for d in (gpu, gpu_ordered, orc)]
+    assert_same(res[0], res[2], "textured icosphere level 6 1080p")
+    assert_same(res[1], res[2], "textured icosphere level 6 1080p (ordered)")
     assert res[0][2] > 500000
 
 
@@ -99,10 +108,26 @@ def test_random_clip_triangles(gpu, orc, seed):
 @pytest.mark.parametrize("compare", [W.CompareFunction.LESS, W.CompareFunction.LESS_EQUAL, W.CompareFunction.GREATER,
                                      W.CompareFunction.GREATER_EQUAL, W.CompareFunction.EQUAL,
                                      W.CompareFunction.NOT_EQUAL, W.CompareFunction.ALWAYS, W.CompareFunction.NEVER])
-def test_depth_compare_functions(gpu, orc, compare):
+def test_depth_compare_functions(gpu, gpu_ordered, orc, compare):
     kw = dict(n_tris=300, width=128, height=96, seed=11, depth=compare, z_range=(0.0, 1.0), spread=0.9)
-    res = [scenes.random_clip_triangles(d, **kw) for d in (gpu, orc)]
-    assert_same(*res, f"depth compare {compare}")
+    res = [scenes.random_clip_triangles(d, **kw) for d in (gpu, gpu_ordered, orc)]
+    assert_same(res[0], res[2], f"depth compare {compare}")
+    assert_same(res[1], res[2], f"depth compare {compare} (ordered)")
+
+
+@pytest.mark.parametrize("compare", [W.CompareFunction.LESS, W.CompareFunction.LESS_EQUAL, W.CompareFunction.GREATER,
+                                     W.CompareFunction.GREATER_EQUAL])
+@pytest.mark.parametrize("z", [0.5, 0.0])
+def test_depth_ties(gpu, gpu_ordered, orc, compare, z):
+    """Triangles at one constant depth, so most fragments tie: Less / Greater keep the first of
+    equal depths, LessEqual / GreaterEqual the last.  z = 0 also mixes -0.0 and +0.0 depths,
+    which compare equal."""
+    for clear_depth in (1.0, z, -0.0):
+        kw = dict(n_tris=250, width=120, height=90, seed=17, depth=compare, z_range=(z, z), spread=0.9,
+                  w_range=(1.0, 1.0))
+        res = [scenes.random_clip_triangles(d, depth_clear=clear_depth, **kw) for d in (gpu, gpu_ordered, orc)]
+        assert_same(res[0], res[2], f"ties {compare} z={z} clear={clear_depth}")
+        assert_same(res[1], res[2], f"ties {compare} z={z} clear={clear_depth} (ordered)")
 
 
 def test_depth_write_disabled(gpu, orc):

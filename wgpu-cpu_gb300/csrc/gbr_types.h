@@ -127,6 +127,21 @@ struct DrawDesc {
     uint32_t blend_color[3], blend_alpha[3];  // src, dst, op
     uint32_t write_mask;
     float blend_constant[4];
+    // setup
+    uint32_t fast_vs;        // FastVs: the vertex stage the fast setup path runs, or FAST_VS_NONE
+    uint32_t _pad_fast;
+};
+
+// Vertex stages the fast setup kernel specialises on: every input an f32 attribute of exactly
+// the program's width.  Anything else (other formats, clipping, errors) goes through the
+// generic setup kernel.
+enum FastVs : uint32_t {
+    FAST_VS_NONE = 0,
+    FAST_VS_MVP_COLOR = 1,  // mesh_color*: f32x3 position, f32x3 colour, MVP from group 0
+    FAST_VS_MVP_TEX = 2,    // mesh_tex_lambert: f32x3 position, f32x3 normal, f32x2 uv
+    FAST_VS_QUAD = 3,       // quad_color: f32x3 position, f32x4 colour
+    FAST_VS_CLIP = 4,       // clip_passthrough: f32x4 clip position, f32x4 colour
+    FAST_VS_TRIANGLE = 5,   // colored_triangle: no inputs
 };
 
 // Per-sub-triangle record written by the setup kernel and read by binning and raster.
@@ -160,7 +175,7 @@ struct BatchStatus {
     uint32_t error;
     uint32_t error_detail;
     uint32_t ovf_used;        // overflow record slots used (may exceed capacity -> retry)
-    uint32_t _pad;
+    uint32_t slow_count;      // primitives queued for the generic setup kernel
     unsigned long long bin_entries;   // tile entries needed
     unsigned long long fragments;     // fragment-shader invocations
     unsigned long long primitives;    // primitives assembled
@@ -188,6 +203,10 @@ struct BatchParams {
     uint32_t* work_counter;   // persistent raster work queue
     BatchStatus* status;
     uint32_t* abort_flag;        // set by a failed batch; later batches of the submission skip
+    uint32_t* slow_prims;        // [total_prims] primitives the fast setup path hands on
+    void* states;                // visibility raster: per-draw fragment-stage state (RasterState)
+    uint32_t vis_compare;        // visibility raster: the batch's depth compare function
+    uint32_t _pad;
 };
 
 }  // namespace gbr

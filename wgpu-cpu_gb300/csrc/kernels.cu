@@ -4,8 +4,10 @@
 
 #include <mutex>
 
+#include "gbr.h"
 #include "kernels.h"
 #include "raster.cuh"
+#include "raster_vis.cuh"
 
 namespace gbr {
 
@@ -37,7 +39,27 @@ cudaError_t launch_raster(const BatchParams& bp, int num_sms, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+template <int T, int W>
+cudaError_t launch_raster_vis(const BatchParams& bp, int num_sms, cudaStream_t s) {
+    auto kern = k_raster_vis<T, W>;
+    static std::mutex mu;
+    static int blocks_per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (blocks_per_sm == 0) {
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, W * 32, 0);
+            if (e != cudaSuccess) return e;
+            if (blocks_per_sm < 1) blocks_per_sm = 1;
+        }
+    }
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)num_sms * blocks_per_sm, bp.total_tiles);
+    kern<<<grid ? grid : 1, W * 32, 0, s>>>(bp);
+    return cudaGetLastError();
+}
+
 }  // namespace
+
+size_t raster_state_bytes() { return sizeof(RasterState); }
 
 // Seeded inputs for the division self-test: random bit patterns, raster-like magnitudes,
 // exact multiples and neighbours of powers of two, in rotation.
@@ -66,7 +88,10 @@ __global__ void k_selftest_division(uint64_t n, uint64_t seed, unsigned long lon
         const float y = __frcp_rn(b);
         const float q = div_by_recip(a, b, y, div_fast_ok(b));
         const float ref = __fdiv_rn(a, b);
-        const bool same = __float_as_uint(q) == __float_as_uint(ref) || (q != q && ref != ref);
+        // the setup kernel also takes RN(1/w) from __frcp_rn for the reference's `1.0 / w`
+        const float one_over = __fdiv_rn(1.0f, b);
+        const bool same = (__float_as_uint(q) == __float_as_uint(ref) || (q != q && ref != ref)) &&
+                          (__float_as_uint(y) == __float_as_uint(one_over) || (y != y && one_over != one_over));
         if (!same && atomicAdd(mismatches, 1ull) == 0ull) {
             first[0] = a;
             first[1] = b;
@@ -74,12 +99,58 @@ __global__ void k_selftest_division(uint64_t n, uint64_t seed, unsigned long lon
     }
 }
 
-bool raster_config_supported(int tile, int warps) {
+// Tile shapes of the ordered raster kernel.
+static bool ordered_config_supported(int tile, int warps) {
     switch (tile) {
         case 8: return warps == 1 || warps == 2;
         case 16: return warps == 2 || warps == 4 || warps == 8;
         case 32: return warps == 4 || warps == 8;
         default: return false;
+    }
+}
+// Tile shapes of the visibility raster kernel.
+static bool vis_config_supported(int tile, int warps) {
+    switch (tile) {
+        case 8: return warps == 1 || warps == 2;
+        case 16: case 32: return warps == 1 || warps == 2 || warps == 4 || warps == 8;
+        default: return false;
+    }
+}
+
+bool raster_config_supported(int tile, int warps) {
+    return ordered_config_supported(tile, warps) || vis_config_supported(tile, warps);
+}
+
+uint32_t batch_kernel_launches(uint32_t total_prims, int tile, int warps, int kind) {
+    if (kind == 3 && !vis_config_supported(tile, warps)) kind = 0;
+    return 2u + (total_prims ? 4u : 0u) + (kind == 3 ? 1u : 0u);
+}
+
+uint32_t fast_vs_kind(const DrawDesc& d) {
+    auto f32 = [&](int loc, uint32_t fmt) {
+        const AttrDesc& a = d.attr[loc];
+        return a.buffer >= 0 && a.format == fmt && a.offset % 4 == 0 && d.vb_stride_vertex[a.buffer] % 4 == 0 &&
+               d.vb_stride_instance[a.buffer] % 4 == 0 && reinterpret_cast<uintptr_t>(d.vb_data[a.buffer]) % 4 == 0;
+    };
+    switch (d.program) {
+        case PROG_MESH_COLOR:
+        case PROG_MESH_COLOR_PERSPECTIVE:
+        case PROG_MESH_COLOR_DISCARD:
+            return f32(0, GBR_VERTEX_FORMAT_FLOAT32X3) && f32(1, GBR_VERTEX_FORMAT_FLOAT32X3) ? FAST_VS_MVP_COLOR
+                                                                                               : FAST_VS_NONE;
+        case PROG_MESH_TEX_LAMBERT:
+            return f32(0, GBR_VERTEX_FORMAT_FLOAT32X3) && f32(1, GBR_VERTEX_FORMAT_FLOAT32X3) &&
+                           f32(2, GBR_VERTEX_FORMAT_FLOAT32X2)
+                       ? FAST_VS_MVP_TEX
+                       : FAST_VS_NONE;
+        case PROG_QUAD_COLOR:
+            return f32(0, GBR_VERTEX_FORMAT_FLOAT32X3) && f32(1, GBR_VERTEX_FORMAT_FLOAT32X4) ? FAST_VS_QUAD
+                                                                                               : FAST_VS_NONE;
+        case PROG_CLIP_PASSTHROUGH:
+            return f32(0, GBR_VERTEX_FORMAT_FLOAT32X4) && f32(1, GBR_VERTEX_FORMAT_FLOAT32X4) ? FAST_VS_CLIP
+                                                                                               : FAST_VS_NONE;
+        case PROG_COLORED_TRIANGLE: return FAST_VS_TRIANGLE;
+        default: return FAST_VS_NONE;
     }
 }
 
@@ -93,7 +164,22 @@ cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms
     const uint32_t cap = (uint32_t)num_sms * 16;
     if (items) {
         uint32_t g = std::min((items + 127) / 128, cap);
-        k_setup<<<g, 128, 0, s>>>(bp);
+        const size_t smem = setup_stage_bytes(bp.record_stride);
+        {
+            static std::mutex mu;
+            static size_t configured = 0;
+            std::lock_guard<std::mutex> lk(mu);
+            if (configured < smem) {
+                if ((e = cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+                    cudaSuccess)
+                    return e;
+                configured = smem;
+            }
+        }
+        k_setup<<<g, kSetupWarps * 32, smem, s>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        ++*launches;
+        k_setup_slow<<<std::min((items + 127) / 128, (uint32_t)num_sms * 4), 128, 0, s>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         ++*launches;
     }
@@ -106,7 +192,23 @@ cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         ++*launches;
     }
-    if (ev_raster && (e = cudaEventRecordWithFlags(ev_raster[0], s, cudaEventRecordExternal)) != cudaSuccess) return e;
+    // Inside a stream capture the raster events must become event-record nodes of the graph
+    // (cudaEventRecordExternal); outside one that flag is not accepted.
+    unsigned int ev_flags = cudaEventRecordDefault;
+    if (ev_raster) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if ((e = cudaStreamIsCapturing(s, &cs)) != cudaSuccess) return e;
+        if (cs == cudaStreamCaptureStatusActive) ev_flags = cudaEventRecordExternal;
+    }
+    if (kind == 3) {
+        k_build_states<<<(bp.num_draws + 127) / 128, 128, 0, s>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        ++*launches;
+    }
+    if (ev_raster && (e = cudaEventRecordWithFlags(ev_raster[0], s, ev_flags)) != cudaSuccess) return e;
+    if (kind == 3 && !vis_config_supported(tile, warps)) kind = 0;
+    // the ordered kernel for a warps-per-tile it has no instantiation for: the tile's default
+    if (kind != 3 && !ordered_config_supported(tile, warps)) warps = tile == 8 ? 2 : 8;
     for (;;) {
     switch ((tile * 16 + warps) * 4 + (kind & 3)) {
         case (8 * 16 + 1) * 4: e = launch_raster<8, 1>(bp, num_sms, s); break;
@@ -122,6 +224,16 @@ cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms
         case (32 * 16 + 8) * 4: e = launch_raster<32, 8>(bp, num_sms, s); break;
         case (32 * 16 + 8) * 4 + 1: e = launch_raster<32, 8, 1>(bp, num_sms, s); break;
         case (32 * 16 + 8) * 4 + 2: e = launch_raster<32, 8, 2>(bp, num_sms, s); break;
+        case (8 * 16 + 1) * 4 + 3: e = launch_raster_vis<8, 1>(bp, num_sms, s); break;
+        case (8 * 16 + 2) * 4 + 3: e = launch_raster_vis<8, 2>(bp, num_sms, s); break;
+        case (16 * 16 + 1) * 4 + 3: e = launch_raster_vis<16, 1>(bp, num_sms, s); break;
+        case (16 * 16 + 2) * 4 + 3: e = launch_raster_vis<16, 2>(bp, num_sms, s); break;
+        case (16 * 16 + 4) * 4 + 3: e = launch_raster_vis<16, 4>(bp, num_sms, s); break;
+        case (16 * 16 + 8) * 4 + 3: e = launch_raster_vis<16, 8>(bp, num_sms, s); break;
+        case (32 * 16 + 1) * 4 + 3: e = launch_raster_vis<32, 1>(bp, num_sms, s); break;
+        case (32 * 16 + 2) * 4 + 3: e = launch_raster_vis<32, 2>(bp, num_sms, s); break;
+        case (32 * 16 + 4) * 4 + 3: e = launch_raster_vis<32, 4>(bp, num_sms, s); break;
+        case (32 * 16 + 8) * 4 + 3: e = launch_raster_vis<32, 8>(bp, num_sms, s); break;
         default:
             if (kind == 0) return cudaErrorInvalidValue;
             kind = 0;  // no specialised instantiation for this tile shape: the generic kernel
@@ -131,7 +243,7 @@ cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms
     }
     if (e != cudaSuccess) return e;
     ++*launches;
-    if (ev_raster) e = cudaEventRecordWithFlags(ev_raster[1], s, cudaEventRecordExternal);
+    if (ev_raster) e = cudaEventRecordWithFlags(ev_raster[1], s, ev_flags);
     return e;
 }
 
@@ -164,12 +276,13 @@ constexpr uint32_t kNaVaryings = 4;  // clip_passthrough carries one vec4f colou
 constexpr uint32_t kNaStride = (uint32_t)((sizeof(TriRecord) + 3 * kNaVaryings * sizeof(float) + 15) & ~size_t(15));
 constexpr size_t kNaOvf = kNaRecords + (size_t)GBR_NOALLOC_MAX_TRIANGLES * kNaStride;
 constexpr size_t kNaBins = kNaOvf + (size_t)GBR_NOALLOC_MAX_CLIPPED * kNaStride;
+constexpr size_t kNaSlow = kNaBins + (size_t)GBR_NOALLOC_MAX_BIN_ENTRIES * sizeof(uint32_t);
 constexpr uint32_t kNaTile = 16, kNaWarps = 8;
 constexpr uint32_t kNaMaxTiles = (GBR_NOALLOC_MAX_DIM / kNaTile) * (GBR_NOALLOC_MAX_DIM / kNaTile);
 static_assert(sizeof(DrawDesc) <= kNaTarget - kNaDraw, "DrawDesc does not fit its slot");
 static_assert(sizeof(TargetDesc) <= kNaTiles - kNaTarget, "TargetDesc does not fit its slot");
 static_assert(kNaTiles + 3 * (kNaMaxTiles + 1) * sizeof(uint32_t) <= kNaRecords, "tile arrays do not fit");
-static_assert(kNaBins + (size_t)GBR_NOALLOC_MAX_BIN_ENTRIES * sizeof(uint32_t) <= GBR_NOALLOC_SCRATCH_BYTES,
+static_assert(kNaSlow + (size_t)GBR_NOALLOC_MAX_TRIANGLES * sizeof(uint32_t) <= GBR_NOALLOC_SCRATCH_BYTES,
               "bins do not fit the scratch array");
 
 std::mutex g_na_mu;
@@ -259,6 +372,7 @@ extern "C" GBR_API gbr_status gbr_render_triangles_noalloc(const float* clip_pos
     d.depth_compare = state->depth_compare;
     d.depth_write = state->depth_write_enabled;
     d.write_mask = 0xF;
+    d.fast_vs = fast_vs_kind(d);
     TargetDesc t;
     std::memset(&t, 0, sizeof t);
     t.color = color_target;
@@ -295,6 +409,7 @@ extern "C" GBR_API gbr_status gbr_render_triangles_noalloc(const float* clip_pos
     bp.tile_offset = tiles + (kNaMaxTiles + 1);
     bp.tile_cursor = tiles + 2 * (kNaMaxTiles + 1);
     bp.bins = reinterpret_cast<uint32_t*>(scratch + kNaBins);
+    bp.slow_prims = reinterpret_cast<uint32_t*>(scratch + kNaSlow);
     bp.work_counter = reinterpret_cast<uint32_t*>(scratch + kNaWork);
     bp.status = reinterpret_cast<BatchStatus*>(scratch + kNaStatus);
     bp.abort_flag = reinterpret_cast<uint32_t*>(scratch + kNaAbort);

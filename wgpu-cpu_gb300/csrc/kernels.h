@@ -12,11 +12,22 @@ namespace gbr {
 // ev_raster[0] / ev_raster[1] are recorded just before / after the raster kernel.
 //
 // `kind` selects a raster kernel specialised for one fragment pipeline (0 = generic, which
-// handles everything; see fragment_kind() in runtime.cu for the conditions of 1 and 2).
+// handles everything; see fragment_kind() in runtime.cu for the conditions of 1 and 2) or, for
+// kind 3, the visibility raster (k_raster_vis) of opaque depth-tested batches.
 cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms, cudaStream_t s, uint32_t* launches,
                          cudaEvent_t* ev_raster = nullptr, int kind = 0);
 
 // Tile side / warps-per-tile pairs compiled into the library.
 bool raster_config_supported(int tile, int warps);
+
+// Bytes of the per-draw fragment-stage state the visibility raster (kind 3) reads from
+// BatchParams::states (one entry per draw of the batch).
+size_t raster_state_bytes();
+
+// Kernels launch_batch enqueues for a batch (its `launches` increment).
+uint32_t batch_kernel_launches(uint32_t total_prims, int tile, int warps, int kind);
+
+// The FastVs shape of a resolved draw (FAST_VS_NONE when the fast setup path cannot run it).
+uint32_t fast_vs_kind(const DrawDesc& d);
 
 }  // namespace gbr

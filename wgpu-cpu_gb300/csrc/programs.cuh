@@ -59,16 +59,15 @@ __device__ __forceinline__ float ld_uniform(const DrawDesc& d, int group, int bi
     return __ldg(reinterpret_cast<const float*>(d.uniform[group][binding] + byte_off));
 }
 
-// mat4x4f (column-major at group/binding/offset) * vec4f, column-sum order.
-__device__ __forceinline__ V4 mat4_mul_vec4(const DrawDesc& d, int group, int binding, V4 v) {
-    const float* m = reinterpret_cast<const float*>(d.uniform[group][binding]);
+// mat4x4f (column-major, 16 floats at m) * vec4f, column-sum order.
+__device__ __forceinline__ V4 mat4_mul_vec4(const float* m, V4 v) {
     float r[4];
 #pragma unroll
     for (int lane = 0; lane < 4; ++lane) {
-        float s = fmul(v.x, __ldg(m + 0 * 4 + lane));
-        s = fadd(s, fmul(v.y, __ldg(m + 1 * 4 + lane)));
-        s = fadd(s, fmul(v.z, __ldg(m + 2 * 4 + lane)));
-        s = fadd(s, fmul(v.w, __ldg(m + 3 * 4 + lane)));
+        float s = fmul(v.x, m[0 * 4 + lane]);
+        s = fadd(s, fmul(v.y, m[1 * 4 + lane]));
+        s = fadd(s, fmul(v.z, m[2 * 4 + lane]));
+        s = fadd(s, fmul(v.w, m[3 * 4 + lane]));
         r[lane] = s;
     }
     return {r[0], r[1], r[2], r[3]};
@@ -118,10 +117,13 @@ __host__ __device__ __forceinline__ uint32_t program_interp(uint32_t prog) {
     return prog == PROG_MESH_COLOR_PERSPECTIVE ? INTERP_PERSPECTIVE : INTERP_LINEAR;
 }
 
-// Vertex stage: position + varyings.  Returns false with *err set on a fetch error.
-__device__ __forceinline__ bool run_vs(const DrawDesc& d, uint32_t vertex, uint32_t instance, V4& pos, float* var,
-                                       uint32_t* err) {
+// Vertex stage: position + varyings.  Returns false with *err set on a fetch error.  `mvp` is a
+// copy of the 16 floats at group 0 / binding 0 (the mesh programs' matrix), or null to read them
+// from the uniform buffer.
+__device__ __forceinline__ bool run_vs(const DrawDesc& d, const float* mvp, uint32_t vertex, uint32_t instance,
+                                       V4& pos, float* var, uint32_t* err) {
     float a0[4], a1[4], a2[4];
+    const float* m = mvp ? mvp : reinterpret_cast<const float*>(d.uniform[0][0]);
     switch (d.program) {
         case PROG_COLORED_TRIANGLE: {
             uint32_t vi = vertex % 3u;
@@ -139,7 +141,7 @@ __device__ __forceinline__ bool run_vs(const DrawDesc& d, uint32_t vertex, uint3
         case PROG_MESH_COLOR_DISCARD: {
             if (!fetch_attr(d, 0, 3, vertex, instance, a0, err)) return false;
             if (!fetch_attr(d, 1, 3, vertex, instance, a1, err)) return false;
-            pos = mat4_mul_vec4(d, 0, 0, V4{a0[0], a0[1], a0[2], 1.0f});
+            pos = mat4_mul_vec4(m, V4{a0[0], a0[1], a0[2], 1.0f});
             var[0] = a1[0];
             var[1] = a1[1];
             var[2] = a1[2];
@@ -149,7 +151,7 @@ __device__ __forceinline__ bool run_vs(const DrawDesc& d, uint32_t vertex, uint3
             if (!fetch_attr(d, 0, 3, vertex, instance, a0, err)) return false;
             if (!fetch_attr(d, 1, 3, vertex, instance, a1, err)) return false;
             if (!fetch_attr(d, 2, 2, vertex, instance, a2, err)) return false;
-            pos = mat4_mul_vec4(d, 0, 0, V4{a0[0], a0[1], a0[2], 1.0f});
+            pos = mat4_mul_vec4(m, V4{a0[0], a0[1], a0[2], 1.0f});
             var[0] = a1[0];
             var[1] = a1[1];
             var[2] = a1[2];

@@ -269,16 +269,13 @@ __device__ __forceinline__ bool resolve_vertex(const DrawDesc& d, uint32_t k, ui
     return true;
 }
 
-// Fills one sub-triangle record; returns false for a w == 0 vertex.
-__device__ __forceinline__ bool build_record(const BatchParams& bp, const DrawDesc& d, TriRecord* r, uint32_t key,
-                                             uint32_t draw, uint32_t prim_index, bool front_facing, const CV v[3],
-                                             const float inv_w0[3], const float var[3][MAX_VARYING_FLOATS],
-                                             uint32_t nvar) {
-    uint32_t fbx[3], fby[3];
-    V4 frag[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-        if (!to_raster(d, v[i].p, fbx[i], fby[i], frag[i])) return false;
+// Fills one sub-triangle record from its vertices' framebuffer coordinates and to_raster
+// outputs (viewport x, y, ndc z, 1/w); var holds up to NVMAX varyings per vertex.
+template <uint32_t NVMAX>
+__device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriRecord* r, uint32_t key, uint32_t draw,
+                                                  uint32_t prim_index, bool front_facing, const CV v[3],
+                                                  const uint32_t fbx[3], const uint32_t fby[3], const V4 frag[3],
+                                                  const float inv_w0[3], const float (*var)[NVMAX], uint32_t nvar) {
     float area = shoelace(frag[0].x, frag[0].y, frag[1].x, frag[1].y, frag[2].x, frag[2].y);
     // scanlines(): sort the framebuffer vertices by y with bubblesort3 (util/sort.rs:3-8)
     int64_t px[3] = {fbx[0], fbx[1], fbx[2]}, py[3] = {fby[0], fby[1], fby[2]};
@@ -339,15 +336,46 @@ __device__ __forceinline__ bool build_record(const BatchParams& bp, const DrawDe
 #pragma unroll
     for (uint32_t i = 0; i < 3; ++i)
 #pragma unroll
-        for (uint32_t k = 0; k < MAX_VARYING_FLOATS; ++k)
+        for (uint32_t k = 0; k < NVMAX; ++k)
             if (k < nvar) rv[i * nvar + k] = var[i][k];
+}
+
+// Fills one sub-triangle record; returns false for a w == 0 vertex.
+__device__ __forceinline__ bool build_record(const BatchParams& bp, const DrawDesc& d, TriRecord* r, uint32_t key,
+                                             uint32_t draw, uint32_t prim_index, bool front_facing, const CV v[3],
+                                             const float inv_w0[3], const float var[3][MAX_VARYING_FLOATS],
+                                             uint32_t nvar) {
+    uint32_t fbx[3], fby[3];
+    V4 frag[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+        if (!to_raster(d, v[i].p, fbx[i], fby[i], frag[i])) return false;
+    build_record_frag<MAX_VARYING_FLOATS>(bp, r, key, draw, prim_index, front_facing, v, fbx, fby, frag, inv_w0, var,
+                                          nvar);
+    return true;
+}
+
+// The one tile a record can emit into, when its bounding box lies inside a single tile and
+// inside the draw's scissor and the target (then every row's span, which lies within the box,
+// is wholly visible there: for_each_tile would visit exactly this tile).
+__device__ __forceinline__ bool single_tile(const TriRecord& r, const DrawDesc& d, const TargetDesc& t, uint32_t shift,
+                                            uint32_t& lt) {
+    if ((r.xmin >> shift) != (r.xmax >> shift) || (r.row0 >> shift) != (r.row1 >> shift)) return false;
+    if (r.xmin < (int)d.sc_x0 || r.row0 < (int)d.sc_y0 || r.xmax >= (int)min(d.sc_x1, t.width) ||
+        r.row1 >= (int)min(d.sc_y1, t.height))
+        return false;
+    lt = (uint32_t)(r.row0 >> shift) * t.tiles_x + (uint32_t)(r.xmin >> shift);
     return true;
 }
 
 __device__ __forceinline__ void count_tiles(const BatchParams& bp, const TriRecord* r, const DrawDesc& d) {
     if (r->flags & 2u) return;
     const TargetDesc& t = bp.targets[d.target];
-    uint32_t base = t.tile_base;
+    uint32_t base = t.tile_base, one;
+    if (single_tile(*r, d, t, bp.tile_shift, one)) {
+        atomicAdd(&bp.tile_count[base + one], 1u);
+        return;
+    }
     for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) { atomicAdd(&bp.tile_count[base + lt], 1u); });
 }
 
@@ -372,137 +400,379 @@ __device__ __forceinline__ void coop_tiles(const BatchParams& bp, const TriRecor
     }
 }
 
-__global__ void __launch_bounds__(128) k_setup(BatchParams bp) {
+// ---- generic setup: any program, format, topology; clipping; error reporting
+// Sets up primitive gp of draw di (record written in place); a record spanning many tile rows
+// is returned in `coop` for the warp to count together.
+__device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp, const TriRecord*& coop) {
+    TriRecord* prim_rec = rec_at(bp.records, bp.record_stride, gp);
+    const uint32_t di = find_draw(bp.draws, bp.num_draws, gp);
+    const DrawDesc& d = bp.draws[di];
+    const uint32_t local = gp - d.prim_base;
+    const uint32_t inst = local / d.prims_per_instance;
+    const uint32_t p = local - inst * d.prims_per_instance;
+    const uint32_t instance = d.instance_start + inst;
+    prim_rec->key = gp << SUBTRI_BITS;
+    prim_rec->flags = 2u;
+    prim_rec->nsub = 0;
+    prim_rec->draw = di;
+    uint32_t sp[3];
+    if (d.topology == 4) {  // triangle strip (primitive.rs:360-392)
+        sp[0] = (p & 1u) ? p + 1 : p;
+        sp[1] = (p & 1u) ? p : p + 1;
+        sp[2] = p + 2;
+    } else {
+        sp[0] = 3 * p;
+        sp[1] = 3 * p + 1;
+        sp[2] = 3 * p + 2;
+    }
+    V4 pos[3];
+    float var[3][MAX_VARYING_FLOATS];
+    uint32_t err = 0;
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        uint32_t vertex = 0;
+        ok = ok && resolve_vertex(d, sp[k], vertex, &err) && run_vs(d, nullptr, vertex, instance, pos[k], var[k], &err);
+    }
+    if (!ok) {
+        raise_error(bp.status, err, gp);
+        return;
+    }
+    if (!d.has_fragment) return;
+    // TriFace (primitive.rs:169-197) and the cull decision (state.rs:542-561)
+    if (pos[0].w == 0.0f || pos[1].w == 0.0f || pos[2].w == 0.0f) {
+        raise_error(bp.status, ERR_W_ZERO, gp);
+        return;
+    }
+    float n[3][2];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        n[i][0] = fdiv(pos[i].x, pos[i].w);
+        n[i][1] = fdiv(pos[i].y, pos[i].w);
+    }
+    float abx = fsub(n[1][0], n[0][0]), aby = fsub(n[1][1], n[0][1]);
+    float acx = fsub(n[2][0], n[0][0]), acy = fsub(n[2][1], n[0][1]);
+    bool ccw = fsub(fmul(abx, acy), fmul(aby, acx)) > 0.0f;
+    bool front_facing = (ccw ? 0u : 1u) == d.front_face;
+    bool cull = d.cull_mode == 1 ? front_facing : d.cull_mode == 2 ? !front_facing : false;
+    if (cull) return;
+    const float inv_w0[3] = {fdiv(1.0f, pos[0].w), fdiv(1.0f, pos[1].w), fdiv(1.0f, pos[2].w)};
+    const uint32_t nvar = d.num_varyings;
+    if (inside_all_planes(pos)) {
+        CV v[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            v[i].p = pos[i];
+            v[i].b[0] = i == 0 ? 1.0f : 0.0f;
+            v[i].b[1] = i == 1 ? 1.0f : 0.0f;
+            v[i].b[2] = i == 2 ? 1.0f : 0.0f;
+        }
+        if (!build_record(bp, d, prim_rec, gp << SUBTRI_BITS, di, p, front_facing, v, inv_w0, var, nvar)) {
+            raise_error(bp.status, ERR_W_ZERO, gp);
+            prim_rec->flags = 2u;
+            return;
+        }
+        prim_rec->nsub = 1;
+        prim_rec->ovf = 0;
+        if (!(prim_rec->flags & 2u) && tiles_are_many(*prim_rec, bp.tile_shift)) coop = prim_rec;
+        else count_tiles(bp, prim_rec, d);
+        return;
+    }
+    // clipped: count the sub-triangles, reserve overflow slots, then emit in order
+    struct Counter {
+        uint32_t n;
+        __device__ void operator()(const CV*) { ++n; }
+    } counter{0};
+    clip_tri_ordered(pos, counter);
+    const uint32_t nsub = counter.n;
+    uint32_t ovf = 0;
+    if (nsub > 1) {
+        ovf = atomicAdd(&bp.status->ovf_used, nsub - 1);
+        if (ovf + nsub - 1 > bp.ovf_capacity) {
+            raise_error(bp.status, ERR_OVERFLOW_RECORDS, gp);
+            return;
+        }
+    }
+    struct Emitter {
+        const BatchParams* bp;
+        const DrawDesc* d;
+        TriRecord* prim_rec;
+        uint32_t gp, di, p, ovf, s;
+        bool ff;
+        const float* inv_w0;
+        const float (*var)[MAX_VARYING_FLOATS];
+        uint32_t nvar;
+        __device__ void operator()(const CV* v) {
+            TriRecord* r = s == 0 ? prim_rec : rec_at(bp->ovf_records, bp->record_stride, ovf + s - 1);
+            if (!build_record(*bp, *d, r, (gp << SUBTRI_BITS) | s, di, p, ff, v, inv_w0, var, nvar)) {
+                raise_error(bp->status, ERR_W_ZERO, gp);
+                r->flags = 2u;
+            } else {
+                count_tiles(*bp, r, *d);
+            }
+            ++s;
+        }
+    };
+    Emitter emitter{&bp, &d, prim_rec, gp, di, p, ovf, 0, front_facing, inv_w0, var, nvar};
+    clip_tri_ordered(pos, emitter);
+    if (nsub == 0) prim_rec->flags = 2u;
+    prim_rec->nsub = nsub;
+    prim_rec->ovf = ovf;
+}
+
+// The primitives the fast kernel queued, one lane each.
+__global__ void __launch_bounds__(128) k_setup_slow(BatchParams bp) {
+    const uint32_t n = bp.status->slow_count;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
+        if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the warp
+        const TriRecord* coop = nullptr;
+        if (base + lane < n) setup_generic(bp, bp.slow_prims[base + lane], coop);
+        coop_tiles(bp, coop, lane, [&](uint32_t tile, uint32_t) { atomicAdd(&bp.tile_count[tile], 1u); });
+    }
+}
+
+// ---- fast setup
+// A warp's copy of the draw all its lanes work on, with the mesh programs' matrix.
+struct alignas(16) DrawCache {
+    DrawDesc d;
+    float mvp[16];
+    uint32_t id;  // draw index, ~0 = empty
+    uint32_t _pad[3];
+};
+
+constexpr int kSetupWarps = 4;
+
+// Shared memory of k_setup beyond its static part: each warp stages its 32 primary records.
+__host__ __device__ __forceinline__ size_t setup_stage_bytes(uint32_t record_stride) {
+    return (size_t)kSetupWarps * 32 * record_stride;
+}
+
+template <int C>
+__device__ __forceinline__ bool fetch_f32(const DrawDesc& d, int loc, uint32_t vertex, uint32_t instance, float* out) {
+    const int b = d.attr[loc].buffer;
+    const uint64_t start = (uint64_t)instance * d.vb_stride_instance[b] + (uint64_t)vertex * d.vb_stride_vertex[b] +
+                           d.attr[loc].offset;
+    if (start + 4 * C > d.vb_size[b]) return false;
+    const float* f = reinterpret_cast<const float*>(d.vb_data[b] + start);
+#pragma unroll
+    for (int k = 0; k < C; ++k) out[k] = __ldg(f + k);
+    return true;
+}
+
+__host__ __device__ constexpr uint32_t fast_vs_varyings(int fvs) {
+    return fvs == FAST_VS_MVP_COLOR ? 3u : fvs == FAST_VS_MVP_TEX ? 5u : 4u;
+}
+
+// The vertex stage of run_vs for one FastVs shape (same operations); false = fetch out of range.
+template <int FVS>
+__device__ __forceinline__ bool fast_vertex(const DrawDesc& d, const float* mvp, uint32_t vertex, uint32_t instance,
+                                            V4& pos, float* var) {
+    float a0[4], a1[4], a2[2];
+    if constexpr (FVS == FAST_VS_MVP_COLOR || FVS == FAST_VS_MVP_TEX) {
+        if (!fetch_f32<3>(d, 0, vertex, instance, a0) || !fetch_f32<3>(d, 1, vertex, instance, a1)) return false;
+        if constexpr (FVS == FAST_VS_MVP_TEX) {
+            if (!fetch_f32<2>(d, 2, vertex, instance, a2)) return false;
+            var[3] = a2[0];
+            var[4] = a2[1];
+        }
+        pos = mat4_mul_vec4(mvp, V4{a0[0], a0[1], a0[2], 1.0f});
+        var[0] = a1[0];
+        var[1] = a1[1];
+        var[2] = a1[2];
+    } else if constexpr (FVS == FAST_VS_QUAD) {
+        if (!fetch_f32<3>(d, 0, vertex, instance, a0) || !fetch_f32<4>(d, 1, vertex, instance, a1)) return false;
+        pos = {a0[0], a0[1], a0[2], 1.0f};
+        for (int k = 0; k < 4; ++k) var[k] = a1[k];
+    } else if constexpr (FVS == FAST_VS_CLIP) {
+        if (!fetch_f32<4>(d, 0, vertex, instance, a0) || !fetch_f32<4>(d, 1, vertex, instance, a1)) return false;
+        pos = {a0[0], a0[1], a0[2], a0[3]};
+        for (int k = 0; k < 4; ++k) var[k] = a1[k];
+    } else {
+        const uint32_t vi = vertex % 3u;
+        pos = {(float)((int32_t)vi - 1), (float)((int32_t)(vi & 1u) * 2 - 1), 0.0f, 1.0f};
+        var[0] = (float)(vi == 0u);
+        var[1] = (float)(vi == 1u);
+        var[2] = (float)(vi == 2u);
+        var[3] = 1.0f;
+    }
+    return true;
+}
+
+// Sets up primitive gp completely when it needs no clipping and raises no error (returns
+// false otherwise: the generic kernel redoes it, reports errors and clips).
+template <int FVS>
+__device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc& d, const float* mvp, uint32_t gp,
+                                          uint32_t di, TriRecord* rec, const TriRecord*& coop) {
+    constexpr uint32_t NV = fast_vs_varyings(FVS);
+    const uint32_t local = gp - d.prim_base;
+    const uint32_t inst = d.instance_count == 1 ? 0u : local / d.prims_per_instance;
+    const uint32_t p = local - inst * d.prims_per_instance;
+    const uint32_t instance = d.instance_start + inst;
+    rec->key = gp << SUBTRI_BITS;
+    rec->flags = 2u;
+    rec->nsub = 0;
+    rec->draw = di;
+    uint32_t sp[3];
+    if (d.topology == 4) {  // triangle strip (primitive.rs:360-392)
+        sp[0] = (p & 1u) ? p + 1 : p;
+        sp[1] = (p & 1u) ? p : p + 1;
+        sp[2] = p + 2;
+    } else {
+        sp[0] = 3 * p;
+        sp[1] = 3 * p + 1;
+        sp[2] = 3 * p + 2;
+    }
+    V4 pos[3];
+    float var[3][NV];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        // index resolution (render_pass/index.rs:45-88)
+        const uint32_t at = d.first + sp[k];
+        uint32_t vertex = at;
+        if (d.index_format != 0) {
+            uint32_t raw;
+            if (d.index_format == 1) {
+                if ((uint64_t)(at + 1) * 2 > d.index_bytes) return false;
+                raw = __ldg(reinterpret_cast<const uint16_t*>(d.index_data) + at);
+            } else {
+                if ((uint64_t)(at + 1) * 4 > d.index_bytes) return false;
+                raw = __ldg(reinterpret_cast<const uint32_t*>(d.index_data) + at);
+            }
+            const int64_t v = (int64_t)raw + (int64_t)d.base_vertex;
+            if (v < 0 || v > 0xFFFFFFFFll) return false;
+            vertex = (uint32_t)v;
+        }
+        if (!fast_vertex<FVS>(d, mvp, vertex, instance, pos[k], var[k])) return false;
+    }
+    if (!d.has_fragment) return true;
+    if (pos[0].w == 0.0f || pos[1].w == 0.0f || pos[2].w == 0.0f) return false;
+    // x/w, y/w, z/w by the correctly rounded reciprocal RN(1/w) (also the reference's
+    // `1.0 / w`) and div_by_recip's exact quotient
+    float rw[3], n[3][2];
+    bool wok[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        rw[i] = __frcp_rn(pos[i].w);
+        wok[i] = div_fast_ok(pos[i].w);
+        n[i][0] = div_by_recip(pos[i].x, pos[i].w, rw[i], wok[i]);
+        n[i][1] = div_by_recip(pos[i].y, pos[i].w, rw[i], wok[i]);
+    }
+    // TriFace (primitive.rs:169-197) and the cull decision (state.rs:542-561)
+    const float abx = fsub(n[1][0], n[0][0]), aby = fsub(n[1][1], n[0][1]);
+    const float acx = fsub(n[2][0], n[0][0]), acy = fsub(n[2][1], n[0][1]);
+    const bool ccw = fsub(fmul(abx, acy), fmul(aby, acx)) > 0.0f;
+    const bool front_facing = (ccw ? 0u : 1u) == d.front_face;
+    const bool cull = d.cull_mode == 1 ? front_facing : d.cull_mode == 2 ? !front_facing : false;
+    if (cull) return true;
+    // clipping: nothing to do inside all planes; dropped, exactly as clip_tri_ordered drops it,
+    // when all three vertices are outside the first plane any of them is outside (the planes
+    // before it pass the triangle through unchanged); a real split goes to the generic path
+#pragma unroll
+    for (int pl = 0; pl < 6; ++pl) {
+        const V4 nrm = clip_plane(pl);
+        const int out = (dot4(pos[0], nrm) < 0.0f) + (dot4(pos[1], nrm) < 0.0f) + (dot4(pos[2], nrm) < 0.0f);
+        if (out == 3) return true;  // no sub-triangles: the record stays empty
+        if (out != 0) return false;
+    }
+    // to_raster (raster.rs:145-160) on the quotients at hand
+    CV v[3];
+    uint32_t fbx[3], fby[3];
+    V4 frag[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        v[i].p = pos[i];
+        v[i].b[0] = i == 0 ? 1.0f : 0.0f;
+        v[i].b[1] = i == 1 ? 1.0f : 0.0f;
+        v[i].b[2] = i == 2 ? 1.0f : 0.0f;
+        const float nz = div_by_recip(pos[i].z, pos[i].w, rw[i], wok[i]);
+        const float vx = rust_max0(fadd(fmul(n[i][0], d.vp_sx), d.vp_tx));
+        const float vy = rust_max0(fadd(fmul(n[i][1], d.vp_sy), d.vp_ty));
+        fbx[i] = rust_f2u32(vx);
+        fby[i] = rust_f2u32(vy);
+        if ((fbx[i] | fby[i]) >= (1u << 30)) return false;  // the generic path reports it
+        frag[i] = {vx, vy, nz, rw[i]};
+    }
+    build_record_frag<NV>(bp, rec, gp << SUBTRI_BITS, di, p, front_facing, v, fbx, fby, frag, rw, var, NV);
+    rec->nsub = 1;
+    rec->ovf = 0;
+    if (!(rec->flags & 2u) && tiles_are_many(*rec, bp.tile_shift)) coop = rec;
+    else count_tiles(bp, rec, d);
+    return true;
+}
+
+// One lane per primitive.  A warp whose lanes share a draw copies its descriptor (and matrix)
+// to shared memory and runs the vertex stage specialised for the draw's FastVs shape; its 32
+// primary records are built in shared memory and written out as one contiguous, coalesced
+// block (records of consecutive primitives are adjacent).  Primitives it cannot finish are
+// queued for k_setup_slow.
+__global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
+    extern __shared__ __align__(16) uint8_t s_stage_raw[];
+    __shared__ DrawCache s_dc[kSetupWarps];
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t rstride = bp.record_stride;
+    uint8_t* stage = s_stage_raw + (size_t)warp * 32 * rstride;
+    DrawCache& dc = s_dc[warp];
+    if (lane == 0) dc.id = 0xFFFFFFFFu;
+    __syncwarp();
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < bp.total_prims; base += stride) {
         if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the warp
         const uint32_t gp = base + lane;
-        const TriRecord* coop = nullptr;  // primary record whose tiles the warp counts together
-        do {
-        if (gp >= bp.total_prims) break;
-        TriRecord* prim_rec = rec_at(bp.records, bp.record_stride, gp);
-        const uint32_t di = find_draw(bp.draws, bp.num_draws, gp);
-        const DrawDesc& d = bp.draws[di];
-        const uint32_t local = gp - d.prim_base;
-        const uint32_t inst = local / d.prims_per_instance;
-        const uint32_t p = local - inst * d.prims_per_instance;
-        const uint32_t instance = d.instance_start + inst;
-        prim_rec->key = gp << SUBTRI_BITS;
-        prim_rec->flags = 2u;
-        prim_rec->nsub = 0;
-        prim_rec->draw = di;
-        uint32_t sp[3];
-        if (d.topology == 4) {  // triangle strip (primitive.rs:360-392)
-            sp[0] = (p & 1u) ? p + 1 : p;
-            sp[1] = (p & 1u) ? p : p + 1;
-            sp[2] = p + 2;
-        } else {
-            sp[0] = 3 * p;
-            sp[1] = 3 * p + 1;
-            sp[2] = 3 * p + 2;
+        const bool live = gp < bp.total_prims;
+        uint32_t di = 0;
+        if (live) {
+            if (dc.id != 0xFFFFFFFFu && gp >= dc.d.prim_base &&
+                gp - dc.d.prim_base < dc.d.prims_per_instance * dc.d.instance_count)
+                di = dc.id;
+            else
+                di = find_draw(bp.draws, bp.num_draws, gp);
         }
-        V4 pos[3];
-        float var[3][MAX_VARYING_FLOATS];
-        uint32_t err = 0;
-        bool ok = true;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            uint32_t vertex = 0;
-            ok = ok && resolve_vertex(d, sp[k], vertex, &err) && run_vs(d, vertex, instance, pos[k], var[k], &err);
+        const uint32_t di0 = __shfl_sync(0xFFFFFFFFu, di, 0);
+        const bool uniform = __all_sync(0xFFFFFFFFu, !live || di == di0);
+        if (uniform && dc.id != di0) {  // warp-uniform
+            __syncwarp();
+            const uint2* src = reinterpret_cast<const uint2*>(bp.draws + di0);
+            uint2* dst = reinterpret_cast<uint2*>(&dc.d);
+            for (uint32_t k = lane; k < sizeof(DrawDesc) / 8; k += 32) dst[k] = __ldg(src + k);
+            const uint8_t* u = bp.draws[di0].uniform[0][0];
+            const bool has = u != nullptr && bp.draws[di0].uniform_size[0][0] >= 64;
+            if (lane < 16) dc.mvp[lane] = has ? __ldg(reinterpret_cast<const float*>(u) + lane) : 0.0f;
+            if (lane == 0) dc.id = di0;
+            __syncwarp();
         }
-        if (!ok) {
-            raise_error(bp.status, err, gp);
-            continue;
-        }
-        if (!d.has_fragment) continue;
-        // TriFace (primitive.rs:169-197) and the cull decision (state.rs:542-561)
-        if (pos[0].w == 0.0f || pos[1].w == 0.0f || pos[2].w == 0.0f) {
-            raise_error(bp.status, ERR_W_ZERO, gp);
-            continue;
-        }
-        float n[3][2];
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            n[i][0] = fdiv(pos[i].x, pos[i].w);
-            n[i][1] = fdiv(pos[i].y, pos[i].w);
-        }
-        float abx = fsub(n[1][0], n[0][0]), aby = fsub(n[1][1], n[0][1]);
-        float acx = fsub(n[2][0], n[0][0]), acy = fsub(n[2][1], n[0][1]);
-        bool ccw = fsub(fmul(abx, acy), fmul(aby, acx)) > 0.0f;
-        bool front_facing = (ccw ? 0u : 1u) == d.front_face;
-        bool cull = d.cull_mode == 1 ? front_facing : d.cull_mode == 2 ? !front_facing : false;
-        if (cull) continue;
-        const float inv_w0[3] = {fdiv(1.0f, pos[0].w), fdiv(1.0f, pos[1].w), fdiv(1.0f, pos[2].w)};
-        const uint32_t nvar = d.num_varyings;
-        if (inside_all_planes(pos)) {
-            CV v[3];
-#pragma unroll
-            for (int i = 0; i < 3; ++i) {
-                v[i].p = pos[i];
-                v[i].b[0] = i == 0 ? 1.0f : 0.0f;
-                v[i].b[1] = i == 1 ? 1.0f : 0.0f;
-                v[i].b[2] = i == 2 ? 1.0f : 0.0f;
-            }
-            if (!build_record(bp, d, prim_rec, gp << SUBTRI_BITS, di, p, front_facing, v, inv_w0, var, nvar)) {
-                raise_error(bp.status, ERR_W_ZERO, gp);
-                prim_rec->flags = 2u;
-                continue;
-            }
-            prim_rec->nsub = 1;
-            prim_rec->ovf = 0;
-            if (!(prim_rec->flags & 2u) && tiles_are_many(*prim_rec, bp.tile_shift)) coop = prim_rec;
-            else count_tiles(bp, prim_rec, d);
-            continue;
-        }
-        // clipped: count the sub-triangles, reserve overflow slots, then emit in order
-        struct Counter {
-            uint32_t n;
-            __device__ void operator()(const CV*) { ++n; }
-        } counter{0};
-        clip_tri_ordered(pos, counter);
-        const uint32_t nsub = counter.n;
-        uint32_t ovf = 0;
-        if (nsub > 1) {
-            ovf = atomicAdd(&bp.status->ovf_used, nsub - 1);
-            if (ovf + nsub - 1 > bp.ovf_capacity) {
-                raise_error(bp.status, ERR_OVERFLOW_RECORDS, gp);
-                continue;
+        TriRecord* rec = reinterpret_cast<TriRecord*>(stage + (size_t)lane * rstride);
+        const TriRecord* coop = nullptr;
+        bool done = false;
+        if (live && uniform) {
+            switch (dc.d.fast_vs) {  // warp-uniform
+                case FAST_VS_MVP_COLOR: done = fast_prim<FAST_VS_MVP_COLOR>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_MVP_TEX: done = fast_prim<FAST_VS_MVP_TEX>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_QUAD: done = fast_prim<FAST_VS_QUAD>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_CLIP: done = fast_prim<FAST_VS_CLIP>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_TRIANGLE: done = fast_prim<FAST_VS_TRIANGLE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                default: break;
             }
         }
-        struct Emitter {
-            const BatchParams* bp;
-            const DrawDesc* d;
-            TriRecord* prim_rec;
-            uint32_t gp, di, p, ovf, s;
-            bool ff;
-            const float* inv_w0;
-            const float (*var)[MAX_VARYING_FLOATS];
-            uint32_t nvar;
-            __device__ void operator()(const CV* v) {
-                TriRecord* r = s == 0 ? prim_rec : rec_at(bp->ovf_records, bp->record_stride, ovf + s - 1);
-                if (!build_record(*bp, *d, r, (gp << SUBTRI_BITS) | s, di, p, ff, v, inv_w0, var, nvar)) {
-                    raise_error(bp->status, ERR_W_ZERO, gp);
-                    r->flags = 2u;
-                } else {
-                    count_tiles(*bp, r, *d);
-                }
-                ++s;
-            }
-        };
-        // a copy for the emitter, so that only this rare path keeps the varyings in local memory
-        float var_copy[3][MAX_VARYING_FLOATS];
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int k = 0; k < (int)MAX_VARYING_FLOATS; ++k) var_copy[i][k] = var[i][k];
-        Emitter emitter{&bp, &d, prim_rec, gp, di, p, ovf, 0, front_facing, inv_w0, var_copy, nvar};
-        clip_tri_ordered(pos, emitter);
-        if (nsub == 0) prim_rec->flags = 2u;
-        prim_rec->nsub = nsub;
-        prim_rec->ovf = ovf;
-        } while (false);
+        // the rest to the generic kernel (its record is rewritten there)
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, live && !done);
+        if (m) {
+            const int leader = __ffs(m) - 1;
+            uint32_t at = 0;
+            if ((int)lane == leader) at = atomicAdd(&bp.status->slow_count, (uint32_t)__popc(m));
+            at = __shfl_sync(0xFFFFFFFFu, at, leader);
+            if (live && !done) bp.slow_prims[at + __popc(m & ((1u << lane) - 1u))] = gp;
+        }
         coop_tiles(bp, coop, lane, [&](uint32_t tile, uint32_t) { atomicAdd(&bp.tile_count[tile], 1u); });
+        // the warp's records, staged above, out as one block
+        __syncwarp();
+        const uint32_t nrec = min(32u, bp.total_prims - base);
+        const uint32_t words = nrec * (rstride / 16);
+        uint4* gdst = reinterpret_cast<uint4*>(bp.records + (size_t)base * rstride);
+        const uint4* ssrc = reinterpret_cast<const uint4*>(stage);
+        for (uint32_t k = lane; k < words; k += 32) gdst[k] = ssrc[k];
+        __syncwarp();
     }
 }
 
@@ -593,7 +863,9 @@ __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
                     const DrawDesc& d = bp.draws[r->draw];
                     const TargetDesc& t = bp.targets[d.target];
                     const uint32_t key = r->key;
-                    for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) { put(t.tile_base + lt, key); });
+                    uint32_t one;
+                    if (single_tile(*r, d, t, bp.tile_shift, one)) put(t.tile_base + one, key);
+                    else for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) { put(t.tile_base + lt, key); });
                 }
             }
         }

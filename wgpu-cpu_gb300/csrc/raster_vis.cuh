@@ -1,0 +1,305 @@
+// raster_vis.cuh — visibility raster for opaque, depth-tested batches.
+//
+// The reference walks fragments in primitive order and runs the late depth test at the first
+// colour output (render_pass/fragment.rs:427-453, 470-479).  When every draw into a target
+// writes depth with one of Less / LessEqual / Greater / GreaterEqual, does not blend and
+// never discards, the last fragment that passes at a pixel is determined without walking in
+// order:
+//
+//   Less          the passing sequence has strictly falling depth; the survivor is the fragment
+//                 of minimum depth, the earliest of those in order.
+//   LessEqual     non-increasing depth; all fragments of minimum depth pass; the survivor is the
+//                 latest of them.
+//   Greater(Eq.)  the same with maximum depth.
+//
+// and it passes iff it passes against the stored depth (every other fragment lies on the far
+// side of it).  So each fragment's (depth, order) is packed into one 64-bit key that orders it
+// by that rule, the tile's keys are reduced with shared-memory atomicMin in any order, and the
+// fragment stage runs once per pixel, for the survivor only.  Coverage, barycentrics and depth
+// are computed with exactly the operations of the ordered kernel (raster.rs:129-363), so the
+// colour, depth and fragment count come out identical; the count still includes every covered
+// fragment, because the reference runs the fragment stage before the depth test.
+//
+// -0 and +0 compare equal in the depth test, so -0 is keyed as +0; a NaN depth fails all four
+// comparisons and takes no part.
+#pragma once
+
+#include "raster.cuh"
+
+namespace gbr {
+
+// The record an order key names: sub-triangle 0 is the primitive's own record, the others are in
+// the overflow area.
+__device__ __forceinline__ const TriRecord* record_of(const BatchParams& bp, uint32_t key) {
+    const uint32_t prim = key >> SUBTRI_BITS, sub = key & ((1u << SUBTRI_BITS) - 1u);
+    const TriRecord* pr = rec_at(bp.records, bp.record_stride, prim);
+    return sub == 0 ? pr : rec_at(bp.ovf_records, bp.record_stride, __ldg(&pr->ovf) + sub - 1);
+}
+
+// Per-record constants of the barycentric evaluation (the same terms the ordered kernel keeps in
+// shared memory).
+struct BaryK {
+    float ax, ay, bx, by, cx, cy;
+    float kc0, kc1, kc2, rcp, area;
+    bool area_ok, ident;
+};
+
+__device__ __forceinline__ void bary_consts(const TriRecord& r, BaryK& k) {
+    k.ax = r.vpx[0]; k.ay = r.vpy[0];
+    k.bx = r.vpx[1]; k.by = r.vpy[1];
+    k.cx = r.vpx[2]; k.cy = r.vpy[2];
+    k.kc0 = fmul(fsub(k.cy, k.by), fadd(k.cx, k.bx));
+    k.kc1 = fmul(fsub(k.ay, k.cy), fadd(k.ax, k.cx));
+    k.kc2 = fmul(fsub(k.by, k.ay), fadd(k.bx, k.ax));
+    k.area = r.area;
+    k.rcp = __frcp_rn(k.area);
+    k.area_ok = div_fast_ok(k.area);
+    k.ident = (r.flags & 16u) != 0;
+}
+
+// Barycentrics at the integer pixel corner composed with the clip barycentrics
+// (raster.rs:313-321, 334-343), as in k_raster.
+__device__ __forceinline__ void bary_at(const TriRecord& r, const BaryK& k, int x, int y, float cmp[3]) {
+    const float fx = (float)x, fy = (float)y;
+    const float s0 = fadd(fadd(fmul(fsub(k.by, fy), fadd(k.bx, fx)), k.kc0), fmul(fsub(fy, k.cy), fadd(fx, k.cx)));
+    const float s1 = fadd(fadd(fmul(fsub(fy, k.ay), fadd(fx, k.ax)), fmul(fsub(k.cy, fy), fadd(k.cx, fx))), k.kc1);
+    const float s2 = fadd(fadd(k.kc2, fmul(fsub(fy, k.by), fadd(fx, k.bx))), fmul(fsub(k.ay, fy), fadd(k.ax, fx)));
+    const float l0 = div_by_recip(s0, k.area, k.rcp, k.area_ok);
+    const float l1 = div_by_recip(s1, k.area, k.rcp, k.area_ok);
+    const float l2 = div_by_recip(s2, k.area, k.rcp, k.area_ok);
+    if (k.ident && k.area_ok && div_fast_ok(s0) && div_fast_ok(s1) && div_fast_ok(s2)) {
+        cmp[0] = l0;
+        cmp[1] = l1;
+        cmp[2] = l2;
+    } else {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) cmp[j] = fadd(fadd(fmul(r.cb[j], l0), fmul(r.cb[3 + j], l1)), fmul(r.cb[6 + j], l2));
+    }
+}
+
+__device__ __forceinline__ float frag_z(const TriRecord& r, const float cmp[3]) {  // raster.rs:345-346
+    return fadd(fadd(fmul(r.fz[0], cmp[0]), fmul(r.fz[1], cmp[1])), fmul(r.fz[2], cmp[2]));
+}
+
+// Monotone map of a float onto u32 (as integers, the keys order like the floats), -0 as +0.
+__device__ __forceinline__ uint32_t depth_order_bits(float z) {
+    const uint32_t u = __float_as_uint(z == 0.0f ? 0.0f : z);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+
+// Survivor key (smaller wins) of a fragment at depth z with order key `order`.
+__device__ __forceinline__ unsigned long long vis_key(uint32_t cmpf, float z, uint32_t order) {
+    uint32_t d = depth_order_bits(z);
+    if (cmpf == 5u || cmpf == 7u) d = ~d;                           // Greater(Equal): the deepest
+    const uint32_t o = (cmpf == 4u || cmpf == 7u) ? ~order : order;  // *Equal: the latest of a tie
+    return ((unsigned long long)d << 32) | o;
+}
+__device__ __forceinline__ uint32_t vis_order(uint32_t cmpf, unsigned long long key) {
+    const uint32_t o = (uint32_t)key;
+    return (cmpf == 4u || cmpf == 7u) ? ~o : o;
+}
+
+template <int WARPS>
+__device__ __forceinline__ void tile_sync() {
+    if constexpr (WARPS == 1) __syncwarp();
+    else __syncthreads();
+}
+
+// One CTA per tile (persistent); a CTA of one warp synchronises with __syncwarp only, so many
+// independent tiles share an SM and hide each other's memory latency.
+// Phase 1: every bin entry of the tile is rasterised by one lane (records whose tile-clipped
+// box holds at most kLanePixels pixels) or by a whole warp
+// (larger ones: lanes split the box), each covered fragment atomicMin-ing its key into the
+// tile's key array.  Phase 2: one thread per pixel re-evaluates the survivor's barycentrics,
+// tests it against the stored depth, runs the fragment stage and writes colour and depth.
+template <int T, int WARPS>
+__global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
+    constexpr int NT = WARPS * 32, NPIX = T * T;
+    constexpr int kLanePixels = 24;
+    constexpr unsigned long long kNone = ~0ull;
+    __shared__ unsigned long long s_vis[NPIX];
+    __shared__ float s_lut[256];
+    __shared__ uint32_t s_tile;
+    __shared__ unsigned long long s_frag;
+
+    const int lane = threadIdx.x & 31;
+    const bool failed = bp.status->error != 0 || *bp.abort_flag != 0;
+    if (failed && blockIdx.x == 0 && threadIdx.x == 0) *bp.abort_flag = 1u;
+    for (int i = threadIdx.x; i < 256; i += NT) s_lut[i] = fdiv((float)i, 255.0f);  // `x as f32 / 255.0`
+    if (threadIdx.x == 0) s_frag = 0;
+    const uint32_t cmpf = bp.vis_compare;
+    const RasterState* states = static_cast<const RasterState*>(bp.states);
+
+    for (;;) {
+        if (threadIdx.x == 0) s_tile = atomicAdd(bp.work_counter, 1u);
+        for (int p = threadIdx.x; p < NPIX; p += NT) s_vis[p] = kNone;
+        tile_sync<WARPS>();
+        const uint32_t tile = s_tile;
+        if (tile >= bp.total_tiles || failed) break;
+        const uint32_t ti = find_target(bp.targets, bp.num_targets, tile);
+        const TargetDesc& tg = bp.targets[ti];
+        const uint32_t lt = tile - tg.tile_base;
+        const int X0 = (int)(lt % tg.tiles_x) * T, Y0 = (int)(lt / tg.tiles_x) * T;
+        const int XE = min(X0 + T, (int)tg.width) - 1, YE = min(Y0 + T, (int)tg.height) - 1;
+        const uint32_t n = bp.tile_count[tile];
+        const uint32_t off = bp.tile_offset[tile];
+        uint32_t frag_count = 0;
+
+        auto fragment = [&](const TriRecord& r, const BaryK& k, uint32_t order, int x, int y) {
+            float cmp[3];
+            bary_at(r, k, x, y, cmp);
+            ++frag_count;
+            const float z = frag_z(r, cmp);
+            if (z != z) return;
+            atomicMin(&s_vis[(y - Y0) * T + (x - X0)], vis_key(cmpf, z, order));
+        };
+
+        // phase 1: coverage and survivor keys
+        for (uint32_t base = (threadIdx.x & ~31u); base < n; base += NT) {
+            const uint32_t i = base + lane;
+            const TriRecord* r = nullptr;
+            uint32_t key = 0;
+            int y0 = 1, y1 = 0, xl = 1, xr = 0;
+            if (i < n) {
+                key = bp.bins[off + i];
+                r = record_of(bp, key);
+                const DrawDesc& d = bp.draws[r->draw];
+                y0 = max(max(r->row0, Y0), (int)d.sc_y0);
+                y1 = min(min(r->row1, YE), (int)d.sc_y1 - 1);
+                xl = max(max(r->xmin, X0), (int)d.sc_x0);
+                xr = min(min(r->xmax, XE), (int)d.sc_x1 - 1);
+            }
+            const int box = (y1 >= y0 && xr >= xl) ? (y1 - y0 + 1) * (xr - xl + 1) : 0;
+            if (box > 0 && box <= kLanePixels) {
+                BaryK k;
+                bary_consts(*r, k);
+                for (int y = y0; y <= y1; ++y) {
+                    int x1, x2;
+                    span_at(*r, y, x1, x2);
+                    x1 = max(x1, xl);
+                    x2 = min(x2, xr);
+                    for (int x = x1; x <= x2; ++x) fragment(*r, k, key, x, y);
+                }
+            }
+            uint32_t big = __ballot_sync(0xFFFFFFFFu, box > kLanePixels);
+            while (big) {
+                const int src = __ffs(big) - 1;
+                big &= big - 1;
+                const TriRecord* br = reinterpret_cast<const TriRecord*>(
+                    __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(r), src));
+                const uint32_t bkey = __shfl_sync(0xFFFFFFFFu, key, src);
+                const int by0 = __shfl_sync(0xFFFFFFFFu, y0, src), by1 = __shfl_sync(0xFFFFFFFFu, y1, src);
+                const int bxl = __shfl_sync(0xFFFFFFFFu, xl, src), bxr = __shfl_sync(0xFFFFFFFFu, xr, src);
+                BaryK k;
+                bary_consts(*br, k);
+                const int w = bxr - bxl + 1;
+                // rows are handed to lanes in groups: lane -> (row offset, x) within the box
+                const int rows_per_pass = max(1, 32 / w);
+                const int cols = w < 32 ? w : 32;
+                const int lr = lane / cols, lc = lane - lr * cols;
+                for (int y = by0 + lr; lr < rows_per_pass && y <= by1; y += rows_per_pass) {
+                    int x1, x2;
+                    span_at(*br, y, x1, x2);
+                    x1 = max(x1, bxl);
+                    x2 = min(x2, bxr);
+                    for (int x = bxl + lc; x <= x2; x += cols)
+                        if (x >= x1) fragment(*br, k, bkey, x, y);
+                }
+            }
+        }
+        tile_sync<WARPS>();
+
+        // phase 2: the survivor of each pixel against the stored depth, fragment stage, write-back
+        uint32_t clear_c[4] = {0, 0, 0, 0};
+        encode_color(tg.color_format, V4{tg.clear[0], tg.clear[1], tg.clear[2], tg.clear[3]}, clear_c);
+        for (int p = threadIdx.x; p < NPIX; p += NT) {
+            const int x = X0 + (p % T), y = Y0 + (p / T);
+            if (x > XE || y > YE) continue;
+            const size_t pix = (size_t)y * tg.width + x;
+            const unsigned long long key = s_vis[p];
+            uint8_t* cdst = tg.color + tg.slice_offset + pix * tg.color_bpp;
+            uint32_t c[4] = {clear_c[0], clear_c[1], clear_c[2], clear_c[3]};
+            const bool load_color = tg.color_load != 1;
+            float depth = tg.depth_load != 1 ? tg.depth[pix] : tg.depth_clear;
+            bool write_color = !load_color;  // a cleared target is written even where nothing lands
+            bool write_depth = tg.depth_load == 1;
+            if (key != kNone) {
+                const TriRecord& r = *record_of(bp, vis_order(cmpf, key));
+                BaryK k;
+                bary_consts(r, k);
+                float cmp[3];
+                bary_at(r, k, x, y, cmp);
+                const float z = frag_z(r, cmp);
+                if (depth_compare(cmpf, z, depth)) {
+                    const RasterState& rs = states[r.draw];
+                    const uint32_t nvar = rs.nvar;
+                    const float* rv = rec_var(&r);
+                    float var[MAX_VARYING_FLOATS];
+                    if (rs.interp == INTERP_PERSPECTIVE) {
+                        const float den = fadd(fadd(fmul(cmp[0], r.inv_w0[0]), fmul(cmp[1], r.inv_w0[1])),
+                                               fmul(cmp[2], r.inv_w0[2]));
+#pragma unroll
+                        for (uint32_t qv = 0; qv < MAX_VARYING_FLOATS; ++qv) {
+                            if (qv >= nvar) break;
+                            float num = fmul(fmul(rv[qv], cmp[0]), r.inv_w0[0]);
+                            num = fadd(num, fmul(fmul(rv[nvar + qv], cmp[1]), r.inv_w0[1]));
+                            num = fadd(num, fmul(fmul(rv[2 * nvar + qv], cmp[2]), r.inv_w0[2]));
+                            var[qv] = fdiv(num, den);
+                        }
+                    } else {
+#pragma unroll
+                        for (uint32_t qv = 0; qv < MAX_VARYING_FLOATS; ++qv) {
+                            if (qv >= nvar) break;
+                            var[qv] = fadd(fadd(fmul(rv[qv], cmp[0]), fmul(rv[nvar + qv], cmp[1])),
+                                           fmul(rv[2 * nvar + qv], cmp[2]));
+                        }
+                    }
+                    V4 col;
+                    run_fs_rs(rs, var, s_lut, col);  // eligible programs never discard
+                    if (rs.write_mask != 0xF) {
+                        uint32_t dc[4] = {c[0], c[1], c[2], c[3]};
+                        if (load_color) {
+                            for (uint32_t q = 0; q < 4; ++q) dc[q] = 0;
+                            if (tg.color_bpp == 4) dc[0] = *reinterpret_cast<const uint32_t*>(cdst);
+                            else if (tg.color_bpp == 8) { dc[0] = reinterpret_cast<const uint32_t*>(cdst)[0]; dc[1] = reinterpret_cast<const uint32_t*>(cdst)[1]; }
+                            else if (tg.color_bpp == 16) { for (int q = 0; q < 4; ++q) dc[q] = reinterpret_cast<const uint32_t*>(cdst)[q]; }
+                            else if (tg.color_bpp == 2) dc[0] = *reinterpret_cast<const uint16_t*>(cdst);
+                            else dc[0] = *cdst;
+                        }
+                        const V4 dst = decode_color(tg.color_format, dc);
+                        if (!(rs.write_mask & 1)) col.x = dst.x;
+                        if (!(rs.write_mask & 2)) col.y = dst.y;
+                        if (!(rs.write_mask & 4)) col.z = dst.z;
+                        if (!(rs.write_mask & 8)) col.w = dst.w;
+                    }
+                    encode_color(tg.color_format, col, c);
+                    write_color = true;
+                    depth = z;
+                    write_depth = true;
+                }
+            }
+            if (write_color) {
+                if (tg.color_bpp == 4) *reinterpret_cast<uint32_t*>(cdst) = c[0];
+                else if (tg.color_bpp == 8) reinterpret_cast<uint2*>(cdst)[0] = make_uint2(c[0], c[1]);
+                else if (tg.color_bpp == 16) reinterpret_cast<uint4*>(cdst)[0] = make_uint4(c[0], c[1], c[2], c[3]);
+                else if (tg.color_bpp == 2) *reinterpret_cast<uint16_t*>(cdst) = (uint16_t)c[0];
+                else *cdst = (uint8_t)c[0];
+            }
+            if (write_depth) tg.depth[pix] = depth;
+        }
+        for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
+        if (lane == 0 && frag_count) atomicAdd(&s_frag, (unsigned long long)frag_count);
+        tile_sync<WARPS>();
+    }
+    tile_sync<WARPS>();
+    if (threadIdx.x == 0 && s_frag) atomicAdd(&bp.status->fragments, s_frag);
+}
+
+// Per-draw fragment-stage state for k_raster_vis, built once per batch.
+__global__ void k_build_states(BatchParams bp) {
+    RasterState* states = static_cast<RasterState*>(bp.states);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < bp.num_draws; i += gridDim.x * blockDim.x)
+        build_raster_state(bp.draws[i], i, states[i]);
+}
+
+}  // namespace gbr

@@ -254,7 +254,7 @@ struct Device {
 
     // worker-owned scratch
     uint64_t scratch_bytes = 0;
-    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf;
+    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf, slow_buf;
     uint32_t ovf_capacity = 4096;
     uint64_t bin_capacity = 1u << 22;
 
@@ -334,7 +334,26 @@ struct Batch {
 // to an Rgba16Float target with SrcAlpha/OneMinusSrcAlpha (alpha One/OneMinusSrcAlpha) blending and
 // no depth test; 2 = the textured Lambert program into Rgba8 with a depth test, no blending, parity
 // profile.  Every draw of the batch must qualify; otherwise 0, the generic kernel.
-int fragment_kind(const Batch& b) {
+// Visibility raster (kind 3): every target has colour and depth, and every draw writes depth
+// with one batch-wide Less / LessEqual / Greater / GreaterEqual, does not blend and runs a
+// fragment stage that never discards.  Returns the compare function, or 0.
+uint32_t visibility_compare(const Batch& b) {
+    if (b.draws.empty()) return 0;
+    for (const TargetDesc& t : b.targets)
+        if (!t.color || !t.depth) return 0;
+    const uint32_t cmp = b.draws[0].depth_compare;
+    if (cmp != GBR_COMPARE_LESS && cmp != GBR_COMPARE_LESS_EQUAL && cmp != GBR_COMPARE_GREATER &&
+        cmp != GBR_COMPARE_GREATER_EQUAL)
+        return 0;
+    for (const DrawDesc& d : b.draws)
+        if (!d.depth_test || !d.depth_write || d.depth_compare != cmp || d.blend_enabled || !d.has_fragment ||
+            d.program == PROG_MESH_COLOR_DISCARD)
+            return 0;
+    return cmp;
+}
+
+int fragment_kind(const Batch& b, bool allow_visibility) {
+    if (allow_visibility && visibility_compare(b)) return 3;
     if (b.draws.empty() || b.targets.size() != 1 || !b.targets[0].color) return 0;
     const uint32_t fmt = b.targets[0].color_format;
     bool k1 = fmt == GBR_TEXTURE_FORMAT_RGBA16_FLOAT, k2 = fmt == GBR_TEXTURE_FORMAT_RGBA8_UNORM ||
@@ -370,7 +389,8 @@ uint64_t log2_bucket(uint64_t v) {
 uint64_t Device::tuner_signature(const Batch& b) const {
     uint64_t pixels = 0;
     for (const TargetDesc& t : b.targets) pixels += (uint64_t)t.width * t.height;
-    return ((uint64_t)fragment_kind(b) << 48) | (log2_bucket(b.total_prims + 1) << 32) |
+    return ((uint64_t)fragment_kind(b, cfg.raster_order == GBR_RASTER_AUTO) << 48) |
+           (log2_bucket(b.total_prims + 1) << 32) |
            (log2_bucket(pixels + 1) << 16) | log2_bucket(b.targets.size());
 }
 int Device::tuner_pick(const Batch& b, int* t, int* w) {
@@ -550,6 +570,7 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
         d.write_mask = ct.write_mask & 0xF;
     }
     for (int k = 0; k < 4; ++k) d.blend_constant[k] = (float)dc.blend_constant[k];
+    d.fast_vs = fast_vs_kind(d);
     return d;
 }
 
@@ -769,11 +790,17 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
     auto align = [](size_t v) { return (v + 255) & ~size_t(255); };
     size_t off_status = 256, off_work = align(off_status + nb * sizeof(BatchStatus));
     size_t off_desc = align(off_work + nb * sizeof(uint32_t) * 4);
-    std::vector<size_t> desc_off(nb);
+    std::vector<size_t> desc_off(nb), states_off(nb, 0);
+    std::vector<int> kinds(nb);
     size_t cur = off_desc;
     for (size_t i = 0; i < nb; ++i) {
+        kinds[i] = fragment_kind(batches[i], cfg.raster_order == GBR_RASTER_AUTO);
         desc_off[i] = cur;
         cur = align(cur + batches[i].draws.size() * sizeof(DrawDesc) + batches[i].targets.size() * sizeof(TargetDesc));
+        if (kinds[i] == 3) {
+            states_off[i] = cur;
+            cur = align(cur + batches[i].draws.size() * raster_state_bytes());
+        }
     }
     std::vector<uint8_t> host_meta(cur, 0);
     for (size_t i = 0; i < nb; ++i) {
@@ -792,7 +819,7 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
     rec.ev_start = ev0;
     rec.ev_end = ev1;
     uint32_t launches = 0;
-    uint64_t fragments = 0;
+    uint64_t fragments = 0, slow_prims = 0;
     size_t first_batch = 0;
     std::vector<BatchStatus> st(nb);
     std::vector<cudaEvent_t> rev;  // raster kernel events (time_kernels)
@@ -818,6 +845,7 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
             max_tiles = std::max(max_tiles, batches[i].total_tiles);
         }
         records_buf.ensure((size_t)std::max(1u, max_prims) * max_stride, &scratch_bytes);
+        slow_buf.ensure((size_t)std::max(1u, max_prims) * sizeof(uint32_t), &scratch_bytes);
         ovf_buf.ensure((size_t)ovf_capacity * max_stride, &scratch_bytes);
         tiles_buf.ensure((size_t)(max_tiles + 1) * 3 * sizeof(uint32_t) + 64, &scratch_bytes);
         bins_buf.ensure((size_t)bin_capacity * sizeof(uint32_t), &scratch_bytes);
@@ -845,6 +873,7 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
             bp.record_stride = (uint32_t)((sizeof(TriRecord) + 3 * b.nvar * sizeof(float) + 15) & ~size_t(15));
             bp.num_varyings = b.nvar;
             bp.records = static_cast<uint8_t*>(records_buf.ptr);
+            bp.slow_prims = static_cast<uint32_t*>(slow_buf.ptr);
             bp.ovf_records = static_cast<uint8_t*>(ovf_buf.ptr);
             bp.ovf_capacity = ovf_capacity;
             bp.bin_capacity = (uint32_t)std::min<uint64_t>(bin_capacity, 0xFFFFFFFFull);
@@ -856,8 +885,12 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
             bp.work_counter = reinterpret_cast<uint32_t*>(meta + off_work) + i * 4;
             bp.status = reinterpret_cast<BatchStatus*>(meta + off_status) + i;
             bp.abort_flag = reinterpret_cast<uint32_t*>(meta);
+            if (kinds[i] == 3) {
+                bp.states = meta + states_off[i];
+                bp.vis_compare = visibility_compare(b);
+            }
             cuda_check(launch_batch(bp, btile[i], bwarps[i], num_sms, stream, &launches,
-                                    revp->empty() ? nullptr : &(*revp)[2 * i], fragment_kind(b)),
+                                    revp->empty() ? nullptr : &(*revp)[2 * i], kinds[i]),
                        "launch");
         }
         };
@@ -867,7 +900,7 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
             for (size_t i = 0; i < nb; ++i) {
                 key.append(reinterpret_cast<const char*>(&btile[i]), sizeof(int));
                 key.append(reinterpret_cast<const char*>(&bwarps[i]), sizeof(int));
-                const int kind = fragment_kind(batches[i]);
+                const int kind = kinds[i];
                 key.append(reinterpret_cast<const char*>(&kind), sizeof(int));
                 key.append(reinterpret_cast<const char*>(&batches[i].total_prims), sizeof(uint32_t));
                 key.append(reinterpret_cast<const char*>(&batches[i].total_tiles), sizeof(uint32_t));
@@ -876,7 +909,7 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
                 key.append(reinterpret_cast<const char*>(&nd), sizeof nd);
                 key.append(reinterpret_cast<const char*>(&nt), sizeof nt);
             }
-            const void* ptrs[6] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, nullptr};
+            const void* ptrs[6] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, slow_buf.ptr};
             key.append(reinterpret_cast<const char*>(ptrs), sizeof ptrs);
             key.append(reinterpret_cast<const char*>(&ovf_capacity), sizeof ovf_capacity);
             key.append(reinterpret_cast<const char*>(&bin_capacity), sizeof bin_capacity);
@@ -913,7 +946,8 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
                 }
             } else {
                 revp = &g.events;
-                for (size_t i = first_batch; i < nb; ++i) launches += 2 + (batches[i].total_prims ? 2 : 0);
+                for (size_t i = first_batch; i < nb; ++i)
+                    launches += batch_kernel_launches(batches[i].total_prims, btile[i], bwarps[i], kinds[i]);
             }
             cuda_check(cudaGraphLaunch(graphs[key].exec, stream), "cudaGraphLaunch");
         } else {
@@ -933,6 +967,7 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
             }
         for (size_t i = first_batch; i < (bad == nb ? nb : bad); ++i) {
             fragments += st[i].fragments;
+            slow_prims += st[i].slow_count;
             if (!revp->empty()) {
                 float ms = 0.0f;
                 if (cudaEventElapsedTime(&ms, (*revp)[2 * i], (*revp)[2 * i + 1]) == cudaSuccess) {
@@ -966,6 +1001,7 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
     rec.stats.fragments_shaded = fragments;
     rec.stats.kernel_launches = launches;
     rec.stats.raster_ms = raster_ms;
+    rec.stats.generic_setup_prims = (uint32_t)std::min<uint64_t>(slow_prims, 0xFFFFFFFFu);
 }
 
 // ---------------------------------------------------------------- command decoding
@@ -1176,6 +1212,7 @@ GBR_API gbr_status gbr_device_create(const gbr_device_config* cfg, gbr_device* o
         if (cfg->bin_capacity) d->bin_capacity = cfg->bin_capacity;
         d->autotune = cfg->tile_size == 0 && cfg->warps_per_tile == 0;
         if (cfg->launch_mode > GBR_LAUNCH_PER_PASS) fail(GBR_ERR_INVALID_ARGUMENT, "launch_mode");
+        if (cfg->raster_order > GBR_RASTER_ORDERED) fail(GBR_ERR_INVALID_ARGUMENT, "raster_order");
         cuda_check(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         Device* raw = d.get();
         d->worker = std::thread([raw] { raw->worker_main(); });
@@ -1215,6 +1252,7 @@ GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
         d->graphs.clear();
         d->objects.clear();
         d->records_buf.release();
+        d->slow_buf.release();
         d->ovf_buf.release();
         d->tiles_buf.release();
         d->bins_buf.release();

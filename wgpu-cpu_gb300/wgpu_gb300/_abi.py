@@ -50,7 +50,8 @@ u32, u64, i32, f32, f64 = C.c_uint32, C.c_uint64, C.c_int32, C.c_float, C.c_doub
 class DeviceConfig(C.Structure):
     _fields_ = [("abi_version", u32), ("profile", u32), ("device_ordinal", u32), ("tile_size", u32),
                 ("bin_capacity", u32), ("warps_per_tile", u32), ("launch_mode", u32), ("batch_submissions", u32),
-                ("use_graphs", u32), ("time_kernels", u32), ("hbm_budget_bytes", u64), ("reserved", u64 * 4)]
+                ("use_graphs", u32), ("time_kernels", u32), ("hbm_budget_bytes", u64), ("raster_order", u32),
+                ("_pad0", u32), ("reserved", u64 * 3)]
 
 
 class Limits(C.Structure):
@@ -126,7 +127,7 @@ class BindGroupDesc(C.Structure):
 class SubmissionStats(C.Structure):
     _fields_ = [("submission_index", u64), ("draws", u64), ("primitives_in", u64), ("fragments_shaded", u64),
                 ("kernel_launches", u64), ("queue_wait_ms", f64), ("gpu_ms", f64), ("submit_to_fence_ms", f64),
-                ("batched_with", u32), ("_pad", u32), ("raster_ms", f64)]
+                ("batched_with", u32), ("generic_setup_prims", u32), ("raster_ms", f64)]
 
 
 class CmdHeader(C.Structure):

@@ -138,6 +138,11 @@ class LaunchMode:
     PER_PASS = 2
 
 
+class RasterOrder:
+    AUTO = 0
+    ORDERED = 1
+
+
 class BindingKind:
     BUFFER = 0
     SAMPLER = 1
@@ -444,7 +449,7 @@ class Device:
     def __init__(self, lib: Optional[A.Lib] = None, profile: int = Profile.PARITY, tile_size: int = 0,
                  warps_per_tile: int = 0, bin_capacity: int = 0, launch_mode: int = LaunchMode.BATCHED,
                  batch_submissions: bool = False, use_graphs: bool = False, hbm_budget_bytes: int = 0,
-                 device_ordinal: int = 0, time_kernels: bool = False):
+                 device_ordinal: int = 0, time_kernels: bool = False, raster_order: int = 0):
         self.lib = lib if lib is not None else gpu_lib()
         cfg = A.DeviceConfig()
         cfg.abi_version = A.GBR_ABI_VERSION
@@ -458,6 +463,7 @@ class Device:
         cfg.use_graphs = int(use_graphs)
         cfg.time_kernels = int(time_kernels)
         cfg.hbm_budget_bytes = hbm_budget_bytes
+        cfg.raster_order = int(raster_order)
         h = C.c_uint64()
         self.handle = 0
         _check(self.lib, self.lib.device_create(C.byref(cfg), C.byref(h)))
