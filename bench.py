@@ -371,6 +371,83 @@ def run_ours(args, wk: Workload):
         torch.distributed.destroy_process_group()
 
 
+def serve_arm(dev, sset, lam, duration, seed, max_submissions):
+    """Poisson arrivals at `lam`/s for `duration` s (at most max_submissions), cycling through the
+    pre-recorded submissions; waits for the last one.  Returns per-submission stats and the wall
+    time from the first submit to the last fence."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / lam, size=max_submissions)
+    arrivals = np.cumsum(gaps)
+    arrivals = arrivals[arrivals < duration]
+    subs = []
+    t0 = time.perf_counter()
+    for k, ta in enumerate(arrivals):
+        while True:
+            now = time.perf_counter() - t0
+            if now >= ta:
+                break
+            if ta - now > 0.0005:
+                time.sleep(min(ta - now - 0.0003, 0.002))
+        subs.append(dev.queue.submit([sset.commands[k % len(sset.commands)]]))
+    dev.poll(True, subs[-1])
+    wall = time.perf_counter() - t0
+    return [dev.submission_stats(i) for i in subs], wall
+
+
+def serve_summary(stats, wall, lam, duration):
+    lat = np.array([s.submit_to_fence_ms for s in stats])
+    frags = int(sum(s.fragments_shaded for s in stats))
+    return {"lambda_per_s": lam, "arrival_window_s": duration, "submissions": len(stats),
+            "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "mean_ms": float(lat.mean()), "frames_per_s": len(stats) / wall, "fragments_per_s": frags / wall,
+            "fragments": frags, "wall_s": wall, "mean_batched_with": float(np.mean([s.batched_with for s in stats])),
+            "kernel_launches": int(sum(s.kernel_launches / max(1, s.batched_with) for s in stats))}
+
+
+def run_serve(args):
+    """Serving loop: Poisson arrivals of pre-recorded submissions over resident meshes, textures and
+    targets; the batched server (continuous batching, HBM-budget admission) and, on the same
+    arrival stream, the plain per-draw path."""
+    import torch
+
+    from wgpu_gb300 import api as W
+    from wgpu_gb300 import workloads as wl
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    lam, duration = args.rate, args.duration
+    arms = {}
+    for name, kw in (("served", dict(batch_submissions=True, launch_mode=W.LaunchMode.BATCHED)),
+                     ("per_draw", dict(batch_submissions=False, launch_mode=W.LaunchMode.PER_DRAW))):
+        dev = W.Device(device_ordinal=local, tile_size=16, warps_per_tile=2, hbm_budget_bytes=80 << 30, **kw)
+        sset = wl.serving_set(dev)
+        for c in sset.commands[:8]:  # warm-up (allocations, first launches)
+            dev.poll(True, dev.queue.submit([c]))
+        with ClockSampler(local) as clocks:
+            stats, wall = serve_arm(dev, sset, lam, duration, seed=11, max_submissions=int(lam * duration * 2) + 16)
+        arms[name] = serve_summary(stats, wall, lam, duration)
+        arms[name]["clocks"] = clocks.summary()
+        dev.close()
+        del sset
+    s = arms["served"]
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": s["fragments_per_s"] * world, "unit": UNIT, "n_gpus": world,
+            "steps": s["submissions"], "warmup": 8, "ms_per_step": s["mean_ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": "serving: Poisson arrivals of submissions with 1-64 draws (log-uniform) of 512 "
+                                   "resident meshes (100..200k tris) and 128 textures into 256^2..1920x1080 "
+                                   "Rgba8Unorm + Depth32Float targets, textured Lambert / vertex colour",
+                       "lambda_per_s": lam, "hbm_budget_gb": 80, "launch_mode": "batched + merged submissions",
+                       "l2": "not flushed (inputs resident; a step is one submission)"},
+            "serving": s, "per_draw_path": arms["per_draw"],
+            "e2e": {"value": s["fragments_per_s"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
+                    "note": "wall clock from first submit to last fence through the C ABI; inputs resident"},
+            "gpu_launches": s["kernel_launches"], "clocks": s["clocks"],
+        }
+        print(json.dumps(line), flush=True)
+
+
 def dev_tile(args):
     return args.tile or 16
 
@@ -385,7 +462,9 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="textured", choices=["textured", "blend", "colored", "batched"])
+    ap.add_argument("--workload", default="batched", choices=["textured", "blend", "colored", "batched", "serve"])
+    ap.add_argument("--rate", type=float, default=1000.0, help="serve workload: submissions per second")
+    ap.add_argument("--duration", type=float, default=2.0, help="serve workload: arrival window in seconds")
     ap.add_argument("--launch-mode", default="batched", choices=list(LAUNCH_MODES))
     ap.add_argument("--graphs", action="store_true", help="replay each submission's launches from a CUDA graph")
     ap.add_argument("--autotune", action="store_true", help="let the device time tile shapes (tile/warps ignored)")
@@ -402,6 +481,13 @@ def main():
         args.tile = args.warps = 0
     elif not args.tile:
         args.tile, args.warps = dev_tile(args), dev_warps(args)
+    if args.workload == "serve":
+        if args.impl == "reference":
+            wk = workloads()["batched"]
+            run_reference(args, wk)
+        else:
+            run_serve(args)
+        return
     wk = workloads()[args.workload]
     if args.impl == "reference":
         run_reference(args, wk)

@@ -83,7 +83,8 @@ struct TargetDesc {
     uint32_t tiles_x, tiles_y;
     uint32_t tile_base;    // first global tile id of this target
     uint32_t slice_offset; // byte offset of the depth_slice layer
-    uint32_t _pad[3];
+    uint32_t _pad;
+    unsigned long long* frag_count;  // fragments shaded into this target are added here (or null)
 };
 
 // One draw call of a batch, fully resolved on the host.

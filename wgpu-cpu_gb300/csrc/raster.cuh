@@ -841,7 +841,8 @@ __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
 }
 
 __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
-    if (bp.status->error) return;
+    // after an abort the setup kernels returned early: the records are not this batch's
+    if (bp.status->error || *bp.abort_flag) return;
     const uint32_t n_ovf = min(bp.status->ovf_used, bp.ovf_capacity);
     const uint32_t total = bp.total_prims + n_ovf;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -1352,7 +1353,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
             if (tg.depth) tg.depth[pix] = px[k].depth;
         }
         for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
-        if (lane == 0 && frag_count) atomicAdd(&s_frag, (unsigned long long)frag_count);
+        if (lane == 0 && frag_count) {
+            atomicAdd(&s_frag, (unsigned long long)frag_count);
+            if (tg.frag_count) atomicAdd(tg.frag_count, (unsigned long long)frag_count);
+        }
         __syncthreads();
     }
     __syncthreads();

@@ -288,7 +288,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
             if (write_depth) tg.depth[pix] = depth;
         }
         for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
-        if (lane == 0 && frag_count) atomicAdd(&s_frag, (unsigned long long)frag_count);
+        if (lane == 0 && frag_count) {
+            atomicAdd(&s_frag, (unsigned long long)frag_count);
+            if (tg.frag_count) atomicAdd(tg.frag_count, (unsigned long long)frag_count);
+        }
         tile_sync<WARPS>();
     }
     tile_sync<WARPS>();

@@ -199,11 +199,40 @@ struct Item {
     uint32_t merged = 0;  // submissions executed together with this one (serving mode)
 };
 
+// Start / end events of a launch sequence, shared by the submissions it ran.
+struct EventPair {
+    cudaEvent_t start = nullptr, end = nullptr;
+    EventPair() = default;
+    EventPair(const EventPair&) = delete;
+    EventPair& operator=(const EventPair&) = delete;
+    ~EventPair() {
+        if (start) cudaEventDestroy(start);
+        if (end) cudaEventDestroy(end);
+    }
+};
+
 struct SubmissionRecord {
     gbr_submission_stats stats{};
     gbr_status status = GBR_OK;
     std::string error;
-    cudaEvent_t ev_start = nullptr, ev_end = nullptr;
+    std::shared_ptr<EventPair> ev;
+};
+
+// Outcome of run_batches: the first batch that failed validation on the device (or the batch
+// count), its error code and message.
+struct RunResult {
+    size_t bad;
+    uint32_t error;
+    std::string msg;
+};
+
+// What the launches of one submission group accumulate.
+struct GroupRun {
+    std::shared_ptr<EventPair> ev;
+    bool started = false;
+    uint32_t launches = 0;
+    uint64_t slow_prims = 0;
+    double raster_ms = 0.0;
 };
 
 // ---------------------------------------------------------------- scratch (grow-only)
@@ -279,8 +308,11 @@ struct Device {
     std::map<std::string, GraphEntry> graphs;
     uint64_t graph_clock = 0;
 
-    std::vector<Batch> plan_batches(const std::vector<PassCmd>& passes, uint64_t* draws, uint64_t* prims_in);
-    void launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec);
+    std::vector<Batch> plan_batches(const std::vector<PassCmd>& passes, uint64_t* draws, uint64_t* prims_in,
+                                    uint32_t item);
+    bool merge_batch(Batch& into, Batch& b);
+    std::vector<Batch> split_batch(const Batch& m);
+    RunResult run_batches(std::vector<Batch>& batches, size_t from, GroupRun& run);
 
     template <class T>
     std::shared_ptr<T> get(uint64_t h, const char* what) {
@@ -309,7 +341,8 @@ struct Device {
     }
     void worker_main();
     void execute(Item& it);
-    void execute_submission(Item& it, SubmissionRecord& rec);
+    void execute_group(std::vector<Item>& items);
+    void note_failure(const Failure& f);
 };
 
 std::mutex g_dev_mu;
@@ -327,13 +360,14 @@ std::shared_ptr<Device> get_device(gbr_device d) {
 struct Batch {
     std::vector<DrawDesc> draws;
     std::vector<TargetDesc> targets;
+    std::vector<uint32_t> target_item;       // submission (index in its group) of each target
+    std::vector<const Texture*> writes, reads;  // attachments written, textures sampled
+    std::vector<uint64_t> target_frags;      // fragments shaded into each target (after the run)
     uint32_t total_prims = 0, total_tiles = 0, nvar = 0;
+    uint32_t item = 0;         // the submission of a single-submission batch
+    bool single_item = true;
 };
 
-// Which specialised raster kernel can run a batch (kernels.h): 1 = a vec4f colour passed straight
-// to an Rgba16Float target with SrcAlpha/OneMinusSrcAlpha (alpha One/OneMinusSrcAlpha) blending and
-// no depth test; 2 = the textured Lambert program into Rgba8 with a depth test, no blending, parity
-// profile.  Every draw of the batch must qualify; otherwise 0, the generic kernel.
 // Visibility raster (kind 3): every target has colour and depth, and every draw writes depth
 // with one batch-wide Less / LessEqual / Greater / GreaterEqual, does not blend and runs a
 // fragment stage that never discards.  Returns the compare function, or 0.
@@ -352,6 +386,11 @@ uint32_t visibility_compare(const Batch& b) {
     return cmp;
 }
 
+// Which raster kernel runs a batch (kernels.h): 3 = the visibility raster (above) when allowed;
+// 1 = a vec4f colour passed straight to an Rgba16Float target with SrcAlpha/OneMinusSrcAlpha
+// (alpha One/OneMinusSrcAlpha) blending and no depth test; 2 = the textured Lambert program into
+// Rgba8 with a depth test, no blending, parity profile.  Every draw of the batch must qualify;
+// otherwise 0, the generic ordered kernel.
 int fragment_kind(const Batch& b, bool allow_visibility) {
     if (allow_visibility && visibility_compare(b)) return 3;
     if (b.draws.empty() || b.targets.size() != 1 || !b.targets[0].color) return 0;
@@ -575,25 +614,40 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
 }
 
 // ---------------------------------------------------------------- worker
+uint64_t submission_estimate(const Item& it);
+constexpr size_t kMaxGroup = 256;  // submissions merged into one launch at most
+
 void Device::worker_main() {
     cudaSetDevice(ordinal);
     for (;;) {
-        Item it;
+        std::vector<Item> group;
         {
             std::unique_lock<std::mutex> lk(q_mu);
             q_cv.wait(lk, [&] { return stopping || !queue.empty(); });
             if (queue.empty() && stopping) return;
-            it = std::move(queue.front());
+            group.push_back(std::move(queue.front()));
             queue.pop_front();
+            // continuous batching: the submissions queued behind this one join its launch while
+            // their expected transient memory fits the HBM budget (the rest wait for the next)
+            if (group[0].kind == Item::SUBMIT && cfg.batch_submissions) {
+                const uint64_t budget = cfg.hbm_budget_bytes ? cfg.hbm_budget_bytes : (80ull << 30);
+                uint64_t est = submission_estimate(group[0]);
+                while (!queue.empty() && queue.front().kind == Item::SUBMIT && group.size() < kMaxGroup) {
+                    const uint64_t e = submission_estimate(queue.front());
+                    if (est + e > budget) break;
+                    est += e;
+                    group.push_back(std::move(queue.front()));
+                    queue.pop_front();
+                }
+            }
         }
-        execute(it);
+        if (group[0].kind == Item::SUBMIT) execute_group(group);
+        else execute(group[0]);
     }
 }
 
 void Device::execute(Item& it) {
     Failure err{GBR_OK, ""};
-    SubmissionRecord rec;
-    bool is_submit = it.kind == Item::SUBMIT;
     try {
         if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
         switch (it.kind) {
@@ -631,52 +685,187 @@ void Device::execute(Item& it) {
                 flush_buf.ensure(256ull << 20, &scratch_bytes);
                 cuda_check(cudaMemsetAsync(flush_buf.ptr, (int)(it.offset & 0xFF), flush_buf.size, stream), "flush");
                 break;
-            case Item::SUBMIT: execute_submission(it, rec); break;
+            case Item::SUBMIT: break;  // submissions run through execute_group
         }
     } catch (const Failure& f) {
         err = f;
-        cudaError_t ce = cudaGetLastError();
-        if (f.status == GBR_ERR_CUDA || ce != cudaSuccess) {
-            std::lock_guard<std::mutex> lk(q_mu);
-            lost = true;
-            lost_msg = f.msg;
-        }
+        note_failure(f);
     }
     if (it.done) it.done->set_value(err);
-    if (is_submit) {
+}
+
+void Device::note_failure(const Failure& f) {
+    cudaError_t ce = cudaGetLastError();
+    if (f.status == GBR_ERR_CUDA || f.status == GBR_ERR_DEVICE_LOST || ce != cudaSuccess) {
         std::lock_guard<std::mutex> lk(q_mu);
-        rec.stats.submission_index = it.index;
-        rec.stats.submit_to_fence_ms = ms_between(it.t_submit, Clock::now());
-        if (err.status != GBR_OK) {
-            rec.status = err.status;
-            rec.error = err.msg;
-        }
-        auto& slot = records[it.index];
-        if (slot.ev_start) cudaEventDestroy(slot.ev_start);
-        if (slot.ev_end) cudaEventDestroy(slot.ev_end);
-        slot = rec;
-        completed_submissions = it.index + 1;
-        // keep the last 4096 records
-        while (records.size() > 4096) {
-            auto f = records.begin();
-            if (f->second.ev_start) cudaEventDestroy(f->second.ev_start);
-            if (f->second.ev_end) cudaEventDestroy(f->second.ev_end);
-            records.erase(f);
-        }
-        done_cv.notify_all();
+        lost = true;
+        if (lost_msg.empty()) lost_msg = f.msg;
     }
 }
 
-void Device::execute_submission(Item& it, SubmissionRecord& rec) {
+// Transient device memory a submission is expected to need (records, bins, tile arrays):
+// what admission counts against the HBM budget.
+uint64_t submission_estimate(const Item& it) {
+    uint64_t prims = 0, pixels = 0;
+    for (const PassCmd& p : it.passes) {
+        pixels += (uint64_t)p.width * p.height;
+        for (const DrawCmd& dc : p.draws) {
+            const uint64_t cnt = dc.end > dc.start ? dc.end - dc.start : 0;
+            prims += (cnt / 3 + 2) * (dc.inst_end > dc.inst_start ? dc.inst_end - dc.inst_start : 0);
+        }
+    }
+    return prims * 512 + pixels / 16 + 4096;
+}
+
+// A run of submissions executed together (one, unless the config merges queued submissions).
+// Each is planned on its own, so a submission that fails validation fails alone; submissions
+// that plan to a single batch are merged into one launch batch while no pass of one writes a
+// texture another reads or writes; the group's batches are launched back to back and every
+// submission gets its own record (fragments counted per target on the device).
+void Device::execute_group(std::vector<Item>& items) {
+    const size_t n = items.size();
+    std::vector<SubmissionRecord> recs(n);
     const auto t_start = Clock::now();
-    rec.stats.queue_wait_ms = ms_between(it.t_submit, t_start);
-    uint64_t draws = 0, prims_in = 0;
-    std::vector<Batch> batches = plan_batches(it.passes, &draws, &prims_in);
-    rec.stats.draws = draws;
-    rec.stats.primitives_in = prims_in;
-    rec.stats.batched_with = it.merged ? it.merged : 1;
-    if (batches.empty()) return;
-    launch_batches(batches, rec);
+    auto fail_item = [&](size_t i, gbr_status st, const std::string& msg) {
+        if (recs[i].status == GBR_OK) {
+            recs[i].status = st;
+            recs[i].error = msg;
+        }
+    };
+    std::vector<Batch> batches;
+    GroupRun run;
+    try {
+        if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
+        bool open = false;  // the last batch accepts another single-batch submission
+        for (size_t i = 0; i < n; ++i) {
+            recs[i].stats.queue_wait_ms = ms_between(items[i].t_submit, t_start);
+            recs[i].stats.batched_with = (uint32_t)n;
+            std::vector<Batch> own;
+            try {
+                uint64_t draws = 0, prims = 0;
+                own = plan_batches(items[i].passes, &draws, &prims, (uint32_t)i);
+                recs[i].stats.draws = draws;
+                recs[i].stats.primitives_in = prims;
+            } catch (const Failure& f) {
+                fail_item(i, f.status, f.msg);
+                continue;
+            }
+            const bool single = own.size() == 1;
+            if (single && open && merge_batch(batches.back(), own[0])) continue;
+            for (Batch& b : own) batches.push_back(std::move(b));
+            open = single && cfg.batch_submissions && cfg.launch_mode == GBR_LAUNCH_BATCHED;
+        }
+        size_t from = 0;
+        while (from < batches.size()) {
+            const RunResult r = run_batches(batches, from, run);
+            if (r.bad == batches.size()) break;
+            Batch& bad = batches[r.bad];
+            std::vector<uint32_t> its;
+            for (uint32_t ti : bad.target_item)
+                if (std::find(its.begin(), its.end(), ti) == its.end()) its.push_back(ti);
+            if (its.size() > 1) {
+                // a merged batch failed: run its submissions' parts separately to find the culprit
+                std::vector<Batch> parts = split_batch(bad);
+                batches.erase(batches.begin() + (ptrdiff_t)r.bad);
+                batches.insert(batches.begin() + (ptrdiff_t)r.bad, std::make_move_iterator(parts.begin()),
+                               std::make_move_iterator(parts.end()));
+                from = r.bad;
+                continue;
+            }
+            const uint32_t culprit = its.empty() ? bad.item : its[0];
+            fail_item(culprit, GBR_ERR_VALIDATION, r.msg);
+            // the failed submission's later batches do not run
+            size_t k = r.bad + 1;
+            while (k < batches.size() && batches[k].item == culprit && batches[k].single_item) batches.erase(batches.begin() + (ptrdiff_t)k);
+            from = r.bad + 1;
+        }
+    } catch (const Failure& f) {
+        note_failure(f);
+        for (size_t i = 0; i < n; ++i) fail_item(i, f.status, f.msg);
+    }
+    // per-submission fragment counts from the per-target counters
+    std::vector<uint64_t> frags(n, 0);
+    for (const Batch& b : batches)
+        for (size_t t = 0; t < b.target_item.size() && t < b.target_frags.size(); ++t) frags[b.target_item[t]] += b.target_frags[t];
+    float group_ms = 0.0f;
+    if (run.ev && run.started) cudaEventElapsedTime(&group_ms, run.ev->start, run.ev->end);
+    std::lock_guard<std::mutex> lk(q_mu);
+    for (size_t i = 0; i < n; ++i) {
+        SubmissionRecord& rec = recs[i];
+        rec.stats.submission_index = items[i].index;
+        rec.stats.submit_to_fence_ms = ms_between(items[i].t_submit, Clock::now());
+        rec.stats.fragments_shaded = rec.status == GBR_OK ? frags[i] : 0;
+        rec.stats.kernel_launches = run.launches;
+        rec.stats.gpu_ms = group_ms;
+        rec.stats.raster_ms = run.raster_ms;
+        rec.stats.generic_setup_prims = (uint32_t)std::min<uint64_t>(run.slow_prims, 0xFFFFFFFFu);
+        rec.ev = run.started ? run.ev : nullptr;
+        records[items[i].index] = rec;
+        completed_submissions = std::max(completed_submissions, items[i].index + 1);
+    }
+    while (records.size() > 4096) records.erase(records.begin());
+    done_cv.notify_all();
+}
+
+// Appends single-submission batch `b` to batch `into` when no pass of one touches a texture the
+// other writes and the primitive ids still fit; returns false (nothing changed) otherwise.
+bool Device::merge_batch(Batch& into, Batch& b) {
+    auto has = [](const std::vector<const Texture*>& v, const Texture* t) {
+        return t && std::find(v.begin(), v.end(), t) != v.end();
+    };
+    for (const Texture* t : b.writes)
+        if (has(into.writes, t) || has(into.reads, t)) return false;
+    for (const Texture* t : b.reads)
+        if (has(into.writes, t)) return false;
+    const uint64_t kMaxPrims = (1ull << (32 - SUBTRI_BITS)) - 1;
+    if ((uint64_t)into.total_prims + b.total_prims > kMaxPrims) return false;
+    const uint32_t tbase = (uint32_t)into.targets.size();
+    for (DrawDesc d : b.draws) {
+        d.prim_base += into.total_prims;
+        d.target += tbase;
+        into.draws.push_back(d);
+    }
+    into.targets.insert(into.targets.end(), b.targets.begin(), b.targets.end());
+    into.target_item.insert(into.target_item.end(), b.target_item.begin(), b.target_item.end());
+    into.writes.insert(into.writes.end(), b.writes.begin(), b.writes.end());
+    into.reads.insert(into.reads.end(), b.reads.begin(), b.reads.end());
+    into.total_prims += b.total_prims;
+    into.nvar = std::max(into.nvar, b.nvar);
+    into.single_item = false;
+    return true;
+}
+
+// The per-submission batches a merged batch was made of.
+std::vector<Batch> Device::split_batch(const Batch& m) {
+    std::vector<Batch> out;
+    std::vector<int> item_batch;
+    std::vector<uint32_t> new_target(m.targets.size());
+    for (size_t t = 0; t < m.targets.size(); ++t) {
+        const uint32_t it = m.target_item[t];
+        size_t k = 0;
+        while (k < out.size() && out[k].item != it) ++k;
+        if (k == out.size()) {
+            out.emplace_back();
+            out.back().item = it;
+            out.back().single_item = true;
+        }
+        new_target[t] = (uint32_t)out[k].targets.size();
+        out[k].targets.push_back(m.targets[t]);
+        out[k].target_item.push_back(it);
+    }
+    for (const DrawDesc& d0 : m.draws) {
+        const uint32_t it = m.target_item[d0.target];
+        size_t k = 0;
+        while (out[k].item != it) ++k;
+        DrawDesc d = d0;
+        const uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
+        d.prim_base = out[k].total_prims;
+        d.target = new_target[d0.target];
+        out[k].total_prims += (uint32_t)np;
+        out[k].nvar = std::max(out[k].nvar, d.num_varyings);
+        out[k].draws.push_back(d);
+    }
+    return out;
 }
 
 // Splits a list of render passes into launch batches.
@@ -685,23 +874,25 @@ void Device::execute_submission(Item& it, SubmissionRecord& rec) {
 //  BATCHED   consecutive passes share a batch until one would touch a texture an earlier pass of
 //            the batch writes (as an attachment) or reads (as a bound texture), or write one it
 //            reads — so no batch contains a dependency between its passes.
-std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint64_t* draws, uint64_t* prims_in) {
+std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint64_t* draws, uint64_t* prims_in,
+                                        uint32_t item) {
     const uint32_t profile = cfg.profile;
     std::vector<Batch> batches;
-    std::vector<const Texture*> written, read;
     bool open = false;
-    auto close = [&] {
-        open = false;
-        written.clear();
-        read.clear();
-    };
     auto has = [](const std::vector<const Texture*>& v, const Texture* t) {
         return t && std::find(v.begin(), v.end(), t) != v.end();
     };
+    auto new_batch = [&]() -> Batch& {
+        batches.emplace_back();
+        batches.back().item = item;
+        batches.back().single_item = true;
+        return batches.back();
+    };
     for (const PassCmd& p : passes) {
         if (p.width == 0 || p.height == 0) continue;
-        std::vector<const Texture*> p_write = {p.color.get(), p.depth.get()};
-        std::vector<const Texture*> p_read;
+        std::vector<const Texture*> p_write, p_read;
+        if (p.color) p_write.push_back(p.color.get());
+        if (p.depth) p_write.push_back(p.depth.get());
         for (const DrawCmd& dc : p.draws)
             for (const auto& g : dc.groups)
                 if (g)
@@ -716,12 +907,15 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
         }
         const uint64_t kMaxPrims = (1ull << (32 - SUBTRI_BITS)) - 1;
         if (cfg.launch_mode == GBR_LAUNCH_PER_DRAW && !p.draws.empty()) {
-            close();
+            open = false;
             bool first = true;
             for (const DrawCmd& dc : p.draws) {
                 ++*draws;
-                Batch b;
+                Batch& b = new_batch();
                 b.targets.push_back(make_target(p, first, tile, profile));
+                b.target_item.push_back(item);
+                b.writes = p_write;
+                b.reads = p_read;
                 first = false;
                 DrawDesc d = make_draw(dc, profile, (bool)p.depth);
                 uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
@@ -730,22 +924,24 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
                 b.total_prims = (uint32_t)np;
                 b.nvar = d.num_varyings;
                 if (np) b.draws.push_back(d);
-                batches.push_back(std::move(b));
             }
             continue;
         }
         bool conflict = !open || cfg.launch_mode == GBR_LAUNCH_PER_PASS;
-        for (const Texture* t : p_write) conflict = conflict || has(written, t) || has(read, t);
-        for (const Texture* t : p_read) conflict = conflict || has(written, t);
-        if (!conflict && (uint64_t)batches.back().total_prims + p_prims > kMaxPrims) conflict = true;
+        if (!conflict) {
+            const Batch& cur = batches.back();
+            for (const Texture* t : p_write) conflict = conflict || has(cur.writes, t) || has(cur.reads, t);
+            for (const Texture* t : p_read) conflict = conflict || has(cur.writes, t);
+            if ((uint64_t)cur.total_prims + p_prims > kMaxPrims) conflict = true;
+        }
         if (conflict) {
-            close();
-            batches.emplace_back();
+            new_batch();
             open = true;
         }
         Batch& b = batches.back();
         const uint32_t ti = (uint32_t)b.targets.size();
         b.targets.push_back(make_target(p, true, tile, profile));
+        b.target_item.push_back(item);
         for (const DrawCmd& dc : p.draws) {
             ++*draws;
             DrawDesc d = make_draw(dc, profile, (bool)p.depth);
@@ -758,18 +954,20 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
             b.nvar = std::max(b.nvar, d.num_varyings);
             if (np) b.draws.push_back(d);
         }
-        for (const Texture* t : p_write)
-            if (t) written.push_back(t);
-        for (const Texture* t : p_read) read.push_back(t);
+        b.writes.insert(b.writes.end(), p_write.begin(), p_write.end());
+        b.reads.insert(b.reads.end(), p_read.begin(), p_read.end());
     }
     return batches;
 }
 
-// Chooses each batch's tile shape (fixed by the config, or by the autotuner), lays out its
-// tiles and launches all batches; re-runs from a batch that ran out of scratch space.
-void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) {
-    std::vector<int> btile(batches.size()), bwarps(batches.size()), tuning(batches.size(), -1);
-    for (size_t i = 0; i < batches.size(); ++i) {
+// Launches batches[from..] back to back: each batch's tile shape (fixed by the config, or by
+// the autotuner), tile layout, descriptors and per-target fragment counters; re-runs from a
+// batch that ran out of scratch space after growing it.  Returns the first batch that failed
+// validation on the device (batches before it completed), or batches.size().
+RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun& run) {
+    const size_t nb = batches.size();
+    std::vector<int> btile(nb, tile), bwarps(nb, warps), tuning(nb, -1);
+    for (size_t i = from; i < nb; ++i) {
         Batch& b = batches[i];
         int t = tile, w = warps;
         if (autotune) tuning[i] = tuner_pick(b, &t, &w);
@@ -785,15 +983,22 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
         b.total_tiles = base;
     }
 
-    // metadata layout: [abort flag][statuses][work counters][draw/target descriptors per batch]
-    const size_t nb = batches.size();
+    // metadata layout: [abort flag][statuses][work counters][fragment counters]
+    //                  [draw/target descriptors (+ raster states) per batch]
     auto align = [](size_t v) { return (v + 255) & ~size_t(255); };
-    size_t off_status = 256, off_work = align(off_status + nb * sizeof(BatchStatus));
-    size_t off_desc = align(off_work + nb * sizeof(uint32_t) * 4);
-    std::vector<size_t> desc_off(nb), states_off(nb, 0);
-    std::vector<int> kinds(nb);
+    size_t n_targets = 0;
+    std::vector<size_t> counter_first(nb, 0);
+    for (size_t i = from; i < nb; ++i) {
+        counter_first[i] = n_targets;
+        n_targets += batches[i].targets.size();
+    }
+    const size_t off_status = 256, off_work = align(off_status + nb * sizeof(BatchStatus));
+    const size_t off_counters = align(off_work + nb * sizeof(uint32_t) * 4);
+    const size_t off_desc = align(off_counters + n_targets * sizeof(unsigned long long));
+    std::vector<size_t> desc_off(nb, 0), states_off(nb, 0);
+    std::vector<int> kinds(nb, 0);
     size_t cur = off_desc;
-    for (size_t i = 0; i < nb; ++i) {
+    for (size_t i = from; i < nb; ++i) {
         kinds[i] = fragment_kind(batches[i], cfg.raster_order == GBR_RASTER_AUTO);
         desc_off[i] = cur;
         cur = align(cur + batches[i].draws.size() * sizeof(DrawDesc) + batches[i].targets.size() * sizeof(TargetDesc));
@@ -802,26 +1007,30 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
             cur = align(cur + batches[i].draws.size() * raster_state_bytes());
         }
     }
+    const uint64_t budget = cfg.hbm_budget_bytes ? cfg.hbm_budget_bytes : (80ull << 30);
+    meta_buf.ensure(cur, &scratch_bytes);
+    uint8_t* meta = static_cast<uint8_t*>(meta_buf.ptr);
     std::vector<uint8_t> host_meta(cur, 0);
-    for (size_t i = 0; i < nb; ++i) {
+    for (size_t i = from; i < nb; ++i) {
         uint8_t* p = host_meta.data() + desc_off[i];
         std::memcpy(p, batches[i].draws.data(), batches[i].draws.size() * sizeof(DrawDesc));
-        std::memcpy(p + batches[i].draws.size() * sizeof(DrawDesc), batches[i].targets.data(),
-                    batches[i].targets.size() * sizeof(TargetDesc));
+        TargetDesc* tp = reinterpret_cast<TargetDesc*>(p + batches[i].draws.size() * sizeof(DrawDesc));
+        for (size_t t = 0; t < batches[i].targets.size(); ++t) {
+            TargetDesc td = batches[i].targets[t];
+            td.frag_count = reinterpret_cast<unsigned long long*>(meta + off_counters) + counter_first[i] + t;
+            std::memcpy(tp + t, &td, sizeof td);
+        }
     }
-    uint64_t budget = cfg.hbm_budget_bytes ? cfg.hbm_budget_bytes : (80ull << 30);
-    meta_buf.ensure(cur, &scratch_bytes);
-    cuda_check(cudaMemcpyAsync(meta_buf.ptr, host_meta.data(), cur, cudaMemcpyHostToDevice, stream), "upload descriptors");
+    cuda_check(cudaMemcpyAsync(meta, host_meta.data(), cur, cudaMemcpyHostToDevice, stream), "upload descriptors");
 
-    cudaEvent_t ev0, ev1;
-    cuda_check(cudaEventCreate(&ev0), "event");
-    cuda_check(cudaEventCreate(&ev1), "event");
-    rec.ev_start = ev0;
-    rec.ev_end = ev1;
-    uint32_t launches = 0;
-    uint64_t fragments = 0, slow_prims = 0;
-    size_t first_batch = 0;
+    if (!run.ev) {
+        run.ev = std::make_shared<EventPair>();
+        cuda_check(cudaEventCreate(&run.ev->start), "event");
+        cuda_check(cudaEventCreate(&run.ev->end), "event");
+    }
+    size_t first_batch = from;
     std::vector<BatchStatus> st(nb);
+    std::vector<unsigned long long> counters(n_targets);
     std::vector<cudaEvent_t> rev;  // raster kernel events (time_kernels)
     struct EventGuard {
         std::vector<cudaEvent_t>* v;
@@ -834,7 +1043,6 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
         rev.resize(2 * nb);
         for (auto& e : rev) cuda_check(cudaEventCreate(&e), "event");
     }
-    double raster_ms = 0.0;
     for (int attempt = 0; attempt < 12; ++attempt) {
         // scratch for the remaining batches
         uint32_t max_prims = 0, max_tiles = 0, max_stride = 0;
@@ -850,69 +1058,73 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
         tiles_buf.ensure((size_t)(max_tiles + 1) * 3 * sizeof(uint32_t) + 64, &scratch_bytes);
         bins_buf.ensure((size_t)bin_capacity * sizeof(uint32_t), &scratch_bytes);
         if (scratch_bytes > budget) fail(GBR_ERR_OUT_OF_MEMORY, "transient memory exceeds the HBM budget");
-        uint8_t* meta = static_cast<uint8_t*>(meta_buf.ptr);
-        if (attempt == 0) cuda_check(cudaEventRecord(ev0, stream), "event");
+        if (!run.started) {
+            cuda_check(cudaEventRecord(run.ev->start, stream), "event");
+            run.started = true;
+        }
         // The launch sequence of the remaining batches; replayed from a CUDA graph when the
         // config asks for graphs and the same parameters were launched before.
         std::vector<BatchParams> params(nb);
         std::vector<cudaEvent_t>* revp = &rev;
         auto enqueue = [&]() {
-        cuda_check(cudaMemsetAsync(meta, 0, 4, stream), "abort flag");
-        for (size_t i = first_batch; i < nb; ++i) {
-            const Batch& b = batches[i];
-            BatchParams& bp = params[i];
-            bp = BatchParams{};
-            bp.draws = reinterpret_cast<const DrawDesc*>(meta + desc_off[i]);
-            bp.targets = reinterpret_cast<const TargetDesc*>(meta + desc_off[i] + b.draws.size() * sizeof(DrawDesc));
-            bp.num_draws = (uint32_t)b.draws.size();
-            bp.num_targets = (uint32_t)b.targets.size();
-            bp.total_prims = b.total_prims;
-            bp.total_tiles = b.total_tiles;
-            bp.tile_size = btile[i];
-            bp.tile_shift = ilog2(btile[i]);
-            bp.record_stride = (uint32_t)((sizeof(TriRecord) + 3 * b.nvar * sizeof(float) + 15) & ~size_t(15));
-            bp.num_varyings = b.nvar;
-            bp.records = static_cast<uint8_t*>(records_buf.ptr);
-            bp.slow_prims = static_cast<uint32_t*>(slow_buf.ptr);
-            bp.ovf_records = static_cast<uint8_t*>(ovf_buf.ptr);
-            bp.ovf_capacity = ovf_capacity;
-            bp.bin_capacity = (uint32_t)std::min<uint64_t>(bin_capacity, 0xFFFFFFFFull);
-            uint32_t* tiles = static_cast<uint32_t*>(tiles_buf.ptr);
-            bp.tile_count = tiles;
-            bp.tile_offset = tiles + (max_tiles + 1);
-            bp.tile_cursor = tiles + 2 * (max_tiles + 1);
-            bp.bins = static_cast<uint32_t*>(bins_buf.ptr);
-            bp.work_counter = reinterpret_cast<uint32_t*>(meta + off_work) + i * 4;
-            bp.status = reinterpret_cast<BatchStatus*>(meta + off_status) + i;
-            bp.abort_flag = reinterpret_cast<uint32_t*>(meta);
-            if (kinds[i] == 3) {
-                bp.states = meta + states_off[i];
-                bp.vis_compare = visibility_compare(b);
+            cuda_check(cudaMemsetAsync(meta, 0, 4, stream), "abort flag");
+            for (size_t i = first_batch; i < nb; ++i) {
+                const Batch& b = batches[i];
+                BatchParams& bp = params[i];
+                bp = BatchParams{};
+                bp.draws = reinterpret_cast<const DrawDesc*>(meta + desc_off[i]);
+                bp.targets =
+                    reinterpret_cast<const TargetDesc*>(meta + desc_off[i] + b.draws.size() * sizeof(DrawDesc));
+                bp.num_draws = (uint32_t)b.draws.size();
+                bp.num_targets = (uint32_t)b.targets.size();
+                bp.total_prims = b.total_prims;
+                bp.total_tiles = b.total_tiles;
+                bp.tile_size = btile[i];
+                bp.tile_shift = ilog2(btile[i]);
+                bp.record_stride = (uint32_t)((sizeof(TriRecord) + 3 * b.nvar * sizeof(float) + 15) & ~size_t(15));
+                bp.num_varyings = b.nvar;
+                bp.records = static_cast<uint8_t*>(records_buf.ptr);
+                bp.slow_prims = static_cast<uint32_t*>(slow_buf.ptr);
+                bp.ovf_records = static_cast<uint8_t*>(ovf_buf.ptr);
+                bp.ovf_capacity = ovf_capacity;
+                bp.bin_capacity = (uint32_t)std::min<uint64_t>(bin_capacity, 0xFFFFFFFFull);
+                uint32_t* tiles = static_cast<uint32_t*>(tiles_buf.ptr);
+                bp.tile_count = tiles;
+                bp.tile_offset = tiles + (max_tiles + 1);
+                bp.tile_cursor = tiles + 2 * (max_tiles + 1);
+                bp.bins = static_cast<uint32_t*>(bins_buf.ptr);
+                bp.work_counter = reinterpret_cast<uint32_t*>(meta + off_work) + i * 4;
+                bp.status = reinterpret_cast<BatchStatus*>(meta + off_status) + i;
+                bp.abort_flag = reinterpret_cast<uint32_t*>(meta);
+                if (kinds[i] == 3) {
+                    bp.states = meta + states_off[i];
+                    bp.vis_compare = visibility_compare(b);
+                }
+                cuda_check(launch_batch(bp, btile[i], bwarps[i], num_sms, stream, &run.launches,
+                                        revp->empty() ? nullptr : &(*revp)[2 * i], kinds[i]),
+                           "launch");
             }
-            cuda_check(launch_batch(bp, btile[i], bwarps[i], num_sms, stream, &launches,
-                                    revp->empty() ? nullptr : &(*revp)[2 * i], kinds[i]),
-                       "launch");
-        }
         };
         if (cfg.use_graphs && attempt == 0 && !any_tuning) {
             // key: every launch parameter of the sequence (descriptors are re-uploaded each time)
             std::string key;
-            for (size_t i = 0; i < nb; ++i) {
-                key.append(reinterpret_cast<const char*>(&btile[i]), sizeof(int));
-                key.append(reinterpret_cast<const char*>(&bwarps[i]), sizeof(int));
-                const int kind = kinds[i];
-                key.append(reinterpret_cast<const char*>(&kind), sizeof(int));
-                key.append(reinterpret_cast<const char*>(&batches[i].total_prims), sizeof(uint32_t));
-                key.append(reinterpret_cast<const char*>(&batches[i].total_tiles), sizeof(uint32_t));
-                key.append(reinterpret_cast<const char*>(&batches[i].nvar), sizeof(uint32_t));
+            auto put = [&](const void* p, size_t len) { key.append(static_cast<const char*>(p), len); };
+            put(&from, sizeof from);
+            for (size_t i = from; i < nb; ++i) {
+                put(&btile[i], sizeof(int));
+                put(&bwarps[i], sizeof(int));
+                put(&kinds[i], sizeof(int));
+                put(&batches[i].total_prims, sizeof(uint32_t));
+                put(&batches[i].total_tiles, sizeof(uint32_t));
+                put(&batches[i].nvar, sizeof(uint32_t));
                 const size_t nd = batches[i].draws.size(), nt = batches[i].targets.size();
-                key.append(reinterpret_cast<const char*>(&nd), sizeof nd);
-                key.append(reinterpret_cast<const char*>(&nt), sizeof nt);
+                put(&nd, sizeof nd);
+                put(&nt, sizeof nt);
             }
             const void* ptrs[6] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, slow_buf.ptr};
-            key.append(reinterpret_cast<const char*>(ptrs), sizeof ptrs);
-            key.append(reinterpret_cast<const char*>(&ovf_capacity), sizeof ovf_capacity);
-            key.append(reinterpret_cast<const char*>(&bin_capacity), sizeof bin_capacity);
+            put(ptrs, sizeof ptrs);
+            put(&ovf_capacity, sizeof ovf_capacity);
+            put(&bin_capacity, sizeof bin_capacity);
             key.push_back(rev.empty() ? 0 : 1);
             GraphEntry& g = graphs[key];
             g.last_use = ++graph_clock;
@@ -947,16 +1159,20 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
             } else {
                 revp = &g.events;
                 for (size_t i = first_batch; i < nb; ++i)
-                    launches += batch_kernel_launches(batches[i].total_prims, btile[i], bwarps[i], kinds[i]);
+                    run.launches += batch_kernel_launches(batches[i].total_prims, btile[i], bwarps[i], kinds[i]);
             }
             cuda_check(cudaGraphLaunch(graphs[key].exec, stream), "cudaGraphLaunch");
         } else {
             enqueue();
         }
-        cuda_check(cudaEventRecord(ev1, stream), "event");
+        cuda_check(cudaEventRecord(run.ev->end, stream), "event");
         cuda_check(cudaMemcpyAsync(st.data(), meta + off_status, nb * sizeof(BatchStatus), cudaMemcpyDeviceToHost,
                                    stream),
                    "status readback");
+        if (n_targets)
+            cuda_check(cudaMemcpyAsync(counters.data(), meta + off_counters, n_targets * sizeof(unsigned long long),
+                                       cudaMemcpyDeviceToHost, stream),
+                       "counter readback");
         cuda_check(cudaStreamSynchronize(stream), "submission");
         // first failing batch
         size_t bad = nb;
@@ -965,18 +1181,20 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
                 bad = i;
                 break;
             }
-        for (size_t i = first_batch; i < (bad == nb ? nb : bad); ++i) {
-            fragments += st[i].fragments;
-            slow_prims += st[i].slow_count;
+        for (size_t i = first_batch; i < bad; ++i) {
+            Batch& b = batches[i];
+            b.target_frags.assign(counters.begin() + (ptrdiff_t)counter_first[i],
+                                  counters.begin() + (ptrdiff_t)(counter_first[i] + b.targets.size()));
+            run.slow_prims += st[i].slow_count;
             if (!revp->empty()) {
                 float ms = 0.0f;
                 if (cudaEventElapsedTime(&ms, (*revp)[2 * i], (*revp)[2 * i + 1]) == cudaSuccess) {
-                    raster_ms += ms;
-                    if (tuning[i] >= 0) tuner_record(batches[i], tuning[i], ms);
+                    run.raster_ms += ms;
+                    if (tuning[i] >= 0) tuner_record(b, tuning[i], ms);
                 }
             }
         }
-        if (bad == nb) break;
+        if (bad == nb) return RunResult{nb, 0, {}};
         const BatchStatus& s = st[bad];
         if (s.error == ERR_OVERFLOW_RECORDS) {
             ovf_capacity = std::max<uint32_t>(ovf_capacity * 2, s.ovf_used + 1024);
@@ -989,19 +1207,20 @@ void Device::launch_batches(std::vector<Batch>& batches, SubmissionRecord& rec) 
                                           "index + base_vertex overflows u32 (index.rs:55-57)", "", "",
                                           "scanline coordinate does not fit u32 (scanline.rs:156-170)",
                                           "unsupported"};
-            fail(GBR_ERR_VALIDATION, "%s (primitive %u)", s.error < 9 ? names[s.error] : "device error",
-                 s.error_detail);
+            char msg[256];
+            std::snprintf(msg, sizeof msg, "%s (primitive %u)", s.error < 9 ? names[s.error] : "device error",
+                          s.error_detail);
+            return RunResult{bad, s.error, msg};
         }
+        // counters of the batches that re-run start from zero
+        if (n_targets > counter_first[bad])
+            cuda_check(cudaMemsetAsync(reinterpret_cast<unsigned long long*>(meta + off_counters) + counter_first[bad],
+                                       0, (n_targets - counter_first[bad]) * sizeof(unsigned long long), stream),
+                       "counters");
         first_batch = bad;
         if (attempt == 11) fail(GBR_ERR_OUT_OF_MEMORY, "scratch growth did not converge");
     }
-    float gms = 0.0f;
-    cudaEventElapsedTime(&gms, ev0, ev1);
-    rec.stats.gpu_ms = gms;
-    rec.stats.fragments_shaded = fragments;
-    rec.stats.kernel_launches = launches;
-    rec.stats.raster_ms = raster_ms;
-    rec.stats.generic_setup_prims = (uint32_t)std::min<uint64_t>(slow_prims, 0xFFFFFFFFu);
+    return RunResult{nb, 0, {}};
 }
 
 // ---------------------------------------------------------------- command decoding
@@ -1241,10 +1460,7 @@ GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
         if (d->worker.joinable()) d->worker.join();
         cudaSetDevice(d->ordinal);
         cudaStreamSynchronize(d->stream);
-        for (auto& r : d->records) {
-            if (r.second.ev_start) cudaEventDestroy(r.second.ev_start);
-            if (r.second.ev_end) cudaEventDestroy(r.second.ev_end);
-        }
+        d->records.clear();  // their events go with them
         for (auto& g : d->graphs) {
             if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
             for (cudaEvent_t e : g.second.events) cudaEventDestroy(e);
@@ -1560,13 +1776,10 @@ GBR_API gbr_status gbr_device_poll(gbr_device dh, uint32_t wait, uint32_t has_in
         }
         auto deadline = timeout_ns == UINT64_MAX ? Clock::time_point::max()
                                                  : Clock::now() + std::chrono::nanoseconds(timeout_ns);
-        if (d->completed_submissions == d->next_submission) {
-            if (out_status) *out_status = GBR_POLL_QUEUE_EMPTY;
-            return GBR_OK;
-        }
-        uint64_t target = has_index ? index + 1 : d->completed_submissions + 1;
         if (has_index && index >= d->next_submission) fail(GBR_ERR_INVALID_ARGUMENT, "unknown submission index");
-        while (d->completed_submissions < target) {
+        const bool empty = d->completed_submissions == d->next_submission;
+        uint64_t target = has_index ? index + 1 : d->completed_submissions + 1;
+        while (!empty && d->completed_submissions < target) {
             if (deadline == Clock::time_point::max()) {
                 d->done_cv.wait(lk);
             } else if (d->done_cv.wait_until(lk, deadline) == std::cv_status::timeout &&
@@ -1574,7 +1787,7 @@ GBR_API gbr_status gbr_device_poll(gbr_device dh, uint32_t wait, uint32_t has_in
                 fail(GBR_ERR_TIMEOUT, "poll timed out");
             }
         }
-        if (out_status) *out_status = GBR_POLL_WAIT_SUCCEEDED;
+        if (out_status) *out_status = empty ? GBR_POLL_QUEUE_EMPTY : GBR_POLL_WAIT_SUCCEEDED;
         if (has_index) {
             auto it = d->records.find(index);
             if (it != d->records.end() && it->second.status != GBR_OK) fail(it->second.status, "%s", it->second.error.c_str());
@@ -1597,10 +1810,10 @@ GBR_API gbr_status gbr_device_elapsed_ms(gbr_device dh, uint64_t first, uint64_t
         auto d = get_device(dh);
         std::lock_guard<std::mutex> lk(d->q_mu);
         auto a = d->records.find(first), b = d->records.find(last);
-        if (a == d->records.end() || b == d->records.end() || !a->second.ev_start || !b->second.ev_end)
+        if (a == d->records.end() || b == d->records.end() || !a->second.ev || !b->second.ev)
             fail(GBR_ERR_INVALID_ARGUMENT, "no device timing for these submissions");
         float ms = 0.0f;
-        cuda_check(cudaEventElapsedTime(&ms, a->second.ev_start, b->second.ev_end), "cudaEventElapsedTime");
+        cuda_check(cudaEventElapsedTime(&ms, a->second.ev->start, b->second.ev->end), "cudaEventElapsedTime");
         *out_ms = ms;
     })
 }

@@ -454,3 +454,107 @@ def scene_batched(dev: W.Device, n_targets: int = 64, n_draws: int = 256, seed: 
     s.passes = targets
     s._keep = keep + [pl_t, pl_c] + [m for v in meshes.values() for m in v]
     return s
+
+
+@dataclass
+class ServingSet:
+    """Resident resources of the serving workload and pre-recorded submissions over them."""
+    device: W.Device
+    commands: list = field(default_factory=list)     # one finished command buffer per submission
+    targets: list = field(default_factory=list)      # (colour, depth) of each submission
+    draws: list = field(default_factory=list)        # draws per submission
+    triangles: list = field(default_factory=list)    # triangles per submission
+    keep: list = field(default_factory=list)
+
+
+def serving_set(dev: W.Device, n_submissions: int = 256, n_meshes: int = 512, n_textures: int = 128,
+                seed: int = 5, max_draws: int = 64, tri_lo: int = 100, tri_hi: int = 200000) -> ServingSet:
+    """Serving workload: n_meshes displaced icospheres (seeded radial jitter of one base mesh per
+    subdivision level) and n_textures 256x256 Rgba8 textures, all resident; each submission
+    renders 1..max_draws draws (log-uniform) into its own Rgba8Unorm + Depth32Float (Less)
+    target of width log-uniform in [256, 1920] and height in [256, 1080]; each draw takes a
+    random mesh, a triangle count log-uniform in [tri_lo, tri_hi] (the first triangles of the
+    mesh, capped at its size), a random rotation and distance, and either the textured Lambert
+    program with a random texture or the vertex-colour program."""
+    rng = np.random.default_rng(seed)
+    s = ServingSet(dev)
+    base = {}
+    levels = []
+    for m in range(n_meshes):
+        lvl = int(rng.integers(2, 8))  # 320 .. 327,680 triangles
+        if lvl not in base:
+            v, f = icosphere(lvl)
+            u = 0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2.0 * math.pi)
+            vv = 0.5 - np.arcsin(np.clip(v[:, 1], -1.0, 1.0)) / math.pi
+            ib = dev.create_buffer_init(f.ravel())
+            base[lvl] = (v, np.stack([u, vv], 1), f, ib)
+            s.keep.append(ib)
+        v, uv, f, ib = base[lvl]
+        r = 1.0 + 0.1 * (rng.random(len(v)) - 0.5) * 2.0
+        pos = v * r[:, None]
+        nrm = v  # the unit sphere's normal: the jitter is small
+        col = rng.random((len(v), 3))
+        vt = dev.create_buffer_init(np.concatenate([pos, nrm, uv], 1).astype(np.float32))
+        vc = dev.create_buffer_init(np.concatenate([pos, col], 1).astype(np.float32))
+        s.keep += [vt, vc]
+        levels.append((vt, vc, ib, len(f)))
+    base_tex = [checker_noise_texture(256, seed + 100 + k) for k in range(8)]
+    textures = []
+    for k in range(n_textures):
+        img = np.ascontiguousarray(np.roll(base_tex[k % 8], shift=(k // 8) * 16, axis=(0, 1)))
+        t = dev.create_texture(256, 256, W.TextureFormat.RGBA8_UNORM)
+        dev.queue.write_texture(t, img)
+        textures.append(t)
+    samp = dev.create_sampler(W.AddressMode.REPEAT, W.AddressMode.REPEAT)
+    sm_t = dev.create_shader_module(native="mesh_tex_lambert")
+    sm_c = dev.create_shader_module(native="mesh_color")
+    fmt = W.TextureFormat.RGBA8_UNORM
+    prim = W.PrimitiveState(W.PrimitiveTopology.TRIANGLE_LIST, cull_mode=W.Face.BACK)
+    depth = W.DepthStencilState(True, W.CompareFunction.LESS)
+    pl_t = dev.create_render_pipeline(
+        sm_t, [W.VertexBufferLayout(32, [_f32x3_layout(0, 0), _f32x3_layout(1, 12),
+                                         W.VertexAttribute(W.VertexFormat.FLOAT32X2, 24, 2)])],
+        prim, depth, sm_t, [W.ColorTargetState(fmt)])
+    pl_c = dev.create_render_pipeline(
+        sm_c, [W.VertexBufferLayout(24, [_f32x3_layout(0, 0), _f32x3_layout(1, 12)])], prim, depth, sm_c,
+        [W.ColorTargetState(fmt)])
+    tex_groups = [dev.create_bind_group([W.BindGroupEntry(0, t), W.BindGroupEntry(1, samp)]) for t in textures]
+    s.keep += textures + tex_groups + [samp, sm_t, sm_c, pl_t, pl_c]
+    for k in range(n_submissions):
+        w = int(np.exp(rng.uniform(math.log(256), math.log(1920))))
+        h = int(np.exp(rng.uniform(math.log(256), math.log(1080))))
+        color = dev.create_texture(w, h, fmt)
+        dtex = dev.create_texture(w, h, W.TextureFormat.DEPTH32_FLOAT)
+        n_draws = int(np.clip(np.round(np.exp(rng.uniform(0.0, math.log(max_draws)))), 1, max_draws))
+        enc = dev.create_command_encoder()
+        rp = enc.begin_render_pass([W.RenderPassColorAttachment(color, (0.0, 0.0, 0.0, 1.0))],
+                                   W.RenderPassDepthStencilAttachment(dtex, 1.0))
+        tris = 0
+        for _ in range(n_draws):
+            vt, vc, ib, nf = levels[int(rng.integers(0, n_meshes))]
+            n = int(min(nf, np.exp(rng.uniform(math.log(tri_lo), math.log(tri_hi)))))
+            mvp = camera_mvp(w, h, eye=(0.0, 0.0, float(rng.uniform(2.6, 4.5))), model=random_rotation(rng))
+            L = rng.normal(size=3)
+            L /= np.linalg.norm(L)
+            ub = dev.create_buffer_init(mvp_bytes(mvp) + np.array([*L, 0.0], dtype=np.float32).tobytes())
+            g0 = dev.create_bind_group([W.BindGroupEntry(0, ub)])
+            s.keep += [ub, g0]
+            if rng.random() < 0.5:
+                rp.set_pipeline(pl_t)
+                rp.set_bind_group(1, tex_groups[int(rng.integers(0, n_textures))])
+                rp.set_vertex_buffer(0, vt)
+            else:
+                rp.set_pipeline(pl_c)
+                rp.set_vertex_buffer(0, vc)
+            rp.set_bind_group(0, g0)
+            rp.set_index_buffer(ib, W.IndexFormat.UINT32)
+            rp.draw_indexed(range(0, 3 * n))
+            tris += n
+        rp.end()
+        s.commands.append(enc.finish())
+        s.targets.append((color, dtex))
+        s.draws.append(n_draws)
+        s.triangles.append(tris)
+        s.keep.append(color)
+        s.keep.append(dtex)
+    return s
