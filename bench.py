@@ -53,8 +53,9 @@ UNIT = "fragments/s"
 
 class Workload:
     def __init__(self, name, profile, builder, kwargs, bytes_per_fragment, pixel_bytes, description, extra_cfg,
-                 cpu_kwargs=None, dtype="f32"):
+                 cpu_kwargs=None, dtype="f32", tile=(16, 8)):
         self.name, self.profile, self.builder, self.kwargs = name, profile, builder, kwargs
+        self.tile = tile  # (side, warps per tile): the fastest shape measured for this workload
         self.bytes_per_fragment, self.pixel_bytes = bytes_per_fragment, pixel_bytes
         self.description, self.extra_cfg = description, extra_cfg
         self.cpu_kwargs = cpu_kwargs if cpu_kwargs is not None else kwargs
@@ -80,14 +81,15 @@ def workloads():
             4 + 4 + 4 + 4, 1920 * 1080 * (4 + 4),
             "textured icosphere: 81,920 tris, 1920x1080 Rgba8UnormSrgb + Depth32Float Less, 1024^2 texture, "
             "texture x Lambert, parity profile (nearest, sRGB as linear)",
-            {"triangles": 81920, "target": "1920x1080", "texture": "1024x1024 rgba8", "profile": "parity", "seed": 2}),
+            {"triangles": 81920, "target": "1920x1080", "texture": "1024x1024 rgba8", "profile": "parity", "seed": 2},
+            tile=(16, 4)),
         "blend": Workload(
             "blend", W.Profile.EXTENSION, "scene_blended_quads", dict(width=3840, height=2160, n_quads=10000),
             8 + 8, 3840 * 2160 * 8,
             "blended quads: 10,000 quads (20,000 tris) sides U[16,1024], painter order, SrcAlpha/OneMinusSrcAlpha "
             "into 3840x2160 Rgba16Float, extension profile",
             {"triangles": 20000, "target": "3840x2160 rgba16float", "profile": "extension", "seed": 4},
-            cpu_kwargs=dict(width=3840, height=2160, n_quads=60), dtype="f32 (f16 storage)"),
+            cpu_kwargs=dict(width=3840, height=2160, n_quads=60), dtype="f32 (f16 storage)", tile=(32, 8)),
         "colored": Workload(
             "colored", W.Profile.PARITY, "scene_colored_sphere", dict(width=512, height=512),
             4, 512 * 512 * 4,
@@ -99,7 +101,7 @@ def workloads():
             "batched draws: 256 draws into 64 targets (sides log-uniform [128,2048], tris log-uniform [100,200k]), "
             "Rgba8Unorm + Depth32Float Less, half texture x Lambert / half vertex colour, one command buffer",
             {"draws": 256, "targets": 64, "profile": "parity", "seed": 3},
-            cpu_kwargs=dict(n_targets=16, n_draws=64, seed=3)),
+            cpu_kwargs=dict(n_targets=16, n_draws=64, seed=3), tile=(16, 2)),
     }
 
 
@@ -479,6 +481,8 @@ def main():
     args.warmup = max(3, args.warmup)
     if args.autotune:
         args.tile = args.warps = 0
+    elif not args.tile and args.workload in workloads():
+        args.tile, args.warps = workloads()[args.workload].tile
     elif not args.tile:
         args.tile, args.warps = dev_tile(args), dev_warps(args)
     if args.workload == "serve":

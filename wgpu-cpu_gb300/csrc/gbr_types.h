@@ -143,6 +143,7 @@ enum FastVs : uint32_t {
     FAST_VS_QUAD = 3,       // quad_color: f32x3 position, f32x4 colour
     FAST_VS_CLIP = 4,       // clip_passthrough: f32x4 clip position, f32x4 colour
     FAST_VS_TRIANGLE = 5,   // colored_triangle: no inputs
+    FAST_VS_QUAD_F16 = 6,   // quad_color, extension profile: f32x3 position, f16x4 colour
 };
 
 // Per-sub-triangle record written by the setup kernel and read by binning and raster.

@@ -143,9 +143,15 @@ uint32_t fast_vs_kind(const DrawDesc& d) {
                            f32(2, GBR_VERTEX_FORMAT_FLOAT32X2)
                        ? FAST_VS_MVP_TEX
                        : FAST_VS_NONE;
-        case PROG_QUAD_COLOR:
-            return f32(0, GBR_VERTEX_FORMAT_FLOAT32X3) && f32(1, GBR_VERTEX_FORMAT_FLOAT32X4) ? FAST_VS_QUAD
-                                                                                               : FAST_VS_NONE;
+        case PROG_QUAD_COLOR: {
+            if (!f32(0, GBR_VERTEX_FORMAT_FLOAT32X3)) return FAST_VS_NONE;
+            if (f32(1, GBR_VERTEX_FORMAT_FLOAT32X4)) return FAST_VS_QUAD;
+            const AttrDesc& a = d.attr[1];
+            const bool h = a.buffer >= 0 && a.format == GBR_VERTEX_FORMAT_FLOAT16X4 && a.offset % 2 == 0 &&
+                           d.vb_stride_vertex[a.buffer] % 2 == 0 && d.vb_stride_instance[a.buffer] % 2 == 0 &&
+                           reinterpret_cast<uintptr_t>(d.vb_data[a.buffer]) % 2 == 0;
+            return h && d.profile == GBR_PROFILE_EXTENSION ? FAST_VS_QUAD_F16 : FAST_VS_NONE;
+        }
         case PROG_CLIP_PASSTHROUGH:
             return f32(0, GBR_VERTEX_FORMAT_FLOAT32X4) && f32(1, GBR_VERTEX_FORMAT_FLOAT32X4) ? FAST_VS_CLIP
                                                                                                : FAST_VS_NONE;
@@ -216,11 +222,16 @@ cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms
         case (8 * 16 + 2) * 4 + 1: e = launch_raster<8, 2, 1>(bp, num_sms, s); break;
         case (8 * 16 + 2) * 4 + 2: e = launch_raster<8, 2, 2>(bp, num_sms, s); break;
         case (16 * 16 + 2) * 4: e = launch_raster<16, 2>(bp, num_sms, s); break;
+        case (16 * 16 + 2) * 4 + 1: e = launch_raster<16, 2, 1>(bp, num_sms, s); break;
+        case (16 * 16 + 2) * 4 + 2: e = launch_raster<16, 2, 2>(bp, num_sms, s); break;
         case (16 * 16 + 4) * 4: e = launch_raster<16, 4>(bp, num_sms, s); break;
+        case (16 * 16 + 4) * 4 + 1: e = launch_raster<16, 4, 1>(bp, num_sms, s); break;
+        case (16 * 16 + 4) * 4 + 2: e = launch_raster<16, 4, 2>(bp, num_sms, s); break;
         case (16 * 16 + 8) * 4: e = launch_raster<16, 8>(bp, num_sms, s); break;
         case (16 * 16 + 8) * 4 + 1: e = launch_raster<16, 8, 1>(bp, num_sms, s); break;
         case (16 * 16 + 8) * 4 + 2: e = launch_raster<16, 8, 2>(bp, num_sms, s); break;
         case (32 * 16 + 4) * 4: e = launch_raster<32, 4>(bp, num_sms, s); break;
+        case (32 * 16 + 4) * 4 + 1: e = launch_raster<32, 4, 1>(bp, num_sms, s); break;
         case (32 * 16 + 8) * 4: e = launch_raster<32, 8>(bp, num_sms, s); break;
         case (32 * 16 + 8) * 4 + 1: e = launch_raster<32, 8, 1>(bp, num_sms, s); break;
         case (32 * 16 + 8) * 4 + 2: e = launch_raster<32, 8, 2>(bp, num_sms, s); break;

@@ -585,6 +585,17 @@ __device__ __forceinline__ bool fast_vertex(const DrawDesc& d, const float* mvp,
         if (!fetch_f32<3>(d, 0, vertex, instance, a0) || !fetch_f32<4>(d, 1, vertex, instance, a1)) return false;
         pos = {a0[0], a0[1], a0[2], 1.0f};
         for (int k = 0; k < 4; ++k) var[k] = a1[k];
+    } else if constexpr (FVS == FAST_VS_QUAD_F16) {
+        // Float16x4 colour widened to f32 (the extension profile's fetch_attr conversion)
+        if (!fetch_f32<3>(d, 0, vertex, instance, a0)) return false;
+        const AttrDesc& a = d.attr[1];
+        const int b = a.buffer;
+        const uint64_t start = (uint64_t)instance * d.vb_stride_instance[b] + (uint64_t)vertex * d.vb_stride_vertex[b] +
+                               a.offset;
+        if (start + 8 > d.vb_size[b]) return false;
+        const uint16_t* h = reinterpret_cast<const uint16_t*>(d.vb_data[b] + start);
+        pos = {a0[0], a0[1], a0[2], 1.0f};
+        for (int k = 0; k < 4; ++k) var[k] = f16_bits_to_f32(__ldg(h + k));
     } else if constexpr (FVS == FAST_VS_CLIP) {
         if (!fetch_f32<4>(d, 0, vertex, instance, a0) || !fetch_f32<4>(d, 1, vertex, instance, a1)) return false;
         pos = {a0[0], a0[1], a0[2], a0[3]};
@@ -752,6 +763,7 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
                 case FAST_VS_QUAD: done = fast_prim<FAST_VS_QUAD>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
                 case FAST_VS_CLIP: done = fast_prim<FAST_VS_CLIP>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
                 case FAST_VS_TRIANGLE: done = fast_prim<FAST_VS_TRIANGLE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_QUAD_F16: done = fast_prim<FAST_VS_QUAD_F16>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
                 default: break;
             }
         }
@@ -932,10 +944,12 @@ __device__ __forceinline__ void encode_color(uint32_t fmt, V4 col, uint32_t c[4]
             c[0] = unorm8_trunc(col.z) | (unorm8_trunc(col.y) << 8) | (unorm8_trunc(col.x) << 16) |
                    (unorm8_trunc(col.w) << 24);
             break;
-        case 7:
-            c[0] = (uint32_t)f32_to_f16_bits(col.x) | ((uint32_t)f32_to_f16_bits(col.y) << 16);
-            c[1] = (uint32_t)f32_to_f16_bits(col.z) | ((uint32_t)f32_to_f16_bits(col.w) << 16);
+        case 7: {  // two round-to-nearest-even conversions per instruction, low half first
+            const __half2 lo = __floats2half2_rn(col.x, col.y), hi = __floats2half2_rn(col.z, col.w);
+            c[0] = *reinterpret_cast<const uint32_t*>(&lo);
+            c[1] = *reinterpret_cast<const uint32_t*>(&hi);
             break;
+        }
         case 8:
             c[0] = __float_as_uint(col.x); c[1] = __float_as_uint(col.y);
             c[2] = __float_as_uint(col.z); c[3] = __float_as_uint(col.w);
@@ -951,9 +965,11 @@ __device__ __forceinline__ V4 decode_color(uint32_t fmt, const uint32_t c[4]) {
         case 5: case 6:
             return {fdiv((float)((c[0] >> 16) & 0xFF), 255.0f), fdiv((float)((c[0] >> 8) & 0xFF), 255.0f),
                     fdiv((float)(c[0] & 0xFF), 255.0f), fdiv((float)(c[0] >> 24), 255.0f)};
-        case 7:
-            return {f16_bits_to_f32(c[0] & 0xFFFF), f16_bits_to_f32(c[0] >> 16), f16_bits_to_f32(c[1] & 0xFFFF),
-                    f16_bits_to_f32(c[1] >> 16)};
+        case 7: {
+            const float2 lo = __half22float2(*reinterpret_cast<const __half2*>(&c[0]));
+            const float2 hi = __half22float2(*reinterpret_cast<const __half2*>(&c[1]));
+            return {lo.x, lo.y, hi.x, hi.y};
+        }
         case 8: return {__uint_as_float(c[0]), __uint_as_float(c[1]), __uint_as_float(c[2]), __uint_as_float(c[3])};
         default: return {0.0f, 0.0f, 0.0f, 0.0f};
     }
@@ -1074,6 +1090,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
         // pixel state: LoadOp::Clear from the clear value, otherwise the stored texels
         PixelState px[PPT];
         int pxx[PPT], pxy[PPT];
+        float pfx[PPT], pfy[PPT];
         bool pvalid[PPT];
         uint32_t clear_c[4] = {0, 0, 0, 0};
         if (tg.color) encode_color(tg.color_format, V4{tg.clear[0], tg.clear[1], tg.clear[2], tg.clear[3]}, clear_c);
@@ -1084,6 +1101,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
             pxx[k] = tx * T + bx * 8 + (lane & 7);
             pxy[k] = ty * T + byy * 4 + (lane >> 3);
             pvalid[k] = blk < NBLK && pxx[k] < (int)tg.width && pxy[k] < (int)tg.height;
+            pfx[k] = (float)pxx[k];
+            pfy[k] = (float)pxy[k];
             const size_t pix = (size_t)pxy[k] * tg.width + pxx[k];
             px[k].c[0] = clear_c[0]; px[k].c[1] = clear_c[1]; px[k].c[2] = clear_c[2]; px[k].c[3] = clear_c[3];
             px[k].depth = tg.depth_clear;
@@ -1153,16 +1172,16 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                 }
                 const int y = ty * T + (int)row;
                 int2 sp = make_int2(1, 0);
-                if (y >= r.row0 && y <= r.row1) {
+                if (y >= r.row0 && y <= r.row1 && y < (int)tg.height) {
                     const DrawDesc& d = bp.draws[r.draw];
                     if ((uint32_t)y >= d.sc_y0 && (uint32_t)y < d.sc_y1) {
                         int x1, x2;
                         span_at(r, y, x1, x2);
                         sp.x = max(max(x1, (int)d.sc_x0), tx * T);
-                        sp.y = min(min(x2, (int)d.sc_x1 - 1), tx * T + T - 1);
+                        sp.y = min(min(min(x2, (int)d.sc_x1 - 1), tx * T + T - 1), (int)tg.width - 1);
                     }
                 }
-                s_span[q] = sp;
+                s_span[q] = sp;  // also empty outside the target, so no pixel test is needed below
             }
             __syncthreads();
             // which 8x4 blocks of the tile each staged record can emit into
@@ -1224,13 +1243,16 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                         {
                             // coverage: the row's span (already cut to scissor and tile)
                             const int2 sp = s_span[ri * T + (y - ty * T)];
-                            if (!pvalid[k] || x < sp.x || x > sp.y) continue;
+                            if (x < sp.x || x > sp.y) continue;
                         }
-                        // barycentrics at the integer pixel corner (raster.rs:313-321, 334-335)
-                        const float fx = (float)x, fy = (float)y;
-                        const float s0 = fadd(fadd(fmul(fsub(by, fy), fadd(bx, fx)), kc0), fmul(fsub(fy, cy), fadd(fx, cx)));
-                        const float s1 = fadd(fadd(fmul(fsub(fy, ay), fadd(fx, ax)), fmul(fsub(cy, fy), fadd(cx, fx))), kc1);
-                        const float s2 = fadd(fadd(kc2, fmul(fsub(fy, by), fadd(fx, bx))), fmul(fsub(ay, fy), fadd(ax, fx)));
+                        // barycentrics at the integer pixel corner (raster.rs:313-321, 334-335); an
+                        // IEEE sum does not depend on operand order, so x + a.x serves both shoelace
+                        // terms that contain it (likewise b, c)
+                        const float fx = pfx[k], fy = pfy[k];
+                        const float xa = fadd(fx, ax), xb = fadd(fx, bx), xc = fadd(fx, cx);
+                        const float s0 = fadd(fadd(fmul(fsub(by, fy), xb), kc0), fmul(fsub(fy, cy), xc));
+                        const float s1 = fadd(fadd(fmul(fsub(fy, ay), xa), fmul(fsub(cy, fy), xc)), kc1);
+                        const float s2 = fadd(fadd(kc2, fmul(fsub(fy, by), xb)), fmul(fsub(ay, fy), xa));
                         const float l0 = div_by_recip(s0, area, rcp, area_ok);
                         const float l1 = div_by_recip(s1, area, rcp, area_ok);
                         const float l2 = div_by_recip(s2, area, rcp, area_ok);

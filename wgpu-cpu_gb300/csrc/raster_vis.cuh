@@ -60,10 +60,12 @@ __device__ __forceinline__ void bary_consts(const TriRecord& r, BaryK& k) {
 // Barycentrics at the integer pixel corner composed with the clip barycentrics
 // (raster.rs:313-321, 334-343), as in k_raster.
 __device__ __forceinline__ void bary_at(const TriRecord& r, const BaryK& k, int x, int y, float cmp[3]) {
+    // an IEEE sum does not depend on operand order: x + a.x serves both terms containing it
     const float fx = (float)x, fy = (float)y;
-    const float s0 = fadd(fadd(fmul(fsub(k.by, fy), fadd(k.bx, fx)), k.kc0), fmul(fsub(fy, k.cy), fadd(fx, k.cx)));
-    const float s1 = fadd(fadd(fmul(fsub(fy, k.ay), fadd(fx, k.ax)), fmul(fsub(k.cy, fy), fadd(k.cx, fx))), k.kc1);
-    const float s2 = fadd(fadd(k.kc2, fmul(fsub(fy, k.by), fadd(fx, k.bx))), fmul(fsub(k.ay, fy), fadd(k.ax, fx)));
+    const float xa = fadd(fx, k.ax), xb = fadd(fx, k.bx), xc = fadd(fx, k.cx);
+    const float s0 = fadd(fadd(fmul(fsub(k.by, fy), xb), k.kc0), fmul(fsub(fy, k.cy), xc));
+    const float s1 = fadd(fadd(fmul(fsub(fy, k.ay), xa), fmul(fsub(k.cy, fy), xc)), k.kc1);
+    const float s2 = fadd(fadd(k.kc2, fmul(fsub(fy, k.by), xb)), fmul(fsub(k.ay, fy), xa));
     const float l0 = div_by_recip(s0, k.area, k.rcp, k.area_ok);
     const float l1 = div_by_recip(s1, k.area, k.rcp, k.area_ok);
     const float l2 = div_by_recip(s2, k.area, k.rcp, k.area_ok);
@@ -108,14 +110,14 @@ __device__ __forceinline__ void tile_sync() {
 // One CTA per tile (persistent); a CTA of one warp synchronises with __syncwarp only, so many
 // independent tiles share an SM and hide each other's memory latency.
 // Phase 1: every bin entry of the tile is rasterised by one lane (records whose tile-clipped
-// box holds at most kLanePixels pixels) or by a whole warp
+// box holds at most lane_px pixels: many when the tile has records enough for every lane, a
+// few otherwise) or by a whole warp
 // (larger ones: lanes split the box), each covered fragment atomicMin-ing its key into the
 // tile's key array.  Phase 2: one thread per pixel re-evaluates the survivor's barycentrics,
 // tests it against the stored depth, runs the fragment stage and writes colour and depth.
 template <int T, int WARPS>
 __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
     constexpr int NT = WARPS * 32, NPIX = T * T;
-    constexpr int kLanePixels = 24;
     constexpr unsigned long long kNone = ~0ull;
     __shared__ unsigned long long s_vis[NPIX];
     __shared__ float s_lut[256];
@@ -143,6 +145,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
         const int XE = min(X0 + T, (int)tg.width) - 1, YE = min(Y0 + T, (int)tg.height) - 1;
         const uint32_t n = bp.tile_count[tile];
         const uint32_t off = bp.tile_offset[tile];
+        const int lane_px = n >= (uint32_t)NT ? 32 : 6;
         uint32_t frag_count = 0;
 
         auto fragment = [&](const TriRecord& r, const BaryK& k, uint32_t order, int x, int y) {
@@ -170,7 +173,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                 xr = min(min(r->xmax, XE), (int)d.sc_x1 - 1);
             }
             const int box = (y1 >= y0 && xr >= xl) ? (y1 - y0 + 1) * (xr - xl + 1) : 0;
-            if (box > 0 && box <= kLanePixels) {
+            if (box > 0 && box <= lane_px) {
                 BaryK k;
                 bary_consts(*r, k);
                 for (int y = y0; y <= y1; ++y) {
@@ -181,7 +184,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                     for (int x = x1; x <= x2; ++x) fragment(*r, k, key, x, y);
                 }
             }
-            uint32_t big = __ballot_sync(0xFFFFFFFFu, box > kLanePixels);
+            uint32_t big = __ballot_sync(0xFFFFFFFFu, box > lane_px);
             while (big) {
                 const int src = __ffs(big) - 1;
                 big &= big - 1;

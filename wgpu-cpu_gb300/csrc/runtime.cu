@@ -410,8 +410,10 @@ int fragment_kind(const Batch& b, bool allow_visibility) {
     return k1 ? 1 : k2 ? 2 : 0;
 }
 
-// Tile shapes the autotuner tries (all compiled into kernels.cu).
-const int kTuneCands[][2] = {{16, 8}, {32, 8}, {8, 2}};
+// Tile shapes (side, warps per tile) the autotuner tries, all compiled into kernels.cu: for the
+// ordered kernels, and for the visibility raster (which favours fewer warps per tile).
+const int kTuneCands[][2] = {{16, 8}, {32, 8}, {32, 4}};
+const int kTuneCandsVis[][2] = {{16, 2}, {16, 4}, {32, 4}};
 constexpr int kNumTuneCands = 3;
 
 uint64_t log2_bucket(uint64_t v) {
@@ -434,14 +436,11 @@ uint64_t Device::tuner_signature(const Batch& b) const {
 }
 int Device::tuner_pick(const Batch& b, int* t, int* w) {
     TuneEntry& e = tuner[tuner_signature(b)];
-    if (e.tried < kNumTuneCands) {
-        *t = kTuneCands[e.tried][0];
-        *w = kTuneCands[e.tried][1];
-        return e.tried;
-    }
-    *t = kTuneCands[e.best][0];
-    *w = kTuneCands[e.best][1];
-    return -1;
+    const auto& cands = fragment_kind(b, cfg.raster_order == GBR_RASTER_AUTO) == 3 ? kTuneCandsVis : kTuneCands;
+    const int c = e.tried < kNumTuneCands ? e.tried : e.best;
+    *t = cands[c][0];
+    *w = cands[c][1];
+    return e.tried < kNumTuneCands ? e.tried : -1;
 }
 void Device::tuner_record(const Batch& b, int cand, float ms) {
     TuneEntry& e = tuner[tuner_signature(b)];
