@@ -466,6 +466,22 @@ GBR_API gbr_status gbr_render_pipeline_create(gbr_device device, const gbr_rende
                                               gbr_render_pipeline* out_pipeline);
 GBR_API gbr_status gbr_render_pipeline_destroy(gbr_device device, gbr_render_pipeline pipeline);
 
+/* No reference counterpart (test and tooling entry points of the WGSL translator).
+ * gbr_render_pipeline_eval_vertices runs the vertex stage of a WGSL pipeline alone for vertex
+ *   indices first..first+count-1 (no vertex buffers, no bindings): per vertex, 4 position
+ *   floats followed by 16 inter-stage floats (integer outputs of a vertex-only program as
+ *   their bits) in `out`, and 0 or a device error code in `errors`.
+ * gbr_wgsl_translate writes the CUDA C a vertex (+ fragment, when fragment_entry is not null)
+ *   program translates to; `needed` receives its size including the terminator.
+ * gbr_wgsl_compile_check translates and compiles with NVRTC (no GPU needed), returning the log. */
+GBR_API gbr_status gbr_render_pipeline_eval_vertices(gbr_device device, gbr_render_pipeline pipeline,
+                                                     uint32_t first_vertex, uint32_t count, float* out,
+                                                     uint32_t* errors);
+GBR_API gbr_status gbr_wgsl_translate(const char* wgsl, uint64_t wgsl_len, const char* vertex_entry,
+                                      const char* fragment_entry, char* out, uint64_t capacity, uint64_t* needed);
+GBR_API gbr_status gbr_wgsl_compile_check(const char* wgsl, uint64_t wgsl_len, const char* vertex_entry,
+                                          const char* fragment_entry, char* log, uint64_t capacity);
+
 /* DeviceInterface::create_bind_group (device.rs:115-120 -> bind_group.rs:58-72,91-117). */
 GBR_API gbr_status gbr_bind_group_create(gbr_device device, const gbr_bind_group_desc* desc,
                                          gbr_bind_group* out_bind_group);

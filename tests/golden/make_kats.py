@@ -157,6 +157,58 @@ def main() -> None:
         size = int(re.search(r"size (\d+)", text).group(1))
         kats["image_goldens"].append({"name": png.stem, "oid": oid, "size": size, "source": rel(png)})
 
+    # naga-cranelift/src/tests.rs: the operator vectors of the shader arithmetic (casts, scalar
+    # binops, comparisons, unops), and the expected outputs of its structural tests (control
+    # flow, calls, constants, globals, composite access, matrices) by test name
+    p = REF / "naga-cranelift" / "src" / "tests.rs"
+    text = p.read_text()
+
+    def line_of(pos: int) -> int:
+        return text.count("\n", 0, pos) + 1
+
+    ops = []
+    for m in re.finditer(r'test_cast\("([^"]*)", "(\w+)", "(\w+)", "([^"]*)"\)', text):
+        ops.append({"kind": "cast", "value": m.group(1), "from": m.group(2), "to": m.group(3), "expected": m.group(4),
+                    "source": f"{rel(p)}:{line_of(m.start())}"})
+    for m in re.finditer(r'test_binop::<(\w+)>\("(\w+)", "([^"]*)", "([^"]+)", "([^"]*)", (-?[\d.]+)\)', text):
+        ops.append({"kind": "binop", "type": m.group(2), "left": m.group(3), "op": m.group(4), "right": m.group(5),
+                    "expected": float(m.group(6)), "source": f"{rel(p)}:{line_of(m.start())}"})
+    for m in re.finditer(r'test_compare\("(\w+)", "([^"]*)", "([^"]+)", "([^"]*)", (true|false)\)', text):
+        ops.append({"kind": "compare", "type": m.group(1), "left": m.group(2), "op": m.group(3), "right": m.group(4),
+                    "expected": m.group(5) == "true", "source": f"{rel(p)}:{line_of(m.start())}"})
+    for m in re.finditer(r'test_unop(?:::<\w+>)?\("(\w+)", "([^"]+)", "([^"]*)", (!?-?[\d.]+)\)', text):
+        exp = m.group(4)
+        val = (~int(exp[1:])) & 0xFFFFFFFF if exp.startswith("!") else float(exp)
+        ops.append({"kind": "unop", "type": m.group(1), "op": m.group(2), "input": m.group(3), "expected": val,
+                    "source": f"{rel(p)}:{line_of(m.start())}"})
+    for m in re.finditer(r'test_bool_unop\("([^"]+)", "(\w+)", (true|false)\)', text):
+        ops.append({"kind": "unop", "type": "bool", "op": m.group(1), "input": m.group(2),
+                    "expected": m.group(3) == "true", "source": f"{rel(p)}:{line_of(m.start())}"})
+    kats["shader_ops"] = ops
+
+    structural = []
+    for m in re.finditer(r"#\[test\]\s*(?:#\[[^\]]*\]\s*)*(?:pub )?fn (\w+)\(\)", text):
+        name = m.group(1)
+        body, line = fn_body(p, name)
+        if re.search(r"#\[ignore", text[m.start():m.end()]):
+            continue
+        vals = []
+        for a in re.finditer(r"assert_(?:abs_diff_)?eq!\(\s*(?:output|out|a)\s*,\s*(\[[^\]]*\]|-?[\d.]+)", body):
+            v = a.group(1)
+            if v.startswith("["):
+                vals.append([float(x) for x in v.strip("[]").split(",") if x.strip()])
+            else:
+                vals.append(float(v))
+        if "DivisionByZero" in body:
+            vals.append("DivisionByZero")
+        if vals:
+            rec = {"test": name, "expected": vals, "source": f"{rel(p)}:{line}"}
+            if "mat4x4f" in body:  # the input columns and vector of the matrix tests
+                rec["vec4_literals"] = [[float(x) for x in v.split(",")]
+                                        for v in re.findall(r"vec4f\(([^()]+,[^()]+,[^()]+,[^()]+)\)", body)]
+            structural.append(rec)
+    kats["shader_programs"] = structural
+
     OUT.write_text(json.dumps(kats, indent=1) + "\n")
     print(f"wrote {OUT} ({sum(len(v) for v in kats.values())} records)")
 

@@ -23,7 +23,9 @@ OUT_DIR = os.path.join(HERE, "wgpu_gb300")
 LIB = os.path.join(OUT_DIR, "libgbr.so")
 BUILD = os.path.join(HERE, "_build")
 
-SOURCES = ["kernels.cu", "runtime.cu"]
+SOURCES = ["kernels.cu", "runtime.cu", "jit.cu", "wgsl.cpp"]
+# headers compiled again at run time by NVRTC for WGSL programs (embedded in the library)
+JIT_HEADERS = ["gbr_types.h", "exact.cuh", "programs.cuh", "raster.cuh", "raster_vis.cuh", "wgsl_rt.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -36,7 +38,28 @@ def nvcc() -> str:
 
 def _flags():
     return ["-std=c++17", "-O3", *ARCH, "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
-            "-I", os.path.join(ROOT, "include"), "-I", CSRC]
+            "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-I", BUILD]
+
+
+def write_jit_sources() -> str:
+    """jit_sources.inc: the kernel headers as raw string literals, with their names."""
+    out = os.path.join(BUILD, "jit_sources.inc")
+    parts = ["// generated by build_lib.py from csrc/: the headers NVRTC compiles with each WGSL program",
+             "static const char* const kJitHeaderNames[] = {" + ", ".join(f'"{h}"' for h in JIT_HEADERS) + "};",
+             "static const char* const kJitHeaders[] = {"]
+    for h in JIT_HEADERS:
+        text = open(os.path.join(CSRC, h)).read()
+        if ")GBRJIT\"" in text:
+            raise RuntimeError(f"{h} contains the raw-string delimiter")
+        # split into pieces below the compiler's string-literal limit
+        chunks = [text[i:i + 12000] for i in range(0, len(text), 12000)] or [""]
+        parts.append("    " + "\n".join(f'R"GBRJIT({c})GBRJIT"' for c in chunks) + ",")
+    parts.append("};")
+    data = "\n".join(parts) + "\n"
+    if not os.path.exists(out) or open(out).read() != data:
+        with open(out, "w") as f:
+            f.write(data)
+    return out
 
 
 def _stale(target: str, deps) -> bool:
@@ -48,12 +71,13 @@ def _stale(target: str, deps) -> bool:
 
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
+    write_jit_sources()
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "gbr.h"))
     objs, jobs = [], []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src.replace(".cu", ".o"))
+        o = os.path.join(BUILD, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s, *headers]):
             jobs.append([nvcc(), *_flags(), "-c", s, "-o", o])
@@ -69,7 +93,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         list(ex.map(run, jobs))
     if force or jobs or _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread"])
+        run([nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart", "-lpthread", "-ldl"])
         os.replace(tmp, LIB)
     return LIB
 

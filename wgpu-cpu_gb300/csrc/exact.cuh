@@ -5,7 +5,9 @@
 #pragma once
 
 #include <cuda_fp16.h>
+#ifndef __CUDACC_RTC__
 #include <stdint.h>
+#endif
 
 #include "gbr_types.h"
 

@@ -2,7 +2,17 @@
 // the render-pass path.  Everything here is device-resident per launch batch.
 #pragma once
 
+#ifdef __CUDACC_RTC__
+typedef unsigned char uint8_t;
+typedef unsigned short uint16_t;
+typedef unsigned int uint32_t;
+typedef int int32_t;
+typedef unsigned long long uint64_t;
+typedef long long int64_t;
+typedef unsigned long long uintptr_t;
+#else
 #include <stdint.h>
+#endif
 
 #ifdef __CUDACC__
 #define GBR_HD __host__ __device__
@@ -28,7 +38,8 @@ enum Program : uint32_t {
     PROG_MESH_TEX_LAMBERT = 4,
     PROG_QUAD_COLOR = 5,
     PROG_CLIP_PASSTHROUGH = 6,
-    PROG_COUNT = 7
+    PROG_JIT = 7,  // a WGSL program compiled into its own module (jit_vs / jit_fs)
+    PROG_COUNT = 8
 };
 
 enum Interp : uint8_t { INTERP_LINEAR = 0, INTERP_PERSPECTIVE = 1, INTERP_FLAT = 2 };
@@ -43,6 +54,7 @@ enum ErrorCode : uint32_t {
     ERR_OVERFLOW_BINS = 6,     // more tile entries than scratch slots (retried)
     ERR_SPAN_RANGE = 7,        // scanline coordinate outside u32 (scanline.rs:156-170)
     ERR_UNSUPPORTED = 8,
+    ERR_SHADER_TRAP = 9,  // a shader divided an integer by zero (EntryPointError::DivisionByZero)
 };
 
 // One texture binding as seen by the kernels.
@@ -130,7 +142,9 @@ struct DrawDesc {
     float blend_constant[4];
     // setup
     uint32_t fast_vs;        // FastVs: the vertex stage the fast setup path runs, or FAST_VS_NONE
-    uint32_t _pad_fast;
+    uint32_t interp;         // INTERP_LINEAR / INTERP_PERSPECTIVE of the program's inter-stage values
+    uint32_t may_discard;    // the fragment stage can discard
+    uint32_t _pad_d;
 };
 
 // Vertex stages the fast setup kernel specialises on: every input an f32 attribute of exactly

@@ -60,6 +60,10 @@ cudaError_t launch_raster_vis(const BatchParams& bp, int num_sms, cudaStream_t s
 }  // namespace
 
 size_t raster_state_bytes() { return sizeof(RasterState); }
+size_t setup_stage_bytes_host(uint32_t record_stride) { return setup_stage_bytes(record_stride); }
+size_t ordered_raster_smem_host(int warps, uint32_t record_stride) {
+    return (kCap + 2 * (size_t)warps * 32) * sizeof(uint32_t) + (size_t)kRW * record_stride;
+}
 
 // Seeded inputs for the division self-test: random bit patterns, raster-like magnitudes,
 // exact multiples and neighbours of powers of two, in rotation.
@@ -369,6 +373,7 @@ extern "C" GBR_API gbr_status gbr_render_triangles_noalloc(const float* clip_pos
     d.program = PROG_CLIP_PASSTHROUGH;
     d.has_fragment = 1;
     d.num_varyings = kNaVaryings;
+    d.interp = INTERP_LINEAR;
     d.profile = GBR_PROFILE_PARITY;
     d.cull_mode = state->cull_mode;
     d.front_face = state->front_face;

@@ -117,6 +117,12 @@ __host__ __device__ __forceinline__ uint32_t program_interp(uint32_t prog) {
     return prog == PROG_MESH_COLOR_PERSPECTIVE ? INTERP_PERSPECTIVE : INTERP_LINEAR;
 }
 
+#ifdef GBR_JIT
+// The WGSL program of a JIT module (emitted by wgsl.cpp, defined later in the same unit).
+__device__ bool jit_vs(const DrawDesc& d, uint32_t vertex, uint32_t instance, V4& pos, float* var, uint32_t* err);
+__device__ int jit_fs(const DrawDesc& d, const float* var, bool front_facing, uint32_t prim_index, V4 frag, V4& color);
+#endif
+
 // Vertex stage: position + varyings.  Returns false with *err set on a fetch error.  `mvp` is a
 // copy of the 16 floats at group 0 / binding 0 (the mesh programs' matrix), or null to read them
 // from the uniform buffer.
@@ -179,6 +185,9 @@ __device__ __forceinline__ bool run_vs(const DrawDesc& d, const float* mvp, uint
             var[3] = a1[3];
             return true;
         }
+#ifdef GBR_JIT
+        case PROG_JIT: return jit_vs(d, vertex, instance, pos, var, err);
+#endif
         default: *err = ERR_UNSUPPORTED; return false;
     }
 }
@@ -186,6 +195,7 @@ __device__ __forceinline__ bool run_vs(const DrawDesc& d, const float* mvp, uint
 // What the fragment stage and the output merger need of a draw, cached per warp in shared
 // memory by the raster kernel (built from the DrawDesc in global memory).
 struct RasterState {
+    const DrawDesc* dd;  // the draw itself (for programs that read more of it)
     uint32_t draw;  // DrawDesc index this copy was built from
     uint32_t program, nvar, interp;
     uint32_t sc_x0, sc_y0, sc_x1, sc_y1;
@@ -200,10 +210,11 @@ struct RasterState {
 };
 
 __device__ __forceinline__ void build_raster_state(const DrawDesc& d, uint32_t di, RasterState& rs) {
+    rs.dd = &d;
     rs.draw = di;
     rs.program = d.program;
     rs.nvar = d.num_varyings;
-    rs.interp = program_interp(d.program);
+    rs.interp = d.interp;
     rs.sc_x0 = d.sc_x0;
     rs.sc_y0 = d.sc_y0;
     rs.sc_x1 = d.sc_x1;

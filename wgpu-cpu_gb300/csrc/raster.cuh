@@ -1010,6 +1010,26 @@ struct PixelState {
     float depth;
 };
 
+// The fragment stage of any program: native programs on the cached state; a JIT module's WGSL
+// program with its builtins — front_facing, primitive_index and @builtin(position), the
+// rasterizer's fragment (x, y, z, 1/w) composed with the barycentrics like any inter-stage
+// value (render_pass/fragment.rs:127-160, raster.rs:338-346).  False when discarded.
+__device__ __forceinline__ bool run_fs_any(const BatchParams& bp, const RasterState& rs, const TriRecord& r,
+                                           const float cmp[3], const float* var, const float* lut, V4& col) {
+#ifdef GBR_JIT
+    if (rs.program == PROG_JIT) {
+        auto lerp3 = [&](const float* v) {
+            return fadd(fadd(fmul(v[0], cmp[0]), fmul(v[1], cmp[1])), fmul(v[2], cmp[2]));
+        };
+        const V4 frag = {lerp3(r.vpx), lerp3(r.vpy), lerp3(r.fz), lerp3(r.fw)};
+        const int st = jit_fs(*rs.dd, var, (r.flags & 1u) != 0, r.prim_index, frag, col);
+        if (st == 2) raise_error(bp.status, ERR_SHADER_TRAP, r.key >> SUBTRI_BITS);
+        return st == 1;
+    }
+#endif
+    return run_fs_rs(rs, var, lut, col);
+}
+
 // Rank sort for small bins: every key counts the keys below it (keys are unique per tile) and
 // goes straight to its place; two barriers instead of a sorting network's log^2 stages.
 __device__ __forceinline__ void rank_sort(const uint32_t* in, uint32_t* out, uint32_t n) {
@@ -1308,7 +1328,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                                                    fmul(rv[2 * nvar + qv], cmp[2]));
                                 }
                             }
-                            if (!run_fs_rs(rs, var, s_lut, col)) continue;  // discard: no depth test, no write
+                            if (!run_fs_any(bp, rs, r, cmp, var, s_lut, col)) continue;  // discard: no depth test, no write
                         }
                         // late depth test at the first colour output (fragment.rs:427-453, 470-479)
                         if (KIND == 2 || (KIND == 0 && rs.depth_test)) {

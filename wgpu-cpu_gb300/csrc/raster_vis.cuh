@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                         }
                     }
                     V4 col;
-                    run_fs_rs(rs, var, s_lut, col);  // eligible programs never discard
+                    run_fs_any(bp, rs, r, cmp, var, s_lut, col);  // eligible programs never discard
                     if (rs.write_mask != 0xF) {
                         uint32_t dc[4] = {c[0], c[1], c[2], c[3]};
                         if (load_color) {

@@ -28,7 +28,9 @@
 
 #include "gbr.h"
 #include "gbr_types.h"
+#include "jit.h"
 #include "kernels.h"
+#include "wgsl.h"
 
 namespace gbr {
 namespace {
@@ -91,11 +93,18 @@ struct ProgramInfo {
     const char* name;
     uint32_t id;
     int num_inputs;
-    int input_loc[3], input_comps[3];
+    int input_loc[16], input_comps[16];
     uint32_t num_varyings;
     bool perspective;
     uint32_t uniform_min;  // bytes required at @group(0) @binding(0), 0 = none
     bool uses_texture;     // @group(1) @binding(0) texture_2d + @binding(1) sampler
+    // WGSL programs (PROG_JIT): every uniform binding's size, the sampled texture / sampler
+    // bindings, inputs read as integers, discard
+    bool jit = false;
+    uint32_t uniform_req[4][8] = {};
+    int tex_group = 1, tex_binding = 0, samp_group = 1, samp_binding = 1;
+    int input_kind[16] = {};
+    bool may_discard = false;
 };
 const ProgramInfo kPrograms[] = {
     {"colored_triangle", PROG_COLORED_TRIANGLE, 0, {0, 0, 0}, {0, 0, 0}, 4, false, 0, false},
@@ -110,6 +119,22 @@ const ProgramInfo* find_program(const char* name) {
     for (const auto& p : kPrograms)
         if (std::strcmp(p.name, name) == 0) return &p;
     return nullptr;
+}
+
+// WGSL front end with its errors as status codes
+std::shared_ptr<wgsl::Module> parse_wgsl(const char* src, uint64_t len) {
+    try {
+        return wgsl::parse(std::string(src, len));
+    } catch (const wgsl::Error& e) {
+        fail(e.unsupported ? GBR_ERR_UNSUPPORTED : GBR_ERR_SHADER, "%s", e.what());
+    }
+}
+wgsl::ProgramCode emit_wgsl(const wgsl::Module& vs, const std::string& ve, const wgsl::Module* fs, const std::string& fe) {
+    try {
+        return wgsl::emit_program(vs, ve, fs, fe);
+    } catch (const wgsl::Error& e) {
+        fail(e.unsupported ? GBR_ERR_UNSUPPORTED : GBR_ERR_SHADER, "%s", e.what());
+    }
 }
 
 // ---------------------------------------------------------------- objects
@@ -142,11 +167,14 @@ struct Sampler : Object {
     gbr_sampler_desc desc{};
 };
 struct ShaderModule : Object {
-    const ProgramInfo* prog = nullptr;
+    const ProgramInfo* prog = nullptr;        // native program
+    std::shared_ptr<wgsl::Module> wgsl;       // or a parsed WGSL module
 };
 struct Pipeline : Object {
     gbr_render_pipeline_desc desc{};
     const ProgramInfo* prog = nullptr;
+    ProgramInfo own;                          // the WGSL program's info (prog points here)
+    std::shared_ptr<JitKernels> jit;          // its kernels
     AttrDesc attr[16];
 };
 struct BindGroup : Object {
@@ -366,6 +394,7 @@ struct Batch {
     uint32_t total_prims = 0, total_tiles = 0, nvar = 0;
     uint32_t item = 0;         // the submission of a single-submission batch
     bool single_item = true;
+    std::shared_ptr<JitKernels> jit;  // the WGSL module whose kernels run this batch (or none)
 };
 
 // Visibility raster (kind 3): every target has colour and depth, and every draw writes depth
@@ -381,7 +410,7 @@ uint32_t visibility_compare(const Batch& b) {
         return 0;
     for (const DrawDesc& d : b.draws)
         if (!d.depth_test || !d.depth_write || d.depth_compare != cmp || d.blend_enabled || !d.has_fragment ||
-            d.program == PROG_MESH_COLOR_DISCARD)
+            d.program == PROG_MESH_COLOR_DISCARD || d.may_discard)
             return 0;
     return cmp;
 }
@@ -393,6 +422,7 @@ uint32_t visibility_compare(const Batch& b) {
 // otherwise 0, the generic ordered kernel.
 int fragment_kind(const Batch& b, bool allow_visibility) {
     if (allow_visibility && visibility_compare(b)) return 3;
+    if (b.jit) return 0;  // a WGSL module carries the generic and the visibility raster only
     if (b.draws.empty() || b.targets.size() != 1 || !b.targets[0].color) return 0;
     const uint32_t fmt = b.targets[0].color_format;
     bool k1 = fmt == GBR_TEXTURE_FORMAT_RGBA16_FLOAT, k2 = fmt == GBR_TEXTURE_FORMAT_RGBA8_UNORM ||
@@ -539,7 +569,7 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
                 uint64_t size = en.size ? en.size : b->size - en.offset;
                 d.uniform[g][en.binding] = b->ptr + en.offset;
                 d.uniform_size[g][en.binding] = size;
-            } else if (en.kind == GBR_BINDING_TEXTURE_VIEW && g == 1 && en.binding == 0) {
+            } else if (en.kind == GBR_BINDING_TEXTURE_VIEW && g == prog.tex_group && (int)en.binding == prog.tex_binding) {
                 auto* t = static_cast<Texture*>(obj);
                 d.tex.data = t->ptr;
                 d.tex.width = t->desc.size.width;
@@ -547,7 +577,7 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
                 d.tex.format = t->desc.format;
                 d.tex.mip_count = t->mips_stored;
                 for (uint32_t m = 0; m < t->mips_stored && m < 16; ++m) d.tex.mip_offset[m] = t->mip_offset[m];
-            } else if (en.kind == GBR_BINDING_SAMPLER && g == 1 && en.binding == 1) {
+            } else if (en.kind == GBR_BINDING_SAMPLER && g == prog.samp_group && (int)en.binding == prog.samp_binding) {
                 auto* s = static_cast<Sampler*>(obj);
                 d.samp.address_u = s->desc.address_mode_u;
                 d.samp.address_v = s->desc.address_mode_v;
@@ -561,24 +591,35 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
     }
     if (prog.uniform_min && (!d.uniform[0][0] || d.uniform_size[0][0] < prog.uniform_min))
         fail(GBR_ERR_VALIDATION, "No such binding resource: uniform @group(0) @binding(0)");
+    for (int g = 0; g < 4; ++g)
+        for (int b = 0; b < 8; ++b)
+            if (prog.uniform_req[g][b] && (!d.uniform[g][b] || d.uniform_size[g][b] < prog.uniform_req[g][b]))
+                fail(GBR_ERR_VALIDATION, "No such binding resource: uniform @group(%d) @binding(%d) of %u bytes", g, b,
+                     prog.uniform_req[g][b]);
     if (prog.uses_texture) {
-        if (!d.tex.data) fail(GBR_ERR_VALIDATION, "No such binding resource: texture @group(1) @binding(0)");
+        if (!d.tex.data)
+            fail(GBR_ERR_VALIDATION, "No such binding resource: texture @group(%d) @binding(%d)", prog.tex_group,
+                 prog.tex_binding);
         if (d.tex.format != GBR_TEXTURE_FORMAT_RGBA8_UNORM && d.tex.format != GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB)
             fail(GBR_ERR_UNSUPPORTED, "sampling this texture format is todo!() (texture.rs:186)");
         if (d.samp.address_u == GBR_ADDRESS_CLAMP_TO_BORDER || d.samp.address_v == GBR_ADDRESS_CLAMP_TO_BORDER)
             fail(GBR_ERR_UNSUPPORTED, "ClampToBorder is todo!() (binding.rs:160)");
         bool have_sampler = false;
-        for (int gi = 1; gi < 2; ++gi)
-            if (dc.groups[gi])
-                for (uint32_t e = 0; e < dc.groups[gi]->desc.entry_count; ++e)
-                    if (dc.groups[gi]->desc.entries[e].kind == GBR_BINDING_SAMPLER &&
-                        dc.groups[gi]->desc.entries[e].binding == 1)
-                        have_sampler = true;
-        if (!have_sampler) fail(GBR_ERR_VALIDATION, "No such binding resource: sampler @group(1) @binding(1)");
+        const int gi = prog.samp_group;
+        if (gi >= 0 && gi < GBR_MAX_BIND_GROUPS && dc.groups[gi])
+            for (uint32_t e = 0; e < dc.groups[gi]->desc.entry_count; ++e)
+                if (dc.groups[gi]->desc.entries[e].kind == GBR_BINDING_SAMPLER &&
+                    (int)dc.groups[gi]->desc.entries[e].binding == prog.samp_binding)
+                    have_sampler = true;
+        if (!have_sampler)
+            fail(GBR_ERR_VALIDATION, "No such binding resource: sampler @group(%d) @binding(%d)", prog.samp_group,
+                 prog.samp_binding);
     }
     d.program = prog.id;
     d.has_fragment = pd.has_fragment;
     d.num_varyings = prog.num_varyings;
+    d.interp = prog.perspective ? INTERP_PERSPECTIVE : INTERP_LINEAR;
+    d.may_discard = prog.may_discard ? 1u : 0u;
     d.profile = profile;
     d.cull_mode = ps.cull_mode;
     d.front_face = ps.front_face;
@@ -818,6 +859,8 @@ bool Device::merge_batch(Batch& into, Batch& b) {
         if (has(into.writes, t)) return false;
     const uint64_t kMaxPrims = (1ull << (32 - SUBTRI_BITS)) - 1;
     if ((uint64_t)into.total_prims + b.total_prims > kMaxPrims) return false;
+    if (into.jit && b.jit && into.jit != b.jit) return false;
+    if (!into.jit) into.jit = b.jit;
     const uint32_t tbase = (uint32_t)into.targets.size();
     for (DrawDesc d : b.draws) {
         d.prim_base += into.total_prims;
@@ -847,6 +890,7 @@ std::vector<Batch> Device::split_batch(const Batch& m) {
             out.emplace_back();
             out.back().item = it;
             out.back().single_item = true;
+            out.back().jit = m.jit;
         }
         new_target[t] = (uint32_t)out[k].targets.size();
         out[k].targets.push_back(m.targets[t]);
@@ -905,7 +949,15 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
             p_prims += (uint64_t)ppi * (dc.inst_end > dc.inst_start ? dc.inst_end - dc.inst_start : 0);
         }
         const uint64_t kMaxPrims = (1ull << (32 - SUBTRI_BITS)) - 1;
-        if (cfg.launch_mode == GBR_LAUNCH_PER_DRAW && !p.draws.empty()) {
+        // the WGSL modules the pass's draws run: one batch runs at most one
+        std::shared_ptr<JitKernels> p_jit;
+        bool several_jit = false;
+        for (const DrawCmd& dc : p.draws)
+            if (dc.pipeline->jit) {
+                if (p_jit && p_jit != dc.pipeline->jit) several_jit = true;
+                p_jit = dc.pipeline->jit;
+            }
+        if ((cfg.launch_mode == GBR_LAUNCH_PER_DRAW || several_jit) && !p.draws.empty()) {
             open = false;
             bool first = true;
             for (const DrawCmd& dc : p.draws) {
@@ -915,6 +967,7 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
                 b.target_item.push_back(item);
                 b.writes = p_write;
                 b.reads = p_read;
+                b.jit = dc.pipeline->jit;
                 first = false;
                 DrawDesc d = make_draw(dc, profile, (bool)p.depth);
                 uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
@@ -932,12 +985,14 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
             for (const Texture* t : p_write) conflict = conflict || has(cur.writes, t) || has(cur.reads, t);
             for (const Texture* t : p_read) conflict = conflict || has(cur.writes, t);
             if ((uint64_t)cur.total_prims + p_prims > kMaxPrims) conflict = true;
+            if (p_jit && cur.jit && p_jit != cur.jit) conflict = true;
         }
         if (conflict) {
             new_batch();
             open = true;
         }
         Batch& b = batches.back();
+        if (p_jit) b.jit = p_jit;
         const uint32_t ti = (uint32_t)b.targets.size();
         b.targets.push_back(make_target(p, true, tile, profile));
         b.target_item.push_back(item);
@@ -969,7 +1024,13 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
     for (size_t i = from; i < nb; ++i) {
         Batch& b = batches[i];
         int t = tile, w = warps;
-        if (autotune) tuning[i] = tuner_pick(b, &t, &w);
+        if (b.jit) {  // a WGSL module is compiled at one tile shape per raster kernel
+            const bool vis = fragment_kind(b, cfg.raster_order == GBR_RASTER_AUTO) == 3;
+            t = vis ? b.jit->vis_tile : b.jit->ord_tile;
+            w = vis ? b.jit->vis_warps : b.jit->ord_warps;
+        } else if (autotune) {
+            tuning[i] = tuner_pick(b, &t, &w);
+        }
         btile[i] = t;
         bwarps[i] = w;
         uint32_t base = 0;
@@ -1099,9 +1160,12 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                     bp.states = meta + states_off[i];
                     bp.vis_compare = visibility_compare(b);
                 }
-                cuda_check(launch_batch(bp, btile[i], bwarps[i], num_sms, stream, &run.launches,
-                                        revp->empty() ? nullptr : &(*revp)[2 * i], kinds[i]),
-                           "launch");
+                cudaEvent_t* ev = revp->empty() ? nullptr : &(*revp)[2 * i];
+                if (b.jit)
+                    cuda_check(launch_batch_jit(*b.jit, bp, num_sms, stream, &run.launches, ev, kinds[i]), "launch");
+                else
+                    cuda_check(launch_batch(bp, btile[i], bwarps[i], num_sms, stream, &run.launches, ev, kinds[i]),
+                               "launch");
             }
         };
         if (cfg.use_graphs && attempt == 0 && !any_tuning) {
@@ -1116,6 +1180,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 put(&batches[i].total_prims, sizeof(uint32_t));
                 put(&batches[i].total_tiles, sizeof(uint32_t));
                 put(&batches[i].nvar, sizeof(uint32_t));
+                const void* jp = batches[i].jit.get();
+                put(&jp, sizeof jp);
                 const size_t nd = batches[i].draws.size(), nt = batches[i].targets.size();
                 put(&nd, sizeof nd);
                 put(&nt, sizeof nt);
@@ -1158,7 +1224,9 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
             } else {
                 revp = &g.events;
                 for (size_t i = first_batch; i < nb; ++i)
-                    run.launches += batch_kernel_launches(batches[i].total_prims, btile[i], bwarps[i], kinds[i]);
+                    run.launches += batches[i].jit ? 2u + (batches[i].total_prims ? 4u : 0u) + (kinds[i] == 3 ? 1u : 0u)
+                                                   : batch_kernel_launches(batches[i].total_prims, btile[i], bwarps[i],
+                                                                           kinds[i]);
             }
             cuda_check(cudaGraphLaunch(graphs[key].exec, stream), "cudaGraphLaunch");
         } else {
@@ -1643,11 +1711,48 @@ GBR_API gbr_status gbr_shader_module_create_native(gbr_device dh, const char* na
 }
 GBR_API gbr_status gbr_shader_module_create(gbr_device dh, const char* wgsl, uint64_t len, gbr_shader_module* out) {
     GBR_TRY({
-        (void)wgsl;
-        (void)len;
-        (void)out;
-        get_device(dh);
-        fail(GBR_ERR_UNSUPPORTED, "WGSL translation is not available in this build; use a native program");
+        auto d = get_device(dh);
+        if (!wgsl || !out) fail(GBR_ERR_INVALID_ARGUMENT, "null argument");
+        auto m = std::make_shared<ShaderModule>();
+        m->wgsl = parse_wgsl(wgsl, len);
+        if (wgsl::entry_points(*m->wgsl).empty()) fail(GBR_ERR_SHADER, "the module has no entry point");
+        *out = d->add(m);
+    })
+}
+
+GBR_API gbr_status gbr_wgsl_translate(const char* wgsl, uint64_t len, const char* vertex_entry, const char* fragment_entry,
+                                      char* out, uint64_t capacity, uint64_t* needed) {
+    GBR_TRY({
+        if (!wgsl) fail(GBR_ERR_INVALID_ARGUMENT, "null argument");
+        auto m = parse_wgsl(wgsl, len);
+        const wgsl::ProgramCode pc = emit_wgsl(*m, vertex_entry ? vertex_entry : "", fragment_entry ? m.get() : nullptr,
+                                               fragment_entry ? fragment_entry : "");
+        if (needed) *needed = pc.cuda.size() + 1;
+        if (out && capacity) {
+            const size_t k = std::min<size_t>(capacity - 1, pc.cuda.size());
+            std::memcpy(out, pc.cuda.data(), k);
+            out[k] = 0;
+        }
+    })
+}
+
+GBR_API gbr_status gbr_wgsl_compile_check(const char* wgsl, uint64_t len, const char* vertex_entry,
+                                          const char* fragment_entry, char* log, uint64_t capacity) {
+    GBR_TRY({
+        if (!wgsl) fail(GBR_ERR_INVALID_ARGUMENT, "null argument");
+        auto m = parse_wgsl(wgsl, len);
+        const wgsl::ProgramCode pc = emit_wgsl(*m, vertex_entry ? vertex_entry : "", fragment_entry ? m.get() : nullptr,
+                                               fragment_entry ? fragment_entry : "");
+        std::vector<char> cubin;
+        std::vector<std::string> names;
+        std::string lg;
+        const bool ok = jit_compile_cubin(pc.cuda, &cubin, &names, &lg);
+        if (log && capacity) {
+            const size_t k = std::min<size_t>(capacity - 1, lg.size());
+            std::memcpy(log, lg.data(), k);
+            log[k] = 0;
+        }
+        if (!ok) fail(GBR_ERR_SHADER, "NVRTC: %s", lg.substr(0, 400).c_str());
     })
 }
 GBR_API gbr_status gbr_shader_module_destroy(gbr_device dh, gbr_shader_module m) {
@@ -1667,7 +1772,56 @@ GBR_API gbr_status gbr_render_pipeline_create(gbr_device dh, const gbr_render_pi
         pl->desc = *desc;
         auto vs = d->get<ShaderModule>(desc->vertex_module, "shader module");
         pl->prog = vs->prog;
-        if (desc->has_fragment) {
+        if (vs->wgsl) {
+            // WGSL: emit the vertex (+ fragment) program and compile it with the kernels
+            std::shared_ptr<ShaderModule> fs;
+            if (desc->has_fragment) {
+                fs = d->get<ShaderModule>(desc->fragment_module, "shader module");
+                if (!fs->wgsl) fail(GBR_ERR_UNSUPPORTED, "a WGSL vertex stage needs a WGSL fragment stage");
+            }
+            auto entry = [](const char* name, const wgsl::Module& m, int stage) {
+                std::string e(name, strnlen(name, GBR_MAX_ENTRY_POINT_NAME));
+                if (!e.empty()) return e;
+                std::string only;
+                int count = 0;
+                for (const auto& ep : wgsl::entry_points(m))
+                    if (ep.second == stage) {
+                        only = ep.first;
+                        ++count;
+                    }
+                if (count != 1) fail(GBR_ERR_VALIDATION, "an entry point name is required (%d candidates)", count);
+                return only;
+            };
+            const wgsl::ProgramCode pc =
+                emit_wgsl(*vs->wgsl, entry(desc->vertex_entry_point, *vs->wgsl, 0), fs ? fs->wgsl.get() : nullptr,
+                          fs ? entry(desc->fragment_entry_point, *fs->wgsl, 1) : std::string());
+            ProgramInfo& pi = pl->own;
+            pi.name = "wgsl";
+            pi.id = PROG_JIT;
+            pi.jit = true;
+            pi.num_inputs = pc.num_inputs;
+            for (int i = 0; i < pc.num_inputs; ++i) {
+                pi.input_loc[i] = pc.input_loc[i];
+                pi.input_comps[i] = pc.input_comps[i];
+                pi.input_kind[i] = pc.input_kind[i];
+            }
+            pi.num_varyings = pc.num_varyings;
+            pi.perspective = pc.perspective;
+            pi.uniform_min = 0;
+            std::memcpy(pi.uniform_req, pc.uniform_size, sizeof pi.uniform_req);
+            pi.uses_texture = pc.tex_group >= 0;
+            if (pi.uses_texture) {
+                pi.tex_group = pc.tex_group;
+                pi.tex_binding = pc.tex_binding;
+                pi.samp_group = pc.samp_group;
+                pi.samp_binding = pc.samp_binding;
+            }
+            pi.may_discard = pc.may_discard;
+            std::string err;
+            pl->jit = jit_module(pc.cuda, &err);
+            if (!pl->jit) fail(GBR_ERR_SHADER, "%s", err.c_str());
+            pl->prog = &pl->own;
+        } else if (desc->has_fragment) {
             auto fs = d->get<ShaderModule>(desc->fragment_module, "shader module");
             if (fs->prog != vs->prog)
                 fail(GBR_ERR_UNSUPPORTED, "native programs pair their own vertex and fragment stages");
@@ -1705,6 +1859,50 @@ GBR_API gbr_status gbr_render_pipeline_create(gbr_device dh, const gbr_render_pi
         *out = d->add(pl);
     })
 }
+GBR_API gbr_status gbr_render_pipeline_eval_vertices(gbr_device dh, gbr_render_pipeline ph, uint32_t first_vertex,
+                                                     uint32_t count, float* out, uint32_t* errors) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        auto pl = d->get<Pipeline>(ph, "pipeline");
+        if (!pl->jit) fail(GBR_ERR_UNSUPPORTED, "only WGSL pipelines can be evaluated");
+        if (!out || !errors || !count) fail(GBR_ERR_INVALID_ARGUMENT, "null argument");
+        // evaluated without bindings: a program that reads a uniform buffer cannot run here
+        for (int g = 0; g < 4; ++g)
+            for (int b = 0; b < 8; ++b)
+                if (pl->prog->uniform_req[g][b]) fail(GBR_ERR_UNSUPPORTED, "the vertex stage reads uniform buffers");
+        cudaSetDevice(d->ordinal);
+        DrawDesc dd{};
+        dd.program = PROG_JIT;
+        for (int l = 0; l < 16; ++l) dd.attr[l] = AttrDesc{-1, 0, 0, 0};
+        dd.num_varyings = pl->prog->num_varyings;
+        dd.profile = d->cfg.profile;
+        dd.instance_count = 1;
+        const size_t per = 4 + MAX_VARYING_FLOATS;
+        void *p_d = nullptr, *p_out = nullptr, *p_err = nullptr;
+        cudaStream_t s = nullptr;
+        auto cleanup = [&] {
+            if (s) cudaStreamDestroy(s);
+            cudaFree(p_d);
+            cudaFree(p_out);
+            cudaFree(p_err);
+        };
+        cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaMalloc(&p_d, sizeof dd);
+        if (e == cudaSuccess) e = cudaMalloc(&p_out, (size_t)count * per * sizeof(float));
+        if (e == cudaSuccess) e = cudaMalloc(&p_err, (size_t)count * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMemcpyAsync(p_d, &dd, sizeof dd, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess)
+            e = jit_eval_vertices(*pl->jit, static_cast<const DrawDesc*>(p_d), first_vertex, count,
+                                  static_cast<float*>(p_out), static_cast<uint32_t*>(p_err), s);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(out, p_out, (size_t)count * per * sizeof(float), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(errors, p_err, (size_t)count * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        cleanup();
+        cuda_check(e, "eval vertices");
+    })
+}
+
 GBR_API gbr_status gbr_render_pipeline_destroy(gbr_device dh, gbr_render_pipeline p) {
     GBR_TRY({
         auto d = get_device(dh);

@@ -217,6 +217,9 @@ OPTIONAL = {
     "shader_module_create": (i32, [u64, C.c_char_p, u64, P(u64)]),
     "device_elapsed_ms": (i32, [u64, u64, u64, P(f64)]),
     "device_flush_caches": (i32, [u64]),
+    "render_pipeline_eval_vertices": (i32, [u64, u64, u32, u32, P(C.c_float), P(u32)]),
+    "wgsl_translate": (i32, [C.c_char_p, u64, C.c_char_p, C.c_char_p, C.c_char_p, u64, P(u64)]),
+    "wgsl_compile_check": (i32, [C.c_char_p, u64, C.c_char_p, C.c_char_p, C.c_char_p, u64]),
 }
 
 

@@ -305,6 +305,39 @@ class ShaderModule(_Object):
 class RenderPipeline(_Object):
     _destroy = "render_pipeline_destroy"
 
+    def eval_vertices(self, first: int, count: int):
+        """Runs a WGSL pipeline's vertex stage alone for `count` vertex indices (no buffers, no
+        bindings): returns (positions [count, 4] f32, inter-stage values [count, 16] as raw
+        32-bit words, device error code per vertex)."""
+        lib = self.device.lib
+        if lib.render_pipeline_eval_vertices is None:
+            raise GbrError(A.ERR_UNSUPPORTED, "this library cannot evaluate vertex stages")
+        out = np.zeros((count, 20), dtype=np.float32)
+        errs = np.zeros(count, dtype=np.uint32)
+        _check(lib, lib.render_pipeline_eval_vertices(
+            self.device.handle, self.handle, first, count, out.ctypes.data_as(C.POINTER(C.c_float)),
+            errs.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return out[:, :4], out[:, 4:].view(np.uint32), errs
+
+
+def wgsl_translate(lib: "A.Lib", source: str, vertex_entry: str, fragment_entry: Optional[str] = None) -> str:
+    """The CUDA C the library emits for a WGSL vertex (+ fragment) program (no GPU needed)."""
+    src = source.encode()
+    need = C.c_uint64()
+    buf = C.create_string_buffer(1 << 22)
+    _check(lib, lib.wgsl_translate(src, len(src), vertex_entry.encode(),
+                                   fragment_entry.encode() if fragment_entry else None, buf, 1 << 22, C.byref(need)))
+    return buf.value.decode()
+
+
+def wgsl_compile_check(lib: "A.Lib", source: str, vertex_entry: str, fragment_entry: Optional[str] = None) -> str:
+    """Translates and compiles a WGSL program with NVRTC for sm_103a (no GPU needed); returns the log."""
+    src = source.encode()
+    buf = C.create_string_buffer(1 << 16)
+    _check(lib, lib.wgsl_compile_check(src, len(src), vertex_entry.encode(),
+                                       fragment_entry.encode() if fragment_entry else None, buf, 1 << 16))
+    return buf.value.decode()
+
 
 class BindGroup(_Object):
     _destroy = "bind_group_destroy"
