@@ -67,3 +67,127 @@ def render_scene(dev, builder, **kw):
     color = dev.read_texture(s.color)
     depth = dev.read_texture(s.depth) if s.depth is not None else None
     return color, depth, dev.submission_stats(idx).fragments_shaded
+
+
+def restart_strips(dev, n_indices, width, height, seed, index_format=W.IndexFormat.UINT32, instances=1,
+                   depth=W.CompareFunction.LESS, cull=W.Face.NONE, sep_prob=0.08):
+    """Triangle strips with primitive restart: a random index stream over random clip-space
+    vertices with separator indices (0xFFFF / 0xFFFFFFFF) at random positions — back to back,
+    first and last included — so runs of every length occur, short ones producing nothing."""
+    rng = np.random.default_rng(seed)
+    nv = 256
+    w = rng.uniform(0.4, 2.0, nv)
+    pos = np.stack([rng.uniform(-1.3, 1.3, nv) * w, rng.uniform(-1.3, 1.3, nv) * w,
+                    rng.uniform(0.0, 1.0, nv) * w, w], 1).astype(np.float32)
+    col = rng.uniform(0, 1, (nv, 4)).astype(np.float32)
+    sep = 0xFFFF if index_format == W.IndexFormat.UINT16 else 0xFFFFFFFF
+    idx = rng.integers(0, nv, n_indices).astype(np.int64)
+    mask = rng.random(n_indices) < sep_prob
+    mask[0] = True
+    mask[-1] = True
+    mask[n_indices // 2: n_indices // 2 + 3] = True
+    idx[mask] = sep
+    vb_pos = dev.create_buffer_init(pos)
+    vb_col = dev.create_buffer_init(col)
+    ib = dev.create_buffer_init(idx.astype(np.uint16 if index_format == W.IndexFormat.UINT16 else np.uint32))
+    sm = dev.create_shader_module(native="clip_passthrough")
+    pl = dev.create_render_pipeline(
+        sm, [W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 0)]),
+             W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 1)])],
+        W.PrimitiveState(W.PrimitiveTopology.TRIANGLE_STRIP, strip_index_format=index_format, cull_mode=cull),
+        W.DepthStencilState(True, depth), sm, [W.ColorTargetState(W.TextureFormat.RGBA8_UNORM)])
+    color = dev.create_texture(width, height, W.TextureFormat.RGBA8_UNORM)
+    dtex = dev.create_texture(width, height, W.TextureFormat.DEPTH32_FLOAT)
+    enc = dev.create_command_encoder()
+    rp = enc.begin_render_pass([W.RenderPassColorAttachment(color, (0.0, 0.0, 0.0, 1.0))],
+                               W.RenderPassDepthStencilAttachment(dtex, 1.0))
+    rp.set_pipeline(pl)
+    rp.set_vertex_buffer(0, vb_pos)
+    rp.set_vertex_buffer(1, vb_col)
+    rp.set_index_buffer(ib, index_format)
+    rp.draw_indexed(range(0, n_indices), 0, range(0, instances))
+    rp.end()
+    sub = dev.queue.submit([enc.finish()])
+    dev.poll(True, sub)
+    return dev.read_texture(color), dev.read_texture(dtex), dev.submission_stats(sub).fragments_shaded
+
+
+def lines_points(dev, topology, n, width, height, seed, index_format=None, restart=False, instances=1,
+                 depth=W.CompareFunction.LESS_EQUAL, scissor=None, clear=(0.0, 0.0, 0.0, 1.0)):
+    """Lines or points given in clip space (clip_passthrough program), crossing the clip planes:
+    line lists / strips (optionally indexed, with separator indices) and point lists."""
+    rng = np.random.default_rng(seed)
+    nv = n
+    w = rng.uniform(0.4, 2.0, nv)
+    pos = np.stack([rng.uniform(-1.4, 1.4, nv) * w, rng.uniform(-1.4, 1.4, nv) * w,
+                    rng.uniform(-0.2, 1.2, nv) * w, w], 1).astype(np.float32)
+    col = rng.uniform(0, 1, (nv, 4)).astype(np.float32)
+    vb_pos = dev.create_buffer_init(pos)
+    vb_col = dev.create_buffer_init(col)
+    sm = dev.create_shader_module(native="clip_passthrough")
+    sif = index_format if restart else W.IndexFormat.NONE
+    pl = dev.create_render_pipeline(
+        sm, [W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 0)]),
+             W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 1)])],
+        W.PrimitiveState(topology, strip_index_format=sif), W.DepthStencilState(True, depth), sm,
+        [W.ColorTargetState(W.TextureFormat.RGBA8_UNORM)])
+    color = dev.create_texture(width, height, W.TextureFormat.RGBA8_UNORM)
+    dtex = dev.create_texture(width, height, W.TextureFormat.DEPTH32_FLOAT)
+    enc = dev.create_command_encoder()
+    rp = enc.begin_render_pass([W.RenderPassColorAttachment(color, clear)], W.RenderPassDepthStencilAttachment(dtex, 1.0))
+    rp.set_pipeline(pl)
+    rp.set_vertex_buffer(0, vb_pos)
+    rp.set_vertex_buffer(1, vb_col)
+    if scissor is not None:
+        rp.set_scissor_rect(*scissor)
+    if index_format is not None:
+        idx = rng.permutation(nv).astype(np.int64)
+        if restart:
+            sep = 0xFFFF if index_format == W.IndexFormat.UINT16 else 0xFFFFFFFF
+            m = rng.random(nv) < 0.1
+            m[3:5] = True
+            idx[m] = sep
+        ib = dev.create_buffer_init(idx.astype(np.uint16 if index_format == W.IndexFormat.UINT16 else np.uint32))
+        rp.set_index_buffer(ib, index_format)
+        rp.draw_indexed(range(0, nv), 0, range(0, instances))
+    else:
+        rp.draw(range(0, nv), range(0, instances))
+    rp.end()
+    sub = dev.queue.submit([enc.finish()])
+    dev.poll(True, sub)
+    return dev.read_texture(color), dev.read_texture(dtex), dev.submission_stats(sub).fragments_shaded
+
+
+def mixed_pass(dev, width, height, seed):
+    """One pass: random triangles, then lines over them, then points, then more triangles, into the
+    same colour + depth target (draw order across topologies)."""
+    rng = np.random.default_rng(seed)
+    sm = dev.create_shader_module(native="clip_passthrough")
+    layouts = [W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 0)]),
+               W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 1)])]
+    ds = W.DepthStencilState(True, W.CompareFunction.LESS_EQUAL)
+    pls = {t: dev.create_render_pipeline(sm, layouts, W.PrimitiveState(t), ds, sm,
+                                         [W.ColorTargetState(W.TextureFormat.RGBA8_UNORM)])
+           for t in (W.PrimitiveTopology.TRIANGLE_LIST, W.PrimitiveTopology.LINE_LIST, W.PrimitiveTopology.POINT_LIST)}
+    color = dev.create_texture(width, height, W.TextureFormat.RGBA8_UNORM)
+    dtex = dev.create_texture(width, height, W.TextureFormat.DEPTH32_FLOAT)
+    enc = dev.create_command_encoder()
+    rp = enc.begin_render_pass([W.RenderPassColorAttachment(color, (0.2, 0.1, 0.0, 1.0))],
+                               W.RenderPassDepthStencilAttachment(dtex, 1.0))
+    keep = []
+    for topo, nv in [(W.PrimitiveTopology.TRIANGLE_LIST, 300), (W.PrimitiveTopology.LINE_LIST, 400),
+                     (W.PrimitiveTopology.POINT_LIST, 500), (W.PrimitiveTopology.TRIANGLE_LIST, 150)]:
+        w = rng.uniform(0.5, 1.5, nv)
+        pos = np.stack([rng.uniform(-1.2, 1.2, nv) * w, rng.uniform(-1.2, 1.2, nv) * w,
+                        rng.uniform(0.0, 1.0, nv) * w, w], 1).astype(np.float32)
+        col = rng.uniform(0, 1, (nv, 4)).astype(np.float32)
+        vp, vc = dev.create_buffer_init(pos), dev.create_buffer_init(col)
+        keep += [vp, vc]
+        rp.set_pipeline(pls[topo])
+        rp.set_vertex_buffer(0, vp)
+        rp.set_vertex_buffer(1, vc)
+        rp.draw(range(0, nv))
+    rp.end()
+    sub = dev.queue.submit([enc.finish()])
+    dev.poll(True, sub)
+    return dev.read_texture(color), dev.read_texture(dtex), dev.submission_stats(sub).fragments_shaded

@@ -239,3 +239,43 @@ def test_errors_are_reported(gpu):
     # the device stays usable after a failed submission
     s2 = wl.scene_colored_sphere(gpu, 64, 64)
     s2.render()
+
+
+@pytest.mark.parametrize("fmt,n,instances,order", [
+    (W.IndexFormat.UINT32, 600, 1, W.RasterOrder.AUTO), (W.IndexFormat.UINT16, 600, 2, W.RasterOrder.AUTO),
+    (W.IndexFormat.UINT32, 3000, 1, W.RasterOrder.ORDERED), (W.IndexFormat.UINT16, 2500, 3, W.RasterOrder.ORDERED)])
+def test_strip_primitive_restart(orc, fmt, n, instances, order):
+    """Triangle strips with separator indices (primitive.rs:428-487): every run restarts its own
+    strip (winding parity included), runs shorter than three yield nothing."""
+    dev = W.Device(raster_order=order)
+    try:
+        kw = dict(n_indices=n, width=160, height=120, seed=n + instances, index_format=fmt, instances=instances)
+        res = [scenes.restart_strips(d, **kw) for d in (dev, orc)]
+        assert_same(*res, f"restart {fmt} n={n}")
+        assert res[0][2] > 0
+    finally:
+        dev.close()
+
+
+@pytest.mark.parametrize("topology,fmt,restart,instances,scissor", [
+    (W.PrimitiveTopology.LINE_LIST, None, False, 1, None),
+    (W.PrimitiveTopology.LINE_LIST, W.IndexFormat.UINT32, False, 2, (13, 7, 150, 100)),
+    (W.PrimitiveTopology.LINE_STRIP, None, False, 1, None),
+    (W.PrimitiveTopology.LINE_STRIP, W.IndexFormat.UINT16, True, 2, None),
+    (W.PrimitiveTopology.LINE_STRIP, W.IndexFormat.UINT32, True, 1, (0, 20, 120, 80)),
+    (W.PrimitiveTopology.POINT_LIST, None, False, 3, None),
+    (W.PrimitiveTopology.POINT_LIST, W.IndexFormat.UINT16, False, 1, (5, 5, 100, 90)),
+])
+def test_lines_and_points(gpu, orc, topology, fmt, restart, instances, scissor):
+    """LineRasterizer (Cohen–Sutherland clip, Bresenham without the end point, t accumulated by
+    1/dx) and PointRasterizer, fragments in primitive order (raster.rs:197-265)."""
+    kw = dict(n=400, width=180, height=130, seed=31 + topology, index_format=fmt, restart=restart,
+              instances=instances, scissor=scissor)
+    res = [scenes.lines_points(d, topology, **kw) for d in (gpu, orc)]
+    assert_same(*res, f"topology {topology} fmt {fmt} restart {restart}")
+    assert res[0][2] > 0
+
+
+def test_mixed_topologies_in_one_pass(gpu, orc):
+    res = [scenes.mixed_pass(d, 200, 150, 5) for d in (gpu, orc)]
+    assert_same(*res, "triangles, lines, points, triangles")

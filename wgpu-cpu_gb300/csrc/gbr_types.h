@@ -144,7 +144,9 @@ struct DrawDesc {
     uint32_t fast_vs;        // FastVs: the vertex stage the fast setup path runs, or FAST_VS_NONE
     uint32_t interp;         // INTERP_LINEAR / INTERP_PERSPECTIVE of the program's inter-stage values
     uint32_t may_discard;    // the fragment stage can discard
-    uint32_t _pad_d;
+    uint32_t strip_restart;  // triangle strip with primitive restart (separator indices)
+    uint32_t strip_table;    // first entry of this draw's strip table in BatchParams::strip_info
+    uint32_t _pad_e;
 };
 
 // Vertex stages the fast setup kernel specialises on: every input an f32 attribute of exactly
@@ -220,6 +222,7 @@ struct BatchParams {
     BatchStatus* status;
     uint32_t* abort_flag;        // set by a failed batch; later batches of the submission skip
     uint32_t* slow_prims;        // [total_prims] primitives the fast setup path hands on
+    uint32_t* strip_info;        // strip tables of the restart draws (null when there are none)
     void* states;                // visibility raster: per-draw fragment-stage state (RasterState)
     uint32_t vis_compare;        // visibility raster: the batch's depth compare function
     uint32_t _pad;

@@ -89,7 +89,8 @@ const Nvrtc& nvrtc() {
 constexpr int kJitVisTile = 16, kJitVisWarps = 4, kJitOrdTile = 16, kJitOrdWarps = 8;
 const char* const kKernelExprs[] = {
     "&gbr::k_setup", "&gbr::k_setup_slow", "&gbr::k_scan", "&gbr::k_fill", "&gbr::k_build_states",
-    "&gbr::k_raster_vis<16, 4>", "&gbr::k_raster<16, 8, 4096, 64, 0>", "&gbr::k_eval_vs"};
+    "&gbr::k_raster_vis<16, 4>", "&gbr::k_raster<16, 8, 4096, 64, 0>", "&gbr::k_eval_vs", "&gbr::k_strip_table",
+    "&gbr::k_clear_targets", "&gbr::k_lines_points"};
 
 std::string program_source(const std::string& code) {
     std::string s;
@@ -105,7 +106,7 @@ std::string program_source(const std::string& code) {
          "  float* o = out + (size_t)i * (4 + MAX_VARYING_FLOATS);\n"
          "  o[0] = pos.x; o[1] = pos.y; o[2] = pos.z; o[3] = pos.w;\n"
          "  for (int k = 0; k < MAX_VARYING_FLOATS; ++k) o[4 + k] = var[k];\n}\n";
-    s += "}  // namespace gbr\n#include \"raster_vis.cuh\"\n";
+    s += "}  // namespace gbr\n#include \"raster_vis.cuh\"\n#include \"raster_lines.cuh\"\n";
     return s;
 }
 
@@ -193,7 +194,8 @@ std::shared_ptr<JitKernels> jit_module(const std::string& code, std::string* err
         *err = std::string("cudaLibraryLoadData: ") + cudaGetErrorString(e);
         return nullptr;
     }
-    cudaKernel_t* slots[] = {&k->setup, &k->slow, &k->scan, &k->fill, &k->states, &k->vis, &k->ordered, &k->eval};
+    cudaKernel_t* slots[] = {&k->setup, &k->slow, &k->scan, &k->fill, &k->states, &k->vis, &k->ordered, &k->eval,
+                             &k->strip, &k->clear, &k->lines};
     for (size_t i = 0; i < names.size(); ++i) {
         if ((e = cudaLibraryGetKernel(slots[i], k->lib, names[i].c_str())) != cudaSuccess) {
             *err = std::string("cudaLibraryGetKernel(") + names[i] + "): " + cudaGetErrorString(e);
@@ -230,6 +232,10 @@ cudaError_t launch_batch_jit(JitKernels& k, const BatchParams& bp, int num_sms, 
     }
     std::lock_guard<std::mutex> lk(k.mu);
     const uint32_t items = bp.total_prims;
+    if (bp.strip_info && items) {
+        if ((e = launch(k.strip, bp.num_draws, 1024, 0, s, bp)) != cudaSuccess) return e;
+        ++*launches;
+    }
     if (items) {
         const uint32_t g = std::min((items + 127) / 128, (uint32_t)num_sms * 16);
         const size_t smem = setup_stage_bytes_host(bp.record_stride);
@@ -279,6 +285,24 @@ cudaError_t launch_batch_jit(JitKernels& k, const BatchParams& bp, int num_sms, 
         if ((e = launch(k.ordered, grid, k.ord_warps * 32, smem, s, bp)) != cudaSuccess) return e;
     }
     ++*launches;
+    if (ev_raster) e = cudaEventRecordWithFlags(ev_raster[1], s, ev_flags);
+    return e;
+}
+
+cudaError_t launch_lines_jit(JitKernels& k, const BatchParams& bp, int num_sms, cudaStream_t s, uint32_t* launches,
+                             cudaEvent_t* ev_raster) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(bp.status, 0, sizeof(BatchStatus), s)) != cudaSuccess) return e;
+    unsigned int ev_flags = cudaEventRecordDefault;
+    if (ev_raster) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if ((e = cudaStreamIsCapturing(s, &cs)) != cudaSuccess) return e;
+        if (cs == cudaStreamCaptureStatusActive) ev_flags = cudaEventRecordExternal;
+    }
+    if ((e = launch(k.clear, num_sms * 4, 256, 0, s, bp)) != cudaSuccess) return e;
+    if (ev_raster && (e = cudaEventRecordWithFlags(ev_raster[0], s, ev_flags)) != cudaSuccess) return e;
+    if ((e = launch(k.lines, 1, 256, 0, s, bp)) != cudaSuccess) return e;
+    *launches += 2;
     if (ev_raster) e = cudaEventRecordWithFlags(ev_raster[1], s, ev_flags);
     return e;
 }

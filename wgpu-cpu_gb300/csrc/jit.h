@@ -17,7 +17,7 @@ namespace gbr {
 struct JitKernels {
     cudaLibrary_t lib = nullptr;
     cudaKernel_t setup = nullptr, slow = nullptr, scan = nullptr, fill = nullptr, states = nullptr, vis = nullptr,
-                 ordered = nullptr, eval = nullptr;
+                 ordered = nullptr, eval = nullptr, strip = nullptr, clear = nullptr, lines = nullptr;
     int vis_tile = 16, vis_warps = 4, ord_tile = 16, ord_warps = 8;
     std::mutex mu;  // launch configuration below
     size_t setup_smem = 0, ord_smem = 0;
@@ -39,6 +39,10 @@ std::shared_ptr<JitKernels> jit_module(const std::string& code, std::string* err
 // launch_batch (kernels.h) with a JIT module's kernels; kind 3 = visibility raster, else ordered.
 cudaError_t launch_batch_jit(JitKernels& k, const BatchParams& bp, int num_sms, cudaStream_t s, uint32_t* launches,
                              cudaEvent_t* ev_raster, int kind);
+
+// launch_lines (kernels.h) with a JIT module's kernels.
+cudaError_t launch_lines_jit(JitKernels& k, const BatchParams& bp, int num_sms, cudaStream_t s, uint32_t* launches,
+                             cudaEvent_t* ev_raster);
 
 // Runs the vertex stage alone for vertices first..first+n-1 of the draw at d_dev: per vertex,
 // 4 position floats and MAX_VARYING_FLOATS inter-stage floats at out_dev, an error code at errs_dev.

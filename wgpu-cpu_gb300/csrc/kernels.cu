@@ -7,6 +7,7 @@
 #include "gbr.h"
 #include "kernels.h"
 #include "raster.cuh"
+#include "raster_lines.cuh"
 #include "raster_vis.cuh"
 
 namespace gbr {
@@ -60,6 +61,25 @@ cudaError_t launch_raster_vis(const BatchParams& bp, int num_sms, cudaStream_t s
 }  // namespace
 
 size_t raster_state_bytes() { return sizeof(RasterState); }
+
+cudaError_t launch_lines(const BatchParams& bp, int num_sms, cudaStream_t s, uint32_t* launches, cudaEvent_t* ev_raster) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(bp.status, 0, sizeof(BatchStatus), s)) != cudaSuccess) return e;
+    unsigned int ev_flags = cudaEventRecordDefault;
+    if (ev_raster) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if ((e = cudaStreamIsCapturing(s, &cs)) != cudaSuccess) return e;
+        if (cs == cudaStreamCaptureStatusActive) ev_flags = cudaEventRecordExternal;
+    }
+    k_clear_targets<<<num_sms * 4, 256, 0, s>>>(bp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (ev_raster && (e = cudaEventRecordWithFlags(ev_raster[0], s, ev_flags)) != cudaSuccess) return e;
+    k_lines_points<<<1, kLineThreads, 0, s>>>(bp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    *launches += 2;
+    if (ev_raster) e = cudaEventRecordWithFlags(ev_raster[1], s, ev_flags);
+    return e;
+}
 size_t setup_stage_bytes_host(uint32_t record_stride) { return setup_stage_bytes(record_stride); }
 size_t ordered_raster_smem_host(int warps, uint32_t record_stride) {
     return (kCap + 2 * (size_t)warps * 32) * sizeof(uint32_t) + (size_t)kRW * record_stride;
@@ -131,6 +151,7 @@ uint32_t batch_kernel_launches(uint32_t total_prims, int tile, int warps, int ki
 }
 
 uint32_t fast_vs_kind(const DrawDesc& d) {
+    if (d.strip_restart) return FAST_VS_NONE;  // the strip table is read by the generic setup
     auto f32 = [&](int loc, uint32_t fmt) {
         const AttrDesc& a = d.attr[loc];
         return a.buffer >= 0 && a.format == fmt && a.offset % 4 == 0 && d.vb_stride_vertex[a.buffer] % 4 == 0 &&
@@ -172,6 +193,11 @@ cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms
     if ((e = cudaMemsetAsync(bp.work_counter, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
     const uint32_t items = bp.total_prims;
     const uint32_t cap = (uint32_t)num_sms * 16;
+    if (bp.strip_info && items) {
+        k_strip_table<<<bp.num_draws, 1024, 0, s>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        ++*launches;
+    }
     if (items) {
         uint32_t g = std::min((items + 127) / 128, cap);
         const size_t smem = setup_stage_bytes(bp.record_stride);
@@ -404,7 +430,7 @@ extern "C" GBR_API gbr_status gbr_render_triangles_noalloc(const float* clip_pos
     t.tiles_x = (width + kNaTile - 1) / kNaTile;
     t.tiles_y = (height + kNaTile - 1) / kNaTile;
 
-    BatchParams bp;
+    BatchParams bp{};
     std::memset(&bp, 0, sizeof bp);
     bp.draws = reinterpret_cast<const DrawDesc*>(scratch + kNaDraw);
     bp.targets = reinterpret_cast<const TargetDesc*>(scratch + kNaTarget);

@@ -17,6 +17,9 @@ namespace gbr {
 cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms, cudaStream_t s, uint32_t* launches,
                          cudaEvent_t* ev_raster = nullptr, int kind = 0);
 
+// The one line / point draw of a batch (k_clear_targets + k_lines_points, primitive order).
+cudaError_t launch_lines(const BatchParams& bp, int num_sms, cudaStream_t s, uint32_t* launches, cudaEvent_t* ev_raster);
+
 // Tile side / warps-per-tile pairs compiled into the library.
 bool raster_config_supported(int tile, int warps);
 

@@ -400,6 +400,94 @@ __device__ __forceinline__ void coop_tiles(const BatchParams& bp, const TriRecor
     }
 }
 
+// ---- strips with primitive restart (render_pass/primitive.rs:428-487, index.rs:90-106)
+// Each run of indices between separators is a strip of its own: the triangle completed at stream
+// position k (at least two positions into its run) is (k-2, k-1, k) or, when k - run_start is
+// odd, (k-1, k-2, k).  k_strip_table writes for every position of a restart draw
+//   (compact primitive index << 1) | parity, or ~0 when k completes no triangle,
+// scanning the index stream once (separator positions by a max-scan, completed triangles by a
+// sum-scan), one CTA per draw.  Setup reads it for primitive slot k - 2.
+constexpr uint32_t kNoStripTri = 0xFFFFFFFFu;
+
+__global__ void __launch_bounds__(1024) k_strip_table(BatchParams bp) {
+    const DrawDesc& d = bp.draws[blockIdx.x];
+    if (!d.strip_restart) return;
+    __shared__ int s_wmax[32];
+    __shared__ uint32_t s_wsum[32];
+    __shared__ int s_carry_max;
+    __shared__ uint32_t s_carry_sum;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    if (tid == 0) {
+        s_carry_max = -1;  // last separator position so far
+        s_carry_sum = 0;   // triangles so far
+    }
+    __syncthreads();
+    const uint32_t n = d.count;
+    const bool u16 = d.index_format == 1;
+    const uint32_t isz = u16 ? 2u : 4u;
+    for (uint32_t base = 0; base < n; base += 1024) {
+        const uint32_t k = base + tid;
+        bool sep = false, valid = k < n;
+        if (valid) {
+            const uint32_t at = d.first + k;
+            if ((uint64_t)(at + 1) * isz <= d.index_bytes) {
+                sep = u16 ? __ldg(reinterpret_cast<const uint16_t*>(d.index_data) + at) == 0xFFFFu
+                          : __ldg(reinterpret_cast<const uint32_t*>(d.index_data) + at) == 0xFFFFFFFFu;
+            }
+        }
+        // inclusive max-scan of separator positions
+        int m = sep ? (int)k : -1;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xFFFFFFFFu, m, o);
+            if (lane >= o) m = max(m, y);
+        }
+        if (lane == 31) s_wmax[wid] = m;
+        __syncthreads();
+        if (wid == 0) {
+            int w = s_wmax[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+                if (lane >= o) w = max(w, y);
+            }
+            s_wmax[lane] = w;
+        }
+        __syncthreads();
+        const int last_sep = max(max(m, wid ? s_wmax[wid - 1] : -1), s_carry_max);
+        const int run_start = last_sep + 1;
+        const bool tri = valid && !sep && (int)k - run_start >= 2;
+        // exclusive sum-scan of completed triangles
+        uint32_t c = tri ? 1u : 0u, x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_wsum[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t w = s_wsum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+                if (lane >= o) w += y;
+            }
+            s_wsum[lane] = w;
+        }
+        __syncthreads();
+        const uint32_t before = s_carry_sum + (wid ? s_wsum[wid - 1] : 0u) + x - c;
+        if (valid)
+            bp.strip_info[d.strip_table + k] = tri ? ((before << 1) | (uint32_t)(((int)k - run_start) & 1)) : kNoStripTri;
+        __syncthreads();
+        if (tid == 1023) {
+            s_carry_max = max(s_carry_max, s_wmax[31]);
+            s_carry_sum = before + c;
+        }
+        __syncthreads();
+    }
+}
+
 // ---- generic setup: any program, format, topology; clipping; error reporting
 // Sets up primitive gp of draw di (record written in place); a record spanning many tile rows
 // is returned in `coop` for the warp to count together.
@@ -416,7 +504,17 @@ __device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp
     prim_rec->nsub = 0;
     prim_rec->draw = di;
     uint32_t sp[3];
-    if (d.topology == 4) {  // triangle strip (primitive.rs:360-392)
+    uint32_t prim_index = p;  // @builtin(primitive_index)
+    if (d.strip_restart) {
+        // slot p is stream position p + 2 (strip table above)
+        const uint32_t info = bp.strip_info[d.strip_table + p + 2];
+        if (info == kNoStripTri) return;  // no triangle ends here: the record stays empty
+        const uint32_t k = p + 2;
+        sp[0] = (info & 1u) ? k - 1 : k - 2;
+        sp[1] = (info & 1u) ? k - 2 : k - 1;
+        sp[2] = k;
+        prim_index = info >> 1;
+    } else if (d.topology == 4) {  // triangle strip (primitive.rs:360-392)
         sp[0] = (p & 1u) ? p + 1 : p;
         sp[1] = (p & 1u) ? p : p + 1;
         sp[2] = p + 2;
@@ -467,7 +565,7 @@ __device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp
             v[i].b[1] = i == 1 ? 1.0f : 0.0f;
             v[i].b[2] = i == 2 ? 1.0f : 0.0f;
         }
-        if (!build_record(bp, d, prim_rec, gp << SUBTRI_BITS, di, p, front_facing, v, inv_w0, var, nvar)) {
+        if (!build_record(bp, d, prim_rec, gp << SUBTRI_BITS, di, prim_index, front_facing, v, inv_w0, var, nvar)) {
             raise_error(bp.status, ERR_W_ZERO, gp);
             prim_rec->flags = 2u;
             return;
@@ -513,7 +611,7 @@ __device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp
             ++s;
         }
     };
-    Emitter emitter{&bp, &d, prim_rec, gp, di, p, ovf, 0, front_facing, inv_w0, var, nvar};
+    Emitter emitter{&bp, &d, prim_rec, gp, di, prim_index, ovf, 0, front_facing, inv_w0, var, nvar};
     clip_tri_ordered(pos, emitter);
     if (nsub == 0) prim_rec->flags = 2u;
     prim_rec->nsub = nsub;

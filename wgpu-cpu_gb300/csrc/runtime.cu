@@ -311,7 +311,7 @@ struct Device {
 
     // worker-owned scratch
     uint64_t scratch_bytes = 0;
-    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf, slow_buf;
+    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf, slow_buf, strip_buf;
     uint32_t ovf_capacity = 4096;
     uint64_t bin_capacity = 1u << 22;
 
@@ -390,10 +390,12 @@ struct Batch {
     std::vector<TargetDesc> targets;
     std::vector<uint32_t> target_item;       // submission (index in its group) of each target
     std::vector<const Texture*> writes, reads;  // attachments written, textures sampled
+    uint32_t strip_entries = 0;              // strip-table entries of the restart draws
     std::vector<uint64_t> target_frags;      // fragments shaded into each target (after the run)
     uint32_t total_prims = 0, total_tiles = 0, nvar = 0;
     uint32_t item = 0;         // the submission of a single-submission batch
     bool single_item = true;
+    bool lines = false;        // one line / point draw, drawn by k_lines_points
     std::shared_ptr<JitKernels> jit;  // the WGSL module whose kernels run this batch (or none)
 };
 
@@ -517,6 +519,19 @@ TargetDesc make_target(const PassCmd& p, bool first_in_pass, uint32_t tile, uint
     return t;
 }
 
+// Primitive slots of `count` stream positions (primitive.rs:248-264, 324-358): lists take whole
+// groups, strips one per position after the first (or two); with primitive restart a slot can stay
+// empty.
+uint32_t primitive_slots(uint32_t topology, uint32_t count) {
+    switch (topology) {
+        case GBR_TOPOLOGY_POINT_LIST: return count;
+        case GBR_TOPOLOGY_LINE_LIST: return count / 2;
+        case GBR_TOPOLOGY_LINE_STRIP: return count >= 2 ? count - 1 : 0;
+        case GBR_TOPOLOGY_TRIANGLE_LIST: return count / 3;
+        default: return count >= 3 ? count - 2 : 0;
+    }
+}
+
 DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachment) {
     DrawDesc d{};
     const Pipeline& pl = *dc.pipeline;
@@ -524,11 +539,13 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
     const ProgramInfo& prog = *pl.prog;
     const gbr_primitive_state& ps = pd.primitive;
     if (ps.polygon_mode != GBR_POLYGON_FILL) fail(GBR_ERR_UNSUPPORTED, "Unsupported polygon mode (state.rs:475-477)");
-    if (ps.topology != GBR_TOPOLOGY_TRIANGLE_LIST && ps.topology != GBR_TOPOLOGY_TRIANGLE_STRIP)
-        fail(GBR_ERR_UNSUPPORTED, "point and line topologies run on the oracle path only");
+    if (ps.topology > GBR_TOPOLOGY_TRIANGLE_STRIP) fail(GBR_ERR_INVALID_ARGUMENT, "topology");
     if (dc.indexed && ps.strip_index_format != GBR_INDEX_NONE) {
-        if (ps.topology != GBR_TOPOLOGY_TRIANGLE_STRIP) fail(GBR_ERR_VALIDATION, "List can't be separated");
-        fail(GBR_ERR_UNSUPPORTED, "primitive restart is not implemented on the GPU path");
+        if (ps.topology != GBR_TOPOLOGY_TRIANGLE_STRIP && ps.topology != GBR_TOPOLOGY_LINE_STRIP)
+            fail(GBR_ERR_VALIDATION, "List can't be separated");
+        if (ps.strip_index_format != dc.index_format)
+            fail(GBR_ERR_VALIDATION, "strip_index_format does not match the index format");
+        d.strip_restart = 1;  // separators split the strip (index.rs:90-106, primitive.rs:428-487)
     }
     if (prog.perspective && profile != GBR_PROFILE_EXTENSION)
         fail(GBR_ERR_UNSUPPORTED, "perspective interpolation is todo!() in the reference (fragment.rs:343-345)");
@@ -539,7 +556,7 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
     d.base_vertex = dc.base_vertex;
     d.instance_start = dc.inst_start;
     d.instance_count = dc.inst_end > dc.inst_start ? dc.inst_end - dc.inst_start : 0;
-    d.prims_per_instance = ps.topology == GBR_TOPOLOGY_TRIANGLE_LIST ? d.count / 3 : (d.count >= 3 ? d.count - 2 : 0);
+    d.prims_per_instance = primitive_slots(ps.topology, d.count);
     if (dc.indexed) {
         if (!dc.index.buf) fail(GBR_ERR_VALIDATION, "No index buffer bound");
         d.index_data = dc.index.buf->ptr + dc.index.offset;
@@ -860,13 +877,16 @@ bool Device::merge_batch(Batch& into, Batch& b) {
     const uint64_t kMaxPrims = (1ull << (32 - SUBTRI_BITS)) - 1;
     if ((uint64_t)into.total_prims + b.total_prims > kMaxPrims) return false;
     if (into.jit && b.jit && into.jit != b.jit) return false;
+    if (into.lines || b.lines) return false;
     if (!into.jit) into.jit = b.jit;
     const uint32_t tbase = (uint32_t)into.targets.size();
     for (DrawDesc d : b.draws) {
         d.prim_base += into.total_prims;
         d.target += tbase;
+        d.strip_table += into.strip_entries;
         into.draws.push_back(d);
     }
+    into.strip_entries += b.strip_entries;
     into.targets.insert(into.targets.end(), b.targets.begin(), b.targets.end());
     into.target_item.insert(into.target_item.end(), b.target_item.begin(), b.target_item.end());
     into.writes.insert(into.writes.end(), b.writes.begin(), b.writes.end());
@@ -904,6 +924,10 @@ std::vector<Batch> Device::split_batch(const Batch& m) {
         const uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
         d.prim_base = out[k].total_prims;
         d.target = new_target[d0.target];
+        if (d.strip_restart) {
+            d.strip_table = out[k].strip_entries;
+            out[k].strip_entries += d.count;
+        }
         out[k].total_prims += (uint32_t)np;
         out[k].nvar = std::max(out[k].nvar, d.num_varyings);
         out[k].draws.push_back(d);
@@ -945,19 +969,23 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
         for (const DrawCmd& dc : p.draws) {
             const auto& ps = dc.pipeline->desc.primitive;
             uint32_t cnt = dc.end > dc.start ? dc.end - dc.start : 0;
-            uint32_t ppi = ps.topology == GBR_TOPOLOGY_TRIANGLE_STRIP ? (cnt >= 3 ? cnt - 2 : 0) : cnt / 3;
+            uint32_t ppi = primitive_slots(ps.topology, cnt);
             p_prims += (uint64_t)ppi * (dc.inst_end > dc.inst_start ? dc.inst_end - dc.inst_start : 0);
         }
         const uint64_t kMaxPrims = (1ull << (32 - SUBTRI_BITS)) - 1;
         // the WGSL modules the pass's draws run: one batch runs at most one
         std::shared_ptr<JitKernels> p_jit;
-        bool several_jit = false;
-        for (const DrawCmd& dc : p.draws)
+        bool several_jit = false, has_lines = false;
+        for (const DrawCmd& dc : p.draws) {
             if (dc.pipeline->jit) {
                 if (p_jit && p_jit != dc.pipeline->jit) several_jit = true;
                 p_jit = dc.pipeline->jit;
             }
-        if ((cfg.launch_mode == GBR_LAUNCH_PER_DRAW || several_jit) && !p.draws.empty()) {
+            has_lines = has_lines || dc.pipeline->desc.primitive.topology < GBR_TOPOLOGY_TRIANGLE_LIST;
+        }
+        // a pass with line or point draws goes draw by draw (each line/point draw is a batch of
+        // its own, drawn in primitive order)
+        if ((cfg.launch_mode == GBR_LAUNCH_PER_DRAW || several_jit || has_lines) && !p.draws.empty()) {
             open = false;
             bool first = true;
             for (const DrawCmd& dc : p.draws) {
@@ -968,6 +996,7 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
                 b.writes = p_write;
                 b.reads = p_read;
                 b.jit = dc.pipeline->jit;
+                b.lines = dc.pipeline->desc.primitive.topology < GBR_TOPOLOGY_TRIANGLE_LIST;
                 first = false;
                 DrawDesc d = make_draw(dc, profile, (bool)p.depth);
                 uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
@@ -975,6 +1004,10 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
                 if (np > kMaxPrims) fail(GBR_ERR_UNSUPPORTED, "too many primitives in one draw");
                 b.total_prims = (uint32_t)np;
                 b.nvar = d.num_varyings;
+                if (d.strip_restart) {
+                    d.strip_table = 0;
+                    b.strip_entries = d.count;
+                }
                 if (np) b.draws.push_back(d);
             }
             continue;
@@ -1006,6 +1039,10 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
             if ((uint64_t)b.total_prims + np > kMaxPrims) fail(GBR_ERR_UNSUPPORTED, "too many primitives in one pass");
             b.total_prims += (uint32_t)np;
             b.nvar = std::max(b.nvar, d.num_varyings);
+            if (d.strip_restart && np) {
+                d.strip_table = b.strip_entries;
+                b.strip_entries += d.count;
+            }
             if (np) b.draws.push_back(d);
         }
         b.writes.insert(b.writes.end(), p_write.begin(), p_write.end());
@@ -1105,8 +1142,9 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
     }
     for (int attempt = 0; attempt < 12; ++attempt) {
         // scratch for the remaining batches
-        uint32_t max_prims = 0, max_tiles = 0, max_stride = 0;
+        uint32_t max_prims = 0, max_tiles = 0, max_stride = 0, max_strip = 0;
         for (size_t i = first_batch; i < nb; ++i) {
+            max_strip = std::max(max_strip, batches[i].strip_entries);
             uint32_t stride = (uint32_t)((sizeof(TriRecord) + 3 * batches[i].nvar * sizeof(float) + 15) & ~size_t(15));
             max_stride = std::max(max_stride, stride);
             max_prims = std::max(max_prims, batches[i].total_prims);
@@ -1114,6 +1152,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         }
         records_buf.ensure((size_t)std::max(1u, max_prims) * max_stride, &scratch_bytes);
         slow_buf.ensure((size_t)std::max(1u, max_prims) * sizeof(uint32_t), &scratch_bytes);
+        if (max_strip) strip_buf.ensure((size_t)max_strip * sizeof(uint32_t), &scratch_bytes);
         ovf_buf.ensure((size_t)ovf_capacity * max_stride, &scratch_bytes);
         tiles_buf.ensure((size_t)(max_tiles + 1) * 3 * sizeof(uint32_t) + 64, &scratch_bytes);
         bins_buf.ensure((size_t)bin_capacity * sizeof(uint32_t), &scratch_bytes);
@@ -1145,6 +1184,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 bp.num_varyings = b.nvar;
                 bp.records = static_cast<uint8_t*>(records_buf.ptr);
                 bp.slow_prims = static_cast<uint32_t*>(slow_buf.ptr);
+            bp.strip_info = b.strip_entries ? static_cast<uint32_t*>(strip_buf.ptr) : nullptr;
                 bp.ovf_records = static_cast<uint8_t*>(ovf_buf.ptr);
                 bp.ovf_capacity = ovf_capacity;
                 bp.bin_capacity = (uint32_t)std::min<uint64_t>(bin_capacity, 0xFFFFFFFFull);
@@ -1161,7 +1201,11 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                     bp.vis_compare = visibility_compare(b);
                 }
                 cudaEvent_t* ev = revp->empty() ? nullptr : &(*revp)[2 * i];
-                if (b.jit)
+                if (b.lines)
+                    cuda_check(b.jit ? launch_lines_jit(*b.jit, bp, num_sms, stream, &run.launches, ev)
+                                     : launch_lines(bp, num_sms, stream, &run.launches, ev),
+                               "launch");
+                else if (b.jit)
                     cuda_check(launch_batch_jit(*b.jit, bp, num_sms, stream, &run.launches, ev, kinds[i]), "launch");
                 else
                     cuda_check(launch_batch(bp, btile[i], bwarps[i], num_sms, stream, &run.launches, ev, kinds[i]),
@@ -1186,7 +1230,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 put(&nd, sizeof nd);
                 put(&nt, sizeof nt);
             }
-            const void* ptrs[6] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, slow_buf.ptr};
+            const void* ptrs[7] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, slow_buf.ptr,
+                                   strip_buf.ptr};
             put(ptrs, sizeof ptrs);
             put(&ovf_capacity, sizeof ovf_capacity);
             put(&bin_capacity, sizeof bin_capacity);
@@ -1224,9 +1269,10 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
             } else {
                 revp = &g.events;
                 for (size_t i = first_batch; i < nb; ++i)
-                    run.launches += batches[i].jit ? 2u + (batches[i].total_prims ? 4u : 0u) + (kinds[i] == 3 ? 1u : 0u)
-                                                   : batch_kernel_launches(batches[i].total_prims, btile[i], bwarps[i],
-                                                                           kinds[i]);
+                    run.launches += batches[i].lines ? 2u : (batches[i].strip_entries ? 1u : 0u) +
+                                    (batches[i].jit ? 2u + (batches[i].total_prims ? 4u : 0u) + (kinds[i] == 3 ? 1u : 0u)
+                                                    : batch_kernel_launches(batches[i].total_prims, btile[i], bwarps[i],
+                                                                            kinds[i]));
             }
             cuda_check(cudaGraphLaunch(graphs[key].exec, stream), "cudaGraphLaunch");
         } else {
@@ -1536,6 +1582,7 @@ GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
         d->objects.clear();
         d->records_buf.release();
         d->slow_buf.release();
+        d->strip_buf.release();
         d->ovf_buf.release();
         d->tiles_buf.release();
         d->bins_buf.release();
