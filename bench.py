@@ -128,6 +128,23 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
 
+def replica_rate(units_per_step: float, steps: int, device_s: float) -> tuple[float, float]:
+    """Replicas only: every rank renders its own copy of the workload (no data-path collective);
+    the job's time is the slowest rank's and its rate is all ranks' units over that time.
+    Returns (max device seconds over ranks, whole-job units per second)."""
+    import torch
+    import torch.distributed as dist
+
+    world = dist.get_world_size() if dist.is_available() and dist.is_initialized() else 1
+    if world > 1:
+        t = torch.tensor([device_s], dtype=torch.float64)
+        if dist.get_backend() == "nccl":
+            t = t.cuda()
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        device_s = float(t.item())
+    return device_s, units_per_step * steps * world / device_s
+
+
 class ClockSampler:
     """nvidia-smi samples during the timed region (clocks, throttle reasons)."""
 
@@ -299,11 +316,7 @@ def run_ours(args, wk: Workload):
     gpu_ms = [s.gpu_ms for s in stats]
     raster_ms = [s.raster_ms for s in stats]
     device_s = sum(gpu_ms) / 1e3
-    if world > 1:
-        t = torch.tensor([device_s], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        device_s = float(t.item())
-    value = frags_per_step * args.steps * world / device_s
+    device_s, value = replica_rate(frags_per_step, args.steps, device_s)
     launches = int(sum(s.kernel_launches for s in stats))
 
     # roofline of the dominant kernel: algorithmic bytes per launch / its event-timed duration
