@@ -513,8 +513,10 @@ GBR_API gbr_status gbr_device_elapsed_ms(gbr_device device, uint64_t first_submi
 GBR_API gbr_status gbr_device_flush_caches(gbr_device device);
 /* No reference counterpart (verification): runs `samples` seeded quotients through the
  * raster kernels' division by a precomputed reciprocal (exact.cuh, div_by_recip) on the current
- * CUDA device and counts results whose bits differ from CUDA's __fdiv_rn.  `first_mismatch`
- * receives (a, b) of the first difference found, if any. */
+ * CUDA device and counts results whose bits differ from CUDA's __fdiv_rn.  The same samples go
+ * through the packed f32x2 helpers (f2add, f2mul, f2fma, and a packed product feeding a packed
+ * sum), which must give the bits of the scalar __fadd_rn / __fmul_rn / __fmaf_rn.
+ * `first_mismatch` receives (a, b) of the first difference found, if any. */
 GBR_API gbr_status gbr_selftest_division(uint64_t samples, uint64_t seed, uint64_t* out_mismatches,
                                          float* first_mismatch);
 

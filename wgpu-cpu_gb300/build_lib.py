@@ -38,7 +38,9 @@ def nvcc() -> str:
 
 
 def _flags():
-    return ["-std=c++17", "-O3", *ARCH, "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
+    # --fmad=false for the front end and for ptxas: no multiply-add contraction of scalar code
+    return ["-std=c++17", "-O3", *ARCH, "-lineinfo", "--fmad=false", "-Xptxas", "--fmad=false",
+            "-Xcompiler", "-fPIC,-ffp-contract=off",
             "-I", os.path.join(ROOT, "include"), "-I", CSRC, "-I", BUILD]
 
 

@@ -88,6 +88,43 @@ __device__ __forceinline__ float div_by_recip(float a, float b, float y, bool b_
     return __fmaf_rn(r1, y, q1);
 }
 
+// Packed f32x2 arithmetic (sm_100+): two IEEE binary32 operations per instruction, each lane
+// rounded to nearest even exactly like the scalar op.
+//
+// Hazard: ptxas fuses a packed product whose only use is a packed sum into one fused
+// multiply-add (a single rounding), whatever the .rn modifiers and --fmad=false say; it also
+// sees through fma(a, b, -0) as the product and fma(p, 1, c) as the sum.  So a product that must
+// be rounded on its own before a sum is always a scalar __fmul_rn (f2mul_rn below: two scalar
+// products, which then feed a packed sum exactly).  Packed f2mul / f2fma are for the
+// correction steps of a division, where every product feeds fused multiply-adds anyway.
+__device__ __forceinline__ float2 f2add(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "add.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+// packed product: only where no sum consumes it (see above)
+__device__ __forceinline__ float2 f2mul(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mul.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+// a * b + c with one rounding per lane, as __fmaf_rn
+__device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 pa, pb, pc, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mov.b64 pc, {%6, %7};\n\tfma.rn.f32x2 pd, pa, pb, pc;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+// two separately rounded scalar products, safe to feed a packed sum
+__device__ __forceinline__ float2 f2mul_rn(float2 a, float2 b) {
+    return make_float2(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y));
+}
+
 __device__ __forceinline__ uint16_t f32_to_f16_bits(float f) { return __half_as_ushort(__float2half_rn(f)); }
 __device__ __forceinline__ float f16_bits_to_f32(uint16_t h) { return __half2float(__ushort_as_half(h)); }
 

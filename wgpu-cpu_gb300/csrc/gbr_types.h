@@ -179,9 +179,10 @@ struct TriRecord {
     float inv_w0[3];     // 1/w of the unclipped vertices (perspective interpolation)
     uint32_t ovf;        // primary record: first overflow slot of sub-triangles 1..nsub-1
     uint32_t nsub;       // primary record: number of sub-triangles
-    uint32_t _pad[2];
-    // float var[3][num_varyings] follows
+    uint32_t _pad[3];
+    // float var[3][num_varyings] follows (16-byte aligned: vector loads of the varyings)
 };
+static_assert(sizeof(TriRecord) % 16 == 0, "varyings start on a 16-byte boundary");
 
 enum : uint32_t {
     TRI_RECORD_HEADER_BYTES = sizeof(TriRecord),

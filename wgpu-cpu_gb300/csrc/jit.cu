@@ -145,7 +145,9 @@ bool jit_compile_cubin(const std::string& code, std::vector<char>* cubin, std::v
     }
     for (const char* e : kKernelExprs) n.add_name(prog, e);
     const std::string inc = "-I" + n.include_dir;
-    const char* opts[] = {"--gpu-architecture=sm_103a", "-fmad=false", "--std=c++17", inc.c_str()};
+    // no multiply-add contraction in the front end nor in ptxas
+    const char* opts[] = {"--gpu-architecture=sm_103a", "-fmad=false", "--ptxas-options=--fmad=false", "--std=c++17",
+                          inc.c_str()};
     const nvrtcResult_t rc = n.compile(prog, (int)(sizeof(opts) / sizeof(opts[0])), opts);
     size_t ls = 0;
     n.log_size(prog, &ls);

@@ -85,7 +85,7 @@ size_t ordered_raster_smem_host(int warps, uint32_t record_stride) {
     return (kCap + 2 * (size_t)warps * 32) * sizeof(uint32_t) + (size_t)kRW * record_stride;
 }
 
-// Seeded inputs for the division self-test: random bit patterns, raster-like magnitudes,
+// Seeded inputs for the arithmetic self-test: random bit patterns, raster-like magnitudes,
 // exact multiples and neighbours of powers of two, in rotation.
 __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
     x += 0x9E3779B97F4A7C15ull;
@@ -114,8 +114,19 @@ __global__ void k_selftest_division(uint64_t n, uint64_t seed, unsigned long lon
         const float ref = __fdiv_rn(a, b);
         // the setup kernel also takes RN(1/w) from __frcp_rn for the reference's `1.0 / w`
         const float one_over = __fdiv_rn(1.0f, b);
-        const bool same = (__float_as_uint(q) == __float_as_uint(ref) || (q != q && ref != ref)) &&
-                          (__float_as_uint(y) == __float_as_uint(one_over) || (y != y && one_over != one_over));
+        // packed f32x2 helpers against the scalar operations, and scalar products feeding a
+        // packed sum (f2mul_rn + f2add), which must keep both roundings
+        const float c = selftest_value(splitmix64(r0 ^ (r1 << 1)), (uint32_t)((i >> 6) & 3u));
+        const float2 pm = f2mul(make_float2(a, c), make_float2(c, b));
+        const float2 ps = f2add(f2mul_rn(make_float2(a, b), make_float2(b, c)), make_float2(c, a));
+        const float2 pf = f2fma(make_float2(a, c), make_float2(b, a), make_float2(c, b));
+        const float sm[2] = {__fmul_rn(a, c), __fmul_rn(c, b)};
+        const float ss[2] = {__fadd_rn(__fmul_rn(a, b), c), __fadd_rn(__fmul_rn(b, c), a)};
+        const float sf[2] = {__fmaf_rn(a, b, c), __fmaf_rn(c, a, b)};
+        auto bits_eq = [](float u, float v) { return __float_as_uint(u) == __float_as_uint(v) || (u != u && v != v); };
+        const bool packed_same = bits_eq(pm.x, sm[0]) && bits_eq(pm.y, sm[1]) && bits_eq(ps.x, ss[0]) &&
+                                 bits_eq(ps.y, ss[1]) && bits_eq(pf.x, sf[0]) && bits_eq(pf.y, sf[1]);
+        const bool same = bits_eq(q, ref) && bits_eq(y, one_over) && packed_same;
         if (!same && atomicAdd(mismatches, 1ull) == 0ull) {
             first[0] = a;
             first[1] = b;

@@ -1178,7 +1178,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
     uint32_t* s_sorted = s_keys + CAP;                         // SMALL
     uint8_t* s_recs = reinterpret_cast<uint8_t*>(s_sorted + SMALL);
     __shared__ uint32_t s_mask[RW];
-    __shared__ float s_kc[RW][4];  // p-independent shoelace terms of the three barycentrics, RN(1/area)
+    __shared__ float4 s_kc[RW];  // p-independent shoelace terms of the three barycentrics, RN(1/area)
     __shared__ int2 s_span[RW * T];  // per staged record and tile row: emitted [x1, x2] within scissor and tile
     __shared__ const uint8_t* s_rec_ptr[RW];
     __shared__ RasterState s_rs[WARPS];
@@ -1282,12 +1282,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
             for (uint32_t q = threadIdx.x; q < nb * T; q += NT) {
                 const uint32_t ri = q / T, row = q - ri * T;
                 const TriRecord& r = *reinterpret_cast<const TriRecord*>(s_recs + (size_t)ri * stride);
-                if (row == 0) {
-                    s_kc[ri][0] = fmul(fsub(r.vpy[2], r.vpy[1]), fadd(r.vpx[2], r.vpx[1]));
-                    s_kc[ri][1] = fmul(fsub(r.vpy[0], r.vpy[2]), fadd(r.vpx[0], r.vpx[2]));
-                    s_kc[ri][2] = fmul(fsub(r.vpy[1], r.vpy[0]), fadd(r.vpx[1], r.vpx[0]));
-                    s_kc[ri][3] = __frcp_rn(r.area);
-                }
+                if (row == 0)
+                    s_kc[ri] = make_float4(fmul(fsub(r.vpy[2], r.vpy[1]), fadd(r.vpx[2], r.vpx[1])),
+                                           fmul(fsub(r.vpy[0], r.vpy[2]), fadd(r.vpx[0], r.vpx[2])),
+                                           fmul(fsub(r.vpy[1], r.vpy[0]), fadd(r.vpx[1], r.vpx[0])),
+                                           __frcp_rn(r.area));
                 const int y = ty * T + (int)row;
                 int2 sp = make_int2(1, 0);
                 if (y >= r.row0 && y <= r.row1 && y < (int)tg.height) {
@@ -1342,17 +1341,29 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                     // per-record constants, held in registers across this lane's pixels
                     const uint32_t rmask = s_mask[ri];
                     const float ax = r.vpx[0], ay = r.vpy[0], bx = r.vpx[1], by = r.vpy[1], cx = r.vpx[2], cy = r.vpy[2];
-                    const float kc0 = s_kc[ri][0], kc1 = s_kc[ri][1], kc2 = s_kc[ri][2], rcp = s_kc[ri][3];
+                    const float4 kc = s_kc[ri];
+                    const float kc0 = kc.x, kc1 = kc.y, kc2 = kc.z, rcp = kc.w;
                     const float area = r.area;
                     const bool area_ok = div_fast_ok(area);
                     const bool ident = (r.flags & 16u) != 0;
                     const float* rv = rec_var(&r);
                     constexpr uint32_t KNV = KIND == 1 ? 4 : KIND == 2 ? 5 : 0;
                     float rvv[3 * (KNV ? KNV : 1)];
-                    if constexpr (KNV != 0) {
+                    if constexpr (KNV == 4) {
+                        // 16-byte aligned: the record header is a multiple of 16 bytes
+#pragma unroll
+                        for (uint32_t q = 0; q < 3; ++q) {
+                            const float4 v4 = reinterpret_cast<const float4*>(rv)[q];
+                            rvv[4 * q] = v4.x; rvv[4 * q + 1] = v4.y; rvv[4 * q + 2] = v4.z; rvv[4 * q + 3] = v4.w;
+                        }
+                    } else if constexpr (KNV != 0) {
 #pragma unroll
                         for (uint32_t q = 0; q < 3 * KNV; ++q) rvv[q] = rv[q];
                     }
+                    // every pixel slot of a thread lies in one column when the warps of a tile
+                    // cover whole block rows: x + a.x (likewise b, c) is then a per-record term
+                    constexpr bool ONE_COL = WARPS % BLK_X == 0;
+                    const float xa0 = fadd(pfx[0], ax), xb0 = fadd(pfx[0], bx), xc0 = fadd(pfx[0], cx);
 #pragma unroll
                     for (int k = 0; k < PPT; ++k) {
                         const int blk = warp + k * WARPS;
@@ -1367,7 +1378,67 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                         // IEEE sum does not depend on operand order, so x + a.x serves both shoelace
                         // terms that contain it (likewise b, c)
                         const float fx = pfx[k], fy = pfy[k];
-                        const float xa = fadd(fx, ax), xb = fadd(fx, bx), xc = fadd(fx, cx);
+                        const float xa = ONE_COL ? xa0 : fadd(fx, ax), xb = ONE_COL ? xb0 : fadd(fx, bx),
+                                    xc = ONE_COL ? xc0 : fadd(fx, cx);
+                        if constexpr (KIND == 1) {
+                            // The same operations as the scalar path below, sums and differences
+                            // two lanes per packed f32x2 instruction (each lane rounds exactly like
+                            // the scalar op; products stay scalar, see f2mul_rn); a - b is
+                            // a + (-b) in IEEE arithmetic, signed zeros included.
+                            const float2 d02 = f2add(make_float2(by, fy), make_float2(-fy, -by));
+                            const float2 t02 = f2add(f2mul_rn(d02, make_float2(xb, xb)), make_float2(kc0, kc2));
+                            const float2 e02 = f2add(make_float2(fy, ay), make_float2(-cy, -fy));
+                            const float2 s02 = f2add(t02, f2mul_rn(e02, make_float2(xc, xa)));
+                            const float2 e1 = f2add(make_float2(fy, cy), make_float2(-ay, -fy));
+                            const float2 m1 = f2mul_rn(e1, make_float2(xa, xc));
+                            const float s1v = fadd(fadd(m1.x, m1.y), kc1);
+                            float c0, c1, c2;
+                            if (area_ok && div_fast_ok(s02.x) && div_fast_ok(s1v) && div_fast_ok(s02.y)) {
+                                // div_by_recip's in-range path for s0 and s2 together (every
+                                // product here feeds a fused multiply-add, as in the scalar steps)
+                                const float2 y2 = make_float2(rcp, rcp), nb2 = make_float2(-area, -area);
+                                float2 q = f2mul(s02, y2);
+                                float2 rr = f2fma(nb2, q, s02);
+                                q = f2fma(rr, y2, q);
+                                rr = f2fma(nb2, q, s02);
+                                const float2 l02 = f2fma(rr, y2, q);
+                                const float l1 = div_by_recip(s1v, area, rcp, true);
+                                if (ident) {
+                                    c0 = l02.x; c1 = l1; c2 = l02.y;
+                                } else {
+                                    c0 = fadd(fadd(fmul(r.cb[0], l02.x), fmul(r.cb[3], l1)), fmul(r.cb[6], l02.y));
+                                    c1 = fadd(fadd(fmul(r.cb[1], l02.x), fmul(r.cb[4], l1)), fmul(r.cb[7], l02.y));
+                                    c2 = fadd(fadd(fmul(r.cb[2], l02.x), fmul(r.cb[5], l1)), fmul(r.cb[8], l02.y));
+                                }
+                            } else {
+                                const float l0 = div_by_recip(s02.x, area, rcp, area_ok);
+                                const float l1 = div_by_recip(s1v, area, rcp, area_ok);
+                                const float l2 = div_by_recip(s02.y, area, rcp, area_ok);
+                                c0 = fadd(fadd(fmul(r.cb[0], l0), fmul(r.cb[3], l1)), fmul(r.cb[6], l2));
+                                c1 = fadd(fadd(fmul(r.cb[1], l0), fmul(r.cb[4], l1)), fmul(r.cb[7], l2));
+                                c2 = fadd(fadd(fmul(r.cb[2], l0), fmul(r.cb[5], l1)), fmul(r.cb[8], l2));
+                            }
+                            ++frag_count;
+                            // linear vec4f colour straight to the output, then Rgba16Float blending
+                            // (colour SrcAlpha/OneMinusSrcAlpha/Add, alpha One/OneMinusSrcAlpha/Add)
+                            const float2 cc0 = make_float2(c0, c0), cc1 = make_float2(c1, c1), cc2 = make_float2(c2, c2);
+                            const float2 v01 = f2add(f2add(f2mul_rn(make_float2(rvv[0], rvv[1]), cc0),
+                                                           f2mul_rn(make_float2(rvv[4], rvv[5]), cc1)),
+                                                     f2mul_rn(make_float2(rvv[8], rvv[9]), cc2));
+                            const float2 v23 = f2add(f2add(f2mul_rn(make_float2(rvv[2], rvv[3]), cc0),
+                                                           f2mul_rn(make_float2(rvv[6], rvv[7]), cc1)),
+                                                     f2mul_rn(make_float2(rvv[10], rvv[11]), cc2));
+                            const float2 dlo = __half22float2(*reinterpret_cast<const __half2*>(&px[k].c[0]));
+                            const float2 dhi = __half22float2(*reinterpret_cast<const __half2*>(&px[k].c[1]));
+                            const float w = v23.y;
+                            const float2 oma = make_float2(fsub(1.0f, w), fsub(1.0f, w));
+                            const float2 olo = f2add(f2mul_rn(v01, make_float2(w, w)), f2mul_rn(dlo, oma));
+                            const float2 ohi = f2add(f2mul_rn(v23, make_float2(w, 1.0f)), f2mul_rn(dhi, oma));
+                            const __half2 hlo = __float22half2_rn(olo), hhi = __float22half2_rn(ohi);
+                            px[k].c[0] = *reinterpret_cast<const uint32_t*>(&hlo);
+                            px[k].c[1] = *reinterpret_cast<const uint32_t*>(&hhi);
+                            continue;
+                        }
                         const float s0 = fadd(fadd(fmul(fsub(by, fy), xb), kc0), fmul(fsub(fy, cy), xc));
                         const float s1 = fadd(fadd(fmul(fsub(fy, ay), xa), fmul(fsub(cy, fy), xc)), kc1);
                         const float s2 = fadd(fadd(kc2, fmul(fsub(fy, by), xb)), fmul(fsub(ay, fy), xa));
@@ -1391,14 +1462,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                         ++frag_count;
                         // inter-stage values (fragment.rs:319-378) and the fragment stage
                         V4 col;
-                        if constexpr (KIND == 1) {
-                            // linear vec4f colour straight to the output (quad_color / clip_passthrough)
-                            float v[4];
-#pragma unroll
-                            for (int q = 0; q < 4; ++q)
-                                v[q] = fadd(fadd(fmul(rvv[q], cmp[0]), fmul(rvv[4 + q], cmp[1])), fmul(rvv[8 + q], cmp[2]));
-                            col = V4{v[0], v[1], v[2], v[3]};
-                        } else if constexpr (KIND == 2) {
+                        if constexpr (KIND == 2) {
                             float v[5];
 #pragma unroll
                             for (int q = 0; q < 5; ++q)
@@ -1436,14 +1500,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                             if (!depth_compare(rs.depth_compare, z, px[k].depth)) continue;
                             if (rs.depth_write) px[k].depth = z;
                         }
-                        if constexpr (KIND == 1) {
-                            // Rgba16Float, colour SrcAlpha/OneMinusSrcAlpha/Add, alpha One/OneMinusSrcAlpha/Add
-                            const V4 dst = decode_color(7, px[k].c);
-                            const float oma = fsub(1.0f, col.w);
-                            col = V4{fadd(fmul(col.x, col.w), fmul(dst.x, oma)), fadd(fmul(col.y, col.w), fmul(dst.y, oma)),
-                                     fadd(fmul(col.z, col.w), fmul(dst.z, oma)), fadd(fmul(col.w, 1.0f), fmul(dst.w, oma))};
-                            encode_color(7, col, px[k].c);
-                        } else if constexpr (KIND == 2) {
+                        if constexpr (KIND == 2) {
                             encode_color(3, col, px[k].c);  // Rgba8Unorm / Rgba8UnormSrgb: same bytes here
                         } else {
                             if (!tg.color) continue;

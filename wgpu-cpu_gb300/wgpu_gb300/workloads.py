@@ -298,21 +298,25 @@ def quad_stream(n_quads: int, width: int, height: int, seed: int, size_lo: int =
 
 
 def scene_blended_quads(dev: W.Device, width: int = 3840, height: int = 2160, n_quads: int = 10000, seed: int = 4,
-                        size_lo: int = 16, size_hi: int = 1024) -> Scene:
+                        size_lo: int = 16, size_hi: int = 1024, depth_always: bool = False) -> Scene:
     """Fill-rate / blend stress: quads in painter order into Rgba16Float with ALPHA_BLENDING,
-    no depth (extension profile: the reference has neither blending nor f16 targets)."""
+    no depth (extension profile: the reference has neither blending nor f16 targets).
+    depth_always adds a Depth32Float target tested with Always and never written: the same
+    colours, through the generic fragment path instead of the specialised blend path."""
     pos, col, idx = quad_stream(n_quads, width, height, seed, size_lo, size_hi)
     vb_pos = dev.create_buffer_init(pos)
     vb_col = dev.create_buffer_init(col)
     ib = dev.create_buffer_init(idx)
     sm = dev.create_shader_module(native="quad_color")
+    ds = W.DepthStencilState(False, W.CompareFunction.ALWAYS) if depth_always else None
     pl = dev.create_render_pipeline(
         sm, [W.VertexBufferLayout(12, [_f32x3_layout(0, 0)]),
              W.VertexBufferLayout(8, [W.VertexAttribute(W.VertexFormat.FLOAT16X4, 0, 1)])],
-        W.PrimitiveState(W.PrimitiveTopology.TRIANGLE_LIST, cull_mode=W.Face.NONE), None, sm,
+        W.PrimitiveState(W.PrimitiveTopology.TRIANGLE_LIST, cull_mode=W.Face.NONE), ds, sm,
         [W.ColorTargetState(W.TextureFormat.RGBA16_FLOAT, W.BlendState.alpha_blending())])
     color = dev.create_texture(width, height, W.TextureFormat.RGBA16_FLOAT)
-    s = Scene(dev, color, None, clear_color=(0.0, 0.0, 0.0, 0.0), triangles=n_quads * 2, label="blended_quads")
+    depth = dev.create_texture(width, height, W.TextureFormat.DEPTH32_FLOAT) if depth_always else None
+    s = Scene(dev, color, depth, clear_color=(0.0, 0.0, 0.0, 0.0), triangles=n_quads * 2, label="blended_quads")
     s.draws.append((pl, [], [vb_pos, vb_col], ib, range(0, idx.size), 0))
     s._keep = [vb_pos, vb_col, ib, sm]
     s.uploads = [(vb_pos, pos), (vb_col, col), (ib, idx)]
