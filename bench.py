@@ -10,6 +10,10 @@ Workloads (seeded synthetic inputs with the configurations' shapes; no dataset e
                       texture, texture x Lambert shading, 1920x1080 Rgba8UnormSrgb + Depth32Float
                       (Less).  Parity profile: nearest sampling, sRGB formats read and written as
                       linear, exactly as wgpu-cpu does (its sampler ignores filter modes).
+  textured_filtered   the same textured scene as the configuration states it, extension profile:
+                      full mip chain, linear min/mag/mip filtering with repeat addressing, sRGB
+                      texture decode and sRGB target encode (LOD per primitive from analytic UV
+                      derivatives; the reference has no filtering, mips or sRGB conversion).
   blend               10,000 screen-aligned quads (20,000 triangles), sides U[16,1024] px, RGBA f16
                       colours with alpha U[0.1,0.9], painter order, SrcAlpha/OneMinusSrcAlpha into
                       3840x2160 Rgba16Float (extension profile: the reference has neither blending
@@ -82,6 +86,15 @@ def workloads():
             "textured icosphere: 81,920 tris, 1920x1080 Rgba8UnormSrgb + Depth32Float Less, 1024^2 texture, "
             "texture x Lambert, parity profile (nearest, sRGB as linear)",
             {"triangles": 81920, "target": "1920x1080", "texture": "1024x1024 rgba8", "profile": "parity", "seed": 2},
+            tile=(16, 4)),
+        "textured_filtered": Workload(
+            "textured_filtered", W.Profile.EXTENSION, "scene_textured_icosphere",
+            dict(width=1920, height=1080, level=6, tex_size=1024, filtering=True, srgb=True),
+            4 + 4 + 4 + 32, 1920 * 1080 * (4 + 4),
+            "textured icosphere: 81,920 tris, 1920x1080 Rgba8UnormSrgb + Depth32Float Less, 1024^2 Rgba8UnormSrgb "
+            "texture with full mip chain, linear min/mag/mip filtering, repeat, texture x Lambert, extension profile",
+            {"triangles": 81920, "target": "1920x1080 rgba8 srgb", "texture": "1024x1024 rgba8 srgb, 11 mips",
+             "filtering": "trilinear", "profile": "extension", "seed": 2},
             tile=(16, 4)),
         "blend": Workload(
             "blend", W.Profile.EXTENSION, "scene_blended_quads", dict(width=3840, height=2160, n_quads=10000),
@@ -477,7 +490,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batched", choices=["textured", "blend", "colored", "batched", "serve"])
+    ap.add_argument("--workload", default="batched",
+                    choices=["textured", "textured_filtered", "blend", "colored", "batched", "serve"])
     ap.add_argument("--rate", type=float, default=1000.0, help="serve workload: submissions per second")
     ap.add_argument("--duration", type=float, default=2.0, help="serve workload: arrival window in seconds")
     ap.add_argument("--launch-mode", default="batched", choices=list(LAUNCH_MODES))

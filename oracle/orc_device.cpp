@@ -19,6 +19,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -29,6 +30,7 @@
 #include "gbr.h"
 #include "orc_core.hpp"
 #include "orc_programs.hpp"
+#include "srgb_tables.h"  // extension-profile sRGB tables, shared with the kernels
 
 #define ORC_API extern "C" __attribute__((visibility("default")))
 
@@ -176,9 +178,6 @@ static V4 get_pixel_rgba8(const Texture* t, uint32_t mip, uint32_t x, uint32_t y
     return {(float)p[0] / 255.0f, (float)p[1] / 255.0f, (float)p[2] / 255.0f, (float)p[3] / 255.0f};
 }
 
-struct SampleCtx {
-    uint32_t profile;
-};
 
 // image_sample (render_pass/binding.rs:93-140).  Nearest, mip 0, layer 0; filters ignored.
 static V4 sample_parity(const TextureView* tv, const SamplerState* s, float u, float v) {
@@ -190,9 +189,133 @@ static V4 sample_parity(const TextureView* tv, const SamplerState* s, float u, f
     return get_pixel_rgba8(t, 0, x, y);
 }
 
-static V4 sample_cb(const TextureView* tv, const SamplerState* s, float u, float v, const void* ctx) {
-    (void)ctx;
+// ---------------------------------------------------------------- extension-profile sampling
+// The reference has no filtering, mips or sRGB decode; the extension profile follows the WebGPU
+// sampling model with these exact steps (restated in the kernels' sampling.cuh):
+//   LOD = 0.5 * log2(max(|d(uv)/dx|^2, |d(uv)/dy|^2)) in level-0 texels, clamped to the sampler's
+//   [lod_min, lod_max]; LOD <= 0 magnifies (mag filter, level 0); the mip filter picks level
+//   ceil(LOD + 0.5) - 1 (nearest) or blends floor(LOD) and the next level (linear); nearest texel
+//   floor(u * w), linear taps at u * w - 0.5; integer coordinates wrap per address mode; sRGB
+//   texels decode through kSrgbToLinear; lerp(a, b, t) = a + (b - a) * t.
+
+// log2 from IEEE basic operations: r = m * 2^e, m in [sqrt(1/2), sqrt(2)), ln(m) = 2 atanh(s),
+// s = (m - 1) / (m + 1), series s + s^3/3 + s^5/5 + s^7/7 (Horner in z = s^2).
+static float log2_spec(float r) {
+    if (!(r > 0.0f)) return -std::numeric_limits<float>::infinity();
+    if (std::isinf(r)) return r;
+    uint32_t bits;
+    std::memcpy(&bits, &r, 4);
+    int e = (int)((bits >> 23) & 0xFFu);
+    if (e == 0) {  // subnormal
+        float q = r * 0x1p24f;
+        std::memcpy(&bits, &q, 4);
+        e = (int)((bits >> 23) & 0xFFu) - 24;
+    }
+    e -= 127;
+    uint32_t mb = (bits & 0x7FFFFFu) | 0x3F800000u;
+    float m;
+    std::memcpy(&m, &mb, 4);
+    if (m > 0x1.6a09e6p+0f) {
+        m = m * 0.5f;
+        e += 1;
+    }
+    float s = (m - 1.0f) / (m + 1.0f);
+    float z = s * s;
+    float p = 0x1.249250p-3f;
+    p = p * z + 0x1.99999ap-3f;
+    p = p * z + 0x1.555556p-2f;
+    p = p * z + 1.0f;
+    float ln = (2.0f * s) * p;
+    return (float)e + ln * 0x1.715476p+0f;
+}
+
+static float lod_from_grad(const float g[4], uint32_t w, uint32_t h, float lod_min, float lod_max) {
+    float sx = g[0] * (float)w, tx = g[1] * (float)h, sy = g[2] * (float)w, ty = g[3] * (float)h;
+    float px2 = sx * sx + tx * tx, py2 = sy * sy + ty * ty;
+    float r2 = px2 >= py2 ? px2 : py2;
+    float lod = 0.5f * log2_spec(r2);
+    if (!(lod >= lod_min)) lod = lod_min;
+    if (lod > lod_max) lod = lod_max;
+    return lod;
+}
+
+static int wrap_texel(int i, int n, uint32_t mode) {
+    if (mode == GBR_ADDRESS_REPEAT) {
+        int r = i % n;
+        return r < 0 ? r + n : r;
+    }
+    if (mode == GBR_ADDRESS_MIRROR_REPEAT) {
+        int p = 2 * n;
+        int t = i % p;
+        if (t < 0) t += p;
+        return t < n ? t : p - 1 - t;
+    }
+    return i < 0 ? 0 : (i >= n ? n - 1 : i);
+}
+
+static float texel_space(float u, uint32_t size, float bias) {
+    float x = u * (float)size - bias;
+    if (!(x >= -16777216.0f)) x = std::isnan(x) ? 0.0f : -16777216.0f;
+    if (x > 16777216.0f) x = 16777216.0f;
+    return x;
+}
+
+static V4 decode_texel(const uint8_t* p, bool srgb) {
+    if (srgb) return {kSrgbToLinear[p[0]], kSrgbToLinear[p[1]], kSrgbToLinear[p[2]], (float)p[3] / 255.0f};
+    return {(float)p[0] / 255.0f, (float)p[1] / 255.0f, (float)p[2] / 255.0f, (float)p[3] / 255.0f};
+}
+static V4 lerp4(V4 a, V4 b, float t) {
+    return {a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t, a.w + (b.w - a.w) * t};
+}
+
+static V4 sample_level(const Texture* t, const gbr_sampler_desc& s, uint32_t level, bool linear, float u, float v) {
+    const bool srgb = t->desc.format == GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB;
+    const int w = (int)t->mip_w(level), h = (int)t->mip_h(level);
+    const uint8_t* base = t->mips[level].data();
+    auto at = [&](int x, int y) { return decode_texel(base + ((size_t)y * w + x) * 4, srgb); };
+    if (!linear) {
+        int x = wrap_texel((int)std::floor(texel_space(u, (uint32_t)w, 0.0f)), w, s.address_mode_u);
+        int y = wrap_texel((int)std::floor(texel_space(v, (uint32_t)h, 0.0f)), h, s.address_mode_v);
+        return at(x, y);
+    }
+    float xs = texel_space(u, (uint32_t)w, 0.5f), ys = texel_space(v, (uint32_t)h, 0.5f);
+    float xf = std::floor(xs), yf = std::floor(ys);
+    float fx = xs - xf, fy = ys - yf;
+    int x0 = wrap_texel((int)xf, w, s.address_mode_u), x1 = wrap_texel((int)xf + 1, w, s.address_mode_u);
+    int y0 = wrap_texel((int)yf, h, s.address_mode_v), y1 = wrap_texel((int)yf + 1, h, s.address_mode_v);
+    return lerp4(lerp4(at(x0, y0), at(x1, y0), fx), lerp4(at(x0, y1), at(x1, y1), fx), fy);
+}
+
+static V4 sample_ext(const TextureView* tv, const SamplerState* ss, float u, float v, const float grad[4]) {
+    const Texture* t = tv->tex;
+    const gbr_sampler_desc& s = ss->desc;
+    if (t->desc.format != GBR_TEXTURE_FORMAT_RGBA8_UNORM && t->desc.format != GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB)
+        fail(GBR_ERR_UNSUPPORTED, "sampling format %u is not implemented", t->desc.format);
+    if (s.address_mode_u == GBR_ADDRESS_CLAMP_TO_BORDER || s.address_mode_v == GBR_ADDRESS_CLAMP_TO_BORDER)
+        fail(GBR_ERR_UNSUPPORTED, "ClampToBorder is todo!() (binding.rs:160)");
+    const float lod = lod_from_grad(grad, t->desc.size.width, t->desc.size.height, s.lod_min_clamp, s.lod_max_clamp);
+    const uint32_t last = t->mips_stored - 1;
+    if (lod <= 0.0f) return sample_level(t, s, 0, s.mag_filter == GBR_FILTER_LINEAR, u, v);
+    const bool lin = s.min_filter == GBR_FILTER_LINEAR;
+    if (s.mipmap_filter != GBR_FILTER_LINEAR) {
+        float lv = std::ceil(lod + 0.5f) - 1.0f;
+        uint32_t level = lv >= (float)last ? last : (uint32_t)lv;
+        return sample_level(t, s, level, lin, u, v);
+    }
+    float lc = lod < (float)last ? lod : (float)last;
+    float lf = std::floor(lc);
+    uint32_t l0 = (uint32_t)lf;
+    float f = lc - lf;
+    V4 c0 = sample_level(t, s, l0, lin, u, v);
+    if (f == 0.0f || l0 >= last) return c0;
+    return lerp4(c0, sample_level(t, s, l0 + 1, lin, u, v), f);
+}
+
+// `grad` = (du/dx, dv/dx, du/dy, dv/dy) of the sampled coordinate (extension profile only).
+static V4 sample_cb(const TextureView* tv, const SamplerState* s, float u, float v, const float grad[4],
+                    const void* ctx) {
     if (!tv || !s) fail(GBR_ERR_VALIDATION, "No such binding resource");
+    if (*static_cast<const uint32_t*>(ctx) == GBR_PROFILE_EXTENSION) return sample_ext(tv, s, u, v, grad);
     return sample_parity(tv, s, u, v);
 }
 
@@ -205,6 +328,22 @@ static inline uint8_t unorm8_trunc(float v) {
     return rust_f32_to_u8(s);
 }
 
+// Extension profile, sRGB targets: linear -> unorm8 sRGB = number of encode thresholds <= v
+// (round to nearest of the encoded value; NaN and negatives 0, v >= the last threshold 255).
+static inline uint8_t linear_to_srgb8(float v) {
+    uint32_t k = 0;
+    for (uint32_t step = 128; step > 0; step >>= 1)
+        if (k + step <= 255u && v >= kSrgbEncodeThreshold[k + step]) k += step;
+    return (uint8_t)k;
+}
+// Extension profile: WebGPU float -> unorm8, clamp then round to nearest even (the alpha of sRGB
+// targets).
+static inline uint8_t unorm8_round(float v) {
+    if (!(v > 0.0f)) return 0;
+    if (v >= 1.0f) return 255;
+    return (uint8_t)std::nearbyint(v * 255.0f);
+}
+
 // TexelWriter::from_color (texture.rs:373-411) + put_pixel (texture.rs:213-218).
 static void write_color(Texture* t, uint32_t x, uint32_t y, uint32_t slice, V4 c, uint32_t profile) {
     uint32_t w = t->desc.size.width, h = t->desc.size.height;
@@ -215,15 +354,31 @@ static void write_color(Texture* t, uint32_t x, uint32_t y, uint32_t slice, V4 c
             p[0] = unorm8_trunc(c.x);
             p[1] = unorm8_trunc(c.y);
             break;
-        case GBR_TEXTURE_FORMAT_RGBA8_UNORM:
         case GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB:
+            if (profile == GBR_PROFILE_EXTENSION) {  // WebGPU: linear -> sRGB on write
+                p[0] = linear_to_srgb8(c.x);
+                p[1] = linear_to_srgb8(c.y);
+                p[2] = linear_to_srgb8(c.z);
+                p[3] = unorm8_round(c.w);
+                break;
+            }
+            [[fallthrough]];
+        case GBR_TEXTURE_FORMAT_RGBA8_UNORM:
             p[0] = unorm8_trunc(c.x);
             p[1] = unorm8_trunc(c.y);
             p[2] = unorm8_trunc(c.z);
             p[3] = unorm8_trunc(c.w);
             break;
-        case GBR_TEXTURE_FORMAT_BGRA8_UNORM:
         case GBR_TEXTURE_FORMAT_BGRA8_UNORM_SRGB:
+            if (profile == GBR_PROFILE_EXTENSION) {
+                p[0] = linear_to_srgb8(c.z);
+                p[1] = linear_to_srgb8(c.y);
+                p[2] = linear_to_srgb8(c.x);
+                p[3] = unorm8_round(c.w);
+                break;
+            }
+            [[fallthrough]];
+        case GBR_TEXTURE_FORMAT_BGRA8_UNORM:
             p[0] = unorm8_trunc(c.z);
             p[1] = unorm8_trunc(c.y);
             p[2] = unorm8_trunc(c.x);
@@ -249,7 +404,7 @@ static void write_color(Texture* t, uint32_t x, uint32_t y, uint32_t slice, V4 c
     }
 }
 
-// Decoded read of a colour target texel (extension-profile blending only).
+// Decoded read of a colour target texel (extension-profile blending only; sRGB targets decode).
 static V4 read_color(const Texture* t, uint32_t x, uint32_t y, uint32_t slice) {
     uint32_t w = t->desc.size.width, h = t->desc.size.height;
     const uint8_t* p = t->mips[0].data() + (((size_t)slice * h + y) * w + x) * t->bpp;
@@ -265,11 +420,13 @@ static V4 read_color(const Texture* t, uint32_t x, uint32_t y, uint32_t slice) {
             return {fv[0], fv[1], fv[2], fv[3]};
         }
         case GBR_TEXTURE_FORMAT_RGBA8_UNORM:
-        case GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB:
             return {p[0] / 255.0f, p[1] / 255.0f, p[2] / 255.0f, p[3] / 255.0f};
+        case GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB:
+            return {kSrgbToLinear[p[0]], kSrgbToLinear[p[1]], kSrgbToLinear[p[2]], p[3] / 255.0f};
         case GBR_TEXTURE_FORMAT_BGRA8_UNORM:
-        case GBR_TEXTURE_FORMAT_BGRA8_UNORM_SRGB:
             return {p[2] / 255.0f, p[1] / 255.0f, p[0] / 255.0f, p[3] / 255.0f};
+        case GBR_TEXTURE_FORMAT_BGRA8_UNORM_SRGB:
+            return {kSrgbToLinear[p[2]], kSrgbToLinear[p[1]], kSrgbToLinear[p[0]], p[3] / 255.0f};
         default: fail(GBR_ERR_UNSUPPORTED, "blend: unsupported target format %u", t->desc.format);
     }
 }
@@ -380,6 +537,7 @@ static void resolve_bindings(Device* dev, const PassState& st, ProgramBindings& 
         }
     }
     pb.sample = sample_cb;
+    pb.sample_ctx = &dev->profile;
 }
 static void free_bindings(ProgramBindings& pb) {
     for (int g = 0; g < 4; ++g)
@@ -454,6 +612,8 @@ static bool compare(uint32_t f, float v, float r) {
 // FragmentOutput::depth_test (fragment.rs:427-453) and ::read_from (fragment.rs:456-489).
 // `coeff` are the interpolation coefficients for the FS inputs (N = 1, 2 or 3 vertices),
 // `vars` the inter-stage variables of the primitive's unclipped vertices.
+static const float kZero3[3] = {0.0f, 0.0f, 0.0f};
+
 struct FragCtx {
     Exec* ex;
     const PassState* st;
@@ -461,9 +621,11 @@ struct FragCtx {
     const ProgramBindings* pb;
 };
 
+// `dcx` / `dcy`: screen-space derivatives of the coefficients (extension-profile sampling; zero
+// for lines and points).
 static void process_fragment(FragCtx& fc, uint32_t fx, uint32_t fy, V4 fragment, bool front_facing,
                              uint32_t primitive_index, int nverts, const float coeff[3], const VsOut* const verts[3],
-                             const float inv_w[3]) {
+                             const float inv_w[3], const float dcx[3], const float dcy[3]) {
     Exec* ex = fc.ex;
     const Pipeline* pl = fc.pl;
     const Program* fs = pl->fs;
@@ -474,6 +636,8 @@ static void process_fragment(FragCtx& fc, uint32_t fx, uint32_t fy, V4 fragment,
     in.primitive_index = primitive_index;
     in.sample_index = 0;
     in.sample_mask = ~0u;
+    std::memset(in.dvar_dx, 0, sizeof in.dvar_dx);
+    std::memset(in.dvar_dy, 0, sizeof in.dvar_dy);
     for (int v = 0; v < fs->num_varyings; ++v) {
         const ProgramVarying& pv = fs->varyings[v];
         for (int c = 0; c < pv.components; ++c) {
@@ -485,6 +649,14 @@ static void process_fragment(FragCtx& fc, uint32_t fx, uint32_t fy, V4 fragment,
                 float accu = verts[0]->var[pv.location][c] * coeff[0];
                 for (int k = 1; k < nverts; ++k) accu = accu + verts[k]->var[pv.location][c] * coeff[k];
                 x = accu;
+                // d/dx and d/dy of the interpolated value, summed in the same order
+                float gx = verts[0]->var[pv.location][c] * dcx[0], gy = verts[0]->var[pv.location][c] * dcy[0];
+                for (int k = 1; k < nverts; ++k) {
+                    gx = gx + verts[k]->var[pv.location][c] * dcx[k];
+                    gy = gy + verts[k]->var[pv.location][c] * dcy[k];
+                }
+                in.dvar_dx[pv.location][c] = gx;
+                in.dvar_dy[pv.location][c] = gy;
             } else {
                 if (ex->profile != GBR_PROFILE_EXTENSION)
                     fail(GBR_ERR_UNSUPPORTED, "perspective interpolation is todo!() (fragment.rs:343-345)");
@@ -698,6 +870,12 @@ static void execute_draw(Exec* ex, const PassState& st, bool indexed, uint32_t s
                     if (total == 0.0f) continue;
                     Bary3 clipb[3] = {sub.v[0].bary, sub.v[1].bary, sub.v[2].bary};
                     V4 frags[3] = {rp[0].frag, rp[1].frag, rp[2].frag};
+                    // d(lambda)/dx, d(lambda)/dy of the shoelace barycentrics (lambda_0 = S(p, b, c) / A:
+                    // (b.y - c.y) / A and (c.x - b.x) / A, cyclically), composed with the clip
+                    // barycentrics like the barycentrics themselves
+                    Bary3 lgx = {{(vb.y - vc.y) / total, (vc.y - va.y) / total, (va.y - vb.y) / total}};
+                    Bary3 lgy = {{(vc.x - vb.x) / total, (va.x - vc.x) / total, (vb.x - va.x) / total}};
+                    Bary3 dcx = compose_bary(clipb, lgx), dcy = compose_bary(clipb, lgy);
                     uint32_t fxs[3] = {rp[0].fbx, rp[1].fbx, rp[2].fbx}, fys[3] = {rp[0].fby, rp[1].fby, rp[2].fby};
                     bool ok = scanlines(fxs, fys, [&](const Scanline& sl) {
                         if (sl.y < (int64_t)ex->band_y0 || sl.y >= (int64_t)ex->band_y1) return;
@@ -710,7 +888,7 @@ static void execute_draw(Exec* ex, const PassState& st, bool indexed, uint32_t s
                             Bary3 comp = compose_bary(clipb, lam);
                             V4 fragment = interp3_v4(frags, comp);
                             process_fragment(fc, px, py, fragment, front_facing, (uint32_t)prim_index, 3, comp.c,
-                                             verts, inv_w);
+                                             verts, inv_w, dcx.c, dcy.c);
                         }
                     });
                     if (!ok) fail(GBR_ERR_VALIDATION, "scanlines generated points that don't fit u32");
@@ -731,7 +909,8 @@ static void execute_draw(Exec* ex, const PassState& st, bool indexed, uint32_t s
                     V4 fragment = v4_add(v4_mul(s.frag, 1.0f - T), v4_mul(e.frag, T));
                     float coeff[3] = {1.0f - T, T, 0.0f};
                     // Lerp::interpolate for the inter-stage values: v0*(1-T) + v1*T
-                    process_fragment(fc, px, py, fragment, true, (uint32_t)prim_index, 2, coeff, verts, inv_w);
+                    process_fragment(fc, px, py, fragment, true, (uint32_t)prim_index, 2, coeff, verts, inv_w, kZero3,
+                                     kZero3);
                 });
             } else {
                 const VsOut* verts[3] = {&vout[pr[0]], nullptr, nullptr};
@@ -741,7 +920,8 @@ static void execute_draw(Exec* ex, const PassState& st, bool indexed, uint32_t s
                 if (!in_scissor(tr, r.fbx, r.fby)) continue;
                 float coeff[3] = {1.0f, 0.0f, 0.0f};
                 float inv_w[3] = {1.0f / verts[0]->position.w, 0.0f, 0.0f};
-                process_fragment(fc, r.fbx, r.fby, r.frag, true, (uint32_t)prim_index, 1, coeff, verts, inv_w);
+                process_fragment(fc, r.fbx, r.fby, r.frag, true, (uint32_t)prim_index, 1, coeff, verts, inv_w, kZero3,
+                                 kZero3);
             }
         }
     }
@@ -1062,7 +1242,7 @@ ORC_API gbr_status orc_texture_create(gbr_device d, const gbr_texture_desc* desc
         t->bpp = bpp;
         // The reference stores mip 0 only (texture.rs:34-43); the extension profile keeps the chain.
         uint32_t mips = desc->mip_level_count ? desc->mip_level_count : 1;
-        t->mips_stored = dev->profile == GBR_PROFILE_EXTENSION ? mips : 1;
+        t->mips_stored = dev->profile == GBR_PROFILE_EXTENSION ? std::min(mips, 16u) : 1;
         t->mips.resize(t->mips_stored);
         for (uint32_t m = 0; m < t->mips_stored; ++m)
             t->mips[m].assign((size_t)t->mip_w(m) * t->mip_h(m) * t->desc.size.depth_or_array_layers * bpp, 0);

@@ -34,6 +34,7 @@ struct FsIn {
     bool front_facing;
     uint32_t primitive_index, sample_index, sample_mask;
     float var[8][4];
+    float dvar_dx[8][4], dvar_dy[8][4];  // screen-space derivatives of linear inputs (extension sampling)
 };
 struct FsOut {
     bool killed;
@@ -47,7 +48,8 @@ struct ProgramBindings {
     uint64_t uniform_size[4][8];
     const TextureView* texture[4][8];
     const SamplerState* sampler[4][8];
-    V4 (*sample)(const TextureView*, const SamplerState*, float u, float v, const void* ctx);
+    // grad = (du/dx, dv/dx, du/dy, dv/dy) of the coordinate; read by extension-profile sampling
+    V4 (*sample)(const TextureView*, const SamplerState*, float u, float v, const float grad[4], const void* ctx);
     const void* sample_ctx;
 };
 
@@ -146,7 +148,8 @@ static bool vs_mesh_tex_lambert(const VsIn& in, const ProgramBindings& b, VsOut&
     return true;
 }
 static void fs_mesh_tex_lambert(const FsIn& in, const ProgramBindings& b, FsOut& out) {
-    V4 t = b.sample(b.texture[1][0], b.sampler[1][1], in.var[1][0], in.var[1][1], b.sample_ctx);
+    const float grad[4] = {in.dvar_dx[1][0], in.dvar_dx[1][1], in.dvar_dy[1][0], in.dvar_dy[1][1]};
+    V4 t = b.sample(b.texture[1][0], b.sampler[1][1], in.var[1][0], in.var[1][1], grad, b.sample_ctx);
     const uint8_t* u = b.uniform[0][0];
     float lx = ld_f32(u, 64), ly = ld_f32(u, 68), lz = ld_f32(u, 72);
     float d = in.var[0][0] * lx + in.var[0][1] * ly;

@@ -191,3 +191,52 @@ def mixed_pass(dev, width, height, seed):
     sub = dev.queue.submit([enc.finish()])
     dev.poll(True, sub)
     return dev.read_texture(color), dev.read_texture(dtex), dev.submission_stats(sub).fragments_shaded
+
+
+def textured_quad(dev, width, height, x0, y0, side, tex_levels, uv_scale=1.0, srgb_texture=False,
+                  color_format=W.TextureFormat.RGBA8_UNORM, address=W.AddressMode.REPEAT,
+                  mag=W.FilterMode.LINEAR, min_=W.FilterMode.LINEAR, mip=W.FilterMode.LINEAR,
+                  lod_min=0.0, lod_max=32.0, clear=(0.0, 0.0, 0.0, 0.0)):
+    """A screen-aligned quad over pixels [x0, x0 + side] x [y0, y0 + side] textured with uv from 0
+    to uv_scale through mesh_tex_lambert, identity MVP, normal and light both +z (Lambert factor
+    exactly 1, so every covered pixel shows the texture sample itself).  tex_levels: RGBA8 mip
+    images, level 0 first.  Returns (colour bytes, fragments shaded)."""
+    def ndc(px, py):
+        return 2.0 * px / width - 1.0, 1.0 - 2.0 * py / height
+    corners = [(x0, y0, 0.0, 0.0), (x0 + side, y0, uv_scale, 0.0), (x0 + side, y0 + side, uv_scale, uv_scale),
+               (x0, y0 + side, 0.0, uv_scale)]
+    vdata = np.array([[*ndc(px, py), 0.5, 0.0, 0.0, 1.0, u, v] for px, py, u, v in corners], np.float32)
+    idx = np.array([0, 1, 2, 0, 2, 3], np.uint32)
+    vb = dev.create_buffer_init(vdata)
+    ib = dev.create_buffer_init(idx)
+    ub = dev.create_buffer_init(np.concatenate([np.eye(4, dtype=np.float32).ravel(),
+                                                np.array([0.0, 0.0, 1.0, 0.0], np.float32)]))
+    tfmt = W.TextureFormat.RGBA8_UNORM_SRGB if srgb_texture else W.TextureFormat.RGBA8_UNORM
+    ts = tex_levels[0].shape[0]
+    tex = dev.create_texture(ts, ts, tfmt, mip_level_count=len(tex_levels))
+    for m, im in enumerate(tex_levels):
+        if m == 0 or dev.profile == W.Profile.EXTENSION:
+            dev.queue.write_texture(tex, im, mip_level=m)
+    samp = dev.create_sampler(address, address, address, mag, min_, mip, lod_min, lod_max)
+    sm = dev.create_shader_module(native="mesh_tex_lambert")
+    pl = dev.create_render_pipeline(
+        sm, [W.VertexBufferLayout(32, [W.VertexAttribute(W.VertexFormat.FLOAT32X3, 0, 0),
+                                       W.VertexAttribute(W.VertexFormat.FLOAT32X3, 12, 1),
+                                       W.VertexAttribute(W.VertexFormat.FLOAT32X2, 24, 2)])],
+        W.PrimitiveState(W.PrimitiveTopology.TRIANGLE_LIST, cull_mode=W.Face.NONE), None, sm,
+        [W.ColorTargetState(color_format)])
+    g0 = dev.create_bind_group([W.BindGroupEntry(0, ub)])
+    g1 = dev.create_bind_group([W.BindGroupEntry(0, tex), W.BindGroupEntry(1, samp)])
+    color = dev.create_texture(width, height, color_format)
+    enc = dev.create_command_encoder()
+    rp = enc.begin_render_pass([W.RenderPassColorAttachment(color, clear)], None)
+    rp.set_pipeline(pl)
+    rp.set_bind_group(0, g0)
+    rp.set_bind_group(1, g1)
+    rp.set_vertex_buffer(0, vb)
+    rp.set_index_buffer(ib, W.IndexFormat.UINT32)
+    rp.draw_indexed(range(0, 6), 0, range(0, 1))
+    rp.end()
+    sub = dev.queue.submit([enc.finish()])
+    dev.poll(True, sub)
+    return dev.read_texture(color), dev.submission_stats(sub).fragments_shaded

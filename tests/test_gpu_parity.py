@@ -210,6 +210,48 @@ def test_blend_kernel_equals_generic_path(gpu_ext):
     assert np.array_equal(cs.view(np.uint16), cg.view(np.uint16))
 
 
+@pytest.mark.parametrize("side,uv_scale,srgb,mode,mag,min_,mip,fmt", [
+    (64, 1.0, False, W.AddressMode.REPEAT, 1, 1, 1, W.TextureFormat.RGBA8_UNORM),
+    (48, 1.0, True, W.AddressMode.REPEAT, 1, 1, 1, W.TextureFormat.RGBA8_UNORM_SRGB),
+    (32, 2.0, False, W.AddressMode.MIRROR_REPEAT, 1, 1, 1, W.TextureFormat.RGBA8_UNORM),
+    (100, 1.5, True, W.AddressMode.CLAMP_TO_EDGE, 1, 0, 1, W.TextureFormat.RGBA8_UNORM_SRGB),
+    (90, 1.3, False, W.AddressMode.REPEAT, 0, 0, 0, W.TextureFormat.BGRA8_UNORM_SRGB),
+    (512, 1.0, True, W.AddressMode.REPEAT, 1, 1, 1, W.TextureFormat.RGBA8_UNORM_SRGB),
+    (7, 9.0, True, W.AddressMode.MIRROR_REPEAT, 1, 1, 1, W.TextureFormat.RGBA8_UNORM),  # LOD past the last mip
+])
+def test_textured_quad_sampling_ext(gpu_ext, orc_ext, side, uv_scale, srgb, mode, mag, min_, mip, fmt):
+    """Extension-profile sampling (sRGB decode, LOD from the record's derivatives, nearest /
+    bilinear / trilinear, address modes) and sRGB target encoding, bit for bit with the oracle."""
+    levels = wl.mip_chain(wl.checker_noise_texture(256, 7))
+    kw = dict(srgb_texture=srgb, address=mode, mag=mag, min_=min_, mip=mip, color_format=fmt, uv_scale=uv_scale,
+              clear=(0.2, 0.1, 0.05, 1.0))
+    (cg, ng), (co, no) = [scenes.textured_quad(d, 600, 560, 17, 9, side, levels, **kw) for d in (gpu_ext, orc_ext)]
+    assert ng == no
+    assert np.array_equal(cg, co), f"{(cg != co).any(-1).sum()} pixels differ"
+
+
+@pytest.mark.parametrize("order", [W.RasterOrder.AUTO, W.RasterOrder.ORDERED])
+def test_textured_icosphere_filtered_ext(orc_ext, order):
+    """The textured configuration as the extension profile renders it: Rgba8UnormSrgb texture with
+    a full mip chain, linear min/mag/mip filtering, repeat, into an Rgba8UnormSrgb target with
+    Depth32Float Less — through the visibility raster and through the ordered raster."""
+    dev = W.Device(profile=W.Profile.EXTENSION, raster_order=order)
+    try:
+        kw = dict(width=480, height=272, level=4, tex_size=256, filtering=True, srgb=True)
+        res = [scenes.render_scene(d, wl.scene_textured_icosphere, **kw) for d in (dev, orc_ext)]
+        assert_same(*res, "filtered textured icosphere")
+    finally:
+        dev.close()
+
+
+def test_srgb_target_blending_ext(gpu_ext, orc_ext):
+    """Alpha blending into an Rgba8UnormSrgb target in the extension profile: the destination is
+    decoded to linear, blended, and encoded back."""
+    kw = dict(n_tris=300, width=200, height=150, seed=11, color_format=W.TextureFormat.RGBA8_UNORM_SRGB,
+              blend=W.BlendState.alpha_blending())
+    assert_same(scenes.random_clip_triangles(gpu_ext, **kw), scenes.random_clip_triangles(orc_ext, **kw), "srgb blend")
+
+
 def test_discard_program(gpu, orc):
     def build(dev):
         s = wl.scene_colored_sphere(dev, 200, 160)

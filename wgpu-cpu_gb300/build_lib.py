@@ -25,8 +25,8 @@ BUILD = os.path.join(HERE, "_build")
 
 SOURCES = ["kernels.cu", "runtime.cu", "jit.cu", "wgsl.cpp"]
 # headers compiled again at run time by NVRTC for WGSL programs (embedded in the library)
-JIT_HEADERS = ["gbr_types.h", "exact.cuh", "programs.cuh", "raster.cuh", "raster_vis.cuh", "raster_lines.cuh",
-               "wgsl_rt.cuh"]
+JIT_HEADERS = ["gbr_types.h", "exact.cuh", "srgb_tables.h", "sampling.cuh", "programs.cuh", "raster.cuh",
+               "raster_vis.cuh", "raster_lines.cuh", "wgsl_rt.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

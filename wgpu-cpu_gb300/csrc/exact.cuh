@@ -50,6 +50,14 @@ __device__ __forceinline__ uint32_t unorm8_trunc(float v) {
     return __float2uint_rz(s);
 }
 
+// Extension profile: float -> unorm8 as WebGPU converts, clamp to [0, 1] then round to nearest
+// (ties to even) of v * 255; NaN -> 0.  (The alpha of sRGB-encoded targets.)
+__device__ __forceinline__ uint32_t unorm8_round(float v) {
+    if (!(v > 0.0f)) return 0u;
+    if (v >= 1.0f) return 255u;
+    return (uint32_t)__float2int_rn(fmul(v, 255.0f));
+}
+
 // shoelace (raster.rs:294-298), left to right.
 __device__ __forceinline__ float shoelace(float ax, float ay, float bx, float by, float cx, float cy) {
     float t1 = fmul(fsub(by, ay), fadd(bx, ax));

@@ -57,6 +57,15 @@ enum ErrorCode : uint32_t {
     ERR_SHADER_TRAP = 9,  // a shader divided an integer by zero (EntryPointError::DivisionByZero)
 };
 
+// gbr_texture_format values the kernels test (gbr.h is not seen by NVRTC modules), and the
+// colour-target codes of sRGB targets in the extension profile, which encode linear -> sRGB on
+// write and decode on blending reads (the parity profile writes Srgb formats as Unorm).
+enum : uint32_t {
+    TEXFMT_RGBA8_UNORM_SRGB = 4,
+    TFMT_RGBA8_SRGB_ENCODE = 20,
+    TFMT_BGRA8_SRGB_ENCODE = 21,
+};
+
 // One texture binding as seen by the kernels.
 struct TexDesc {
     const uint8_t* data;  // mip 0 .. mip n-1 back to back
@@ -146,7 +155,7 @@ struct DrawDesc {
     uint32_t may_discard;    // the fragment stage can discard
     uint32_t strip_restart;  // triangle strip with primitive restart (separator indices)
     uint32_t strip_table;    // first entry of this draw's strip table in BatchParams::strip_info
-    uint32_t _pad_e;
+    uint32_t lod_var;        // extension-profile sampling: 1 + varying index of u (v follows), 0 = none
 };
 
 // Vertex stages the fast setup kernel specialises on: every input an f32 attribute of exactly
@@ -179,7 +188,8 @@ struct TriRecord {
     float inv_w0[3];     // 1/w of the unclipped vertices (perspective interpolation)
     uint32_t ovf;        // primary record: first overflow slot of sub-triangles 1..nsub-1
     uint32_t nsub;       // primary record: number of sub-triangles
-    uint32_t _pad[3];
+    float lod;           // extension-profile texture LOD of the draw's sampler (0 without one)
+    uint32_t _pad[2];
     // float var[3][num_varyings] follows (16-byte aligned: vector loads of the varyings)
 };
 static_assert(sizeof(TriRecord) % 16 == 0, "varyings start on a 16-byte boundary");

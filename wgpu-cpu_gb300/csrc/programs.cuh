@@ -9,6 +9,7 @@
 
 #include "exact.cuh"
 #include "gbr_types.h"
+#include "sampling.cuh"
 
 namespace gbr {
 
@@ -206,6 +207,7 @@ struct RasterState {
     float blend_constant[4];
     const uint8_t* tex_data;
     uint32_t tex_w, tex_h, addr_u, addr_v;
+    uint32_t tex_ext;  // extension-profile sampling (sample_ext with the record's LOD)
     float uconst[4];  // program constants read from the uniform block (light direction)
 };
 
@@ -236,6 +238,7 @@ __device__ __forceinline__ void build_raster_state(const DrawDesc& d, uint32_t d
     rs.tex_h = d.tex.height;
     rs.addr_u = d.samp.address_u;
     rs.addr_v = d.samp.address_v;
+    rs.tex_ext = d.lod_var != 0;
     for (int k = 0; k < 4; ++k) rs.uconst[k] = 0.0f;
     if (d.program == PROG_MESH_TEX_LAMBERT) {
         rs.uconst[0] = ld_uniform(d, 0, 0, 64);
@@ -266,8 +269,10 @@ __device__ __forceinline__ V4 sample_nearest_rgba8_lut(const RasterState& rs, fl
     return {lut[px & 0xFFu], lut[(px >> 8) & 0xFFu], lut[(px >> 16) & 0xFFu], lut[px >> 24]};
 }
 
-// Fragment stage on the cached state.  Returns false when the fragment is discarded.
-__device__ __forceinline__ bool run_fs_rs(const RasterState& rs, const float* var, const float* lut, V4& color) {
+// Fragment stage on the cached state.  Returns false when the fragment is discarded.  `lod` is
+// the record's texture LOD (extension-profile sampling only).
+__device__ __forceinline__ bool run_fs_rs(const RasterState& rs, const float* var, const float* lut, V4& color,
+                                          float lod = 0.0f) {
     switch (rs.program) {
         case PROG_COLORED_TRIANGLE:
         case PROG_QUAD_COLOR:
@@ -279,34 +284,10 @@ __device__ __forceinline__ bool run_fs_rs(const RasterState& rs, const float* va
             color = {var[0], var[1], var[2], 1.0f};
             return true;
         case PROG_MESH_TEX_LAMBERT: {
-            V4 t = sample_nearest_rgba8_lut(rs, var[3], var[4], lut);
+            V4 t = rs.tex_ext ? sample_ext(rs.dd->tex, rs.dd->samp, var[3], var[4], lod, lut)
+                              : sample_nearest_rgba8_lut(rs, var[3], var[4], lut);
             float dd = fadd(fmul(var[0], rs.uconst[0]), fmul(var[1], rs.uconst[1]));
             dd = fadd(dd, fmul(var[2], rs.uconst[2]));
-            float k = (dd > 0.0f) ? dd : 0.0f;  // select(0.0, d, d > 0.0)
-            color = {fmul(t.x, k), fmul(t.y, k), fmul(t.z, k), fmul(t.w, k)};
-            return true;
-        }
-        default: return false;
-    }
-}
-
-// Fragment stage.  Returns false when the fragment is discarded.
-__device__ __forceinline__ bool run_fs(const DrawDesc& d, const float* var, V4& color) {
-    switch (d.program) {
-        case PROG_COLORED_TRIANGLE:
-        case PROG_QUAD_COLOR:
-        case PROG_CLIP_PASSTHROUGH: color = {var[0], var[1], var[2], var[3]}; return true;
-        case PROG_MESH_COLOR:
-        case PROG_MESH_COLOR_PERSPECTIVE: color = {var[0], var[1], var[2], 1.0f}; return true;
-        case PROG_MESH_COLOR_DISCARD:
-            if (var[0] < 0.5f) return false;
-            color = {var[0], var[1], var[2], 1.0f};
-            return true;
-        case PROG_MESH_TEX_LAMBERT: {
-            V4 t = sample_nearest_rgba8(d.tex, d.samp, var[3], var[4]);
-            float lx = ld_uniform(d, 0, 0, 64), ly = ld_uniform(d, 0, 0, 68), lz = ld_uniform(d, 0, 0, 72);
-            float dd = fadd(fmul(var[0], lx), fmul(var[1], ly));
-            dd = fadd(dd, fmul(var[2], lz));
             float k = (dd > 0.0f) ? dd : 0.0f;  // select(0.0, d, d > 0.0)
             color = {fmul(t.x, k), fmul(t.y, k), fmul(t.z, k), fmul(t.w, k)};
             return true;

@@ -271,6 +271,21 @@ __device__ __forceinline__ bool resolve_vertex(const DrawDesc& d, uint32_t k, ui
 
 // Fills one sub-triangle record from its vertices' framebuffer coordinates and to_raster
 // outputs (viewport x, y, ndc z, 1/w); var holds up to NVMAX varyings per vertex.
+// Extension-profile texture LOD of a finished record: screen-space derivatives of the draw's
+// (u, v) varyings (u at varying index q) from the record's viewport vertices, area and clip
+// barycentrics.  Kept out of line: only extension-profile textured draws call it, and the setup
+// kernels' register budget stays with the common path.
+__device__ __noinline__ void record_lod(const DrawDesc& dd, uint32_t q, uint32_t nvar, TriRecord* r) {
+    float dcx[3], dcy[3];
+    bary_gradients(r->vpx, r->vpy, r->area, r->cb, dcx, dcy);
+    const float* rv = rec_var(r);
+    auto dvar = [&](uint32_t c, const float* dc) {
+        return fadd(fadd(fmul(rv[q + c], dc[0]), fmul(rv[nvar + q + c], dc[1])), fmul(rv[2 * nvar + q + c], dc[2]));
+    };
+    r->lod = lod_from_grad(dvar(0, dcx), dvar(1, dcx), dvar(0, dcy), dvar(1, dcy), dd.tex.width, dd.tex.height,
+                           dd.samp.lod_min, dd.samp.lod_max);
+}
+
 template <uint32_t NVMAX>
 __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriRecord* r, uint32_t key, uint32_t draw,
                                                   uint32_t prim_index, bool front_facing, const CV v[3],
@@ -332,12 +347,15 @@ __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriReco
         for (int j = 0; j < 3; ++j) r->cb[i * 3 + j] = v[i].b[j];
     }
     r->area = area;
+    r->lod = 0.0f;
     float* rv = rec_var(r);
 #pragma unroll
     for (uint32_t i = 0; i < 3; ++i)
 #pragma unroll
         for (uint32_t k = 0; k < NVMAX; ++k)
             if (k < nvar) rv[i * nvar + k] = var[i][k];
+    const uint32_t lod_var = bp.draws[draw].lod_var;
+    if (lod_var != 0 && !(flags & 2u)) record_lod(bp.draws[draw], lod_var - 1, nvar, r);
 }
 
 // Fills one sub-triangle record; returns false for a w == 0 vertex.
@@ -1052,6 +1070,14 @@ __device__ __forceinline__ void encode_color(uint32_t fmt, V4 col, uint32_t c[4]
             c[0] = __float_as_uint(col.x); c[1] = __float_as_uint(col.y);
             c[2] = __float_as_uint(col.z); c[3] = __float_as_uint(col.w);
             break;
+        case TFMT_RGBA8_SRGB_ENCODE:  // extension profile: RGB encoded to sRGB, alpha linear
+            c[0] = linear_to_srgb8(col.x) | (linear_to_srgb8(col.y) << 8) | (linear_to_srgb8(col.z) << 16) |
+                   (unorm8_round(col.w) << 24);
+            break;
+        case TFMT_BGRA8_SRGB_ENCODE:
+            c[0] = linear_to_srgb8(col.z) | (linear_to_srgb8(col.y) << 8) | (linear_to_srgb8(col.x) << 16) |
+                   (unorm8_round(col.w) << 24);
+            break;
         default: break;
     }
 }
@@ -1069,6 +1095,12 @@ __device__ __forceinline__ V4 decode_color(uint32_t fmt, const uint32_t c[4]) {
             return {lo.x, lo.y, hi.x, hi.y};
         }
         case 8: return {__uint_as_float(c[0]), __uint_as_float(c[1]), __uint_as_float(c[2]), __uint_as_float(c[3])};
+        case TFMT_RGBA8_SRGB_ENCODE:
+            return {srgb_to_linear(c[0]), srgb_to_linear(c[0] >> 8), srgb_to_linear(c[0] >> 16),
+                    fdiv((float)(c[0] >> 24), 255.0f)};
+        case TFMT_BGRA8_SRGB_ENCODE:
+            return {srgb_to_linear(c[0] >> 16), srgb_to_linear(c[0] >> 8), srgb_to_linear(c[0]),
+                    fdiv((float)(c[0] >> 24), 255.0f)};
         default: return {0.0f, 0.0f, 0.0f, 0.0f};
     }
 }
@@ -1125,7 +1157,7 @@ __device__ __forceinline__ bool run_fs_any(const BatchParams& bp, const RasterSt
         return st == 1;
     }
 #endif
-    return run_fs_rs(rs, var, lut, col);
+    return run_fs_rs(rs, var, lut, col, r.lod);
 }
 
 // Rank sort for small bins: every key counts the keys below it (keys are unique per tile) and

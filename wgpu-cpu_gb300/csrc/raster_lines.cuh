@@ -136,7 +136,13 @@ __device__ __forceinline__ void line_fragment(const BatchParams& bp, const DrawD
         keep = st == 1;
     } else
 #endif
-        keep = run_fs_rs(rs, var, lut, col);
+    {
+        // lines and points have no area: zero derivatives, the sampler's minimum LOD
+        const float lod = rs.tex_ext ? lod_from_grad(0.0f, 0.0f, 0.0f, 0.0f, rs.dd->tex.width, rs.dd->tex.height,
+                                                     rs.dd->samp.lod_min, rs.dd->samp.lod_max)
+                                     : 0.0f;
+        keep = run_fs_rs(rs, var, lut, col, lod);
+    }
     if (!keep) return;  // discard
     const size_t pix = (size_t)y * tg.width + x;
     if (rs.depth_test) {

@@ -507,6 +507,12 @@ TargetDesc make_target(const PassCmd& p, bool first_in_pass, uint32_t tile, uint
         uint32_t f = t.color_format;
         if (profile == GBR_PROFILE_PARITY && (f == GBR_TEXTURE_FORMAT_RGBA16_FLOAT || f == GBR_TEXTURE_FORMAT_RGBA32_FLOAT))
             fail(GBR_ERR_UNSUPPORTED, "Unsupported texture format for colour writes (texture.rs:407)");
+        // the reference writes Srgb formats as Unorm (texture.rs:389-398); the extension profile
+        // encodes linear -> sRGB on write and decodes for blending
+        if (profile == GBR_PROFILE_EXTENSION && f == GBR_TEXTURE_FORMAT_RGBA8_UNORM_SRGB)
+            t.color_format = TFMT_RGBA8_SRGB_ENCODE;
+        if (profile == GBR_PROFILE_EXTENSION && f == GBR_TEXTURE_FORMAT_BGRA8_UNORM_SRGB)
+            t.color_format = TFMT_BGRA8_SRGB_ENCODE;
     }
     if (p.depth) {
         const gbr_depth_attachment& da = p.begin.depth_attachment;
@@ -638,6 +644,9 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
     d.interp = prog.perspective ? INTERP_PERSPECTIVE : INTERP_LINEAR;
     d.may_discard = prog.may_discard ? 1u : 0u;
     d.profile = profile;
+    // extension-profile sampling needs the (u, v) derivatives: the native textured program's uv
+    // are varyings 3 and 4 (lod_var = 1 + the index of u)
+    d.lod_var = profile == GBR_PROFILE_EXTENSION && prog.id == PROG_MESH_TEX_LAMBERT ? 4u : 0u;
     d.cull_mode = ps.cull_mode;
     d.front_face = ps.front_face;
     // ToRaster::new (raster.rs:130-143): translation = offset + 0.5 size, scaling = 0.5 size, y *= -1
