@@ -165,7 +165,7 @@ typedef struct gbr_device_config {
     uint32_t time_kernels;      /* 1 = CUDA events around the raster kernels (stats.raster_ms) */
     uint64_t hbm_budget_bytes;  /* transient (per-submission) memory budget; 0 = 80 GB       */
     uint32_t raster_order;      /* gbr_raster_order                                          */
-    uint32_t _pad0;
+    uint32_t raster_rule;       /* gbr_raster_rule (EDGE requires the extension profile)     */
     uint64_t reserved[3];
 } gbr_device_config;
 
@@ -184,6 +184,16 @@ enum gbr_launch_mode { GBR_LAUNCH_BATCHED = 0, GBR_LAUNCH_PER_DRAW = 1, GBR_LAUN
  *             count as the ordered walk); every other batch walks its fragments in order.
  *  ORDERED  — always walk fragments in primitive order. */
 enum gbr_raster_order { GBR_RASTER_AUTO = 0, GBR_RASTER_ORDERED = 1 };
+
+/* Which pixels a triangle covers.
+ *  SCANLINE — the reference's rule (raster.rs:280-363, util/scanline.rs): integer framebuffer
+ *             vertices, inclusive spans walked by its scanline state machine, attributes
+ *             sampled at the integer pixel corner.  Bit-exact with wgpu-cpu.
+ *  EDGE     — extension profile: vertices snapped to 1/256 pixel, fixed-point edge functions
+ *             evaluated at pixel centres with the top-left rule (shared edges cover each pixel
+ *             exactly once), attributes sampled at the pixel centre.  Lines and points keep
+ *             the reference's Bresenham rule. */
+enum gbr_raster_rule { GBR_RASTER_RULE_SCANLINE = 0, GBR_RASTER_RULE_EDGE = 1 };
 
 typedef struct gbr_limits {
     uint32_t max_texture_dimension_2d;

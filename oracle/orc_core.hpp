@@ -389,6 +389,56 @@ static inline bool scanlines(const uint32_t fx[3], const uint32_t fy[3], Emit em
     return true;
 }
 
+// ------------------------------------------------------------------------------------------
+// Extension profile, edge-function rule (no reference counterpart): vertices snapped to 1/256
+// pixel (round to nearest even), coverage of pixel centres by three integer edge functions with
+// the top-left rule.  The kernels' span_edge (raster.cuh) follows the same steps.
+static inline int64_t floor_div64(int64_t a, int64_t b) {  // b > 0
+    int64_t q = a / b;
+    if ((a % b) != 0 && a < 0) --q;
+    return q;
+}
+static inline int64_t ceil_div64(int64_t a, int64_t b) { return -floor_div64(-a, b); }
+
+// Snapped vertices ordered to a positive doubled area, which is returned (0: nothing covered).
+static inline int64_t snap_triangle(const float vx[3], const float vy[3], int64_t X[3], int64_t Y[3]) {
+    for (int i = 0; i < 3; ++i) {
+        X[i] = (int64_t)std::nearbyint(vx[i] * 256.0f);
+        Y[i] = (int64_t)std::nearbyint(vy[i] * 256.0f);
+    }
+    int64_t a2 = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
+    if (a2 < 0) {
+        std::swap(X[1], X[2]);
+        std::swap(Y[1], Y[2]);
+        a2 = -a2;
+    }
+    return a2;
+}
+
+// Covered pixels [x1, x2] of row y: every edge i -> j (d = (dx, dy)) needs
+// E = dx (P.y - Y_i) - dy (P.x - X_i) > 0 at the centre P = (256 x + 128, 256 y + 128), or E == 0 on
+// a top (dy == 0, dx > 0) or left (dy < 0) edge.
+static inline void span_edge(const int64_t X[3], const int64_t Y[3], int64_t y, int64_t* x1, int64_t* x2) {
+    const int64_t py = y * 256 + 128;
+    int64_t lo = -(int64_t(1) << 30), hi = int64_t(1) << 30;
+    for (int e = 0; e < 3; ++e) {
+        const int i = e, j = (e + 1) % 3;
+        const int64_t dx = X[j] - X[i], dy = Y[j] - Y[i];
+        const bool owns_on_edge = dy < 0 || (dy == 0 && dx > 0);
+        // E(x) = -dy * (256 x + 128) + dx * (py - Y_i) + dy * X_i, needed >= (owns ? 0 : 1)
+        const int64_t a = -256 * dy;
+        const int64_t b = -128 * dy + dx * (py - Y[i]) + dy * X[i] - (owns_on_edge ? 0 : 1);
+        if (a > 0) lo = std::max(lo, ceil_div64(-b, a));
+        else if (a < 0) hi = std::min(hi, floor_div64(b, -a));
+        else if (b < 0) {
+            lo = 1;
+            hi = 0;
+        }
+    }
+    *x1 = lo;
+    *x2 = hi;
+}
+
 // shoelace (raster.rs:294-298), evaluated left to right.
 struct P2 {
     float x, y;

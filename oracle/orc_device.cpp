@@ -114,6 +114,7 @@ struct BindGroup : Object {
 
 struct Device {
     uint32_t profile = GBR_PROFILE_PARITY;
+    uint32_t raster_rule = GBR_RASTER_RULE_SCANLINE;
     std::mutex mu;
     uint64_t next_handle = 1;
     std::unordered_map<uint64_t, std::unique_ptr<Object>> objects;
@@ -876,19 +877,42 @@ static void execute_draw(Exec* ex, const PassState& st, bool indexed, uint32_t s
                     Bary3 lgx = {{(vb.y - vc.y) / total, (vc.y - va.y) / total, (va.y - vb.y) / total}};
                     Bary3 lgy = {{(vc.x - vb.x) / total, (va.x - vc.x) / total, (vb.x - va.x) / total}};
                     Bary3 dcx = compose_bary(clipb, lgx), dcy = compose_bary(clipb, lgy);
+                    auto emit = [&](uint32_t px, uint32_t py, P2 p) {
+                        if (!in_scissor(tr, px, py)) return;
+                        Bary3 lam = {{shoelace(p, vb, vc) / total, shoelace(va, p, vc) / total,
+                                      shoelace(va, vb, p) / total}};
+                        Bary3 comp = compose_bary(clipb, lam);
+                        V4 fragment = interp3_v4(frags, comp);
+                        process_fragment(fc, px, py, fragment, front_facing, (uint32_t)prim_index, 3, comp.c, verts,
+                                         inv_w, dcx.c, dcy.c);
+                    };
+                    if (ex->dev->raster_rule == GBR_RASTER_RULE_EDGE) {
+                        // extension: pixel centres inside the snapped edges (top-left rule),
+                        // attributes sampled at the centre
+                        const float vxs[3] = {va.x, vb.x, vc.x}, vys[3] = {va.y, vb.y, vc.y};
+                        for (int i = 0; i < 3; ++i)
+                            if (!(std::fabs(vxs[i]) < 4194304.0f && std::fabs(vys[i]) < 4194304.0f))
+                                fail(GBR_ERR_VALIDATION, "raster coordinates out of range for the edge rule");
+                        int64_t X[3], Y[3];
+                        if (snap_triangle(vxs, vys, X, Y) == 0) continue;
+                        const int64_t ylo = std::min(Y[0], std::min(Y[1], Y[2]));
+                        const int64_t yhi = std::max(Y[0], std::max(Y[1], Y[2]));
+                        int64_t r0 = std::max(ceil_div64(ylo - 128, 256), (int64_t)ex->band_y0);
+                        int64_t r1 = std::min(floor_div64(yhi - 128, 256), (int64_t)ex->band_y1 - 1);
+                        for (int64_t y = r0; y <= r1; ++y) {
+                            int64_t x1, x2;
+                            span_edge(X, Y, y, &x1, &x2);
+                            for (int64_t x = std::max<int64_t>(x1, 0); x <= x2; ++x)
+                                emit((uint32_t)x, (uint32_t)y, P2{(float)x + 0.5f, (float)y + 0.5f});
+                        }
+                        continue;
+                    }
                     uint32_t fxs[3] = {rp[0].fbx, rp[1].fbx, rp[2].fbx}, fys[3] = {rp[0].fby, rp[1].fby, rp[2].fby};
                     bool ok = scanlines(fxs, fys, [&](const Scanline& sl) {
                         if (sl.y < (int64_t)ex->band_y0 || sl.y >= (int64_t)ex->band_y1) return;
                         for (int64_t x = sl.x1; x <= sl.x2; ++x) {
                             uint32_t px = (uint32_t)x, py = (uint32_t)sl.y;
-                            if (!in_scissor(tr, px, py)) continue;
-                            P2 p = {(float)px, (float)py};
-                            Bary3 lam = {{shoelace(p, vb, vc) / total, shoelace(va, p, vc) / total,
-                                          shoelace(va, vb, p) / total}};
-                            Bary3 comp = compose_bary(clipb, lam);
-                            V4 fragment = interp3_v4(frags, comp);
-                            process_fragment(fc, px, py, fragment, front_facing, (uint32_t)prim_index, 3, comp.c,
-                                             verts, inv_w, dcx.c, dcy.c);
+                            emit(px, py, P2{(float)px, (float)py});
                         }
                     });
                     if (!ok) fail(GBR_ERR_VALIDATION, "scanlines generated points that don't fit u32");
@@ -1171,6 +1195,10 @@ ORC_API gbr_status orc_device_create(const gbr_device_config* cfg, gbr_device* o
         if (cfg->abi_version != GBR_ABI_VERSION) fail(GBR_ERR_INVALID_ARGUMENT, "ABI version mismatch");
         auto d = std::make_unique<Device>();
         d->profile = cfg->profile;
+        if (cfg->raster_rule > GBR_RASTER_RULE_EDGE) fail(GBR_ERR_INVALID_ARGUMENT, "raster_rule");
+        if (cfg->raster_rule == GBR_RASTER_RULE_EDGE && cfg->profile != GBR_PROFILE_EXTENSION)
+            fail(GBR_ERR_INVALID_ARGUMENT, "the edge-function raster rule belongs to the extension profile");
+        d->raster_rule = cfg->raster_rule;
         std::lock_guard<std::mutex> lk(g_devices_mu);
         uint64_t h = g_next_device++;
         g_devices[h] = std::move(d);

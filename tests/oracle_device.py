@@ -17,6 +17,6 @@ def lib() -> _abi.Lib:
     return _abi_lib
 
 
-def device(profile: int = Profile.PARITY, threads: int = 1) -> Device:
+def device(profile: int = Profile.PARITY, threads: int = 1, raster_rule: int = 0) -> Device:
     oracle_lib.load().orc_set_threads(threads)
-    return Device(lib=lib(), profile=profile)
+    return Device(lib=lib(), profile=profile, raster_rule=raster_rule)

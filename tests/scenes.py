@@ -240,3 +240,35 @@ def textured_quad(dev, width, height, x0, y0, side, tex_levels, uv_scale=1.0, sr
     sub = dev.queue.submit([enc.finish()])
     dev.poll(True, sub)
     return dev.read_texture(color), dev.submission_stats(sub).fragments_shaded
+
+
+def coverage_counts(dev, width, height, tris_px):
+    """Triangles given in framebuffer pixel coordinates (tris_px: (n, 3, 2)), drawn with colour
+    (1, 0, 0, 1) and additive blending (One/One) into an Rgba16Float target: each texel's red
+    channel counts the fragments that landed on it (exact in f16 for small counts).  Extension
+    profile.  Returns (counts (height, width) int array, fragments shaded)."""
+    t = np.asarray(tris_px, np.float64).reshape(-1, 2)
+    ndc = np.stack([2.0 * t[:, 0] / width - 1.0, 1.0 - 2.0 * t[:, 1] / height], 1)
+    pos = np.concatenate([ndc, np.full((len(t), 1), 0.5), np.ones((len(t), 1))], 1).astype(np.float32)
+    col = np.tile(np.array([1.0, 0.0, 0.0, 1.0], np.float32), (len(t), 1))
+    vb_pos = dev.create_buffer_init(pos)
+    vb_col = dev.create_buffer_init(col)
+    add = W.BlendComponent(W.BlendFactor.ONE, W.BlendFactor.ONE)
+    sm = dev.create_shader_module(native="clip_passthrough")
+    pl = dev.create_render_pipeline(
+        sm, [W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 0)]),
+             W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 1)])],
+        W.PrimitiveState(W.PrimitiveTopology.TRIANGLE_LIST, cull_mode=W.Face.NONE), None, sm,
+        [W.ColorTargetState(W.TextureFormat.RGBA16_FLOAT, W.BlendState(add, add))])
+    color = dev.create_texture(width, height, W.TextureFormat.RGBA16_FLOAT)
+    enc = dev.create_command_encoder()
+    rp = enc.begin_render_pass([W.RenderPassColorAttachment(color, (0.0, 0.0, 0.0, 0.0))], None)
+    rp.set_pipeline(pl)
+    rp.set_vertex_buffer(0, vb_pos)
+    rp.set_vertex_buffer(1, vb_col)
+    rp.draw(range(0, len(t)), range(0, 1))
+    rp.end()
+    sub = dev.queue.submit([enc.finish()])
+    dev.poll(True, sub)
+    img = dev.read_texture(color).view(np.float16).astype(np.float32)
+    return img[..., 0].astype(np.int64), dev.submission_stats(sub).fragments_shaded

@@ -252,6 +252,53 @@ def test_srgb_target_blending_ext(gpu_ext, orc_ext):
     assert_same(scenes.random_clip_triangles(gpu_ext, **kw), scenes.random_clip_triangles(orc_ext, **kw), "srgb blend")
 
 
+@pytest.fixture(scope="module", params=[W.RasterOrder.AUTO, W.RasterOrder.ORDERED], ids=["auto", "ordered"])
+def gpu_edge(request):
+    d = W.Device(profile=W.Profile.EXTENSION, raster_rule=W.RasterRule.EDGE, raster_order=request.param)
+    yield d
+    d.close()
+
+
+@pytest.fixture(scope="module")
+def orc_edge():
+    return oracle_device.device(profile=W.Profile.EXTENSION, threads=8, raster_rule=W.RasterRule.EDGE)
+
+
+def test_edge_rule_coverage(gpu_edge, orc_edge):
+    """Edge-function rule: hand-placed triangles with edges through pixel centres, random
+    triangles, and a mesh tiling a rectangle (each centre once), counted by additive blending."""
+    rng = np.random.default_rng(5)
+    tris = [[(10.5, 10.5), (20.5, 10.5), (10.5, 20.5)], [(20.5, 10.5), (20.5, 20.5), (10.5, 20.5)]]
+    for _ in range(200):
+        pts = rng.uniform([0, 0], [128, 64], (3, 2))
+        grid = 2 if rng.random() < 0.3 else 256  # half-pixel corners put edges through centres
+        pts = np.round(pts * grid) / grid
+        tris.append([tuple(p) for p in pts])
+    res = [scenes.coverage_counts(d, 128, 64, tris) for d in (gpu_edge, orc_edge)]
+    assert res[0][1] == res[1][1]
+    assert np.array_equal(res[0][0], res[1][0])
+
+
+@pytest.mark.parametrize("depth,blend", [(W.CompareFunction.LESS, None), (None, "alpha"),
+                                         (W.CompareFunction.GREATER_EQUAL, None)])
+def test_edge_rule_clipped_triangles(gpu_edge, orc_edge, depth, blend):
+    """Random clip-space triangles crossing every plane (sub-triangles, composed barycentrics) under
+    the edge rule: colour, depth and fragment counts bit for bit."""
+    kw = dict(n_tris=400, width=256, height=192, seed=17, depth=depth,
+              blend=W.BlendState.alpha_blending() if blend else None)
+    assert_same(scenes.random_clip_triangles(gpu_edge, **kw), scenes.random_clip_triangles(orc_edge, **kw), "edge")
+
+
+def test_edge_rule_textured_and_blended(gpu_edge, orc_edge):
+    kw = dict(width=480, height=272, level=4, tex_size=256, filtering=True, srgb=True)
+    res = [scenes.render_scene(d, wl.scene_textured_icosphere, **kw) for d in (gpu_edge, orc_edge)]
+    assert_same(*res, "edge textured")
+    kw = dict(width=320, height=192, n_quads=300, size_lo=8, size_hi=160)
+    (cg, _, ng), (co, _, no) = [scenes.render_scene(d, wl.scene_blended_quads, **kw) for d in (gpu_edge, orc_edge)]
+    assert ng == no
+    assert np.array_equal(cg.view(np.uint16), co.view(np.uint16))
+
+
 def test_discard_program(gpu, orc):
     def build(dev):
         s = wl.scene_colored_sphere(dev, 200, 160)

@@ -23,7 +23,7 @@ OUT_DIR = os.path.join(HERE, "wgpu_gb300")
 LIB = os.path.join(OUT_DIR, "libgbr.so")
 BUILD = os.path.join(HERE, "_build")
 
-SOURCES = ["kernels.cu", "runtime.cu", "jit.cu", "wgsl.cpp"]
+SOURCES = ["kernels.cu", "kernels_edge.cu", "runtime.cu", "jit.cu", "wgsl.cpp"]
 # headers compiled again at run time by NVRTC for WGSL programs (embedded in the library)
 JIT_HEADERS = ["gbr_types.h", "exact.cuh", "srgb_tables.h", "sampling.cuh", "programs.cuh", "raster.cuh",
                "raster_vis.cuh", "raster_lines.cuh", "wgsl_rt.cuh"]

@@ -156,6 +156,8 @@ struct DrawDesc {
     uint32_t strip_restart;  // triangle strip with primitive restart (separator indices)
     uint32_t strip_table;    // first entry of this draw's strip table in BatchParams::strip_info
     uint32_t lod_var;        // extension-profile sampling: 1 + varying index of u (v follows), 0 = none
+    uint32_t raster_rule;    // RASTER_RULE_SCANLINE / RASTER_RULE_EDGE
+    uint32_t _pad_f;
 };
 
 // Vertex stages the fast setup kernel specialises on: every input an f32 attribute of exactly
@@ -197,7 +199,12 @@ static_assert(sizeof(TriRecord) % 16 == 0, "varyings start on a 16-byte boundary
 enum : uint32_t {
     TRI_RECORD_HEADER_BYTES = sizeof(TriRecord),
     SPAN_DEGENERATE = 1,  // all three vertices on one row: single span xmin..xmax
+    SPAN_EDGE = 2,        // edge-function rule: pixel centres, top-left, 8-bit sub-pixel snapping
 };
+
+// How triangles cover pixels (gbr_raster_rule): the reference's scanline walk at integer pixel
+// corners, or (extension profile) fixed-point edge functions at pixel centres.
+enum : uint32_t { RASTER_RULE_SCANLINE = 0, RASTER_RULE_EDGE = 1 };
 
 // Device-side status of a batch (zeroed before launch).
 struct BatchStatus {
@@ -236,7 +243,7 @@ struct BatchParams {
     uint32_t* strip_info;        // strip tables of the restart draws (null when there are none)
     void* states;                // visibility raster: per-draw fragment-stage state (RasterState)
     uint32_t vis_compare;        // visibility raster: the batch's depth compare function
-    uint32_t _pad;
+    uint32_t raster_rule;        // RASTER_RULE_*: which instantiation of the kernels runs the batch
 };
 
 }  // namespace gbr

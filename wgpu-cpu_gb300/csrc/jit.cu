@@ -85,12 +85,17 @@ const Nvrtc& nvrtc() {
     return n;
 }
 
-// The kernels a JIT module exports, by name expression.
+// The kernels a JIT module exports, by name expression, for the reference's raster rule and for
+// the edge-function rule.
 constexpr int kJitVisTile = 16, kJitVisWarps = 4, kJitOrdTile = 16, kJitOrdWarps = 8;
-const char* const kKernelExprs[] = {
-    "&gbr::k_setup", "&gbr::k_setup_slow", "&gbr::k_scan", "&gbr::k_fill", "&gbr::k_build_states",
-    "&gbr::k_raster_vis<16, 4>", "&gbr::k_raster<16, 8, 4096, 64, 0>", "&gbr::k_eval_vs", "&gbr::k_strip_table",
-    "&gbr::k_clear_targets", "&gbr::k_lines_points"};
+constexpr int kJitKernels = 11;
+const char* const kKernelExprs[2][kJitKernels] = {
+    {"&gbr::k_setup<false>", "&gbr::k_setup_slow<false>", "&gbr::k_scan<0>", "&gbr::k_fill<false>",
+     "&gbr::k_build_states<0>", "&gbr::k_raster_vis<16, 4, false>", "&gbr::k_raster<16, 8, 4096, 64, 0, false>",
+     "&gbr::k_eval_vs", "&gbr::k_strip_table<0>", "&gbr::k_clear_targets", "&gbr::k_lines_points"},
+    {"&gbr::k_setup<true>", "&gbr::k_setup_slow<true>", "&gbr::k_scan<0>", "&gbr::k_fill<true>",
+     "&gbr::k_build_states<0>", "&gbr::k_raster_vis<16, 4, true>", "&gbr::k_raster<16, 8, 4096, 64, 0, true>",
+     "&gbr::k_eval_vs", "&gbr::k_strip_table<0>", "&gbr::k_clear_targets", "&gbr::k_lines_points"}};
 
 std::string program_source(const std::string& code) {
     std::string s;
@@ -128,8 +133,9 @@ bool jit_available(std::string* why) {
     return true;
 }
 
-bool jit_compile_cubin(const std::string& code, std::vector<char>* cubin, std::vector<std::string>* lowered,
+bool jit_compile_cubin(const std::string& code, bool edge, std::vector<char>* cubin, std::vector<std::string>* lowered,
                        std::string* log) {
+    const char* const* exprs = kKernelExprs[edge ? 1 : 0];
     std::string why;
     if (!jit_available(&why)) {
         *log = why;
@@ -143,7 +149,7 @@ bool jit_compile_cubin(const std::string& code, std::vector<char>* cubin, std::v
         *log = "nvrtcCreateProgram failed";
         return false;
     }
-    for (const char* e : kKernelExprs) n.add_name(prog, e);
+    for (int i = 0; i < kJitKernels; ++i) n.add_name(prog, exprs[i]);
     const std::string inc = "-I" + n.include_dir;
     // no multiply-add contraction in the front end nor in ptxas
     const char* opts[] = {"--gpu-architecture=sm_103a", "-fmad=false", "--ptxas-options=--fmad=false", "--std=c++17",
@@ -163,9 +169,9 @@ bool jit_compile_cubin(const std::string& code, std::vector<char>* cubin, std::v
     cubin->resize(cs);
     n.cubin(prog, cubin->data());
     lowered->clear();
-    for (const char* e : kKernelExprs) {
+    for (int i = 0; i < kJitKernels; ++i) {
         const char* name = nullptr;
-        n.lowered(prog, e, &name);
+        n.lowered(prog, exprs[i], &name);
         lowered->push_back(name ? name : "");
     }
     n.destroy(&prog);
@@ -176,17 +182,18 @@ JitKernels::~JitKernels() {
     if (lib) cudaLibraryUnload(lib);
 }
 
-std::shared_ptr<JitKernels> jit_module(const std::string& code, std::string* err) {
+std::shared_ptr<JitKernels> jit_module(const std::string& code, bool edge, std::string* err) {
+    const std::string key = (edge ? "edge\n" : "scanline\n") + code;
     {
         std::lock_guard<std::mutex> lk(g_cache_mu);
-        auto it = g_cache.find(code);
+        auto it = g_cache.find(key);
         if (it != g_cache.end())
             if (auto sp = it->second.lock()) return sp;
     }
     std::vector<char> cubin;
     std::vector<std::string> names;
     std::string log;
-    if (!jit_compile_cubin(code, &cubin, &names, &log)) {
+    if (!jit_compile_cubin(code, edge, &cubin, &names, &log)) {
         *err = "NVRTC: " + log;
         return nullptr;
     }
@@ -209,7 +216,7 @@ std::shared_ptr<JitKernels> jit_module(const std::string& code, std::string* err
     k->ord_tile = kJitOrdTile;
     k->ord_warps = kJitOrdWarps;
     std::lock_guard<std::mutex> lk(g_cache_mu);
-    g_cache[code] = k;
+    g_cache[key] = k;
     return k;
 }
 

@@ -29,12 +29,14 @@ struct JitKernels {
 bool jit_available(std::string* why);
 
 // Compiles emitted program code with the kernels (NVRTC, sm_103a) without loading it: the cubin
-// and the kernels' lowered names.  False with the compiler log on failure.
-bool jit_compile_cubin(const std::string& code, std::vector<char>* cubin, std::vector<std::string>* lowered,
+// and the kernels' lowered names, the kernels instantiated for the reference's raster rule or
+// (edge) the edge-function rule.  False with the compiler log on failure.
+bool jit_compile_cubin(const std::string& code, bool edge, std::vector<char>* cubin, std::vector<std::string>* lowered,
                        std::string* log);
 
-// A loaded module for the code (cached while any pipeline holds it); null with *err on failure.
-std::shared_ptr<JitKernels> jit_module(const std::string& code, std::string* err);
+// A loaded module for the code under one raster rule (cached while any pipeline holds it); null
+// with *err on failure.
+std::shared_ptr<JitKernels> jit_module(const std::string& code, bool edge, std::string* err);
 
 // launch_batch (kernels.h) with a JIT module's kernels; kind 3 = visibility raster, else ordered.
 cudaError_t launch_batch_jit(JitKernels& k, const BatchParams& bp, int num_sms, cudaStream_t s, uint32_t* launches,

@@ -1,64 +1,20 @@
-// kernels.cu — instantiates the render-pass kernels for the supported tile shapes and launches
-// one batch (setup -> scan -> fill -> raster) on a stream.
+// kernels.cu — instantiates the render-pass kernels for the supported tile shapes under the
+// reference's raster rule (kernels_edge.cu: the edge-function rule) and launches one batch
+// (setup -> scan -> fill -> raster) on a stream.
 #include <cuda_runtime.h>
 
 #include <mutex>
 
 #include "gbr.h"
 #include "kernels.h"
-#include "raster.cuh"
+#include "launch.cuh"
 #include "raster_lines.cuh"
-#include "raster_vis.cuh"
 
 namespace gbr {
 
-namespace {
+extern template cudaError_t launch_batch_t<true>(const BatchParams&, int, int, int, cudaStream_t, uint32_t*,
+                                                 cudaEvent_t*, int);
 
-constexpr int kCap = 4096;  // keys per tile sorted in shared memory; larger bins sort in place
-constexpr int kRW = 64;     // records staged in shared memory per window
-
-template <int T, int W, int KIND = 0>
-cudaError_t launch_raster(const BatchParams& bp, int num_sms, cudaStream_t s) {
-    auto kern = k_raster<T, W, kCap, kRW, KIND>;
-    const size_t smem = (kCap + 2 * W * 32) * sizeof(uint32_t) + (size_t)kRW * bp.record_stride;
-    static std::mutex mu;
-    static size_t configured = 0;
-    static int blocks_per_sm = 0;
-    {
-        std::lock_guard<std::mutex> lk(mu);
-        if (configured < smem) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, W * 32, smem);
-            if (e != cudaSuccess) return e;
-            if (blocks_per_sm < 1) blocks_per_sm = 1;
-            configured = smem;
-        }
-    }
-    const uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)num_sms * blocks_per_sm, bp.total_tiles);
-    kern<<<grid ? grid : 1, W * 32, smem, s>>>(bp);
-    return cudaGetLastError();
-}
-
-template <int T, int W>
-cudaError_t launch_raster_vis(const BatchParams& bp, int num_sms, cudaStream_t s) {
-    auto kern = k_raster_vis<T, W>;
-    static std::mutex mu;
-    static int blocks_per_sm = 0;
-    {
-        std::lock_guard<std::mutex> lk(mu);
-        if (blocks_per_sm == 0) {
-            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, W * 32, 0);
-            if (e != cudaSuccess) return e;
-            if (blocks_per_sm < 1) blocks_per_sm = 1;
-        }
-    }
-    const uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)num_sms * blocks_per_sm, bp.total_tiles);
-    kern<<<grid ? grid : 1, W * 32, 0, s>>>(bp);
-    return cudaGetLastError();
-}
-
-}  // namespace
 
 size_t raster_state_bytes() { return sizeof(RasterState); }
 
@@ -82,7 +38,7 @@ cudaError_t launch_lines(const BatchParams& bp, int num_sms, cudaStream_t s, uin
 }
 size_t setup_stage_bytes_host(uint32_t record_stride) { return setup_stage_bytes(record_stride); }
 size_t ordered_raster_smem_host(int warps, uint32_t record_stride) {
-    return (kCap + 2 * (size_t)warps * 32) * sizeof(uint32_t) + (size_t)kRW * record_stride;
+    return (launch_detail::kCap + 2 * (size_t)warps * 32) * sizeof(uint32_t) + (size_t)launch_detail::kRW * record_stride;
 }
 
 // Seeded inputs for the arithmetic self-test: random bit patterns, raster-like magnitudes,
@@ -134,30 +90,12 @@ __global__ void k_selftest_division(uint64_t n, uint64_t seed, unsigned long lon
     }
 }
 
-// Tile shapes of the ordered raster kernel.
-static bool ordered_config_supported(int tile, int warps) {
-    switch (tile) {
-        case 8: return warps == 1 || warps == 2;
-        case 16: return warps == 2 || warps == 4 || warps == 8;
-        case 32: return warps == 4 || warps == 8;
-        default: return false;
-    }
-}
-// Tile shapes of the visibility raster kernel.
-static bool vis_config_supported(int tile, int warps) {
-    switch (tile) {
-        case 8: return warps == 1 || warps == 2;
-        case 16: case 32: return warps == 1 || warps == 2 || warps == 4 || warps == 8;
-        default: return false;
-    }
-}
-
 bool raster_config_supported(int tile, int warps) {
-    return ordered_config_supported(tile, warps) || vis_config_supported(tile, warps);
+    return launch_detail::ordered_config_supported(tile, warps) || launch_detail::vis_config_supported(tile, warps);
 }
 
 uint32_t batch_kernel_launches(uint32_t total_prims, int tile, int warps, int kind) {
-    if (kind == 3 && !vis_config_supported(tile, warps)) kind = 0;
+    if (kind == 3 && !launch_detail::vis_config_supported(tile, warps)) kind = 0;
     return 2u + (total_prims ? 4u : 0u) + (kind == 3 ? 1u : 0u);
 }
 
@@ -198,105 +136,8 @@ uint32_t fast_vs_kind(const DrawDesc& d) {
 
 cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms, cudaStream_t s,
                          uint32_t* launches, cudaEvent_t* ev_raster, int kind) {
-    cudaError_t e;
-    if ((e = cudaMemsetAsync(bp.tile_count, 0, (bp.total_tiles + 1) * sizeof(uint32_t), s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(bp.status, 0, sizeof(BatchStatus), s)) != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(bp.work_counter, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
-    const uint32_t items = bp.total_prims;
-    const uint32_t cap = (uint32_t)num_sms * 16;
-    if (bp.strip_info && items) {
-        k_strip_table<<<bp.num_draws, 1024, 0, s>>>(bp);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        ++*launches;
-    }
-    if (items) {
-        uint32_t g = std::min((items + 127) / 128, cap);
-        const size_t smem = setup_stage_bytes(bp.record_stride);
-        {
-            static std::mutex mu;
-            static size_t configured = 0;
-            std::lock_guard<std::mutex> lk(mu);
-            if (configured < smem) {
-                if ((e = cudaFuncSetAttribute(k_setup, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-                    cudaSuccess)
-                    return e;
-                configured = smem;
-            }
-        }
-        k_setup<<<g, kSetupWarps * 32, smem, s>>>(bp);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        ++*launches;
-        k_setup_slow<<<std::min((items + 127) / 128, (uint32_t)num_sms * 4), 128, 0, s>>>(bp);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        ++*launches;
-    }
-    k_scan<<<1, 1024, 0, s>>>(bp);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    ++*launches;
-    if (items) {
-        uint32_t g = std::min((items + bp.ovf_capacity + 127) / 128, cap);
-        k_fill<<<g, 128, 0, s>>>(bp);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        ++*launches;
-    }
-    // Inside a stream capture the raster events must become event-record nodes of the graph
-    // (cudaEventRecordExternal); outside one that flag is not accepted.
-    unsigned int ev_flags = cudaEventRecordDefault;
-    if (ev_raster) {
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        if ((e = cudaStreamIsCapturing(s, &cs)) != cudaSuccess) return e;
-        if (cs == cudaStreamCaptureStatusActive) ev_flags = cudaEventRecordExternal;
-    }
-    if (kind == 3) {
-        k_build_states<<<(bp.num_draws + 127) / 128, 128, 0, s>>>(bp);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        ++*launches;
-    }
-    if (ev_raster && (e = cudaEventRecordWithFlags(ev_raster[0], s, ev_flags)) != cudaSuccess) return e;
-    if (kind == 3 && !vis_config_supported(tile, warps)) kind = 0;
-    // the ordered kernel for a warps-per-tile it has no instantiation for: the tile's default
-    if (kind != 3 && !ordered_config_supported(tile, warps)) warps = tile == 8 ? 2 : 8;
-    for (;;) {
-    switch ((tile * 16 + warps) * 4 + (kind & 3)) {
-        case (8 * 16 + 1) * 4: e = launch_raster<8, 1>(bp, num_sms, s); break;
-        case (8 * 16 + 2) * 4: e = launch_raster<8, 2>(bp, num_sms, s); break;
-        case (8 * 16 + 2) * 4 + 1: e = launch_raster<8, 2, 1>(bp, num_sms, s); break;
-        case (8 * 16 + 2) * 4 + 2: e = launch_raster<8, 2, 2>(bp, num_sms, s); break;
-        case (16 * 16 + 2) * 4: e = launch_raster<16, 2>(bp, num_sms, s); break;
-        case (16 * 16 + 2) * 4 + 1: e = launch_raster<16, 2, 1>(bp, num_sms, s); break;
-        case (16 * 16 + 2) * 4 + 2: e = launch_raster<16, 2, 2>(bp, num_sms, s); break;
-        case (16 * 16 + 4) * 4: e = launch_raster<16, 4>(bp, num_sms, s); break;
-        case (16 * 16 + 4) * 4 + 1: e = launch_raster<16, 4, 1>(bp, num_sms, s); break;
-        case (16 * 16 + 4) * 4 + 2: e = launch_raster<16, 4, 2>(bp, num_sms, s); break;
-        case (16 * 16 + 8) * 4: e = launch_raster<16, 8>(bp, num_sms, s); break;
-        case (16 * 16 + 8) * 4 + 1: e = launch_raster<16, 8, 1>(bp, num_sms, s); break;
-        case (16 * 16 + 8) * 4 + 2: e = launch_raster<16, 8, 2>(bp, num_sms, s); break;
-        case (32 * 16 + 4) * 4: e = launch_raster<32, 4>(bp, num_sms, s); break;
-        case (32 * 16 + 4) * 4 + 1: e = launch_raster<32, 4, 1>(bp, num_sms, s); break;
-        case (32 * 16 + 8) * 4: e = launch_raster<32, 8>(bp, num_sms, s); break;
-        case (32 * 16 + 8) * 4 + 1: e = launch_raster<32, 8, 1>(bp, num_sms, s); break;
-        case (32 * 16 + 8) * 4 + 2: e = launch_raster<32, 8, 2>(bp, num_sms, s); break;
-        case (8 * 16 + 1) * 4 + 3: e = launch_raster_vis<8, 1>(bp, num_sms, s); break;
-        case (8 * 16 + 2) * 4 + 3: e = launch_raster_vis<8, 2>(bp, num_sms, s); break;
-        case (16 * 16 + 1) * 4 + 3: e = launch_raster_vis<16, 1>(bp, num_sms, s); break;
-        case (16 * 16 + 2) * 4 + 3: e = launch_raster_vis<16, 2>(bp, num_sms, s); break;
-        case (16 * 16 + 4) * 4 + 3: e = launch_raster_vis<16, 4>(bp, num_sms, s); break;
-        case (16 * 16 + 8) * 4 + 3: e = launch_raster_vis<16, 8>(bp, num_sms, s); break;
-        case (32 * 16 + 1) * 4 + 3: e = launch_raster_vis<32, 1>(bp, num_sms, s); break;
-        case (32 * 16 + 2) * 4 + 3: e = launch_raster_vis<32, 2>(bp, num_sms, s); break;
-        case (32 * 16 + 4) * 4 + 3: e = launch_raster_vis<32, 4>(bp, num_sms, s); break;
-        case (32 * 16 + 8) * 4 + 3: e = launch_raster_vis<32, 8>(bp, num_sms, s); break;
-        default:
-            if (kind == 0) return cudaErrorInvalidValue;
-            kind = 0;  // no specialised instantiation for this tile shape: the generic kernel
-            continue;
-    }
-    break;
-    }
-    if (e != cudaSuccess) return e;
-    ++*launches;
-    if (ev_raster) e = cudaEventRecordWithFlags(ev_raster[1], s, ev_flags);
-    return e;
+    return bp.raster_rule == RASTER_RULE_EDGE ? launch_batch_t<true>(bp, tile, warps, num_sms, s, launches, ev_raster, kind)
+                                              : launch_batch_t<false>(bp, tile, warps, num_sms, s, launches, ev_raster, kind);
 }
 
 }  // namespace gbr

@@ -1,0 +1,195 @@
+// launch.cuh — the launch sequence of one batch (setup -> scan -> fill -> raster) with its tile-
+// shape dispatch, templated on the raster rule: kernels.cu instantiates it for the reference's
+// scanline rule and kernels_edge.cu for the edge-function rule, so each rule's kernels carry only
+// their own coverage code (and the two translation units compile in parallel).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <mutex>
+
+#include "kernels.h"
+#include "raster.cuh"
+#include "raster_vis.cuh"
+
+namespace gbr {
+
+namespace launch_detail {
+
+constexpr int kCap = 4096;  // keys per tile sorted in shared memory; larger bins sort in place
+constexpr int kRW = 64;     // records staged in shared memory per window
+
+template <int T, int W, int KIND, bool EDGE>
+cudaError_t launch_raster(const BatchParams& bp, int num_sms, cudaStream_t s) {
+    if constexpr (EDGE && KIND == 2) {
+        return cudaErrorInvalidValue;  // the textured specialisation is parity-profile only
+    } else {
+    auto kern = k_raster<T, W, kCap, kRW, KIND, EDGE>;
+    const size_t smem = (kCap + 2 * W * 32) * sizeof(uint32_t) + (size_t)kRW * bp.record_stride;
+    static std::mutex mu;
+    static size_t configured = 0;
+    static int blocks_per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (configured < smem) {
+            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (e != cudaSuccess) return e;
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, W * 32, smem);
+            if (e != cudaSuccess) return e;
+            if (blocks_per_sm < 1) blocks_per_sm = 1;
+            configured = smem;
+        }
+    }
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)num_sms * blocks_per_sm, bp.total_tiles);
+    kern<<<grid ? grid : 1, W * 32, smem, s>>>(bp);
+    return cudaGetLastError();
+    }
+}
+
+template <int T, int W, bool EDGE>
+cudaError_t launch_raster_vis(const BatchParams& bp, int num_sms, cudaStream_t s) {
+    auto kern = k_raster_vis<T, W, EDGE>;
+    static std::mutex mu;
+    static int blocks_per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (blocks_per_sm == 0) {
+            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, W * 32, 0);
+            if (e != cudaSuccess) return e;
+            if (blocks_per_sm < 1) blocks_per_sm = 1;
+        }
+    }
+    const uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)num_sms * blocks_per_sm, bp.total_tiles);
+    kern<<<grid ? grid : 1, W * 32, 0, s>>>(bp);
+    return cudaGetLastError();
+}
+
+
+// Tile shapes of the ordered raster kernel.
+inline bool ordered_config_supported(int tile, int warps) {
+    switch (tile) {
+        case 8: return warps == 1 || warps == 2;
+        case 16: return warps == 2 || warps == 4 || warps == 8;
+        case 32: return warps == 4 || warps == 8;
+        default: return false;
+    }
+}
+// Tile shapes of the visibility raster kernel.
+inline bool vis_config_supported(int tile, int warps) {
+    switch (tile) {
+        case 8: return warps == 1 || warps == 2;
+        case 16: case 32: return warps == 1 || warps == 2 || warps == 4 || warps == 8;
+        default: return false;
+    }
+}
+
+}  // namespace launch_detail
+
+template <bool EDGE>
+cudaError_t launch_batch_t(const BatchParams& bp, int tile, int warps, int num_sms, cudaStream_t s,
+                           uint32_t* launches, cudaEvent_t* ev_raster, int kind) {
+    using namespace launch_detail;
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(bp.tile_count, 0, (bp.total_tiles + 1) * sizeof(uint32_t), s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(bp.status, 0, sizeof(BatchStatus), s)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(bp.work_counter, 0, sizeof(uint32_t), s)) != cudaSuccess) return e;
+    const uint32_t items = bp.total_prims;
+    const uint32_t cap = (uint32_t)num_sms * 16;
+    if (bp.strip_info && items) {
+        k_strip_table<><<<bp.num_draws, 1024, 0, s>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        ++*launches;
+    }
+    if (items) {
+        uint32_t g = std::min((items + 127) / 128, cap);
+        const size_t smem = setup_stage_bytes(bp.record_stride);
+        {
+            static std::mutex mu;
+            static size_t configured = 0;
+            std::lock_guard<std::mutex> lk(mu);
+            if (configured < smem) {
+                if ((e = cudaFuncSetAttribute(k_setup<EDGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
+                    cudaSuccess)
+                    return e;
+                configured = smem;
+            }
+        }
+        k_setup<EDGE><<<g, kSetupWarps * 32, smem, s>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        ++*launches;
+        k_setup_slow<EDGE><<<std::min((items + 127) / 128, (uint32_t)num_sms * 4), 128, 0, s>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        ++*launches;
+    }
+    k_scan<><<<1, 1024, 0, s>>>(bp);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    ++*launches;
+    if (items) {
+        uint32_t g = std::min((items + bp.ovf_capacity + 127) / 128, cap);
+        k_fill<EDGE><<<g, 128, 0, s>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        ++*launches;
+    }
+    // Inside a stream capture the raster events must become event-record nodes of the graph
+    // (cudaEventRecordExternal); outside one that flag is not accepted.
+    unsigned int ev_flags = cudaEventRecordDefault;
+    if (ev_raster) {
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if ((e = cudaStreamIsCapturing(s, &cs)) != cudaSuccess) return e;
+        if (cs == cudaStreamCaptureStatusActive) ev_flags = cudaEventRecordExternal;
+    }
+    if (kind == 3) {
+        k_build_states<><<<(bp.num_draws + 127) / 128, 128, 0, s>>>(bp);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        ++*launches;
+    }
+    if (ev_raster && (e = cudaEventRecordWithFlags(ev_raster[0], s, ev_flags)) != cudaSuccess) return e;
+    if (kind == 3 && !vis_config_supported(tile, warps)) kind = 0;
+    if (EDGE && kind == 2) kind = 0;  // no textured specialisation under the edge rule
+    // the ordered kernel for a warps-per-tile it has no instantiation for: the tile's default
+    if (kind != 3 && !ordered_config_supported(tile, warps)) warps = tile == 8 ? 2 : 8;
+    for (;;) {
+    switch ((tile * 16 + warps) * 4 + (kind & 3)) {
+        case (8 * 16 + 1) * 4: e = launch_raster<8, 1, 0, EDGE>(bp, num_sms, s); break;
+        case (8 * 16 + 2) * 4: e = launch_raster<8, 2, 0, EDGE>(bp, num_sms, s); break;
+        case (8 * 16 + 2) * 4 + 1: e = launch_raster<8, 2, 1, EDGE>(bp, num_sms, s); break;
+        case (8 * 16 + 2) * 4 + 2: e = launch_raster<8, 2, 2, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 2) * 4: e = launch_raster<16, 2, 0, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 2) * 4 + 1: e = launch_raster<16, 2, 1, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 2) * 4 + 2: e = launch_raster<16, 2, 2, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 4) * 4: e = launch_raster<16, 4, 0, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 4) * 4 + 1: e = launch_raster<16, 4, 1, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 4) * 4 + 2: e = launch_raster<16, 4, 2, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 8) * 4: e = launch_raster<16, 8, 0, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 8) * 4 + 1: e = launch_raster<16, 8, 1, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 8) * 4 + 2: e = launch_raster<16, 8, 2, EDGE>(bp, num_sms, s); break;
+        case (32 * 16 + 4) * 4: e = launch_raster<32, 4, 0, EDGE>(bp, num_sms, s); break;
+        case (32 * 16 + 4) * 4 + 1: e = launch_raster<32, 4, 1, EDGE>(bp, num_sms, s); break;
+        case (32 * 16 + 8) * 4: e = launch_raster<32, 8, 0, EDGE>(bp, num_sms, s); break;
+        case (32 * 16 + 8) * 4 + 1: e = launch_raster<32, 8, 1, EDGE>(bp, num_sms, s); break;
+        case (32 * 16 + 8) * 4 + 2: e = launch_raster<32, 8, 2, EDGE>(bp, num_sms, s); break;
+        case (8 * 16 + 1) * 4 + 3: e = launch_raster_vis<8, 1, EDGE>(bp, num_sms, s); break;
+        case (8 * 16 + 2) * 4 + 3: e = launch_raster_vis<8, 2, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 1) * 4 + 3: e = launch_raster_vis<16, 1, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 2) * 4 + 3: e = launch_raster_vis<16, 2, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 4) * 4 + 3: e = launch_raster_vis<16, 4, EDGE>(bp, num_sms, s); break;
+        case (16 * 16 + 8) * 4 + 3: e = launch_raster_vis<16, 8, EDGE>(bp, num_sms, s); break;
+        case (32 * 16 + 1) * 4 + 3: e = launch_raster_vis<32, 1, EDGE>(bp, num_sms, s); break;
+        case (32 * 16 + 2) * 4 + 3: e = launch_raster_vis<32, 2, EDGE>(bp, num_sms, s); break;
+        case (32 * 16 + 4) * 4 + 3: e = launch_raster_vis<32, 4, EDGE>(bp, num_sms, s); break;
+        case (32 * 16 + 8) * 4 + 3: e = launch_raster_vis<32, 8, EDGE>(bp, num_sms, s); break;
+        default:
+            if (kind == 0) return cudaErrorInvalidValue;
+            kind = 0;  // no specialised instantiation for this tile shape: the generic kernel
+            continue;
+    }
+    break;
+    }
+    if (e != cudaSuccess) return e;
+    ++*launches;
+    if (ev_raster) e = cudaEventRecordWithFlags(ev_raster[1], s, ev_flags);
+    return e;
+}
+
+}  // namespace gbr

@@ -181,10 +181,72 @@ __device__ __forceinline__ bool inside_all_planes(const V4 pos[3]) {
     return true;
 }
 
+// ------------------------------------------------------------------------- edge-function rule
+// Extension profile, RASTER_RULE_EDGE (no reference counterpart: wgpu-cpu walks scanlines):
+// viewport coordinates snap to 1/256 pixel (round to nearest even), a pixel is covered when its
+// centre (x + 1/2, y + 1/2) lies inside all three edges, with the top-left rule on edges through
+// the centre.  Integer arithmetic throughout (snapped coordinates stay below 2^30, products below
+// 2^62), so the oracle reproduces every decision exactly.
+__device__ __forceinline__ int64_t floor_div(int64_t a, int64_t b) {  // b > 0
+    int64_t q = a / b;
+    if ((a % b) != 0 && a < 0) --q;
+    return q;
+}
+__device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b) { return -floor_div(-a, b); }
+
+// Snapped vertices in an order with positive doubled area (X1-X0)(Y2-Y0) - (Y1-Y0)(X2-X0); returns
+// that area (0: nothing is covered).
+__device__ __forceinline__ int64_t snap_triangle(const float vx[3], const float vy[3], int64_t X[3], int64_t Y[3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        X[i] = (int64_t)rintf(fmul(vx[i], 256.0f));
+        Y[i] = (int64_t)rintf(fmul(vy[i], 256.0f));
+    }
+    int64_t a2 = (X[1] - X[0]) * (Y[2] - Y[0]) - (Y[1] - Y[0]) * (X[2] - X[0]);
+    if (a2 < 0) {
+        int64_t t = X[1]; X[1] = X[2]; X[2] = t;
+        t = Y[1]; Y[1] = Y[2]; Y[2] = t;
+        a2 = -a2;
+    }
+    return a2;
+}
+
+// Row y's covered pixels [x1, x2] (empty when x1 > x2): per edge i -> j with d = (dx, dy),
+// E(P) = dx (P.y - Y_i) - dy (P.x - X_i) >= 0 on the inside; a top edge (dy == 0, dx > 0) or a
+// left edge (dy < 0) also owns the centres exactly on it.  At P.x = 256 x + 128 each edge bounds
+// x from one side.  Only the EDGE instantiations of the kernels contain it.
+__device__ __forceinline__ void span_edge(const TriRecord& r, int y, int& x1, int& x2) {
+    int64_t X[3], Y[3];
+    snap_triangle(r.vpx, r.vpy, X, Y);
+    const int64_t py = (int64_t)y * 256 + 128;
+    int64_t lo = -((int64_t)1 << 30), hi = (int64_t)1 << 30;
+#pragma unroll
+    for (int e = 0; e < 3; ++e) {
+        const int i = e, j = e == 2 ? 0 : e + 1;
+        const int64_t dx = X[j] - X[i], dy = Y[j] - Y[i];
+        const int64_t bias = (dy < 0 || (dy == 0 && dx > 0)) ? 0 : 1;
+        const int64_t a = -256 * dy;
+        const int64_t b = -128 * dy + dx * (py - Y[i]) + dy * X[i] - bias;  // a x + b >= 0
+        if (a > 0) lo = max(lo, ceil_div(-b, a));
+        else if (a < 0) hi = min(hi, floor_div(b, -a));
+        else if (b < 0) { lo = 1; hi = 0; }
+    }
+    const int64_t lim = (int64_t)1 << 30;
+    x1 = (int)(lo < -lim ? -lim : lo);
+    x2 = (int)(hi > lim ? lim : hi);
+}
+
 // ------------------------------------------------------------------------- spans
 // The row's inclusive span [x1, x2] of the scanline state machine, in closed form
 // (util/scanline.rs:14-146): x1 on edge AC, x2 on AB before row b.y and on BC from row b.y.
+// EDGE: the kernels are instantiated for the edge-function rule, whose records all use span_edge
+// (a batch's draws share their device's rule).
+template <bool EDGE = false>
 __device__ __forceinline__ void span_at(const TriRecord& r, int y, int& x1, int& x2) {
+    if constexpr (EDGE) {
+        span_edge(r, y, x1, x2);
+        return;
+    }
     if (r.flags & (SPAN_DEGENERATE << 2)) {
         x1 = r.xmin;
         x2 = r.xmax;
@@ -202,7 +264,7 @@ __device__ __forceinline__ void span_at(const TriRecord& r, int y, int& x1, int&
 
 // Calls f(tile_index_in_target) for every tile whose pixels the record can emit.
 // Tile rows are visited from `first` in steps of `step` (1, or 32 when a warp shares a record).
-template <class F>
+template <bool EDGE, class F>
 __device__ __forceinline__ void for_each_tile(const TriRecord& r, const DrawDesc& d, const TargetDesc& t, uint32_t shift,
                                               F&& f, int first = 0, int step = 1) {
     int lo = max(r.row0, (int)d.sc_y0);
@@ -214,17 +276,17 @@ __device__ __forceinline__ void for_each_tile(const TriRecord& r, const DrawDesc
     for (int ty = (lo >> shift) + first; ty <= (hi >> shift); ty += step) {
         int y0 = max(lo, ty << shift), y1 = min(hi, (ty << shift) + T - 1);
         int xa, xb, mn, mx;
-        span_at(r, y0, xa, xb);
+        span_at<EDGE>(r, y0, xa, xb);
         mn = xa; mx = xb;
-        span_at(r, y1, xa, xb);
+        span_at<EDGE>(r, y1, xa, xb);
         mn = min(mn, xa); mx = max(mx, xb);
         const int by = r.sy[1];
         if (by - 1 >= y0 && by - 1 <= y1) {
-            span_at(r, by - 1, xa, xb);
+            span_at<EDGE>(r, by - 1, xa, xb);
             mn = min(mn, xa); mx = max(mx, xb);
         }
         if (by >= y0 && by <= y1) {
-            span_at(r, by, xa, xb);
+            span_at<EDGE>(r, by, xa, xb);
             mn = min(mn, xa); mx = max(mx, xb);
         }
         mn = max(mn, sx_lo);
@@ -275,7 +337,7 @@ __device__ __forceinline__ bool resolve_vertex(const DrawDesc& d, uint32_t k, ui
 // (u, v) varyings (u at varying index q) from the record's viewport vertices, area and clip
 // barycentrics.  Kept out of line: only extension-profile textured draws call it, and the setup
 // kernels' register budget stays with the common path.
-__device__ __noinline__ void record_lod(const DrawDesc& dd, uint32_t q, uint32_t nvar, TriRecord* r) {
+static __device__ __noinline__ void record_lod(const DrawDesc& dd, uint32_t q, uint32_t nvar, TriRecord* r) {
     float dcx[3], dcy[3];
     bary_gradients(r->vpx, r->vpy, r->area, r->cb, dcx, dcy);
     const float* rv = rec_var(r);
@@ -286,7 +348,7 @@ __device__ __noinline__ void record_lod(const DrawDesc& dd, uint32_t q, uint32_t
                            dd.samp.lod_min, dd.samp.lod_max);
 }
 
-template <uint32_t NVMAX>
+template <uint32_t NVMAX, bool EDGE>
 __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriRecord* r, uint32_t key, uint32_t draw,
                                                   uint32_t prim_index, bool front_facing, const CV v[3],
                                                   const uint32_t fbx[3], const uint32_t fby[3], const V4 frag[3],
@@ -305,39 +367,77 @@ __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriReco
     cas(0, 2);
     cas(1, 2);
     uint32_t flags = front_facing ? 1u : 0u;
-    int64_t lim = 1ll << 30;
-    if (px[0] >= lim || px[1] >= lim || px[2] >= lim || py[2] >= lim) {
-        raise_error(bp.status, ERR_SPAN_RANGE, key);
-        flags |= 2u;
+    int row0, row1;
+    const DrawDesc& dd = bp.draws[draw];
+    if constexpr (EDGE) {
+        // rows whose centres lie within the snapped y extent, columns likewise; the span of each
+        // row comes from span_edge, and sy[1] is the first row past the middle vertex (where a
+        // span bound changes edge), which the tile and block range helpers sample
+        flags |= SPAN_EDGE << 2;
+        bool ok = true;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            ok = ok && fabsf(frag[i].x) < 4194304.0f && fabsf(frag[i].y) < 4194304.0f;  // 2^22 px
+        if (!ok) {
+            raise_error(bp.status, ERR_SPAN_RANGE, key);
+            flags |= 2u;
+            row0 = 1; row1 = 0;
+            r->xmin = 1; r->xmax = 0;
+            r->sy[1] = 0;
+        } else {
+            const float vx[3] = {frag[0].x, frag[1].x, frag[2].x}, vy[3] = {frag[0].y, frag[1].y, frag[2].y};
+            int64_t X[3], Y[3];
+            if (snap_triangle(vx, vy, X, Y) == 0 || area == 0.0f) flags |= 2u;
+            const int64_t ylo = min(Y[0], min(Y[1], Y[2])), yhi = max(Y[0], max(Y[1], Y[2]));
+            const int64_t ymid = Y[0] + Y[1] + Y[2] - ylo - yhi;
+            const int64_t xlo = min(X[0], min(X[1], X[2])), xhi = max(X[0], max(X[1], X[2]));
+            row0 = (int)ceil_div(ylo - 128, 256);
+            row1 = (int)floor_div(yhi - 128, 256);
+            r->xmin = (int)ceil_div(xlo - 128, 256);
+            r->xmax = (int)floor_div(xhi - 128, 256);
+            r->sy[1] = (int)floor_div(ymid - 128, 256) + 1;
+            if (row0 > row1 || r->xmin > r->xmax) flags |= 2u;
+        }
+        r->sx[0] = r->sx[1] = r->sx[2] = 0;
+        r->sy[0] = r->sy[2] = 0;
+    } else {
+        const int64_t lim = 1ll << 30;
+        if (px[0] >= lim || px[1] >= lim || px[2] >= lim || py[2] >= lim) {
+            raise_error(bp.status, ERR_SPAN_RANGE, key);
+            flags |= 2u;
+        }
+        if (area == 0.0f) flags |= 2u;  // raster.rs:308-311: no fragments
+        row0 = (int)py[0];
+        if (py[2] == py[0]) {
+            flags |= SPAN_DEGENERATE << 2;
+            row1 = row0;
+        } else if (py[1] == py[0]) {
+            row1 = (int)py[2];
+        } else if (py[2] == py[1]) {
+            row1 = (int)py[1] - 1;  // the state machine stops before row c.y (scanline.rs:114-121)
+        } else {
+            row1 = (int)py[2];
+        }
+        r->xmin = (int)min(px[0], min(px[1], px[2]));
+        r->xmax = (int)max(px[0], max(px[1], px[2]));
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            r->sx[i] = (int)px[i];
+            r->sy[i] = (int)py[i];
+        }
     }
-    if (area == 0.0f) flags |= 2u;  // raster.rs:308-311: no fragments
     // bit 4: the clip barycentrics are exactly the unit vectors (an unclipped triangle)
     if (v[0].b[0] == 1.0f && v[0].b[1] == 0.0f && v[0].b[2] == 0.0f && v[1].b[0] == 0.0f && v[1].b[1] == 1.0f &&
         v[1].b[2] == 0.0f && v[2].b[0] == 0.0f && v[2].b[1] == 0.0f && v[2].b[2] == 1.0f)
         flags |= 16u;
-    int row0 = (int)py[0], row1;
-    if (py[2] == py[0]) {
-        flags |= SPAN_DEGENERATE << 2;
-        row1 = row0;
-    } else if (py[1] == py[0]) {
-        row1 = (int)py[2];
-    } else if (py[2] == py[1]) {
-        row1 = (int)py[1] - 1;  // the state machine stops before row c.y (scanline.rs:114-121)
-    } else {
-        row1 = (int)py[2];
-    }
     r->key = key;
     r->draw = draw;
     r->prim_index = prim_index;
     r->flags = flags;
     r->row0 = row0;
     r->row1 = row1;
-    r->xmin = (int)min(px[0], min(px[1], px[2]));
-    r->xmax = (int)max(px[0], max(px[1], px[2]));
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        r->sx[i] = (int)px[i];
-        r->sy[i] = (int)py[i];
         r->vpx[i] = frag[i].x;
         r->vpy[i] = frag[i].y;
         r->fz[i] = frag[i].z;
@@ -354,11 +454,11 @@ __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriReco
 #pragma unroll
         for (uint32_t k = 0; k < NVMAX; ++k)
             if (k < nvar) rv[i * nvar + k] = var[i][k];
-    const uint32_t lod_var = bp.draws[draw].lod_var;
-    if (lod_var != 0 && !(flags & 2u)) record_lod(bp.draws[draw], lod_var - 1, nvar, r);
+    if (dd.lod_var != 0 && !(flags & 2u)) record_lod(dd, dd.lod_var - 1, nvar, r);
 }
 
 // Fills one sub-triangle record; returns false for a w == 0 vertex.
+template <bool EDGE>
 __device__ __forceinline__ bool build_record(const BatchParams& bp, const DrawDesc& d, TriRecord* r, uint32_t key,
                                              uint32_t draw, uint32_t prim_index, bool front_facing, const CV v[3],
                                              const float inv_w0[3], const float var[3][MAX_VARYING_FLOATS],
@@ -368,7 +468,7 @@ __device__ __forceinline__ bool build_record(const BatchParams& bp, const DrawDe
 #pragma unroll
     for (int i = 0; i < 3; ++i)
         if (!to_raster(d, v[i].p, fbx[i], fby[i], frag[i])) return false;
-    build_record_frag<MAX_VARYING_FLOATS>(bp, r, key, draw, prim_index, front_facing, v, fbx, fby, frag, inv_w0, var,
+    build_record_frag<MAX_VARYING_FLOATS, EDGE>(bp, r, key, draw, prim_index, front_facing, v, fbx, fby, frag, inv_w0, var,
                                           nvar);
     return true;
 }
@@ -386,6 +486,7 @@ __device__ __forceinline__ bool single_tile(const TriRecord& r, const DrawDesc& 
     return true;
 }
 
+template <bool EDGE>
 __device__ __forceinline__ void count_tiles(const BatchParams& bp, const TriRecord* r, const DrawDesc& d) {
     if (r->flags & 2u) return;
     const TargetDesc& t = bp.targets[d.target];
@@ -394,7 +495,7 @@ __device__ __forceinline__ void count_tiles(const BatchParams& bp, const TriReco
         atomicAdd(&bp.tile_count[base + one], 1u);
         return;
     }
-    for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) { atomicAdd(&bp.tile_count[base + lt], 1u); });
+    for_each_tile<EDGE>(*r, d, t, bp.tile_shift, [&](uint32_t lt) { atomicAdd(&bp.tile_count[base + lt], 1u); });
 }
 
 // A record spanning more than two tile rows is handed to the whole warp, whose lanes take its
@@ -402,7 +503,7 @@ __device__ __forceinline__ void count_tiles(const BatchParams& bp, const TriReco
 __device__ __forceinline__ bool tiles_are_many(const TriRecord& r, uint32_t shift) {
     return (r.row1 >> shift) - (r.row0 >> shift) >= 2;
 }
-template <class F>
+template <bool EDGE, class F>
 __device__ __forceinline__ void coop_tiles(const BatchParams& bp, const TriRecord* mine, uint32_t lane, F&& f) {
     uint32_t todo = __ballot_sync(0xFFFFFFFFu, mine != nullptr);
     while (todo) {
@@ -414,7 +515,7 @@ __device__ __forceinline__ void coop_tiles(const BatchParams& bp, const TriRecor
         const DrawDesc& d = bp.draws[r->draw];
         const TargetDesc& t = bp.targets[d.target];
         const uint32_t key = r->key;
-        for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) { f(t.tile_base + lt, key); }, (int)lane, 32);
+        for_each_tile<EDGE>(*r, d, t, bp.tile_shift, [&](uint32_t lt) { f(t.tile_base + lt, key); }, (int)lane, 32);
     }
 }
 
@@ -427,6 +528,8 @@ __device__ __forceinline__ void coop_tiles(const BatchParams& bp, const TriRecor
 // sum-scan), one CTA per draw.  Setup reads it for primitive slot k - 2.
 constexpr uint32_t kNoStripTri = 0xFFFFFFFFu;
 
+// (a template only so that both kernel translation units can instantiate it)
+template <int = 0>
 __global__ void __launch_bounds__(1024) k_strip_table(BatchParams bp) {
     const DrawDesc& d = bp.draws[blockIdx.x];
     if (!d.strip_restart) return;
@@ -509,6 +612,7 @@ __global__ void __launch_bounds__(1024) k_strip_table(BatchParams bp) {
 // ---- generic setup: any program, format, topology; clipping; error reporting
 // Sets up primitive gp of draw di (record written in place); a record spanning many tile rows
 // is returned in `coop` for the warp to count together.
+template <bool EDGE>
 __device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp, const TriRecord*& coop) {
     TriRecord* prim_rec = rec_at(bp.records, bp.record_stride, gp);
     const uint32_t di = find_draw(bp.draws, bp.num_draws, gp);
@@ -583,7 +687,7 @@ __device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp
             v[i].b[1] = i == 1 ? 1.0f : 0.0f;
             v[i].b[2] = i == 2 ? 1.0f : 0.0f;
         }
-        if (!build_record(bp, d, prim_rec, gp << SUBTRI_BITS, di, prim_index, front_facing, v, inv_w0, var, nvar)) {
+        if (!build_record<EDGE>(bp, d, prim_rec, gp << SUBTRI_BITS, di, prim_index, front_facing, v, inv_w0, var, nvar)) {
             raise_error(bp.status, ERR_W_ZERO, gp);
             prim_rec->flags = 2u;
             return;
@@ -591,7 +695,7 @@ __device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp
         prim_rec->nsub = 1;
         prim_rec->ovf = 0;
         if (!(prim_rec->flags & 2u) && tiles_are_many(*prim_rec, bp.tile_shift)) coop = prim_rec;
-        else count_tiles(bp, prim_rec, d);
+        else count_tiles<EDGE>(bp, prim_rec, d);
         return;
     }
     // clipped: count the sub-triangles, reserve overflow slots, then emit in order
@@ -620,11 +724,11 @@ __device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp
         uint32_t nvar;
         __device__ void operator()(const CV* v) {
             TriRecord* r = s == 0 ? prim_rec : rec_at(bp->ovf_records, bp->record_stride, ovf + s - 1);
-            if (!build_record(*bp, *d, r, (gp << SUBTRI_BITS) | s, di, p, ff, v, inv_w0, var, nvar)) {
+            if (!build_record<EDGE>(*bp, *d, r, (gp << SUBTRI_BITS) | s, di, p, ff, v, inv_w0, var, nvar)) {
                 raise_error(bp->status, ERR_W_ZERO, gp);
                 r->flags = 2u;
             } else {
-                count_tiles(*bp, r, *d);
+                count_tiles<EDGE>(*bp, r, *d);
             }
             ++s;
         }
@@ -637,6 +741,7 @@ __device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp
 }
 
 // The primitives the fast kernel queued, one lane each.
+template <bool EDGE>
 __global__ void __launch_bounds__(128) k_setup_slow(BatchParams bp) {
     const uint32_t n = bp.status->slow_count;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -644,8 +749,8 @@ __global__ void __launch_bounds__(128) k_setup_slow(BatchParams bp) {
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
         if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the warp
         const TriRecord* coop = nullptr;
-        if (base + lane < n) setup_generic(bp, bp.slow_prims[base + lane], coop);
-        coop_tiles(bp, coop, lane, [&](uint32_t tile, uint32_t) { atomicAdd(&bp.tile_count[tile], 1u); });
+        if (base + lane < n) setup_generic<EDGE>(bp, bp.slow_prims[base + lane], coop);
+        coop_tiles<EDGE>(bp, coop, lane, [&](uint32_t tile, uint32_t) { atomicAdd(&bp.tile_count[tile], 1u); });
     }
 }
 
@@ -729,7 +834,7 @@ __device__ __forceinline__ bool fast_vertex(const DrawDesc& d, const float* mvp,
 
 // Sets up primitive gp completely when it needs no clipping and raises no error (returns
 // false otherwise: the generic kernel redoes it, reports errors and clips).
-template <int FVS>
+template <int FVS, bool EDGE>
 __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc& d, const float* mvp, uint32_t gp,
                                           uint32_t di, TriRecord* rec, const TriRecord*& coop) {
     constexpr uint32_t NV = fast_vs_varyings(FVS);
@@ -821,11 +926,11 @@ __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc&
         if ((fbx[i] | fby[i]) >= (1u << 30)) return false;  // the generic path reports it
         frag[i] = {vx, vy, nz, rw[i]};
     }
-    build_record_frag<NV>(bp, rec, gp << SUBTRI_BITS, di, p, front_facing, v, fbx, fby, frag, rw, var, NV);
+    build_record_frag<NV, EDGE>(bp, rec, gp << SUBTRI_BITS, di, p, front_facing, v, fbx, fby, frag, rw, var, NV);
     rec->nsub = 1;
     rec->ovf = 0;
     if (!(rec->flags & 2u) && tiles_are_many(*rec, bp.tile_shift)) coop = rec;
-    else count_tiles(bp, rec, d);
+    else count_tiles<EDGE>(bp, rec, d);
     return true;
 }
 
@@ -834,6 +939,7 @@ __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc&
 // primary records are built in shared memory and written out as one contiguous, coalesced
 // block (records of consecutive primitives are adjacent).  Primitives it cannot finish are
 // queued for k_setup_slow.
+template <bool EDGE>
 __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
     extern __shared__ __align__(16) uint8_t s_stage_raw[];
     __shared__ DrawCache s_dc[kSetupWarps];
@@ -874,12 +980,12 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
         bool done = false;
         if (live && uniform) {
             switch (dc.d.fast_vs) {  // warp-uniform
-                case FAST_VS_MVP_COLOR: done = fast_prim<FAST_VS_MVP_COLOR>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                case FAST_VS_MVP_TEX: done = fast_prim<FAST_VS_MVP_TEX>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                case FAST_VS_QUAD: done = fast_prim<FAST_VS_QUAD>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                case FAST_VS_CLIP: done = fast_prim<FAST_VS_CLIP>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                case FAST_VS_TRIANGLE: done = fast_prim<FAST_VS_TRIANGLE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                case FAST_VS_QUAD_F16: done = fast_prim<FAST_VS_QUAD_F16>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_MVP_COLOR: done = fast_prim<FAST_VS_MVP_COLOR, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_MVP_TEX: done = fast_prim<FAST_VS_MVP_TEX, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_QUAD: done = fast_prim<FAST_VS_QUAD, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_CLIP: done = fast_prim<FAST_VS_CLIP, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_TRIANGLE: done = fast_prim<FAST_VS_TRIANGLE, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                case FAST_VS_QUAD_F16: done = fast_prim<FAST_VS_QUAD_F16, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
                 default: break;
             }
         }
@@ -892,7 +998,7 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
             at = __shfl_sync(0xFFFFFFFFu, at, leader);
             if (live && !done) bp.slow_prims[at + __popc(m & ((1u << lane) - 1u))] = gp;
         }
-        coop_tiles(bp, coop, lane, [&](uint32_t tile, uint32_t) { atomicAdd(&bp.tile_count[tile], 1u); });
+        coop_tiles<EDGE>(bp, coop, lane, [&](uint32_t tile, uint32_t) { atomicAdd(&bp.tile_count[tile], 1u); });
         // the warp's records, staged above, out as one block
         __syncwarp();
         const uint32_t nrec = min(32u, bp.total_prims - base);
@@ -907,6 +1013,8 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
 // Single-CTA exclusive scan of tile counts -> tile_offset; zeroes tile_cursor.
 // Chunks of 4096 counts are loaded coalesced into shared memory, each thread scans four
 // consecutive counts, and warps combine through shuffles; a carry links the chunks.
+// (a template only so that both kernel translation units can instantiate it)
+template <int = 0>
 __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
     __shared__ uint32_t buf[4096];
     __shared__ uint32_t warp_sum[32];
@@ -968,6 +1076,7 @@ __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
     }
 }
 
+template <bool EDGE>
 __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
     // after an abort the setup kernels returned early: the records are not this batch's
     if (bp.status->error || *bp.abort_flag) return;
@@ -994,11 +1103,11 @@ __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
                     const uint32_t key = r->key;
                     uint32_t one;
                     if (single_tile(*r, d, t, bp.tile_shift, one)) put(t.tile_base + one, key);
-                    else for_each_tile(*r, d, t, bp.tile_shift, [&](uint32_t lt) { put(t.tile_base + lt, key); });
+                    else for_each_tile<EDGE>(*r, d, t, bp.tile_shift, [&](uint32_t lt) { put(t.tile_base + lt, key); });
                 }
             }
         }
-        coop_tiles(bp, coop, lane, put);
+        coop_tiles<EDGE>(bp, coop, lane, put);
     }
 }
 
@@ -1171,34 +1280,12 @@ __device__ __forceinline__ void rank_sort(const uint32_t* in, uint32_t* out, uin
     }
 }
 
-// x-range of the pixels a record emits on rows [y0, y1] (already inside [row0, row1]).
-__device__ __forceinline__ void band_xrange(const TriRecord& r, int y0, int y1, int& mn, int& mx) {
-    int xa, xb;
-    span_at(r, y0, xa, xb);
-    mn = xa;
-    mx = xb;
-    span_at(r, y1, xa, xb);
-    mn = min(mn, xa);
-    mx = max(mx, xb);
-    const int by = r.sy[1];
-    if (by - 1 >= y0 && by - 1 <= y1) {
-        span_at(r, by - 1, xa, xb);
-        mn = min(mn, xa);
-        mx = max(mx, xb);
-    }
-    if (by >= y0 && by <= y1) {
-        span_at(r, by, xa, xb);
-        mn = min(mn, xa);
-        mx = max(mx, xb);
-    }
-}
-
 // One tile per CTA iteration.  Pixels are owned by threads in 8x4 blocks (one block per warp
 // per PPT slot); their colour and depth stay in registers for the whole tile.  Records are
 // staged RW at a time; for each staged record the CTA computes which 8x4 blocks it can touch
 // (exact per-block-row x ranges of its spans), and every warp walks only the records whose bit
 // is set for its block, in key order (ballot + find-first-set), without further barriers.
-template <int T, int WARPS, int CAP, int RW, int KIND>
+template <int T, int WARPS, int CAP, int RW, int KIND, bool EDGE = false>
 __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
     constexpr int NT = WARPS * 32;
     constexpr int BLK_X = T / 8, BLK_Y = T / 4, NBLK = BLK_X * BLK_Y;
@@ -1325,7 +1412,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                     const DrawDesc& d = bp.draws[r.draw];
                     if ((uint32_t)y >= d.sc_y0 && (uint32_t)y < d.sc_y1) {
                         int x1, x2;
-                        span_at(r, y, x1, x2);
+                        span_at<EDGE>(r, y, x1, x2);
                         sp.x = max(max(x1, (int)d.sc_x0), tx * T);
                         sp.y = min(min(min(x2, (int)d.sc_x1 - 1), tx * T + T - 1), (int)tg.width - 1);
                     }
@@ -1395,7 +1482,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                     // every pixel slot of a thread lies in one column when the warps of a tile
                     // cover whole block rows: x + a.x (likewise b, c) is then a per-record term
                     constexpr bool ONE_COL = WARPS % BLK_X == 0;
-                    const float xa0 = fadd(pfx[0], ax), xb0 = fadd(pfx[0], bx), xc0 = fadd(pfx[0], cx);
+                    // the sample point: the integer pixel corner (the reference), or the pixel
+                    // centre under the edge-function rule (x + 1/2 is exact)
+                    const float px0 = EDGE ? fadd(pfx[0], 0.5f) : pfx[0];
+                    const float xa0 = fadd(px0, ax), xb0 = fadd(px0, bx), xc0 = fadd(px0, cx);
 #pragma unroll
                     for (int k = 0; k < PPT; ++k) {
                         const int blk = warp + k * WARPS;
@@ -1409,7 +1499,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                         // barycentrics at the integer pixel corner (raster.rs:313-321, 334-335); an
                         // IEEE sum does not depend on operand order, so x + a.x serves both shoelace
                         // terms that contain it (likewise b, c)
-                        const float fx = pfx[k], fy = pfy[k];
+                        const float fx = EDGE ? fadd(pfx[k], 0.5f) : pfx[k], fy = EDGE ? fadd(pfy[k], 0.5f) : pfy[k];
                         const float xa = ONE_COL ? xa0 : fadd(fx, ax), xb = ONE_COL ? xb0 : fadd(fx, bx),
                                     xc = ONE_COL ? xc0 : fadd(fx, cx);
                         if constexpr (KIND == 1) {

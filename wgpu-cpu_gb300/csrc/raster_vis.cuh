@@ -57,11 +57,12 @@ __device__ __forceinline__ void bary_consts(const TriRecord& r, BaryK& k) {
     k.ident = (r.flags & 16u) != 0;
 }
 
-// Barycentrics at the integer pixel corner composed with the clip barycentrics
-// (raster.rs:313-321, 334-343), as in k_raster.
+// Barycentrics at the integer pixel corner (the edge-function rule: the pixel centre) composed
+// with the clip barycentrics (raster.rs:313-321, 334-343), as in k_raster.
+template <bool EDGE>
 __device__ __forceinline__ void bary_at(const TriRecord& r, const BaryK& k, int x, int y, float cmp[3]) {
     // an IEEE sum does not depend on operand order: x + a.x serves both terms containing it
-    const float fx = (float)x, fy = (float)y;
+    const float fx = EDGE ? fadd((float)x, 0.5f) : (float)x, fy = EDGE ? fadd((float)y, 0.5f) : (float)y;
     const float xa = fadd(fx, k.ax), xb = fadd(fx, k.bx), xc = fadd(fx, k.cx);
     const float s0 = fadd(fadd(fmul(fsub(k.by, fy), xb), k.kc0), fmul(fsub(fy, k.cy), xc));
     const float s1 = fadd(fadd(fmul(fsub(fy, k.ay), xa), fmul(fsub(k.cy, fy), xc)), k.kc1);
@@ -115,7 +116,7 @@ __device__ __forceinline__ void tile_sync() {
 // (larger ones: lanes split the box), each covered fragment atomicMin-ing its key into the
 // tile's key array.  Phase 2: one thread per pixel re-evaluates the survivor's barycentrics,
 // tests it against the stored depth, runs the fragment stage and writes colour and depth.
-template <int T, int WARPS>
+template <int T, int WARPS, bool EDGE = false>
 __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
     constexpr int NT = WARPS * 32, NPIX = T * T;
     constexpr unsigned long long kNone = ~0ull;
@@ -150,7 +151,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
 
         auto fragment = [&](const TriRecord& r, const BaryK& k, uint32_t order, int x, int y) {
             float cmp[3];
-            bary_at(r, k, x, y, cmp);
+            bary_at<EDGE>(r, k, x, y, cmp);
             ++frag_count;
             const float z = frag_z(r, cmp);
             if (z != z) return;
@@ -178,7 +179,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                 bary_consts(*r, k);
                 for (int y = y0; y <= y1; ++y) {
                     int x1, x2;
-                    span_at(*r, y, x1, x2);
+                    span_at<EDGE>(*r, y, x1, x2);
                     x1 = max(x1, xl);
                     x2 = min(x2, xr);
                     for (int x = x1; x <= x2; ++x) fragment(*r, k, key, x, y);
@@ -202,7 +203,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                 const int lr = lane / cols, lc = lane - lr * cols;
                 for (int y = by0 + lr; lr < rows_per_pass && y <= by1; y += rows_per_pass) {
                     int x1, x2;
-                    span_at(*br, y, x1, x2);
+                    span_at<EDGE>(*br, y, x1, x2);
                     x1 = max(x1, bxl);
                     x2 = min(x2, bxr);
                     for (int x = bxl + lc; x <= x2; x += cols)
@@ -231,7 +232,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                 BaryK k;
                 bary_consts(r, k);
                 float cmp[3];
-                bary_at(r, k, x, y, cmp);
+                bary_at<EDGE>(r, k, x, y, cmp);
                 const float z = frag_z(r, cmp);
                 if (depth_compare(cmpf, z, depth)) {
                     const RasterState& rs = states[r.draw];
@@ -302,6 +303,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
 }
 
 // Per-draw fragment-stage state for k_raster_vis, built once per batch.
+// (a template only so that both kernel translation units can instantiate it)
+template <int = 0>
 __global__ void k_build_states(BatchParams bp) {
     RasterState* states = static_cast<RasterState*>(bp.states);
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < bp.num_draws; i += gridDim.x * blockDim.x)

@@ -1008,6 +1008,7 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
                 b.lines = dc.pipeline->desc.primitive.topology < GBR_TOPOLOGY_TRIANGLE_LIST;
                 first = false;
                 DrawDesc d = make_draw(dc, profile, (bool)p.depth);
+                d.raster_rule = cfg.raster_rule;
                 uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
                 *prims_in += np;
                 if (np > kMaxPrims) fail(GBR_ERR_UNSUPPORTED, "too many primitives in one draw");
@@ -1041,6 +1042,7 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
         for (const DrawCmd& dc : p.draws) {
             ++*draws;
             DrawDesc d = make_draw(dc, profile, (bool)p.depth);
+            d.raster_rule = cfg.raster_rule;
             d.prim_base = b.total_prims;
             d.target = ti;
             uint64_t np = (uint64_t)d.prims_per_instance * d.instance_count;
@@ -1205,6 +1207,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 bp.work_counter = reinterpret_cast<uint32_t*>(meta + off_work) + i * 4;
                 bp.status = reinterpret_cast<BatchStatus*>(meta + off_status) + i;
                 bp.abort_flag = reinterpret_cast<uint32_t*>(meta);
+                bp.raster_rule = cfg.raster_rule;
                 if (kinds[i] == 3) {
                     bp.states = meta + states_off[i];
                     bp.vis_compare = visibility_compare(b);
@@ -1554,6 +1557,9 @@ GBR_API gbr_status gbr_device_create(const gbr_device_config* cfg, gbr_device* o
         d->autotune = cfg->tile_size == 0 && cfg->warps_per_tile == 0;
         if (cfg->launch_mode > GBR_LAUNCH_PER_PASS) fail(GBR_ERR_INVALID_ARGUMENT, "launch_mode");
         if (cfg->raster_order > GBR_RASTER_ORDERED) fail(GBR_ERR_INVALID_ARGUMENT, "raster_order");
+        if (cfg->raster_rule > GBR_RASTER_RULE_EDGE) fail(GBR_ERR_INVALID_ARGUMENT, "raster_rule");
+        if (cfg->raster_rule == GBR_RASTER_RULE_EDGE && cfg->profile != GBR_PROFILE_EXTENSION)
+            fail(GBR_ERR_INVALID_ARGUMENT, "the edge-function raster rule belongs to the extension profile");
         cuda_check(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         Device* raw = d.get();
         d->worker = std::thread([raw] { raw->worker_main(); });
@@ -1802,7 +1808,7 @@ GBR_API gbr_status gbr_wgsl_compile_check(const char* wgsl, uint64_t len, const 
         std::vector<char> cubin;
         std::vector<std::string> names;
         std::string lg;
-        const bool ok = jit_compile_cubin(pc.cuda, &cubin, &names, &lg);
+        const bool ok = jit_compile_cubin(pc.cuda, false, &cubin, &names, &lg);
         if (log && capacity) {
             const size_t k = std::min<size_t>(capacity - 1, lg.size());
             std::memcpy(log, lg.data(), k);
@@ -1874,7 +1880,7 @@ GBR_API gbr_status gbr_render_pipeline_create(gbr_device dh, const gbr_render_pi
             }
             pi.may_discard = pc.may_discard;
             std::string err;
-            pl->jit = jit_module(pc.cuda, &err);
+            pl->jit = jit_module(pc.cuda, d->cfg.raster_rule == GBR_RASTER_RULE_EDGE, &err);
             if (!pl->jit) fail(GBR_ERR_SHADER, "%s", err.c_str());
             pl->prog = &pl->own;
         } else if (desc->has_fragment) {

@@ -51,7 +51,7 @@ class DeviceConfig(C.Structure):
     _fields_ = [("abi_version", u32), ("profile", u32), ("device_ordinal", u32), ("tile_size", u32),
                 ("bin_capacity", u32), ("warps_per_tile", u32), ("launch_mode", u32), ("batch_submissions", u32),
                 ("use_graphs", u32), ("time_kernels", u32), ("hbm_budget_bytes", u64), ("raster_order", u32),
-                ("_pad0", u32), ("reserved", u64 * 3)]
+                ("raster_rule", u32), ("reserved", u64 * 3)]
 
 
 class Limits(C.Structure):

@@ -143,6 +143,11 @@ class RasterOrder:
     ORDERED = 1
 
 
+class RasterRule:
+    SCANLINE = 0  # the reference's scanline walk at integer pixel corners (bit-exact)
+    EDGE = 1      # extension profile: fixed-point edge functions, pixel centres, top-left rule
+
+
 class BindingKind:
     BUFFER = 0
     SAMPLER = 1
@@ -482,7 +487,8 @@ class Device:
     def __init__(self, lib: Optional[A.Lib] = None, profile: int = Profile.PARITY, tile_size: int = 0,
                  warps_per_tile: int = 0, bin_capacity: int = 0, launch_mode: int = LaunchMode.BATCHED,
                  batch_submissions: bool = False, use_graphs: bool = False, hbm_budget_bytes: int = 0,
-                 device_ordinal: int = 0, time_kernels: bool = False, raster_order: int = 0):
+                 device_ordinal: int = 0, time_kernels: bool = False, raster_order: int = 0,
+                 raster_rule: int = RasterRule.SCANLINE):
         self.lib = lib if lib is not None else gpu_lib()
         cfg = A.DeviceConfig()
         cfg.abi_version = A.GBR_ABI_VERSION
@@ -497,11 +503,13 @@ class Device:
         cfg.time_kernels = int(time_kernels)
         cfg.hbm_budget_bytes = hbm_budget_bytes
         cfg.raster_order = int(raster_order)
+        cfg.raster_rule = int(raster_rule)
         h = C.c_uint64()
         self.handle = 0
         _check(self.lib, self.lib.device_create(C.byref(cfg), C.byref(h)))
         self.handle = h.value
         self.profile = profile
+        self.raster_rule = raster_rule
         self.queue = Queue(self)
 
     def close(self) -> None:
