@@ -355,10 +355,7 @@ def run_ours(args, wk: Workload):
                 dev.queue.write_buffer(obj, 0, host.numpy())
         i = dev.queue.submit([cmd])
         dev.poll(True, i)
-        for t, o in reads:
-            st = dev.lib.texture_read(dev.handle, t.handle, 0, o.data_ptr(), o.numel())
-            if st != 0:
-                raise W.GbrError(st, dev.lib.error_text())
+        dev.read_textures_into([(t, 0, o.data_ptr(), o.numel()) for t, o in reads])
 
     for _ in range(max(1, min(args.warmup, 3))):
         e2e_step()

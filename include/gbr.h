@@ -454,6 +454,12 @@ GBR_API gbr_status gbr_queue_write_texture(gbr_device device, gbr_texture textur
 /* wgpu_cpu::image::rgba_texture_image (lib.rs:158-173): waits for prior submissions and
  * copies the whole mip level (tightly packed rows) into `dst`. */
 GBR_API gbr_status gbr_texture_read(gbr_device device, gbr_texture texture, uint32_t mip_level, void* dst, uint64_t size);
+/* No reference counterpart (readback of many targets): gbr_texture_read for `count` textures in
+ * one queue operation — one wait for prior submissions, the copies back to back, one return.
+ * dsts[k] receives mip level mips[k] of textures[k] and must hold sizes[k] >= its bytes; pinned
+ * destinations (cudaHostAlloc / cudaHostRegister) move at full DMA speed. */
+GBR_API gbr_status gbr_textures_read(gbr_device device, uint32_t count, const gbr_texture* textures,
+                                     const uint32_t* mip_levels, void* const* dsts, const uint64_t* sizes);
 
 /* DeviceInterface::create_sampler (device.rs:185-187 -> sampler.rs:4-29). */
 GBR_API gbr_status gbr_sampler_create(gbr_device device, const gbr_sampler_desc* desc, gbr_sampler* out_sampler);

@@ -18,6 +18,31 @@ extern template cudaError_t launch_batch_t<true>(const BatchParams&, int, int, i
 
 size_t raster_state_bytes() { return sizeof(RasterState); }
 
+// One block per segment (grid-stride over segments): 16-byte copies where the destination and
+// size allow, else 4-byte, else bytes.
+__global__ void __launch_bounds__(256) k_scatter_writes(const uint8_t* stage, const uint64_t* desc, uint32_t n) {
+    for (uint32_t seg = blockIdx.x; seg < n; seg += gridDim.x) {
+        uint8_t* dst = reinterpret_cast<uint8_t*>(desc[3 * seg]);
+        const uint8_t* src = stage + desc[3 * seg + 1];
+        const uint64_t size = desc[3 * seg + 2];
+        const uintptr_t a = reinterpret_cast<uintptr_t>(dst);
+        if ((a & 15) == 0 && (size & 15) == 0) {
+            for (uint64_t k = threadIdx.x; k < size / 16; k += blockDim.x)
+                reinterpret_cast<uint4*>(dst)[k] = reinterpret_cast<const uint4*>(src)[k];
+        } else if ((a & 3) == 0 && (size & 3) == 0) {
+            for (uint64_t k = threadIdx.x; k < size / 4; k += blockDim.x)
+                reinterpret_cast<uint32_t*>(dst)[k] = reinterpret_cast<const uint32_t*>(src)[k];
+        } else {
+            for (uint64_t k = threadIdx.x; k < size; k += blockDim.x) dst[k] = src[k];
+        }
+    }
+}
+cudaError_t launch_scatter_writes(const uint8_t* stage, const uint64_t* desc, uint32_t n, cudaStream_t s) {
+    if (!n) return cudaSuccess;
+    k_scatter_writes<<<n < 1024u ? n : 1024u, 256, 0, s>>>(stage, desc, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_lines(const BatchParams& bp, int num_sms, cudaStream_t s, uint32_t* launches, cudaEvent_t* ev_raster) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(bp.status, 0, sizeof(BatchStatus), s)) != cudaSuccess) return e;

@@ -33,4 +33,8 @@ uint32_t batch_kernel_launches(uint32_t total_prims, int tile, int warps, int ki
 // The FastVs shape of a resolved draw (FAST_VS_NONE when the fast setup path cannot run it).
 uint32_t fast_vs_kind(const DrawDesc& d);
 
+// Places n coalesced writes: segment k copies desc[3k + 2] bytes from stage + desc[3k + 1] to the
+// device address desc[3k] (stage offsets are 16-byte aligned).
+cudaError_t launch_scatter_writes(const uint8_t* stage, const uint64_t* desc, uint32_t n, cudaStream_t s);
+
 }  // namespace gbr

@@ -771,30 +771,56 @@ __host__ __device__ __forceinline__ size_t setup_stage_bytes(uint32_t record_str
 }
 
 template <int C>
-__device__ __forceinline__ bool fetch_f32(const DrawDesc& d, int loc, uint32_t vertex, uint32_t instance, float* out) {
+__device__ __forceinline__ void fetch_f32_unchecked(const DrawDesc& d, int loc, uint32_t vertex, uint32_t instance,
+                                                    float* out) {
     const int b = d.attr[loc].buffer;
     const uint64_t start = (uint64_t)instance * d.vb_stride_instance[b] + (uint64_t)vertex * d.vb_stride_vertex[b] +
                            d.attr[loc].offset;
-    if (start + 4 * C > d.vb_size[b]) return false;
     const float* f = reinterpret_cast<const float*>(d.vb_data[b] + start);
 #pragma unroll
     for (int k = 0; k < C; ++k) out[k] = __ldg(f + k);
-    return true;
 }
 
 __host__ __device__ constexpr uint32_t fast_vs_varyings(int fvs) {
     return fvs == FAST_VS_MVP_COLOR ? 3u : fvs == FAST_VS_MVP_TEX ? 5u : 4u;
 }
 
-// The vertex stage of run_vs for one FastVs shape (same operations); false = fetch out of range.
+// Whether every attribute fetch of one FastVs vertex stays inside its vertex buffer.
+__device__ __forceinline__ bool attr_in_range(const DrawDesc& d, int loc, uint32_t vertex, uint32_t instance,
+                                              uint32_t bytes) {
+    const int b = d.attr[loc].buffer;
+    return (uint64_t)instance * d.vb_stride_instance[b] + (uint64_t)vertex * d.vb_stride_vertex[b] + d.attr[loc].offset +
+               bytes <= d.vb_size[b];
+}
 template <int FVS>
-__device__ __forceinline__ bool fast_vertex(const DrawDesc& d, const float* mvp, uint32_t vertex, uint32_t instance,
+__device__ __forceinline__ bool fast_vertex_in_range(const DrawDesc& d, uint32_t vertex, uint32_t instance) {
+    if constexpr (FVS == FAST_VS_MVP_COLOR)
+        return attr_in_range(d, 0, vertex, instance, 12) && attr_in_range(d, 1, vertex, instance, 12);
+    else if constexpr (FVS == FAST_VS_MVP_TEX)
+        return attr_in_range(d, 0, vertex, instance, 12) && attr_in_range(d, 1, vertex, instance, 12) &&
+               attr_in_range(d, 2, vertex, instance, 8);
+    else if constexpr (FVS == FAST_VS_QUAD)
+        return attr_in_range(d, 0, vertex, instance, 12) && attr_in_range(d, 1, vertex, instance, 16);
+    else if constexpr (FVS == FAST_VS_QUAD_F16)
+        return attr_in_range(d, 0, vertex, instance, 12) && attr_in_range(d, 1, vertex, instance, 8);
+    else if constexpr (FVS == FAST_VS_CLIP)
+        return attr_in_range(d, 0, vertex, instance, 16) && attr_in_range(d, 1, vertex, instance, 16);
+    else
+        return true;
+}
+
+// The vertex stage of run_vs for one FastVs shape (same operations), for a vertex whose fetches
+// fast_vertex_in_range has checked: no branch stands between the loads of a primitive's three
+// vertices, so they are all in flight together.
+template <int FVS>
+__device__ __forceinline__ void fast_vertex(const DrawDesc& d, const float* mvp, uint32_t vertex, uint32_t instance,
                                             V4& pos, float* var) {
     float a0[4], a1[4], a2[2];
     if constexpr (FVS == FAST_VS_MVP_COLOR || FVS == FAST_VS_MVP_TEX) {
-        if (!fetch_f32<3>(d, 0, vertex, instance, a0) || !fetch_f32<3>(d, 1, vertex, instance, a1)) return false;
+        fetch_f32_unchecked<3>(d, 0, vertex, instance, a0);
+        fetch_f32_unchecked<3>(d, 1, vertex, instance, a1);
         if constexpr (FVS == FAST_VS_MVP_TEX) {
-            if (!fetch_f32<2>(d, 2, vertex, instance, a2)) return false;
+            fetch_f32_unchecked<2>(d, 2, vertex, instance, a2);
             var[3] = a2[0];
             var[4] = a2[1];
         }
@@ -803,22 +829,23 @@ __device__ __forceinline__ bool fast_vertex(const DrawDesc& d, const float* mvp,
         var[1] = a1[1];
         var[2] = a1[2];
     } else if constexpr (FVS == FAST_VS_QUAD) {
-        if (!fetch_f32<3>(d, 0, vertex, instance, a0) || !fetch_f32<4>(d, 1, vertex, instance, a1)) return false;
+        fetch_f32_unchecked<3>(d, 0, vertex, instance, a0);
+        fetch_f32_unchecked<4>(d, 1, vertex, instance, a1);
         pos = {a0[0], a0[1], a0[2], 1.0f};
         for (int k = 0; k < 4; ++k) var[k] = a1[k];
     } else if constexpr (FVS == FAST_VS_QUAD_F16) {
         // Float16x4 colour widened to f32 (the extension profile's fetch_attr conversion)
-        if (!fetch_f32<3>(d, 0, vertex, instance, a0)) return false;
+        fetch_f32_unchecked<3>(d, 0, vertex, instance, a0);
         const AttrDesc& a = d.attr[1];
         const int b = a.buffer;
         const uint64_t start = (uint64_t)instance * d.vb_stride_instance[b] + (uint64_t)vertex * d.vb_stride_vertex[b] +
                                a.offset;
-        if (start + 8 > d.vb_size[b]) return false;
         const uint16_t* h = reinterpret_cast<const uint16_t*>(d.vb_data[b] + start);
         pos = {a0[0], a0[1], a0[2], 1.0f};
         for (int k = 0; k < 4; ++k) var[k] = f16_bits_to_f32(__ldg(h + k));
     } else if constexpr (FVS == FAST_VS_CLIP) {
-        if (!fetch_f32<4>(d, 0, vertex, instance, a0) || !fetch_f32<4>(d, 1, vertex, instance, a1)) return false;
+        fetch_f32_unchecked<4>(d, 0, vertex, instance, a0);
+        fetch_f32_unchecked<4>(d, 1, vertex, instance, a1);
         pos = {a0[0], a0[1], a0[2], a0[3]};
         for (int k = 0; k < 4; ++k) var[k] = a1[k];
     } else {
@@ -829,7 +856,6 @@ __device__ __forceinline__ bool fast_vertex(const DrawDesc& d, const float* mvp,
         var[2] = (float)(vi == 2u);
         var[3] = 1.0f;
     }
-    return true;
 }
 
 // Sets up primitive gp completely when it needs no clipping and raises no error (returns
@@ -856,28 +882,35 @@ __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc&
         sp[1] = 3 * p + 1;
         sp[2] = 3 * p + 2;
     }
+    // index resolution (render_pass/index.rs:45-88) and the vertex stage, every range check first
+    // (any failure hands the primitive to the generic kernel, which reports it in the reference's
+    // order), so the three index loads and then all attribute loads issue back to back
+    uint32_t vtx[3];
+    const uint64_t at_last = (uint64_t)d.first + max(sp[0], max(sp[1], sp[2]));
+#pragma unroll
+    for (int k = 0; k < 3; ++k) vtx[k] = d.first + sp[k];
+    if (d.index_format != 0) {
+        const uint32_t isz = d.index_format == 1 ? 2u : 4u;
+        if ((at_last + 1) * isz > d.index_bytes) return false;
+        uint32_t raw[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+            raw[k] = d.index_format == 1 ? (uint32_t)__ldg(reinterpret_cast<const uint16_t*>(d.index_data) + vtx[k])
+                                         : __ldg(reinterpret_cast<const uint32_t*>(d.index_data) + vtx[k]);
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const int64_t v = (int64_t)raw[k] + (int64_t)d.base_vertex;
+            if (v < 0 || v > 0xFFFFFFFFll) return false;
+            vtx[k] = (uint32_t)v;
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+        if (!fast_vertex_in_range<FVS>(d, vtx[k], instance)) return false;
     V4 pos[3];
     float var[3][NV];
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        // index resolution (render_pass/index.rs:45-88)
-        const uint32_t at = d.first + sp[k];
-        uint32_t vertex = at;
-        if (d.index_format != 0) {
-            uint32_t raw;
-            if (d.index_format == 1) {
-                if ((uint64_t)(at + 1) * 2 > d.index_bytes) return false;
-                raw = __ldg(reinterpret_cast<const uint16_t*>(d.index_data) + at);
-            } else {
-                if ((uint64_t)(at + 1) * 4 > d.index_bytes) return false;
-                raw = __ldg(reinterpret_cast<const uint32_t*>(d.index_data) + at);
-            }
-            const int64_t v = (int64_t)raw + (int64_t)d.base_vertex;
-            if (v < 0 || v > 0xFFFFFFFFll) return false;
-            vertex = (uint32_t)v;
-        }
-        if (!fast_vertex<FVS>(d, mvp, vertex, instance, pos[k], var[k])) return false;
-    }
+    for (int k = 0; k < 3; ++k) fast_vertex<FVS>(d, mvp, vtx[k], instance, pos[k], var[k]);
     if (!d.has_fragment) return true;
     if (pos[0].w == 0.0f || pos[1].w == 0.0f || pos[2].w == 0.0f) return false;
     // x/w, y/w, z/w by the correctly rounded reciprocal RN(1/w) (also the reference's

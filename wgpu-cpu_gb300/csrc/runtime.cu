@@ -211,7 +211,7 @@ struct PassCmd {
 
 // ---------------------------------------------------------------- queue items
 struct Item {
-    enum Kind { SUBMIT, WRITE_BUFFER, WRITE_TEXTURE, READ_BUFFER, READ_TEXTURE, FLUSH } kind = SUBMIT;
+    enum Kind { SUBMIT, WRITE_BUFFER, WRITE_TEXTURE, READ_BUFFER, READ_TEXTURE, READ_TEXTURES, FLUSH } kind = SUBMIT;
     uint64_t index = 0;
     std::vector<PassCmd> passes;
     std::shared_ptr<Buffer> buffer;
@@ -219,7 +219,12 @@ struct Item {
     uint32_t mip = 0;
     uint64_t offset = 0;
     std::vector<uint8_t> data;
+    void* staged = nullptr;  // writes: the caller's bytes already on the device (freed by the worker)
+    uint64_t staged_size = 0;
     gbr_texel_copy_buffer_layout layout{};
+    std::vector<std::shared_ptr<Texture>> textures;  // READ_TEXTURES: texture, mip, destination each
+    std::vector<uint32_t> mips;
+    std::vector<void*> dsts;
     void* dst = nullptr;
     uint64_t size = 0;
     std::promise<Failure>* done = nullptr;  // reads: completion for the blocked caller
@@ -287,12 +292,20 @@ struct DevBuf {
 
 struct Batch;
 
+constexpr size_t kLazyWakeItems = 1024;  // queued writes that wake the worker by themselves
+
 struct Device {
     gbr_device_config cfg{};
     int ordinal = 0;
     int num_sms = 0;
     int tile = 16, warps = 8;
     cudaStream_t stream = nullptr;
+    // Writes copy the caller's bytes to device staging at call time on copy_stream (not ordered
+    // with the queue; a pinned source moves at full DMA speed), and the worker applies them in
+    // queue order with a device-to-device copy.
+    cudaStream_t copy_stream = nullptr;
+    cudaMemPool_t staging_pool = nullptr;
+    std::mutex copy_mu;
 
     std::mutex obj_mu;
     uint64_t next_handle = 1;
@@ -311,7 +324,15 @@ struct Device {
 
     // worker-owned scratch
     uint64_t scratch_bytes = 0;
-    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf, slow_buf, strip_buf;
+    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf, slow_buf, strip_buf, upload_buf;
+    // coalesced small writes: double-buffered pinned staging, each free again once its event (the
+    // upload copy from it) has completed
+    struct PinnedStage {
+        uint8_t* ptr = nullptr;
+        size_t size = 0;
+        cudaEvent_t done = nullptr;
+    } pinned_stage[2];
+    int pinned_next = 0;
     uint32_t ovf_capacity = 4096;
     uint64_t bin_capacity = 1u << 22;
 
@@ -361,14 +382,19 @@ struct Device {
         std::lock_guard<std::mutex> lk(obj_mu);
         objects.erase(h);
     }
+    // Writes only need to be applied before whatever is queued after them, so they do not wake
+    // the worker: the next submission, read, poll or device destruction does, and the worker then
+    // takes the whole run of writes at once (and coalesces the small ones).
     void enqueue(Item&& it) {
         std::lock_guard<std::mutex> lk(q_mu);
         if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
+        const bool lazy = it.kind == Item::WRITE_BUFFER || it.kind == Item::WRITE_TEXTURE;
         queue.push_back(std::move(it));
-        q_cv.notify_all();
+        if (!lazy || queue.size() >= kLazyWakeItems) q_cv.notify_all();
     }
     void worker_main();
     void execute(Item& it);
+    void execute_writes(std::vector<Item>& items);
     void execute_group(std::vector<Item>& items);
     void note_failure(const Failure& f);
 };
@@ -682,6 +708,8 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
 // ---------------------------------------------------------------- worker
 uint64_t submission_estimate(const Item& it);
 constexpr size_t kMaxGroup = 256;  // submissions merged into one launch at most
+constexpr size_t kMaxCoalescedWrites = 4096;           // small buffer writes uploaded together at most
+constexpr uint64_t kMaxCoalescedBytes = 16ull << 20;  // and their bytes
 
 void Device::worker_main() {
     cudaSetDevice(ordinal);
@@ -695,6 +723,30 @@ void Device::worker_main() {
             queue.pop_front();
             // continuous batching: the submissions queued behind this one join its launch while
             // their expected transient memory fits the HBM budget (the rest wait for the next)
+            // a run of small host-side buffer writes (per-draw uniforms and the like) goes up as
+            // one copy and one scatter kernel, still in queue order
+            // (a write overlapping an earlier one of the run ends it: the scatter kernel places
+            // segments concurrently, and the later bytes must win)
+            if (group[0].kind == Item::WRITE_BUFFER && !group[0].staged) {
+                uint64_t bytes = group[0].data.size();
+                std::map<uint64_t, uint64_t> spans;  // destination [begin, end) of the run's writes
+                auto span_of = [](const Item& it) {
+                    const uint64_t b = reinterpret_cast<uint64_t>(it.buffer->ptr) + it.offset;
+                    return std::make_pair(b, b + it.data.size());
+                };
+                spans.insert(span_of(group[0]));
+                while (!queue.empty() && queue.front().kind == Item::WRITE_BUFFER && !queue.front().staged &&
+                       group.size() < kMaxCoalescedWrites && bytes + queue.front().data.size() <= kMaxCoalescedBytes) {
+                    const auto sp = span_of(queue.front());
+                    auto next = spans.lower_bound(sp.first);
+                    if (next != spans.end() && next->first < sp.second) break;
+                    if (next != spans.begin() && std::prev(next)->second > sp.first) break;
+                    spans.insert(sp);
+                    bytes += queue.front().data.size();
+                    group.push_back(std::move(queue.front()));
+                    queue.pop_front();
+                }
+            }
             if (group[0].kind == Item::SUBMIT && cfg.batch_submissions) {
                 const uint64_t budget = cfg.hbm_budget_bytes ? cfg.hbm_budget_bytes : (80ull << 30);
                 uint64_t est = submission_estimate(group[0]);
@@ -708,7 +760,50 @@ void Device::worker_main() {
             }
         }
         if (group[0].kind == Item::SUBMIT) execute_group(group);
+        else if (group.size() > 1) execute_writes(group);
         else execute(group[0]);
+    }
+}
+
+// Coalesced buffer writes: every segment copied into one pinned block (16-byte aligned offsets,
+// the segment table after them), one upload copy into device scratch, one scatter kernel.
+void Device::execute_writes(std::vector<Item>& items) {
+    try {
+        if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
+        const uint32_t n = (uint32_t)items.size();
+        uint64_t data_bytes = 0;
+        for (const Item& it : items) data_bytes += (it.data.size() + 15) & ~uint64_t(15);
+        const uint64_t total = data_bytes + (uint64_t)n * 3 * sizeof(uint64_t);
+        PinnedStage& ps = pinned_stage[pinned_next];
+        pinned_next ^= 1;
+        if (ps.done) cuda_check(cudaEventSynchronize(ps.done), "pinned staging reuse");
+        else cuda_check(cudaEventCreateWithFlags(&ps.done, cudaEventDisableTiming), "cudaEventCreate");
+        if (ps.size < total) {
+            if (ps.ptr) cudaFreeHost(ps.ptr);
+            ps.ptr = nullptr;
+            ps.size = 0;
+            const size_t want = std::max<size_t>(total, 1u << 20);
+            cuda_check(cudaHostAlloc(reinterpret_cast<void**>(&ps.ptr), want, cudaHostAllocDefault), "cudaHostAlloc");
+            ps.size = want;
+        }
+        upload_buf.ensure(total, &scratch_bytes);
+        uint64_t* desc = reinterpret_cast<uint64_t*>(ps.ptr + data_bytes);
+        uint64_t off = 0;
+        for (uint32_t k = 0; k < n; ++k) {
+            const Item& it = items[k];
+            std::memcpy(ps.ptr + off, it.data.data(), it.data.size());
+            desc[3 * k] = reinterpret_cast<uint64_t>(it.buffer->ptr + it.offset);
+            desc[3 * k + 1] = off;
+            desc[3 * k + 2] = it.data.size();
+            off += (it.data.size() + 15) & ~uint64_t(15);
+        }
+        cuda_check(cudaMemcpyAsync(upload_buf.ptr, ps.ptr, total, cudaMemcpyHostToDevice, stream), "coalesced writes");
+        cuda_check(cudaEventRecord(ps.done, stream), "cudaEventRecord");
+        const uint8_t* stage = static_cast<const uint8_t*>(upload_buf.ptr);
+        cuda_check(launch_scatter_writes(stage, reinterpret_cast<const uint64_t*>(stage + data_bytes), n, stream),
+                   "scatter writes");
+    } catch (const Failure& f) {
+        note_failure(f);
     }
 }
 
@@ -718,22 +813,37 @@ void Device::execute(Item& it) {
         if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
         switch (it.kind) {
             case Item::WRITE_BUFFER:
-                cuda_check(cudaMemcpyAsync(it.buffer->ptr + it.offset, it.data.data(), it.data.size(),
-                                           cudaMemcpyHostToDevice, stream),
-                           "write_buffer");
+                if (it.staged) {
+                    cuda_check(cudaMemcpyAsync(it.buffer->ptr + it.offset, it.staged, it.staged_size,
+                                               cudaMemcpyDeviceToDevice, stream),
+                               "write_buffer");
+                    cuda_check(cudaFreeAsync(it.staged, stream), "write_buffer staging");
+                    it.staged = nullptr;
+                } else {
+                    cuda_check(cudaMemcpyAsync(it.buffer->ptr + it.offset, it.data.data(), it.data.size(),
+                                               cudaMemcpyHostToDevice, stream),
+                               "write_buffer");
+                }
                 break;
             case Item::WRITE_TEXTURE: {
                 Texture& t = *it.texture;
                 uint32_t w = t.mip_w(it.mip), h = t.mip_h(it.mip), layers = t.layers();
                 uint64_t row = (uint64_t)w * t.bpp;
-                uint64_t src_row = it.layout.bytes_per_row ? it.layout.bytes_per_row : it.data.size();
+                const uint64_t src_size = it.staged ? it.staged_size : it.data.size();
+                uint64_t src_row = it.layout.bytes_per_row ? it.layout.bytes_per_row : src_size;
                 uint64_t rows_per_image = it.layout.rows_per_image ? it.layout.rows_per_image : h;
                 uint8_t* dst = t.ptr + t.mip_offset[it.mip];
+                const uint8_t* src = it.staged ? static_cast<const uint8_t*>(it.staged) : it.data.data();
                 for (uint32_t z = 0; z < layers; ++z)
                     cuda_check(cudaMemcpy2DAsync(dst + (uint64_t)z * h * row, row,
-                                                 it.data.data() + it.layout.offset + z * rows_per_image * src_row,
-                                                 src_row, row, h, cudaMemcpyHostToDevice, stream),
+                                                 src + it.layout.offset + z * rows_per_image * src_row, src_row, row,
+                                                 h, it.staged ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                                 stream),
                                "write_texture");
+                if (it.staged) {
+                    cuda_check(cudaFreeAsync(it.staged, stream), "write_texture staging");
+                    it.staged = nullptr;
+                }
                 break;
             }
             case Item::READ_BUFFER:
@@ -746,6 +856,15 @@ void Device::execute(Item& it) {
                                            it.texture->mip_bytes(it.mip), cudaMemcpyDeviceToHost, stream),
                            "texture_read");
                 cuda_check(cudaStreamSynchronize(stream), "texture_read sync");
+                break;
+            case Item::READ_TEXTURES:
+                for (size_t k = 0; k < it.textures.size(); ++k) {
+                    const Texture& t = *it.textures[k];
+                    cuda_check(cudaMemcpyAsync(it.dsts[k], t.ptr + t.mip_offset[it.mips[k]], t.mip_bytes(it.mips[k]),
+                                               cudaMemcpyDeviceToHost, stream),
+                               "textures_read");
+                }
+                cuda_check(cudaStreamSynchronize(stream), "textures_read sync");
                 break;
             case Item::FLUSH:
                 flush_buf.ensure(256ull << 20, &scratch_bytes);
@@ -1561,6 +1680,17 @@ GBR_API gbr_status gbr_device_create(const gbr_device_config* cfg, gbr_device* o
         if (cfg->raster_rule == GBR_RASTER_RULE_EDGE && cfg->profile != GBR_PROFILE_EXTENSION)
             fail(GBR_ERR_INVALID_ARGUMENT, "the edge-function raster rule belongs to the extension profile");
         cuda_check(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        cuda_check(cudaStreamCreateWithFlags(&d->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        {
+            cudaMemPoolProps props{};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = d->ordinal;
+            cuda_check(cudaMemPoolCreate(&d->staging_pool, &props), "cudaMemPoolCreate");
+            uint64_t keep = 1ull << 30;  // staging kept for reuse up to 1 GiB
+            cuda_check(cudaMemPoolSetAttribute(d->staging_pool, cudaMemPoolAttrReleaseThreshold, &keep),
+                       "cudaMemPoolSetAttribute");
+        }
         Device* raw = d.get();
         d->worker = std::thread([raw] { raw->worker_main(); });
         std::lock_guard<std::mutex> lk(g_dev_mu);
@@ -1603,7 +1733,17 @@ GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
         d->bins_buf.release();
         d->meta_buf.release();
         d->flush_buf.release();
+        cudaStreamSynchronize(d->stream);
+        d->upload_buf.release();
+        for (auto& ps : d->pinned_stage) {
+            if (ps.ptr) cudaFreeHost(ps.ptr);
+            if (ps.done) cudaEventDestroy(ps.done);
+            ps.ptr = nullptr;
+            ps.done = nullptr;
+        }
         cudaStreamDestroy(d->stream);
+        cudaStreamDestroy(d->copy_stream);
+        if (d->staging_pool) cudaMemPoolDestroy(d->staging_pool);
     })
 }
 
@@ -1639,6 +1779,23 @@ GBR_API gbr_status gbr_buffer_destroy(gbr_device dh, gbr_buffer b) {
         d->remove(b);
     })
 }
+// The caller's bytes on the device, copied now (the queue applies them later, in order); null
+// for small writes (a host copy costs less than a synchronised transfer) or when the staging
+// pool has no room, and the item then keeps a host copy instead.
+constexpr uint64_t kStageMinBytes = 256u << 10;
+void* stage_on_device(Device* d, const void* src, uint64_t n) {
+    if (n < kStageMinBytes) return nullptr;
+    std::lock_guard<std::mutex> lk(d->copy_mu);
+    void* p = nullptr;
+    if (cudaMallocFromPoolAsync(&p, n, d->staging_pool, d->copy_stream) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    cuda_check(cudaMemcpyAsync(p, src, n, cudaMemcpyHostToDevice, d->copy_stream), "write staging");
+    cuda_check(cudaStreamSynchronize(d->copy_stream), "write staging sync");
+    return p;
+}
+
 GBR_API gbr_status gbr_queue_write_buffer(gbr_device dh, gbr_buffer b, uint64_t offset, const void* data, uint64_t size) {
     GBR_TRY({
         auto d = get_device(dh);
@@ -1648,7 +1805,9 @@ GBR_API gbr_status gbr_queue_write_buffer(gbr_device dh, gbr_buffer b, uint64_t 
         if (offset + size > it.buffer->size) fail(GBR_ERR_VALIDATION, "write_buffer out of range");
         if (!size) return GBR_OK;
         it.offset = offset;
-        it.data.assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + size);
+        it.staged = stage_on_device(d.get(), data, size);
+        it.staged_size = size;
+        if (!it.staged) it.data.assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + size);
         d->enqueue(std::move(it));
     })
 }
@@ -1722,7 +1881,10 @@ GBR_API gbr_status gbr_queue_write_texture(gbr_device dh, gbr_texture th, uint32
         if (src_row < row) fail(GBR_ERR_VALIDATION, "bytes_per_row smaller than a texel row");
         uint64_t need = layout->offset + ((uint64_t)(t.layers() - 1) * rows_per_image + (t.mip_h(mip) - 1)) * src_row + row;
         if (need > data_size) fail(GBR_ERR_VALIDATION, "write_texture source out of range");
-        it.data.assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + data_size);
+        it.staged = stage_on_device(d.get(), data, data_size);
+        it.staged_size = data_size;
+        if (!it.staged)
+            it.data.assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + data_size);
         d->enqueue(std::move(it));
     })
 }
@@ -1736,6 +1898,31 @@ GBR_API gbr_status gbr_texture_read(gbr_device dh, gbr_texture th, uint32_t mip,
         if (size < it.texture->mip_bytes(mip)) fail(GBR_ERR_VALIDATION, "destination too small");
         it.mip = mip;
         it.dst = dst;
+        std::promise<Failure> done;
+        auto fut = done.get_future();
+        it.done = &done;
+        d->enqueue(std::move(it));
+        Failure f = fut.get();
+        if (f.status != GBR_OK) throw f;
+    })
+}
+GBR_API gbr_status gbr_textures_read(gbr_device dh, uint32_t count, const gbr_texture* textures, const uint32_t* mips,
+                                     void* const* dsts, const uint64_t* sizes) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        if (count && (!textures || !mips || !dsts || !sizes)) fail(GBR_ERR_INVALID_ARGUMENT, "null argument");
+        Item it;
+        it.kind = Item::READ_TEXTURES;
+        for (uint32_t k = 0; k < count; ++k) {
+            auto t = d->get<Texture>(textures[k], "texture");
+            if (mips[k] >= t->mips_stored) fail(GBR_ERR_VALIDATION, "mip level not stored");
+            if (sizes[k] < t->mip_bytes(mips[k])) fail(GBR_ERR_VALIDATION, "destination too small");
+            if (!dsts[k]) fail(GBR_ERR_INVALID_ARGUMENT, "null destination");
+            it.textures.push_back(std::move(t));
+            it.mips.push_back(mips[k]);
+            it.dsts.push_back(dsts[k]);
+        }
+        if (!count) return GBR_OK;
         std::promise<Failure> done;
         auto fut = done.get_future();
         it.done = &done;
@@ -2027,6 +2214,11 @@ GBR_API gbr_status gbr_queue_submit(gbr_device dh, const void* cmds, uint64_t le
 GBR_API gbr_status gbr_device_poll(gbr_device dh, uint32_t wait, uint32_t has_index, uint64_t index,
                                    uint64_t timeout_ns, uint32_t* out_status) {
     GBR_TRY({
+        {  // queued writes run now (they do not wake the worker themselves)
+            auto dq = get_device(dh);
+            std::lock_guard<std::mutex> lk(dq->q_mu);
+            if (!dq->queue.empty()) dq->q_cv.notify_all();
+        }
         auto d = get_device(dh);
         std::unique_lock<std::mutex> lk(d->q_mu);
         if (!wait) {

@@ -220,6 +220,7 @@ OPTIONAL = {
     "render_pipeline_eval_vertices": (i32, [u64, u64, u32, u32, P(C.c_float), P(u32)]),
     "wgsl_translate": (i32, [C.c_char_p, u64, C.c_char_p, C.c_char_p, C.c_char_p, u64, P(u64)]),
     "wgsl_compile_check": (i32, [C.c_char_p, u64, C.c_char_p, C.c_char_p, C.c_char_p, u64]),
+    "textures_read": (i32, [u64, u32, P(u64), P(u32), P(C.c_void_p), P(u64)]),
 }
 
 

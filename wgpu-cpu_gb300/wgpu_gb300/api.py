@@ -11,7 +11,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 from dataclasses import dataclass, field
-from typing import Optional, Sequence
+from typing import List, Optional, Sequence
 
 import numpy as np
 
@@ -457,8 +457,12 @@ class Queue:
         self.device = device
 
     def write_buffer(self, buffer: Buffer, offset: int, data) -> None:
-        arr = np.ascontiguousarray(np.frombuffer(memoryview(data).cast("B"), dtype=np.uint8))
         d = self.device
+        if isinstance(data, np.ndarray) and data.flags.c_contiguous:  # no copy, no view objects
+            _check(d.lib, d.lib.queue_write_buffer(d.handle, buffer.handle, offset,
+                                                   data.__array_interface__["data"][0], data.nbytes))
+            return
+        arr = np.ascontiguousarray(np.frombuffer(memoryview(data).cast("B"), dtype=np.uint8))
         _check(d.lib, d.lib.queue_write_buffer(d.handle, buffer.handle, offset, arr.ctypes.data, arr.nbytes))
 
     def write_texture(self, texture: Texture, data, bytes_per_row: int = 0, rows_per_image: int = 0,
@@ -664,6 +668,32 @@ class Device:
     def flush_caches(self) -> None:
         if self.lib.device_flush_caches is not None:
             _check(self.lib, self.lib.device_flush_caches(self.handle))
+
+    def read_textures_into(self, items) -> None:
+        """Reads several textures in one queue operation: items = [(texture, mip_level, address,
+        nbytes)], each destination at least the mip level's size (gbr_textures_read; one
+        gbr_texture_read per texture where the library lacks it)."""
+        items = list(items)
+        if not items:
+            return
+        if self.lib.textures_read is None:
+            for t, mip, ptr, n in items:
+                _check(self.lib, self.lib.texture_read(self.handle, t.handle, mip, ptr, n))
+            return
+        k = len(items)
+        hs = (C.c_uint64 * k)(*[t.handle for t, _, _, _ in items])
+        ms = (C.c_uint32 * k)(*[m for _, m, _, _ in items])
+        ps = (C.c_void_p * k)(*[p for _, _, p, _ in items])
+        ns = (C.c_uint64 * k)(*[n for _, _, _, n in items])
+        _check(self.lib, self.lib.textures_read(self.handle, k, hs, ms, ps, ns))
+
+    def read_textures(self, textures: Sequence[Texture], mip_level: int = 0) -> List[np.ndarray]:
+        outs = []
+        for t in textures:
+            w, h = t.mip_size(mip_level)
+            outs.append(np.empty((t.layers, h, w, BYTES_PER_TEXEL[t.format]), dtype=np.uint8))
+        self.read_textures_into([(t, mip_level, o.ctypes.data, o.nbytes) for t, o in zip(textures, outs)])
+        return [o[0] if t.layers == 1 else o for t, o in zip(textures, outs)]
 
     def read_texture(self, texture: Texture, mip_level: int = 0) -> np.ndarray:
         w, h = texture.mip_size(mip_level)
