@@ -351,13 +351,73 @@ enum gbr_opcode {
     GBR_OP_SET_BLEND_CONSTANT = 9, /* payload: gbr_cmd_set_blend_constant */
     GBR_OP_SET_STENCIL_REFERENCE = 10, /* payload: u32 + pad */
     GBR_OP_DRAW = 11,              /* payload: gbr_cmd_draw */
-    GBR_OP_DRAW_INDEXED = 12       /* payload: gbr_cmd_draw_indexed */
+    GBR_OP_DRAW_INDEXED = 12,      /* payload: gbr_cmd_draw_indexed */
+    /* Encoder commands outside render passes.  The reference leaves every one `todo!`
+     * (command.rs:37-115): the parity profile rejects them with GBR_ERR_UNSUPPORTED; the
+     * extension profile executes them with WebGPU semantics, in order with the passes. */
+    GBR_OP_COPY_BUFFER_TO_BUFFER = 13,   /* payload: gbr_cmd_copy_buffer_to_buffer */
+    GBR_OP_COPY_BUFFER_TO_TEXTURE = 14,  /* payload: gbr_cmd_copy_buffer_texture */
+    GBR_OP_COPY_TEXTURE_TO_BUFFER = 15,  /* payload: gbr_cmd_copy_buffer_texture */
+    GBR_OP_COPY_TEXTURE_TO_TEXTURE = 16, /* payload: gbr_cmd_copy_texture_to_texture */
+    GBR_OP_CLEAR_BUFFER = 17,            /* payload: gbr_cmd_clear_buffer */
+    GBR_OP_CLEAR_TEXTURE = 18            /* payload: gbr_cmd_clear_texture */
 };
 
 typedef struct gbr_cmd_header {
     uint32_t opcode;
     uint32_t payload_bytes;
 } gbr_cmd_header;
+
+/* CommandEncoderInterface::copy_buffer_to_buffer (command.rs:37-46).  Offsets and size are
+ * multiples of 4, source and destination differ; size = UINT64_MAX copies to the source's end. */
+typedef struct gbr_cmd_copy_buffer_to_buffer {
+    gbr_buffer source;
+    uint64_t source_offset;
+    gbr_buffer destination;
+    uint64_t destination_offset;
+    uint64_t size;
+} gbr_cmd_copy_buffer_to_buffer;
+
+/* wgpu::TexelCopyTextureInfo: a mip level of a texture and the texel origin (x, y, array layer). */
+typedef struct gbr_texel_copy_texture_info {
+    gbr_texture texture;
+    uint32_t mip_level;
+    uint32_t origin_x, origin_y, origin_z;
+} gbr_texel_copy_texture_info;
+
+/* copy_buffer_to_texture / copy_texture_to_buffer (command.rs:48-64): `size` texels per layer
+ * row/column/layer; the buffer side is laid out by `layout` (bytes_per_row a multiple of 256
+ * when the copy has more than one row, 0 = tightly packed single row; rows_per_image 0 = height). */
+typedef struct gbr_cmd_copy_buffer_texture {
+    gbr_buffer buffer;
+    gbr_texel_copy_buffer_layout layout;
+    gbr_texel_copy_texture_info texture;
+    gbr_extent3d size;
+    uint32_t _pad;
+} gbr_cmd_copy_buffer_texture;
+
+/* copy_texture_to_texture (command.rs:66-73): same format, different textures or ranges. */
+typedef struct gbr_cmd_copy_texture_to_texture {
+    gbr_texel_copy_texture_info source;
+    gbr_texel_copy_texture_info destination;
+    gbr_extent3d size;
+    uint32_t _pad;
+} gbr_cmd_copy_texture_to_texture;
+
+/* clear_buffer (command.rs:108-115): zeroes [offset, offset + size); size = UINT64_MAX to the end. */
+typedef struct gbr_cmd_clear_buffer {
+    gbr_buffer buffer;
+    uint64_t offset;
+    uint64_t size;
+} gbr_cmd_clear_buffer;
+
+/* clear_texture (command.rs:100-106): zeroes the mip levels and array layers of the subresource
+ * range (counts of 0 = all remaining). */
+typedef struct gbr_cmd_clear_texture {
+    gbr_texture texture;
+    uint32_t base_mip_level, mip_level_count;
+    uint32_t base_array_layer, array_layer_count;
+} gbr_cmd_clear_texture;
 
 typedef struct gbr_color_attachment {
     gbr_texture view;      /* texture (mip 0, layer `depth_slice`) */

@@ -966,6 +966,7 @@ static const T* payload(const gbr_cmd_header* h, const uint8_t* body) {
 struct DecodedPass {
     gbr_cmd_begin_render_pass begin;
     std::vector<std::pair<gbr_cmd_header, std::vector<uint8_t>>> cmds;
+    bool is_copy = false;  // an encoder copy / clear between passes: cmds holds that one record
 };
 
 static std::vector<DecodedPass> decode_stream(const uint8_t* data, uint64_t len) {
@@ -989,6 +990,12 @@ static std::vector<DecodedPass> decode_stream(const uint8_t* data, uint64_t len)
         } else if (h.opcode == GBR_OP_END_RENDER_PASS) {
             if (!cur) fail(GBR_ERR_INVALID_ARGUMENT, "end without begin");
             cur = nullptr;
+        } else if (h.opcode >= GBR_OP_COPY_BUFFER_TO_BUFFER && h.opcode <= GBR_OP_CLEAR_TEXTURE) {
+            if (cur) fail(GBR_ERR_INVALID_ARGUMENT, "command %u inside a render pass", h.opcode);
+            passes.emplace_back();
+            std::memset(&passes.back().begin, 0, sizeof passes.back().begin);
+            passes.back().is_copy = true;
+            passes.back().cmds.emplace_back(h, std::vector<uint8_t>(body, body + h.payload_bytes));
         } else {
             if (!cur) fail(GBR_ERR_INVALID_ARGUMENT, "command %u outside a render pass", h.opcode);
             cur->cmds.emplace_back(h, std::vector<uint8_t>(body, body + h.payload_bytes));
@@ -1409,6 +1416,120 @@ ORC_API gbr_status orc_bind_group_destroy(gbr_device d, gbr_bind_group g) {
 }
 // Submission executes immediately on the calling thread (the engine loop of engine.rs:26-46
 // without the thread hop).
+// Encoder copies and clears (extension profile; the reference has them as todo!,
+// command.rs:37-115), with WebGPU's validation rules, on the host copies of the resources.
+static void execute_copy(Device* dev, const gbr_cmd_header& h, const uint8_t* b) {
+    static const char* const kNames[] = {"copy_buffer_to_buffer", "copy_buffer_to_texture", "copy_texture_to_buffer",
+                                         "copy_texture_to_texture", "clear_buffer", "clear_texture"};
+    static const char* const kLines[] = {"37-46", "48-55", "57-64", "66-73", "108-115", "100-106"};
+    const uint32_t k = h.opcode - GBR_OP_COPY_BUFFER_TO_BUFFER;
+    if (dev->profile != GBR_PROFILE_EXTENSION)
+        fail(GBR_ERR_UNSUPPORTED, "%s is todo!() (command.rs:%s)", kNames[k], kLines[k]);
+    auto region_ok = [](const Texture* t, uint32_t mip, uint32_t x, uint32_t y, uint32_t z, const gbr_extent3d& e) {
+        const uint32_t layers = t->desc.size.depth_or_array_layers ? t->desc.size.depth_or_array_layers : 1;
+        if (mip >= t->mips_stored) fail(GBR_ERR_VALIDATION, "copy: mip level %u not stored", mip);
+        if ((uint64_t)x + e.width > t->mip_w(mip) || (uint64_t)y + e.height > t->mip_h(mip) ||
+            (uint64_t)z + e.depth_or_array_layers > layers)
+            fail(GBR_ERR_VALIDATION, "copy: texture region out of range");
+    };
+    auto texel = [](Texture* t, uint32_t mip, uint32_t x, uint32_t y, uint32_t z) {
+        return t->mips[mip].data() + (((size_t)z * t->mip_h(mip) + y) * t->mip_w(mip) + x) * t->bpp;
+    };
+    switch (h.opcode) {
+        case GBR_OP_COPY_BUFFER_TO_BUFFER: {
+            auto* p = payload<gbr_cmd_copy_buffer_to_buffer>(&h, b);
+            Buffer* src = dev->get<Buffer>(p->source, "buffer");
+            Buffer* dst = dev->get<Buffer>(p->destination, "buffer");
+            const uint64_t size = p->size == UINT64_MAX ? src->data.size() - std::min<uint64_t>(p->source_offset,
+                                                                                              src->data.size())
+                                                        : p->size;
+            if (src == dst) fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: source and destination are the same buffer");
+            if (p->source_offset % 4 || p->destination_offset % 4 || size % 4)
+                fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: alignment");
+            if (p->source_offset + size > src->data.size() || p->destination_offset + size > dst->data.size())
+                fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: range out of bounds");
+            std::memcpy(dst->data.data() + p->destination_offset, src->data.data() + p->source_offset, size);
+            break;
+        }
+        case GBR_OP_COPY_BUFFER_TO_TEXTURE:
+        case GBR_OP_COPY_TEXTURE_TO_BUFFER: {
+            auto* p = payload<gbr_cmd_copy_buffer_texture>(&h, b);
+            Buffer* buf = dev->get<Buffer>(p->buffer, "buffer");
+            Texture* t = dev->get<Texture>(p->texture.texture, "texture");
+            const gbr_extent3d e = p->size;
+            region_ok(t, p->texture.mip_level, p->texture.origin_x, p->texture.origin_y, p->texture.origin_z, e);
+            const uint64_t width = (uint64_t)e.width * t->bpp;
+            const uint64_t bpr = p->layout.bytes_per_row ? p->layout.bytes_per_row : width;
+            const uint64_t rpi = p->layout.rows_per_image ? p->layout.rows_per_image : e.height;
+            if ((e.height > 1 || e.depth_or_array_layers > 1) && (p->layout.bytes_per_row % 256 || !p->layout.bytes_per_row))
+                fail(GBR_ERR_VALIDATION, "%s: bytes_per_row must be a multiple of 256", kNames[k]);
+            if (bpr < width || rpi < e.height) fail(GBR_ERR_VALIDATION, "%s: layout smaller than the copy", kNames[k]);
+            if (p->layout.offset % t->bpp) fail(GBR_ERR_VALIDATION, "%s: offset not a multiple of the texel size", kNames[k]);
+            if (!e.width || !e.height || !e.depth_or_array_layers) break;
+            const uint64_t need = p->layout.offset + ((uint64_t)(e.depth_or_array_layers - 1) * rpi + (e.height - 1)) * bpr + width;
+            if (need > buf->data.size()) fail(GBR_ERR_VALIDATION, "%s: buffer range out of bounds", kNames[k]);
+            for (uint32_t z = 0; z < e.depth_or_array_layers; ++z)
+                for (uint32_t y = 0; y < e.height; ++y) {
+                    uint8_t* tp = texel(t, p->texture.mip_level, p->texture.origin_x, p->texture.origin_y + y,
+                                        p->texture.origin_z + z);
+                    uint8_t* bp = buf->data.data() + p->layout.offset + (z * rpi + y) * bpr;
+                    if (h.opcode == GBR_OP_COPY_BUFFER_TO_TEXTURE) std::memcpy(tp, bp, width);
+                    else std::memcpy(bp, tp, width);
+                }
+            break;
+        }
+        case GBR_OP_COPY_TEXTURE_TO_TEXTURE: {
+            auto* p = payload<gbr_cmd_copy_texture_to_texture>(&h, b);
+            Texture* a = dev->get<Texture>(p->source.texture, "texture");
+            Texture* c = dev->get<Texture>(p->destination.texture, "texture");
+            const gbr_extent3d e = p->size;
+            if (a->desc.format != c->desc.format) fail(GBR_ERR_VALIDATION, "copy_texture_to_texture: formats differ");
+            region_ok(a, p->source.mip_level, p->source.origin_x, p->source.origin_y, p->source.origin_z, e);
+            region_ok(c, p->destination.mip_level, p->destination.origin_x, p->destination.origin_y,
+                      p->destination.origin_z, e);
+            if (a == c && p->source.mip_level == p->destination.mip_level &&
+                p->source.origin_z < p->destination.origin_z + e.depth_or_array_layers &&
+                p->destination.origin_z < p->source.origin_z + e.depth_or_array_layers)
+                fail(GBR_ERR_VALIDATION, "copy_texture_to_texture: source and destination overlap");
+            for (uint32_t z = 0; z < e.depth_or_array_layers; ++z)
+                for (uint32_t y = 0; y < e.height; ++y)
+                    std::memcpy(texel(c, p->destination.mip_level, p->destination.origin_x, p->destination.origin_y + y,
+                                      p->destination.origin_z + z),
+                                texel(a, p->source.mip_level, p->source.origin_x, p->source.origin_y + y,
+                                      p->source.origin_z + z),
+                                (size_t)e.width * a->bpp);
+            break;
+        }
+        case GBR_OP_CLEAR_BUFFER: {
+            auto* p = payload<gbr_cmd_clear_buffer>(&h, b);
+            Buffer* buf = dev->get<Buffer>(p->buffer, "buffer");
+            const uint64_t size = p->size == UINT64_MAX ? buf->data.size() - std::min<uint64_t>(p->offset, buf->data.size())
+                                                        : p->size;
+            if (p->offset % 4 || size % 4) fail(GBR_ERR_VALIDATION, "clear_buffer: alignment");
+            if (p->offset + size > buf->data.size()) fail(GBR_ERR_VALIDATION, "clear_buffer: range out of bounds");
+            std::memset(buf->data.data() + p->offset, 0, size);
+            break;
+        }
+        case GBR_OP_CLEAR_TEXTURE: {
+            auto* p = payload<gbr_cmd_clear_texture>(&h, b);
+            Texture* t = dev->get<Texture>(p->texture, "texture");
+            const uint32_t layers = t->desc.size.depth_or_array_layers ? t->desc.size.depth_or_array_layers : 1;
+            if (p->base_mip_level >= t->mips_stored || p->base_array_layer >= layers)
+                fail(GBR_ERR_VALIDATION, "clear_texture: subresource range out of range");
+            const uint32_t mc = p->mip_level_count ? p->mip_level_count : t->mips_stored - p->base_mip_level;
+            const uint32_t lc = p->array_layer_count ? p->array_layer_count : layers - p->base_array_layer;
+            if ((uint64_t)p->base_mip_level + mc > t->mips_stored || (uint64_t)p->base_array_layer + lc > layers)
+                fail(GBR_ERR_VALIDATION, "clear_texture: subresource range out of range");
+            for (uint32_t m = p->base_mip_level; m < p->base_mip_level + mc; ++m) {
+                const size_t layer = (size_t)t->mip_w(m) * t->mip_h(m) * t->bpp;
+                std::memset(t->mips[m].data() + p->base_array_layer * layer, 0, lc * layer);
+            }
+            break;
+        }
+        default: break;
+    }
+}
+
 ORC_API gbr_status orc_queue_submit(gbr_device d, const void* cmds, uint64_t len, uint64_t* out_index) {
     ORC_TRY({
         Device* dev = get_device(d);
@@ -1418,6 +1539,10 @@ ORC_API gbr_status orc_queue_submit(gbr_device d, const void* cmds, uint64_t len
         Counters total;
         uint64_t draws = 0;
         for (const auto& p : passes) {
+            if (p.is_copy) {
+                execute_copy(dev, p.cmds[0].first, p.cmds[0].second.data());
+                continue;
+            }
             for (const auto& c : p.cmds)
                 if (c.first.opcode == GBR_OP_DRAW || c.first.opcode == GBR_OP_DRAW_INDEXED) ++draws;
             execute_pass(dev, p, total);

@@ -272,3 +272,50 @@ def coverage_counts(dev, width, height, tris_px):
     dev.poll(True, sub)
     img = dev.read_texture(color).view(np.float16).astype(np.float32)
     return img[..., 0].astype(np.int64), dev.submission_stats(sub).fragments_shaded
+
+
+def copy_scenario(dev, seed=5):
+    """Encoder copies and clears (extension profile) between and around render passes.  Returns
+    the initial data and every resource the commands touched, read back:
+      A (4096 B) -> B: copy A[256:1280] to B[512:1536], clear B[0:64];
+      A -> T1 mip 0 layer 1 at (5, 3), 16 x 8 texels, 256-byte rows;
+      T1 mip 1 layer 0 (2, 1) 10 x 6 -> T2 mip 1 layer 1 (20, 10); clear T2 mip 2, all layers;
+      T1 mip 0 layer 1 (5, 3) 16 x 8 -> C at 0, 256-byte rows;
+      render a sphere into X, copy X to Y, render X again cleared to red (Y keeps the first frame)."""
+    rng = np.random.default_rng(seed)
+    a_data = rng.integers(0, 256, 4096, dtype=np.uint8)
+    A = dev.create_buffer_init(a_data)
+    B = dev.create_buffer_init(np.zeros(4096, np.uint8))
+    C = dev.create_buffer_init(np.zeros(4096, np.uint8))
+    f = W.TextureFormat.RGBA8_UNORM
+    t1_levels = [rng.integers(0, 256, (2, 32 >> m, 64 >> m, 4), dtype=np.uint8) for m in range(3)]
+    t2_levels = [rng.integers(0, 256, (2, 32 >> m, 64 >> m, 4), dtype=np.uint8) for m in range(3)]
+    T1 = dev.create_texture(64, 32, f, mip_level_count=3, layers=2)
+    T2 = dev.create_texture(64, 32, f, mip_level_count=3, layers=2)
+    for m in range(3):
+        dev.queue.write_texture(T1, t1_levels[m], mip_level=m)
+        dev.queue.write_texture(T2, t2_levels[m], mip_level=m)
+    enc = dev.create_command_encoder()
+    enc.copy_buffer_to_buffer(A, 256, B, 512, 1024)
+    enc.clear_buffer(B, 0, 64)
+    enc.copy_buffer_to_texture(A, 0, 256, 8, T1, (16, 8, 1), mip_level=0, origin=(5, 3, 1))
+    enc.copy_texture_to_texture(T1, T2, (10, 6, 1), source_mip=1, source_origin=(2, 1, 0), destination_mip=1,
+                                destination_origin=(20, 10, 1))
+    enc.clear_texture(T2, base_mip_level=2)
+    enc.copy_texture_to_buffer(T1, C, 0, 256, 8, (16, 8, 1), mip_level=0, origin=(5, 3, 1))
+    dev.poll(True, dev.queue.submit([enc.finish()]))
+
+    s = wl.scene_colored_sphere(dev, 64, 64)
+    Y = dev.create_texture(64, 64, W.TextureFormat.RGBA8_UNORM)
+    enc = dev.create_command_encoder()
+    s.record(enc)
+    enc.copy_texture_to_texture(s.color, Y, (64, 64, 1))
+    rp = enc.begin_render_pass([W.RenderPassColorAttachment(s.color, (1.0, 0.0, 0.0, 1.0))], None)
+    rp.end()
+    dev.poll(True, dev.queue.submit([enc.finish()]))
+    return {
+        "a": a_data, "t1_init": t1_levels, "t2_init": t2_levels,
+        "B": np.frombuffer(B.read(), np.uint8), "C": np.frombuffer(C.read(), np.uint8),
+        "T1": [dev.read_texture(T1, m) for m in range(3)], "T2": [dev.read_texture(T2, m) for m in range(3)],
+        "X": dev.read_texture(s.color), "Y": dev.read_texture(Y),
+    }

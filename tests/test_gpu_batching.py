@@ -76,7 +76,7 @@ def test_autotuned_tiles_match_oracle(oracle_result):
     dev = W.Device()
     try:
         s = wl.scene_batched(dev, **SMALL)
-        for rep in range(5):
+        for rep in range(7):  # the five candidate shapes, then the chosen one
             idx = s.render()
             out = [(dev.read_texture(c), dev.read_texture(d)) for c, d, _ in s.passes]
             assert_targets_same((out, dev.submission_stats(idx).fragments_shaded), oracle_result, f"autotune rep {rep}")

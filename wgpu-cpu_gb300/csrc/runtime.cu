@@ -201,7 +201,22 @@ struct DrawCmd {
     uint32_t scissor[4] = {};
     double blend_constant[4] = {};
 };
+// An encoder command outside render passes (extension profile): a copy or a clear, resolved and
+// validated at submit.  Texture regions are (mip, origin x/y/layer) with an extent.
+struct CopyCmd {
+    uint32_t op = 0;  // gbr_opcode
+    std::shared_ptr<Buffer> buf, buf2;
+    std::shared_ptr<Texture> tex, tex2;
+    uint64_t off = 0, off2 = 0, size = 0;
+    gbr_texel_copy_buffer_layout layout{};
+    uint32_t mip = 0, mip2 = 0;
+    uint32_t ox = 0, oy = 0, oz = 0, ox2 = 0, oy2 = 0, oz2 = 0;
+    gbr_extent3d ext{};
+    uint32_t mip_count = 0, layer_count = 0;
+};
+
 struct PassCmd {
+    std::shared_ptr<CopyCmd> copy;  // set: this entry is a copy or clear, not a render pass
     gbr_cmd_begin_render_pass begin{};
     std::shared_ptr<Texture> color;
     std::shared_ptr<Texture> depth;
@@ -423,6 +438,7 @@ struct Batch {
     bool single_item = true;
     bool lines = false;        // one line / point draw, drawn by k_lines_points
     std::shared_ptr<JitKernels> jit;  // the WGSL module whose kernels run this batch (or none)
+    std::shared_ptr<CopyCmd> copy;    // a copy or clear between passes (no draws, no targets)
 };
 
 // Visibility raster (kind 3): every target has colour and depth, and every draw writes depth
@@ -470,9 +486,12 @@ int fragment_kind(const Batch& b, bool allow_visibility) {
 
 // Tile shapes (side, warps per tile) the autotuner tries, all compiled into kernels.cu: for the
 // ordered kernels, and for the visibility raster (which favours fewer warps per tile).
-const int kTuneCands[][2] = {{16, 8}, {32, 8}, {32, 4}};
-const int kTuneCandsVis[][2] = {{16, 2}, {16, 4}, {32, 4}};
-constexpr int kNumTuneCands = 3;
+// The first is the shape used before any measurement.  The tuner times the raster kernel, so it
+// sweeps 16- and 32-pixel tiles (binning costs the same or less there) and warps per tile; 8x8
+// tiles, whose four-fold bins the raster time does not show, are chosen through the config.
+const int kTuneCands[][2] = {{16, 8}, {32, 8}, {32, 4}, {16, 4}, {16, 2}};
+const int kTuneCandsVis[][2] = {{16, 2}, {16, 4}, {32, 4}, {16, 1}, {32, 2}};
+constexpr int kNumTuneCands = 5;
 
 uint64_t log2_bucket(uint64_t v) {
     uint64_t r = 0;
@@ -1005,6 +1024,7 @@ bool Device::merge_batch(Batch& into, Batch& b) {
     const uint64_t kMaxPrims = (1ull << (32 - SUBTRI_BITS)) - 1;
     if ((uint64_t)into.total_prims + b.total_prims > kMaxPrims) return false;
     if (into.jit && b.jit && into.jit != b.jit) return false;
+    if (into.copy || b.copy) return false;
     if (into.lines || b.lines) return false;
     if (!into.jit) into.jit = b.jit;
     const uint32_t tbase = (uint32_t)into.targets.size();
@@ -1084,6 +1104,11 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
         return batches.back();
     };
     for (const PassCmd& p : passes) {
+        if (p.copy) {  // ordered between the passes around it: closes the open batch
+            open = false;
+            new_batch().copy = p.copy;
+            continue;
+        }
         if (p.width == 0 || p.height == 0) continue;
         std::vector<const Texture*> p_write, p_read;
         if (p.color) p_write.push_back(p.color.get());
@@ -1185,6 +1210,63 @@ std::vector<Batch> Device::plan_batches(const std::vector<PassCmd>& passes, uint
 // the autotuner), tile layout, descriptors and per-target fragment counters; re-runs from a
 // batch that ran out of scratch space after growing it.  Returns the first batch that failed
 // validation on the device (batches before it completed), or batches.size().
+// Stream-ordered execution of a copy or clear (extension profile).  Textures store mip m at
+// mip_offset[m], its layers back to back, rows tightly packed.
+void execute_copy(const CopyCmd& c, cudaStream_t s) {
+    auto texel = [](const Texture& t, uint32_t mip, uint32_t x, uint32_t y, uint32_t z) {
+        const uint64_t row = (uint64_t)t.mip_w(mip) * t.bpp;
+        return t.ptr + t.mip_offset[mip] + ((uint64_t)z * t.mip_h(mip) + y) * row + (uint64_t)x * t.bpp;
+    };
+    switch (c.op) {
+        case GBR_OP_COPY_BUFFER_TO_BUFFER:
+            cuda_check(cudaMemcpyAsync(c.buf2->ptr + c.off2, c.buf->ptr + c.off, c.size, cudaMemcpyDeviceToDevice, s),
+                       "copy_buffer_to_buffer");
+            break;
+        case GBR_OP_COPY_BUFFER_TO_TEXTURE:
+        case GBR_OP_COPY_TEXTURE_TO_BUFFER: {
+            const Texture& t = *c.tex;
+            const uint64_t width = (uint64_t)c.ext.width * t.bpp;
+            const uint64_t bpr = c.layout.bytes_per_row ? c.layout.bytes_per_row : width;
+            const uint64_t rpi = c.layout.rows_per_image ? c.layout.rows_per_image : c.ext.height;
+            const uint64_t trow = (uint64_t)t.mip_w(c.mip) * t.bpp;
+            for (uint32_t z = 0; z < c.ext.depth_or_array_layers; ++z) {
+                uint8_t* tp = texel(t, c.mip, c.ox, c.oy, c.oz + z);
+                uint8_t* bp = c.buf->ptr + c.layout.offset + z * rpi * bpr;
+                if (c.op == GBR_OP_COPY_BUFFER_TO_TEXTURE)
+                    cuda_check(cudaMemcpy2DAsync(tp, trow, bp, bpr, width, c.ext.height, cudaMemcpyDeviceToDevice, s),
+                               "copy_buffer_to_texture");
+                else
+                    cuda_check(cudaMemcpy2DAsync(bp, bpr, tp, trow, width, c.ext.height, cudaMemcpyDeviceToDevice, s),
+                               "copy_texture_to_buffer");
+            }
+            break;
+        }
+        case GBR_OP_COPY_TEXTURE_TO_TEXTURE: {
+            const Texture &a = *c.tex, &b = *c.tex2;
+            const uint64_t width = (uint64_t)c.ext.width * a.bpp;
+            for (uint32_t z = 0; z < c.ext.depth_or_array_layers; ++z)
+                cuda_check(cudaMemcpy2DAsync(texel(b, c.mip2, c.ox2, c.oy2, c.oz2 + z), (uint64_t)b.mip_w(c.mip2) * b.bpp,
+                                             texel(a, c.mip, c.ox, c.oy, c.oz + z), (uint64_t)a.mip_w(c.mip) * a.bpp,
+                                             width, c.ext.height, cudaMemcpyDeviceToDevice, s),
+                           "copy_texture_to_texture");
+            break;
+        }
+        case GBR_OP_CLEAR_BUFFER:
+            cuda_check(cudaMemsetAsync(c.buf->ptr + c.off, 0, c.size, s), "clear_buffer");
+            break;
+        case GBR_OP_CLEAR_TEXTURE: {
+            const Texture& t = *c.tex;
+            for (uint32_t m = c.mip; m < c.mip + c.mip_count; ++m) {
+                const uint64_t layer = (uint64_t)t.mip_w(m) * t.mip_h(m) * t.bpp;
+                cuda_check(cudaMemsetAsync(t.ptr + t.mip_offset[m] + c.oz * layer, 0, c.layer_count * layer, s),
+                           "clear_texture");
+            }
+            break;
+        }
+        default: fail(GBR_ERR_INVALID_ARGUMENT, "copy opcode %u", c.op);
+    }
+}
+
 RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun& run) {
     const size_t nb = batches.size();
     std::vector<int> btile(nb, tile), bwarps(nb, warps), tuning(nb, -1);
@@ -1332,6 +1414,13 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                     bp.vis_compare = visibility_compare(b);
                 }
                 cudaEvent_t* ev = revp->empty() ? nullptr : &(*revp)[2 * i];
+                if (b.copy) {
+                    cuda_check(cudaMemsetAsync(bp.status, 0, sizeof(BatchStatus), stream), "status");
+                    if (ev) cuda_check(cudaEventRecord(ev[0], stream), "event");
+                    execute_copy(*b.copy, stream);
+                    if (ev) cuda_check(cudaEventRecord(ev[1], stream), "event");
+                    continue;
+                }
                 if (b.lines)
                     cuda_check(b.jit ? launch_lines_jit(*b.jit, bp, num_sms, stream, &run.launches, ev)
                                      : launch_lines(bp, num_sms, stream, &run.launches, ev),
@@ -1343,7 +1432,9 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                                "launch");
             }
         };
-        if (cfg.use_graphs && attempt == 0 && !any_tuning) {
+        bool any_copy = false;  // a captured graph would keep a copy's addresses: no graphs then
+        for (size_t i = from; i < nb; ++i) any_copy = any_copy || (bool)batches[i].copy;
+        if (cfg.use_graphs && attempt == 0 && !any_tuning && !any_copy) {
             // key: every launch parameter of the sequence (descriptors are re-uploaded each time)
             std::string key;
             auto put = [&](const void* p, size_t len) { key.append(static_cast<const char*>(p), len); };
@@ -1474,6 +1565,110 @@ const T* payload(const gbr_cmd_header& h, const uint8_t* body) {
     return reinterpret_cast<const T*>(body);
 }
 
+// A texture region of a copy: mip level stored, origin + extent inside it.
+void check_region(const Texture& t, uint32_t mip, uint32_t x, uint32_t y, uint32_t z, const gbr_extent3d& e) {
+    if (mip >= t.mips_stored) fail(GBR_ERR_VALIDATION, "copy: mip level %u not stored", mip);
+    if ((uint64_t)x + e.width > t.mip_w(mip) || (uint64_t)y + e.height > t.mip_h(mip) ||
+        (uint64_t)z + e.depth_or_array_layers > t.layers())
+        fail(GBR_ERR_VALIDATION, "copy: texture region out of range");
+}
+
+CopyCmd decode_copy(Device& dev, const gbr_cmd_header& h, const uint8_t* b) {
+    static const char* const kNames[] = {"copy_buffer_to_buffer", "copy_buffer_to_texture", "copy_texture_to_buffer",
+                                         "copy_texture_to_texture", "clear_buffer", "clear_texture"};
+    static const char* const kLines[] = {"37-46", "48-55", "57-64", "66-73", "108-115", "100-106"};
+    const uint32_t k = h.opcode - GBR_OP_COPY_BUFFER_TO_BUFFER;
+    if (dev.cfg.profile != GBR_PROFILE_EXTENSION)
+        fail(GBR_ERR_UNSUPPORTED, "%s is todo!() (command.rs:%s)", kNames[k], kLines[k]);
+    CopyCmd c;
+    c.op = h.opcode;
+    switch (h.opcode) {
+        case GBR_OP_COPY_BUFFER_TO_BUFFER: {
+            auto* p = payload<gbr_cmd_copy_buffer_to_buffer>(h, b);
+            c.buf = dev.get<Buffer>(p->source, "buffer");
+            c.buf2 = dev.get<Buffer>(p->destination, "buffer");
+            c.off = p->source_offset;
+            c.off2 = p->destination_offset;
+            c.size = p->size == UINT64_MAX ? c.buf->size - std::min(c.off, c.buf->size) : p->size;
+            if (c.buf == c.buf2) fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: source and destination are the same buffer");
+            if (c.off % 4 || c.off2 % 4 || c.size % 4) fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: alignment");
+            if (c.off + c.size > c.buf->size || c.off2 + c.size > c.buf2->size)
+                fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: range out of bounds");
+            break;
+        }
+        case GBR_OP_COPY_BUFFER_TO_TEXTURE:
+        case GBR_OP_COPY_TEXTURE_TO_BUFFER: {
+            auto* p = payload<gbr_cmd_copy_buffer_texture>(h, b);
+            c.buf = dev.get<Buffer>(p->buffer, "buffer");
+            c.tex = dev.get<Texture>(p->texture.texture, "texture");
+            c.layout = p->layout;
+            c.mip = p->texture.mip_level;
+            c.ox = p->texture.origin_x;
+            c.oy = p->texture.origin_y;
+            c.oz = p->texture.origin_z;
+            c.ext = p->size;
+            check_region(*c.tex, c.mip, c.ox, c.oy, c.oz, c.ext);
+            const uint64_t width = (uint64_t)c.ext.width * c.tex->bpp;
+            const uint64_t bpr = c.layout.bytes_per_row ? c.layout.bytes_per_row : width;
+            const uint64_t rpi = c.layout.rows_per_image ? c.layout.rows_per_image : c.ext.height;
+            if ((c.ext.height > 1 || c.ext.depth_or_array_layers > 1) && (c.layout.bytes_per_row % 256 || !c.layout.bytes_per_row))
+                fail(GBR_ERR_VALIDATION, "%s: bytes_per_row must be a multiple of 256", kNames[k]);
+            if (bpr < width || rpi < c.ext.height) fail(GBR_ERR_VALIDATION, "%s: layout smaller than the copy", kNames[k]);
+            if (c.layout.offset % c.tex->bpp) fail(GBR_ERR_VALIDATION, "%s: offset not a multiple of the texel size", kNames[k]);
+            if (c.ext.width && c.ext.height && c.ext.depth_or_array_layers) {
+                const uint64_t need = c.layout.offset + ((uint64_t)(c.ext.depth_or_array_layers - 1) * rpi +
+                                                         (c.ext.height - 1)) * bpr + width;
+                if (need > c.buf->size) fail(GBR_ERR_VALIDATION, "%s: buffer range out of bounds", kNames[k]);
+            }
+            break;
+        }
+        case GBR_OP_COPY_TEXTURE_TO_TEXTURE: {
+            auto* p = payload<gbr_cmd_copy_texture_to_texture>(h, b);
+            c.tex = dev.get<Texture>(p->source.texture, "texture");
+            c.tex2 = dev.get<Texture>(p->destination.texture, "texture");
+            c.mip = p->source.mip_level;
+            c.ox = p->source.origin_x;
+            c.oy = p->source.origin_y;
+            c.oz = p->source.origin_z;
+            c.mip2 = p->destination.mip_level;
+            c.ox2 = p->destination.origin_x;
+            c.oy2 = p->destination.origin_y;
+            c.oz2 = p->destination.origin_z;
+            c.ext = p->size;
+            if (c.tex->desc.format != c.tex2->desc.format) fail(GBR_ERR_VALIDATION, "copy_texture_to_texture: formats differ");
+            check_region(*c.tex, c.mip, c.ox, c.oy, c.oz, c.ext);
+            check_region(*c.tex2, c.mip2, c.ox2, c.oy2, c.oz2, c.ext);
+            if (c.tex == c.tex2 && c.mip == c.mip2 &&
+                c.oz < c.oz2 + c.ext.depth_or_array_layers && c.oz2 < c.oz + c.ext.depth_or_array_layers)
+                fail(GBR_ERR_VALIDATION, "copy_texture_to_texture: source and destination overlap");
+            break;
+        }
+        case GBR_OP_CLEAR_BUFFER: {
+            auto* p = payload<gbr_cmd_clear_buffer>(h, b);
+            c.buf = dev.get<Buffer>(p->buffer, "buffer");
+            c.off = p->offset;
+            c.size = p->size == UINT64_MAX ? c.buf->size - std::min(c.off, c.buf->size) : p->size;
+            if (c.off % 4 || c.size % 4) fail(GBR_ERR_VALIDATION, "clear_buffer: alignment");
+            if (c.off + c.size > c.buf->size) fail(GBR_ERR_VALIDATION, "clear_buffer: range out of bounds");
+            break;
+        }
+        case GBR_OP_CLEAR_TEXTURE: {
+            auto* p = payload<gbr_cmd_clear_texture>(h, b);
+            c.tex = dev.get<Texture>(p->texture, "texture");
+            c.mip = p->base_mip_level;
+            c.oz = p->base_array_layer;
+            if (c.mip >= c.tex->mips_stored || c.oz >= c.tex->layers())
+                fail(GBR_ERR_VALIDATION, "clear_texture: subresource range out of range");
+            c.mip_count = p->mip_level_count ? p->mip_level_count : c.tex->mips_stored - c.mip;
+            c.layer_count = p->array_layer_count ? p->array_layer_count : c.tex->layers() - c.oz;
+            if ((uint64_t)c.mip + c.mip_count > c.tex->mips_stored || (uint64_t)c.oz + c.layer_count > c.tex->layers())
+                fail(GBR_ERR_VALIDATION, "clear_texture: subresource range out of range");
+            break;
+        }
+    }
+    return c;
+}
+
 std::vector<PassCmd> decode(Device& dev, const uint8_t* data, uint64_t len) {
     std::vector<PassCmd> passes;
     uint64_t off = 0;
@@ -1532,6 +1727,12 @@ std::vector<PassCmd> decode(Device& dev, const uint8_t* data, uint64_t len) {
         if (h.opcode == GBR_OP_END_RENDER_PASS) {
             if (!cur) fail(GBR_ERR_INVALID_ARGUMENT, "end without begin");
             cur = nullptr;
+            continue;
+        }
+        if (h.opcode >= GBR_OP_COPY_BUFFER_TO_BUFFER && h.opcode <= GBR_OP_CLEAR_TEXTURE) {
+            if (cur) fail(GBR_ERR_INVALID_ARGUMENT, "command %u inside a render pass", h.opcode);
+            passes.emplace_back();
+            passes.back().copy = std::make_shared<CopyCmd>(decode_copy(dev, h, b));
             continue;
         }
         if (!cur) fail(GBR_ERR_INVALID_ARGUMENT, "command %u outside a render pass", h.opcode);

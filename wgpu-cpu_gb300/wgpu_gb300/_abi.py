@@ -43,6 +43,12 @@ OP_SET_BLEND_CONSTANT = 9
 OP_SET_STENCIL_REFERENCE = 10
 OP_DRAW = 11
 OP_DRAW_INDEXED = 12
+OP_COPY_BUFFER_TO_BUFFER = 13
+OP_COPY_BUFFER_TO_TEXTURE = 14
+OP_COPY_TEXTURE_TO_BUFFER = 15
+OP_COPY_TEXTURE_TO_TEXTURE = 16
+OP_CLEAR_BUFFER = 17
+OP_CLEAR_TEXTURE = 18
 
 u32, u64, i32, f32, f64 = C.c_uint32, C.c_uint64, C.c_int32, C.c_float, C.c_double
 
@@ -184,6 +190,34 @@ class CmdDraw(C.Structure):
 class CmdDrawIndexed(C.Structure):
     _fields_ = [("index_start", u32), ("index_end", u32), ("base_vertex", i32), ("instance_start", u32),
                 ("instance_end", u32), ("_pad", u32)]
+
+
+class CmdCopyBufferToBuffer(C.Structure):
+    _fields_ = [("source", u64), ("source_offset", u64), ("destination", u64), ("destination_offset", u64),
+                ("size", u64)]
+
+
+class TexelCopyTextureInfo(C.Structure):
+    _fields_ = [("texture", u64), ("mip_level", u32), ("origin_x", u32), ("origin_y", u32), ("origin_z", u32)]
+
+
+class CmdCopyBufferTexture(C.Structure):
+    _fields_ = [("buffer", u64), ("layout", TexelCopyBufferLayout), ("texture", TexelCopyTextureInfo),
+                ("size", Extent3d), ("_pad", u32)]
+
+
+class CmdCopyTextureToTexture(C.Structure):
+    _fields_ = [("source", TexelCopyTextureInfo), ("destination", TexelCopyTextureInfo), ("size", Extent3d),
+                ("_pad", u32)]
+
+
+class CmdClearBuffer(C.Structure):
+    _fields_ = [("buffer", u64), ("offset", u64), ("size", u64)]
+
+
+class CmdClearTexture(C.Structure):
+    _fields_ = [("texture", u64), ("base_mip_level", u32), ("mip_level_count", u32), ("base_array_layer", u32),
+                ("array_layer_count", u32)]
 
 
 P = C.POINTER

@@ -366,6 +366,46 @@ class CommandEncoder:
         pad = (-len(body)) % 8
         self._chunks.append(bytes(hdr) + body + b"\0" * pad)
 
+    # Copies and clears outside render passes (extension profile; the reference's encoder has
+    # them as todo!, command.rs:37-115).  size=None: to the end of the source / buffer.
+    def copy_buffer_to_buffer(self, source: "Buffer", source_offset: int, destination: "Buffer",
+                              destination_offset: int, size: Optional[int] = None) -> None:
+        self._push(A.OP_COPY_BUFFER_TO_BUFFER, A.CmdCopyBufferToBuffer(
+            source.handle, source_offset, destination.handle, destination_offset,
+            0xFFFFFFFFFFFFFFFF if size is None else size))
+
+    @staticmethod
+    def _texture_info(texture, mip_level=0, origin=(0, 0, 0)):
+        return A.TexelCopyTextureInfo(texture.handle, mip_level, *origin)
+
+    def copy_buffer_to_texture(self, buffer: "Buffer", offset: int, bytes_per_row: int, rows_per_image: int,
+                               texture: "Texture", size, mip_level: int = 0, origin=(0, 0, 0)) -> None:
+        self._push(A.OP_COPY_BUFFER_TO_TEXTURE, A.CmdCopyBufferTexture(
+            buffer.handle, A.TexelCopyBufferLayout(offset, bytes_per_row, rows_per_image),
+            self._texture_info(texture, mip_level, origin), A.Extent3d(*size), 0))
+
+    def copy_texture_to_buffer(self, texture: "Texture", buffer: "Buffer", offset: int, bytes_per_row: int,
+                               rows_per_image: int, size, mip_level: int = 0, origin=(0, 0, 0)) -> None:
+        self._push(A.OP_COPY_TEXTURE_TO_BUFFER, A.CmdCopyBufferTexture(
+            buffer.handle, A.TexelCopyBufferLayout(offset, bytes_per_row, rows_per_image),
+            self._texture_info(texture, mip_level, origin), A.Extent3d(*size), 0))
+
+    def copy_texture_to_texture(self, source: "Texture", destination: "Texture", size, source_mip: int = 0,
+                                source_origin=(0, 0, 0), destination_mip: int = 0,
+                                destination_origin=(0, 0, 0)) -> None:
+        self._push(A.OP_COPY_TEXTURE_TO_TEXTURE, A.CmdCopyTextureToTexture(
+            self._texture_info(source, source_mip, source_origin),
+            self._texture_info(destination, destination_mip, destination_origin), A.Extent3d(*size), 0))
+
+    def clear_buffer(self, buffer: "Buffer", offset: int = 0, size: Optional[int] = None) -> None:
+        self._push(A.OP_CLEAR_BUFFER, A.CmdClearBuffer(buffer.handle, offset,
+                                                       0xFFFFFFFFFFFFFFFF if size is None else size))
+
+    def clear_texture(self, texture: "Texture", base_mip_level: int = 0, mip_level_count: int = 0,
+                      base_array_layer: int = 0, array_layer_count: int = 0) -> None:
+        self._push(A.OP_CLEAR_TEXTURE, A.CmdClearTexture(texture.handle, base_mip_level, mip_level_count,
+                                                         base_array_layer, array_layer_count))
+
     def begin_render_pass(self, color_attachments: Sequence[Optional[RenderPassColorAttachment]] = (),
                           depth_stencil_attachment: Optional[RenderPassDepthStencilAttachment] = None
                           ) -> "RenderPassEncoder":
