@@ -148,3 +148,23 @@ def test_trap_fails_the_draw(gpu):
         s.render()
     assert e.value.status == -4
     frame(gpu, wl.scene_colored_sphere(gpu, 64, 64))  # the device stays usable
+
+
+@pytest.mark.parametrize("order", [W.RasterOrder.AUTO, W.RasterOrder.ORDERED])
+def test_edge_rule_frames(order):
+    """WGSL modules are compiled with the edge-function instantiations of the kernels when the
+    device uses that rule: their frames equal the native programs' under the same rule."""
+    dev = W.Device(profile=W.Profile.EXTENSION, raster_rule=W.RasterRule.EDGE, raster_order=order)
+    try:
+        nat = frame(dev, wl.scene_colored_sphere(dev, 300, 200))
+        s = with_wgsl(wl.scene_colored_sphere(dev, 300, 200), dev, P.MESH_COLOR, MESH_LAYOUT,
+                      W.PrimitiveState(cull_mode=W.Face.BACK), None, W.TextureFormat.RGBA8_UNORM)
+        assert_frames_equal(frame(dev, s), nat, f"edge rule mesh colour ({order})")
+        ff, cull = W.FrontFace.CCW, W.Face.NONE
+        nat = frame(dev, wl.scene_reference_triangle(dev, front_face=ff, cull_mode=cull))
+        s = with_wgsl(wl.scene_reference_triangle(dev, front_face=ff, cull_mode=cull), dev, P.TRIANGLE, [],
+                      W.PrimitiveState(front_face=ff, cull_mode=cull), W.DepthStencilState(True, W.CompareFunction.LESS),
+                      W.TextureFormat.RGBA8_UNORM_SRGB)
+        assert_frames_equal(frame(dev, s), nat, f"edge rule triangle ({order})")
+    finally:
+        dev.close()

@@ -240,6 +240,7 @@ struct BatchParams {
     BatchStatus* status;
     uint32_t* abort_flag;        // set by a failed batch; later batches of the submission skip
     uint32_t* slow_prims;        // [total_prims] primitives the fast setup path hands on
+    uint32_t* tile_hint;         // [total_prims] binning hint per primary record (null: none), TILE_HINT_*
     uint32_t* strip_info;        // strip tables of the restart draws (null when there are none)
     void* states;                // visibility raster: per-draw fragment-stage state (RasterState)
     uint32_t vis_compare;        // visibility raster: the batch's depth compare function

@@ -503,6 +503,17 @@ __device__ __forceinline__ void count_tiles(const BatchParams& bp, const TriReco
 __device__ __forceinline__ bool tiles_are_many(const TriRecord& r, uint32_t shift) {
     return (r.row1 >> shift) - (r.row0 >> shift) >= 2;
 }
+
+// Binning hint of a primary record, written by the fast setup so that k_fill need not read the
+// record back: the record covers nothing, exactly one tile (its global index), or anything else.
+enum : uint32_t { TILE_HINT_EMPTY = 0xFFFFFFFEu, TILE_HINT_WALK = 0xFFFFFFFFu };
+__device__ __forceinline__ uint32_t tile_hint_of(const BatchParams& bp, const TriRecord& r, const DrawDesc& d) {
+    if (r.flags & 2u) return TILE_HINT_EMPTY;
+    const TargetDesc& t = bp.targets[d.target];
+    uint32_t one;
+    if (!tiles_are_many(r, bp.tile_shift) && single_tile(r, d, t, bp.tile_shift, one)) return t.tile_base + one;
+    return TILE_HINT_WALK;
+}
 template <bool EDGE, class F>
 __device__ __forceinline__ void coop_tiles(const BatchParams& bp, const TriRecord* mine, uint32_t lane, F&& f) {
     uint32_t todo = __ballot_sync(0xFFFFFFFFu, mine != nullptr);
@@ -614,6 +625,7 @@ __global__ void __launch_bounds__(1024) k_strip_table(BatchParams bp) {
 // is returned in `coop` for the warp to count together.
 template <bool EDGE>
 __device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp, const TriRecord*& coop) {
+    if (bp.tile_hint) bp.tile_hint[gp] = TILE_HINT_WALK;  // k_fill reads the generic path's records
     TriRecord* prim_rec = rec_at(bp.records, bp.record_stride, gp);
     const uint32_t di = find_draw(bp.draws, bp.num_draws, gp);
     const DrawDesc& d = bp.draws[di];
@@ -976,13 +988,15 @@ template <bool EDGE>
 __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
     extern __shared__ __align__(16) uint8_t s_stage_raw[];
     __shared__ DrawCache s_dc[kSetupWarps];
-    const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t rstride = bp.record_stride;
     uint8_t* stage = s_stage_raw + (size_t)warp * 32 * rstride;
     DrawCache& dc = s_dc[warp];
     if (lane == 0) dc.id = 0xFFFFFFFFu;
     __syncwarp();
+    // grid-stride over 32-primitive groups (measured faster than giving each warp a contiguous run
+    // of groups, which concentrates the tile-count atomics of neighbouring triangles)
+    const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < bp.total_prims; base += stride) {
         if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the warp
         const uint32_t gp = base + lane;
@@ -1022,6 +1036,7 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
                 default: break;
             }
         }
+        if (live && done && bp.tile_hint) bp.tile_hint[gp] = tile_hint_of(bp, *rec, dc.d);
         // the rest to the generic kernel (its record is rewritten there)
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, live && !done);
         if (m) {
@@ -1124,7 +1139,10 @@ __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < total; base += stride) {
         const uint32_t i = base + lane;
         const TriRecord* coop = nullptr;
-        if (i < total) {
+        const uint32_t hint = i < bp.total_prims && bp.tile_hint ? bp.tile_hint[i] : TILE_HINT_WALK;
+        if (hint < TILE_HINT_EMPTY) {
+            put(hint, i << SUBTRI_BITS);  // a primary record is sub-triangle 0 of its primitive
+        } else if (i < total && hint == TILE_HINT_WALK) {
             const TriRecord* r = i < bp.total_prims ? rec_at(bp.records, bp.record_stride, i)
                                                     : rec_at(bp.ovf_records, bp.record_stride, i - bp.total_prims);
             if (!(r->flags & 2u)) {

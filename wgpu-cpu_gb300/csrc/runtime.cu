@@ -339,7 +339,7 @@ struct Device {
 
     // worker-owned scratch
     uint64_t scratch_bytes = 0;
-    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf, slow_buf, strip_buf, upload_buf;
+    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf, slow_buf, strip_buf, upload_buf, hint_buf;
     // coalesced small writes: double-buffered pinned staging, each free again once its event (the
     // upload copy from it) has completed
     struct PinnedStage {
@@ -1364,6 +1364,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         }
         records_buf.ensure((size_t)std::max(1u, max_prims) * max_stride, &scratch_bytes);
         slow_buf.ensure((size_t)std::max(1u, max_prims) * sizeof(uint32_t), &scratch_bytes);
+        hint_buf.ensure((size_t)std::max(1u, max_prims) * sizeof(uint32_t), &scratch_bytes);
         if (max_strip) strip_buf.ensure((size_t)max_strip * sizeof(uint32_t), &scratch_bytes);
         ovf_buf.ensure((size_t)ovf_capacity * max_stride, &scratch_bytes);
         tiles_buf.ensure((size_t)(max_tiles + 1) * 3 * sizeof(uint32_t) + 64, &scratch_bytes);
@@ -1396,6 +1397,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 bp.num_varyings = b.nvar;
                 bp.records = static_cast<uint8_t*>(records_buf.ptr);
                 bp.slow_prims = static_cast<uint32_t*>(slow_buf.ptr);
+                bp.tile_hint = static_cast<uint32_t*>(hint_buf.ptr);
             bp.strip_info = b.strip_entries ? static_cast<uint32_t*>(strip_buf.ptr) : nullptr;
                 bp.ovf_records = static_cast<uint8_t*>(ovf_buf.ptr);
                 bp.ovf_capacity = ovf_capacity;
@@ -1452,8 +1454,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 put(&nd, sizeof nd);
                 put(&nt, sizeof nt);
             }
-            const void* ptrs[7] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, slow_buf.ptr,
-                                   strip_buf.ptr};
+            const void* ptrs[8] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, slow_buf.ptr,
+                                   strip_buf.ptr, hint_buf.ptr};
             put(ptrs, sizeof ptrs);
             put(&ovf_capacity, sizeof ovf_capacity);
             put(&bin_capacity, sizeof bin_capacity);
@@ -1928,6 +1930,7 @@ GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
         d->objects.clear();
         d->records_buf.release();
         d->slow_buf.release();
+        d->hint_buf.release();
         d->strip_buf.release();
         d->ovf_buf.release();
         d->tiles_buf.release();
