@@ -114,7 +114,7 @@ def workloads():
             "batched draws: 256 draws into 64 targets (sides log-uniform [128,2048], tris log-uniform [100,200k]), "
             "Rgba8Unorm + Depth32Float Less, half texture x Lambert / half vertex colour, one command buffer",
             {"draws": 256, "targets": 64, "profile": "parity", "seed": 3},
-            cpu_kwargs=dict(n_targets=16, n_draws=64, seed=3), tile=(16, 2)),
+            cpu_kwargs=dict(n_targets=16, n_draws=64, seed=3), tile=(32, 8)),
     }
 
 

@@ -110,12 +110,10 @@ __device__ __forceinline__ void tile_sync() {
 
 // One CTA per tile (persistent); a CTA of one warp synchronises with __syncwarp only, so many
 // independent tiles share an SM and hide each other's memory latency.
-// Phase 1: every bin entry of the tile is rasterised by one lane (records whose tile-clipped
-// box holds at most lane_px pixels: many when the tile has records enough for every lane, a
-// few otherwise) or by a whole warp
-// (larger ones: lanes split the box), each covered fragment atomicMin-ing its key into the
-// tile's key array.  Phase 2: one thread per pixel re-evaluates the survivor's barycentrics,
-// tests it against the stored depth, runs the fragment stage and writes colour and depth.
+// Phase 1: the row segments of the tile's records are dealt to lanes (one span per segment), each
+// covered fragment atomicMin-ing its key into the tile's key array.  Phase 2: one thread per
+// pixel re-evaluates the survivor's barycentrics, tests it against the stored depth, runs the
+// fragment stage and writes colour and depth.
 template <int T, int WARPS, bool EDGE = false>
 __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
     constexpr int NT = WARPS * 32, NPIX = T * T;
@@ -146,7 +144,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
         const int XE = min(X0 + T, (int)tg.width) - 1, YE = min(Y0 + T, (int)tg.height) - 1;
         const uint32_t n = bp.tile_count[tile];
         const uint32_t off = bp.tile_offset[tile];
-        const int lane_px = n >= (uint32_t)NT ? 32 : 6;
         uint32_t frag_count = 0;
 
         auto fragment = [&](const TriRecord& r, const BaryK& k, uint32_t order, int x, int y) {
@@ -158,7 +155,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
             atomicMin(&s_vis[(y - Y0) * T + (x - X0)], vis_key(cmpf, z, order));
         };
 
-        // phase 1: coverage and survivor keys
+        // phase 1: coverage and survivor keys.  A warp takes the tile's records 32 at a time; their
+        // rows (clipped to tile and scissor), cut into segments of at most kSeg pixels, are dealt
+        // to the lanes through a warp scan of the per-record segment counts, so each pass gives
+        // every lane one row segment: one span, then the covered pixels of the segment.
+        constexpr int kSeg = 8;
+        constexpr unsigned kFull = 0xFFFFFFFFu;
         for (uint32_t base = (threadIdx.x & ~31u); base < n; base += NT) {
             const uint32_t i = base + lane;
             const TriRecord* r = nullptr;
@@ -173,42 +175,45 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                 xl = max(max(r->xmin, X0), (int)d.sc_x0);
                 xr = min(min(r->xmax, XE), (int)d.sc_x1 - 1);
             }
-            const int box = (y1 >= y0 && xr >= xl) ? (y1 - y0 + 1) * (xr - xl + 1) : 0;
-            if (box > 0 && box <= lane_px) {
-                BaryK k;
-                bary_consts(*r, k);
-                for (int y = y0; y <= y1; ++y) {
-                    int x1, x2;
-                    span_at<EDGE>(*r, y, x1, x2);
-                    x1 = max(x1, xl);
-                    x2 = min(x2, xr);
-                    for (int x = x1; x <= x2; ++x) fragment(*r, k, key, x, y);
-                }
+            const bool any = y1 >= y0 && xr >= xl;
+            const int segs_row = any ? (xr - xl + kSeg) / kSeg : 0;
+            const uint32_t slots = any ? (uint32_t)((y1 - y0 + 1) * segs_row) : 0u;
+            uint32_t incl = slots;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(kFull, incl, o);
+                if (lane >= (uint32_t)o) incl += v;
             }
-            uint32_t big = __ballot_sync(0xFFFFFFFFu, box > lane_px);
-            while (big) {
-                const int src = __ffs(big) - 1;
-                big &= big - 1;
-                const TriRecord* br = reinterpret_cast<const TriRecord*>(
-                    __shfl_sync(0xFFFFFFFFu, reinterpret_cast<unsigned long long>(r), src));
-                const uint32_t bkey = __shfl_sync(0xFFFFFFFFu, key, src);
-                const int by0 = __shfl_sync(0xFFFFFFFFu, y0, src), by1 = __shfl_sync(0xFFFFFFFFu, y1, src);
-                const int bxl = __shfl_sync(0xFFFFFFFFu, xl, src), bxr = __shfl_sync(0xFFFFFFFFu, xr, src);
+            const uint32_t total = __shfl_sync(kFull, incl, 31);
+            const uint32_t excl = incl - slots;
+            for (uint32_t t0 = 0; t0 < total; t0 += 32) {  // warp-uniform
+                const uint32_t t = t0 + lane;
+                // the owner of slot t: the last lane whose exclusive prefix is <= t (it has slots)
+                int src = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(kFull, excl, src + step) <= t) src += step;
+                const uint32_t first = __shfl_sync(kFull, excl, src);
+                const int sr = __shfl_sync(kFull, segs_row, src);
+                const int ry0 = __shfl_sync(kFull, y0, src), rxl = __shfl_sync(kFull, xl, src);
+                const int rxr = __shfl_sync(kFull, xr, src);
+                const uint32_t rkey = __shfl_sync(kFull, key, src);
+                const TriRecord* rr = reinterpret_cast<const TriRecord*>(
+                    __shfl_sync(kFull, reinterpret_cast<unsigned long long>(r), src));
+                if (t >= total) continue;
+                const uint32_t local = t - first;
+                const int row = sr == 1 ? (int)local : (int)(local / (uint32_t)sr);
+                const int seg = (int)local - row * sr;
+                const int y = ry0 + row;
+                const int sx0 = rxl + seg * kSeg, sx1 = min(rxr, sx0 + kSeg - 1);
+                int x1, x2;
+                span_at<EDGE>(*rr, y, x1, x2);
+                x1 = max(x1, sx0);
+                x2 = min(x2, sx1);
+                if (x1 > x2) continue;
                 BaryK k;
-                bary_consts(*br, k);
-                const int w = bxr - bxl + 1;
-                // rows are handed to lanes in groups: lane -> (row offset, x) within the box
-                const int rows_per_pass = max(1, 32 / w);
-                const int cols = w < 32 ? w : 32;
-                const int lr = lane / cols, lc = lane - lr * cols;
-                for (int y = by0 + lr; lr < rows_per_pass && y <= by1; y += rows_per_pass) {
-                    int x1, x2;
-                    span_at<EDGE>(*br, y, x1, x2);
-                    x1 = max(x1, bxl);
-                    x2 = min(x2, bxr);
-                    for (int x = bxl + lc; x <= x2; x += cols)
-                        if (x >= x1) fragment(*br, k, bkey, x, y);
-                }
+                bary_consts(*rr, k);
+                for (int x = x1; x <= x2; ++x) fragment(*rr, k, rkey, x, y);
             }
         }
         tile_sync<WARPS>();
