@@ -62,22 +62,45 @@ __device__ __forceinline__ void bary_consts(const TriRecord& r, BaryK& k) {
 template <bool EDGE>
 __device__ __forceinline__ void bary_at(const TriRecord& r, const BaryK& k, int x, int y, float cmp[3]) {
     // an IEEE sum does not depend on operand order: x + a.x serves both terms containing it
+    // The operations of the scalar formulas, sums and differences two lanes per packed f32x2
+    // instruction (exact per lane; products scalar, see f2mul_rn); a - b is a + (-b).
     const float fx = EDGE ? fadd((float)x, 0.5f) : (float)x, fy = EDGE ? fadd((float)y, 0.5f) : (float)y;
-    const float xa = fadd(fx, k.ax), xb = fadd(fx, k.bx), xc = fadd(fx, k.cx);
-    const float s0 = fadd(fadd(fmul(fsub(k.by, fy), xb), k.kc0), fmul(fsub(fy, k.cy), xc));
-    const float s1 = fadd(fadd(fmul(fsub(fy, k.ay), xa), fmul(fsub(k.cy, fy), xc)), k.kc1);
-    const float s2 = fadd(fadd(k.kc2, fmul(fsub(fy, k.by), xb)), fmul(fsub(k.ay, fy), xa));
-    const float l0 = div_by_recip(s0, k.area, k.rcp, k.area_ok);
-    const float l1 = div_by_recip(s1, k.area, k.rcp, k.area_ok);
-    const float l2 = div_by_recip(s2, k.area, k.rcp, k.area_ok);
-    if (k.ident && k.area_ok && div_fast_ok(s0) && div_fast_ok(s1) && div_fast_ok(s2)) {
-        cmp[0] = l0;
-        cmp[1] = l1;
-        cmp[2] = l2;
-    } else {
+    const float2 xab = f2add(make_float2(fx, fx), make_float2(k.ax, k.bx));
+    const float xa = xab.x, xb = xab.y, xc = fadd(fx, k.cx);
+    // s0 = ((b.y - y) (x + b.x) + kc0) + (y - c.y) (x + c.x); s2 = (kc2 + (y - b.y) (x + b.x)) + (a.y - y) (x + a.x)
+    const float2 d02 = f2add(make_float2(k.by, fy), make_float2(-fy, -k.by));
+    const float2 t02 = f2add(f2mul_rn(d02, make_float2(xb, xb)), make_float2(k.kc0, k.kc2));
+    const float2 e02 = f2add(make_float2(fy, k.ay), make_float2(-k.cy, -fy));
+    const float2 s02 = f2add(t02, f2mul_rn(e02, make_float2(xc, xa)));
+    // s1 = ((y - a.y) (x + a.x) + (c.y - y) (x + c.x)) + kc1
+    const float2 e1 = f2add(make_float2(fy, k.cy), make_float2(-k.ay, -fy));
+    const float2 m1 = f2mul_rn(e1, make_float2(xa, xc));
+    const float s1 = fadd(fadd(m1.x, m1.y), k.kc1);
+    if (k.area_ok && div_fast_ok(s02.x) && div_fast_ok(s1) && div_fast_ok(s02.y)) {
+        // div_by_recip's in-range path for s0 and s2 together
+        const float2 y2 = make_float2(k.rcp, k.rcp), nb2 = make_float2(-k.area, -k.area);
+        float2 q = f2mul(s02, y2);
+        float2 rr = f2fma(nb2, q, s02);
+        q = f2fma(rr, y2, q);
+        rr = f2fma(nb2, q, s02);
+        const float2 l02 = f2fma(rr, y2, q);
+        const float l1 = div_by_recip(s1, k.area, k.rcp, true);
+        if (k.ident) {
+            cmp[0] = l02.x;
+            cmp[1] = l1;
+            cmp[2] = l02.y;
+            return;
+        }
 #pragma unroll
-        for (int j = 0; j < 3; ++j) cmp[j] = fadd(fadd(fmul(r.cb[j], l0), fmul(r.cb[3 + j], l1)), fmul(r.cb[6 + j], l2));
+        for (int j = 0; j < 3; ++j)
+            cmp[j] = fadd(fadd(fmul(r.cb[j], l02.x), fmul(r.cb[3 + j], l1)), fmul(r.cb[6 + j], l02.y));
+        return;
     }
+    const float l0 = div_by_recip(s02.x, k.area, k.rcp, k.area_ok);
+    const float l1 = div_by_recip(s1, k.area, k.rcp, k.area_ok);
+    const float l2 = div_by_recip(s02.y, k.area, k.rcp, k.area_ok);
+#pragma unroll
+    for (int j = 0; j < 3; ++j) cmp[j] = fadd(fadd(fmul(r.cb[j], l0), fmul(r.cb[3 + j], l1)), fmul(r.cb[6 + j], l2));
 }
 
 __device__ __forceinline__ float frag_z(const TriRecord& r, const float cmp[3]) {  // raster.rs:345-346
