@@ -355,10 +355,10 @@ __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriReco
                                                   const float inv_w0[3], const float (*var)[NVMAX], uint32_t nvar) {
     float area = shoelace(frag[0].x, frag[0].y, frag[1].x, frag[1].y, frag[2].x, frag[2].y);
     // scanlines(): sort the framebuffer vertices by y with bubblesort3 (util/sort.rs:3-8)
-    int64_t px[3] = {fbx[0], fbx[1], fbx[2]}, py[3] = {fby[0], fby[1], fby[2]};
+    uint32_t px[3] = {fbx[0], fbx[1], fbx[2]}, py[3] = {fby[0], fby[1], fby[2]};
     auto cas = [&](int l, int rr) {
         if (py[l] > py[rr]) {
-            int64_t tx = px[l], tyy = py[l];
+            uint32_t tx = px[l], tyy = py[l];
             px[l] = px[rr]; py[l] = py[rr];
             px[rr] = tx; py[rr] = tyy;
         }
@@ -401,7 +401,7 @@ __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriReco
         r->sx[0] = r->sx[1] = r->sx[2] = 0;
         r->sy[0] = r->sy[2] = 0;
     } else {
-        const int64_t lim = 1ll << 30;
+        const uint32_t lim = 1u << 30;
         if (px[0] >= lim || px[1] >= lim || px[2] >= lim || py[2] >= lim) {
             raise_error(bp.status, ERR_SPAN_RANGE, key);
             flags |= 2u;
@@ -946,12 +946,40 @@ __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc&
     // clipping: nothing to do inside all planes; dropped, exactly as clip_tri_ordered drops it,
     // when all three vertices are outside the first plane any of them is outside (the planes
     // before it pass the triangle through unchanged); a real split goes to the generic path
+    // For finite coordinates dot4 against these planes (coefficients 0 and +-1) is the plain sum
+    // of its two non-zero terms up to the sign of a zero result, and only `< 0` is asked: the
+    // sums (x + w, -x + w, y + w, -y + w, z, -z + w) decide exactly as dot4 does.
+    const float inf = __int_as_float(0x7F800000);
+    bool finite = true;
 #pragma unroll
-    for (int pl = 0; pl < 6; ++pl) {
-        const V4 nrm = clip_plane(pl);
-        const int out = (dot4(pos[0], nrm) < 0.0f) + (dot4(pos[1], nrm) < 0.0f) + (dot4(pos[2], nrm) < 0.0f);
-        if (out == 3) return true;  // no sub-triangles: the record stays empty
-        if (out != 0) return false;
+    for (int i = 0; i < 3; ++i)
+        finite = finite && fabsf(pos[i].x) < inf && fabsf(pos[i].y) < inf && fabsf(pos[i].z) < inf &&
+                 fabsf(pos[i].w) < inf;
+    if (finite) {
+        float dist[3][6];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            dist[i][0] = fadd(pos[i].x, pos[i].w);
+            dist[i][1] = fadd(-pos[i].x, pos[i].w);
+            dist[i][2] = fadd(pos[i].y, pos[i].w);
+            dist[i][3] = fadd(-pos[i].y, pos[i].w);
+            dist[i][4] = pos[i].z;
+            dist[i][5] = fadd(-pos[i].z, pos[i].w);
+        }
+#pragma unroll
+        for (int pl = 0; pl < 6; ++pl) {
+            const int out = (dist[0][pl] < 0.0f) + (dist[1][pl] < 0.0f) + (dist[2][pl] < 0.0f);
+            if (out == 3) return true;  // no sub-triangles: the record stays empty
+            if (out != 0) return false;
+        }
+    } else {
+#pragma unroll
+        for (int pl = 0; pl < 6; ++pl) {
+            const V4 nrm = clip_plane(pl);
+            const int out = (dot4(pos[0], nrm) < 0.0f) + (dot4(pos[1], nrm) < 0.0f) + (dot4(pos[2], nrm) < 0.0f);
+            if (out == 3) return true;
+            if (out != 0) return false;
+        }
     }
     // to_raster (raster.rs:145-160) on the quotients at hand
     CV v[3];
