@@ -143,6 +143,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
     constexpr unsigned long long kNone = ~0ull;
     __shared__ unsigned long long s_vis[NPIX];
     __shared__ float s_lut[256];
+    // phase 1: the record table of the chunk being rasterised (per thread: record, key, clipped box
+    // and segments per row, exclusive prefix of the segment counts) and the warps' segment sums
+    __shared__ const TriRecord* s_rec[NT];
+    __shared__ uint32_t s_key[NT], s_excl[NT];
+    __shared__ int4 s_box[NT];
+    __shared__ uint32_t s_wsum[WARPS];
     __shared__ uint32_t s_tile;
     __shared__ unsigned long long s_frag;
 
@@ -178,14 +184,16 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
             atomicMin(&s_vis[(y - Y0) * T + (x - X0)], vis_key(cmpf, z, order));
         };
 
-        // phase 1: coverage and survivor keys.  A warp takes the tile's records 32 at a time; their
-        // rows (clipped to tile and scissor), cut into segments of at most kSeg pixels, are dealt
-        // to the lanes through a warp scan of the per-record segment counts, so each pass gives
-        // every lane one row segment: one span, then the covered pixels of the segment.
+        // phase 1: coverage and survivor keys.  The CTA takes the tile's records NT at a time; their
+        // rows (clipped to tile and scissor), cut into segments of at most kSeg pixels, are dealt to
+        // all NT threads through a block scan of the per-record segment counts, so every thread
+        // rasterises whole row segments (one span each, then the covered pixels) and no warp idles
+        // while another finishes its records.
         constexpr int kSeg = 8;
         constexpr unsigned kFull = 0xFFFFFFFFu;
-        for (uint32_t base = (threadIdx.x & ~31u); base < n; base += NT) {
-            const uint32_t i = base + lane;
+        const int warp = (int)(threadIdx.x >> 5);
+        for (uint32_t c0 = 0; c0 < n; c0 += NT) {
+            const uint32_t i = c0 + threadIdx.x;
             const TriRecord* r = nullptr;
             uint32_t key = 0;
             int y0 = 1, y1 = 0, xl = 1, xr = 0;
@@ -205,30 +213,36 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const uint32_t v = __shfl_up_sync(kFull, incl, o);
-                if (lane >= (uint32_t)o) incl += v;
+                if (lane >= o) incl += v;
             }
-            const uint32_t total = __shfl_sync(kFull, incl, 31);
-            const uint32_t excl = incl - slots;
-            for (uint32_t t0 = 0; t0 < total; t0 += 32) {  // warp-uniform
-                const uint32_t t = t0 + lane;
-                // the owner of slot t: the last lane whose exclusive prefix is <= t (it has slots)
-                int src = 0;
+            if (lane == 31) s_wsum[warp] = incl;
+            tile_sync<WARPS>();
+            uint32_t woff = 0, total = 0;
 #pragma unroll
-                for (int step = 16; step > 0; step >>= 1)
-                    if (__shfl_sync(kFull, excl, src + step) <= t) src += step;
-                const uint32_t first = __shfl_sync(kFull, excl, src);
-                const int sr = __shfl_sync(kFull, segs_row, src);
-                const int ry0 = __shfl_sync(kFull, y0, src), rxl = __shfl_sync(kFull, xl, src);
-                const int rxr = __shfl_sync(kFull, xr, src);
-                const uint32_t rkey = __shfl_sync(kFull, key, src);
-                const TriRecord* rr = reinterpret_cast<const TriRecord*>(
-                    __shfl_sync(kFull, reinterpret_cast<unsigned long long>(r), src));
-                if (t >= total) continue;
-                const uint32_t local = t - first;
+            for (int w = 0; w < WARPS; ++w) {
+                const uint32_t ws = s_wsum[w];
+                woff += w < warp ? ws : 0u;
+                total += ws;
+            }
+            s_excl[threadIdx.x] = woff + incl - slots;
+            s_rec[threadIdx.x] = r;
+            s_key[threadIdx.x] = key;
+            s_box[threadIdx.x] = make_int4(y0, xl, xr, segs_row);
+            tile_sync<WARPS>();
+            for (uint32_t t = threadIdx.x; t < total; t += NT) {
+                // the record of slot t: the last entry whose exclusive prefix is <= t (it has slots)
+                int j = 0;
+#pragma unroll
+                for (int step = NT / 2; step > 0; step >>= 1)
+                    if (s_excl[j + step] <= t) j += step;
+                const int4 bx = s_box[j];
+                const TriRecord* rr = s_rec[j];
+                const uint32_t local = t - s_excl[j];
+                const int sr = bx.w;
                 const int row = sr == 1 ? (int)local : (int)(local / (uint32_t)sr);
                 const int seg = (int)local - row * sr;
-                const int y = ry0 + row;
-                const int sx0 = rxl + seg * kSeg, sx1 = min(rxr, sx0 + kSeg - 1);
+                const int y = bx.x + row;
+                const int sx0 = bx.y + seg * kSeg, sx1 = min(bx.z, sx0 + kSeg - 1);
                 int x1, x2;
                 span_at<EDGE>(*rr, y, x1, x2);
                 x1 = max(x1, sx0);
@@ -236,8 +250,10 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                 if (x1 > x2) continue;
                 BaryK k;
                 bary_consts(*rr, k);
+                const uint32_t rkey = s_key[j];
                 for (int x = x1; x <= x2; ++x) fragment(*rr, k, rkey, x, y);
             }
+            tile_sync<WARPS>();  // the shared record table is refilled by the next chunk
         }
         tile_sync<WARPS>();
 
