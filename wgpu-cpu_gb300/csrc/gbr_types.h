@@ -215,7 +215,14 @@ struct BatchStatus {
     unsigned long long bin_entries;   // tile entries needed
     unsigned long long fragments;     // fragment-shader invocations
     unsigned long long primitives;    // primitives assembled
+    uint32_t split_items;     // visibility raster: chunk work items of the split tiles (k_scan)
+    uint32_t _pad_s;
 };
+
+// Visibility raster: a tile binned more than VIS_SPLIT_CHUNK records is rasterised as chunks of
+// that many records, one work item each, taken ahead of the other tiles; each chunk leaves its
+// survivor keys in global memory and the last chunk to finish merges them and shades the tile.
+constexpr uint32_t VIS_SPLIT_CHUNK = 2048;
 
 struct BatchParams {
     const DrawDesc* draws;
@@ -245,6 +252,12 @@ struct BatchParams {
     void* states;                // visibility raster: per-draw fragment-stage state (RasterState)
     uint32_t vis_compare;        // visibility raster: the batch's depth compare function
     uint32_t raster_rule;        // RASTER_RULE_*: which instantiation of the kernels runs the batch
+    // visibility raster, split tiles (split_heavy null: no tile is split)
+    uint32_t* split_tile;        // [total_tiles] for a tile over VIS_SPLIT_CHUNK records: its heavy-list index, ~0 = not split
+    uint32_t* split_heavy;       // [split_cap_heavy][4] per split tile: tile, chunks, first work item, chunks finished
+    uint32_t* split_item;        // [split_cap_items] heavy-list index of each chunk work item
+    unsigned long long* split_keys;  // [split_cap_items][T * T] survivor keys each chunk leaves
+    uint32_t split_cap_heavy, split_cap_items;
 };
 
 }  // namespace gbr

@@ -1089,15 +1089,22 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
 // Single-CTA exclusive scan of tile counts -> tile_offset; zeroes tile_cursor.
 // Chunks of 4096 counts are loaded coalesced into shared memory, each thread scans four
 // consecutive counts, and warps combine through shuffles; a carry links the chunks.
+// For the visibility raster it also lists the tiles over VIS_SPLIT_CHUNK records and gives each
+// of them ceil(count / VIS_SPLIT_CHUNK) chunk work items, as many as the split buffers hold (a
+// tile that does not fit is rasterised whole).
 // (a template only so that both kernel translation units can instantiate it)
 template <int = 0>
 __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
     __shared__ uint32_t buf[4096];
     __shared__ uint32_t warp_sum[32];
     __shared__ unsigned long long s_carry;
+    __shared__ uint32_t s_heavy;
     const uint32_t n = bp.total_tiles;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (tid == 0) s_carry = 0;
+    if (tid == 0) {
+        s_carry = 0;
+        s_heavy = 0;
+    }
     __syncthreads();
     for (uint32_t base = 0; base < n; base += 4096) {
 #pragma unroll
@@ -1108,6 +1115,21 @@ __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
         __syncthreads();
         const uint32_t a0 = buf[4 * tid], a1 = buf[4 * tid + 1], a2 = buf[4 * tid + 2], a3 = buf[4 * tid + 3];
         const uint32_t s = a0 + a1 + a2 + a3;
+        if (bp.split_heavy && max(max(a0, a1), max(a2, a3)) > VIS_SPLIT_CHUNK) {
+            const uint32_t a[4] = {a0, a1, a2, a3};
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                if (a[k] <= VIS_SPLIT_CHUNK) continue;
+                const uint32_t tile = base + 4 * tid + k;  // < n: counts past the end load as 0
+                const uint32_t h = atomicAdd(&s_heavy, 1u);
+                if (h < bp.split_cap_heavy) {
+                    uint32_t* e = bp.split_heavy + 4 * (size_t)h;
+                    e[0] = tile;
+                    e[1] = (a[k] + VIS_SPLIT_CHUNK - 1) / VIS_SPLIT_CHUNK;
+                }
+                bp.split_tile[tile] = h < bp.split_cap_heavy ? h : ~0u;
+            }
+        }
         uint32_t x = s;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -1149,6 +1171,43 @@ __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
         bp.tile_offset[n] = (uint32_t)total;
         bp.status->bin_entries = total;
         if (total > bp.bin_capacity) raise_error(bp.status, ERR_OVERFLOW_BINS, (uint32_t)min(total, 0xFFFFFFFFull));
+    }
+    if (bp.split_heavy && wid == 0) {
+        // chunk work items of the listed tiles, in list order, while they fit split_cap_items;
+        // the tiles past that point are rasterised whole (the kept ones form a prefix of the list)
+        const uint32_t nh = min(s_heavy, bp.split_cap_heavy);
+        uint32_t carry = 0;
+        bool full = false;
+        for (uint32_t h0 = 0; h0 < nh; h0 += 32) {
+            const uint32_t h = h0 + lane;
+            uint32_t* e = bp.split_heavy + 4 * (size_t)h;
+            const uint32_t c = h < nh ? e[1] : 0u;
+            uint32_t incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= o) incl += y;
+            }
+            const bool keep = h < nh && !full && (unsigned long long)carry + incl <= bp.split_cap_items;
+            const uint32_t first = carry + incl - c;
+            if (h < nh) {
+                if (keep) {
+                    e[2] = first;
+                    e[3] = 0;
+                } else {
+                    bp.split_tile[e[0]] = ~0u;  // rasterised whole
+                }
+            }
+            const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);  // a prefix of the lanes
+            const int last = kept ? 31 - __clz(kept) : -1;
+            for (int k = 0; k <= last; ++k) {  // item -> list index
+                const uint32_t ck = __shfl_sync(0xFFFFFFFFu, c, k), fk = __shfl_sync(0xFFFFFFFFu, first, k);
+                for (uint32_t j = lane; j < ck; j += 32) bp.split_item[fk + j] = h0 + k;
+            }
+            if (last >= 0) carry += __shfl_sync(0xFFFFFFFFu, incl, last);
+            if (__any_sync(0xFFFFFFFFu, h < nh && !keep)) full = true;
+        }
+        if (lane == 0) bp.status->split_items = carry;
     }
 }
 

@@ -137,6 +137,11 @@ __device__ __forceinline__ void tile_sync() {
 // covered fragment atomicMin-ing its key into the tile's key array.  Phase 2: one thread per
 // pixel re-evaluates the survivor's barycentrics, tests it against the stored depth, runs the
 // fragment stage and writes colour and depth.
+// Work items: first the chunks of the split tiles (VIS_SPLIT_CHUNK records each; k_scan lists
+// them), then every tile that is not split.  A chunk runs phase 1 over its records only and stores
+// its key array in its own global slot; the chunk that finishes last (a per-tile ticket) takes
+// the minimum over the tile's slots, which is the key array of the whole tile since the survivor
+// key is a minimum, and runs phase 2.  No CTA waits for another.
 template <int T, int WARPS, bool EDGE = false>
 __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
     constexpr int NT = WARPS * 32, NPIX = T * T;
@@ -149,7 +154,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
     __shared__ uint32_t s_key[NT], s_excl[NT];
     __shared__ int4 s_box[NT];
     __shared__ uint32_t s_wsum[WARPS];
-    __shared__ uint32_t s_tile;
+    __shared__ uint32_t s_tile, s_last;
     __shared__ unsigned long long s_frag;
 
     const int lane = threadIdx.x & 31;
@@ -159,19 +164,35 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
     if (threadIdx.x == 0) s_frag = 0;
     const uint32_t cmpf = bp.vis_compare;
     const RasterState* states = static_cast<const RasterState*>(bp.states);
+    const uint32_t n_split = bp.split_heavy ? bp.status->split_items : 0u;  // written by k_scan
 
     for (;;) {
         if (threadIdx.x == 0) s_tile = atomicAdd(bp.work_counter, 1u);
         for (int p = threadIdx.x; p < NPIX; p += NT) s_vis[p] = kNone;
         tile_sync<WARPS>();
-        const uint32_t tile = s_tile;
-        if (tile >= bp.total_tiles || failed) break;
+        const uint32_t item = s_tile;
+        if (failed) break;
+        uint32_t tile, heavy = ~0u, r_begin = 0, r_end;
+        if (item < n_split) {  // a chunk of a split tile
+            heavy = bp.split_item[item];
+            const uint32_t* e = bp.split_heavy + 4 * (size_t)heavy;
+            tile = e[0];
+            r_begin = (item - e[2]) * VIS_SPLIT_CHUNK;
+            r_end = min(bp.tile_count[tile], r_begin + VIS_SPLIT_CHUNK);
+        } else {
+            tile = item - n_split;
+            if (tile >= bp.total_tiles) break;
+            r_end = bp.tile_count[tile];
+            if (n_split && r_end > VIS_SPLIT_CHUNK && bp.split_tile[tile] != ~0u) {
+                tile_sync<WARPS>();  // s_tile is rewritten at the top
+                continue;            // its chunks rasterise it
+            }
+        }
         const uint32_t ti = find_target(bp.targets, bp.num_targets, tile);
         const TargetDesc& tg = bp.targets[ti];
         const uint32_t lt = tile - tg.tile_base;
         const int X0 = (int)(lt % tg.tiles_x) * T, Y0 = (int)(lt / tg.tiles_x) * T;
         const int XE = min(X0 + T, (int)tg.width) - 1, YE = min(Y0 + T, (int)tg.height) - 1;
-        const uint32_t n = bp.tile_count[tile];
         const uint32_t off = bp.tile_offset[tile];
         uint32_t frag_count = 0;
 
@@ -192,12 +213,12 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
         constexpr int kSeg = 8;
         constexpr unsigned kFull = 0xFFFFFFFFu;
         const int warp = (int)(threadIdx.x >> 5);
-        for (uint32_t c0 = 0; c0 < n; c0 += NT) {
+        for (uint32_t c0 = r_begin; c0 < r_end; c0 += NT) {
             const uint32_t i = c0 + threadIdx.x;
             const TriRecord* r = nullptr;
             uint32_t key = 0;
             int y0 = 1, y1 = 0, xl = 1, xr = 0;
-            if (i < n) {
+            if (i < r_end) {
                 key = bp.bins[off + i];
                 r = record_of(bp, key);
                 const DrawDesc& d = bp.draws[r->draw];
@@ -256,6 +277,34 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
             tile_sync<WARPS>();  // the shared record table is refilled by the next chunk
         }
         tile_sync<WARPS>();
+        for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
+        if (lane == 0 && frag_count) {
+            atomicAdd(&s_frag, (unsigned long long)frag_count);
+            if (tg.frag_count) atomicAdd(tg.frag_count, (unsigned long long)frag_count);
+        }
+
+        if (heavy != ~0u) {
+            // a chunk: its keys to its slot; the last of the tile's chunks merges them all
+            unsigned long long* slot = bp.split_keys + (size_t)item * NPIX;
+            for (int p = threadIdx.x; p < NPIX; p += NT) slot[p] = s_vis[p];
+            __threadfence();
+            tile_sync<WARPS>();
+            uint32_t* e = bp.split_heavy + 4 * (size_t)heavy;
+            if (threadIdx.x == 0) {
+                s_last = atomicAdd(&e[3], 1u) == e[1] - 1u;
+                __threadfence();
+            }
+            tile_sync<WARPS>();
+            if (!s_last) continue;  // no shared state is read past the barrier above
+            const unsigned long long* slots = bp.split_keys + (size_t)e[2] * NPIX;
+            const uint32_t chunks = e[1];
+            for (int p = threadIdx.x; p < NPIX; p += NT) {
+                unsigned long long m = kNone;
+                for (uint32_t c = 0; c < chunks; ++c) m = min(m, __ldcg(slots + (size_t)c * NPIX + p));
+                s_vis[p] = m;
+            }
+            tile_sync<WARPS>();
+        }
 
         // phase 2: the survivor of each pixel against the stored depth, fragment stage, write-back
         uint32_t clear_c[4] = {0, 0, 0, 0};
@@ -334,11 +383,6 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                 else *cdst = (uint8_t)c[0];
             }
             if (write_depth) tg.depth[pix] = depth;
-        }
-        for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
-        if (lane == 0 && frag_count) {
-            atomicAdd(&s_frag, (unsigned long long)frag_count);
-            if (tg.frag_count) atomicAdd(tg.frag_count, (unsigned long long)frag_count);
         }
         tile_sync<WARPS>();
     }

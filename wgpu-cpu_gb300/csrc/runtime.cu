@@ -15,6 +15,7 @@
 #include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <deque>
 #include <future>
@@ -280,6 +281,7 @@ struct GroupRun {
     bool started = false;
     uint32_t launches = 0;
     uint64_t slow_prims = 0;
+    uint64_t split_chunks = 0;  // chunk work items of split visibility-raster tiles
     double raster_ms = 0.0;
 };
 
@@ -339,7 +341,8 @@ struct Device {
 
     // worker-owned scratch
     uint64_t scratch_bytes = 0;
-    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf, slow_buf, strip_buf, upload_buf, hint_buf;
+    DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf, slow_buf, strip_buf, upload_buf, hint_buf,
+        split_buf;
     // coalesced small writes: double-buffered pinned staging, each free again once its event (the
     // upload copy from it) has completed
     struct PinnedStage {
@@ -350,6 +353,9 @@ struct Device {
     int pinned_next = 0;
     uint32_t ovf_capacity = 4096;
     uint64_t bin_capacity = 1u << 22;
+    // chunk work items the visibility raster may split heavy tiles into (0: 32 MiB of key arrays);
+    // GBR_VIS_SPLIT_ITEMS sets it at device creation
+    uint32_t split_cap_override = 0;
 
     // autotuner: per batch signature, each candidate tile shape is timed once, then the fastest
     // is kept (all shapes give bit-identical results, only the time differs)
@@ -1003,6 +1009,7 @@ void Device::execute_group(std::vector<Item>& items) {
         rec.stats.gpu_ms = group_ms;
         rec.stats.raster_ms = run.raster_ms;
         rec.stats.generic_setup_prims = (uint32_t)std::min<uint64_t>(run.slow_prims, 0xFFFFFFFFu);
+        rec.stats.split_tile_chunks = (uint32_t)std::min<uint64_t>(run.split_chunks, 0xFFFFFFFFu);
         rec.ev = run.started ? run.ev : nullptr;
         records[items[i].index] = rec;
         completed_submissions = std::max(completed_submissions, items[i].index + 1);
@@ -1369,6 +1376,19 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         ovf_buf.ensure((size_t)ovf_capacity * max_stride, &scratch_bytes);
         tiles_buf.ensure((size_t)(max_tiles + 1) * 3 * sizeof(uint32_t) + 64, &scratch_bytes);
         bins_buf.ensure((size_t)bin_capacity * sizeof(uint32_t), &scratch_bytes);
+        // visibility raster, split tiles: per-tile marker, heavy list, item table, the chunks' key
+        // arrays (32 MiB of them at the largest tile of the batches)
+        uint32_t vis_npix = 0;
+        for (size_t i = first_batch; i < nb; ++i)
+            if (kinds[i] == 3) vis_npix = std::max(vis_npix, (uint32_t)(btile[i] * btile[i]));
+        uint32_t split_items = vis_npix ? std::max(64u, (uint32_t)((32u << 20) / (vis_npix * 8u))) : 0u;
+        if (vis_npix && split_cap_override) split_items = split_cap_override;
+        const uint32_t split_heavy = split_items / 2;  // a split tile has two chunks or more
+        const size_t split_off_heavy = align((size_t)max_tiles * sizeof(uint32_t));
+        const size_t split_off_items = align(split_off_heavy + (size_t)split_heavy * 16);
+        const size_t split_off_keys = align(split_off_items + (size_t)split_items * sizeof(uint32_t));
+        if (vis_npix)
+            split_buf.ensure(split_off_keys + (size_t)split_items * vis_npix * sizeof(unsigned long long), &scratch_bytes);
         if (scratch_bytes > budget) fail(GBR_ERR_OUT_OF_MEMORY, "transient memory exceeds the HBM budget");
         if (!run.started) {
             cuda_check(cudaEventRecord(run.ev->start, stream), "event");
@@ -1414,6 +1434,13 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 if (kinds[i] == 3) {
                     bp.states = meta + states_off[i];
                     bp.vis_compare = visibility_compare(b);
+                    uint8_t* sb = static_cast<uint8_t*>(split_buf.ptr);
+                    bp.split_tile = reinterpret_cast<uint32_t*>(sb);
+                    bp.split_heavy = reinterpret_cast<uint32_t*>(sb + split_off_heavy);
+                    bp.split_item = reinterpret_cast<uint32_t*>(sb + split_off_items);
+                    bp.split_keys = reinterpret_cast<unsigned long long*>(sb + split_off_keys);
+                    bp.split_cap_heavy = split_heavy;
+                    bp.split_cap_items = split_items;
                 }
                 cudaEvent_t* ev = revp->empty() ? nullptr : &(*revp)[2 * i];
                 if (b.copy) {
@@ -1454,8 +1481,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 put(&nd, sizeof nd);
                 put(&nt, sizeof nt);
             }
-            const void* ptrs[8] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, slow_buf.ptr,
-                                   strip_buf.ptr, hint_buf.ptr};
+            const void* ptrs[9] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, slow_buf.ptr,
+                                   strip_buf.ptr, hint_buf.ptr, split_buf.ptr};
             put(ptrs, sizeof ptrs);
             put(&ovf_capacity, sizeof ovf_capacity);
             put(&bin_capacity, sizeof bin_capacity);
@@ -1523,6 +1550,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
             b.target_frags.assign(counters.begin() + (ptrdiff_t)counter_first[i],
                                   counters.begin() + (ptrdiff_t)(counter_first[i] + b.targets.size()));
             run.slow_prims += st[i].slow_count;
+            run.split_chunks += st[i].split_items;
             if (!revp->empty()) {
                 float ms = 0.0f;
                 if (cudaEventElapsedTime(&ms, (*revp)[2 * i], (*revp)[2 * i + 1]) == cudaSuccess) {
@@ -1876,6 +1904,7 @@ GBR_API gbr_status gbr_device_create(const gbr_device_config* cfg, gbr_device* o
         if (!raster_config_supported(d->tile, d->warps))
             fail(GBR_ERR_INVALID_ARGUMENT, "unsupported tile size / warps per tile %d/%d", d->tile, d->warps);
         if (cfg->bin_capacity) d->bin_capacity = cfg->bin_capacity;
+        if (const char* e = std::getenv("GBR_VIS_SPLIT_ITEMS")) d->split_cap_override = (uint32_t)std::strtoul(e, nullptr, 10);
         d->autotune = cfg->tile_size == 0 && cfg->warps_per_tile == 0;
         if (cfg->launch_mode > GBR_LAUNCH_PER_PASS) fail(GBR_ERR_INVALID_ARGUMENT, "launch_mode");
         if (cfg->raster_order > GBR_RASTER_ORDERED) fail(GBR_ERR_INVALID_ARGUMENT, "raster_order");
@@ -1931,6 +1960,7 @@ GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
         d->records_buf.release();
         d->slow_buf.release();
         d->hint_buf.release();
+        d->split_buf.release();
         d->strip_buf.release();
         d->ovf_buf.release();
         d->tiles_buf.release();
