@@ -348,6 +348,20 @@ static __device__ __noinline__ void record_lod(const DrawDesc& dd, uint32_t q, u
                            dd.samp.lod_min, dd.samp.lod_max);
 }
 
+// The record header as eleven 16-byte words, in the order build_record_frag stores them.
+#ifndef __CUDACC_RTC__  // (offsetof needs <cstddef>; the layout is the same under NVRTC)
+static_assert(offsetof(TriRecord, row0) == 16 && offsetof(TriRecord, sx) == 32 && offsetof(TriRecord, sy) == 44 &&
+                  offsetof(TriRecord, vpx) == 56 && offsetof(TriRecord, vpy) == 68 && offsetof(TriRecord, area) == 80 &&
+                  offsetof(TriRecord, fz) == 84 && offsetof(TriRecord, fw) == 96 && offsetof(TriRecord, cb) == 108 &&
+                  offsetof(TriRecord, inv_w0) == 144 && offsetof(TriRecord, ovf) == 156 &&
+                  offsetof(TriRecord, nsub) == 160 && offsetof(TriRecord, lod) == 164 && sizeof(TriRecord) == 176,
+              "TriRecord layout assumed by build_record_frag");
+#endif
+
+// Writes a complete record (nsub = 1, ovf = 0; callers that emit more sub-triangles overwrite
+// both).  `r` is 16-byte aligned (records, overflow records and the setup stage all are): the
+// header goes out as eleven 16-byte stores, which a warp whose lanes write records 240 bytes
+// apart in shared memory issues without bank conflicts (scalar stores there conflict 4 ways).
 template <uint32_t NVMAX, bool EDGE>
 __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriRecord* r, uint32_t key, uint32_t draw,
                                                   uint32_t prim_index, bool front_facing, const CV v[3],
@@ -367,7 +381,8 @@ __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriReco
     cas(0, 2);
     cas(1, 2);
     uint32_t flags = front_facing ? 1u : 0u;
-    int row0, row1;
+    int row0, row1, xmin, xmax;
+    int sxv[3], syv[3];
     const DrawDesc& dd = bp.draws[draw];
     if constexpr (EDGE) {
         // rows whose centres lie within the snapped y extent, columns likewise; the span of each
@@ -378,12 +393,12 @@ __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriReco
 #pragma unroll
         for (int i = 0; i < 3; ++i)
             ok = ok && fabsf(frag[i].x) < 4194304.0f && fabsf(frag[i].y) < 4194304.0f;  // 2^22 px
+        int sy1 = 0;
         if (!ok) {
             raise_error(bp.status, ERR_SPAN_RANGE, key);
             flags |= 2u;
             row0 = 1; row1 = 0;
-            r->xmin = 1; r->xmax = 0;
-            r->sy[1] = 0;
+            xmin = 1; xmax = 0;
         } else {
             const float vx[3] = {frag[0].x, frag[1].x, frag[2].x}, vy[3] = {frag[0].y, frag[1].y, frag[2].y};
             int64_t X[3], Y[3];
@@ -393,13 +408,15 @@ __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriReco
             const int64_t xlo = min(X[0], min(X[1], X[2])), xhi = max(X[0], max(X[1], X[2]));
             row0 = (int)ceil_div(ylo - 128, 256);
             row1 = (int)floor_div(yhi - 128, 256);
-            r->xmin = (int)ceil_div(xlo - 128, 256);
-            r->xmax = (int)floor_div(xhi - 128, 256);
-            r->sy[1] = (int)floor_div(ymid - 128, 256) + 1;
-            if (row0 > row1 || r->xmin > r->xmax) flags |= 2u;
+            xmin = (int)ceil_div(xlo - 128, 256);
+            xmax = (int)floor_div(xhi - 128, 256);
+            sy1 = (int)floor_div(ymid - 128, 256) + 1;
+            if (row0 > row1 || xmin > xmax) flags |= 2u;
         }
-        r->sx[0] = r->sx[1] = r->sx[2] = 0;
-        r->sy[0] = r->sy[2] = 0;
+        sxv[0] = sxv[1] = sxv[2] = 0;
+        syv[0] = 0;
+        syv[1] = sy1;
+        syv[2] = 0;
     } else {
         const uint32_t lim = 1u << 30;
         if (px[0] >= lim || px[1] >= lim || px[2] >= lim || py[2] >= lim) {
@@ -418,42 +435,52 @@ __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriReco
         } else {
             row1 = (int)py[2];
         }
-        r->xmin = (int)min(px[0], min(px[1], px[2]));
-        r->xmax = (int)max(px[0], max(px[1], px[2]));
+        xmin = (int)min(px[0], min(px[1], px[2]));
+        xmax = (int)max(px[0], max(px[1], px[2]));
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            r->sx[i] = (int)px[i];
-            r->sy[i] = (int)py[i];
+            sxv[i] = (int)px[i];
+            syv[i] = (int)py[i];
         }
     }
     // bit 4: the clip barycentrics are exactly the unit vectors (an unclipped triangle)
     if (v[0].b[0] == 1.0f && v[0].b[1] == 0.0f && v[0].b[2] == 0.0f && v[1].b[0] == 0.0f && v[1].b[1] == 1.0f &&
         v[1].b[2] == 0.0f && v[2].b[0] == 0.0f && v[2].b[1] == 0.0f && v[2].b[2] == 1.0f)
         flags |= 16u;
-    r->key = key;
-    r->draw = draw;
-    r->prim_index = prim_index;
-    r->flags = flags;
-    r->row0 = row0;
-    r->row1 = row1;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        r->vpx[i] = frag[i].x;
-        r->vpy[i] = frag[i].y;
-        r->fz[i] = frag[i].z;
-        r->fw[i] = frag[i].w;
-        r->inv_w0[i] = inv_w0[i];
-#pragma unroll
-        for (int j = 0; j < 3; ++j) r->cb[i * 3 + j] = v[i].b[j];
-    }
-    r->area = area;
-    r->lod = 0.0f;
+    auto fb = [](float x) { return __float_as_uint(x); };
+    auto ib = [](int x) { return (uint32_t)x; };
+    uint4* h = reinterpret_cast<uint4*>(r);
+    h[0] = make_uint4(key, draw, prim_index, flags);
+    h[1] = make_uint4(ib(row0), ib(row1), ib(xmin), ib(xmax));
+    h[2] = make_uint4(ib(sxv[0]), ib(sxv[1]), ib(sxv[2]), ib(syv[0]));
+    h[3] = make_uint4(ib(syv[1]), ib(syv[2]), fb(frag[0].x), fb(frag[1].x));
+    h[4] = make_uint4(fb(frag[2].x), fb(frag[0].y), fb(frag[1].y), fb(frag[2].y));
+    h[5] = make_uint4(fb(area), fb(frag[0].z), fb(frag[1].z), fb(frag[2].z));
+    h[6] = make_uint4(fb(frag[0].w), fb(frag[1].w), fb(frag[2].w), fb(v[0].b[0]));
+    h[7] = make_uint4(fb(v[0].b[1]), fb(v[0].b[2]), fb(v[1].b[0]), fb(v[1].b[1]));
+    h[8] = make_uint4(fb(v[1].b[2]), fb(v[2].b[0]), fb(v[2].b[1]), fb(v[2].b[2]));
+    h[9] = make_uint4(fb(inv_w0[0]), fb(inv_w0[1]), fb(inv_w0[2]), 0u);  // ovf
+    h[10] = make_uint4(1u, fb(0.0f), 0u, 0u);                          // nsub, lod, padding
     float* rv = rec_var(r);
+    if (nvar == NVMAX) {
+        // all of the draw's varyings (a compile-time count on the fast path): 16-byte stores
+        constexpr uint32_t NF = 3 * NVMAX;
+        uint32_t flat[NF];
 #pragma unroll
-    for (uint32_t i = 0; i < 3; ++i)
+        for (uint32_t q = 0; q < NF; ++q) flat[q] = fb(var[q / NVMAX][q % NVMAX]);
+        uint4* hv = reinterpret_cast<uint4*>(rv);
 #pragma unroll
-        for (uint32_t k = 0; k < NVMAX; ++k)
-            if (k < nvar) rv[i * nvar + k] = var[i][k];
+        for (uint32_t q = 0; q + 4 <= NF; q += 4) hv[q / 4] = make_uint4(flat[q], flat[q + 1], flat[q + 2], flat[q + 3]);
+        uint32_t* tail = reinterpret_cast<uint32_t*>(rv);
+#pragma unroll
+        for (uint32_t q = NF & ~3u; q < NF; ++q) tail[q] = flat[q];
+    } else {
+#pragma unroll
+        for (uint32_t q = 0; q < 3; ++q)
+#pragma unroll
+            for (uint32_t k = 0; k < NVMAX; ++k)
+                if (k < nvar) rv[q * nvar + k] = var[q][k];
+    }
     if (dd.lod_var != 0 && !(flags & 2u)) record_lod(dd, dd.lod_var - 1, nvar, r);
 }
 
@@ -880,10 +907,9 @@ __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc&
     const uint32_t inst = d.instance_count == 1 ? 0u : local / d.prims_per_instance;
     const uint32_t p = local - inst * d.prims_per_instance;
     const uint32_t instance = d.instance_start + inst;
-    rec->key = gp << SUBTRI_BITS;
-    rec->flags = 2u;
+    // an empty record until it is built (the exits below that drop the primitive leave it so)
+    *reinterpret_cast<uint4*>(rec) = make_uint4(gp << SUBTRI_BITS, di, p, 2u);
     rec->nsub = 0;
-    rec->draw = di;
     uint32_t sp[3];
     if (d.topology == 4) {  // triangle strip (primitive.rs:360-392)
         sp[0] = (p & 1u) ? p + 1 : p;
@@ -1000,8 +1026,6 @@ __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc&
         frag[i] = {vx, vy, nz, rw[i]};
     }
     build_record_frag<NV, EDGE>(bp, rec, gp << SUBTRI_BITS, di, p, front_facing, v, fbx, fby, frag, rw, var, NV);
-    rec->nsub = 1;
-    rec->ovf = 0;
     if (!(rec->flags & 2u) && tiles_are_many(*rec, bp.tile_shift)) coop = rec;
     else count_tiles<EDGE>(bp, rec, d);
     return true;
@@ -1172,42 +1196,64 @@ __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
         bp.status->bin_entries = total;
         if (total > bp.bin_capacity) raise_error(bp.status, ERR_OVERFLOW_BINS, (uint32_t)min(total, 0xFFFFFFFFull));
     }
-    if (bp.split_heavy && wid == 0) {
-        // chunk work items of the listed tiles, in list order, while they fit split_cap_items;
-        // the tiles past that point are rasterised whole (the kept ones form a prefix of the list)
+    if (bp.split_heavy) {
+        // chunk work items of the listed tiles in list order, while their running total fits
+        // split_cap_items (a prefix of the list, the running total being monotone); the tiles
+        // past it are rasterised whole.  Four entries per thread, block scan, carry per 4096.
+        __shared__ uint32_t s_items;
         const uint32_t nh = min(s_heavy, bp.split_cap_heavy);
-        uint32_t carry = 0;
-        bool full = false;
-        for (uint32_t h0 = 0; h0 < nh; h0 += 32) {
-            const uint32_t h = h0 + lane;
-            uint32_t* e = bp.split_heavy + 4 * (size_t)h;
-            const uint32_t c = h < nh ? e[1] : 0u;
-            uint32_t incl = c;
+        if (tid == 0) {
+            s_items = 0;
+            s_carry = 0;
+        }
+        __syncthreads();
+        for (uint32_t base = 0; base < nh; base += 4096) {
+            uint32_t c[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t h = base + 4 * tid + k;
+                c[k] = h < nh ? bp.split_heavy[4 * (size_t)h + 1] : 0u;
+            }
+            const uint32_t sum = c[0] + c[1] + c[2] + c[3];
+            uint32_t x = sum;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-                if (lane >= o) incl += y;
+                const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+                if (lane >= o) x += y;
             }
-            const bool keep = h < nh && !full && (unsigned long long)carry + incl <= bp.split_cap_items;
-            const uint32_t first = carry + incl - c;
-            if (h < nh) {
-                if (keep) {
-                    e[2] = first;
-                    e[3] = 0;
-                } else {
-                    bp.split_tile[e[0]] = ~0u;  // rasterised whole
+            if (lane == 31) warp_sum[wid] = x;
+            __syncthreads();
+            if (wid == 0) {
+                uint32_t w = warp_sum[lane];
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+                    if (lane >= o) w += y;
                 }
+                warp_sum[lane] = w;
             }
-            const uint32_t kept = __ballot_sync(0xFFFFFFFFu, keep);  // a prefix of the lanes
-            const int last = kept ? 31 - __clz(kept) : -1;
-            for (int k = 0; k <= last; ++k) {  // item -> list index
-                const uint32_t ck = __shfl_sync(0xFFFFFFFFu, c, k), fk = __shfl_sync(0xFFFFFFFFu, first, k);
-                for (uint32_t j = lane; j < ck; j += 32) bp.split_item[fk + j] = h0 + k;
+            __syncthreads();
+            unsigned long long first = s_carry + (wid ? warp_sum[wid - 1] : 0u) + x - sum;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const uint32_t h = base + 4 * tid + k;
+                if (h >= nh) break;
+                uint32_t* e = bp.split_heavy + 4 * (size_t)h;
+                if (first + c[k] <= bp.split_cap_items) {
+                    e[2] = (uint32_t)first;
+                    e[3] = 0;
+                    for (uint32_t j = 0; j < c[k]; ++j) bp.split_item[first + j] = h;
+                    atomicMax(&s_items, (uint32_t)(first + c[k]));
+                } else {
+                    bp.split_tile[e[0]] = ~0u;
+                }
+                first += c[k];
             }
-            if (last >= 0) carry += __shfl_sync(0xFFFFFFFFu, incl, last);
-            if (__any_sync(0xFFFFFFFFu, h < nh && !keep)) full = true;
+            __syncthreads();
+            if (tid == 0) s_carry += warp_sum[31];
+            __syncthreads();
         }
-        if (lane == 0) bp.status->split_items = carry;
+        if (tid == 0) bp.status->split_items = s_items;
     }
 }
 
