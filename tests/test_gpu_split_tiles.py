@@ -1,6 +1,7 @@
 """GPU parity of the visibility raster's split tiles: dense meshes drawn into small targets bin
-thousands of records into single tiles, which the raster cuts into chunks of VIS_SPLIT_CHUNK
-(2048) records run by different CTAs and merged by the last one to finish.  Colour, depth and the
+thousands of records into single tiles, which the raster cuts into chunks of 2048 records (or
+the chunk size GBR_VIS_SPLIT_CHUNK gives) run by different CTAs and merged by the last one to
+finish.  Colour, depth and the
 fragment count must equal the oracle's bit for bit, at every tile shape, under both raster
 rules, and when the split buffers hold only some of the heavy tiles (the rest are rasterised
 whole)."""
@@ -90,3 +91,17 @@ def test_split_capacity_leaves_the_rest_whole(oracle_dense, monkeypatch):
             assert st.fragments_shaded == oracle_dense[1]
         finally:
             dev.close()
+
+
+@pytest.mark.parametrize("chunk", [100, 700])
+def test_split_chunk_sizes(oracle_dense, chunk, monkeypatch):
+    """Chunks smaller than a CTA's width and of sizes that are no multiple of it."""
+    monkeypatch.setenv("GBR_VIS_SPLIT_CHUNK", str(chunk))
+    dev = W.Device(tile_size=16, warps_per_tile=4)
+    try:
+        out, st = render_all(dev, **DENSE)
+        assert st.split_tile_chunks >= 20
+        assert_targets_same(out, oracle_dense[0], f"chunk {chunk}")
+        assert st.fragments_shaded == oracle_dense[1]
+    finally:
+        dev.close()

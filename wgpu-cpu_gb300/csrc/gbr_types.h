@@ -219,9 +219,10 @@ struct BatchStatus {
     uint32_t _pad_s;
 };
 
-// Visibility raster: a tile binned more than VIS_SPLIT_CHUNK records is rasterised as chunks of
-// that many records, one work item each, taken ahead of the other tiles; each chunk leaves its
-// survivor keys in global memory and the last chunk to finish merges them and shades the tile.
+// Visibility raster: a tile binned more than BatchParams::split_chunk records (VIS_SPLIT_CHUNK
+// unless the device is told otherwise) is rasterised as chunks of that many records, one work
+// item each, taken ahead of the other tiles; each chunk leaves its survivor keys in global memory
+// and the last chunk to finish merges them and shades the tile.
 constexpr uint32_t VIS_SPLIT_CHUNK = 2048;
 
 struct BatchParams {
@@ -253,11 +254,13 @@ struct BatchParams {
     uint32_t vis_compare;        // visibility raster: the batch's depth compare function
     uint32_t raster_rule;        // RASTER_RULE_*: which instantiation of the kernels runs the batch
     // visibility raster, split tiles (split_heavy null: no tile is split)
-    uint32_t* split_tile;        // [total_tiles] for a tile over VIS_SPLIT_CHUNK records: its heavy-list index, ~0 = not split
+    uint32_t* split_tile;        // [total_tiles] for a tile over split_chunk records: its heavy-list index, ~0 = not split
     uint32_t* split_heavy;       // [split_cap_heavy][4] per split tile: tile, chunks, first work item, chunks finished
     uint32_t* split_item;        // [split_cap_items] heavy-list index of each chunk work item
     unsigned long long* split_keys;  // [split_cap_items][T * T] survivor keys each chunk leaves
     uint32_t split_cap_heavy, split_cap_items;
+    uint32_t split_chunk;        // records per chunk work item (> 0 when split_heavy is set)
+    uint32_t _pad_split;
 };
 
 }  // namespace gbr

@@ -246,7 +246,6 @@ cudaError_t launch_batch_jit(JitKernels& k, const BatchParams& bp, int num_sms, 
         ++*launches;
     }
     if (items) {
-        const uint32_t g = std::min((items + 127) / 128, (uint32_t)num_sms * 16);
         const size_t smem = setup_stage_bytes_host(bp.record_stride);
         if (k.setup_smem < smem) {
             if ((e = cudaFuncSetAttribute(reinterpret_cast<const void*>(k.setup), cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -254,6 +253,14 @@ cudaError_t launch_batch_jit(JitKernels& k, const BatchParams& bp, int num_sms, 
                 return e;
             k.setup_smem = smem;
         }
+        if (k.setup_occ_smem != smem) {  // blocks an SM holds at this stage size (grid-stride: one wave)
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&k.setup_blocks, reinterpret_cast<const void*>(k.setup),
+                                                                   128, smem)) != cudaSuccess)
+                return e;
+            k.setup_blocks = std::max(1, k.setup_blocks);
+            k.setup_occ_smem = smem;
+        }
+        const uint32_t g = std::min((items + 127) / 128, std::min((uint32_t)num_sms * 16, (uint32_t)(num_sms * k.setup_blocks)));
         if ((e = launch(k.setup, g, 128, smem, s, bp)) != cudaSuccess) return e;
         if ((e = launch(k.slow, std::min((items + 127) / 128, (uint32_t)num_sms * 4), 128, 0, s, bp)) != cudaSuccess) return e;
         *launches += 2;

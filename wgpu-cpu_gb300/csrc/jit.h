@@ -20,8 +20,8 @@ struct JitKernels {
                  ordered = nullptr, eval = nullptr, strip = nullptr, clear = nullptr, lines = nullptr;
     int vis_tile = 16, vis_warps = 4, ord_tile = 16, ord_warps = 8;
     std::mutex mu;  // launch configuration below
-    size_t setup_smem = 0, ord_smem = 0;
-    int vis_blocks = 0, ord_blocks = 0;
+    size_t setup_smem = 0, ord_smem = 0, setup_occ_smem = 0;
+    int vis_blocks = 0, ord_blocks = 0, setup_blocks = 1;
     ~JitKernels();
 };
 

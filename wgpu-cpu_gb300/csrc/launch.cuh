@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <map>
 #include <mutex>
 
 #include "kernels.h"
@@ -102,11 +103,12 @@ cudaError_t launch_batch_t(const BatchParams& bp, int tile, int warps, int num_s
         ++*launches;
     }
     if (items) {
-        uint32_t g = std::min((items + 127) / 128, cap);
         const size_t smem = setup_stage_bytes(bp.record_stride);
+        int resident = 0;  // k_setup blocks an SM holds at this stage size (grid-stride: one wave)
         {
             static std::mutex mu;
             static size_t configured = 0;
+            static std::map<size_t, int> occupancy;
             std::lock_guard<std::mutex> lk(mu);
             if (configured < smem) {
                 if ((e = cudaFuncSetAttribute(k_setup<EDGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
@@ -114,7 +116,16 @@ cudaError_t launch_batch_t(const BatchParams& bp, int tile, int warps, int num_s
                     return e;
                 configured = smem;
             }
+            auto it = occupancy.find(smem);
+            if (it == occupancy.end()) {
+                if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_setup<EDGE>, kSetupWarps * 32, smem)) !=
+                    cudaSuccess)
+                    return e;
+                it = occupancy.emplace(smem, std::max(resident, 1)).first;
+            }
+            resident = it->second;
         }
+        const uint32_t g = std::min((items + 127) / 128, std::min(cap, (uint32_t)(resident * num_sms)));
         k_setup<EDGE><<<g, kSetupWarps * 32, smem, s>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         ++*launches;

@@ -1026,8 +1026,7 @@ __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc&
         frag[i] = {vx, vy, nz, rw[i]};
     }
     build_record_frag<NV, EDGE>(bp, rec, gp << SUBTRI_BITS, di, p, front_facing, v, fbx, fby, frag, rw, var, NV);
-    if (!(rec->flags & 2u) && tiles_are_many(*rec, bp.tile_shift)) coop = rec;
-    else count_tiles<EDGE>(bp, rec, d);
+    if (!(rec->flags & 2u) && tiles_are_many(*rec, bp.tile_shift)) coop = rec;  // k_setup counts the rest
     return true;
 }
 
@@ -1088,7 +1087,22 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
                 default: break;
             }
         }
-        if (live && done && bp.tile_hint) bp.tile_hint[gp] = tile_hint_of(bp, *rec, dc.d);
+        // tile counts of the finished records: one atomic per distinct tile of the warp's
+        // single-tile records (neighbouring triangles of a mesh mostly share one), a walk over the
+        // tiles for the other records but those handed to the warp as a whole (coop)
+        uint32_t hint = TILE_HINT_EMPTY;
+        if (live && done) {
+            hint = tile_hint_of(bp, *rec, dc.d);
+            if (bp.tile_hint) bp.tile_hint[gp] = hint;
+        }
+        const uint32_t single = hint < TILE_HINT_EMPTY ? hint : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single);
+        if (single != 0xFFFFFFFFu && (int)lane == __ffs(peers) - 1) atomicAdd(&bp.tile_count[single], (uint32_t)__popc(peers));
+        if (hint == TILE_HINT_WALK && coop == nullptr) {
+            const TargetDesc& t = bp.targets[dc.d.target];
+            for_each_tile<EDGE>(*rec, dc.d, t, bp.tile_shift,
+                                [&](uint32_t lt) { atomicAdd(&bp.tile_count[t.tile_base + lt], 1u); });
+        }
         // the rest to the generic kernel (its record is rewritten there)
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, live && !done);
         if (m) {
@@ -1113,9 +1127,9 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
 // Single-CTA exclusive scan of tile counts -> tile_offset; zeroes tile_cursor.
 // Chunks of 4096 counts are loaded coalesced into shared memory, each thread scans four
 // consecutive counts, and warps combine through shuffles; a carry links the chunks.
-// For the visibility raster it also lists the tiles over VIS_SPLIT_CHUNK records and gives each
-// of them ceil(count / VIS_SPLIT_CHUNK) chunk work items, as many as the split buffers hold (a
-// tile that does not fit is rasterised whole).
+// For the visibility raster it also lists the tiles over split_chunk records and gives each of
+// them ceil(count / split_chunk) chunk work items, as many as the split buffers hold (a tile that
+// does not fit is rasterised whole).
 // (a template only so that both kernel translation units can instantiate it)
 template <int = 0>
 __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
@@ -1139,17 +1153,17 @@ __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
         __syncthreads();
         const uint32_t a0 = buf[4 * tid], a1 = buf[4 * tid + 1], a2 = buf[4 * tid + 2], a3 = buf[4 * tid + 3];
         const uint32_t s = a0 + a1 + a2 + a3;
-        if (bp.split_heavy && max(max(a0, a1), max(a2, a3)) > VIS_SPLIT_CHUNK) {
+        if (bp.split_heavy && max(max(a0, a1), max(a2, a3)) > bp.split_chunk) {
             const uint32_t a[4] = {a0, a1, a2, a3};
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                if (a[k] <= VIS_SPLIT_CHUNK) continue;
+                if (a[k] <= bp.split_chunk) continue;
                 const uint32_t tile = base + 4 * tid + k;  // < n: counts past the end load as 0
                 const uint32_t h = atomicAdd(&s_heavy, 1u);
                 if (h < bp.split_cap_heavy) {
                     uint32_t* e = bp.split_heavy + 4 * (size_t)h;
                     e[0] = tile;
-                    e[1] = (a[k] + VIS_SPLIT_CHUNK - 1) / VIS_SPLIT_CHUNK;
+                    e[1] = (a[k] - 1) / bp.split_chunk + 1;
                 }
                 bp.split_tile[tile] = h < bp.split_cap_heavy ? h : ~0u;
             }
@@ -1273,8 +1287,16 @@ __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
         const uint32_t i = base + lane;
         const TriRecord* coop = nullptr;
         const uint32_t hint = i < bp.total_prims && bp.tile_hint ? bp.tile_hint[i] : TILE_HINT_WALK;
-        if (hint < TILE_HINT_EMPTY) {
-            put(hint, i << SUBTRI_BITS);  // a primary record is sub-triangle 0 of its primitive
+        // single-tile records (a primary record is sub-triangle 0 of its primitive): one cursor
+        // atomic per distinct tile of the warp, each lane taking the slot of its rank among peers
+        const uint32_t single = hint < TILE_HINT_EMPTY ? hint : 0xFFFFFFFFu;
+        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single);
+        if (single != 0xFFFFFFFFu) {
+            const int leader = __ffs(peers) - 1;
+            uint32_t pos = 0;
+            if ((int)lane == leader) pos = atomicAdd(&bp.tile_cursor[single], (uint32_t)__popc(peers));
+            pos = __shfl_sync(peers, pos, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
+            bp.bins[bp.tile_offset[single] + pos] = i << SUBTRI_BITS;
         } else if (i < total && hint == TILE_HINT_WALK) {
             const TriRecord* r = i < bp.total_prims ? rec_at(bp.records, bp.record_stride, i)
                                                     : rec_at(bp.ovf_records, bp.record_stride, i - bp.total_prims);

@@ -137,8 +137,7 @@ __device__ __forceinline__ void tile_sync() {
 // covered fragment atomicMin-ing its key into the tile's key array.  Phase 2: one thread per
 // pixel re-evaluates the survivor's barycentrics, tests it against the stored depth, runs the
 // fragment stage and writes colour and depth.
-// Work items: first the chunks of the split tiles (VIS_SPLIT_CHUNK records each; k_scan lists
-// them), then every tile that is not split.  A chunk runs phase 1 over its records only and stores
+// Work items: first the chunks of the split tiles (split_chunk records each; k_scan lists them), then every tile that is not split.  A chunk runs phase 1 over its records only and stores
 // its key array in its own global slot; the chunk that finishes last (a per-tile ticket) takes
 // the minimum over the tile's slots, which is the key array of the whole tile since the survivor
 // key is a minimum, and runs phase 2.  No CTA waits for another.
@@ -177,13 +176,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
             heavy = bp.split_item[item];
             const uint32_t* e = bp.split_heavy + 4 * (size_t)heavy;
             tile = e[0];
-            r_begin = (item - e[2]) * VIS_SPLIT_CHUNK;
-            r_end = min(bp.tile_count[tile], r_begin + VIS_SPLIT_CHUNK);
+            r_begin = (item - e[2]) * bp.split_chunk;
+            r_end = min(bp.tile_count[tile], r_begin + bp.split_chunk);
         } else {
             tile = item - n_split;
             if (tile >= bp.total_tiles) break;
             r_end = bp.tile_count[tile];
-            if (n_split && r_end > VIS_SPLIT_CHUNK && bp.split_tile[tile] != ~0u) {
+            if (n_split && r_end > bp.split_chunk && bp.split_tile[tile] != ~0u) {
                 tile_sync<WARPS>();  // s_tile is rewritten at the top
                 continue;            // its chunks rasterise it
             }
@@ -300,7 +299,15 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
             const uint32_t chunks = e[1];
             for (int p = threadIdx.x; p < NPIX; p += NT) {
                 unsigned long long m = kNone;
-                for (uint32_t c = 0; c < chunks; ++c) m = min(m, __ldcg(slots + (size_t)c * NPIX + p));
+                uint32_t c = 0;
+                for (; c + 8 <= chunks; c += 8) {  // eight independent loads in flight
+                    unsigned long long v[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) v[u] = __ldcg(slots + (size_t)(c + u) * NPIX + p);
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) m = min(m, v[u]);
+                }
+                for (; c < chunks; ++c) m = min(m, __ldcg(slots + (size_t)c * NPIX + p));
                 s_vis[p] = m;
             }
             tile_sync<WARPS>();

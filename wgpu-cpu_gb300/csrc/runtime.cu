@@ -356,6 +356,7 @@ struct Device {
     // chunk work items the visibility raster may split heavy tiles into (0: 32 MiB of key arrays);
     // GBR_VIS_SPLIT_ITEMS sets it at device creation
     uint32_t split_cap_override = 0;
+    uint32_t split_chunk = VIS_SPLIT_CHUNK;  // records per chunk; GBR_VIS_SPLIT_CHUNK sets it
 
     // autotuner: per batch signature, each candidate tile shape is timed once, then the fastest
     // is kept (all shapes give bit-identical results, only the time differs)
@@ -1441,6 +1442,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                     bp.split_keys = reinterpret_cast<unsigned long long*>(sb + split_off_keys);
                     bp.split_cap_heavy = split_heavy;
                     bp.split_cap_items = split_items;
+                    bp.split_chunk = split_chunk;
                 }
                 cudaEvent_t* ev = revp->empty() ? nullptr : &(*revp)[2 * i];
                 if (b.copy) {
@@ -1905,6 +1907,8 @@ GBR_API gbr_status gbr_device_create(const gbr_device_config* cfg, gbr_device* o
             fail(GBR_ERR_INVALID_ARGUMENT, "unsupported tile size / warps per tile %d/%d", d->tile, d->warps);
         if (cfg->bin_capacity) d->bin_capacity = cfg->bin_capacity;
         if (const char* e = std::getenv("GBR_VIS_SPLIT_ITEMS")) d->split_cap_override = (uint32_t)std::strtoul(e, nullptr, 10);
+        if (const char* e = std::getenv("GBR_VIS_SPLIT_CHUNK"))
+            d->split_chunk = std::max<uint32_t>(32u, (uint32_t)std::strtoul(e, nullptr, 10));
         d->autotune = cfg->tile_size == 0 && cfg->warps_per_tile == 0;
         if (cfg->launch_mode > GBR_LAUNCH_PER_PASS) fail(GBR_ERR_INVALID_ARGUMENT, "launch_mode");
         if (cfg->raster_order > GBR_RASTER_ORDERED) fail(GBR_ERR_INVALID_ARGUMENT, "raster_order");
