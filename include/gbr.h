@@ -500,6 +500,17 @@ GBR_API gbr_status gbr_buffer_destroy(gbr_device device, gbr_buffer buffer);
 /* QueueInterface::write_buffer (device.rs:332-344).  Ordered with later submissions. */
 GBR_API gbr_status gbr_queue_write_buffer(gbr_device device, gbr_buffer buffer, uint64_t offset,
                                           const void* data, uint64_t size);
+/* Many QueueInterface::write_buffer calls (device.rs:332-344) in one: the writes are queued in
+ * array order, as that many gbr_queue_write_buffer calls would queue them, after every entry has
+ * been validated (an invalid entry queues none of them).  Serving loops that upload a fixed set
+ * of buffers every frame pass one prepared array instead of crossing the ABI per buffer. */
+typedef struct gbr_buffer_write {
+    gbr_buffer buffer;
+    uint64_t offset;
+    const void* data;
+    uint64_t size;
+} gbr_buffer_write;
+GBR_API gbr_status gbr_queue_write_buffers(gbr_device device, uint32_t count, const gbr_buffer_write* writes);
 /* BufferInterface::map_async + get_mapped_range for reads (buffer.rs:112-136): waits for all
  * prior submissions, then copies `size` bytes at `offset` into `dst`. */
 GBR_API gbr_status gbr_buffer_read(gbr_device device, gbr_buffer buffer, uint64_t offset, void* dst, uint64_t size);

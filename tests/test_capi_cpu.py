@@ -62,12 +62,15 @@ STRUCTS = ["gbr_device_config", "gbr_limits", "gbr_texture_desc", "gbr_texel_cop
            "gbr_depth_stencil_state", "gbr_render_pipeline_desc", "gbr_bind_group_entry", "gbr_bind_group_desc",
            "gbr_submission_stats", "gbr_color_attachment", "gbr_depth_attachment", "gbr_cmd_begin_render_pass",
            "gbr_cmd_set_bind_group", "gbr_cmd_set_index_buffer", "gbr_cmd_set_vertex_buffer", "gbr_cmd_set_viewport",
-           "gbr_cmd_draw", "gbr_cmd_draw_indexed"]
+           "gbr_cmd_draw", "gbr_cmd_draw_indexed", "gbr_cmd_copy_buffer_to_buffer", "gbr_texel_copy_texture_info",
+           "gbr_cmd_copy_buffer_texture", "gbr_cmd_copy_texture_to_texture", "gbr_cmd_clear_buffer",
+           "gbr_cmd_clear_texture", "gbr_buffer_write"]
 PY = ["DeviceConfig", "Limits", "TextureDesc", "TexelCopyBufferLayout", "SamplerDesc", "VertexAttribute",
       "VertexBufferLayout", "ColorTargetState", "PrimitiveState", "DepthStencilState", "RenderPipelineDesc",
       "BindGroupEntry", "BindGroupDesc", "SubmissionStats", "ColorAttachment", "DepthAttachment",
       "CmdBeginRenderPass", "CmdSetBindGroup", "CmdSetIndexBuffer", "CmdSetVertexBuffer", "CmdSetViewport",
-      "CmdDraw", "CmdDrawIndexed"]
+      "CmdDraw", "CmdDrawIndexed", "CmdCopyBufferToBuffer", "TexelCopyTextureInfo", "CmdCopyBufferTexture",
+      "CmdCopyTextureToTexture", "CmdClearBuffer", "CmdClearTexture", "BufferWrite"]
 
 
 def test_ctypes_layouts_match_header(tmp_path):

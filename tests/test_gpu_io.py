@@ -94,3 +94,53 @@ def test_many_small_writes_apply_in_order(gpu):
         st = gpu.lib.buffer_read(gpu.handle, buf.handle, 0, out.ctypes.data_as(ctypes.c_void_p), out.nbytes)
         assert st == 0, gpu.lib.error_text()
         assert np.array_equal(out, want)
+
+
+def test_batched_writes_equal_single_writes(gpu):
+    """gbr_queue_write_buffers: the writes land in array order (a later entry overlapping an
+    earlier one wins), small and large (device-staged) entries alike, and an invalid entry
+    queues none of the batch."""
+    import ctypes
+
+    rng = np.random.default_rng(23)
+    big = gpu.create_buffer_init(np.zeros(3 << 20, np.uint8))
+    small = gpu.create_buffer_init(np.zeros(4096, np.uint8))
+    want_big, want_small = np.zeros(3 << 20, np.uint8), np.zeros(4096, np.uint8)
+    items = []
+    for k in range(40):
+        if k % 10 == 0:
+            n, off = 1 << 20, int(rng.integers(0, 2 << 20))
+            buf, want = big, want_big
+        else:
+            n = int(rng.integers(1, 600))
+            off = int(rng.integers(0, 4096 - n + 1))
+            buf, want = small, want_small
+        data = rng.integers(0, 256, n, dtype=np.uint8)
+        items.append((buf, off, data))
+        want[off:off + n] = data
+    prepared = W.PreparedWrites(items)
+    gpu.queue.write_buffers(prepared)
+    for buf, want in ((big, want_big), (small, want_small)):
+        out = np.empty(want.size, np.uint8)
+        st = gpu.lib.buffer_read(gpu.handle, buf.handle, 0, out.ctypes.data_as(ctypes.c_void_p), out.nbytes)
+        assert st == 0, gpu.lib.error_text()
+        assert np.array_equal(out, want)
+    # the prepared list reads its arrays at each call: change them and write again
+    for _, off, data in prepared.items:
+        data[:] = 7
+    gpu.queue.write_buffers(prepared)
+    out = np.empty(4096, np.uint8)
+    gpu.lib.buffer_read(gpu.handle, small.handle, 0, out.ctypes.data_as(ctypes.c_void_p), out.nbytes)
+    touched = np.zeros(4096, bool)
+    for buf, off, data in items:
+        if buf is small:
+            touched[off:off + data.size] = True
+    assert (out[touched] == 7).all() and np.array_equal(out[~touched], want_small[~touched])
+    # an out-of-range entry: an error, and the valid entry before it is not applied either
+    before = out.copy()
+    bad = [(small, 0, np.full(16, 9, np.uint8)), (small, 4090, np.zeros(16, np.uint8))]
+    with pytest.raises(W.GbrError):
+        gpu.queue.write_buffers(bad)
+    gpu.lib.buffer_read(gpu.handle, small.handle, 0, out.ctypes.data_as(ctypes.c_void_p), out.nbytes)
+    assert np.array_equal(out, before)
+    assert gpu.lib.queue_write_buffers is not None

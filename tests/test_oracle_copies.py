@@ -59,3 +59,21 @@ def test_parity_profile_rejects_copies(op):
         dev.queue.submit([enc.finish()])
     assert e.value.status == A.ERR_UNSUPPORTED
     assert "todo" in e.value.message
+
+
+def test_write_buffers_falls_back_to_single_writes():
+    """Queue.write_buffers on a library without gbr_queue_write_buffers (the oracle) issues one
+    write_buffer per entry, in order."""
+    import ctypes
+
+    dev = oracle_device.device(profile=W.Profile.EXTENSION)
+    assert dev.lib.queue_write_buffers is None
+    buf = dev.create_buffer_init(np.zeros(256, np.uint8))
+    items = [(buf, 0, np.full(100, 1, np.uint8)), (buf, 50, np.full(100, 2, np.uint8)), (buf, 200, np.arange(56, dtype=np.uint8))]
+    dev.queue.write_buffers(items)
+    out = np.empty(256, np.uint8)
+    assert dev.lib.buffer_read(dev.handle, buf.handle, 0, out.ctypes.data_as(ctypes.c_void_p), out.nbytes) == 0
+    want = np.zeros(256, np.uint8)
+    for _, off, data in items:
+        want[off:off + data.size] = data
+    assert np.array_equal(out, want)

@@ -414,6 +414,14 @@ struct Device {
         queue.push_back(std::move(it));
         if (!lazy || queue.size() >= kLazyWakeItems) q_cv.notify_all();
     }
+    // Queues writes back to back under one lock (they wake the worker as single writes do).
+    void enqueue_all(std::vector<Item>& items) {
+        if (items.empty()) return;
+        std::lock_guard<std::mutex> lk(q_mu);
+        if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
+        for (Item& it : items) queue.push_back(std::move(it));
+        if (queue.size() >= kLazyWakeItems) q_cv.notify_all();
+    }
     void worker_main();
     void execute(Item& it);
     void execute_writes(std::vector<Item>& items);
@@ -2047,6 +2055,34 @@ GBR_API gbr_status gbr_queue_write_buffer(gbr_device dh, gbr_buffer b, uint64_t 
         it.staged_size = size;
         if (!it.staged) it.data.assign(static_cast<const uint8_t*>(data), static_cast<const uint8_t*>(data) + size);
         d->enqueue(std::move(it));
+    })
+}
+GBR_API gbr_status gbr_queue_write_buffers(gbr_device dh, uint32_t count, const gbr_buffer_write* writes) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        if (count && !writes) fail(GBR_ERR_INVALID_ARGUMENT, "null write array");
+        std::vector<Item> items;
+        items.reserve(count);
+        for (uint32_t k = 0; k < count; ++k) {  // validate everything before queuing anything
+            const gbr_buffer_write& w = writes[k];
+            Item it;
+            it.kind = Item::WRITE_BUFFER;
+            it.buffer = d->get<Buffer>(w.buffer, "buffer");
+            if (w.offset + w.size > it.buffer->size) fail(GBR_ERR_VALIDATION, "write_buffer out of range (entry %u)", k);
+            if (w.size && !w.data) fail(GBR_ERR_INVALID_ARGUMENT, "null data (entry %u)", k);
+            it.offset = w.offset;
+            it.staged_size = w.size;
+            if (w.size) items.push_back(std::move(it));
+        }
+        size_t j = 0;
+        for (uint32_t k = 0; k < count; ++k) {
+            const gbr_buffer_write& w = writes[k];
+            if (!w.size) continue;
+            Item& it = items[j++];
+            it.staged = stage_on_device(d.get(), w.data, w.size);
+            if (!it.staged) it.data.assign(static_cast<const uint8_t*>(w.data), static_cast<const uint8_t*>(w.data) + w.size);
+        }
+        d->enqueue_all(items);
     })
 }
 GBR_API gbr_status gbr_buffer_read(gbr_device dh, gbr_buffer b, uint64_t offset, void* dst, uint64_t size) {

@@ -79,6 +79,10 @@ class TexelCopyBufferLayout(C.Structure):
     _fields_ = [("offset", u64), ("bytes_per_row", u32), ("rows_per_image", u32)]
 
 
+class BufferWrite(C.Structure):
+    _fields_ = [("buffer", u64), ("offset", u64), ("data", C.c_void_p), ("size", u64)]
+
+
 class SamplerDesc(C.Structure):
     _fields_ = [("address_mode_u", u32), ("address_mode_v", u32), ("address_mode_w", u32),
                 ("mag_filter", u32), ("min_filter", u32), ("mipmap_filter", u32),
@@ -256,6 +260,7 @@ OPTIONAL = {
     "wgsl_translate": (i32, [C.c_char_p, u64, C.c_char_p, C.c_char_p, C.c_char_p, u64, P(u64)]),
     "wgsl_compile_check": (i32, [C.c_char_p, u64, C.c_char_p, C.c_char_p, C.c_char_p, u64]),
     "textures_read": (i32, [u64, u32, P(u64), P(u32), P(C.c_void_p), P(u64)]),
+    "queue_write_buffers": (i32, [u64, u32, C.c_void_p]),
 }
 
 

@@ -492,9 +492,38 @@ class RenderPassEncoder:
 
 
 # ------------------------------------------------------------------------------------ device
+class PreparedWrites:
+    """A fixed list of buffer writes [(buffer, offset, data)] for Queue.write_buffers: the data
+    arrays are referenced, not copied, and their contents at each write_buffers call are what
+    gets written (as with write_buffer, the bytes are captured by the call)."""
+
+    def __init__(self, items):
+        self.items = []
+        for buf, off, data in items:
+            if not (isinstance(data, np.ndarray) and data.flags.c_contiguous):
+                data = np.ascontiguousarray(np.frombuffer(memoryview(data).cast("B"), dtype=np.uint8))
+            self.items.append((buf, int(off), data))
+        self.array = (A.BufferWrite * max(1, len(self.items)))()
+        for k, (buf, off, data) in enumerate(self.items):
+            self.array[k] = A.BufferWrite(buf.handle, off, data.__array_interface__["data"][0], data.nbytes)
+
+
 class Queue:
     def __init__(self, device: "Device"):
         self.device = device
+
+    def write_buffers(self, writes) -> None:
+        """Many write_buffer calls in one (gbr_queue_write_buffers): `writes` is a PreparedWrites
+        or a list of (buffer, offset, data).  Queued in order; nothing is queued if an entry is
+        invalid.  Libraries without the batched entry point get one write_buffer per entry."""
+        if not isinstance(writes, PreparedWrites):
+            writes = PreparedWrites(writes)
+        d = self.device
+        if d.lib.queue_write_buffers is None:
+            for buf, off, data in writes.items:
+                self.write_buffer(buf, off, data)
+            return
+        _check(d.lib, d.lib.queue_write_buffers(d.handle, len(writes.items), C.cast(writes.array, C.c_void_p)))
 
     def write_buffer(self, buffer: Buffer, offset: int, data) -> None:
         d = self.device
