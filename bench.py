@@ -432,6 +432,9 @@ def serve_summary(stats, wall, lam, duration):
             "kernel_launches": int(sum(s.kernel_launches / max(1, s.batched_with) for s in stats))}
 
 
+SERVE_TILE = (32, 8)  # tile side, warps per tile of both serving arms (--tile / --warps override)
+
+
 def run_serve(args):
     """Serving loop: Poisson arrivals of pre-recorded submissions over resident meshes, textures and
     targets; the batched server (continuous batching, HBM-budget admission) and, on the same
@@ -447,7 +450,8 @@ def run_serve(args):
     arms = {}
     for name, kw in (("served", dict(batch_submissions=True, launch_mode=W.LaunchMode.BATCHED)),
                      ("per_draw", dict(batch_submissions=False, launch_mode=W.LaunchMode.PER_DRAW))):
-        dev = W.Device(device_ordinal=local, tile_size=16, warps_per_tile=2, hbm_budget_bytes=80 << 30, **kw)
+        dev = W.Device(device_ordinal=local, tile_size=args.tile or SERVE_TILE[0], warps_per_tile=args.warps or SERVE_TILE[1],
+                       hbm_budget_bytes=80 << 30, **kw)
         sset = wl.serving_set(dev)
         for c in sset.commands[:8]:  # warm-up (allocations, first launches)
             dev.poll(True, dev.queue.submit([c]))
@@ -467,6 +471,7 @@ def run_serve(args):
                                    "resident meshes (100..200k tris) and 128 textures into 256^2..1920x1080 "
                                    "Rgba8Unorm + Depth32Float targets, textured Lambert / vertex colour",
                        "lambda_per_s": lam, "hbm_budget_gb": 80, "launch_mode": "batched + merged submissions",
+                       "tile": args.tile or SERVE_TILE[0], "warps_per_tile": args.warps or SERVE_TILE[1],
                        "l2": "not flushed (inputs resident; a step is one submission)"},
             "serving": s, "per_draw_path": arms["per_draw"],
             "e2e": {"value": s["fragments_per_s"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,

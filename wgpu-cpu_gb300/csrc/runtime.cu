@@ -310,6 +310,7 @@ struct DevBuf {
 struct Batch;
 
 constexpr size_t kLazyWakeItems = 1024;  // queued writes that wake the worker by themselves
+constexpr size_t kKeptRecords = 16384;   // finished submissions whose stats stay queryable
 
 struct Device {
     gbr_device_config cfg{};
@@ -1023,7 +1024,7 @@ void Device::execute_group(std::vector<Item>& items) {
         records[items[i].index] = rec;
         completed_submissions = std::max(completed_submissions, items[i].index + 1);
     }
-    while (records.size() > 4096) records.erase(records.begin());
+    while (records.size() > kKeptRecords) records.erase(records.begin());
     done_cv.notify_all();
 }
 
