@@ -144,3 +144,35 @@ def test_batched_writes_equal_single_writes(gpu):
     gpu.lib.buffer_read(gpu.handle, small.handle, 0, out.ctypes.data_as(ctypes.c_void_p), out.nbytes)
     assert np.array_equal(out, before)
     assert gpu.lib.queue_write_buffers is not None
+
+
+def test_texture_reads_into_pinned_memory(gpu):
+    """Batched reads into pinned host memory (written by the copy kernel), into pinned memory at an
+    unaligned offset and into pageable memory (both copied by cudaMemcpyAsync) all return the
+    bytes of single reads."""
+    import torch
+
+    ms = wl.scene_batched(gpu, n_targets=5, n_draws=10, seed=4, tri_hi=4000, side_hi=300)
+    ms.render()
+    targets = [p[0] for p in ms.passes]
+    want = [gpu.read_texture(t) for t in targets]
+    sizes = [w.nbytes for w in want]
+    pinned = [torch.zeros(n + 16, dtype=torch.uint8).pin_memory() for n in sizes]
+    pageable = [np.zeros(n, np.uint8) for n in sizes]
+    items = []
+    for k, t in enumerate(targets):
+        if k % 3 == 0:
+            items.append((t, 0, pinned[k].data_ptr(), sizes[k]))           # aligned pinned: kernel
+        elif k % 3 == 1:
+            items.append((t, 0, pinned[k].data_ptr() + 4, sizes[k]))       # unaligned pinned: copy
+        else:
+            items.append((t, 0, pageable[k].ctypes.data, sizes[k]))        # pageable: copy
+    gpu.read_textures_into(items)
+    for k, w in enumerate(want):
+        if k % 3 == 2:
+            got = pageable[k]
+        else:
+            off = 0 if k % 3 == 0 else 4
+            got = pinned[k].numpy()[off:off + sizes[k]]
+            assert not pinned[k].numpy()[off + sizes[k]:].any()  # nothing past the destination
+        assert np.array_equal(got, w.reshape(-1)), k

@@ -43,6 +43,22 @@ cudaError_t launch_scatter_writes(const uint8_t* stage, const uint64_t* desc, ui
     return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(256) k_copy_out(CopyOutJobs j) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, nt = (uint64_t)gridDim.x * blockDim.x;
+    for (uint32_t k = 0; k < j.n; ++k) {
+        const uint64_t n16 = j.bytes[k] >> 4;
+        const uint4* src = reinterpret_cast<const uint4*>(j.src[k]);
+        uint4* dst = reinterpret_cast<uint4*>(j.dst[k]);
+        for (uint64_t i = t; i < n16; i += nt) dst[i] = src[i];
+        for (uint64_t i = (n16 << 4) + t; i < j.bytes[k]; i += nt) j.dst[k][i] = j.src[k][i];
+    }
+}
+cudaError_t launch_copy_out(const CopyOutJobs& jobs, int num_sms, cudaStream_t s) {
+    if (!jobs.n) return cudaSuccess;
+    k_copy_out<<<num_sms * 4, 256, 0, s>>>(jobs);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_lines(const BatchParams& bp, int num_sms, cudaStream_t s, uint32_t* launches, cudaEvent_t* ev_raster) {
     cudaError_t e;
     if ((e = cudaMemsetAsync(bp.status, 0, sizeof(BatchStatus), s)) != cudaSuccess) return e;

@@ -37,4 +37,17 @@ uint32_t fast_vs_kind(const DrawDesc& d);
 // device address desc[3k] (stage offsets are 16-byte aligned).
 cudaError_t launch_scatter_writes(const uint8_t* stage, const uint64_t* desc, uint32_t n, cudaStream_t s);
 
+// Copies of device textures into host memory the device can address (pinned, mapped): up to
+// kCopyOutMax per launch, every source and destination 16-byte aligned.  All SMs take part in
+// every copy (grid-stride over 16-byte words, the ragged tail byte by byte).
+constexpr uint32_t kCopyOutMax = 64;
+struct CopyOutJobs {
+    uint32_t n;
+    uint32_t _pad;
+    const uint8_t* src[kCopyOutMax];
+    uint8_t* dst[kCopyOutMax];
+    uint64_t bytes[kCopyOutMax];
+};
+cudaError_t launch_copy_out(const CopyOutJobs& jobs, int num_sms, cudaStream_t s);
+
 }  // namespace gbr

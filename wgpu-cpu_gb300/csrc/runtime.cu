@@ -892,15 +892,43 @@ void Device::execute(Item& it) {
                            "texture_read");
                 cuda_check(cudaStreamSynchronize(stream), "texture_read sync");
                 break;
-            case Item::READ_TEXTURES:
+            case Item::READ_TEXTURES: {
+                // Destinations the device can address (pinned host memory, as the attributes report
+                // it) are written by one copy kernel over all SMs, which moves the bytes over the
+                // CPU-GPU link faster than one copy-engine transfer per texture; any other
+                // destination (pageable, unaligned) takes cudaMemcpyAsync.
+                CopyOutJobs jobs{};
                 for (size_t k = 0; k < it.textures.size(); ++k) {
                     const Texture& t = *it.textures[k];
-                    cuda_check(cudaMemcpyAsync(it.dsts[k], t.ptr + t.mip_offset[it.mips[k]], t.mip_bytes(it.mips[k]),
-                                               cudaMemcpyDeviceToHost, stream),
-                               "textures_read");
+                    const uint8_t* src = t.ptr + t.mip_offset[it.mips[k]];
+                    const uint64_t n = t.mip_bytes(it.mips[k]);
+                    // both ends of the destination mapped, at the same distance on the device side
+                    cudaPointerAttributes pa{}, pe{};
+                    void* dev_dst = nullptr;
+                    const uint8_t* last = static_cast<const uint8_t*>(it.dsts[k]) + (n ? n - 1 : 0);
+                    if (cudaPointerGetAttributes(&pa, it.dsts[k]) == cudaSuccess && pa.type == cudaMemoryTypeHost &&
+                        pa.devicePointer != nullptr && cudaPointerGetAttributes(&pe, last) == cudaSuccess &&
+                        pe.type == cudaMemoryTypeHost &&
+                        static_cast<const uint8_t*>(pe.devicePointer) == static_cast<const uint8_t*>(pa.devicePointer) + (n ? n - 1 : 0))
+                        dev_dst = pa.devicePointer;
+                    else
+                        cudaGetLastError();  // clear a failed query: the copy below takes over
+                    if (dev_dst && ((reinterpret_cast<uintptr_t>(dev_dst) | reinterpret_cast<uintptr_t>(src)) & 15) == 0) {
+                        jobs.src[jobs.n] = src;
+                        jobs.dst[jobs.n] = static_cast<uint8_t*>(dev_dst);
+                        jobs.bytes[jobs.n] = n;
+                        if (++jobs.n == kCopyOutMax) {
+                            cuda_check(launch_copy_out(jobs, num_sms, stream), "textures_read");
+                            jobs.n = 0;
+                        }
+                    } else {
+                        cuda_check(cudaMemcpyAsync(it.dsts[k], src, n, cudaMemcpyDeviceToHost, stream), "textures_read");
+                    }
                 }
+                cuda_check(launch_copy_out(jobs, num_sms, stream), "textures_read");
                 cuda_check(cudaStreamSynchronize(stream), "textures_read sync");
                 break;
+            }
             case Item::FLUSH:
                 flush_buf.ensure(256ull << 20, &scratch_bytes);
                 cuda_check(cudaMemsetAsync(flush_buf.ptr, (int)(it.offset & 0xFF), flush_buf.size, stream), "flush");
