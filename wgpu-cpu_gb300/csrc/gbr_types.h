@@ -157,7 +157,7 @@ struct DrawDesc {
     uint32_t strip_table;    // first entry of this draw's strip table in BatchParams::strip_info
     uint32_t lod_var;        // extension-profile sampling: 1 + varying index of u (v follows), 0 = none
     uint32_t raster_rule;    // RASTER_RULE_SCANLINE / RASTER_RULE_EDGE
-    uint32_t _pad_f;
+    uint32_t fast_vcount;    // fast setup: every vertex index below this fetches its FastVs attributes in range
 };
 
 // Vertex stages the fast setup kernel specialises on: every input an f32 attribute of exactly
@@ -261,6 +261,7 @@ struct BatchParams {
     uint32_t split_cap_heavy, split_cap_items;
     uint32_t split_chunk;        // records per chunk work item (> 0 when split_heavy is set)
     uint32_t _pad_split;
+    const uint32_t* draw_base;   // [num_draws] prim_base of each draw, contiguous (null: read the descriptors)
 };
 
 }  // namespace gbr

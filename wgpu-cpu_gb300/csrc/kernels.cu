@@ -3,6 +3,7 @@
 // (setup -> scan -> fill -> raster) on a stream.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <mutex>
 
 #include "gbr.h"
@@ -175,6 +176,35 @@ uint32_t fast_vs_kind(const DrawDesc& d) {
     }
 }
 
+uint32_t fast_vs_vcount(const DrawDesc& d) {
+    // (location, bytes) of the attributes each FastVs shape fetches, as fast_vertex_in_range
+    struct Use { int loc; uint32_t bytes; };
+    Use u[3];
+    int n = 0;
+    switch (d.fast_vs) {
+        case FAST_VS_MVP_COLOR: u[n++] = {0, 12}; u[n++] = {1, 12}; break;
+        case FAST_VS_MVP_TEX: u[n++] = {0, 12}; u[n++] = {1, 12}; u[n++] = {2, 8}; break;
+        case FAST_VS_QUAD: u[n++] = {0, 12}; u[n++] = {1, 16}; break;
+        case FAST_VS_QUAD_F16: u[n++] = {0, 12}; u[n++] = {1, 8}; break;
+        case FAST_VS_CLIP: u[n++] = {0, 16}; u[n++] = {1, 16}; break;
+        case FAST_VS_TRIANGLE: return 0xFFFFFFFFu;
+        default: return 0;
+    }
+    // the last instance reads furthest (instance strides are not negative)
+    const uint64_t inst = d.instance_count ? (uint64_t)d.instance_start + d.instance_count - 1 : d.instance_start;
+    uint64_t count = 0xFFFFFFFFull;
+    for (int k = 0; k < n; ++k) {
+        const AttrDesc& a = d.attr[u[k].loc];
+        if (a.buffer < 0) return 0;
+        const uint64_t base = inst * d.vb_stride_instance[a.buffer] + a.offset + u[k].bytes;
+        const uint64_t size = d.vb_size[a.buffer];
+        if (base > size) return 0;
+        const uint64_t stride = d.vb_stride_vertex[a.buffer];
+        if (stride) count = std::min<uint64_t>(count, (size - base) / stride + 1);
+    }
+    return (uint32_t)count;
+}
+
 cudaError_t launch_batch(const BatchParams& bp, int tile, int warps, int num_sms, cudaStream_t s,
                          uint32_t* launches, cudaEvent_t* ev_raster, int kind) {
     return bp.raster_rule == RASTER_RULE_EDGE ? launch_batch_t<true>(bp, tile, warps, num_sms, s, launches, ev_raster, kind)
@@ -308,6 +338,7 @@ extern "C" GBR_API gbr_status gbr_render_triangles_noalloc(const float* clip_pos
     d.depth_write = state->depth_write_enabled;
     d.write_mask = 0xF;
     d.fast_vs = fast_vs_kind(d);
+    d.fast_vcount = fast_vs_vcount(d);
     TargetDesc t;
     std::memset(&t, 0, sizeof t);
     t.color = color_target;

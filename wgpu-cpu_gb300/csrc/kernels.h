@@ -32,6 +32,9 @@ uint32_t batch_kernel_launches(uint32_t total_prims, int tile, int warps, int ki
 
 // The FastVs shape of a resolved draw (FAST_VS_NONE when the fast setup path cannot run it).
 uint32_t fast_vs_kind(const DrawDesc& d);
+// Vertex indices below the result fetch every attribute of the draw's FastVs shape in range, for
+// every instance of the draw (0 when none does, or no shape applies).
+uint32_t fast_vs_vcount(const DrawDesc& d);
 
 // Places n coalesced writes: segment k copies desc[3k + 2] bytes from stage + desc[3k + 1] to the
 // device address desc[3k] (stage offsets are 16-byte aligned).

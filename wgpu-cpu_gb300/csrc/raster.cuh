@@ -33,11 +33,20 @@ __device__ __forceinline__ void raise_error(BatchStatus* st, uint32_t code, uint
     if (atomicCAS(&st->error, 0u, code) == 0u) st->error_detail = detail;
 }
 
-__device__ __forceinline__ uint32_t find_draw(const DrawDesc* draws, uint32_t n, uint32_t prim) {
-    uint32_t lo = 0, hi = n;
-    while (hi - lo > 1) {
-        uint32_t mid = (lo + hi) >> 1;
-        if (__ldg(&draws[mid].prim_base) <= prim) lo = mid; else hi = mid;
+// The draw of global primitive `prim`: a binary search over the draws' first primitives, in the
+// batch's contiguous table when it has one (a few cache lines) or else in the descriptors.
+__device__ __forceinline__ uint32_t find_draw(const BatchParams& bp, uint32_t prim) {
+    uint32_t lo = 0, hi = bp.num_draws;
+    if (bp.draw_base) {
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(bp.draw_base + mid) <= prim) lo = mid; else hi = mid;
+        }
+    } else {
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (__ldg(&bp.draws[mid].prim_base) <= prim) lo = mid; else hi = mid;
+        }
     }
     return lo;
 }
@@ -654,7 +663,7 @@ template <bool EDGE>
 __device__ __forceinline__ void setup_generic(const BatchParams& bp, uint32_t gp, const TriRecord*& coop) {
     if (bp.tile_hint) bp.tile_hint[gp] = TILE_HINT_WALK;  // k_fill reads the generic path's records
     TriRecord* prim_rec = rec_at(bp.records, bp.record_stride, gp);
-    const uint32_t di = find_draw(bp.draws, bp.num_draws, gp);
+    const uint32_t di = find_draw(bp, gp);
     const DrawDesc& d = bp.draws[di];
     const uint32_t local = gp - d.prim_base;
     const uint32_t inst = local / d.prims_per_instance;
@@ -942,9 +951,11 @@ __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc&
             vtx[k] = (uint32_t)v;
         }
     }
+    if (max(vtx[0], max(vtx[1], vtx[2])) >= d.fast_vcount) {  // past the draw's safe range: check each fetch
 #pragma unroll
-    for (int k = 0; k < 3; ++k)
-        if (!fast_vertex_in_range<FVS>(d, vtx[k], instance)) return false;
+        for (int k = 0; k < 3; ++k)
+            if (!fast_vertex_in_range<FVS>(d, vtx[k], instance)) return false;
+    }
     V4 pos[3];
     float var[3][NV];
 #pragma unroll
@@ -1059,7 +1070,7 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
                 gp - dc.d.prim_base < dc.d.prims_per_instance * dc.d.instance_count)
                 di = dc.id;
             else
-                di = find_draw(bp.draws, bp.num_draws, gp);
+                di = find_draw(bp, gp);
         }
         const uint32_t di0 = __shfl_sync(0xFFFFFFFFu, di, 0);
         const bool uniform = __all_sync(0xFFFFFFFFu, !live || di == di0);

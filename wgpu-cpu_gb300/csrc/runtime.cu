@@ -737,6 +737,7 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
     }
     for (int k = 0; k < 4; ++k) d.blend_constant[k] = (float)dc.blend_constant[k];
     d.fast_vs = fast_vs_kind(d);
+    d.fast_vcount = fast_vs_vcount(d);
     return d;
 }
 
@@ -1355,7 +1356,9 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
     for (size_t i = from; i < nb; ++i) {
         kinds[i] = fragment_kind(batches[i], cfg.raster_order == GBR_RASTER_AUTO);
         desc_off[i] = cur;
-        cur = align(cur + batches[i].draws.size() * sizeof(DrawDesc) + batches[i].targets.size() * sizeof(TargetDesc));
+        // descriptors, targets, then the draws' first primitives as one contiguous table
+        cur = align(cur + batches[i].draws.size() * (sizeof(DrawDesc) + sizeof(uint32_t)) +
+                    batches[i].targets.size() * sizeof(TargetDesc));
         if (kinds[i] == 3) {
             states_off[i] = cur;
             cur = align(cur + batches[i].draws.size() * raster_state_bytes());
@@ -1374,6 +1377,9 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
             td.frag_count = reinterpret_cast<unsigned long long*>(meta + off_counters) + counter_first[i] + t;
             std::memcpy(tp + t, &td, sizeof td);
         }
+        uint8_t* bases = p + batches[i].draws.size() * sizeof(DrawDesc) + batches[i].targets.size() * sizeof(TargetDesc);
+        for (size_t k = 0; k < batches[i].draws.size(); ++k)
+            std::memcpy(bases + k * sizeof(uint32_t), &batches[i].draws[k].prim_base, sizeof(uint32_t));
     }
     cuda_check(cudaMemcpyAsync(meta, host_meta.data(), cur, cudaMemcpyHostToDevice, stream), "upload descriptors");
 
@@ -1445,6 +1451,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 bp.draws = reinterpret_cast<const DrawDesc*>(meta + desc_off[i]);
                 bp.targets =
                     reinterpret_cast<const TargetDesc*>(meta + desc_off[i] + b.draws.size() * sizeof(DrawDesc));
+                bp.draw_base = reinterpret_cast<const uint32_t*>(meta + desc_off[i] + b.draws.size() * sizeof(DrawDesc) +
+                                                                 b.targets.size() * sizeof(TargetDesc));
                 bp.num_draws = (uint32_t)b.draws.size();
                 bp.num_targets = (uint32_t)b.targets.size();
                 bp.total_prims = b.total_prims;
