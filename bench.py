@@ -5,7 +5,7 @@
 One step = one render pass (one frame) of the workload, submitted through the library's queue.
 
 Workloads (seeded synthetic inputs with the configurations' shapes; no dataset exists):
-  textured (default)  displaced icosphere subdivided 6 times (81,920 triangles; f32x3 position,
+  textured            displaced icosphere subdivided 6 times (81,920 triangles; f32x3 position,
                       f32x3 normal, f32x2 UV), 1024x1024 Rgba8UnormSrgb checker x value-noise
                       texture, texture x Lambert shading, 1920x1080 Rgba8UnormSrgb + Depth32Float
                       (Less).  Parity profile: nearest sampling, sRGB formats read and written as
@@ -20,11 +20,14 @@ Workloads (seeded synthetic inputs with the configurations' shapes; no dataset e
                       nor f16 targets).  The fill-rate-bound configuration.
   colored             UV sphere 32x16 (992 triangles), per-vertex colours, back-face cull,
                       512x512 Rgba8Unorm (the reference's CPU-runnable configuration).
-  batched             256 draws into 64 render targets (sides log-uniform in [128, 2048], triangle
+  batched (default)   256 draws into 64 render targets (sides log-uniform in [128, 2048], triangle
                       counts log-uniform in [100, 200k], random model rotations, half textured x
                       Lambert and half vertex-colour programs), Rgba8Unorm + Depth32Float (Less),
-                      one command buffer.  Besides the batched launch sequence the line reports
-                      the same command buffer launched per draw, the plain path it replaces.
+                      one command buffer, replayed from a CUDA graph with the tile shape chosen by
+                      the device's autotuner (its trial submissions run before warm-up; `--fixed`
+                      or `--tile/--warps` run a fixed shape without graphs).  Besides the batched
+                      launch sequence the line reports the same command buffer launched per draw,
+                      the plain path it replaces, at the same tile shape.
 
 `value` is shaded fragments per second (fragment-shader invocations, counted as the reference
 counts them) with every input resident in HBM, over the device time of the K steps (CUDA events on
@@ -217,15 +220,20 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def raster_traffic(name):
-    """DRAM bytes per raster launch from the committed ncu summary of this workload, if any."""
+def raster_profile(name):
+    """The committed ncu summary of this workload's raster kernel ({} when there is none)."""
     p = os.path.join(ROOT, "profiles", f"raster_{name}.json")
     if os.path.exists(p):
         try:
-            return json.load(open(p)).get("dram_bytes_per_launch")
+            return json.load(open(p))
         except (OSError, ValueError):
-            return None
-    return None
+            return {}
+    return {}
+
+
+def raster_traffic(name):
+    """DRAM bytes per raster launch from the committed ncu summary of this workload, if any."""
+    return raster_profile(name).get("dram_bytes_per_launch")
 
 
 def cpu_baseline(wk: Workload, target_seconds: float = 12.0):
@@ -282,6 +290,10 @@ def run_ours(args, wk: Workload):
     scene.record(enc)
     cmd = enc.finish()
 
+    if args.autotune:  # the tuner's trial submissions (one per candidate tile shape), before warm-up
+        for _ in range(TUNE_TRIALS):
+            dev.flush_caches()
+            dev.poll(True, dev.queue.submit([cmd]))
     for _ in range(args.warmup):
         dev.flush_caches()
         idx = dev.queue.submit([cmd])
@@ -311,8 +323,10 @@ def run_ours(args, wk: Workload):
     # the same command buffer on the plain per-draw path (one launch sequence per draw)
     per_draw = None
     if wk.name == "batched" and args.launch_mode != "per_draw" and not args.no_per_draw:
-        d2 = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True, tile_size=dev_tile(args),
-                      warps_per_tile=dev_warps(args), launch_mode=W.LaunchMode.PER_DRAW)
+        shape = stats[-1].tile_shape  # the batched arm's tile shape (the tuner's choice when autotuned)
+        d2 = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True,
+                      tile_size=(shape >> 8) or dev_tile(args), warps_per_tile=(shape & 0xFF) or dev_warps(args),
+                      launch_mode=W.LaunchMode.PER_DRAW)
         scene2 = wk.build(d2, **over)
         enc2 = d2.create_command_encoder()
         scene2.record(enc2)
@@ -376,14 +390,14 @@ def run_ours(args, wk: Workload):
             "warmup": args.warmup, "ms_per_step": float(np.mean(gpu_ms)), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": wk.dtype, "data": "synthetic (seeded)",
             "config": {**wk.config(launch_mode=args.launch_mode, graphs=args.graphs),
-                       "tile": dev_tile(args) if not args.autotune else "autotuned",
-                       "warps_per_tile": dev_warps(args) if not args.autotune else "autotuned",
+                       "tile": dev_tile(args) if not args.autotune else f"autotuned: {stats[-1].tile_shape >> 8}",
+                       "warps_per_tile": dev_warps(args) if not args.autotune else f"autotuned: {stats[-1].tile_shape & 0xFF}",
                        **over},
             "fragments_per_step": frags_per_step, "wall_ms_per_step": wall * 1e3 / args.steps,
             "generic_setup_prims_per_step": int(stats[-1].generic_setup_prims),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak if achieved else None, "traffic": raster_traffic(wk.name) if not over else None,
-                         "peak_source": peak_src, "kernel": "k_raster (tile sort + raster + shade + depth/blend + ROP)",
+                         "peak_source": peak_src, "kernel": raster_profile(wk.name).get("kernel", "raster kernel (k_raster_vis or k_raster)"),
                          "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": r_ms},
             "cpu_baseline": base,
             "e2e": {"value": frags_per_step / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
@@ -481,6 +495,9 @@ def run_serve(args):
         print(json.dumps(line), flush=True)
 
 
+TUNE_TRIALS = 6  # the library times five candidate tile shapes per batch shape, then keeps the fastest
+
+
 def dev_tile(args):
     return args.tile or 16
 
@@ -509,8 +526,14 @@ def main():
     ap.add_argument("--targets", type=int, default=0, help="batched workload: number of targets (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-per-draw", action="store_true", help="batched workload: skip the per-draw comparison")
+    ap.add_argument("--fixed", action="store_true",
+                    help="batched workload: no CUDA graph and no autotuner (the workload's fixed tile shape)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
+    if args.workload == "batched" and not args.fixed and not args.tile and args.impl == "ours":
+        # the configuration as specified: one launch sequence captured in a CUDA graph, tile shape
+        # and warps per tile chosen by the device's autotuner (its trials run before warm-up)
+        args.autotune = args.graphs = True
     if args.autotune:
         args.tile = args.warps = 0
     elif not args.tile and args.workload in workloads():

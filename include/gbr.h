@@ -331,7 +331,7 @@ typedef struct gbr_submission_stats {
     uint32_t generic_setup_prims;  /* primitives set up by the generic (clipping) setup kernel */
     double raster_ms;              /* device time of the raster kernels (config.time_kernels) */
     uint32_t split_tile_chunks;    /* visibility raster: work items of tiles split by record count */
-    uint32_t _reserved;
+    uint32_t tile_shape;           /* tile side << 8 | warps per tile of the submission's largest batch */
 } gbr_submission_stats;
 
 /* ---------------------------------------------------------------- command stream

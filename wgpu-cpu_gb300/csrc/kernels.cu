@@ -138,7 +138,9 @@ bool raster_config_supported(int tile, int warps) {
 
 uint32_t batch_kernel_launches(uint32_t total_prims, int tile, int warps, int kind) {
     if (kind == 3 && !launch_detail::vis_config_supported(tile, warps)) kind = 0;
-    return 2u + (total_prims ? 4u : 0u) + (kind == 3 ? 1u : 0u);
+    // scan + raster, setup + generic setup + fill when there are primitives, the states of the
+    // visibility raster (the strip table is counted by the caller)
+    return 2u + (total_prims ? 3u : 0u) + (kind == 3 ? 1u : 0u);
 }
 
 uint32_t fast_vs_kind(const DrawDesc& d) {

@@ -282,6 +282,7 @@ struct GroupRun {
     uint32_t launches = 0;
     uint64_t slow_prims = 0;
     uint64_t split_chunks = 0;  // chunk work items of split visibility-raster tiles
+    uint32_t tile_shape = 0, tile_shape_prims = 0;  // side << 8 | warps of the largest batch
     double raster_ms = 0.0;
 };
 
@@ -501,12 +502,11 @@ int fragment_kind(const Batch& b, bool allow_visibility) {
 }
 
 // Tile shapes (side, warps per tile) the autotuner tries, all compiled into kernels.cu: for the
-// ordered kernels, and for the visibility raster (which favours fewer warps per tile).
-// The first is the shape used before any measurement.  The tuner times the raster kernel, so it
-// sweeps 16- and 32-pixel tiles (binning costs the same or less there) and warps per tile; 8x8
-// tiles, whose four-fold bins the raster time does not show, are chosen through the config.
+// ordered kernels, and for the visibility raster.  The first is the shape used before any
+// measurement.  The tuner times each batch's whole launch sequence (setup, binning and raster:
+// the tile side changes the binning cost as well), one candidate per submission of a batch shape.
 const int kTuneCands[][2] = {{16, 8}, {32, 8}, {32, 4}, {16, 4}, {16, 2}};
-const int kTuneCandsVis[][2] = {{16, 2}, {16, 4}, {32, 4}, {16, 1}, {32, 2}};
+const int kTuneCandsVis[][2] = {{32, 8}, {16, 4}, {32, 4}, {16, 2}, {16, 1}};
 constexpr int kNumTuneCands = 5;
 
 uint64_t log2_bucket(uint64_t v) {
@@ -1049,6 +1049,7 @@ void Device::execute_group(std::vector<Item>& items) {
         rec.stats.raster_ms = run.raster_ms;
         rec.stats.generic_setup_prims = (uint32_t)std::min<uint64_t>(run.slow_prims, 0xFFFFFFFFu);
         rec.stats.split_tile_chunks = (uint32_t)std::min<uint64_t>(run.split_chunks, 0xFFFFFFFFu);
+        rec.stats.tile_shape = run.tile_shape;
         rec.ev = run.started ? run.ev : nullptr;
         records[items[i].index] = rec;
         completed_submissions = std::max(completed_submissions, items[i].index + 1);
@@ -1403,6 +1404,13 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         rev.resize(2 * nb);
         for (auto& e : rev) cuda_check(cudaEventCreate(&e), "event");
     }
+    // the whole launch sequence of each batch the tuner times (tile shapes change binning too)
+    std::vector<cudaEvent_t> tev;
+    EventGuard tev_guard{&tev};
+    if (any_tuning) {
+        tev.resize(2 * nb);
+        for (auto& e : tev) cuda_check(cudaEventCreate(&e), "event");
+    }
     for (int attempt = 0; attempt < 12; ++attempt) {
         // scratch for the remaining batches
         uint32_t max_prims = 0, max_tiles = 0, max_stride = 0, max_strip = 0;
@@ -1497,6 +1505,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                     if (ev) cuda_check(cudaEventRecord(ev[1], stream), "event");
                     continue;
                 }
+                const bool timed = !tev.empty() && tuning[i] >= 0;
+                if (timed) cuda_check(cudaEventRecord(tev[2 * i], stream), "event");
                 if (b.lines)
                     cuda_check(b.jit ? launch_lines_jit(*b.jit, bp, num_sms, stream, &run.launches, ev)
                                      : launch_lines(bp, num_sms, stream, &run.launches, ev),
@@ -1506,6 +1516,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 else
                     cuda_check(launch_batch(bp, btile[i], bwarps[i], num_sms, stream, &run.launches, ev, kinds[i]),
                                "launch");
+                if (timed) cuda_check(cudaEventRecord(tev[2 * i + 1], stream), "event");
             }
         };
         bool any_copy = false;  // a captured graph would keep a copy's addresses: no graphs then
@@ -1568,7 +1579,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 revp = &g.events;
                 for (size_t i = first_batch; i < nb; ++i)
                     run.launches += batches[i].lines ? 2u : (batches[i].strip_entries ? 1u : 0u) +
-                                    (batches[i].jit ? 2u + (batches[i].total_prims ? 4u : 0u) + (kinds[i] == 3 ? 1u : 0u)
+                                    (batches[i].jit ? 2u + (batches[i].total_prims ? 3u : 0u) + (kinds[i] == 3 ? 1u : 0u)
                                                     : batch_kernel_launches(batches[i].total_prims, btile[i], bwarps[i],
                                                                             kinds[i]));
             }
@@ -1598,12 +1609,17 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                                   counters.begin() + (ptrdiff_t)(counter_first[i] + b.targets.size()));
             run.slow_prims += st[i].slow_count;
             run.split_chunks += st[i].split_items;
+            if (!b.copy && !b.lines && (!run.tile_shape || b.total_prims > run.tile_shape_prims)) {
+                run.tile_shape = (uint32_t)btile[i] << 8 | (uint32_t)bwarps[i];
+                run.tile_shape_prims = b.total_prims;
+            }
             if (!revp->empty()) {
                 float ms = 0.0f;
-                if (cudaEventElapsedTime(&ms, (*revp)[2 * i], (*revp)[2 * i + 1]) == cudaSuccess) {
-                    run.raster_ms += ms;
-                    if (tuning[i] >= 0) tuner_record(b, tuning[i], ms);
-                }
+                if (cudaEventElapsedTime(&ms, (*revp)[2 * i], (*revp)[2 * i + 1]) == cudaSuccess) run.raster_ms += ms;
+            }
+            if (!tev.empty() && tuning[i] >= 0 && !b.copy) {
+                float ms = 0.0f;
+                if (cudaEventElapsedTime(&ms, tev[2 * i], tev[2 * i + 1]) == cudaSuccess) tuner_record(b, tuning[i], ms);
             }
         }
         if (bad == nb) return RunResult{nb, 0, {}};
