@@ -271,37 +271,51 @@ __device__ __forceinline__ void span_at(const TriRecord& r, int y, int& x1, int&
     x2 = (int)(a < b ? b : a);
 }
 
+// The rows [lo, hi] a record can emit into, clipped to the scissor and the target (lo > hi: none).
+__device__ __forceinline__ void record_rows(const TriRecord& r, const DrawDesc& d, const TargetDesc& t, int& lo, int& hi) {
+    lo = max(r.row0, (int)d.sc_y0);
+    hi = min(r.row1, min((int)d.sc_y1 - 1, (int)t.height - 1));
+}
+
+// The tile columns [c0, c1] of tile row ty (within rows [lo, hi]) the record can emit into: the
+// spans at the row band's ends and around the middle vertex bound the band's pixels (c0 > c1: none).
+template <bool EDGE>
+__device__ __forceinline__ void tile_row_cols(const TriRecord& r, const DrawDesc& d, const TargetDesc& t, uint32_t shift,
+                                              int lo, int hi, int ty, int& c0, int& c1) {
+    const int T = 1 << shift;
+    const int y0 = max(lo, ty << shift), y1 = min(hi, (ty << shift) + T - 1);
+    int xa, xb, mn, mx;
+    span_at<EDGE>(r, y0, xa, xb);
+    mn = xa; mx = xb;
+    span_at<EDGE>(r, y1, xa, xb);
+    mn = min(mn, xa); mx = max(mx, xb);
+    const int by = r.sy[1];
+    if (by - 1 >= y0 && by - 1 <= y1) {
+        span_at<EDGE>(r, by - 1, xa, xb);
+        mn = min(mn, xa); mx = max(mx, xb);
+    }
+    if (by >= y0 && by <= y1) {
+        span_at<EDGE>(r, by, xa, xb);
+        mn = min(mn, xa); mx = max(mx, xb);
+    }
+    mn = max(mn, (int)d.sc_x0);
+    mx = min(mx, min((int)d.sc_x1 - 1, (int)t.width - 1));
+    c0 = mn > mx ? 1 : mn >> shift;
+    c1 = mn > mx ? 0 : mx >> shift;
+}
+
 // Calls f(tile_index_in_target) for every tile whose pixels the record can emit.
 // Tile rows are visited from `first` in steps of `step` (1, or 32 when a warp shares a record).
 template <bool EDGE, class F>
 __device__ __forceinline__ void for_each_tile(const TriRecord& r, const DrawDesc& d, const TargetDesc& t, uint32_t shift,
                                               F&& f, int first = 0, int step = 1) {
-    int lo = max(r.row0, (int)d.sc_y0);
-    int hi = min(r.row1, min((int)d.sc_y1 - 1, (int)t.height - 1));
+    int lo, hi;
+    record_rows(r, d, t, lo, hi);
     if (lo > hi) return;
-    const int T = 1 << shift;
-    const int sx_hi = min((int)d.sc_x1 - 1, (int)t.width - 1);
-    const int sx_lo = (int)d.sc_x0;
     for (int ty = (lo >> shift) + first; ty <= (hi >> shift); ty += step) {
-        int y0 = max(lo, ty << shift), y1 = min(hi, (ty << shift) + T - 1);
-        int xa, xb, mn, mx;
-        span_at<EDGE>(r, y0, xa, xb);
-        mn = xa; mx = xb;
-        span_at<EDGE>(r, y1, xa, xb);
-        mn = min(mn, xa); mx = max(mx, xb);
-        const int by = r.sy[1];
-        if (by - 1 >= y0 && by - 1 <= y1) {
-            span_at<EDGE>(r, by - 1, xa, xb);
-            mn = min(mn, xa); mx = max(mx, xb);
-        }
-        if (by >= y0 && by <= y1) {
-            span_at<EDGE>(r, by, xa, xb);
-            mn = min(mn, xa); mx = max(mx, xb);
-        }
-        mn = max(mn, sx_lo);
-        mx = min(mx, sx_hi);
-        if (mn > mx) continue;
-        for (int tx = mn >> shift; tx <= (mx >> shift); ++tx) f((uint32_t)ty * t.tiles_x + (uint32_t)tx);
+        int c0, c1;
+        tile_row_cols<EDGE>(r, d, t, shift, lo, hi, ty, c0, c1);
+        for (int tx = c0; tx <= c1; ++tx) f((uint32_t)ty * t.tiles_x + (uint32_t)tx);
     }
 }
 
@@ -539,6 +553,10 @@ __device__ __forceinline__ void count_tiles(const BatchParams& bp, const TriReco
 __device__ __forceinline__ bool tiles_are_many(const TriRecord& r, uint32_t shift) {
     return (r.row1 >> shift) - (r.row0 >> shift) >= 2;
 }
+// Tiles of the record's unclipped bounding box (an upper bound of the tiles it emits into).
+__device__ __forceinline__ uint32_t bbox_tiles(const TriRecord& r, uint32_t shift) {
+    return (uint32_t)((r.row1 >> shift) - (r.row0 >> shift) + 1) * (uint32_t)((r.xmax >> shift) - (r.xmin >> shift) + 1);
+}
 
 // Binning hint of a primary record, written by the fast setup so that k_fill need not read the
 // record back: the record covers nothing, exactly one tile (its global index), or anything else.
@@ -563,6 +581,54 @@ __device__ __forceinline__ void coop_tiles(const BatchParams& bp, const TriRecor
         const TargetDesc& t = bp.targets[d.target];
         const uint32_t key = r->key;
         for_each_tile<EDGE>(*r, d, t, bp.tile_shift, [&](uint32_t lt) { f(t.tile_base + lt, key); }, (int)lane, 32);
+    }
+}
+
+// The tiles of the lanes' records (mine, or null) walked by the whole warp, one record at a time,
+// in row-major order 32 tiles per pass: the column ranges of up to 32 tile rows are computed one
+// row per lane, a warp scan numbers the rows' tiles, and each lane finds the row of its tile by a
+// shuffle search — the tiles for_each_tile visits, for records wide or tall alike.
+template <bool EDGE, class F>
+__device__ __forceinline__ void coop_tiles_flat(const BatchParams& bp, const TriRecord* mine, uint32_t lane, F&& f) {
+    constexpr unsigned kFull = 0xFFFFFFFFu;
+    uint32_t todo = __ballot_sync(kFull, mine != nullptr);
+    while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        __syncwarp();  // the record was written by lane `src`
+        const TriRecord* r = reinterpret_cast<const TriRecord*>(
+            __shfl_sync(kFull, reinterpret_cast<unsigned long long>(mine), src));
+        const DrawDesc& d = bp.draws[r->draw];
+        const TargetDesc& t = bp.targets[d.target];
+        const uint32_t key = r->key;
+        int lo, hi;
+        record_rows(*r, d, t, lo, hi);
+        if (lo > hi) continue;  // warp-uniform
+        const int ty_hi = hi >> bp.tile_shift;
+        for (int base = lo >> bp.tile_shift; base <= ty_hi; base += 32) {
+            const int ty = base + (int)lane;
+            int c0 = 1, c1 = 0;
+            if (ty <= ty_hi) tile_row_cols<EDGE>(*r, d, t, bp.tile_shift, lo, hi, ty, c0, c1);
+            const uint32_t n = c1 >= c0 ? (uint32_t)(c1 - c0 + 1) : 0u;
+            uint32_t incl = n;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t v = __shfl_up_sync(kFull, incl, o);
+                if (lane >= (uint32_t)o) incl += v;
+            }
+            const uint32_t total = __shfl_sync(kFull, incl, 31), excl = incl - n;
+            for (uint32_t k0 = 0; k0 < total; k0 += 32) {  // warp-uniform
+                const uint32_t k = k0 + lane;
+                int row = 0;  // the last lane whose first tile number is <= k (it has tiles)
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1)
+                    if (__shfl_sync(kFull, excl, row + step) <= k) row += step;
+                const int rc0 = __shfl_sync(kFull, c0, row);
+                const uint32_t rexcl = __shfl_sync(kFull, excl, row);
+                if (k < total)
+                    f(t.tile_base + (uint32_t)(base + row) * t.tiles_x + (uint32_t)rc0 + (k - rexcl), key);
+            }
+        }
     }
 }
 
@@ -1313,8 +1379,8 @@ __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
             const TriRecord* r = i < bp.total_prims ? rec_at(bp.records, bp.record_stride, i)
                                                     : rec_at(bp.ovf_records, bp.record_stride, i - bp.total_prims);
             if (!(r->flags & 2u)) {
-                if (tiles_are_many(*r, bp.tile_shift)) {
-                    coop = r;
+                if (tiles_are_many(*r, bp.tile_shift) || bbox_tiles(*r, bp.tile_shift) > 8u) {
+                    coop = r;  // the warp walks it (coop_tiles_flat below)
                 } else {
                     const DrawDesc& d = bp.draws[r->draw];
                     const TargetDesc& t = bp.targets[d.target];
@@ -1325,7 +1391,7 @@ __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
                 }
             }
         }
-        coop_tiles<EDGE>(bp, coop, lane, put);
+        coop_tiles_flat<EDGE>(bp, coop, lane, put);
     }
 }
 
