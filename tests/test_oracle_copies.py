@@ -77,3 +77,45 @@ def test_write_buffers_falls_back_to_single_writes():
     for _, off, data in items:
         want[off:off + data.size] = data
     assert np.array_equal(out, want)
+
+
+def test_prepared_writes_accept_any_buffer():
+    """PreparedWrites takes bytes, bytearrays, memoryviews and non-contiguous arrays (copied to a
+    contiguous array it keeps), and contiguous arrays by reference: the bytes written are the
+    array's contents at each write_buffers call."""
+    import ctypes
+
+    dev = oracle_device.device(profile=W.Profile.EXTENSION)
+    buf = dev.create_buffer_init(np.zeros(64, np.uint8))
+    live = np.zeros(8, np.uint8)
+    strided = np.arange(32, dtype=np.uint8)[::2]  # not contiguous
+    items = [(buf, 0, b"\x01\x02\x03\x04"), (buf, 4, bytearray(b"\x05\x06")), (buf, 8, memoryview(b"\x07" * 4)),
+             (buf, 16, strided), (buf, 40, live), (buf, 60, b"")]
+    prepared = W.PreparedWrites(items)
+    live[:] = 9  # after preparing: the contiguous array is read when written
+    dev.queue.write_buffers(prepared)
+    out = np.empty(64, np.uint8)
+    assert dev.lib.buffer_read(dev.handle, buf.handle, 0, out.ctypes.data_as(ctypes.c_void_p), out.nbytes) == 0
+    want = np.zeros(64, np.uint8)
+    want[0:4] = [1, 2, 3, 4]
+    want[4:6] = [5, 6]
+    want[8:12] = 7
+    want[16:32] = strided
+    want[40:48] = 9
+    assert np.array_equal(out, want)
+
+
+def test_buffer_init_from_strided_array():
+    """create_buffer_init and write_buffer take a non-contiguous array's elements in order."""
+    import ctypes
+
+    dev = oracle_device.device(profile=W.Profile.EXTENSION)
+    src = np.arange(40, dtype=np.float32).reshape(8, 5)[:, 1:4]  # 8 x 3, not contiguous
+    buf = dev.create_buffer_init(src)
+    assert buf.size == src.nbytes
+    out = np.empty(src.size, np.float32)
+    assert dev.lib.buffer_read(dev.handle, buf.handle, 0, out.ctypes.data_as(ctypes.c_void_p), out.nbytes) == 0
+    assert np.array_equal(out, src.reshape(-1))
+    dev.queue.write_buffer(buf, 0, src[::-1])
+    assert dev.lib.buffer_read(dev.handle, buf.handle, 0, out.ctypes.data_as(ctypes.c_void_p), out.nbytes) == 0
+    assert np.array_equal(out, src[::-1].reshape(-1))

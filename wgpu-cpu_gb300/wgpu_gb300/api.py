@@ -492,6 +492,17 @@ class RenderPassEncoder:
 
 
 # ------------------------------------------------------------------------------------ device
+def _byte_array(data) -> np.ndarray:
+    """The bytes of `data` as a contiguous uint8 array: a contiguous ndarray is viewed, not copied;
+    other arrays and buffer objects (bytes, bytearray, memoryview, ...) are copied when needed."""
+    if isinstance(data, np.ndarray):
+        return np.ascontiguousarray(data).reshape(-1).view(np.uint8)
+    mv = memoryview(data)
+    if not mv.c_contiguous:
+        return np.frombuffer(mv.tobytes(), dtype=np.uint8)
+    return np.frombuffer(mv.cast("B"), dtype=np.uint8)
+
+
 class PreparedWrites:
     """A fixed list of buffer writes [(buffer, offset, data)] for Queue.write_buffers: the data
     arrays are referenced, not copied, and their contents at each write_buffers call are what
@@ -501,7 +512,7 @@ class PreparedWrites:
         self.items = []
         for buf, off, data in items:
             if not (isinstance(data, np.ndarray) and data.flags.c_contiguous):
-                data = np.ascontiguousarray(np.frombuffer(memoryview(data).cast("B"), dtype=np.uint8))
+                data = _byte_array(data)
             self.items.append((buf, int(off), data))
         self.array = (A.BufferWrite * max(1, len(self.items)))()
         for k, (buf, off, data) in enumerate(self.items):
@@ -531,12 +542,12 @@ class Queue:
             _check(d.lib, d.lib.queue_write_buffer(d.handle, buffer.handle, offset,
                                                    data.__array_interface__["data"][0], data.nbytes))
             return
-        arr = np.ascontiguousarray(np.frombuffer(memoryview(data).cast("B"), dtype=np.uint8))
+        arr = _byte_array(data)
         _check(d.lib, d.lib.queue_write_buffer(d.handle, buffer.handle, offset, arr.ctypes.data, arr.nbytes))
 
     def write_texture(self, texture: Texture, data, bytes_per_row: int = 0, rows_per_image: int = 0,
                       mip_level: int = 0, offset: int = 0) -> None:
-        arr = np.ascontiguousarray(np.frombuffer(memoryview(data).cast("B"), dtype=np.uint8))
+        arr = _byte_array(data)
         w, h = texture.mip_size(mip_level)
         layout = A.TexelCopyBufferLayout(offset, bytes_per_row or w * BYTES_PER_TEXEL[texture.format],
                                          rows_per_image or h)
@@ -617,8 +628,8 @@ class Device:
         return b
 
     def create_buffer_init(self, data, usage: int = 0) -> Buffer:
-        mv = memoryview(data).cast("B")
-        return self.create_buffer(len(mv), usage, mv)
+        arr = _byte_array(data)
+        return self.create_buffer(arr.nbytes, usage, arr)
 
     def create_texture(self, width: int, height: int, format: int, mip_level_count: int = 1, layers: int = 1,
                        usage: int = 0) -> Texture:
