@@ -3,8 +3,8 @@
  *
  * Every entry point below replaces one method of the wgpu 28 "custom backend" traits that
  * wgpu-cpu implements in Rust.  The reference method is cited beside each declaration as
- * `file:line` relative to the wgpu-cpu repository.  A Rust `wgpu::custom` shim would bind these
- * symbols with `extern "C"` declarations (see INTEGRATION.md for the binding stubs).
+ * `file:line` relative to the wgpu-cpu repository.  A Rust `wgpu::custom` shim binds these
+ * symbols with `extern "C"` declarations and forwards each trait method to one of them.
  *
  * Conventions
  *  - Objects are opaque 64-bit handles owned by the library; 0 is never a valid handle.
@@ -635,8 +635,11 @@ GBR_API gbr_status gbr_selftest_division(uint64_t samples, uint64_t seed, uint64
  * Every call shares that one scratch array and overwrites what the previous call left there,
  * so calls whose GPU work overlaps (two host threads, or two streams) race with each other:
  * serialise them.  The first call on a device looks up the array's device address (once per
- * device, with that device current); make that first call before any stream capture.  The
- * call returns after the work on `stream` has finished.
+ * device, with that device current); make that first call before any stream capture.  Every
+ * call ends by reading its status back to the host and waiting for `stream`, so it returns after
+ * the work on `stream` has finished, and it cannot be made while `stream` is being captured
+ * into a CUDA graph.  color_load_op and depth_load_op must be GBR_LOAD_OP_LOAD or
+ * GBR_LOAD_OP_CLEAR (anything else returns GBR_ERR_INVALID_ARGUMENT).
  *
  *   clip_positions  device pointer, 3 * triangle_count float4 (x, y, z, w), 16-byte aligned
  *   colors          device pointer, 3 * triangle_count float4 (r, g, b, a), 16-byte aligned

@@ -52,6 +52,19 @@ struct Error {
     throw Error{st, buf};
 }
 
+// [offset, offset + size) inside [0, total) with no wrapping sum: the reference's try_into and
+// slice bounds (buffer.rs, device.rs:332-344) reject such ranges with a panic.
+static inline bool range_fits(uint64_t offset, uint64_t size, uint64_t total) {
+    return size <= total && offset <= total - size;
+}
+// a + b * c + d, or UINT64_MAX when it does not fit in 64 bits
+static inline uint64_t span_end(uint64_t a, uint64_t b, uint64_t c, uint64_t d) {
+    uint64_t p, s, r;
+    if (__builtin_mul_overflow(b, c, &p) || __builtin_add_overflow(a, p, &s) || __builtin_add_overflow(s, d, &r))
+        return UINT64_MAX;
+    return r;
+}
+
 // ---------------------------------------------------------------- texture formats
 // bytes_per_texel (texture.rs:456-505) for the formats this ABI exposes.
 static uint32_t bytes_per_texel(uint32_t f) {
@@ -524,8 +537,9 @@ static void resolve_bindings(Device* dev, const PassState& st, ProgramBindings& 
             if (en.binding >= 8) continue;
             if (en.kind == GBR_BINDING_BUFFER) {
                 Buffer* b = dev->get<Buffer>(en.resource, "buffer");
+                if (en.offset > b->data.size()) fail(GBR_ERR_VALIDATION, "bind group buffer range out of bounds");
                 uint64_t size = en.size ? en.size : b->data.size() - en.offset;
-                if (en.offset + size > b->data.size()) fail(GBR_ERR_VALIDATION, "bind group buffer range out of bounds");
+                if (!range_fits(en.offset, size, b->data.size())) fail(GBR_ERR_VALIDATION, "bind group buffer range out of bounds");
                 pb.uniform[g][en.binding] = b->data.data() + en.offset;
                 pb.uniform_size[g][en.binding] = size;
             } else if (en.kind == GBR_BINDING_TEXTURE_VIEW) {
@@ -1056,7 +1070,7 @@ static void run_pass_band(Exec* ex, const DecodedPass& dp) {
                 auto* p = payload<gbr_cmd_set_index_buffer>(&h, b);
                 Buffer* buf = dev->get<Buffer>(p->buffer, "buffer");
                 uint64_t size = p->size ? p->size : buf->data.size() - p->offset;
-                if (p->offset + size > buf->data.size()) fail(GBR_ERR_VALIDATION, "index buffer slice out of range");
+                if (!range_fits(p->offset, size, buf->data.size())) fail(GBR_ERR_VALIDATION, "index buffer slice out of range");
                 st.index = {buf, p->offset, size};
                 st.index_format = p->index_format;
                 break;
@@ -1066,7 +1080,7 @@ static void run_pass_band(Exec* ex, const DecodedPass& dp) {
                 if (p->slot >= GBR_MAX_VERTEX_BUFFERS) fail(GBR_ERR_VALIDATION, "vertex buffer slot");
                 Buffer* buf = dev->get<Buffer>(p->buffer, "buffer");
                 uint64_t size = p->size ? p->size : buf->data.size() - p->offset;
-                if (p->offset + size > buf->data.size()) fail(GBR_ERR_VALIDATION, "vertex buffer slice out of range");
+                if (!range_fits(p->offset, size, buf->data.size())) fail(GBR_ERR_VALIDATION, "vertex buffer slice out of range");
                 st.vb[p->slot] = {buf, p->offset, size};
                 break;
             }
@@ -1253,7 +1267,7 @@ ORC_API gbr_status orc_queue_write_buffer(gbr_device d, gbr_buffer b, uint64_t o
         Device* dev = get_device(d);
         std::lock_guard<std::mutex> lk(dev->mu);
         Buffer* buf = dev->get<Buffer>(b, "buffer");
-        if (offset + size > buf->data.size()) fail(GBR_ERR_VALIDATION, "write_buffer out of range");
+        if (!range_fits(offset, size, buf->data.size())) fail(GBR_ERR_VALIDATION, "write_buffer out of range");
         std::memcpy(buf->data.data() + offset, data, size);
     })
 }
@@ -1262,7 +1276,7 @@ ORC_API gbr_status orc_buffer_read(gbr_device d, gbr_buffer b, uint64_t offset, 
         Device* dev = get_device(d);
         std::lock_guard<std::mutex> lk(dev->mu);
         Buffer* buf = dev->get<Buffer>(b, "buffer");
-        if (offset + size > buf->data.size()) fail(GBR_ERR_VALIDATION, "buffer read out of range");
+        if (!range_fits(offset, size, buf->data.size())) fail(GBR_ERR_VALIDATION, "buffer read out of range");
         std::memcpy(dst, buf->data.data() + offset, size);
     })
 }
@@ -1312,8 +1326,8 @@ ORC_API gbr_status orc_queue_write_texture(gbr_device d, gbr_texture tex, uint32
         uint8_t* dst = t->mips[mip].data();
         for (uint32_t z = 0; z < layers; ++z)
             for (uint32_t y = 0; y < h; ++y) {
-                uint64_t so = layout->offset + (z * rows_per_image + y) * row;
-                if (so + dst_row > data_size) fail(GBR_ERR_VALIDATION, "write_texture source out of range");
+                uint64_t so = span_end(layout->offset, (uint64_t)z * rows_per_image + y, row, 0);
+                if (!range_fits(so, dst_row, data_size)) fail(GBR_ERR_VALIDATION, "write_texture source out of range");
                 std::memcpy(dst + ((uint64_t)z * h + y) * dst_row, src + so, dst_row);
             }
     })
@@ -1400,9 +1414,18 @@ ORC_API gbr_status orc_render_pipeline_destroy(gbr_device d, gbr_render_pipeline
 ORC_API gbr_status orc_bind_group_create(gbr_device d, const gbr_bind_group_desc* desc, gbr_bind_group* out) {
     ORC_TRY({
         Device* dev = get_device(d);
+        if (!desc || desc->entry_count > GBR_MAX_BIND_GROUP_ENTRIES) fail(GBR_ERR_INVALID_ARGUMENT, "bad descriptor");
+        std::lock_guard<std::mutex> lk(dev->mu);
+        // buffer entries must lie inside their buffer (a BufferSlice of the reference, bind_group.rs:58-72)
+        for (uint32_t e = 0; e < desc->entry_count; ++e) {
+            const gbr_bind_group_entry& en = desc->entries[e];
+            if (en.kind != GBR_BINDING_BUFFER) continue;
+            Buffer* b = dev->get<Buffer>(en.resource, "buffer");
+            if (en.offset > b->data.size() || (en.size && !range_fits(en.offset, en.size, b->data.size())))
+                fail(GBR_ERR_VALIDATION, "bind group buffer range out of bounds");
+        }
         auto* g = new BindGroup;
         g->desc = *desc;
-        std::lock_guard<std::mutex> lk(dev->mu);
         *out = dev->add(g);
     })
 }
@@ -1446,7 +1469,7 @@ static void execute_copy(Device* dev, const gbr_cmd_header& h, const uint8_t* b)
             if (src == dst) fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: source and destination are the same buffer");
             if (p->source_offset % 4 || p->destination_offset % 4 || size % 4)
                 fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: alignment");
-            if (p->source_offset + size > src->data.size() || p->destination_offset + size > dst->data.size())
+            if (!range_fits(p->source_offset, size, src->data.size()) || !range_fits(p->destination_offset, size, dst->data.size()))
                 fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: range out of bounds");
             std::memcpy(dst->data.data() + p->destination_offset, src->data.data() + p->source_offset, size);
             break;
@@ -1466,7 +1489,7 @@ static void execute_copy(Device* dev, const gbr_cmd_header& h, const uint8_t* b)
             if (bpr < width || rpi < e.height) fail(GBR_ERR_VALIDATION, "%s: layout smaller than the copy", kNames[k]);
             if (p->layout.offset % t->bpp) fail(GBR_ERR_VALIDATION, "%s: offset not a multiple of the texel size", kNames[k]);
             if (!e.width || !e.height || !e.depth_or_array_layers) break;
-            const uint64_t need = p->layout.offset + ((uint64_t)(e.depth_or_array_layers - 1) * rpi + (e.height - 1)) * bpr + width;
+            const uint64_t need = span_end(p->layout.offset, (uint64_t)(e.depth_or_array_layers - 1) * rpi + (e.height - 1), bpr, width);
             if (need > buf->data.size()) fail(GBR_ERR_VALIDATION, "%s: buffer range out of bounds", kNames[k]);
             for (uint32_t z = 0; z < e.depth_or_array_layers; ++z)
                 for (uint32_t y = 0; y < e.height; ++y) {
@@ -1506,7 +1529,7 @@ static void execute_copy(Device* dev, const gbr_cmd_header& h, const uint8_t* b)
             const uint64_t size = p->size == UINT64_MAX ? buf->data.size() - std::min<uint64_t>(p->offset, buf->data.size())
                                                         : p->size;
             if (p->offset % 4 || size % 4) fail(GBR_ERR_VALIDATION, "clear_buffer: alignment");
-            if (p->offset + size > buf->data.size()) fail(GBR_ERR_VALIDATION, "clear_buffer: range out of bounds");
+            if (!range_fits(p->offset, size, buf->data.size())) fail(GBR_ERR_VALIDATION, "clear_buffer: range out of bounds");
             std::memset(buf->data.data() + p->offset, 0, size);
             break;
         }

@@ -5,7 +5,8 @@ The reference is Rust and cannot be built here, so its unit tests are read as te
 matching, and the literal inputs / expected outputs are parsed with small regular expressions.
 Every record keeps the `file:line` of the test it came from.
 
-Run from the repository root:  python tests/golden/make_kats.py [/path/to/wgpu-cpu]
+Run from the repository root:  python tests/golden/make_kats.py /path/to/wgpu-cpu
+(or set WGPU_CPU_REPO to the checkout of the reference repository).
 """
 
 from __future__ import annotations
@@ -15,7 +16,14 @@ import re
 import sys
 from pathlib import Path
 
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+import os
+
+if len(sys.argv) > 1:
+    REF = Path(sys.argv[1])
+elif os.environ.get("WGPU_CPU_REPO"):
+    REF = Path(os.environ["WGPU_CPU_REPO"])
+else:
+    raise SystemExit("usage: make_kats.py /path/to/wgpu-cpu  (or set WGPU_CPU_REPO)")
 SRC = REF / "wgpu-cpu" / "src"
 OUT = Path(__file__).with_name("reference_kats.json")
 

@@ -183,7 +183,11 @@ JitKernels::~JitKernels() {
 }
 
 std::shared_ptr<JitKernels> jit_module(const std::string& code, bool edge, std::string* err) {
-    const std::string key = (edge ? "edge\n" : "scanline\n") + code;
+    // one module per device: the kernels' shared-memory attributes and occupancy below are
+    // per-device properties, so a module (and its cached launch settings) never serves two devices
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) dev = -1;
+    const std::string key = std::to_string(dev) + (edge ? "\nedge\n" : "\nscanline\n") + code;
     {
         std::lock_guard<std::mutex> lk(g_cache_mu);
         auto it = g_cache.find(key);

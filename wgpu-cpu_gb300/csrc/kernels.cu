@@ -284,6 +284,9 @@ extern "C" GBR_API gbr_status gbr_render_triangles_noalloc(const float* clip_pos
         return na_fail(GBR_ERR_INVALID_ARGUMENT, "misaligned device pointer");
     if (state->depth_compare > GBR_COMPARE_ALWAYS || state->cull_mode > GBR_CULL_BACK || state->front_face > 1)
         return na_fail(GBR_ERR_INVALID_ARGUMENT, "invalid raster state");
+    if ((state->color_load_op != GBR_LOAD_OP_LOAD && state->color_load_op != GBR_LOAD_OP_CLEAR) ||
+        (state->depth_load_op != GBR_LOAD_OP_LOAD && state->depth_load_op != GBR_LOAD_OP_CLEAR))
+        return na_fail(GBR_ERR_INVALID_ARGUMENT, "load op must be GBR_LOAD_OP_LOAD or GBR_LOAD_OP_CLEAR");
 
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);

@@ -21,6 +21,40 @@ namespace launch_detail {
 constexpr int kCap = 4096;  // keys per tile sorted in shared memory; larger bins sort in place
 constexpr int kRW = 64;     // records staged in shared memory per window
 
+// Launch configuration of one kernel, kept per CUDA device: cudaFuncSetAttribute applies to the
+// current device only, so the dynamic shared memory a kernel may use is raised on each device the
+// first time a launch there needs it, and its resident blocks per SM are looked up per device and
+// shared-memory size.
+struct LaunchCache {
+    std::mutex mu;
+    std::map<int, size_t> smem_allowed;              // device -> dynamic smem the kernel may use
+    std::map<std::pair<int, size_t>, int> resident;  // (device, dynamic smem) -> blocks per SM
+};
+
+// Blocks of `kern` an SM holds with `threads` threads and `smem` bytes of dynamic shared memory
+// on the current device (at least 1), raising the kernel's dynamic shared-memory limit first.
+template <class Kernel>
+cudaError_t resident_blocks(LaunchCache& c, Kernel kern, int threads, size_t smem, int* out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lk(c.mu);
+    auto allowed = c.smem_allowed.find(dev);
+    if (smem && (allowed == c.smem_allowed.end() || allowed->second < smem)) {
+        if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) != cudaSuccess)
+            return e;
+        c.smem_allowed[dev] = smem;
+    }
+    auto it = c.resident.find({dev, smem});
+    if (it == c.resident.end()) {
+        int blocks = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks, kern, threads, smem)) != cudaSuccess) return e;
+        it = c.resident.emplace(std::make_pair(dev, smem), std::max(blocks, 1)).first;
+    }
+    *out = it->second;
+    return cudaSuccess;
+}
+
 template <int T, int W, int KIND, bool EDGE>
 cudaError_t launch_raster(const BatchParams& bp, int num_sms, cudaStream_t s) {
     if constexpr (EDGE && KIND == 2) {
@@ -28,20 +62,9 @@ cudaError_t launch_raster(const BatchParams& bp, int num_sms, cudaStream_t s) {
     } else {
     auto kern = k_raster<T, W, kCap, kRW, KIND, EDGE>;
     const size_t smem = (kCap + 2 * W * 32) * sizeof(uint32_t) + (size_t)kRW * bp.record_stride;
-    static std::mutex mu;
-    static size_t configured = 0;
-    static int blocks_per_sm = 0;
-    {
-        std::lock_guard<std::mutex> lk(mu);
-        if (configured < smem) {
-            cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (e != cudaSuccess) return e;
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, W * 32, smem);
-            if (e != cudaSuccess) return e;
-            if (blocks_per_sm < 1) blocks_per_sm = 1;
-            configured = smem;
-        }
-    }
+    static LaunchCache cache;
+    int blocks_per_sm = 1;
+    if (cudaError_t e = resident_blocks(cache, kern, W * 32, smem, &blocks_per_sm); e != cudaSuccess) return e;
     const uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)num_sms * blocks_per_sm, bp.total_tiles);
     kern<<<grid ? grid : 1, W * 32, smem, s>>>(bp);
     return cudaGetLastError();
@@ -51,16 +74,9 @@ cudaError_t launch_raster(const BatchParams& bp, int num_sms, cudaStream_t s) {
 template <int T, int W, bool EDGE>
 cudaError_t launch_raster_vis(const BatchParams& bp, int num_sms, cudaStream_t s) {
     auto kern = k_raster_vis<T, W, EDGE>;
-    static std::mutex mu;
-    static int blocks_per_sm = 0;
-    {
-        std::lock_guard<std::mutex> lk(mu);
-        if (blocks_per_sm == 0) {
-            cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, W * 32, 0);
-            if (e != cudaSuccess) return e;
-            if (blocks_per_sm < 1) blocks_per_sm = 1;
-        }
-    }
+    static LaunchCache cache;
+    int blocks_per_sm = 1;
+    if (cudaError_t e = resident_blocks(cache, kern, W * 32, 0, &blocks_per_sm); e != cudaSuccess) return e;
     const uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)num_sms * blocks_per_sm, bp.total_tiles);
     kern<<<grid ? grid : 1, W * 32, 0, s>>>(bp);
     return cudaGetLastError();
@@ -104,27 +120,9 @@ cudaError_t launch_batch_t(const BatchParams& bp, int tile, int warps, int num_s
     }
     if (items) {
         const size_t smem = setup_stage_bytes(bp.record_stride);
-        int resident = 0;  // k_setup blocks an SM holds at this stage size (grid-stride: one wave)
-        {
-            static std::mutex mu;
-            static size_t configured = 0;
-            static std::map<size_t, int> occupancy;
-            std::lock_guard<std::mutex> lk(mu);
-            if (configured < smem) {
-                if ((e = cudaFuncSetAttribute(k_setup<EDGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)) !=
-                    cudaSuccess)
-                    return e;
-                configured = smem;
-            }
-            auto it = occupancy.find(smem);
-            if (it == occupancy.end()) {
-                if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, k_setup<EDGE>, kSetupWarps * 32, smem)) !=
-                    cudaSuccess)
-                    return e;
-                it = occupancy.emplace(smem, std::max(resident, 1)).first;
-            }
-            resident = it->second;
-        }
+        int resident = 1;  // k_setup blocks an SM holds at this stage size (grid-stride: one wave)
+        static LaunchCache setup_cache;
+        if ((e = resident_blocks(setup_cache, k_setup<EDGE>, kSetupWarps * 32, smem, &resident)) != cudaSuccess) return e;
         const uint32_t g = std::min((items + 127) / 128, std::min(cap, (uint32_t)(resident * num_sms)));
         k_setup<EDGE><<<g, kSetupWarps * 32, smem, s>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;

@@ -54,6 +54,19 @@ void cuda_check(cudaError_t e, const char* what) {
     if (e != cudaSuccess) fail(GBR_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
 }
 
+// [offset, offset + size) inside [0, total), written so that no sum can wrap around 2^64
+// (the reference converts with try_into and slices, which panics on such ranges).
+inline bool range_fits(uint64_t offset, uint64_t size, uint64_t total) {
+    return size <= total && offset <= total - size;
+}
+// a + b * c + d without wrapping; UINT64_MAX when the true value does not fit (never "in range")
+inline uint64_t span_end(uint64_t a, uint64_t b, uint64_t c, uint64_t d) {
+    uint64_t p, s, r;
+    if (__builtin_mul_overflow(b, c, &p) || __builtin_add_overflow(a, p, &s) || __builtin_add_overflow(s, d, &r))
+        return UINT64_MAX;
+    return r;
+}
+
 using Clock = std::chrono::steady_clock;
 double ms_between(Clock::time_point a, Clock::time_point b) {
     return std::chrono::duration<double, std::milli>(b - a).count();
@@ -1685,7 +1698,7 @@ CopyCmd decode_copy(Device& dev, const gbr_cmd_header& h, const uint8_t* b) {
             c.size = p->size == UINT64_MAX ? c.buf->size - std::min(c.off, c.buf->size) : p->size;
             if (c.buf == c.buf2) fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: source and destination are the same buffer");
             if (c.off % 4 || c.off2 % 4 || c.size % 4) fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: alignment");
-            if (c.off + c.size > c.buf->size || c.off2 + c.size > c.buf2->size)
+            if (!range_fits(c.off, c.size, c.buf->size) || !range_fits(c.off2, c.size, c.buf2->size))
                 fail(GBR_ERR_VALIDATION, "copy_buffer_to_buffer: range out of bounds");
             break;
         }
@@ -1709,8 +1722,8 @@ CopyCmd decode_copy(Device& dev, const gbr_cmd_header& h, const uint8_t* b) {
             if (bpr < width || rpi < c.ext.height) fail(GBR_ERR_VALIDATION, "%s: layout smaller than the copy", kNames[k]);
             if (c.layout.offset % c.tex->bpp) fail(GBR_ERR_VALIDATION, "%s: offset not a multiple of the texel size", kNames[k]);
             if (c.ext.width && c.ext.height && c.ext.depth_or_array_layers) {
-                const uint64_t need = c.layout.offset + ((uint64_t)(c.ext.depth_or_array_layers - 1) * rpi +
-                                                         (c.ext.height - 1)) * bpr + width;
+                const uint64_t need = span_end(c.layout.offset, (uint64_t)(c.ext.depth_or_array_layers - 1) * rpi +
+                                                                    (c.ext.height - 1), bpr, width);
                 if (need > c.buf->size) fail(GBR_ERR_VALIDATION, "%s: buffer range out of bounds", kNames[k]);
             }
             break;
@@ -1742,7 +1755,7 @@ CopyCmd decode_copy(Device& dev, const gbr_cmd_header& h, const uint8_t* b) {
             c.off = p->offset;
             c.size = p->size == UINT64_MAX ? c.buf->size - std::min(c.off, c.buf->size) : p->size;
             if (c.off % 4 || c.size % 4) fail(GBR_ERR_VALIDATION, "clear_buffer: alignment");
-            if (c.off + c.size > c.buf->size) fail(GBR_ERR_VALIDATION, "clear_buffer: range out of bounds");
+            if (!range_fits(c.off, c.size, c.buf->size)) fail(GBR_ERR_VALIDATION, "clear_buffer: range out of bounds");
             break;
         }
         case GBR_OP_CLEAR_TEXTURE: {
@@ -1843,7 +1856,7 @@ std::vector<PassCmd> decode(Device& dev, const uint8_t* data, uint64_t len) {
                 auto* p = payload<gbr_cmd_set_index_buffer>(h, b);
                 auto buf = dev.get<Buffer>(p->buffer, "buffer");
                 uint64_t size = p->size ? p->size : buf->size - std::min(p->offset, buf->size);
-                if (p->offset + size > buf->size) fail(GBR_ERR_VALIDATION, "index buffer slice out of range");
+                if (!range_fits(p->offset, size, buf->size)) fail(GBR_ERR_VALIDATION, "index buffer slice out of range");
                 st.index = {buf, p->offset, size};
                 st.index_format = p->index_format;
                 break;
@@ -1854,7 +1867,7 @@ std::vector<PassCmd> decode(Device& dev, const uint8_t* data, uint64_t len) {
                 if (p->offset % 4) fail(GBR_ERR_VALIDATION, "vertex buffer offset must be a multiple of 4");
                 auto buf = dev.get<Buffer>(p->buffer, "buffer");
                 uint64_t size = p->size ? p->size : buf->size - std::min(p->offset, buf->size);
-                if (p->offset + size > buf->size) fail(GBR_ERR_VALIDATION, "vertex buffer slice out of range");
+                if (!range_fits(p->offset, size, buf->size)) fail(GBR_ERR_VALIDATION, "vertex buffer slice out of range");
                 st.vb[p->slot] = {buf, p->offset, size};
                 break;
             }
@@ -2101,7 +2114,7 @@ GBR_API gbr_status gbr_queue_write_buffer(gbr_device dh, gbr_buffer b, uint64_t 
         Item it;
         it.kind = Item::WRITE_BUFFER;
         it.buffer = d->get<Buffer>(b, "buffer");
-        if (offset + size > it.buffer->size) fail(GBR_ERR_VALIDATION, "write_buffer out of range");
+        if (!range_fits(offset, size, it.buffer->size)) fail(GBR_ERR_VALIDATION, "write_buffer out of range");
         if (!size) return GBR_OK;
         it.offset = offset;
         it.staged = stage_on_device(d.get(), data, size);
@@ -2121,7 +2134,7 @@ GBR_API gbr_status gbr_queue_write_buffers(gbr_device dh, uint32_t count, const 
             Item it;
             it.kind = Item::WRITE_BUFFER;
             it.buffer = d->get<Buffer>(w.buffer, "buffer");
-            if (w.offset + w.size > it.buffer->size) fail(GBR_ERR_VALIDATION, "write_buffer out of range (entry %u)", k);
+            if (!range_fits(w.offset, w.size, it.buffer->size)) fail(GBR_ERR_VALIDATION, "write_buffer out of range (entry %u)", k);
             if (w.size && !w.data) fail(GBR_ERR_INVALID_ARGUMENT, "null data (entry %u)", k);
             it.offset = w.offset;
             it.staged_size = w.size;
@@ -2144,7 +2157,7 @@ GBR_API gbr_status gbr_buffer_read(gbr_device dh, gbr_buffer b, uint64_t offset,
         Item it;
         it.kind = Item::READ_BUFFER;
         it.buffer = d->get<Buffer>(b, "buffer");
-        if (offset + size > it.buffer->size) fail(GBR_ERR_VALIDATION, "buffer read out of range");
+        if (!range_fits(offset, size, it.buffer->size)) fail(GBR_ERR_VALIDATION, "buffer read out of range");
         it.offset = offset;
         it.dst = dst;
         it.size = size;
@@ -2206,7 +2219,8 @@ GBR_API gbr_status gbr_queue_write_texture(gbr_device dh, gbr_texture th, uint32
         uint64_t src_row = layout->bytes_per_row ? layout->bytes_per_row : data_size;
         uint64_t rows_per_image = layout->rows_per_image ? layout->rows_per_image : t.mip_h(mip);
         if (src_row < row) fail(GBR_ERR_VALIDATION, "bytes_per_row smaller than a texel row");
-        uint64_t need = layout->offset + ((uint64_t)(t.layers() - 1) * rows_per_image + (t.mip_h(mip) - 1)) * src_row + row;
+        uint64_t need = span_end(layout->offset, span_end(0, (uint64_t)(t.layers() - 1), rows_per_image, t.mip_h(mip) - 1),
+                                 src_row, row);
         if (need > data_size) fail(GBR_ERR_VALIDATION, "write_texture source out of range");
         it.staged = stage_on_device(d.get(), data, data_size);
         it.staged_size = data_size;
@@ -2497,7 +2511,7 @@ GBR_API gbr_status gbr_bind_group_create(gbr_device dh, const gbr_bind_group_des
             const gbr_bind_group_entry& en = desc->entries[e];
             if (en.kind == GBR_BINDING_BUFFER) {
                 auto b = d->get<Buffer>(en.resource, "buffer");
-                if (en.offset > b->size || (en.size && en.offset + en.size > b->size))
+                if (en.offset > b->size || (en.size && !range_fits(en.offset, en.size, b->size)))
                     fail(GBR_ERR_VALIDATION, "bind group buffer range out of bounds");
                 if (en.offset % 16) fail(GBR_ERR_VALIDATION, "uniform binding offset must be a multiple of 16");
                 g->refs.push_back(b);

@@ -504,9 +504,13 @@ def _byte_array(data) -> np.ndarray:
 
 
 class PreparedWrites:
-    """A fixed list of buffer writes [(buffer, offset, data)] for Queue.write_buffers: the data
-    arrays are referenced, not copied, and their contents at each write_buffers call are what
-    gets written (as with write_buffer, the bytes are captured by the call)."""
+    """A fixed list of buffer writes [(buffer, offset, data)] for Queue.write_buffers.
+
+    C-contiguous numpy arrays are referenced, not copied: their contents at each write_buffers
+    call are what gets written (as with write_buffer, the bytes are captured by the call).  Every
+    other input (bytes, bytearray, memoryview, non-contiguous arrays) is copied once, here, into a
+    contiguous snapshot; later changes to such an object are not seen by later write_buffers
+    calls — build a new PreparedWrites, or pass a contiguous ndarray, to send new contents."""
 
     def __init__(self, items):
         self.items = []
