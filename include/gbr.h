@@ -332,6 +332,12 @@ typedef struct gbr_submission_stats {
     double raster_ms;              /* device time of the raster kernels (config.time_kernels) */
     uint32_t split_tile_chunks;    /* visibility raster: work items of tiles split by record count */
     uint32_t tile_shape;           /* tile side << 8 | warps per tile of the submission's largest batch */
+    /* Fragment-stage runs.  The reference runs the fragment stage for every fragment it counts
+     * (fragments_shaded) unless an @early_depth_test rejects it first; the visibility raster
+     * (gbr_raster_order AUTO) runs it once per pixel, for the fragment whose output survives,
+     * with the same resulting colours and depths. */
+    uint64_t fs_invocations;
+    uint64_t texture_fs_invocations; /* the part of fs_invocations whose program samples a texture */
 } gbr_submission_stats;
 
 /* ---------------------------------------------------------------- command stream

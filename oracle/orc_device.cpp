@@ -516,7 +516,15 @@ struct PassTargets {
 struct Counters {
     uint64_t fragments = 0;
     uint64_t primitives = 0;
+    uint64_t fs_runs = 0;   // fragment-stage invocations
+    uint64_t tex_runs = 0;  // those of programs with a texture binding
 };
+
+static bool program_samples_texture(const Program* p) {
+    for (int b = 0; b < p->num_bindings; ++b)
+        if (p->bindings[b].kind == 1) return true;
+    return false;
+}
 
 struct Exec {
     Device* dev;
@@ -689,6 +697,8 @@ static void process_fragment(FragCtx& fc, uint32_t fx, uint32_t fy, V4 fragment,
     }
     FsOut out;
     out.killed = false;
+    ex->cnt.fs_runs++;
+    if (program_samples_texture(fs)) ex->cnt.tex_runs++;
     fs->fs(in, *fc.pb, out);
     if (out.killed) return;  // EntryPointError::Killed (fragment.rs:204-208)
     if (fs->num_outputs == 0) return;
@@ -1178,8 +1188,11 @@ static void execute_pass(Device* dev, const DecodedPass& dp, Counters& total) {
     }
     for (int i = 0; i < nt; ++i)
         if (sts[i] != GBR_OK) throw Error{sts[i], errs[i]};
-    total.fragments += ex[0].cnt.fragments;
-    for (int i = 1; i < nt; ++i) total.fragments += ex[i].cnt.fragments;
+    for (int i = 0; i < nt; ++i) {
+        total.fragments += ex[i].cnt.fragments;
+        total.fs_runs += ex[i].cnt.fs_runs;
+        total.tex_runs += ex[i].cnt.tex_runs;
+    }
     total.primitives += ex[0].cnt.primitives;  // every thread assembles all primitives
 }
 
@@ -1576,6 +1589,8 @@ ORC_API gbr_status orc_queue_submit(gbr_device d, const void* cmds, uint64_t len
         s.draws = draws;
         s.primitives_in = total.primitives;
         s.fragments_shaded = total.fragments;
+        s.fs_invocations = total.fs_runs;
+        s.texture_fs_invocations = total.tex_runs;
         s.batched_with = 1;
         dev->stats[idx] = s;
         if (out_index) *out_index = idx;

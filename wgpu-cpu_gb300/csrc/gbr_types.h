@@ -105,7 +105,10 @@ struct TargetDesc {
     uint32_t tile_base;    // first global tile id of this target
     uint32_t slice_offset; // byte offset of the depth_slice layer
     uint32_t _pad;
-    unsigned long long* frag_count;  // fragments shaded into this target are added here (or null)
+    // three counters of this target (or null): [0] covered fragments, counted as the reference
+    // counts fragment_processing calls; [1] fragment-stage invocations; [2] those of programs
+    // that sample a texture
+    unsigned long long* frag_count;
 };
 
 // One draw call of a batch, fully resolved on the host.
@@ -207,6 +210,8 @@ enum : uint32_t {
 enum : uint32_t { RASTER_RULE_SCANLINE = 0, RASTER_RULE_EDGE = 1 };
 
 // Device-side status of a batch (zeroed before launch).
+constexpr uint32_t kTargetCounters = 3;  // per-target counters behind TargetDesc::frag_count
+
 struct BatchStatus {
     uint32_t error;
     uint32_t error_detail;

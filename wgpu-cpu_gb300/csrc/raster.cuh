@@ -1660,6 +1660,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
         __syncthreads();
 
         uint32_t frag_count = 0;
+        uint32_t fs_runs = 0, tex_runs = 0;  // fragment-stage invocations, and those that sample a texture
         const uint32_t stride = bp.record_stride;
         for (uint32_t w0 = 0; w0 < n; w0 += RW) {
             const uint32_t nb = min((uint32_t)RW, n - w0);
@@ -1825,6 +1826,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                                 c2 = fadd(fadd(fmul(r.cb[2], l0), fmul(r.cb[5], l1)), fmul(r.cb[8], l2));
                             }
                             ++frag_count;
+                            ++fs_runs;
                             // linear vec4f colour straight to the output, then Rgba16Float blending
                             // (colour SrcAlpha/OneMinusSrcAlpha/Add, alpha One/OneMinusSrcAlpha/Add)
                             const float2 cc0 = make_float2(c0, c0), cc1 = make_float2(c1, c1), cc2 = make_float2(c2, c2);
@@ -1868,6 +1870,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                         ++frag_count;
                         // inter-stage values (fragment.rs:319-378) and the fragment stage
                         V4 col;
+                        ++fs_runs;
+                        tex_runs += KIND == 2 || rs.tex_data != nullptr;
                         if constexpr (KIND == 2) {
                             float v[5];
 #pragma unroll
@@ -1955,10 +1959,18 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
             }
             if (tg.depth) tg.depth[pix] = px[k].depth;
         }
-        for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
+        for (int o = 16; o > 0; o >>= 1) {
+            frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
+            fs_runs += __shfl_xor_sync(0xFFFFFFFFu, fs_runs, o);
+            tex_runs += __shfl_xor_sync(0xFFFFFFFFu, tex_runs, o);
+        }
         if (lane == 0 && frag_count) {
             atomicAdd(&s_frag, (unsigned long long)frag_count);
-            if (tg.frag_count) atomicAdd(tg.frag_count, (unsigned long long)frag_count);
+            if (tg.frag_count) {
+                atomicAdd(tg.frag_count, (unsigned long long)frag_count);
+                if (fs_runs) atomicAdd(tg.frag_count + 1, (unsigned long long)fs_runs);
+                if (tex_runs) atomicAdd(tg.frag_count + 2, (unsigned long long)tex_runs);
+            }
         }
         __syncthreads();
     }

@@ -358,7 +358,12 @@ __global__ void __launch_bounds__(kLineThreads) k_lines_points(BatchParams bp) {
     for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
     if ((threadIdx.x & 31) == 0 && frag_count) {
         atomicAdd(&s_frag, (unsigned long long)frag_count);
-        if (tg.frag_count) atomicAdd(tg.frag_count, (unsigned long long)frag_count);
+        if (tg.frag_count) {
+            // every line or point fragment runs the fragment stage (one draw per CTA)
+            atomicAdd(tg.frag_count, (unsigned long long)frag_count);
+            atomicAdd(tg.frag_count + 1, (unsigned long long)frag_count);
+            if (s_rs.tex_data) atomicAdd(tg.frag_count + 2, (unsigned long long)frag_count);
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0 && s_frag) atomicAdd(&bp.status->fragments, s_frag);

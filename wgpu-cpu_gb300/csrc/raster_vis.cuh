@@ -316,6 +316,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
         // phase 2: the survivor of each pixel against the stored depth, fragment stage, write-back
         uint32_t clear_c[4] = {0, 0, 0, 0};
         encode_color(tg.color_format, V4{tg.clear[0], tg.clear[1], tg.clear[2], tg.clear[3]}, clear_c);
+        uint32_t fs_runs = 0, tex_runs = 0;  // fragment-stage invocations (survivors that pass), texture-sampling ones
         for (int p = threadIdx.x; p < NPIX; p += NT) {
             const int x = X0 + (p % T), y = Y0 + (p / T);
             if (x > XE || y > YE) continue;
@@ -359,6 +360,8 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                         }
                     }
                     V4 col;
+                    ++fs_runs;
+                    tex_runs += rs.tex_data != nullptr;
                     run_fs_any(bp, rs, r, cmp, var, s_lut, col);  // eligible programs never discard
                     if (rs.write_mask != 0xF) {
                         uint32_t dc[4] = {c[0], c[1], c[2], c[3]};
@@ -390,6 +393,14 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                 else *cdst = (uint8_t)c[0];
             }
             if (write_depth) tg.depth[pix] = depth;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            fs_runs += __shfl_xor_sync(0xFFFFFFFFu, fs_runs, o);
+            tex_runs += __shfl_xor_sync(0xFFFFFFFFu, tex_runs, o);
+        }
+        if (lane == 0 && fs_runs && tg.frag_count) {
+            atomicAdd(tg.frag_count + 1, (unsigned long long)fs_runs);
+            if (tex_runs) atomicAdd(tg.frag_count + 2, (unsigned long long)tex_runs);
         }
         tile_sync<WARPS>();
     }

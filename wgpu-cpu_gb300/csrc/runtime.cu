@@ -462,7 +462,7 @@ struct Batch {
     std::vector<uint32_t> target_item;       // submission (index in its group) of each target
     std::vector<const Texture*> writes, reads;  // attachments written, textures sampled
     uint32_t strip_entries = 0;              // strip-table entries of the restart draws
-    std::vector<uint64_t> target_frags;      // fragments shaded into each target (after the run)
+    std::vector<uint64_t> target_frags;      // kTargetCounters counters per target (after the run)
     uint32_t total_prims = 0, total_tiles = 0, nvar = 0;
     uint32_t item = 0;         // the submission of a single-submission batch
     bool single_item = true;
@@ -1046,9 +1046,13 @@ void Device::execute_group(std::vector<Item>& items) {
         for (size_t i = 0; i < n; ++i) fail_item(i, f.status, f.msg);
     }
     // per-submission fragment counts from the per-target counters
-    std::vector<uint64_t> frags(n, 0);
+    std::vector<uint64_t> frags(n, 0), fs_runs(n, 0), tex_runs(n, 0);
     for (const Batch& b : batches)
-        for (size_t t = 0; t < b.target_item.size() && t < b.target_frags.size(); ++t) frags[b.target_item[t]] += b.target_frags[t];
+        for (size_t t = 0; t < b.target_item.size() && (t + 1) * kTargetCounters <= b.target_frags.size(); ++t) {
+            frags[b.target_item[t]] += b.target_frags[t * kTargetCounters];
+            fs_runs[b.target_item[t]] += b.target_frags[t * kTargetCounters + 1];
+            tex_runs[b.target_item[t]] += b.target_frags[t * kTargetCounters + 2];
+        }
     float group_ms = 0.0f;
     if (run.ev && run.started) cudaEventElapsedTime(&group_ms, run.ev->start, run.ev->end);
     std::lock_guard<std::mutex> lk(q_mu);
@@ -1057,6 +1061,8 @@ void Device::execute_group(std::vector<Item>& items) {
         rec.stats.submission_index = items[i].index;
         rec.stats.submit_to_fence_ms = ms_between(items[i].t_submit, Clock::now());
         rec.stats.fragments_shaded = rec.status == GBR_OK ? frags[i] : 0;
+        rec.stats.fs_invocations = rec.status == GBR_OK ? fs_runs[i] : 0;
+        rec.stats.texture_fs_invocations = rec.status == GBR_OK ? tex_runs[i] : 0;
         rec.stats.kernel_launches = run.launches;
         rec.stats.gpu_ms = group_ms;
         rec.stats.raster_ms = run.raster_ms;
@@ -1363,7 +1369,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
     }
     const size_t off_status = 256, off_work = align(off_status + nb * sizeof(BatchStatus));
     const size_t off_counters = align(off_work + nb * sizeof(uint32_t) * 4);
-    const size_t off_desc = align(off_counters + n_targets * sizeof(unsigned long long));
+    const size_t off_desc = align(off_counters + n_targets * kTargetCounters * sizeof(unsigned long long));
     std::vector<size_t> desc_off(nb, 0), states_off(nb, 0);
     std::vector<int> kinds(nb, 0);
     size_t cur = off_desc;
@@ -1388,7 +1394,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         TargetDesc* tp = reinterpret_cast<TargetDesc*>(p + batches[i].draws.size() * sizeof(DrawDesc));
         for (size_t t = 0; t < batches[i].targets.size(); ++t) {
             TargetDesc td = batches[i].targets[t];
-            td.frag_count = reinterpret_cast<unsigned long long*>(meta + off_counters) + counter_first[i] + t;
+            td.frag_count = reinterpret_cast<unsigned long long*>(meta + off_counters) + (counter_first[i] + t) * kTargetCounters;
             std::memcpy(tp + t, &td, sizeof td);
         }
         uint8_t* bases = p + batches[i].draws.size() * sizeof(DrawDesc) + batches[i].targets.size() * sizeof(TargetDesc);
@@ -1404,7 +1410,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
     }
     size_t first_batch = from;
     std::vector<BatchStatus> st(nb);
-    std::vector<unsigned long long> counters(n_targets);
+    std::vector<unsigned long long> counters(n_targets * kTargetCounters);
     std::vector<cudaEvent_t> rev;  // raster kernel events (time_kernels)
     struct EventGuard {
         std::vector<cudaEvent_t>* v;
@@ -1605,8 +1611,9 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                                    stream),
                    "status readback");
         if (n_targets)
-            cuda_check(cudaMemcpyAsync(counters.data(), meta + off_counters, n_targets * sizeof(unsigned long long),
-                                       cudaMemcpyDeviceToHost, stream),
+            cuda_check(cudaMemcpyAsync(counters.data(), meta + off_counters,
+                                       n_targets * kTargetCounters * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                                       stream),
                        "counter readback");
         cuda_check(cudaStreamSynchronize(stream), "submission");
         // first failing batch
@@ -1618,8 +1625,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
             }
         for (size_t i = first_batch; i < bad; ++i) {
             Batch& b = batches[i];
-            b.target_frags.assign(counters.begin() + (ptrdiff_t)counter_first[i],
-                                  counters.begin() + (ptrdiff_t)(counter_first[i] + b.targets.size()));
+            b.target_frags.assign(counters.begin() + (ptrdiff_t)(counter_first[i] * kTargetCounters),
+                                  counters.begin() + (ptrdiff_t)((counter_first[i] + b.targets.size()) * kTargetCounters));
             run.slow_prims += st[i].slow_count;
             run.split_chunks += st[i].split_items;
             if (!b.copy && !b.lines && (!run.tile_shape || b.total_prims > run.tile_shape_prims)) {
@@ -1655,8 +1662,10 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         }
         // counters of the batches that re-run start from zero
         if (n_targets > counter_first[bad])
-            cuda_check(cudaMemsetAsync(reinterpret_cast<unsigned long long*>(meta + off_counters) + counter_first[bad],
-                                       0, (n_targets - counter_first[bad]) * sizeof(unsigned long long), stream),
+            cuda_check(cudaMemsetAsync(reinterpret_cast<unsigned long long*>(meta + off_counters) +
+                                           counter_first[bad] * kTargetCounters,
+                                       0, (n_targets - counter_first[bad]) * kTargetCounters * sizeof(unsigned long long),
+                                       stream),
                        "counters");
         first_batch = bad;
         if (attempt == 11) fail(GBR_ERR_OUT_OF_MEMORY, "scratch growth did not converge");

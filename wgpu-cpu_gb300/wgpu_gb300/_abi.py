@@ -138,7 +138,8 @@ class SubmissionStats(C.Structure):
     _fields_ = [("submission_index", u64), ("draws", u64), ("primitives_in", u64), ("fragments_shaded", u64),
                 ("kernel_launches", u64), ("queue_wait_ms", f64), ("gpu_ms", f64), ("submit_to_fence_ms", f64),
                 ("batched_with", u32), ("generic_setup_prims", u32), ("raster_ms", f64),
-                ("split_tile_chunks", u32), ("tile_shape", u32)]
+                ("split_tile_chunks", u32), ("tile_shape", u32), ("fs_invocations", u64),
+                ("texture_fs_invocations", u64)]
 
 
 class CmdHeader(C.Structure):

@@ -390,12 +390,13 @@ class MultiScene:
 
 
 def scene_batched(dev: W.Device, n_targets: int = 64, n_draws: int = 256, seed: int = 3, tri_lo: int = 100,
-                  tri_hi: int = 200000, side_lo: int = 128, side_hi: int = 2048, tex_size: int = 256) -> MultiScene:
+                  tri_hi: int = 200000, side_lo: int = 128, side_hi: int = 2048, tex_size: int = 1024) -> MultiScene:
     """Batching workload: n_draws draws into n_targets targets (Rgba8Unorm + Depth32Float Less),
     target sides log-uniform in [side_lo, side_hi], triangle counts log-uniform in [tri_lo, tri_hi]
     taken from the front of a displaced icosphere of the smallest sufficient level, random model
     rotations seen from a random distance (every vertex in front of the camera, so w > 0), half
-    vertex-colour and half textured programs, draw d into target d mod n_targets."""
+    vertex-colour and half textured programs (the tex_size^2 checker x value-noise texture of the
+    textured configuration, nearest, repeat), draw d into target d mod n_targets."""
     rng = np.random.default_rng(seed)
     tw = np.exp(rng.uniform(math.log(side_lo), math.log(side_hi), n_targets)).astype(int)
     th = np.exp(rng.uniform(math.log(side_lo), math.log(side_hi), n_targets)).astype(int)
@@ -562,3 +563,31 @@ def serving_set(dev: W.Device, n_submissions: int = 256, n_meshes: int = 512, n_
         s.keep.append(color)
         s.keep.append(dtex)
     return s
+
+
+# ------------------------------------------------------------------------------------ configurations
+# The benchmark configurations at their full sizes: name -> (scene builder, profile, arguments).
+# The parity fixtures (tests/golden/frame_digests.json), the full-size GPU tests and bench.py all
+# build their scenes from this table, so they always render the same inputs.
+FULL_SIZE = {
+    "colored": ("scene_colored_sphere", W.Profile.PARITY, dict(width=512, height=512)),
+    "textured": ("scene_textured_icosphere", W.Profile.PARITY,
+                 dict(width=1920, height=1080, level=6, tex_size=1024)),
+    "textured_filtered": ("scene_textured_icosphere", W.Profile.EXTENSION,
+                          dict(width=1920, height=1080, level=6, tex_size=1024, filtering=True, srgb=True)),
+    "blend": ("scene_blended_quads", W.Profile.EXTENSION, dict(width=3840, height=2160, n_quads=10000)),
+    "batched": ("scene_batched", W.Profile.PARITY, dict(n_targets=64, n_draws=256, seed=3, tex_size=1024)),
+}
+
+
+def build_config(dev: W.Device, name: str, **over):
+    """The scene of configuration `name` (FULL_SIZE) on `dev`, with `over` replacing arguments."""
+    builder, _, kwargs = FULL_SIZE[name]
+    return globals()[builder](dev, **{**kwargs, **over})
+
+
+def scene_targets(scene) -> list:
+    """(colour, depth or None) of every render pass of a Scene or MultiScene, in pass order."""
+    if hasattr(scene, "passes"):
+        return [(p[0], p[1]) for p in scene.passes]
+    return [(scene.color, scene.depth)]
