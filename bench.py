@@ -2,41 +2,46 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--workload NAME]
 
-One step = one render pass (one frame) of the workload, submitted through the library's queue.
+One step = one render pass set (one frame) of the workload, submitted through the library's queue.
 
-Workloads (seeded synthetic inputs with the configurations' shapes; no dataset exists):
-  textured            displaced icosphere subdivided 6 times (81,920 triangles; f32x3 position,
-                      f32x3 normal, f32x2 UV), 1024x1024 Rgba8UnormSrgb checker x value-noise
-                      texture, texture x Lambert shading, 1920x1080 Rgba8UnormSrgb + Depth32Float
-                      (Less).  Parity profile: nearest sampling, sRGB formats read and written as
-                      linear, exactly as wgpu-cpu does (its sampler ignores filter modes).
-  textured_filtered   the same textured scene as the configuration states it, extension profile:
-                      full mip chain, linear min/mag/mip filtering with repeat addressing, sRGB
-                      texture decode and sRGB target encode (LOD per primitive from analytic UV
-                      derivatives; the reference has no filtering, mips or sRGB conversion).
-  blend               10,000 screen-aligned quads (20,000 triangles), sides U[16,1024] px, RGBA f16
-                      colours with alpha U[0.1,0.9], painter order, SrcAlpha/OneMinusSrcAlpha into
-                      3840x2160 Rgba16Float (extension profile: the reference has neither blending
-                      nor f16 targets).  The fill-rate-bound configuration.
-  colored             UV sphere 32x16 (992 triangles), per-vertex colours, back-face cull,
-                      512x512 Rgba8Unorm (the reference's CPU-runnable configuration).
+Workloads (seeded synthetic inputs with the configurations' shapes; no dataset exists; the scenes
+and their arguments are wgpu_gb300.workloads.FULL_SIZE):
   batched (default)   256 draws into 64 render targets (sides log-uniform in [128, 2048], triangle
                       counts log-uniform in [100, 200k], random model rotations, half textured x
-                      Lambert and half vertex-colour programs), Rgba8Unorm + Depth32Float (Less),
-                      one command buffer, replayed from a CUDA graph with the tile shape chosen by
-                      the device's autotuner (its trial submissions run before warm-up; `--fixed`
-                      or `--tile/--warps` run a fixed shape without graphs).  Besides the batched
-                      launch sequence the line reports the same command buffer launched per draw,
-                      the plain path it replaces, at the same tile shape.
+                      Lambert with the 1024^2 checker x value-noise texture (nearest, repeat) and
+                      half vertex-colour programs), Rgba8Unorm + Depth32Float (Less), one command
+                      buffer replayed from a CUDA graph with the tile shape chosen by the device's
+                      autotuner (its trial submissions run before warm-up; `--fixed` or
+                      `--tile/--warps` run a fixed shape without graphs).  Beside it the line
+                      reports the same command buffer on the plain per-draw path (one launch
+                      sequence per draw), launched directly and replayed from CUDA graphs; the
+                      fill-bound configuration (`fill_bound`); and the serving loop at 2,000
+                      submissions/s (`serving`).
+  textured            displaced icosphere subdivided 6 times (81,920 triangles), 1024x1024
+                      checker x value-noise texture, texture x Lambert, 1920x1080 Rgba8UnormSrgb +
+                      Depth32Float (Less); parity profile (nearest, sRGB read and written as
+                      linear, exactly as wgpu-cpu does).
+  textured_filtered   the same scene as the configuration states it, extension profile: full mip
+                      chain, trilinear filtering, sRGB decode and encode.
+  blend               10,000 screen-aligned quads (20,000 triangles), sides U[16,1024] px, RGBA f16
+                      colours with alpha U[0.1,0.9], painter order, SrcAlpha/OneMinusSrcAlpha into
+                      3840x2160 Rgba16Float (extension profile).  The fill-rate-bound configuration.
+  colored             UV sphere 32x16 (992 triangles), per-vertex colours, back-face cull,
+                      512x512 Rgba8Unorm (the reference's CPU-runnable configuration).
+  serve               the serving loop alone (Poisson arrivals, --rate, --duration).
 
-`value` is shaded fragments per second (fragment-shader invocations, counted as the reference
-counts them) with every input resident in HBM, over the device time of the K steps (CUDA events on
-the library's stream; a 256 MiB L2 flush is enqueued between steps, so each step starts cold).
+`value` is shaded fragments per second (fragments counted as the reference counts its
+fragment_processing calls) with every input resident in HBM, over the device time of the K steps
+(CUDA events on the library's stream; a 256 MiB L2 flush is enqueued between steps, so each step
+starts cold).  `fs_invocations_per_step` counts fragment-stage runs: the visibility raster runs
+the fragment stage once per pixel, for the surviving fragment.  `parity` compares the last timed
+frame of every arm with the oracle's frame (SHA-256 digests in tests/golden/frame_digests.json).
 `e2e` is the same metric through the C ABI with host buffers: each step uploads the pass's inputs
-from pinned host memory, renders, and reads the colour target back.  `roofline` covers the
-dominant kernel (k_raster).  `--impl reference` times the CPU restatement of wgpu-cpu's rasteriser
-(the oracle; the Rust reference cannot be built here) on all host cores.  One GPU per process;
-with N > 1 each rank renders its own replica and `value` sums them.
+from pinned host memory, renders, and reads every colour target back.  `roofline` covers the
+dominant kernel (the raster kernel).  `--impl reference` times the CPU restatement of wgpu-cpu's
+rasteriser (the oracle; the Rust reference cannot be built here) on all host cores, on the same
+configuration.  One GPU per process; with N > 1 each rank renders its own replica and `value`
+sums them.
 """
 
 from __future__ import annotations
@@ -56,88 +61,65 @@ import numpy as np  # noqa: E402
 
 METRIC = "shaded fragments/s, batched vs per-draw GPU at bit-exact coverage; p99 submit ms"
 UNIT = "fragments/s"
+TEXEL_BYTES_NEAREST = 4  # one Rgba8 texel per nearest sample
 
 
 class Workload:
-    def __init__(self, name, profile, builder, kwargs, bytes_per_fragment, pixel_bytes, description, extra_cfg,
-                 cpu_kwargs=None, dtype="f32", tile=(16, 8)):
-        self.name, self.profile, self.builder, self.kwargs = name, profile, builder, kwargs
-        self.tile = tile  # (side, warps per tile): the fastest shape measured for this workload
-        self.bytes_per_fragment, self.pixel_bytes = bytes_per_fragment, pixel_bytes
+    def __init__(self, name, description, extra_cfg, tile, dtype="f32", texel_bytes=TEXEL_BYTES_NEAREST,
+                 blend_bytes=0):
+        from wgpu_gb300 import workloads as wl
+
+        self.name = name
+        self.builder, self.profile, self.kwargs = wl.FULL_SIZE[name]
         self.description, self.extra_cfg = description, extra_cfg
-        self.cpu_kwargs = cpu_kwargs if cpu_kwargs is not None else kwargs
+        self.tile = tile  # (side, warps per tile): the fastest fixed shape measured for this workload
         self.dtype = dtype
+        self.texel_bytes = texel_bytes  # bytes read per texture sample
+        self.blend_bytes = blend_bytes  # colour bytes read back per fragment when blending
 
     def build(self, dev, **over):
         from wgpu_gb300 import workloads as wl
 
-        return getattr(wl, self.builder)(dev, **{**self.kwargs, **over})
+        return wl.build_config(dev, self.name, **over)
 
-    def config(self, flush=True, launch_mode="batched", graphs=False):
-        return {"workload": self.description, **self.extra_cfg, "launch_mode": launch_mode, "cuda_graphs": graphs,
-                "l2": "flushed between timed steps (256 MiB write)" if flush else "n/a (CPU)"}
+    def config(self):
+        """The workload as both arms run it (identical for --impl ours and --impl reference)."""
+        return {"workload": self.description, **self.extra_cfg,
+                "l2": "GPU: flushed between timed steps (256 MiB write); CPU: n/a"}
 
 
 def workloads():
-    from wgpu_gb300 import api as W
-
     return {
+        "batched": Workload(
+            "batched",
+            "batched draws: 256 draws into 64 targets (sides log-uniform [128,2048], tris log-uniform [100,200k]), "
+            "Rgba8Unorm + Depth32Float Less, half texture x Lambert (1024^2 checker x noise, nearest, repeat) / half "
+            "vertex colour, one command buffer",
+            {"draws": 256, "targets": 64, "texture": "1024x1024 rgba8", "profile": "parity", "seed": 3},
+            tile=(32, 8)),
         "textured": Workload(
-            "textured", W.Profile.PARITY, "scene_textured_icosphere",
-            dict(width=1920, height=1080, level=6, tex_size=1024),
-            4 + 4 + 4 + 4, 1920 * 1080 * (4 + 4),
+            "textured",
             "textured icosphere: 81,920 tris, 1920x1080 Rgba8UnormSrgb + Depth32Float Less, 1024^2 texture, "
             "texture x Lambert, parity profile (nearest, sRGB as linear)",
             {"triangles": 81920, "target": "1920x1080", "texture": "1024x1024 rgba8", "profile": "parity", "seed": 2},
             tile=(16, 4)),
         "textured_filtered": Workload(
-            "textured_filtered", W.Profile.EXTENSION, "scene_textured_icosphere",
-            dict(width=1920, height=1080, level=6, tex_size=1024, filtering=True, srgb=True),
-            4 + 4 + 4 + 32, 1920 * 1080 * (4 + 4),
+            "textured_filtered",
             "textured icosphere: 81,920 tris, 1920x1080 Rgba8UnormSrgb + Depth32Float Less, 1024^2 Rgba8UnormSrgb "
             "texture with full mip chain, linear min/mag/mip filtering, repeat, texture x Lambert, extension profile",
             {"triangles": 81920, "target": "1920x1080 rgba8 srgb", "texture": "1024x1024 rgba8 srgb, 11 mips",
              "filtering": "trilinear", "profile": "extension", "seed": 2},
-            tile=(16, 4)),
+            tile=(16, 4), texel_bytes=32),
         "blend": Workload(
-            "blend", W.Profile.EXTENSION, "scene_blended_quads", dict(width=3840, height=2160, n_quads=10000),
-            8 + 8, 3840 * 2160 * 8,
+            "blend",
             "blended quads: 10,000 quads (20,000 tris) sides U[16,1024], painter order, SrcAlpha/OneMinusSrcAlpha "
             "into 3840x2160 Rgba16Float, extension profile",
             {"triangles": 20000, "target": "3840x2160 rgba16float", "profile": "extension", "seed": 4},
-            cpu_kwargs=dict(width=3840, height=2160, n_quads=60), dtype="f32 (f16 storage)", tile=(32, 8)),
+            tile=(32, 8), dtype="f32 (f16 storage)", texel_bytes=0, blend_bytes=8),
         "colored": Workload(
-            "colored", W.Profile.PARITY, "scene_colored_sphere", dict(width=512, height=512),
-            4, 512 * 512 * 4,
-            "colored UV sphere: 992 tris, 512x512 Rgba8Unorm, back-face cull, no depth",
-            {"triangles": 992, "target": "512x512", "profile": "parity", "seed": 1}),
-        "batched": Workload(
-            "batched", W.Profile.PARITY, "scene_batched", dict(n_targets=64, n_draws=256, seed=3),
-            4 + 4 + 4 + 4, None,
-            "batched draws: 256 draws into 64 targets (sides log-uniform [128,2048], tris log-uniform [100,200k]), "
-            "Rgba8Unorm + Depth32Float Less, half texture x Lambert / half vertex colour, one command buffer",
-            {"draws": 256, "targets": 64, "profile": "parity", "seed": 3},
-            cpu_kwargs=dict(n_targets=16, n_draws=64, seed=3), tile=(32, 8)),
+            "colored", "colored UV sphere: 992 tris, 512x512 Rgba8Unorm, back-face cull, no depth",
+            {"triangles": 992, "target": "512x512", "profile": "parity", "seed": 1}, tile=(16, 8)),
     }
-
-
-def pixel_bytes(wk: Workload, scene) -> int:
-    """Target bytes written per step: colour plus depth of every target."""
-    from wgpu_gb300 import api as W
-
-    if wk.pixel_bytes is not None:
-        return wk.pixel_bytes
-    total = 0
-    for color, depth, _ in scene.passes:
-        total += color.width * color.height * (W.BYTES_PER_TEXEL[color.format] + (4 if depth is not None else 0))
-    return total
-
-
-def color_targets(scene):
-    return [p[0] for p in scene.passes] if hasattr(scene, "passes") else [scene.color]
-
-
-LAUNCH_MODES = {"batched": 0, "per_pass": 2, "per_draw": 1}
 
 
 def dist_env():
@@ -231,189 +213,179 @@ def raster_profile(name):
     return {}
 
 
-def raster_traffic(name):
-    """DRAM bytes per raster launch from the committed ncu summary of this workload, if any."""
-    return raster_profile(name).get("dram_bytes_per_launch")
+# ------------------------------------------------------------------------------------ byte model
+def algorithmic_bytes(wk: Workload, scene, stats) -> dict:
+    """Bytes the raster kernel must move at least, per launch:
+      every target pixel written once (colour + depth: the clear is fused into the raster),
+      per covered fragment the depth read and write (8 B) when the pass has depth,
+      per fragment-stage run the colour write (plus the colour read when blending) and the texel
+      bytes of a texture-sampling program (4 B nearest, 32 B trilinear Rgba8)."""
+    from wgpu_gb300 import api as W
+    from wgpu_gb300 import workloads as wl
+
+    pixels, has_depth, bpp = 0, False, 4
+    for color, depth in wl.scene_targets(scene):
+        bpp = W.BYTES_PER_TEXEL[color.format]
+        pixels += color.width * color.height * (bpp + (4 if depth is not None else 0))
+        has_depth = has_depth or depth is not None
+    covered = int(stats.fragments_shaded)
+    fs_runs = int(stats.fs_invocations)
+    tex_runs = int(stats.texture_fs_invocations)
+    total = pixels + covered * (8 if has_depth else 0) + fs_runs * (bpp + wk.blend_bytes) + tex_runs * wk.texel_bytes
+    return {"total": total, "target_pixels": pixels, "covered_fragments": covered, "fs_invocations": fs_runs,
+            "texture_fs_invocations": tex_runs}
 
 
-def cpu_baseline(wk: Workload, target_seconds: float = 12.0):
-    """The oracle (CPU restatement of wgpu-cpu's rasteriser) on all host cores, bounded sample."""
+# ------------------------------------------------------------------------------------ parity
+def parity_of(name, dev, scene, stats) -> dict:
+    """The rendered frame against the oracle's (tests/golden/frame_digests.json)."""
+    import frame_digests as fd
+
+    diffs = fd.compare(name, fd.input_digest(scene), fd.target_digests(dev, scene), int(stats.fragments_shaded))
+    return {"status": "ok" if not diffs else "MISMATCH", "checked": "colour + depth bytes of every target and the "
+            "fragment count vs the oracle (sha256)", **({"diffs": diffs[:8]} if diffs else {})}
+
+
+# ------------------------------------------------------------------------------------ CPU (oracle)
+def oracle_frames(wk: Workload, threads: int, budget_s: float, max_frames: int, warmup: int = 0, passes=None):
+    """Renders the workload's frame with the oracle (the CPU restatement of wgpu-cpu's rasteriser)
+    on `threads` host threads: `warmup` untimed frames, then frames until `max_frames` or the time
+    budget.  `passes` limits a multi-pass scene to its first passes (a bounded sample).
+    Returns (fragments per frame, frames, seconds)."""
     import oracle_device
+    from wgpu_gb300 import workloads as wl
 
+    dev = oracle_device.device(profile=wk.profile, threads=threads)
+    try:
+        scene = wl.build_config(dev, wk.name)
+        if passes is not None:
+            scene.passes = scene.passes[:passes]
+        enc = dev.create_command_encoder()
+        scene.record(enc)
+        cmd = enc.finish()
+        for _ in range(warmup):
+            dev.queue.submit([cmd])
+        frags, frames = 0, 0
+        t0 = time.perf_counter()
+        while True:
+            idx = dev.queue.submit([cmd])
+            frags = dev.submission_stats(idx).fragments_shaded
+            frames += 1
+            if frames >= max_frames or time.perf_counter() - t0 > budget_s:
+                break
+        return frags, frames, time.perf_counter() - t0
+    finally:
+        dev.close()
+        oracle_device.oracle_lib.load().orc_set_threads(1)
+
+
+def cpu_baseline(wk: Workload, budget_s: float = 12.0, single_thread_s: float = 10.0) -> dict:
+    """The oracle on the host cores, on the same workload: all cores on whole frames (bounded by
+    the time budget), and one thread — the reference's single engine thread (engine.rs:15-22) —
+    on a bounded sample (the first passes of the frame, or whole frames of a single-pass one)."""
     cores = os.cpu_count() or 1
-    dev = oracle_device.device(profile=wk.profile, threads=cores)
-    scene = getattr(__import__("wgpu_gb300.workloads", fromlist=["x"]), wk.builder)(dev, **wk.cpu_kwargs)
-    frags, frames = 0, 0
-    t0 = time.perf_counter()
-    while True:
-        idx = scene.render()
-        frags += dev.submission_stats(idx).fragments_shaded
-        frames += 1
-        if time.perf_counter() - t0 > target_seconds or frames >= 200:
-            break
-    dt = time.perf_counter() - t0
-    oracle_device.oracle_lib.load().orc_set_threads(1)
-    what = "full frames of the workload" if wk.cpu_kwargs == wk.kwargs else f"frames of the workload cut to {wk.cpu_kwargs}"
-    return {"value": frags / dt, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{frames} {what} ({frags // frames} fragments each) in {dt:.1f} s, row bands per thread"}
+    frags, frames, dt = oracle_frames(wk, cores, budget_s, 200)
+    out = {"value": frags * frames / dt, "unit": UNIT, "cores": cores, "kind": "port",
+           "sample": f"{frames} full frames of the workload ({frags} fragments each) in {dt:.1f} s, "
+                     f"{cores} threads (row bands / passes per thread)"}
+    passes = 4 if wk.name == "batched" else None
+    f1, n1, d1 = oracle_frames(wk, 1, single_thread_s, 50, passes=passes)
+    what = f"the first {passes} of the frame's 64 passes" if passes else "full frames"
+    out["single_thread"] = {"value": f1 * n1 / d1, "unit": UNIT, "cores": 1,
+                            "sample": f"{n1} x {what} ({f1} fragments each) in {d1:.1f} s"}
+    return out
 
 
 def run_reference(args, wk: Workload):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    base = cpu_baseline(wk, target_seconds=max(5.0, min(60.0, 2.0 * args.steps)))
-    line = {"impl": "reference", "metric": METRIC, "value": base["value"], "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": wk.dtype, "data": "synthetic (seeded)", "config": wk.config(False),
-            "cpu_baseline": base,
-            "e2e": {"value": base["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    cores = os.cpu_count() or 1
+    # whole frames of the same configuration as the GPU arm: W untimed, then K timed (at most 150 s)
+    frags, frames, dt = oracle_frames(wk, cores, 150.0, args.steps, warmup=args.warmup)
+    value = frags * frames / dt
+    base = {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{frames} timed full frames ({frags} fragments each) after {args.warmup} untimed, "
+                      f"{dt:.1f} s, {cores} threads"}
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3 / frames, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": wk.dtype, "data": "synthetic (seeded)",
+            "config": wk.config(), "cpu_baseline": base, "fragments_per_step": frags,
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def run_ours(args, wk: Workload):
-    import torch
-
-    from wgpu_gb300 import api as W
-
-    rank, world, local = dist_env()
-    if world > 1:
-        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    torch.cuda.set_device(local)
-    dev = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True, tile_size=args.tile,
-                   warps_per_tile=args.warps, launch_mode=LAUNCH_MODES[args.launch_mode], use_graphs=args.graphs)
-    over = {"n_quads": args.quads} if args.quads and wk.name == "blend" else {}
-    if wk.name == "batched" and (args.draws or args.targets):
-        over = {"n_draws": args.draws or wk.kwargs["n_draws"], "n_targets": args.targets or wk.kwargs["n_targets"]}
-    scene = wk.build(dev, **over)
+# ------------------------------------------------------------------------------------ GPU arms
+def record(dev, scene):
     enc = dev.create_command_encoder()
     scene.record(enc)
-    cmd = enc.finish()
+    return enc.finish()
 
-    if args.autotune:  # the tuner's trial submissions (one per candidate tile shape), before warm-up
-        for _ in range(TUNE_TRIALS):
+
+def timed_steps(dev, cmd, steps, flush=True):
+    subs = []
+    for _ in range(steps):
+        if flush:
             dev.flush_caches()
-            dev.poll(True, dev.queue.submit([cmd]))
-    for _ in range(args.warmup):
-        dev.flush_caches()
-        idx = dev.queue.submit([cmd])
-    dev.poll(True, idx)
-    frags_per_step = dev.submission_stats(idx).fragments_shaded
+        subs.append(dev.queue.submit([cmd]))
+    dev.poll(True, subs[-1])
+    return [dev.submission_stats(i) for i in subs]
 
-    def barrier():
-        if world > 1:
-            torch.distributed.barrier()
-        torch.cuda.synchronize()
 
-    def timed_steps(d, c, steps):
-        subs = []
-        for _ in range(steps):
-            d.flush_caches()
-            subs.append(d.queue.submit([c]))
-        d.poll(True, subs[-1])
-        return [d.submission_stats(i) for i in subs]
+def per_draw_arm(wk, local, shape, graphs, steps):
+    """The same command buffer on the plain path: one launch sequence per draw, at `shape`."""
+    from wgpu_gb300 import api as W
 
-    barrier()
-    with ClockSampler(local) as clocks:
-        t0 = time.perf_counter()
-        stats = timed_steps(dev, cmd, args.steps)
-        wall = time.perf_counter() - t0
-    barrier()
+    dev = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True, tile_size=shape[0],
+                   warps_per_tile=shape[1], launch_mode=W.LaunchMode.PER_DRAW, use_graphs=graphs)
+    try:
+        scene = wk.build(dev)
+        cmd = record(dev, scene)
+        timed_steps(dev, cmd, 3)  # warm-up (graph capture on the first)
+        st = timed_steps(dev, cmd, steps)
+        ms = float(np.mean([s.gpu_ms for s in st]))
+        return {"value": st[-1].fragments_shaded / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "cuda_graphs": graphs,
+                "gpu_launches_per_step": int(st[-1].kernel_launches), "draws": int(st[-1].draws),
+                "kernels_per_draw": round(st[-1].kernel_launches / max(1, st[-1].draws), 2),
+                "parity": parity_of(wk.name, dev, scene, st[-1])["status"]}
+    finally:
+        dev.close()
 
-    # the same command buffer on the plain per-draw path (one launch sequence per draw)
-    per_draw = None
-    if wk.name == "batched" and args.launch_mode != "per_draw" and not args.no_per_draw:
-        shape = stats[-1].tile_shape  # the batched arm's tile shape (the tuner's choice when autotuned)
-        d2 = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True,
-                      tile_size=(shape >> 8) or dev_tile(args), warps_per_tile=(shape & 0xFF) or dev_warps(args),
-                      launch_mode=W.LaunchMode.PER_DRAW)
-        scene2 = wk.build(d2, **over)
-        enc2 = d2.create_command_encoder()
-        scene2.record(enc2)
-        cmd2 = enc2.finish()
-        timed_steps(d2, cmd2, 3)
-        st2 = timed_steps(d2, cmd2, max(3, min(args.steps, 10)))
-        ms2 = float(np.mean([s.gpu_ms for s in st2]))
-        if st2[-1].fragments_shaded != frags_per_step:
-            raise RuntimeError("per-draw launches shaded a different number of fragments")
-        per_draw = {"value": st2[-1].fragments_shaded / (ms2 / 1e3), "unit": UNIT, "ms_per_step": ms2,
-                    "gpu_launches_per_step": int(st2[-1].kernel_launches)}
-        del scene2, cmd2
-        d2.close()
-    gpu_ms = [s.gpu_ms for s in stats]
-    raster_ms = [s.raster_ms for s in stats]
-    device_s = sum(gpu_ms) / 1e3
-    device_s, value = replica_rate(frags_per_step, args.steps, device_s)
-    launches = int(sum(s.kernel_launches for s in stats))
 
-    # roofline of the dominant kernel: algorithmic bytes per launch / its event-timed duration
-    alg_bytes = pixel_bytes(wk, scene) + frags_per_step * wk.bytes_per_fragment
-    peak, peak_src = measured_peak_hbm()
-    r_ms = float(np.mean(raster_ms))
-    achieved = alg_bytes / (r_ms / 1e3) / 1e9 if r_ms > 0 else None
+def fill_bound_arm(local, steps):
+    """The fill-bound configuration (10,000 blended quads into 3840x2160 Rgba16Float)."""
+    from wgpu_gb300 import api as W
 
-    # end to end through the C ABI: inputs from pinned host memory, colour target read back
-    pinned = [(obj, torch.from_numpy(np.array(arr).reshape(-1).view(np.uint8)).pin_memory())
-              for obj, arr in scene.uploads]
-    reads = []
-    for t in color_targets(scene):
-        n = t.width * t.height * W.BYTES_PER_TEXEL[t.format]
-        reads.append((t, torch.empty(n, dtype=torch.uint8).pin_memory()))
-    out_bytes = sum(o.numel() for _, o in reads)
+    wk = workloads()["blend"]
+    dev = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True, tile_size=wk.tile[0],
+                   warps_per_tile=wk.tile[1])
+    try:
+        scene = wk.build(dev)
+        cmd = record(dev, scene)
+        timed_steps(dev, cmd, 3)
+        st = timed_steps(dev, cmd, steps)
+        ms = float(np.mean([s.gpu_ms for s in st]))
+        r_ms = float(np.mean([s.raster_ms for s in st]))
+        ab = algorithmic_bytes(wk, scene, st[-1])
+        peak, src = measured_peak_hbm()
+        achieved = ab["total"] / (r_ms / 1e3) / 1e9
+        prof = raster_profile("blend")
+        return {"workload": wk.description, "value": st[-1].fragments_shaded / (ms / 1e3), "unit": UNIT,
+                "ms_per_step": ms, "steps": steps, "fragments_per_step": int(st[-1].fragments_shaded),
+                "fs_invocations_per_step": int(st[-1].fs_invocations), "tile": f"{wk.tile[0]}x{wk.tile[1]}",
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                             "traffic": prof.get("dram_bytes_per_launch"), "peak_source": src,
+                             "kernel": prof.get("kernel", "k_raster"), "kernel_ms": r_ms,
+                             "algorithmic_bytes_per_launch": ab["total"], "byte_model": ab,
+                             "note": "algorithmic bytes: the Rgba16Float read + write of every blended fragment; DRAM "
+                                     "traffic is the target once (tiles stay in registers), so the kernel is "
+                                     "instruction-bound, not HBM-bound"},
+                "parity": parity_of("blend", dev, scene, st[-1])}
+    finally:
+        dev.close()
 
-    # the buffer uploads as one prepared batch (gbr_queue_write_buffers), textures one by one; the
-    # read is queue-ordered after the submission (it waits for it)
-    buffer_writes = W.PreparedWrites([(obj, 0, host.numpy()) for obj, host in pinned if not isinstance(obj, W.Texture)])
-    texture_writes = [(obj, host.numpy()) for obj, host in pinned if isinstance(obj, W.Texture)]
-    read_items = [(t, 0, o.data_ptr(), o.numel()) for t, o in reads]
 
-    def e2e_step():
-        dev.queue.write_buffers(buffer_writes)
-        for obj, host in texture_writes:
-            dev.queue.write_texture(obj, host)
-        dev.queue.submit([cmd])
-        dev.read_textures_into(read_items)
-
-    for _ in range(max(1, min(args.warmup, 3))):
-        e2e_step()
-    e_steps = max(3, min(args.steps, 20))
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(e_steps):
-        e2e_step()
-    e2e_s = (time.perf_counter() - t0) / e_steps
-    # replicas: the slowest rank's time per step, every rank's fragments
-    e2e_s, e2e_rate = replica_rate(frags_per_step, 1, e2e_s)
-    h2d = sum(h.numel() for _, h in pinned)
-
-    if rank == 0:
-        base = cpu_baseline(wk) if world == 1 and not args.no_cpu_baseline else None
-        line = {
-            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": float(np.mean(gpu_ms)), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": wk.dtype, "data": "synthetic (seeded)",
-            "config": {**wk.config(launch_mode=args.launch_mode, graphs=args.graphs),
-                       "tile": dev_tile(args) if not args.autotune else f"autotuned: {stats[-1].tile_shape >> 8}",
-                       "warps_per_tile": dev_warps(args) if not args.autotune else f"autotuned: {stats[-1].tile_shape & 0xFF}",
-                       **over},
-            "fragments_per_step": frags_per_step, "wall_ms_per_step": wall * 1e3 / args.steps,
-            "generic_setup_prims_per_step": int(stats[-1].generic_setup_prims),
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak if achieved else None, "traffic": raster_traffic(wk.name) if not over else None,
-                         "peak_source": peak_src, "kernel": raster_profile(wk.name).get("kernel", "raster kernel (k_raster_vis or k_raster)"),
-                         "algorithmic_bytes_per_launch": alg_bytes, "kernel_ms": r_ms},
-            "cpu_baseline": base,
-            "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": int(h2d) * world,
-                    "d2h_bytes_per_step": int(out_bytes) * world, "ms_per_step": e2e_s * 1e3},
-            "gpu_launches": launches,
-            "clocks": clocks.summary(),
-        }
-        if per_draw is not None:
-            line["per_draw_path"] = per_draw
-        print(json.dumps(line), flush=True)
-    dev.close()
-    if world > 1:
-        torch.distributed.destroy_process_group()
+SERVE_TILE = (32, 8)  # tile side, warps per tile of both serving arms (--tile / --warps override)
 
 
 def serve_arm(dev, sset, lam, duration, seed, max_submissions):
@@ -449,48 +421,188 @@ def serve_summary(stats, wall, lam, duration):
             "kernel_launches": int(sum(s.kernel_launches / max(1, s.batched_with) for s in stats))}
 
 
-SERVE_TILE = (32, 8)  # tile side, warps per tile of both serving arms (--tile / --warps override)
-
-
-def run_serve(args):
-    """Serving loop: Poisson arrivals of pre-recorded submissions over resident meshes, textures and
-    targets; the batched server (continuous batching, HBM-budget admission) and, on the same
-    arrival stream, the plain per-draw path."""
-    import torch
-
+def serving_arms(local, lam, duration, tile, warps):
+    """The served (continuous batching, HBM-budget admission) and the per-draw arm on the same
+    Poisson arrival stream of pre-recorded submissions over resident resources."""
     from wgpu_gb300 import api as W
     from wgpu_gb300 import workloads as wl
 
-    rank, world, local = dist_env()
-    torch.cuda.set_device(local)
-    lam, duration = args.rate, args.duration
     arms = {}
     for name, kw in (("served", dict(batch_submissions=True, launch_mode=W.LaunchMode.BATCHED)),
                      ("per_draw", dict(batch_submissions=False, launch_mode=W.LaunchMode.PER_DRAW))):
-        dev = W.Device(device_ordinal=local, tile_size=args.tile or SERVE_TILE[0], warps_per_tile=args.warps or SERVE_TILE[1],
-                       hbm_budget_bytes=80 << 30, **kw)
-        sset = wl.serving_set(dev)
-        for c in sset.commands[:8]:  # warm-up (allocations, first launches)
-            dev.poll(True, dev.queue.submit([c]))
-        with ClockSampler(local) as clocks:
-            stats, wall = serve_arm(dev, sset, lam, duration, seed=11, max_submissions=int(lam * duration * 2) + 16)
-        arms[name] = serve_summary(stats, wall, lam, duration)
-        arms[name]["clocks"] = clocks.summary()
-        dev.close()
-        del sset
+        dev = W.Device(device_ordinal=local, tile_size=tile, warps_per_tile=warps, hbm_budget_bytes=80 << 30, **kw)
+        try:
+            sset = wl.serving_set(dev)
+            for c in sset.commands[:8]:  # warm-up (allocations, first launches)
+                dev.poll(True, dev.queue.submit([c]))
+            with ClockSampler(local) as clocks:
+                stats, wall = serve_arm(dev, sset, lam, duration, seed=11, max_submissions=int(lam * duration * 2) + 16)
+            arms[name] = serve_summary(stats, wall, lam, duration)
+            arms[name]["clocks"] = clocks.summary()
+            del sset
+        finally:
+            dev.close()
+    return arms
+
+
+SERVE_WORKLOAD = ("serving: Poisson arrivals of submissions with 1-64 draws (log-uniform) of 512 resident meshes "
+                  "(100..200k tris) and 128 textures into 256^2..1920x1080 Rgba8Unorm + Depth32Float targets, "
+                  "textured Lambert / vertex colour, 80 GB HBM admission budget")
+
+
+def run_ours(args, wk: Workload):
+    import torch
+
+    from wgpu_gb300 import api as W
+
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.distributed.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    dev = W.Device(device_ordinal=local, profile=wk.profile, time_kernels=True, tile_size=args.tile,
+                   warps_per_tile=args.warps, launch_mode=LAUNCH_MODES[args.launch_mode], use_graphs=args.graphs)
+    over = {}
+    if args.quads and wk.name == "blend":
+        over = {"n_quads": args.quads}
+    if wk.name == "batched" and (args.draws or args.targets):
+        over = {"n_draws": args.draws or wk.kwargs["n_draws"], "n_targets": args.targets or wk.kwargs["n_targets"]}
+    scene = wk.build(dev, **over)
+    cmd = record(dev, scene)
+
+    if args.autotune:  # the tuner's trial submissions (one per candidate tile shape), before warm-up
+        for _ in range(TUNE_TRIALS):
+            dev.flush_caches()
+            dev.poll(True, dev.queue.submit([cmd]))
+    timed_steps(dev, cmd, args.warmup)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    barrier()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        stats = timed_steps(dev, cmd, args.steps)
+        wall = time.perf_counter() - t0
+    barrier()
+    last = stats[-1]
+    frags_per_step = int(last.fragments_shaded)
+    parity = parity_of(wk.name, dev, scene, last) if not over else {"status": "not checked (cut workload)"}
+    shape = (last.tile_shape >> 8, last.tile_shape & 0xFF)
+
+    gpu_ms = [s.gpu_ms for s in stats]
+    raster_ms = [s.raster_ms for s in stats]
+    device_s, value = replica_rate(frags_per_step, args.steps, sum(gpu_ms) / 1e3)
+    launches = int(sum(s.kernel_launches for s in stats))
+
+    # roofline of the dominant kernel: algorithmic bytes per launch / its event-timed duration
+    ab = algorithmic_bytes(wk, scene, last)
+    peak, peak_src = measured_peak_hbm()
+    r_ms = float(np.mean(raster_ms))
+    achieved = ab["total"] / (r_ms / 1e3) / 1e9 if r_ms > 0 else None
+    prof = raster_profile(wk.name)
+
+    # end to end through the C ABI: inputs from pinned host memory, every colour target read back
+    pinned = [(obj, torch.from_numpy(np.array(arr).reshape(-1).view(np.uint8)).pin_memory())
+              for obj, arr in scene.uploads]
+    from wgpu_gb300 import workloads as wl
+
+    reads = []
+    for t, _ in wl.scene_targets(scene):
+        n = t.width * t.height * W.BYTES_PER_TEXEL[t.format]
+        reads.append((t, torch.empty(n, dtype=torch.uint8).pin_memory()))
+    out_bytes = sum(o.numel() for _, o in reads)
+    buffer_writes = W.PreparedWrites([(obj, 0, host.numpy()) for obj, host in pinned if not isinstance(obj, W.Texture)])
+    texture_writes = [(obj, host.numpy()) for obj, host in pinned if isinstance(obj, W.Texture)]
+    read_items = [(t, 0, o.data_ptr(), o.numel()) for t, o in reads]
+
+    def e2e_step():
+        dev.queue.write_buffers(buffer_writes)
+        for obj, host in texture_writes:
+            dev.queue.write_texture(obj, host)
+        dev.queue.submit([cmd])
+        dev.read_textures_into(read_items)  # queue-ordered after the submission (it waits for it)
+
+    for _ in range(max(1, min(args.warmup, 3))):
+        e2e_step()
+    e_steps = max(3, min(args.steps, 20))
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / e_steps
+    e2e_s, e2e_rate = replica_rate(frags_per_step, 1, e2e_s)
+    h2d = sum(h.numel() for _, h in pinned)
+    dev.close()
+    del pinned, reads
+
+    extras = {}
+    if wk.name == "batched" and not args.no_extras:
+        pd_steps = max(3, min(args.steps, 10))
+        extras["per_draw_path"] = per_draw_arm(wk, local, shape, False, pd_steps)
+        extras["per_draw_path_graphs"] = per_draw_arm(wk, local, shape, True, pd_steps)
+        extras["fill_bound"] = fill_bound_arm(local, max(5, min(args.steps, 20)))
+        arms = serving_arms(local, 2000.0, 1.0, *SERVE_TILE)
+        extras["serving"] = {"workload": SERVE_WORKLOAD, "tile": f"{SERVE_TILE[0]}x{SERVE_TILE[1]}", **arms}
+        extras["p99_submit_ms"] = arms["served"]["p99_ms"]
+
+    if rank == 0:
+        base = cpu_baseline(wk) if world == 1 and not args.no_cpu_baseline and not over else None
+        cfg = wk.config()
+        if over:
+            cfg = {**cfg, "cut_for_profiling": over}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(np.mean(gpu_ms)), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": wk.dtype, "data": "synthetic (seeded)",
+            "config": cfg,
+            "launch": {"launch_mode": args.launch_mode, "cuda_graphs": bool(args.graphs),
+                       "tile": f"autotuned: {shape[0]}" if args.autotune else shape[0],
+                       "warps_per_tile": f"autotuned: {shape[1]}" if args.autotune else shape[1]},
+            "parity": parity["status"], "parity_detail": parity,
+            "fragments_per_step": frags_per_step, "fs_invocations_per_step": int(last.fs_invocations),
+            "texture_fs_invocations_per_step": int(last.texture_fs_invocations),
+            "wall_ms_per_step": wall * 1e3 / args.steps,
+            "generic_setup_prims_per_step": int(last.generic_setup_prims),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak if achieved else None,
+                         "traffic": prof.get("dram_bytes_per_launch") if not over else None,
+                         "peak_source": peak_src, "kernel": prof.get("kernel", "raster kernel (k_raster_vis or k_raster)"),
+                         "algorithmic_bytes_per_launch": ab["total"], "byte_model": ab, "kernel_ms": r_ms},
+            "cpu_baseline": base,
+            "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": int(h2d) * world,
+                    "d2h_bytes_per_step": int(out_bytes) * world, "ms_per_step": e2e_s * 1e3},
+            "gpu_launches": launches,
+            "clocks": clocks.summary(),
+            **extras,
+        }
+        if "per_draw_path" in extras:
+            line["batched_vs_per_draw"] = value / extras["per_draw_path"]["value"]
+            line["batched_vs_per_draw_graphs"] = value / extras["per_draw_path_graphs"]["value"]
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_serve(args):
+    """The serving loop alone at --rate for --duration seconds."""
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    arms = serving_arms(local, args.rate, args.duration, args.tile or SERVE_TILE[0], args.warps or SERVE_TILE[1])
     s = arms["served"]
     if rank == 0:
         line = {
             "metric": METRIC, "value": s["fragments_per_s"] * world, "unit": UNIT, "n_gpus": world,
             "steps": s["submissions"], "warmup": 8, "ms_per_step": s["mean_ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": "serving: Poisson arrivals of submissions with 1-64 draws (log-uniform) of 512 "
-                                   "resident meshes (100..200k tris) and 128 textures into 256^2..1920x1080 "
-                                   "Rgba8Unorm + Depth32Float targets, textured Lambert / vertex colour",
-                       "lambda_per_s": lam, "hbm_budget_gb": 80, "launch_mode": "batched + merged submissions",
-                       "tile": args.tile or SERVE_TILE[0], "warps_per_tile": args.warps or SERVE_TILE[1],
+            "config": {"workload": SERVE_WORKLOAD, "lambda_per_s": args.rate, "hbm_budget_gb": 80,
                        "l2": "not flushed (inputs resident; a step is one submission)"},
-            "serving": s, "per_draw_path": arms["per_draw"],
+            "launch": {"launch_mode": "batched + merged submissions", "tile": args.tile or SERVE_TILE[0],
+                       "warps_per_tile": args.warps or SERVE_TILE[1]},
+            "serving": s, "per_draw_path": arms["per_draw"], "p99_submit_ms": s["p99_ms"],
             "e2e": {"value": s["fragments_per_s"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0,
                     "note": "wall clock from first submit to last fence through the C ABI; inputs resident"},
             "gpu_launches": s["kernel_launches"], "clocks": s["clocks"],
@@ -498,15 +610,8 @@ def run_serve(args):
         print(json.dumps(line), flush=True)
 
 
+LAUNCH_MODES = {"batched": 0, "per_pass": 2, "per_draw": 1}
 TUNE_TRIALS = 6  # the library times five candidate tile shapes per batch shape, then keeps the fastest
-
-
-def dev_tile(args):
-    return args.tile or 16
-
-
-def dev_warps(args):
-    return args.warps or (2 if dev_tile(args) == 8 else 8)
 
 
 def main():
@@ -517,7 +622,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batched",
                     choices=["textured", "textured_filtered", "blend", "colored", "batched", "serve"])
-    ap.add_argument("--rate", type=float, default=1000.0, help="serve workload: submissions per second")
+    ap.add_argument("--rate", type=float, default=2000.0, help="serve workload: submissions per second")
     ap.add_argument("--duration", type=float, default=2.0, help="serve workload: arrival window in seconds")
     ap.add_argument("--launch-mode", default="batched", choices=list(LAUNCH_MODES))
     ap.add_argument("--graphs", action="store_true", help="replay each submission's launches from a CUDA graph")
@@ -528,7 +633,8 @@ def main():
     ap.add_argument("--draws", type=int, default=0, help="batched workload: number of draws (profiling runs)")
     ap.add_argument("--targets", type=int, default=0, help="batched workload: number of targets (profiling runs)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-per-draw", action="store_true", help="batched workload: skip the per-draw comparison")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="batched workload: skip the per-draw, fill-bound and serving arms (profiling runs)")
     ap.add_argument("--fixed", action="store_true",
                     help="batched workload: no CUDA graph and no autotuner (the workload's fixed tile shape)")
     args = ap.parse_args()
@@ -541,12 +647,9 @@ def main():
         args.tile = args.warps = 0
     elif not args.tile and args.workload in workloads():
         args.tile, args.warps = workloads()[args.workload].tile
-    elif not args.tile:
-        args.tile, args.warps = dev_tile(args), dev_warps(args)
     if args.workload == "serve":
         if args.impl == "reference":
-            wk = workloads()["batched"]
-            run_reference(args, wk)
+            run_reference(args, workloads()["batched"])
         else:
             run_serve(args)
         return

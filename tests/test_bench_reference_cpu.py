@@ -1,6 +1,7 @@
 """The benchmark's reference arm (the oracle on the host cores) runs without a GPU: one JSON line
-with the contract's keys, `impl: reference`, a cpu_baseline describing the run and an e2e object
-with no transfers; under torchrun with two ranks only rank 0 prints, and both exit 0."""
+with the contract's keys, `impl: reference`, the same `config` as the GPU arm's line, a
+cpu_baseline describing the run and an e2e object with no transfers; under torchrun with two
+ranks only rank 0 prints, and both exit 0."""
 
 import json
 import os
@@ -32,14 +33,19 @@ def check_line(d, n_gpus):
 
 
 def test_reference_arm_single_process():
+    """The default workload: whole frames of the batched configuration, as the GPU arm renders."""
+    import bench
+
     lines = reference_lines([sys.executable] + ARGS)
     assert len(lines) == 1
     check_line(lines[0], 1)
+    assert lines[0]["config"] == json.loads(json.dumps(bench.workloads()["batched"].config()))
+    assert lines[0]["fragments_per_step"] == 45935231  # the full frame: 64 targets, 256 draws
 
 
 def test_reference_arm_under_torchrun_two_ranks():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
-           "127.0.0.1", "--master-port", "29573"] + ARGS + ["--gpus", "2"]
+           "127.0.0.1", "--master-port", "29573"] + ARGS + ["--gpus", "2", "--workload", "colored"]
     lines = reference_lines(cmd)
     assert len(lines) == 1  # rank 0 alone
     check_line(lines[0], 2)
