@@ -32,7 +32,7 @@ extern "C" {
 #define GBR_API __attribute__((visibility("default")))
 #endif
 
-#define GBR_ABI_VERSION 1u
+#define GBR_ABI_VERSION 2u
 
 typedef int32_t gbr_status;
 enum {
@@ -281,6 +281,14 @@ typedef struct gbr_depth_stencil_state {
     uint32_t _pad;
 } gbr_depth_stencil_state;
 
+/* One pipeline-overridable constant (wgpu::PipelineCompilationOptions::constants entry): `key`
+ * is an `override`'s @id as a decimal string, or its name; `value` is converted to the override's
+ * type as naga's process_overrides does (shader.rs:52-74).  Read during the call only. */
+typedef struct gbr_pipeline_constant {
+    const char* key;
+    double value;
+} gbr_pipeline_constant;
+
 typedef struct gbr_render_pipeline_desc {
     gbr_shader_module vertex_module;
     char vertex_entry_point[GBR_MAX_ENTRY_POINT_NAME];
@@ -298,6 +306,11 @@ typedef struct gbr_render_pipeline_desc {
     uint32_t color_target_count;
     uint32_t _pad2;
     gbr_color_target_state color_targets[GBR_MAX_COLOR_TARGETS];
+    /* VertexState / FragmentState compilation_options.constants (WGSL modules only) */
+    const gbr_pipeline_constant* vertex_constants;
+    const gbr_pipeline_constant* fragment_constants;
+    uint32_t vertex_constant_count;
+    uint32_t fragment_constant_count;
 } gbr_render_pipeline_desc;
 
 enum gbr_binding_kind { GBR_BINDING_BUFFER = 0, GBR_BINDING_SAMPLER = 1, GBR_BINDING_TEXTURE_VIEW = 2 };

@@ -22,6 +22,7 @@
 #include <limits>
 #include <memory>
 #include <mutex>
+#include <set>
 #include <string>
 #include <thread>
 #include <unordered_map>
@@ -695,6 +696,24 @@ static void process_fragment(FragCtx& fc, uint32_t fx, uint32_t fy, V4 fragment,
             in.var[pv.location][c] = x;
         }
     }
+    PassTargets* tg = ex->tg;
+    // FragmentOutput::depth_test (fragment.rs:427-453): compare with the stored depth, write on a
+    // pass when depth writes are on; true when there is no depth attachment or no depth state
+    auto depth_test = [&]() {
+        if (!(tg->depth && pl->desc.has_depth_stencil)) return true;
+        Texture* d = tg->depth;
+        float* dp = reinterpret_cast<float*>(d->mips[0].data()) + (size_t)fy * d->desc.size.width + fx;
+        if (!compare(pl->desc.depth_stencil.depth_compare, fragment.z, *dp)) return false;
+        if (pl->desc.depth_stencil.depth_write_enabled) *dp = fragment.z;
+        return true;
+    };
+    // @early_depth_test (fragment.rs:166-194): none = late test only; Force = early test only
+    // (its result stands at the colour output); Allow = early test, then the late test again
+    bool have_result = false, result = true;
+    if (fs->early_depth != 0) {
+        if (!depth_test()) return;  // early depth test reject: the fragment stage does not run
+        if (fs->early_depth == 1) have_result = true;
+    }
     FsOut out;
     out.killed = false;
     ex->cnt.fs_runs++;
@@ -703,18 +722,7 @@ static void process_fragment(FragCtx& fc, uint32_t fx, uint32_t fy, V4 fragment,
     if (out.killed) return;  // EntryPointError::Killed (fragment.rs:204-208)
     if (fs->num_outputs == 0) return;
     // Late depth test at the first @location output (fragment.rs:470-479).
-    bool pass = true;
-    PassTargets* tg = ex->tg;
-    if (tg->depth && pl->desc.has_depth_stencil) {
-        Texture* d = tg->depth;
-        float* dp = reinterpret_cast<float*>(d->mips[0].data()) + (size_t)fy * d->desc.size.width + fx;
-        float stored = *dp;
-        if (compare(pl->desc.depth_stencil.depth_compare, fragment.z, stored)) {
-            if (pl->desc.depth_stencil.depth_write_enabled) *dp = fragment.z;
-        } else {
-            pass = false;
-        }
-    }
+    const bool pass = have_result ? result : depth_test();
     if (!pass) return;
     for (int o = 0; o < fs->num_outputs; ++o) {
         Texture* t = tg->color[o];
@@ -1134,7 +1142,7 @@ static void run_pass_band(Exec* ex, const DecodedPass& dp) {
     }
 }
 
-static void execute_pass(Device* dev, const DecodedPass& dp, Counters& total) {
+static void execute_pass(Device* dev, const DecodedPass& dp, Counters& total, int threads) {
     // State::new (render_pass/state.rs:77-133): all attachments must have the same size.
     PassTargets tg;
     bool have = false;
@@ -1161,7 +1169,7 @@ static void execute_pass(Device* dev, const DecodedPass& dp, Counters& total) {
         tg.depth = t;
         size_of(t);
     }
-    int nt = std::max(1, g_threads);
+    int nt = std::max(1, threads);
     if ((uint32_t)nt > tg.height) nt = std::max(1u, tg.height);
     std::vector<Exec> ex(nt);
     std::vector<std::string> errs(nt);
@@ -1194,6 +1202,95 @@ static void execute_pass(Device* dev, const DecodedPass& dp, Counters& total) {
         total.tex_runs += ex[i].cnt.tex_runs;
     }
     total.primitives += ex[0].cnt.primitives;  // every thread assembles all primitives
+}
+
+// The textures a render pass renders to (its attachments) and samples (texture views of the bind
+// groups it sets).
+static void pass_textures(Device* dev, const DecodedPass& dp, std::set<Texture*>& writes, std::set<Texture*>& reads) {
+    for (uint32_t a = 0; a < dp.begin.color_attachment_count && a < GBR_MAX_COLOR_TARGETS; ++a)
+        if (dp.begin.color_attachments[a].view) writes.insert(dev->get<Texture>(dp.begin.color_attachments[a].view, "texture"));
+    if (dp.begin.has_depth_attachment && dp.begin.depth_attachment.view)
+        writes.insert(dev->get<Texture>(dp.begin.depth_attachment.view, "texture"));
+    for (const auto& c : dp.cmds) {
+        if (c.first.opcode != GBR_OP_SET_BIND_GROUP || c.second.size() < sizeof(gbr_cmd_set_bind_group)) continue;
+        gbr_cmd_set_bind_group sb;
+        std::memcpy(&sb, c.second.data(), sizeof sb);
+        if (!sb.bind_group) continue;
+        const BindGroup* g = dev->get<BindGroup>(sb.bind_group, "bind group");
+        for (uint32_t e = 0; e < g->desc.entry_count; ++e)
+            if (g->desc.entries[e].kind == GBR_BINDING_TEXTURE_VIEW)
+                reads.insert(dev->get<Texture>(g->desc.entries[e].resource, "texture"));
+    }
+}
+
+// End of the run of render passes from `first` that do not depend on one another: none renders
+// to a texture another one renders to or samples.  Their results do not depend on their order.
+static size_t independent_run(Device* dev, const std::vector<DecodedPass>& passes, size_t first) {
+    std::set<Texture*> writes, reads;
+    size_t j = first;
+    for (; j < passes.size() && !passes[j].is_copy; ++j) {
+        std::set<Texture*> w, r;
+        try {
+            pass_textures(dev, passes[j], w, r);
+        } catch (const Error&) {
+            return j == first ? first + 1 : j;  // the pass reports its own error when it runs
+        }
+        bool clash = false;
+        for (Texture* t : w) clash = clash || writes.count(t) || reads.count(t);
+        for (Texture* t : r) clash = clash || writes.count(t);
+        if (clash) break;
+        writes.insert(w.begin(), w.end());
+        reads.insert(r.begin(), r.end());
+    }
+    return std::max(j, first + 1);
+}
+
+// Independent passes [first, last) on g_threads host threads, one pass per thread at a time
+// (largest target first).  The first error in pass order is reported.
+static void execute_passes_parallel(Device* dev, const std::vector<DecodedPass>& passes, size_t first, size_t last,
+                                    Counters& total) {
+    const size_t n = last - first;
+    std::vector<size_t> order(n);
+    std::vector<uint64_t> area(n, 0);
+    for (size_t k = 0; k < n; ++k) {
+        order[k] = first + k;
+        const gbr_cmd_begin_render_pass& b = passes[first + k].begin;
+        const uint64_t h = b.color_attachment_count && b.color_attachments[0].view ? b.color_attachments[0].view
+                           : b.has_depth_attachment                                ? b.depth_attachment.view
+                                                                                   : 0;
+        if (h) {
+            const Texture* t = dev->get<Texture>(h, "texture");
+            area[k] = (uint64_t)t->desc.size.width * t->desc.size.height;
+        }
+    }
+    std::stable_sort(order.begin(), order.end(), [&](size_t a, size_t b) { return area[a - first] > area[b - first]; });
+    std::vector<Counters> cnt(n);
+    std::vector<gbr_status> sts(n, GBR_OK);
+    std::vector<std::string> errs(n);
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+        for (size_t k; (k = next.fetch_add(1)) < n;) {
+            const size_t p = order[k];
+            try {
+                execute_pass(dev, passes[p], cnt[p - first], 1);
+            } catch (const Error& e) {
+                sts[p - first] = e.status;
+                errs[p - first] = e.msg;
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    const int nt = (int)std::min<size_t>((size_t)g_threads, n);
+    for (int i = 0; i < nt; ++i) th.emplace_back(work);
+    for (auto& t : th) t.join();
+    for (size_t k = 0; k < n; ++k)
+        if (sts[k] != GBR_OK) throw Error{sts[k], errs[k]};
+    for (const Counters& c : cnt) {
+        total.fragments += c.fragments;
+        total.primitives += c.primitives;
+        total.fs_runs += c.fs_runs;
+        total.tex_runs += c.tex_runs;
+    }
 }
 
 }  // namespace orc
@@ -1574,14 +1671,22 @@ ORC_API gbr_status orc_queue_submit(gbr_device d, const void* cmds, uint64_t len
         uint64_t idx = dev->next_submission++;
         Counters total;
         uint64_t draws = 0;
-        for (const auto& p : passes) {
-            if (p.is_copy) {
-                execute_copy(dev, p.cmds[0].first, p.cmds[0].second.data());
-                continue;
-            }
+        for (const auto& p : passes)
             for (const auto& c : p.cmds)
                 if (c.first.opcode == GBR_OP_DRAW || c.first.opcode == GBR_OP_DRAW_INDEXED) ++draws;
-            execute_pass(dev, p, total);
+        for (size_t i = 0; i < passes.size();) {
+            if (passes[i].is_copy) {
+                execute_copy(dev, passes[i].cmds[0].first, passes[i].cmds[0].second.data());
+                ++i;
+                continue;
+            }
+            const size_t j = independent_run(dev, passes, i);
+            if (g_threads > 1 && j - i > 1) {
+                execute_passes_parallel(dev, passes, i, j, total);
+            } else {
+                for (size_t k = i; k < j; ++k) execute_pass(dev, passes[k], total, g_threads);
+            }
+            i = j;
         }
         gbr_submission_stats s;
         std::memset(&s, 0, sizeof s);

@@ -10,6 +10,9 @@
 
 #include <cstdint>
 #include <cstring>
+#include <iterator>
+#include <string>
+#include <vector>
 
 #include "orc_core.hpp"
 
@@ -80,6 +83,9 @@ struct Program {
     ProgramBinding bindings[4];
     bool (*vs)(const VsIn&, const ProgramBindings&, VsOut&);
     void (*fs)(const FsIn&, const ProgramBindings&, FsOut&);
+    // @early_depth_test of the fragment entry point (naga::EarlyDepthTest, read by
+    // fragment.rs:83-86): 0 = none, 1 = Force, 2 = Allow
+    int early_depth = 0;
 };
 
 static inline float ld_f32(const uint8_t* p, size_t off) {
@@ -184,7 +190,33 @@ static void fs_mesh_color_discard(const FsIn& in, const ProgramBindings&, FsOut&
     out.color[0] = {in.var[0][0], in.var[0][1], in.var[0][2], 1.0f};
 }
 
-static const Program kPrograms[] = {
+// ---- clip_flat_id: @location(0) @interpolate(flat) id: u32 = 0x7fc00000 | (vertex_index &
+// 0xffff) (as an f32 a NaN: any arithmetic on the slot would show) and a linear colour; the
+// fragment stage returns vec4f(f32(id & 0xffu) / 255.0, colour.x, colour.y, 1.0).
+static bool vs_clip_flat_id(const VsIn& in, const ProgramBindings&, VsOut& out) {
+    out.position = {in.attr[0][0], in.attr[0][1], in.attr[0][2], in.attr[0][3]};
+    const uint32_t id = 0x7fc00000u | (in.vertex_index & 0xffffu);
+    std::memcpy(&out.var[0][0], &id, 4);
+    for (int k = 0; k < 3; ++k) out.var[1][k] = in.attr[1][k];
+    return true;
+}
+static void fs_clip_flat_id(const FsIn& in, const ProgramBindings&, FsOut& out) {
+    uint32_t id;
+    std::memcpy(&id, &in.var[0][0], 4);
+    out.killed = false;
+    out.color[0] = {(float)(id & 0xffu) / 255.0f, in.var[1][0], in.var[1][1], 1.0f};
+}
+// ---- clip_discard: clip_passthrough that discards fragments whose red channel is below 0.5.
+static void fs_clip_discard(const FsIn& in, const ProgramBindings&, FsOut& out) {
+    if (in.var[0][0] < 0.5f) {
+        out.killed = true;
+        return;
+    }
+    out.killed = false;
+    out.color[0] = {in.var[0][0], in.var[0][1], in.var[0][2], in.var[0][3]};
+}
+
+static const Program kBasePrograms[] = {
     {"colored_triangle", 0, {}, 1, {{0, 4, INTERP_LINEAR}}, 1, 0, {}, vs_colored_triangle, fs_passthrough_vec4},
     {"mesh_color", 2, {{0, 3, SK_F32}, {1, 3, SK_F32}}, 1, {{0, 3, INTERP_LINEAR}}, 1, 1, {{0, 0, 0, 64}},
      vs_mesh_color, fs_mesh_color},
@@ -199,10 +231,41 @@ static const Program kPrograms[] = {
      fs_passthrough_vec4},
     {"clip_passthrough", 2, {{0, 4, SK_F32}, {1, 4, SK_F32}}, 1, {{0, 4, INTERP_LINEAR}}, 1, 0, {},
      vs_clip_passthrough, fs_passthrough_vec4},
+    {"clip_flat", 2, {{0, 4, SK_F32}, {1, 4, SK_F32}}, 1, {{0, 4, INTERP_FLAT}}, 1, 0, {}, vs_clip_passthrough,
+     fs_passthrough_vec4},
+    {"clip_flat_id", 2, {{0, 4, SK_F32}, {1, 4, SK_F32}}, 2, {{0, 1, INTERP_FLAT}, {1, 3, INTERP_LINEAR}}, 1, 0, {},
+     vs_clip_flat_id, fs_clip_flat_id},
+    {"clip_discard", 2, {{0, 4, SK_F32}, {1, 4, SK_F32}}, 1, {{0, 4, INTERP_LINEAR}}, 1, 0, {}, vs_clip_passthrough,
+     fs_clip_discard},
 };
 
+// The programs, and the variants whose fragment entry point carries @early_depth_test(force)
+// ("<name>@early_force") or @early_depth_test(<conservative>) ("<name>@early_allow").
+static inline const std::vector<Program>& programs() {
+    static const std::vector<Program> table = [] {
+        std::vector<Program> v(std::begin(kBasePrograms), std::end(kBasePrograms));
+        static const char* const kEarly[] = {"clip_passthrough", "clip_discard", "clip_flat_id", "mesh_color",
+                                             "mesh_color_discard"};
+        static std::vector<std::string> names;
+        names.reserve(2 * (sizeof kEarly / sizeof kEarly[0]));
+        const size_t base = v.size();
+        for (const char* n : kEarly)
+            for (int mode : {1, 2})
+                for (size_t i = 0; i < base; ++i)
+                    if (std::strcmp(v[i].name, n) == 0) {
+                        names.push_back(std::string(n) + (mode == 1 ? "@early_force" : "@early_allow"));
+                        Program q = v[i];
+                        q.name = names.back().c_str();
+                        q.early_depth = mode;
+                        v.push_back(q);
+                    }
+        return v;
+    }();
+    return table;
+}
+
 static inline const Program* find_program(const char* name) {
-    for (const Program& p : kPrograms)
+    for (const Program& p : programs())
         if (std::strcmp(p.name, name) == 0) return &p;
     return nullptr;
 }

@@ -10,7 +10,8 @@ def random_clip_triangles(dev, n_tris, width, height, seed, topology=W.Primitive
                           index_format=None, depth=None, cull=W.Face.NONE, front_face=W.FrontFace.CCW,
                           depth_write=True, spread=1.6, w_range=(0.3, 2.0), z_range=(-0.3, 1.3),
                           clear=(0.1, 0.2, 0.3, 1.0), color_format=W.TextureFormat.RGBA8_UNORM,
-                          instances=1, base_vertex=0, scissor=None, viewport=None, blend=None, depth_clear=0.75):
+                          instances=1, base_vertex=0, scissor=None, viewport=None, blend=None, depth_clear=0.75,
+                          program="clip_passthrough", stats=None):
     """Random triangles given directly in clip space (clip_passthrough program): they cross
     every clip plane, so the clipper, the sub-triangle order and degenerate spans all get hit."""
     rng = np.random.default_rng(seed)
@@ -29,7 +30,7 @@ def random_clip_triangles(dev, n_tris, width, height, seed, topology=W.Primitive
             idx = dev.create_buffer_init(perm.astype(np.uint16))
         else:
             idx = dev.create_buffer_init(perm.astype(np.uint32))
-    sm = dev.create_shader_module(native="clip_passthrough")
+    sm = dev.create_shader_module(native=program)
     pl = dev.create_render_pipeline(
         sm, [W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 0)]),
              W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 1)])],
@@ -58,6 +59,8 @@ def random_clip_triangles(dev, n_tris, width, height, seed, topology=W.Primitive
     dev.poll(True, sub)
     out = dev.read_texture(color)
     d = dev.read_texture(dtex) if dtex is not None else None
+    if stats is not None:
+        stats.append(dev.submission_stats(sub))
     return out, d, dev.submission_stats(sub).fragments_shaded
 
 
@@ -113,7 +116,8 @@ def restart_strips(dev, n_indices, width, height, seed, index_format=W.IndexForm
 
 
 def lines_points(dev, topology, n, width, height, seed, index_format=None, restart=False, instances=1,
-                 depth=W.CompareFunction.LESS_EQUAL, scissor=None, clear=(0.0, 0.0, 0.0, 1.0)):
+                 depth=W.CompareFunction.LESS_EQUAL, scissor=None, clear=(0.0, 0.0, 0.0, 1.0),
+                 program="clip_passthrough", depth_write=True):
     """Lines or points given in clip space (clip_passthrough program), crossing the clip planes:
     line lists / strips (optionally indexed, with separator indices) and point lists."""
     rng = np.random.default_rng(seed)
@@ -124,12 +128,12 @@ def lines_points(dev, topology, n, width, height, seed, index_format=None, resta
     col = rng.uniform(0, 1, (nv, 4)).astype(np.float32)
     vb_pos = dev.create_buffer_init(pos)
     vb_col = dev.create_buffer_init(col)
-    sm = dev.create_shader_module(native="clip_passthrough")
+    sm = dev.create_shader_module(native=program)
     sif = index_format if restart else W.IndexFormat.NONE
     pl = dev.create_render_pipeline(
         sm, [W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 0)]),
              W.VertexBufferLayout(16, [W.VertexAttribute(W.VertexFormat.FLOAT32X4, 0, 1)])],
-        W.PrimitiveState(topology, strip_index_format=sif), W.DepthStencilState(True, depth), sm,
+        W.PrimitiveState(topology, strip_index_format=sif), W.DepthStencilState(depth_write, depth), sm,
         [W.ColorTargetState(W.TextureFormat.RGBA8_UNORM)])
     color = dev.create_texture(width, height, W.TextureFormat.RGBA8_UNORM)
     dtex = dev.create_texture(width, height, W.TextureFormat.DEPTH32_FLOAT)
@@ -319,3 +323,40 @@ def copy_scenario(dev, seed=5):
         "T1": [dev.read_texture(T1, m) for m in range(3)], "T2": [dev.read_texture(T2, m) for m in range(3)],
         "X": dev.read_texture(s.color), "Y": dev.read_texture(Y),
     }
+
+
+def perspective_sphere(dev, width, height, seed=9, level=3, eye=1.25, near=0.45, depth=W.CompareFunction.LESS):
+    """A vertex-coloured icosphere seen from close by with perspective-correct interpolation
+    (mesh_color_perspective, extension profile): the near plane cuts through the sphere, so
+    clipped triangles interpolate with the clip barycentrics and 1/w of the unclipped vertices."""
+    v, f = wl.icosphere(level)
+    rng = np.random.default_rng(seed)
+    col = rng.random((len(v), 3))
+    vdata = np.concatenate([v, col], 1).astype(np.float32)
+    vb = dev.create_buffer_init(vdata)
+    ib = dev.create_buffer_init(f.ravel())
+    mvp = wl.camera_mvp(width, height, eye=(0.3, 0.2, eye), near=near)
+    ub = dev.create_buffer_init(wl.mvp_bytes(mvp))
+    sm = dev.create_shader_module(native="mesh_color_perspective")
+    pl = dev.create_render_pipeline(
+        sm, [W.VertexBufferLayout(24, [W.VertexAttribute(W.VertexFormat.FLOAT32X3, 0, 0),
+                                       W.VertexAttribute(W.VertexFormat.FLOAT32X3, 12, 1)])],
+        W.PrimitiveState(W.PrimitiveTopology.TRIANGLE_LIST, cull_mode=W.Face.NONE),
+        W.DepthStencilState(True, depth) if depth is not None else None, sm,
+        [W.ColorTargetState(W.TextureFormat.RGBA8_UNORM)])
+    bg = dev.create_bind_group([W.BindGroupEntry(0, ub)])
+    color = dev.create_texture(width, height, W.TextureFormat.RGBA8_UNORM)
+    dtex = dev.create_texture(width, height, W.TextureFormat.DEPTH32_FLOAT) if depth is not None else None
+    enc = dev.create_command_encoder()
+    rp = enc.begin_render_pass([W.RenderPassColorAttachment(color, (0.0, 0.0, 0.0, 1.0))],
+                               W.RenderPassDepthStencilAttachment(dtex, 1.0) if dtex is not None else None)
+    rp.set_pipeline(pl)
+    rp.set_bind_group(0, bg)
+    rp.set_vertex_buffer(0, vb)
+    rp.set_index_buffer(ib, W.IndexFormat.UINT32)
+    rp.draw_indexed(range(0, f.size))
+    rp.end()
+    sub = dev.queue.submit([enc.finish()])
+    dev.poll(True, sub)
+    st = dev.submission_stats(sub)
+    return (dev.read_texture(color), dev.read_texture(dtex) if dtex is not None else None, st.fragments_shaded), st

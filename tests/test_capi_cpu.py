@@ -37,7 +37,9 @@ def test_library_exports_every_declared_symbol(libgbr):
 
 def test_abi_version(libgbr):
     libgbr.gbr_abi_version.restype = ctypes.c_uint32
-    assert libgbr.gbr_abi_version() == 1
+    from wgpu_gb300 import _abi as A
+
+    assert libgbr.gbr_abi_version() == A.GBR_ABI_VERSION == 2
 
 
 def test_device_create_without_gpu_fails_cleanly(libgbr):
@@ -49,7 +51,7 @@ def test_device_create_without_gpu_fails_cleanly(libgbr):
     from wgpu_gb300 import _abi as A
 
     cfg = A.DeviceConfig()
-    cfg.abi_version = 1
+    cfg.abi_version = A.GBR_ABI_VERSION
     out = ctypes.c_uint64()
     lib = A.Lib(libgbr, "gbr_")
     st = lib.device_create(ctypes.byref(cfg), ctypes.byref(out))
@@ -64,13 +66,13 @@ STRUCTS = ["gbr_device_config", "gbr_limits", "gbr_texture_desc", "gbr_texel_cop
            "gbr_cmd_set_bind_group", "gbr_cmd_set_index_buffer", "gbr_cmd_set_vertex_buffer", "gbr_cmd_set_viewport",
            "gbr_cmd_draw", "gbr_cmd_draw_indexed", "gbr_cmd_copy_buffer_to_buffer", "gbr_texel_copy_texture_info",
            "gbr_cmd_copy_buffer_texture", "gbr_cmd_copy_texture_to_texture", "gbr_cmd_clear_buffer",
-           "gbr_cmd_clear_texture", "gbr_buffer_write"]
+           "gbr_cmd_clear_texture", "gbr_buffer_write", "gbr_pipeline_constant"]
 PY = ["DeviceConfig", "Limits", "TextureDesc", "TexelCopyBufferLayout", "SamplerDesc", "VertexAttribute",
       "VertexBufferLayout", "ColorTargetState", "PrimitiveState", "DepthStencilState", "RenderPipelineDesc",
       "BindGroupEntry", "BindGroupDesc", "SubmissionStats", "ColorAttachment", "DepthAttachment",
       "CmdBeginRenderPass", "CmdSetBindGroup", "CmdSetIndexBuffer", "CmdSetVertexBuffer", "CmdSetViewport",
       "CmdDraw", "CmdDrawIndexed", "CmdCopyBufferToBuffer", "TexelCopyTextureInfo", "CmdCopyBufferTexture",
-      "CmdCopyTextureToTexture", "CmdClearBuffer", "CmdClearTexture", "BufferWrite"]
+      "CmdCopyTextureToTexture", "CmdClearBuffer", "CmdClearTexture", "BufferWrite", "PipelineConstant"]
 
 
 def test_ctypes_layouts_match_header(tmp_path):

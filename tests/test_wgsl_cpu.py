@@ -78,3 +78,64 @@ def test_parse_error(lib):
     with pytest.raises(W.GbrError) as e:
         W.wgsl_translate(lib, "@vertex fn main( -> { }", "main")
     assert e.value.status == -7
+
+
+# Attributes, interpolation and overrides: what the front end cannot honour fails the module
+# instead of being dropped.
+VS_HEAD = "struct V { @builtin(position) p: vec4f, %s };\n"
+VS_FN = ("@vertex fn vmain(@builtin(vertex_index) vi: u32) -> V {\n  var o: V;\n  o.p = vec4f(0.0, 0.0, 0.0, 1.0);\n"
+         "  %s\n  return o;\n}\n")
+FS_FN = "%s@fragment fn fmain(%s) -> @location(0) vec4f {\n  return vec4f(%s);\n}\n"
+
+
+def program(member, assign, fs_attr, fs_param, fs_value):
+    return VS_HEAD % member + VS_FN % assign + FS_FN % (fs_attr, fs_param, fs_value)
+
+
+@pytest.mark.parametrize("src,status", [
+    # an attribute nobody knows
+    (program("@location(0) c: f32", "o.c = 1.0;", "@foo ", "@location(0) c: f32", "c, 0.0, 0.0, 1.0"), -7),
+    # layout attributes the uniform loader would not honour
+    ("struct U { @align(16) a: f32 };\n" + program("@location(0) c: f32", "o.c = 1.0;", "", "@location(0) c: f32",
+                                                   "c, 0.0, 0.0, 1.0"), A.ERR_UNSUPPORTED),
+    # integer inter-stage values must be flat (naga validation; the reference panics otherwise)
+    (program("@location(0) @interpolate(linear) i: u32", "o.i = vi;", "",
+             "@location(0) @interpolate(linear) i: u32", "f32(i), 0.0, 0.0, 1.0"), -7),
+    # a sampling that does not fit the interpolation type
+    (program("@location(0) @interpolate(flat, center) c: f32", "o.c = 1.0;", "",
+             "@location(0) @interpolate(flat, center) c: f32", "c, 0.0, 0.0, 1.0"), -7),
+    # @early_depth_test on a vertex entry point, and with an unknown argument
+    (program("@location(0) c: f32", "o.c = 1.0;", "", "@location(0) c: f32",
+             "c, 0.0, 0.0, 1.0").replace("@vertex fn", "@early_depth_test(force) @vertex fn"), -7),
+    # attributes on declarations that take none
+    ("@group(0) " + program("@location(0) c: f32", "o.c = 1.0;", "", "@location(0) c: f32", "c, 0.0, 0.0, 1.0"), -7),
+    ("@location(1) const q = 1.0;\n" + program("@location(0) c: f32", "o.c = q;", "", "@location(0) c: f32",
+                                                 "c, 0.0, 0.0, 1.0"), -7),
+    (program("@location(0) c: f32", "o.c = 1.0;", "@early_depth_test(sometimes) ", "@location(0) c: f32",
+             "c, 0.0, 0.0, 1.0"), -7),
+    # an override with neither a pipeline value nor an initializer
+    ("@id(3) override k: f32;\n" + program("@location(0) c: f32", "o.c = k;", "", "@location(0) c: f32",
+                                           "c, 0.0, 0.0, 1.0"), -7),
+])
+def test_unhonoured_attributes_fail(lib, src, status):
+    with pytest.raises(W.GbrError) as e:
+        W.wgsl_translate(lib, src, "vmain", "fmain")
+    assert e.value.status == status, str(e.value)
+
+
+def test_flat_and_early_depth_translate(lib):
+    """Integer flat values travel as bits (no arithmetic); integers default to flat, floats to
+    perspective; @early_depth_test(force) is accepted on the fragment entry point."""
+    src = program("@location(0) i: u32, @location(1) @interpolate(flat, either) c: vec2f",
+                  "o.i = vi;\n  o.c = vec2f(1.0, 2.0);", "@early_depth_test(force) ",
+                  "@location(0) i: u32, @location(1) @interpolate(flat) c: vec2f", "f32(i), c.x, c.y, 1.0")
+    code = W.wgsl_translate(lib, src, "vmain", "fmain")
+    assert "__uint_as_float" in code and "__float_as_uint" in code
+
+
+def test_override_initializer_is_used_without_a_pipeline_value(lib):
+    src = ("override k: f32 = 0.25;\n" +
+           program("@location(0) @interpolate(linear) c: f32", "o.c = k;", "",
+                   "@location(0) @interpolate(linear) c: f32", "c, 0.0, 0.0, 1.0"))
+    code = W.wgsl_translate(lib, src, "vmain", "fmain")
+    assert "g_v_k" in code

@@ -39,8 +39,16 @@ enum Program : uint32_t {
     PROG_QUAD_COLOR = 5,
     PROG_CLIP_PASSTHROUGH = 6,
     PROG_JIT = 7,  // a WGSL program compiled into its own module (jit_vs / jit_fs)
-    PROG_COUNT = 8
+    PROG_CLIP_FLAT = 8,     // clip_passthrough with the colour @interpolate(flat)
+    PROG_CLIP_FLAT_ID = 9,  // an integer @interpolate(flat) vertex id and a linear colour
+    PROG_CLIP_DISCARD = 10, // clip_passthrough that discards where red < 0.5
+    PROG_COUNT = 11
 };
+
+// @early_depth_test of a fragment entry point (naga::EarlyDepthTest, read by
+// render_pass/fragment.rs:83-86, 166-194): none = the late test only, Force = the early test
+// only, Allow = the early test and then the late test again at the colour output.
+enum EarlyDepth : uint32_t { EARLY_DEPTH_NONE = 0, EARLY_DEPTH_FORCE = 1, EARLY_DEPTH_ALLOW = 2 };
 
 enum Interp : uint8_t { INTERP_LINEAR = 0, INTERP_PERSPECTIVE = 1, INTERP_FLAT = 2 };
 
@@ -161,6 +169,8 @@ struct DrawDesc {
     uint32_t lod_var;        // extension-profile sampling: 1 + varying index of u (v follows), 0 = none
     uint32_t raster_rule;    // RASTER_RULE_SCANLINE / RASTER_RULE_EDGE
     uint32_t fast_vcount;    // fast setup: every vertex index below this fetches its FastVs attributes in range
+    uint32_t flat_mask;      // bit k: inter-stage float k is @interpolate(flat) (vertex 0's value, bits kept)
+    uint32_t early_depth;    // EarlyDepth of the fragment entry point
 };
 
 // Vertex stages the fast setup kernel specialises on: every input an f32 attribute of exactly

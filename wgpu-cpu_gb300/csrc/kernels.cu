@@ -171,6 +171,8 @@ uint32_t fast_vs_kind(const DrawDesc& d) {
             return h && d.profile == GBR_PROFILE_EXTENSION ? FAST_VS_QUAD_F16 : FAST_VS_NONE;
         }
         case PROG_CLIP_PASSTHROUGH:
+        case PROG_CLIP_FLAT:
+        case PROG_CLIP_DISCARD:
             return f32(0, GBR_VERTEX_FORMAT_FLOAT32X4) && f32(1, GBR_VERTEX_FORMAT_FLOAT32X4) ? FAST_VS_CLIP
                                                                                                : FAST_VS_NONE;
         case PROG_COLORED_TRIANGLE: return FAST_VS_TRIANGLE;

@@ -110,7 +110,10 @@ __host__ __device__ __forceinline__ uint32_t program_num_varyings(uint32_t prog)
         case PROG_MESH_COLOR_DISCARD: return 3;
         case PROG_MESH_TEX_LAMBERT: return 5;
         case PROG_QUAD_COLOR:
-        case PROG_CLIP_PASSTHROUGH: return 4;
+        case PROG_CLIP_PASSTHROUGH:
+        case PROG_CLIP_FLAT:
+        case PROG_CLIP_FLAT_ID:
+        case PROG_CLIP_DISCARD: return 4;
         default: return 0;
     }
 }
@@ -176,7 +179,9 @@ __device__ __forceinline__ bool run_vs(const DrawDesc& d, const float* mvp, uint
             var[3] = a1[3];
             return true;
         }
-        case PROG_CLIP_PASSTHROUGH: {
+        case PROG_CLIP_PASSTHROUGH:
+        case PROG_CLIP_FLAT:
+        case PROG_CLIP_DISCARD: {
             if (!fetch_attr(d, 0, 4, vertex, instance, a0, err)) return false;
             if (!fetch_attr(d, 1, 4, vertex, instance, a1, err)) return false;
             pos = {a0[0], a0[1], a0[2], a0[3]};
@@ -184,6 +189,18 @@ __device__ __forceinline__ bool run_vs(const DrawDesc& d, const float* mvp, uint
             var[1] = a1[1];
             var[2] = a1[2];
             var[3] = a1[3];
+            return true;
+        }
+        case PROG_CLIP_FLAT_ID: {
+            // @location(0) @interpolate(flat) id: u32 = 0x7fc00000 | (vertex_index & 0xffff) — as
+            // an f32 a NaN, so any arithmetic on the slot would show; @location(1) colour.xyz linear
+            if (!fetch_attr(d, 0, 4, vertex, instance, a0, err)) return false;
+            if (!fetch_attr(d, 1, 4, vertex, instance, a1, err)) return false;
+            pos = {a0[0], a0[1], a0[2], a0[3]};
+            var[0] = __uint_as_float(0x7fc00000u | (vertex & 0xffffu));
+            var[1] = a1[0];
+            var[2] = a1[1];
+            var[3] = a1[2];
             return true;
         }
 #ifdef GBR_JIT
@@ -209,6 +226,8 @@ struct RasterState {
     uint32_t tex_w, tex_h, addr_u, addr_v;
     uint32_t tex_ext;  // extension-profile sampling (sample_ext with the record's LOD)
     float uconst[4];  // program constants read from the uniform block (light direction)
+    uint32_t flat_mask;    // DrawDesc::flat_mask
+    uint32_t early_depth;  // DrawDesc::early_depth
 };
 
 __device__ __forceinline__ void build_raster_state(const DrawDesc& d, uint32_t di, RasterState& rs) {
@@ -239,6 +258,8 @@ __device__ __forceinline__ void build_raster_state(const DrawDesc& d, uint32_t d
     rs.addr_u = d.samp.address_u;
     rs.addr_v = d.samp.address_v;
     rs.tex_ext = d.lod_var != 0;
+    rs.flat_mask = d.flat_mask;
+    rs.early_depth = d.early_depth;
     for (int k = 0; k < 4; ++k) rs.uconst[k] = 0.0f;
     if (d.program == PROG_MESH_TEX_LAMBERT) {
         rs.uconst[0] = ld_uniform(d, 0, 0, 64);
@@ -276,7 +297,15 @@ __device__ __forceinline__ bool run_fs_rs(const RasterState& rs, const float* va
     switch (rs.program) {
         case PROG_COLORED_TRIANGLE:
         case PROG_QUAD_COLOR:
-        case PROG_CLIP_PASSTHROUGH: color = {var[0], var[1], var[2], var[3]}; return true;
+        case PROG_CLIP_PASSTHROUGH:
+        case PROG_CLIP_FLAT: color = {var[0], var[1], var[2], var[3]}; return true;
+        case PROG_CLIP_FLAT_ID:  // vec4f(f32(id & 0xffu) / 255.0, colour.x, colour.y, 1.0)
+            color = {fdiv((float)(__float_as_uint(var[0]) & 0xffu), 255.0f), var[1], var[2], 1.0f};
+            return true;
+        case PROG_CLIP_DISCARD:
+            if (var[0] < 0.5f) return false;
+            color = {var[0], var[1], var[2], var[3]};
+            return true;
         case PROG_MESH_COLOR:
         case PROG_MESH_COLOR_PERSPECTIVE: color = {var[0], var[1], var[2], 1.0f}; return true;
         case PROG_MESH_COLOR_DISCARD:

@@ -1868,6 +1868,17 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                                 cmp[j] = fadd(fadd(fmul(r.cb[j], l0), fmul(r.cb[3 + j], l1)), fmul(r.cb[6 + j], l2));
                         }
                         ++frag_count;
+                        if constexpr (KIND == 0) {
+                            // @early_depth_test (fragment.rs:166-194): the depth test, and the
+                            // depth write when it passes, before the fragment stage runs; a
+                            // rejected fragment never reaches it
+                            if (rs.early_depth != EARLY_DEPTH_NONE && rs.depth_test) {
+                                const float z =
+                                    fadd(fadd(fmul(r.fz[0], cmp[0]), fmul(r.fz[1], cmp[1])), fmul(r.fz[2], cmp[2]));
+                                if (!depth_compare(rs.depth_compare, z, px[k].depth)) continue;
+                                if (rs.depth_write) px[k].depth = z;
+                            }
+                        }
                         // inter-stage values (fragment.rs:319-378) and the fragment stage
                         V4 col;
                         ++fs_runs;
@@ -1900,10 +1911,17 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster(BatchParams bp) {
                                                    fmul(rv[2 * nvar + qv], cmp[2]));
                                 }
                             }
+                            // @interpolate(flat): the first vertex's value, bits unchanged (fragment.rs:395-405)
+                            if (rs.flat_mask) {
+#pragma unroll
+                                for (uint32_t qv = 0; qv < MAX_VARYING_FLOATS; ++qv)
+                                    if (qv < nvar && ((rs.flat_mask >> qv) & 1u)) var[qv] = rv[qv];
+                            }
                             if (!run_fs_any(bp, rs, r, cmp, var, s_lut, col)) continue;  // discard: no depth test, no write
                         }
-                        // late depth test at the first colour output (fragment.rs:427-453, 470-479)
-                        if (KIND == 2 || (KIND == 0 && rs.depth_test)) {
+                        // late depth test at the first colour output (fragment.rs:427-453, 470-479);
+                        // with @early_depth_test(force) the early result stands (fragment.rs:185-191)
+                        if (KIND == 2 || (KIND == 0 && rs.depth_test && rs.early_depth != EARLY_DEPTH_FORCE)) {
                             // fragment.z (raster.rs:345-346); only the depth test reads it here
                             const float z =
                                 fadd(fadd(fmul(r.fz[0], cmp[0]), fmul(r.fz[1], cmp[1])), fmul(r.fz[2], cmp[2]));

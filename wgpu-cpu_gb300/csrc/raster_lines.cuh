@@ -106,8 +106,15 @@ struct LinePrim {
 // depth test at the first colour output, blend / write mask, colour write — in global memory.
 __device__ __forceinline__ void line_fragment(const BatchParams& bp, const DrawDesc& d, const TargetDesc& tg,
                                               const RasterState& rs, const float* lut, const LinePrim& lp, uint32_t x,
-                                              uint32_t y, V4 fragment, const float coeff[2], uint32_t& frag_count) {
+                                              uint32_t y, V4 fragment, const float coeff[2], uint32_t& frag_count,
+                                              uint32_t& fs_count) {
     ++frag_count;
+    const size_t pix = (size_t)y * tg.width + x;
+    if (rs.early_depth != EARLY_DEPTH_NONE && rs.depth_test) {  // @early_depth_test (fragment.rs:166-194)
+        if (!depth_compare(rs.depth_compare, fragment.z, tg.depth[pix])) return;
+        if (rs.depth_write) tg.depth[pix] = fragment.z;
+    }
+    ++fs_count;
     const uint32_t nvar = rs.nvar;
     float var[MAX_VARYING_FLOATS];
 #pragma unroll
@@ -126,6 +133,7 @@ __device__ __forceinline__ void line_fragment(const BatchParams& bp, const DrawD
             if (lp.verts == 2) a = fadd(a, fmul(lp.var[1][q], coeff[1]));
             var[q] = a;
         }
+        if ((rs.flat_mask >> q) & 1u) var[q] = lp.var[0][q];  // @interpolate(flat): the first vertex
     }
     V4 col;
     bool keep;
@@ -144,8 +152,7 @@ __device__ __forceinline__ void line_fragment(const BatchParams& bp, const DrawD
         keep = run_fs_rs(rs, var, lut, col, lod);
     }
     if (!keep) return;  // discard
-    const size_t pix = (size_t)y * tg.width + x;
-    if (rs.depth_test) {
+    if (rs.depth_test && rs.early_depth != EARLY_DEPTH_FORCE) {  // the late test
         const float stored = tg.depth[pix];
         if (!depth_compare(rs.depth_compare, fragment.z, stored)) return;
         if (rs.depth_write) tg.depth[pix] = fragment.z;
@@ -223,7 +230,7 @@ __global__ void __launch_bounds__(kLineThreads) k_lines_points(BatchParams bp) {
     __syncthreads();
     const bool point = d.topology == 0;
     const bool strip = d.topology == 2;
-    uint32_t frag_count = 0;
+    uint32_t frag_count = 0, fs_count = 0;
     for (uint32_t inst = 0; inst < d.instance_count; ++inst) {
         uint32_t compact = 0;  // primitive_index of the next primitive (thread 0)
         for (uint32_t p = 0; p < d.prims_per_instance; ++p) {
@@ -288,7 +295,7 @@ __global__ void __launch_bounds__(kLineThreads) k_lines_points(BatchParams bp) {
                         const uint32_t x = lp.fbx[0], y = lp.fby[0];
                         if (x >= d.sc_x0 && x < d.sc_x1 && y >= d.sc_y0 && y < d.sc_y1 && x < tg.width && y < tg.height) {
                             const float coeff[2] = {1.0f, 0.0f};
-                            line_fragment(bp, d, tg, s_rs, s_lut, lp, x, y, lp.frag[0], coeff, frag_count);
+                            line_fragment(bp, d, tg, s_rs, s_lut, lp, x, y, lp.frag[0], coeff, frag_count, fs_count);
                         }
                     }
                 } else {
@@ -348,21 +355,23 @@ __global__ void __launch_bounds__(kLineThreads) k_lines_points(BatchParams bp) {
                         const float omT = fsub(1.0f, T);
                         const V4 fragment = v4_add(v4_mul(lp.frag[0], omT), v4_mul(lp.frag[1], T));
                         const float coeff[2] = {omT, T};
-                        line_fragment(bp, d, tg, s_rs, s_lut, lp, x, y, fragment, coeff, frag_count);
+                        line_fragment(bp, d, tg, s_rs, s_lut, lp, x, y, fragment, coeff, frag_count, fs_count);
                     }
                 }
             }
             __syncthreads();
         }
     }
-    for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
+    for (int o = 16; o > 0; o >>= 1) {
+        frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
+        fs_count += __shfl_xor_sync(0xFFFFFFFFu, fs_count, o);
+    }
     if ((threadIdx.x & 31) == 0 && frag_count) {
         atomicAdd(&s_frag, (unsigned long long)frag_count);
-        if (tg.frag_count) {
-            // every line or point fragment runs the fragment stage (one draw per CTA)
+        if (tg.frag_count) {  // one draw per CTA: its program samples a texture or not
             atomicAdd(tg.frag_count, (unsigned long long)frag_count);
-            atomicAdd(tg.frag_count + 1, (unsigned long long)frag_count);
-            if (s_rs.tex_data) atomicAdd(tg.frag_count + 2, (unsigned long long)frag_count);
+            if (fs_count) atomicAdd(tg.frag_count + 1, (unsigned long long)fs_count);
+            if (fs_count && s_rs.tex_data) atomicAdd(tg.frag_count + 2, (unsigned long long)fs_count);
         }
     }
     __syncthreads();

@@ -359,6 +359,11 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                                            fmul(rv[2 * nvar + qv], cmp[2]));
                         }
                     }
+                    if (rs.flat_mask) {  // @interpolate(flat): the first vertex's value, bits unchanged
+#pragma unroll
+                        for (uint32_t qv = 0; qv < MAX_VARYING_FLOATS; ++qv)
+                            if (qv < nvar && ((rs.flat_mask >> qv) & 1u)) var[qv] = rv[qv];
+                    }
                     V4 col;
                     ++fs_runs;
                     tex_runs += rs.tex_data != nullptr;

@@ -119,18 +119,51 @@ struct ProgramInfo {
     int tex_group = 1, tex_binding = 0, samp_group = 1, samp_binding = 1;
     int input_kind[16] = {};
     bool may_discard = false;
+    uint32_t flat_mask = 0;    // inter-stage floats interpolated flat (bit per float)
+    uint32_t early_depth = 0;  // EarlyDepth of the fragment entry point
 };
-const ProgramInfo kPrograms[] = {
-    {"colored_triangle", PROG_COLORED_TRIANGLE, 0, {0, 0, 0}, {0, 0, 0}, 4, false, 0, false},
-    {"mesh_color", PROG_MESH_COLOR, 2, {0, 1, 0}, {3, 3, 0}, 3, false, 64, false},
-    {"mesh_color_perspective", PROG_MESH_COLOR_PERSPECTIVE, 2, {0, 1, 0}, {3, 3, 0}, 3, true, 64, false},
-    {"mesh_color_discard", PROG_MESH_COLOR_DISCARD, 2, {0, 1, 0}, {3, 3, 0}, 3, false, 64, false},
-    {"mesh_tex_lambert", PROG_MESH_TEX_LAMBERT, 3, {0, 1, 2}, {3, 3, 2}, 5, false, 80, true},
-    {"quad_color", PROG_QUAD_COLOR, 2, {0, 1, 0}, {3, 4, 0}, 4, false, 0, false},
-    {"clip_passthrough", PROG_CLIP_PASSTHROUGH, 2, {0, 1, 0}, {4, 4, 0}, 4, false, 0, false},
-};
+// The native programs, and variants whose fragment entry point carries @early_depth_test(force)
+// ("<name>@early_force") or @early_depth_test(<conservative>) ("<name>@early_allow").
+const std::vector<ProgramInfo>& native_programs() {
+    static const std::vector<ProgramInfo> table = [] {
+        std::vector<ProgramInfo> v = {
+            {"colored_triangle", PROG_COLORED_TRIANGLE, 0, {0, 0, 0}, {0, 0, 0}, 4, false, 0, false},
+            {"mesh_color", PROG_MESH_COLOR, 2, {0, 1, 0}, {3, 3, 0}, 3, false, 64, false},
+            {"mesh_color_perspective", PROG_MESH_COLOR_PERSPECTIVE, 2, {0, 1, 0}, {3, 3, 0}, 3, true, 64, false},
+            {"mesh_color_discard", PROG_MESH_COLOR_DISCARD, 2, {0, 1, 0}, {3, 3, 0}, 3, false, 64, false},
+            {"mesh_tex_lambert", PROG_MESH_TEX_LAMBERT, 3, {0, 1, 2}, {3, 3, 2}, 5, false, 80, true},
+            {"quad_color", PROG_QUAD_COLOR, 2, {0, 1, 0}, {3, 4, 0}, 4, false, 0, false},
+            {"clip_passthrough", PROG_CLIP_PASSTHROUGH, 2, {0, 1, 0}, {4, 4, 0}, 4, false, 0, false},
+            {"clip_flat", PROG_CLIP_FLAT, 2, {0, 1, 0}, {4, 4, 0}, 4, false, 0, false},
+            {"clip_flat_id", PROG_CLIP_FLAT_ID, 2, {0, 1, 0}, {4, 4, 0}, 4, false, 0, false},
+            {"clip_discard", PROG_CLIP_DISCARD, 2, {0, 1, 0}, {4, 4, 0}, 4, false, 0, false},
+        };
+        for (auto& p : v) {
+            if (p.id == PROG_CLIP_FLAT) p.flat_mask = 0xFu;
+            if (p.id == PROG_CLIP_FLAT_ID) p.flat_mask = 0x1u;
+            if (p.id == PROG_CLIP_DISCARD || p.id == PROG_MESH_COLOR_DISCARD) p.may_discard = true;
+        }
+        static const char* const kEarly[] = {"clip_passthrough", "clip_discard", "clip_flat_id", "mesh_color",
+                                             "mesh_color_discard"};
+        static std::vector<std::string> names;  // storage of the variants' names
+        names.reserve(2 * (sizeof kEarly / sizeof kEarly[0]));
+        const size_t base = v.size();
+        for (const char* n : kEarly)
+            for (uint32_t mode : {EARLY_DEPTH_FORCE, EARLY_DEPTH_ALLOW})
+                for (size_t i = 0; i < base; ++i)
+                    if (std::strcmp(v[i].name, n) == 0) {
+                        names.push_back(std::string(n) + (mode == EARLY_DEPTH_FORCE ? "@early_force" : "@early_allow"));
+                        ProgramInfo q = v[i];
+                        q.name = names.back().c_str();
+                        q.early_depth = mode;
+                        v.push_back(q);
+                    }
+        return v;
+    }();
+    return table;
+}
 const ProgramInfo* find_program(const char* name) {
-    for (const auto& p : kPrograms)
+    for (const auto& p : native_programs())
         if (std::strcmp(p.name, name) == 0) return &p;
     return nullptr;
 }
@@ -143,9 +176,10 @@ std::shared_ptr<wgsl::Module> parse_wgsl(const char* src, uint64_t len) {
         fail(e.unsupported ? GBR_ERR_UNSUPPORTED : GBR_ERR_SHADER, "%s", e.what());
     }
 }
-wgsl::ProgramCode emit_wgsl(const wgsl::Module& vs, const std::string& ve, const wgsl::Module* fs, const std::string& fe) {
+wgsl::ProgramCode emit_wgsl(const wgsl::Module& vs, const std::string& ve, const wgsl::Module* fs, const std::string& fe,
+                            const wgsl::Constants& vc = {}, const wgsl::Constants& fc = {}) {
     try {
-        return wgsl::emit_program(vs, ve, fs, fe);
+        return wgsl::emit_program(vs, ve, fs, fe, vc, fc);
     } catch (const wgsl::Error& e) {
         fail(e.unsupported ? GBR_ERR_UNSUPPORTED : GBR_ERR_SHADER, "%s", e.what());
     }
@@ -484,7 +518,7 @@ uint32_t visibility_compare(const Batch& b) {
         return 0;
     for (const DrawDesc& d : b.draws)
         if (!d.depth_test || !d.depth_write || d.depth_compare != cmp || d.blend_enabled || !d.has_fragment ||
-            d.program == PROG_MESH_COLOR_DISCARD || d.may_discard)
+            d.program == PROG_MESH_COLOR_DISCARD || d.may_discard || d.early_depth != EARLY_DEPTH_NONE)
             return 0;
     return cmp;
 }
@@ -717,6 +751,8 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
     d.num_varyings = prog.num_varyings;
     d.interp = prog.perspective ? INTERP_PERSPECTIVE : INTERP_LINEAR;
     d.may_discard = prog.may_discard ? 1u : 0u;
+    d.flat_mask = prog.flat_mask;
+    d.early_depth = prog.early_depth;
     d.profile = profile;
     // extension-profile sampling needs the (u, v) derivatives: the native textured program's uv
     // are varyings 3 and 4 (lod_var = 1 + the index of u)
@@ -2369,6 +2405,8 @@ GBR_API gbr_status gbr_render_pipeline_create(gbr_device dh, const gbr_render_pi
         if (!desc) fail(GBR_ERR_INVALID_ARGUMENT, "null descriptor");
         auto pl = std::make_shared<Pipeline>();
         pl->desc = *desc;
+        pl->desc.vertex_constants = pl->desc.fragment_constants = nullptr;  // the caller's, read below only
+        pl->desc.vertex_constant_count = pl->desc.fragment_constant_count = 0;
         auto vs = d->get<ShaderModule>(desc->vertex_module, "shader module");
         pl->prog = vs->prog;
         if (vs->wgsl) {
@@ -2391,9 +2429,21 @@ GBR_API gbr_status gbr_render_pipeline_create(gbr_device dh, const gbr_render_pi
                 if (count != 1) fail(GBR_ERR_VALIDATION, "an entry point name is required (%d candidates)", count);
                 return only;
             };
+            // PipelineCompilationOptions::constants of each stage (shader.rs:52-74)
+            auto constants = [](const gbr_pipeline_constant* c, uint32_t n) {
+                wgsl::Constants m;
+                if (n && !c) fail(GBR_ERR_INVALID_ARGUMENT, "null pipeline constants");
+                for (uint32_t i = 0; i < n; ++i) {
+                    if (!c[i].key) fail(GBR_ERR_INVALID_ARGUMENT, "pipeline constant %u has no key", i);
+                    m[c[i].key] = c[i].value;
+                }
+                return m;
+            };
+            const wgsl::Constants vconsts = constants(desc->vertex_constants, desc->vertex_constant_count);
+            const wgsl::Constants fconsts = constants(desc->fragment_constants, desc->fragment_constant_count);
             const wgsl::ProgramCode pc =
                 emit_wgsl(*vs->wgsl, entry(desc->vertex_entry_point, *vs->wgsl, 0), fs ? fs->wgsl.get() : nullptr,
-                          fs ? entry(desc->fragment_entry_point, *fs->wgsl, 1) : std::string());
+                          fs ? entry(desc->fragment_entry_point, *fs->wgsl, 1) : std::string(), vconsts, fconsts);
             ProgramInfo& pi = pl->own;
             pi.name = "wgsl";
             pi.id = PROG_JIT;
@@ -2416,6 +2466,8 @@ GBR_API gbr_status gbr_render_pipeline_create(gbr_device dh, const gbr_render_pi
                 pi.samp_binding = pc.samp_binding;
             }
             pi.may_discard = pc.may_discard;
+            pi.flat_mask = pc.flat_mask;
+            pi.early_depth = pc.early_depth;
             std::string err;
             pl->jit = jit_module(pc.cuda, d->cfg.raster_rule == GBR_RASTER_RULE_EDGE, &err);
             if (!pl->jit) fail(GBR_ERR_SHADER, "%s", err.c_str());

@@ -192,6 +192,8 @@ struct Global {
     ExprP init;
     int group = -1, binding = -1;
     int line = 0;
+    bool is_override = false;     // `override`: a Const whose value the pipeline may set
+    long long override_id = -1;   // its @id, or -1 (then the name is its key)
 };
 struct Func {
     std::string name;
@@ -199,6 +201,7 @@ struct Func {
     bool has_ret = false;
     TypeExpr ret;
     std::vector<Attr> ret_attrs;
+    std::vector<Attr> attrs;  // the function's own attributes (@vertex, @early_depth_test, ...)
     std::vector<StmtP> body;
     int stage = -1;  // 0 vertex, 1 fragment, -1 helper
     int line = 0;
@@ -219,12 +222,20 @@ class Parser {
         auto m = std::make_shared<Module>();
         while (!at_end()) {
             std::vector<Attr> attrs = attributes();
+            const int decl_line = line();
+            auto no_attrs = [&](const char* what) {
+                if (!attrs.empty()) bad(decl_line, "@" + attrs[0].name + " does not apply to " + what);
+            };
             if (accept_kw("struct")) {
+                no_attrs("a struct");
                 m->structs.push_back(struct_def());
             } else if (accept_kw("fn")) {
                 m->funcs.push_back(func(attrs));
-            } else if (peek_kw("const") || peek_kw("override")) {
-                if (peek_kw("override")) unsupported(line(), "override declarations");
+            } else if (accept_kw("override")) {
+                m->globals.push_back(override_decl(attrs));
+                expect(";");
+            } else if (peek_kw("const")) {
+                no_attrs("a const");
                 next();
                 m->globals.push_back(global_value(Global::Const));
                 expect(";");
@@ -250,7 +261,8 @@ class Parser {
                 if (g.has_type && g.ty.name == "sampler") g.k = Global::Sampler;
                 for (const Attr& a : attrs) {
                     if (a.name == "group" && !a.args.empty()) g.group = std::atoi(a.args[0].c_str());
-                    if (a.name == "binding" && !a.args.empty()) g.binding = std::atoi(a.args[0].c_str());
+                    else if (a.name == "binding" && !a.args.empty()) g.binding = std::atoi(a.args[0].c_str());
+                    else bad(g.line, "@" + a.name + " does not apply to a module-scope var");
                 }
                 if (g.k != Global::Private && g.k != Global::Const && (g.group < 0 || g.binding < 0))
                     bad(g.line, "resource variable '" + g.name + "' needs @group and @binding");
@@ -311,11 +323,27 @@ class Parser {
         return s;
     }
 
+    // Attributes this front end acts on, and those with no effect on what is rendered (invariant:
+    // the arithmetic here is deterministic anyway; must_use and diagnostic: checks and messages
+    // only).  Everything else fails the module instead of being ignored.
+    static void check_attribute(const std::string& n, int line) {
+        static const char* const kUsed[] = {"location", "builtin", "interpolate", "group", "binding", "vertex",
+                                            "fragment", "compute", "early_depth_test", "id", "invariant", "must_use",
+                                            "diagnostic"};
+        for (const char* k : kUsed)
+            if (n == k) return;
+        if (n == "align" || n == "size" || n == "blend_src" || n == "workgroup_size")
+            unsupported(line, "attribute @" + n);
+        bad(line, "unknown attribute @" + n);
+    }
+
     std::vector<Attr> attributes() {
         std::vector<Attr> out;
         while (accept("@")) {
             Attr a;
+            const int at_line = line();
             a.name = ident();
+            check_attribute(a.name, at_line);
             if (accept("(")) {
                 while (!peek(")")) {
                     if (cur().t == Tk::End) bad(line(), "unterminated attribute");
@@ -379,6 +407,32 @@ class Parser {
         return s;
     }
 
+    // `override name [: type] [= initializer]` with an optional @id(n) (a pipeline-overridable
+    // constant, set through PipelineCompilationOptions::constants)
+    Global override_decl(const std::vector<Attr>& attrs) {
+        Global g;
+        g.k = Global::Const;
+        g.is_override = true;
+        g.line = line();
+        g.name = ident();
+        for (const Attr& a : attrs) {
+            if (a.name != "id") bad(g.line, "@" + a.name + " does not apply to an override");
+            if (a.args.size() != 1) bad(g.line, "@id takes one argument");
+            char* end = nullptr;
+            const long long id = std::strtoll(a.args[0].c_str(), &end, 0);
+            if (!end || (*end && std::strcmp(end, "u") && std::strcmp(end, "i")) || id < 0 || id > 65535)
+                bad(g.line, "@id must be an integer in [0, 65535]");
+            g.override_id = id;
+        }
+        if (accept(":")) {
+            g.ty = type();
+            g.has_type = true;
+        }
+        if (accept("=")) g.init = expr();
+        if (!g.has_type && !g.init) bad(g.line, "override '" + g.name + "' needs a type or an initializer");
+        return g;
+    }
+
     Global global_value(Global::K k) {
         Global g;
         g.k = k;
@@ -397,11 +451,16 @@ class Parser {
         Func f;
         f.line = line();
         f.name = ident();
+        f.attrs = attrs;
         for (const Attr& a : attrs) {
             if (a.name == "vertex") f.stage = 0;
             else if (a.name == "fragment") f.stage = 1;
             else if (a.name == "compute") unsupported(f.line, "compute entry points");
+            else if (a.name != "early_depth_test" && a.name != "must_use" && a.name != "diagnostic")
+                bad(f.line, "@" + a.name + " does not apply to a function");
         }
+        for (const Attr& a : attrs)
+            if (a.name == "early_depth_test" && f.stage != 1) bad(f.line, "@early_depth_test applies to fragment entry points");
         expect("(");
         while (!accept(")")) {
             Member p;
@@ -788,14 +847,49 @@ struct Val {
     double num = 0.0;
 };
 
+// A pipeline constant (f64) as a literal of the override's type, converted as naga's
+// process_overrides does (WebIDL conversions): bool = value != 0 and not NaN; i32 / u32 =
+// the value truncated toward zero, which must be finite and in range; f32 = the value rounded to
+// nearest, finite before and after.
+std::string override_literal(double value, const Ty& t, const std::string& name, int line) {
+    char buf[64];
+    switch (t.k) {
+        case Ty::Bool: return value != 0.0 && value == value ? "true" : "false";
+        case Ty::I32:
+        case Ty::U32: {
+            if (!std::isfinite(value)) bad(line, "pipeline constant '" + name + "' must be finite");
+            const double v = std::trunc(value);
+            const bool i = t.k == Ty::I32;
+            if (i ? (v < -2147483648.0 || v > 2147483647.0) : (v < 0.0 || v > 4294967295.0))
+                bad(line, "pipeline constant '" + name + "' is out of range of its type");
+            if (i) std::snprintf(buf, sizeof buf, "(int32_t)%lldll", (long long)v);
+            else std::snprintf(buf, sizeof buf, "%lluu", (unsigned long long)v);
+            return buf;
+        }
+        case Ty::F32: {
+            if (!std::isfinite(value)) bad(line, "pipeline constant '" + name + "' must be finite");
+            const float f = (float)value;
+            if (!std::isfinite(f)) bad(line, "pipeline constant '" + name + "' overflows f32");
+            uint32_t bits;
+            std::memcpy(&bits, &f, 4);
+            std::snprintf(buf, sizeof buf, "__uint_as_float(0x%08xu)", bits);
+            return buf;
+        }
+        default: unsupported(line, "an override of this type");
+    }
+}
+
 class Emitter {
   public:
-    Emitter(const Module& vs, const Module* fs) : vs_(vs), fs_(fs) {}
+    Emitter(const Module& vs, const Module* fs, const Constants& vc, const Constants& fc)
+        : vs_(vs), fs_(fs), vconsts_(vc), fconsts_(fc) {}
 
     ProgramCode run(const std::string& vs_entry, const std::string& fs_entry);
 
   private:
     const Module& vs_;
+    const Constants& vconsts_;  // pipeline-overridable constants of the vertex / fragment stage
+    const Constants& fconsts_;
     const Module* fs_;
     const Module* mod_ = nullptr;  // module being emitted
     std::string prefix_;           // name prefix of that module's declarations
@@ -804,6 +898,27 @@ class Emitter {
     std::map<std::string, Ty> const_types_, private_, uniforms_;
     std::vector<std::tuple<int, std::string, int, bool, Ty::K>> post_src_;  // location, source, comps, vector, scalar
     std::map<int, std::pair<int, int>> slot_off_;                    // location -> (first float, comps)
+    std::map<int, Ty::K> slot_kind_;                                  // location -> scalar type
+    struct Slot {
+        int loc;
+        int comps;
+        int interp;  // interp_of
+    };
+    // flat_mask (per float) and the one mode of the other interpolated values (perspective or linear)
+    void set_interpolation(const std::vector<Slot>& slots, int line) {
+        pc_.flat_mask = 0;
+        int mode = -1;
+        for (const Slot& s : slots) {
+            if (s.interp == 2) {
+                const int first = slot_off_.at(s.loc).first;
+                for (int k = 0; k < s.comps; ++k) pc_.flat_mask |= 1u << (first + k);
+                continue;
+            }
+            if (mode >= 0 && s.interp != mode) unsupported(line, "linear and perspective interpolation in one program");
+            mode = s.interp;
+        }
+        pc_.perspective = mode == 0;
+    }
     std::map<std::string, int> struct_ids_;  // prefixed name -> index
     std::vector<std::pair<const StructDef*, std::string>> structs_;  // def, C name
     std::set<std::string> emitted_fns_;
@@ -1874,26 +1989,36 @@ int location_of(const std::vector<Attr>& attrs) {
         if (a.name == "location" && !a.args.empty()) return std::atoi(a.args[0].c_str());
     return -1;
 }
-// 0 = perspective (the default), 1 = linear, 2 = flat
-int interp_of(const std::vector<Attr>& attrs) {
+// @interpolate(type[, sampling]) of an inter-stage value: 0 = perspective, 1 = linear, 2 = flat.
+// Without the attribute naga applies the default: perspective for floats, flat for integers
+// (Binding::apply_default_interpolation).  The sampling must fit the type as naga validates it (flat: first / either;
+// perspective / linear: center / centroid / sample); the reference interpolates every sampling
+// the same way (fragment.rs:278-378, FlatSampling at :395-405).
+int interp_of(const std::vector<Attr>& attrs, int line, bool integer) {
     for (const Attr& a : attrs)
-        if (a.name == "interpolate" && !a.args.empty()) {
-            if (a.args[0] == "linear") return 1;
-            if (a.args[0] == "flat") return 2;
-            return 0;
+        if (a.name == "interpolate") {
+            if (a.args.empty() || a.args.size() > 2) bad(line, "@interpolate takes a type and an optional sampling");
+            int type = -1;
+            if (a.args[0] == "perspective") type = 0;
+            else if (a.args[0] == "linear") type = 1;
+            else if (a.args[0] == "flat") type = 2;
+            else bad(line, "unknown interpolation type '" + a.args[0] + "'");
+            if (a.args.size() == 2) {
+                const std::string& s = a.args[1];
+                const bool flat_ok = s == "first" || s == "either";
+                const bool other_ok = s == "center" || s == "centroid" || s == "sample";
+                if (!flat_ok && !other_ok) bad(line, "unknown interpolation sampling '" + s + "'");
+                if ((type == 2) != flat_ok) bad(line, "sampling '" + s + "' does not apply to " + a.args[0] + " interpolation");
+            }
+            return type;
         }
-    return 0;
+    return integer ? 2 : 0;
 }
 }  // namespace
 
 ProgramCode Emitter::run(const std::string& vs_entry, const std::string& fs_entry) {
     for (auto& g : pc_.input_loc) g = -1;
     std::ostringstream body;
-    struct Slot {
-        int loc;
-        int comps;
-        int interp;
-    };
     std::vector<Slot> slots;  // varyings in location order
 
     // ---------- vertex stage
@@ -1903,26 +2028,39 @@ ProgramCode Emitter::run(const std::string& vs_entry, const std::string& fs_entr
     for (const Func& f : vs_.funcs)
         if (f.name == vs_entry && f.stage == 0) vf = &f;
     if (!vf) throw Error("no @vertex entry point '" + vs_entry + "'", false);
-    auto emit_consts = [&](const Module& m) {
+    auto emit_consts = [&](const Module& m, const Constants& consts) {
         for (const Global& g : m.globals)
             if (g.k == Global::Const) {
                 scopes_.clear();
                 push();
-                Val v = ex(g.init);
+                // an override takes the pipeline's value when one is given under its key (its
+                // @id, else its name), else its initializer (process_overrides)
+                const Constants::const_iterator given =
+                    g.is_override ? consts.find(g.override_id >= 0 ? std::to_string(g.override_id) : g.name)
+                                  : consts.end();
                 Ty t;
-                if (g.has_type) {
-                    t = resolve(g.ty);
-                    v = v.t.abstract() ? coerce(v, t, g.line) : v;
+                Val v;
+                if (given != consts.end()) {
+                    t = g.has_type ? resolve(g.ty) : concretize(ex(g.init), g.line).t;
+                    v.t = t;
+                    v.c = override_literal(given->second, t, g.name, g.line);
                 } else {
-                    v = concretize(v, g.line);
-                    t = v.t;
+                    if (!g.init) bad(g.line, "override '" + g.name + "' has no value: the pipeline gives none and it has no initializer");
+                    v = ex(g.init);
+                    if (g.has_type) {
+                        t = resolve(g.ty);
+                        v = v.t.abstract() ? coerce(v, t, g.line) : v;
+                    } else {
+                        v = concretize(v, g.line);
+                        t = v.t;
+                    }
                 }
                 const_types_[prefix_ + g.name] = t;
                 decl_ << "__device__ __forceinline__ " << ctype(t) << " g_" << prefix_ << g.name << "(bool& __tr) { return "
                       << v.c << "; }\n";
             }
     };
-    emit_consts(vs_);
+    emit_consts(vs_, vconsts_);
 
     // the context: private globals, uniform values, the draw
     auto ctx_members = [&](const Module& m, std::ostringstream& members, std::ostringstream& init) {
@@ -2049,13 +2187,14 @@ ProgramCode Emitter::run(const std::string& vs_entry, const std::string& fs_entr
             const int loc = location_of(attrs);
             if (loc < 0) bad(vf->line, "vertex output needs @location or @builtin(position)");
             int comps = t.k == Ty::Vec ? t.n : 1;
-            // integer values need flat interpolation; a vertex-only program (evaluated alone) keeps
-            // their bits
-            if (t.scal() != Ty::F32 && (fs_ || (t.scal() != Ty::I32 && t.scal() != Ty::U32)))
-                unsupported(vf->line, "integer inter-stage values (flat interpolation)");
-            const int it = t.scal() != Ty::F32 ? 1 : interp_of(attrs);
-            if (it == 2) unsupported(vf->line, "flat interpolation");
+            if (t.scal() != Ty::F32 && t.scal() != Ty::I32 && t.scal() != Ty::U32)
+                unsupported(vf->line, "inter-stage values of this type");
+            const int it = interp_of(attrs, vf->line, t.scal() != Ty::F32);
+            // integer values are carried bit for bit and must be flat (naga validates this; the
+            // reference panics on anything else, fragment.rs:337-339)
+            if (t.scal() != Ty::F32 && it != 2) bad(vf->line, "integer inter-stage values need @interpolate(flat)");
             slots.push_back(Slot{loc, comps, it});
+            slot_kind_[loc] = t.scal();
             post_src_.push_back({loc, src, comps, t.k == Ty::Vec, t.scal()});
         };
         if (ret_ty_.k == Ty::Struct) {
@@ -2081,12 +2220,9 @@ ProgramCode Emitter::run(const std::string& vs_entry, const std::string& fs_entr
         }
         pc_.num_varyings = off;
         if (off > 16) unsupported(vf->line, "more than 16 inter-stage floats");
-        int mode = -1;
-        for (const Slot& s : slots) {
-            if (mode >= 0 && s.interp != mode) unsupported(vf->line, "mixed interpolation modes");
-            mode = s.interp;
-        }
-        pc_.perspective = mode == 0;
+        // a vertex-only program: the interpolation its outputs declare (a fragment stage decides
+        // below, from its inputs, as the reference does)
+        if (!fs_) set_interpolation(slots, vf->line);
         std::ostringstream lam;
         stmts(vf->body, lam, 2);
         vw << "__device__ bool jit_vs(const DrawDesc& d, uint32_t vertex, uint32_t instance, V4& pos, float* var, uint32_t* err) {\n"
@@ -2108,7 +2244,7 @@ ProgramCode Emitter::run(const std::string& vs_entry, const std::string& fs_entr
             if (f.name == fs_entry && f.stage == 1) ff = &f;
         if (!ff) throw Error("no @fragment entry point '" + fs_entry + "'", false);
         if (fs_ != &vs_) {
-            emit_consts(*fs_);
+            emit_consts(*fs_, fconsts_);
             ctx_members(*fs_, fmembers, finit);
         }
         stage_ = 1;
@@ -2117,6 +2253,17 @@ ProgramCode Emitter::run(const std::string& vs_entry, const std::string& fs_entr
         push_globals(*fs_);
         push();
         std::ostringstream pre, decls;
+        std::vector<Slot> fs_slots;  // the inputs at @location, with their interpolation
+        // @early_depth_test(force) / @early_depth_test(<conservative depth>) (naga::EarlyDepthTest,
+        // read by the reference at fragment.rs:83-86)
+        for (const Attr& a : ff->attrs)
+            if (a.name == "early_depth_test") {
+                if (a.args.size() != 1) bad(ff->line, "@early_depth_test takes one argument");
+                if (a.args[0] == "force") pc_.early_depth = 1;
+                else if (a.args[0] == "greater_equal" || a.args[0] == "less_equal" || a.args[0] == "unchanged")
+                    pc_.early_depth = 2;
+                else bad(ff->line, "unknown @early_depth_test argument '" + a.args[0] + "'");
+            }
         auto input = [&](const Member& p, const Ty& t, const std::string& dst) {
             std::string bname;
             if (builtin_of(p.attrs, &bname)) {
@@ -2141,10 +2288,17 @@ ProgramCode Emitter::run(const std::string& vs_entry, const std::string& fs_entr
             auto it = slot_off_.find(loc);
             if (loc < 0 || it == slot_off_.end()) bad(ff->line, "fragment input @location(" + std::to_string(loc) + ") is not written by the vertex stage");
             const int comps = t.k == Ty::Vec ? t.n : 1;
-            if (t.scal() != Ty::F32 || comps != it->second.second) bad(ff->line, "fragment input type differs from the vertex output");
+            if (t.scal() != slot_kind_.at(loc) || comps != it->second.second)
+                bad(ff->line, "fragment input type differs from the vertex output");
+            // the fragment input's @interpolate decides how the value is interpolated
+            // (Interpolation::from_naga on the input's binding, fragment.rs:250-262)
+            const int interp = interp_of(p.attrs, ff->line, t.scal() != Ty::F32);
+            if (t.scal() != Ty::F32 && interp != 2) bad(ff->line, "integer inter-stage values need @interpolate(flat)");
+            fs_slots.push_back({loc, comps, interp});
+            const char* conv = t.scal() == Ty::I32 ? "__float_as_int" : t.scal() == Ty::U32 ? "__float_as_uint" : "";
             for (int k = 0; k < comps; ++k)
-                pre << "  " << (t.k == Ty::Vec ? dst + ".c[" + std::to_string(k) + "]" : dst) << " = var["
-                    << it->second.first + k << "];\n";
+                pre << "  " << (t.k == Ty::Vec ? dst + ".c[" + std::to_string(k) + "]" : dst) << " = " << conv << "(var["
+                    << it->second.first + k << "]);\n";
         };
         for (const Member& p : ff->params) {
             Ty t = resolve(p.ty);
@@ -2158,6 +2312,9 @@ ProgramCode Emitter::run(const std::string& vs_entry, const std::string& fs_entr
                 input(p, t, c);
             }
         }
+        // interpolation of the values the fragment stage reads: flat ones per float, one mode for
+        // the others
+        set_interpolation(fs_slots, ff->line);
         if (!ff->has_ret) unsupported(ff->line, "fragment entry point without a colour output");
         ret_ty_ = resolve(ff->ret);
         std::string colour;
@@ -2205,8 +2362,16 @@ ProgramCode Emitter::run(const std::string& vs_entry, const std::string& fs_entr
 
 namespace gbr {
 namespace wgsl {
-ProgramCode emit_program(const Module& vs, const std::string& vs_entry, const Module* fs, const std::string& fs_entry) {
-    Emitter em(vs, fs);
+ProgramCode emit_program(const Module& vs, const std::string& vs_entry, const Module* fs, const std::string& fs_entry,
+                         const Constants& vertex_constants, const Constants& fragment_constants) {
+    // one module for both stages, with different constants per stage: the fragment stage gets a
+    // copy of its own (its constants and globals are then emitted apart from the vertex stage's)
+    Module fs_copy;
+    if (fs == &vs && vertex_constants != fragment_constants) {
+        fs_copy = vs;
+        fs = &fs_copy;
+    }
+    Emitter em(vs, fs, vertex_constants, fragment_constants);
     return em.run(vs_entry, fs_entry);
 }
 }  // namespace wgsl

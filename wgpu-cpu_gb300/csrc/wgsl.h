@@ -12,6 +12,7 @@
 #pragma once
 
 #include <cstdint>
+#include <map>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -37,7 +38,9 @@ std::vector<std::pair<std::string, int>> entry_points(const Module& m);
 struct ProgramCode {
     std::string cuda;               // defines jit_vs and (if any) jit_fs
     uint32_t num_varyings = 0;      // f32 inter-stage values per vertex
-    bool perspective = false;       // inter-stage interpolation (one mode per program)
+    bool perspective = false;       // interpolation of the non-flat inter-stage values (one mode per program)
+    uint32_t flat_mask = 0;         // bit k: inter-stage float k is @interpolate(flat)
+    uint32_t early_depth = 0;       // fragment entry point's @early_depth_test: 0 none, 1 force, 2 allow
     bool may_discard = false;
     bool uses_position = false;     // the fragment stage reads @builtin(position)
     int input_loc[16];              // vertex inputs: location and f32 component count
@@ -48,8 +51,14 @@ struct ProgramCode {
     int tex_group = -1, tex_binding = -1, samp_group = -1, samp_binding = -1;
 };
 
-// Emits the program of `vs_entry` (in vs) and, when fs is given, `fs_entry` (in fs).
-ProgramCode emit_program(const Module& vs, const std::string& vs_entry, const Module* fs, const std::string& fs_entry);
+// Pipeline-overridable constants of one stage (PipelineCompilationOptions::constants): key (an
+// override's @id as a decimal string, or its name) -> value.
+using Constants = std::map<std::string, double>;
+
+// Emits the program of `vs_entry` (in vs) and, when fs is given, `fs_entry` (in fs), with the
+// stages' override values.
+ProgramCode emit_program(const Module& vs, const std::string& vs_entry, const Module* fs, const std::string& fs_entry,
+                         const Constants& vertex_constants = {}, const Constants& fragment_constants = {});
 
 }  // namespace wgsl
 }  // namespace gbr

@@ -4,7 +4,7 @@ from __future__ import annotations
 
 import ctypes as C
 
-GBR_ABI_VERSION = 1
+GBR_ABI_VERSION = 2
 
 # status codes
 OK = 0
@@ -123,7 +123,13 @@ class RenderPipelineDesc(C.Structure):
                 ("has_depth_stencil", u32), ("_pad1", u32), ("depth_stencil", DepthStencilState),
                 ("multisample_count", u32), ("has_fragment", u32), ("fragment_module", u64),
                 ("fragment_entry_point", C.c_char * MAX_ENTRY_POINT_NAME), ("color_target_count", u32),
-                ("_pad2", u32), ("color_targets", ColorTargetState * MAX_COLOR_TARGETS)]
+                ("_pad2", u32), ("color_targets", ColorTargetState * MAX_COLOR_TARGETS),
+                ("vertex_constants", C.c_void_p), ("fragment_constants", C.c_void_p),
+                ("vertex_constant_count", u32), ("fragment_constant_count", u32)]
+
+
+class PipelineConstant(C.Structure):
+    _fields_ = [("key", C.c_char_p), ("value", f64)]
 
 
 class BindGroupEntry(C.Structure):

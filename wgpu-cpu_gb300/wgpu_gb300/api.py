@@ -668,9 +668,27 @@ class Device:
                                depth_stencil: Optional[DepthStencilState] = None,
                                fragment_module: Optional[ShaderModule] = None,
                                targets: Sequence[Optional[ColorTargetState]] = (),
-                               vertex_entry_point: str = "vs_main", fragment_entry_point: str = "fs_main"
+                               vertex_entry_point: str = "vs_main", fragment_entry_point: str = "fs_main",
+                               vertex_constants: Optional[dict] = None, fragment_constants: Optional[dict] = None
                                ) -> RenderPipeline:
+        """wgpu's create_render_pipeline.  `vertex_constants` / `fragment_constants` are the
+        stages' PipelineCompilationOptions::constants: {override @id (as a string) or name: value}."""
         d = A.RenderPipelineDesc()
+        keep = []
+
+        def constants(cs):
+            if not cs:
+                return None, 0
+            arr = (A.PipelineConstant * len(cs))()
+            for i, (k, v) in enumerate(cs.items()):
+                kb = C.create_string_buffer(str(k).encode())
+                keep.append(kb)
+                arr[i] = A.PipelineConstant(C.cast(kb, C.c_char_p), float(v))
+            keep.append(arr)
+            return C.cast(arr, C.c_void_p), len(cs)
+
+        d.vertex_constants, d.vertex_constant_count = constants(vertex_constants)
+        d.fragment_constants, d.fragment_constant_count = constants(fragment_constants)
         d.vertex_module = vertex_module.handle
         d.vertex_entry_point = vertex_entry_point.encode()
         d.vertex_buffer_count = len(vertex_buffers)
