@@ -163,7 +163,7 @@ typedef struct gbr_device_config {
     uint32_t batch_submissions; /* 1 = the worker merges queued submissions into one launch  */
     uint32_t use_graphs;        /* 1 = replay per-shape CUDA graphs                          */
     uint32_t time_kernels;      /* 1 = CUDA events around the raster kernels (stats.raster_ms) */
-    uint64_t hbm_budget_bytes;  /* transient (per-submission) memory budget; 0 = 80 GB       */
+    uint64_t hbm_budget_bytes;  /* HBM for resident resources + transient scratch; 0 = 80 GB  */
     uint32_t raster_order;      /* gbr_raster_order                                          */
     uint32_t raster_rule;       /* gbr_raster_rule (EDGE requires the extension profile)     */
     uint64_t reserved[3];
@@ -617,6 +617,17 @@ GBR_API gbr_status gbr_submission_stats_get(gbr_device device, uint64_t submissi
  * submission `first` to the end of submission `last`, from CUDA events on the device stream. */
 GBR_API gbr_status gbr_device_elapsed_ms(gbr_device device, uint64_t first_submission, uint64_t last_submission,
                                          double* out_ms);
+/* No reference counterpart (serving): the device's HBM use as admission counts it.
+ * resident_bytes: live buffers and textures; transient_bytes: the worker's scratch arena
+ * (grow-only).  With batch_submissions, the worker merges the submissions queued behind the one
+ * it starts while resident_bytes + GBR_ADMISSION_GROUP_BYTES + the sum of their estimates stays
+ * within hbm_budget_bytes; a submission is estimated at GBR_ADMISSION_BYTES_PER_PRIMITIVE per
+ * primitive slot + one byte per 16 target pixels + 4 KiB.  The first submission of a group always
+ * runs; a group whose scratch and the resident resources exceed the budget fails with
+ * GBR_ERR_OUT_OF_MEMORY. */
+#define GBR_ADMISSION_GROUP_BYTES (64ull << 20)
+#define GBR_ADMISSION_BYTES_PER_PRIMITIVE 512u
+GBR_API gbr_status gbr_device_memory(gbr_device device, uint64_t* out_resident_bytes, uint64_t* out_transient_bytes);
 /* No reference counterpart (measurement): enqueues a write of a 256 MiB scratch buffer on the
  * device stream, evicting the L2 cache between timed submissions. */
 GBR_API gbr_status gbr_device_flush_caches(gbr_device device);

@@ -122,3 +122,96 @@ def test_failing_submission_fails_alone():
     finally:
         dev.close()
         ref.close()
+
+
+def equal_submissions(dev, n, tris=4000, side=200, seed=9):
+    """n submissions of the same size: one mesh draw each into its own target."""
+    s = wl.scene_batched(dev, n_targets=n, n_draws=n, tri_lo=tris, tri_hi=tris, side_lo=side, side_hi=side, seed=seed)
+    cmds, targets = [], []
+    for k in range(n):
+        enc = dev.create_command_encoder()
+        wl.MultiScene(dev, passes=[s.passes[k]]).record(enc)
+        cmds.append(enc.finish())
+        targets.append([s.passes[k][:2]])
+    return cmds, targets, s
+
+
+def estimate(tris, side):
+    """The documented per-submission estimate (include/gbr.h, GBR_ADMISSION_*)."""
+    from wgpu_gb300 import _abi as A
+
+    prims = tris + 2  # the draw's primitive slots: index count / 3 + 2
+    return prims * A.ADMISSION_BYTES_PER_PRIMITIVE + side * side // 16 + 4096
+
+
+def busy_submission(dev):
+    """A submission that keeps the device busy for milliseconds with little memory: 2,000 large
+    alpha-blended quads into a 3840x2160 Rgba16Float target (extension profile)."""
+    q = wl.scene_blended_quads(dev, n_quads=2000, size_lo=400, size_hi=1024, seed=6)
+    enc = dev.create_command_encoder()
+    q.record(enc)
+    return enc.finish(), q
+
+
+def test_hbm_budget_admits_one_submission_per_launch():
+    """A budget that holds the resident resources and one submission but not two: submissions that
+    queue up behind a busy one run one per launch (batched_with == 1) with the same results as
+    alone and the oracle; with the default budget the same stream merges."""
+    from wgpu_gb300 import _abi as A
+
+    ext = W.Profile.EXTENSION
+    n, tris, side = 10, 4000, 200
+    probe = W.Device(profile=ext, batch_submissions=True, tile_size=16, warps_per_tile=2)
+    try:
+        keep = (equal_submissions(probe, n, tris, side), busy_submission(probe))
+        resident, _ = probe.memory()
+    finally:
+        probe.close()
+    assert resident > 60 << 20  # the busy target alone holds 66 MB
+    # resident + group + one estimate < budget < resident + group + two estimates
+    budget = resident + A.ADMISSION_GROUP_BYTES + int(1.5 * estimate(tris, side))
+    results = {}
+    for name, kw in (("tight", dict(hbm_budget_bytes=budget)), ("default", {})):
+        dev = W.Device(profile=ext, batch_submissions=True, tile_size=16, warps_per_tile=2, **kw)
+        try:
+            cmds, targets, keep = equal_submissions(dev, n, tris, side)
+            busy, keep_busy = busy_submission(dev)
+            assert dev.memory()[0] == resident
+            h = dev.queue.submit([busy])
+            subs = [dev.queue.submit([c]) for c in cmds]  # they queue while the busy one runs
+            dev.poll(True, subs[-1])
+            dev.poll(True, h)
+            results[name] = ([dev.submission_stats(i) for i in subs], read_all(dev, targets))
+        finally:
+            dev.close()
+    tight_stats, tight_frames = results["tight"]
+    assert all(s.batched_with == 1 for s in tight_stats), [s.batched_with for s in tight_stats]
+    assert max(s.batched_with for s in results["default"][0]) > 1, "the default budget should merge"
+    assert_same_targets(tight_frames, results["default"][1], "one per launch vs merged")
+
+    alone = W.Device(profile=ext, tile_size=16, warps_per_tile=2)
+    orc = oracle_device.device(profile=ext, threads=8)
+    try:
+        for dev, what in ((alone, "alone"), (orc, "oracle")):
+            cmds, targets, keep = equal_submissions(dev, n, tris, side)
+            frags = []
+            for c in cmds:
+                i = dev.queue.submit([c])
+                dev.poll(True, i)
+                frags.append(dev.submission_stats(i).fragments_shaded)
+            assert_same_targets(tight_frames, read_all(dev, targets), f"budgeted vs {what}")
+            assert [s.fragments_shaded for s in tight_stats] == frags
+    finally:
+        alone.close()
+
+
+def test_budget_below_resident_fails_with_out_of_memory():
+    """Resources alone above the budget: a submission fails with OUT_OF_MEMORY, as documented."""
+    dev = W.Device(batch_submissions=True, hbm_budget_bytes=1 << 20)
+    try:
+        s = wl.scene_colored_sphere(dev, 512, 512)
+        with pytest.raises(W.GbrError) as e:
+            s.render()
+        assert e.value.status == -2
+    finally:
+        dev.close()

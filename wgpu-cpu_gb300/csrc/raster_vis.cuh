@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
     __shared__ int4 s_box[NT];
     __shared__ uint32_t s_wsum[WARPS];
     __shared__ uint32_t s_tile, s_last;
+    __shared__ uint2 s_runs;  // fragment-stage runs of the tile, and those that sample a texture
     __shared__ unsigned long long s_frag;
 
     const int lane = threadIdx.x & 31;
@@ -316,10 +317,13 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
         // phase 2: the survivor of each pixel against the stored depth, fragment stage, write-back
         uint32_t clear_c[4] = {0, 0, 0, 0};
         encode_color(tg.color_format, V4{tg.clear[0], tg.clear[1], tg.clear[2], tg.clear[3]}, clear_c);
-        uint32_t fs_runs = 0, tex_runs = 0;  // fragment-stage invocations (survivors that pass), texture-sampling ones
+        if (threadIdx.x == 0) s_runs = make_uint2(0u, 0u);
+        tile_sync<WARPS>();
         for (int p = threadIdx.x; p < NPIX; p += NT) {
             const int x = X0 + (p % T), y = Y0 + (p / T);
-            if (x > XE || y > YE) continue;
+            // fragment-stage runs of this pass over the tile's pixels, counted per warp below
+            bool ran = false, sampled = false;
+            if (x <= XE && y <= YE) {
             const size_t pix = (size_t)y * tg.width + x;
             const unsigned long long key = s_vis[p];
             uint8_t* cdst = tg.color + tg.slice_offset + pix * tg.color_bpp;
@@ -355,18 +359,17 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
 #pragma unroll
                         for (uint32_t qv = 0; qv < MAX_VARYING_FLOATS; ++qv) {
                             if (qv >= nvar) break;
-                            var[qv] = fadd(fadd(fmul(rv[qv], cmp[0]), fmul(rv[nvar + qv], cmp[1])),
-                                           fmul(rv[2 * nvar + qv], cmp[2]));
+                            // @interpolate(flat): the first vertex's value, bits unchanged
+                            const float v0 = rv[qv];
+                            var[qv] = ((rs.flat_mask >> qv) & 1u)
+                                          ? v0
+                                          : fadd(fadd(fmul(v0, cmp[0]), fmul(rv[nvar + qv], cmp[1])),
+                                                 fmul(rv[2 * nvar + qv], cmp[2]));
                         }
                     }
-                    if (rs.flat_mask) {  // @interpolate(flat): the first vertex's value, bits unchanged
-#pragma unroll
-                        for (uint32_t qv = 0; qv < MAX_VARYING_FLOATS; ++qv)
-                            if (qv < nvar && ((rs.flat_mask >> qv) & 1u)) var[qv] = rv[qv];
-                    }
                     V4 col;
-                    ++fs_runs;
-                    tex_runs += rs.tex_data != nullptr;
+                    ran = true;
+                    sampled = rs.tex_data != nullptr;
                     run_fs_any(bp, rs, r, cmp, var, s_lut, col);  // eligible programs never discard
                     if (rs.write_mask != 0xF) {
                         uint32_t dc[4] = {c[0], c[1], c[2], c[3]};
@@ -398,14 +401,17 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                 else *cdst = (uint8_t)c[0];
             }
             if (write_depth) tg.depth[pix] = depth;
+            }
+            const uint32_t mr = __ballot_sync(0xFFFFFFFFu, ran), ms = __ballot_sync(0xFFFFFFFFu, sampled);
+            if (lane == 0 && mr) {
+                atomicAdd(&s_runs.x, (uint32_t)__popc(mr));
+                atomicAdd(&s_runs.y, (uint32_t)__popc(ms));
+            }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            fs_runs += __shfl_xor_sync(0xFFFFFFFFu, fs_runs, o);
-            tex_runs += __shfl_xor_sync(0xFFFFFFFFu, tex_runs, o);
-        }
-        if (lane == 0 && fs_runs && tg.frag_count) {
-            atomicAdd(tg.frag_count + 1, (unsigned long long)fs_runs);
-            if (tex_runs) atomicAdd(tg.frag_count + 2, (unsigned long long)tex_runs);
+        tile_sync<WARPS>();
+        if (threadIdx.x == 0 && s_runs.x && tg.frag_count) {
+            atomicAdd(tg.frag_count + 1, (unsigned long long)s_runs.x);
+            if (s_runs.y) atomicAdd(tg.frag_count + 2, (unsigned long long)s_runs.y);
         }
         tile_sync<WARPS>();
     }

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <cstdarg>
@@ -189,11 +190,19 @@ wgsl::ProgramCode emit_wgsl(const wgsl::Module& vs, const std::string& ve, const
 struct Object {
     virtual ~Object() {}
 };
+// Bytes of resident resources (buffers and textures) a device holds: admission counts them
+// against the HBM budget.  Shared with the resources, which outlive their handles while a queued
+// submission still uses them.
+using ResidentCounter = std::shared_ptr<std::atomic<uint64_t>>;
+
 struct Buffer : Object {
     uint8_t* ptr = nullptr;
     uint64_t size = 0;
+    uint64_t allocated = 0;
+    ResidentCounter resident;
     ~Buffer() override {
         if (ptr) cudaFree(ptr);
+        if (resident) resident->fetch_sub(allocated);
     }
 };
 struct Texture : Object {
@@ -207,8 +216,10 @@ struct Texture : Object {
     uint32_t mip_w(uint32_t m) const { return std::max(1u, desc.size.width >> m); }
     uint32_t mip_h(uint32_t m) const { return std::max(1u, desc.size.height >> m); }
     uint64_t mip_bytes(uint32_t m) const { return (uint64_t)mip_w(m) * mip_h(m) * layers() * bpp; }
+    ResidentCounter resident;
     ~Texture() override {
         if (ptr) cudaFree(ptr);
+        if (resident) resident->fetch_sub(bytes);
     }
 };
 struct Sampler : Object {
@@ -337,16 +348,16 @@ struct GroupRun {
 struct DevBuf {
     void* ptr = nullptr;
     size_t size = 0;
-    void ensure(size_t need, uint64_t* total) {
+    void ensure(size_t need, std::atomic<uint64_t>* total) {
         if (need <= size) return;
         size_t n = std::max(need, size + size / 2);
         if (ptr) cudaFree(ptr);
         ptr = nullptr;
-        *total -= size;
+        total->fetch_sub(size);
         size = 0;
         cuda_check(cudaMalloc(&ptr, n), "cudaMalloc(scratch)");
         size = n;
-        *total += n;
+        total->fetch_add(n);
     }
     void release() {
         if (ptr) cudaFree(ptr);
@@ -359,6 +370,8 @@ struct Batch;
 
 constexpr size_t kLazyWakeItems = 1024;  // queued writes that wake the worker by themselves
 constexpr size_t kKeptRecords = 16384;   // finished submissions whose stats stay queryable
+
+struct PlannedGroup;
 
 struct Device {
     gbr_device_config cfg{};
@@ -376,6 +389,13 @@ struct Device {
     std::mutex obj_mu;
     uint64_t next_handle = 1;
     std::unordered_map<uint64_t, std::shared_ptr<Object>> objects;
+    ResidentCounter resident = std::make_shared<std::atomic<uint64_t>>(0);
+    // HBM a submission group may use for transient memory: the budget less the resident resources
+    uint64_t transient_budget() const {
+        const uint64_t budget = cfg.hbm_budget_bytes ? cfg.hbm_budget_bytes : (80ull << 30);
+        const uint64_t res = resident->load();
+        return budget > res ? budget - res : 0;
+    }
 
     std::mutex q_mu;
     std::condition_variable q_cv, done_cv;
@@ -389,7 +409,7 @@ struct Device {
     std::thread worker;
 
     // worker-owned scratch
-    uint64_t scratch_bytes = 0;
+    std::atomic<uint64_t> scratch_bytes{0};  // the arena below (read by gbr_device_memory)
     DevBuf records_buf, ovf_buf, tiles_buf, bins_buf, meta_buf, flush_buf, slow_buf, strip_buf, upload_buf, hint_buf,
         split_buf;
     // coalesced small writes: double-buffered pinned staging, each free again once its event (the
@@ -472,9 +492,11 @@ struct Device {
         if (queue.size() >= kLazyWakeItems) q_cv.notify_all();
     }
     void worker_main();
+    std::vector<Item> pop_group_locked();
     void execute(Item& it);
     void execute_writes(std::vector<Item>& items);
-    void execute_group(std::vector<Item>& items);
+    PlannedGroup plan_group(std::vector<Item>&& items);
+    void run_group(PlannedGroup& g);
     void note_failure(const Failure& f);
 };
 
@@ -503,6 +525,73 @@ struct Batch {
     bool lines = false;        // one line / point draw, drawn by k_lines_points
     std::shared_ptr<JitKernels> jit;  // the WGSL module whose kernels run this batch (or none)
     std::shared_ptr<CopyCmd> copy;    // a copy or clear between passes (no draws, no targets)
+};
+
+// A submission group planned on the host, ready for the device.
+struct PlannedGroup {
+    std::vector<Item> items;
+    std::vector<SubmissionRecord> recs;
+    std::vector<Batch> batches;
+    Failure failure{GBR_OK, ""};  // a failure of the whole group while planning
+};
+
+// The worker's planning helper: one thread that plans the group handed to start() and hands the
+// result back at finish().
+class Planner {
+  public:
+    explicit Planner(Device* d) : dev_(d), thread_([this] { loop(); }) {}
+    ~Planner() {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            stop_ = true;
+        }
+        cv_.notify_all();
+        thread_.join();
+    }
+    void start(std::vector<Item>&& items) {
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            in_ = std::move(items);
+            have_in_ = true;
+            have_out_ = false;
+        }
+        cv_.notify_all();
+    }
+    PlannedGroup finish() {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return have_out_; });
+        have_out_ = false;
+        return std::move(out_);
+    }
+
+  private:
+    void loop() {
+        cudaSetDevice(dev_->ordinal);
+        for (;;) {
+            std::vector<Item> items;
+            {
+                std::unique_lock<std::mutex> lk(mu_);
+                cv_.wait(lk, [&] { return stop_ || have_in_; });
+                if (stop_) return;
+                items = std::move(in_);
+                have_in_ = false;
+            }
+            PlannedGroup g = dev_->plan_group(std::move(items));
+            {
+                std::lock_guard<std::mutex> lk(mu_);
+                out_ = std::move(g);
+                have_out_ = true;
+            }
+            cv_.notify_all();
+        }
+    }
+    Device* dev_;
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::vector<Item> in_;
+    PlannedGroup out_;
+    bool have_in_ = false, have_out_ = false, stop_ = false;
+    std::thread thread_;
 };
 
 // Visibility raster (kind 3): every target has colour and depth, and every draw writes depth
@@ -796,14 +885,12 @@ constexpr size_t kMaxGroup = 256;  // submissions merged into one launch at most
 constexpr size_t kMaxCoalescedWrites = 4096;           // small buffer writes uploaded together at most
 constexpr uint64_t kMaxCoalescedBytes = 16ull << 20;  // and their bytes
 
-void Device::worker_main() {
-    cudaSetDevice(ordinal);
-    for (;;) {
-        std::vector<Item> group;
+// The next group of queue items (q_mu held): one item, a run of small buffer writes, or a
+// submission with the submissions queued behind it that the HBM budget admits to its launch.
+std::vector<Item> Device::pop_group_locked() {
+    std::vector<Item> group;
+    {
         {
-            std::unique_lock<std::mutex> lk(q_mu);
-            q_cv.wait(lk, [&] { return stopping || !queue.empty(); });
-            if (queue.empty() && stopping) return;
             group.push_back(std::move(queue.front()));
             queue.pop_front();
             // continuous batching: the submissions queued behind this one join its launch while
@@ -833,8 +920,9 @@ void Device::worker_main() {
                 }
             }
             if (group[0].kind == Item::SUBMIT && cfg.batch_submissions) {
-                const uint64_t budget = cfg.hbm_budget_bytes ? cfg.hbm_budget_bytes : (80ull << 30);
-                uint64_t est = submission_estimate(group[0]);
+                // the first submission always runs (it fails with OUT_OF_MEMORY if it cannot fit)
+                const uint64_t budget = transient_budget();
+                uint64_t est = GBR_ADMISSION_GROUP_BYTES + submission_estimate(group[0]);
                 while (!queue.empty() && queue.front().kind == Item::SUBMIT && group.size() < kMaxGroup) {
                     const uint64_t e = submission_estimate(queue.front());
                     if (est + e > budget) break;
@@ -844,9 +932,43 @@ void Device::worker_main() {
                 }
             }
         }
-        if (group[0].kind == Item::SUBMIT) execute_group(group);
-        else if (group.size() > 1) execute_writes(group);
-        else execute(group[0]);
+    }
+    return group;
+}
+
+void Device::worker_main() {
+    cudaSetDevice(ordinal);
+    // Host planning of the next queued submission group runs on this helper thread while the
+    // worker's current group is on the device (planning reads only host-side objects).
+    Planner planner(this);
+    for (;;) {
+        std::vector<Item> group;
+        {
+            std::unique_lock<std::mutex> lk(q_mu);
+            q_cv.wait(lk, [&] { return stopping || !queue.empty(); });
+            if (queue.empty() && stopping) return;
+            group = pop_group_locked();
+        }
+        if (group[0].kind != Item::SUBMIT) {
+            if (group.size() > 1) execute_writes(group);
+            else execute(group[0]);
+            continue;
+        }
+        PlannedGroup cur = plan_group(std::move(group));
+        for (;;) {
+            // look ahead: a submission group already queued is planned while this one runs
+            bool ahead = false;
+            {
+                std::lock_guard<std::mutex> lk(q_mu);
+                if (!queue.empty() && queue.front().kind == Item::SUBMIT) {
+                    planner.start(pop_group_locked());
+                    ahead = true;
+                }
+            }
+            run_group(cur);
+            if (!ahead) break;
+            cur = planner.finish();
+        }
     }
 }
 
@@ -1012,7 +1134,7 @@ uint64_t submission_estimate(const Item& it) {
             prims += (cnt / 3 + 2) * (dc.inst_end > dc.inst_start ? dc.inst_end - dc.inst_start : 0);
         }
     }
-    return prims * 512 + pixels / 16 + 4096;
+    return prims * GBR_ADMISSION_BYTES_PER_PRIMITIVE + pixels / 16 + 4096;
 }
 
 // A run of submissions executed together (one, unless the config merges queued submissions).
@@ -1020,28 +1142,29 @@ uint64_t submission_estimate(const Item& it) {
 // that plan to a single batch are merged into one launch batch while no pass of one writes a
 // texture another reads or writes; the group's batches are launched back to back and every
 // submission gets its own record (fragments counted per target on the device).
-void Device::execute_group(std::vector<Item>& items) {
-    const size_t n = items.size();
-    std::vector<SubmissionRecord> recs(n);
-    const auto t_start = Clock::now();
+// Host planning of a submission group (no device work): each submission planned on its own (a
+// validation failure fails only it), single-batch submissions merged while hazard-free.
+PlannedGroup Device::plan_group(std::vector<Item>&& items) {
+    PlannedGroup g;
+    g.items = std::move(items);
+    const size_t n = g.items.size();
+    g.recs.resize(n);
+    auto& recs = g.recs;
+    auto& batches = g.batches;
     auto fail_item = [&](size_t i, gbr_status st, const std::string& msg) {
         if (recs[i].status == GBR_OK) {
             recs[i].status = st;
             recs[i].error = msg;
         }
     };
-    std::vector<Batch> batches;
-    GroupRun run;
     try {
-        if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
         bool open = false;  // the last batch accepts another single-batch submission
         for (size_t i = 0; i < n; ++i) {
-            recs[i].stats.queue_wait_ms = ms_between(items[i].t_submit, t_start);
             recs[i].stats.batched_with = (uint32_t)n;
             std::vector<Batch> own;
             try {
                 uint64_t draws = 0, prims = 0;
-                own = plan_batches(items[i].passes, &draws, &prims, (uint32_t)i);
+                own = plan_batches(g.items[i].passes, &draws, &prims, (uint32_t)i);
                 recs[i].stats.draws = draws;
                 recs[i].stats.primitives_in = prims;
             } catch (const Failure& f) {
@@ -1053,6 +1176,30 @@ void Device::execute_group(std::vector<Item>& items) {
             for (Batch& b : own) batches.push_back(std::move(b));
             open = single && cfg.batch_submissions && cfg.launch_mode == GBR_LAUNCH_BATCHED;
         }
+    } catch (const Failure& f) {
+        g.failure = f;
+    }
+    return g;
+}
+
+// The group's batches on the device (retries included), then every submission's record.
+void Device::run_group(PlannedGroup& g) {
+    std::vector<Item>& items = g.items;
+    const size_t n = items.size();
+    std::vector<SubmissionRecord>& recs = g.recs;
+    std::vector<Batch>& batches = g.batches;
+    const auto t_start = Clock::now();
+    for (size_t i = 0; i < n; ++i) recs[i].stats.queue_wait_ms = ms_between(items[i].t_submit, t_start);
+    auto fail_item = [&](size_t i, gbr_status st, const std::string& msg) {
+        if (recs[i].status == GBR_OK) {
+            recs[i].status = st;
+            recs[i].error = msg;
+        }
+    };
+    GroupRun run;
+    try {
+        if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
+        if (g.failure.status != GBR_OK) throw g.failure;
         size_t from = 0;
         while (from < batches.size()) {
             const RunResult r = run_batches(batches, from, run);
@@ -1496,7 +1643,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         const size_t split_off_keys = align(split_off_items + (size_t)split_items * sizeof(uint32_t));
         if (vis_npix)
             split_buf.ensure(split_off_keys + (size_t)split_items * vis_npix * sizeof(unsigned long long), &scratch_bytes);
-        if (scratch_bytes > budget) fail(GBR_ERR_OUT_OF_MEMORY, "transient memory exceeds the HBM budget");
+        if (scratch_bytes.load() + resident->load() > budget)
+            fail(GBR_ERR_OUT_OF_MEMORY, "resident resources and transient memory exceed the HBM budget");
         if (!run.started) {
             cuda_check(cudaEventRecord(run.ev->start, stream), "event");
             run.started = true;
@@ -2125,6 +2273,9 @@ GBR_API gbr_status gbr_buffer_create(gbr_device dh, uint64_t size, uint32_t usag
         auto b = std::make_shared<Buffer>();
         b->size = size;
         cuda_check(cudaMalloc(&b->ptr, std::max<uint64_t>(size, 16)), "cudaMalloc(buffer)");
+        b->allocated = std::max<uint64_t>(size, 16);
+        b->resident = d->resident;
+        d->resident->fetch_add(b->allocated);
         cuda_check(cudaMemset(b->ptr, 0, std::max<uint64_t>(size, 16)), "cudaMemset(buffer)");
         *out = d->add(b);
     })
@@ -2236,6 +2387,8 @@ GBR_API gbr_status gbr_texture_create(gbr_device dh, const gbr_texture_desc* des
         }
         t->bytes = off;
         cuda_check(cudaMalloc(&t->ptr, off), "cudaMalloc(texture)");
+        t->resident = d->resident;
+        d->resident->fetch_add(off);
         cuda_check(cudaMemset(t->ptr, 0, off), "cudaMemset(texture)");
         *out = d->add(t);
     })
@@ -2668,6 +2821,14 @@ GBR_API gbr_status gbr_device_elapsed_ms(gbr_device dh, uint64_t first, uint64_t
         float ms = 0.0f;
         cuda_check(cudaEventElapsedTime(&ms, a->second.ev->start, b->second.ev->end), "cudaEventElapsedTime");
         *out_ms = ms;
+    })
+}
+
+GBR_API gbr_status gbr_device_memory(gbr_device dh, uint64_t* resident_bytes, uint64_t* transient_bytes) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        if (resident_bytes) *resident_bytes = d->resident->load();
+        if (transient_bytes) *transient_bytes = d->scratch_bytes.load();
     })
 }
 

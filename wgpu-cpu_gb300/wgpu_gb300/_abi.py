@@ -268,7 +268,13 @@ OPTIONAL = {
     "wgsl_compile_check": (i32, [C.c_char_p, u64, C.c_char_p, C.c_char_p, C.c_char_p, u64]),
     "textures_read": (i32, [u64, u32, P(u64), P(u32), P(C.c_void_p), P(u64)]),
     "queue_write_buffers": (i32, [u64, u32, C.c_void_p]),
+    "device_memory": (i32, [u64, P(u64), P(u64)]),
 }
+
+# admission (include/gbr.h): a group adds this much to the sum of its submissions' estimates,
+# each estimated at ADMISSION_BYTES_PER_PRIMITIVE per primitive slot + pixels / 16 + 4 KiB
+ADMISSION_GROUP_BYTES = 64 << 20
+ADMISSION_BYTES_PER_PRIMITIVE = 512
 
 
 class Lib:

@@ -767,6 +767,14 @@ class Device:
         _check(self.lib, self.lib.device_elapsed_ms(self.handle, first, last, C.byref(out)))
         return out.value
 
+    def memory(self) -> tuple:
+        """(resident bytes of live buffers and textures, bytes of the worker's scratch arena)."""
+        if self.lib.device_memory is None:
+            raise GbrError(A.ERR_UNSUPPORTED, "no memory query in this library")
+        r, t = C.c_uint64(), C.c_uint64()
+        _check(self.lib, self.lib.device_memory(self.handle, C.byref(r), C.byref(t)))
+        return r.value, t.value
+
     def flush_caches(self) -> None:
         if self.lib.device_flush_caches is not None:
             _check(self.lib, self.lib.device_flush_caches(self.handle))
