@@ -250,6 +250,17 @@ __device__ __forceinline__ void span_edge(const TriRecord& r, int y, int& x1, in
 // (util/scanline.rs:14-146): x1 on edge AC, x2 on AB before row b.y and on BC from row b.y.
 // EDGE: the kernels are instantiated for the edge-function rule, whose records all use span_edge
 // (a batch's draws share their device's rule).
+// The scanline rule's span of row y for the framebuffer vertices a, b, c sorted by y.
+__device__ __forceinline__ void span_rows(int ax, int ay, int bx, int by, int cx, int cy, int y, int& x1, int& x2) {
+    int64_t i = y - ay;
+    int64_t a = ax + div_trunc((int64_t)(cx - ax) * i, (int64_t)(cy - ay));
+    int64_t b;
+    if (y < by) b = ax + div_trunc((int64_t)(bx - ax) * i, (int64_t)(by - ay));
+    else b = bx + div_trunc((int64_t)(cx - bx) * (int64_t)(y - by), (int64_t)(cy - by));
+    x1 = (int)(a < b ? a : b);
+    x2 = (int)(a < b ? b : a);
+}
+
 template <bool EDGE = false>
 __device__ __forceinline__ void span_at(const TriRecord& r, int y, int& x1, int& x2) {
     if constexpr (EDGE) {
@@ -261,14 +272,7 @@ __device__ __forceinline__ void span_at(const TriRecord& r, int y, int& x1, int&
         x2 = r.xmax;
         return;
     }
-    const int ax = r.sx[0], ay = r.sy[0], bx = r.sx[1], by = r.sy[1], cx = r.sx[2], cy = r.sy[2];
-    int64_t i = y - ay;
-    int64_t a = ax + div_trunc((int64_t)(cx - ax) * i, (int64_t)(cy - ay));
-    int64_t b;
-    if (y < by) b = ax + div_trunc((int64_t)(bx - ax) * i, (int64_t)(by - ay));
-    else b = bx + div_trunc((int64_t)(cx - bx) * (int64_t)(y - by), (int64_t)(cy - by));
-    x1 = (int)(a < b ? a : b);
-    x2 = (int)(a < b ? b : a);
+    span_rows(r.sx[0], r.sy[0], r.sx[1], r.sy[1], r.sx[2], r.sy[2], y, x1, x2);
 }
 
 // The rows [lo, hi] a record can emit into, clipped to the scissor and the target (lo > hi: none).

@@ -142,16 +142,26 @@ __device__ __forceinline__ void tile_sync() {
 // the minimum over the tile's slots, which is the key array of the whole tile since the survivor
 // key is a minimum, and runs phase 2.  No CTA waits for another.
 template <int T, int WARPS, bool EDGE = false>
-__global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
+__global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchParams bp) {
     constexpr int NT = WARPS * 32, NPIX = T * T;
     constexpr unsigned long long kNone = ~0ull;
     __shared__ unsigned long long s_vis[NPIX];
     __shared__ float s_lut[256];
-    // phase 1: the record table of the chunk being rasterised (per thread: record, key, clipped box
-    // and segments per row, exclusive prefix of the segment counts) and the warps' segment sums
+    // phase 1: the record table of the chunk being rasterised (per thread: record, key, clipped box,
+    // exclusive prefix of the row counts) and the warps' partial sums
     __shared__ const TriRecord* s_rec[NT];
     __shared__ uint32_t s_key[NT], s_excl[NT];
     __shared__ int4 s_box[NT];
+    // per record of the chunk: barycentric terms (a, b, c, the three shoelace constants, 1/area,
+    // area), vertex depths, the span rule's sorted vertices (or the degenerate row's extent) and
+    // flags (bit 0 area in the fast-division range, bit 1 unclipped, bit 2 degenerate)
+    __shared__ float4 s_b0[NT], s_b1[NT], s_b2[NT];
+    __shared__ float2 s_b3[NT];
+    __shared__ int4 s_sp0[NT], s_sp1[NT];
+    // a wave of the chunk's rows: (record | row << 8 | first pixel << 16) and the exclusive prefix
+    // of their covered widths (s_pre[WAVE] = the wave's pixels)
+    constexpr int WAVE = 2 * NT;
+    __shared__ uint32_t s_row[WAVE], s_pre[WAVE + 1];
     __shared__ uint32_t s_wsum[WARPS];
     __shared__ uint32_t s_tile, s_last;
     __shared__ uint2 s_runs;  // fragment-stage runs of the tile, and those that sample a texture
@@ -196,45 +206,24 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
         const uint32_t off = bp.tile_offset[tile];
         uint32_t frag_count = 0;
 
-        auto fragment = [&](const TriRecord& r, const BaryK& k, uint32_t order, int x, int y) {
-            float cmp[3];
-            bary_at<EDGE>(r, k, x, y, cmp);
-            ++frag_count;
-            const float z = frag_z(r, cmp);
-            if (z != z) return;
-            atomicMin(&s_vis[(y - Y0) * T + (x - X0)], vis_key(cmpf, z, order));
-        };
-
-        // phase 1: coverage and survivor keys.  The CTA takes the tile's records NT at a time; their
-        // rows (clipped to tile and scissor), cut into segments of at most kSeg pixels, are dealt to
-        // all NT threads through a block scan of the per-record segment counts, so every thread
-        // rasterises whole row segments (one span each, then the covered pixels) and no warp idles
-        // while another finishes its records.
-        constexpr int kSeg = 8;
+        // phase 1: coverage and survivor keys.  The CTA takes the tile's records NT at a time;
+        // each thread stages its record's constants in shared memory once (the span rule's sorted
+        // framebuffer vertices, the barycentric terms, the vertex depths) and counts its rows
+        // clipped to tile and scissor.  The chunk's rows are then processed in waves of WAVE rows:
+        // (a) every thread takes WAVE / NT consecutive rows, computes each row's span once and
+        // stores it (record, row, first pixel, width); (b) a block scan of the widths deals the
+        // wave's covered pixels to the threads in equal, contiguous ranges, so every lane of a warp
+        // evaluates the same number of fragments (barycentrics, depth, survivor atomicMin).
         constexpr unsigned kFull = 0xFFFFFFFFu;
+        constexpr int RPT = WAVE / NT;  // rows per thread and wave
         const int warp = (int)(threadIdx.x >> 5);
-        for (uint32_t c0 = r_begin; c0 < r_end; c0 += NT) {
-            const uint32_t i = c0 + threadIdx.x;
-            const TriRecord* r = nullptr;
-            uint32_t key = 0;
-            int y0 = 1, y1 = 0, xl = 1, xr = 0;
-            if (i < r_end) {
-                key = bp.bins[off + i];
-                r = record_of(bp, key);
-                const DrawDesc& d = bp.draws[r->draw];
-                y0 = max(max(r->row0, Y0), (int)d.sc_y0);
-                y1 = min(min(r->row1, YE), (int)d.sc_y1 - 1);
-                xl = max(max(r->xmin, X0), (int)d.sc_x0);
-                xr = min(min(r->xmax, XE), (int)d.sc_x1 - 1);
-            }
-            const bool any = y1 >= y0 && xr >= xl;
-            const int segs_row = any ? (xr - xl + kSeg) / kSeg : 0;
-            const uint32_t slots = any ? (uint32_t)((y1 - y0 + 1) * segs_row) : 0u;
-            uint32_t incl = slots;
+        // exclusive block scan of v (one value per thread); returns the prefix, *tot the sum
+        auto block_scan = [&](uint32_t v, uint32_t* tot) -> uint32_t {
+            uint32_t incl = v;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t v = __shfl_up_sync(kFull, incl, o);
-                if (lane >= o) incl += v;
+                const uint32_t u = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += u;
             }
             if (lane == 31) s_wsum[warp] = incl;
             tile_sync<WARPS>();
@@ -245,36 +234,138 @@ __global__ void __launch_bounds__(WARPS * 32) k_raster_vis(BatchParams bp) {
                 woff += w < warp ? ws : 0u;
                 total += ws;
             }
-            s_excl[threadIdx.x] = woff + incl - slots;
-            s_rec[threadIdx.x] = r;
-            s_key[threadIdx.x] = key;
-            s_box[threadIdx.x] = make_int4(y0, xl, xr, segs_row);
-            tile_sync<WARPS>();
-            for (uint32_t t = threadIdx.x; t < total; t += NT) {
-                // the record of slot t: the last entry whose exclusive prefix is <= t (it has slots)
-                int j = 0;
-#pragma unroll
-                for (int step = NT / 2; step > 0; step >>= 1)
-                    if (s_excl[j + step] <= t) j += step;
-                const int4 bx = s_box[j];
-                const TriRecord* rr = s_rec[j];
-                const uint32_t local = t - s_excl[j];
-                const int sr = bx.w;
-                const int row = sr == 1 ? (int)local : (int)(local / (uint32_t)sr);
-                const int seg = (int)local - row * sr;
-                const int y = bx.x + row;
-                const int sx0 = bx.y + seg * kSeg, sx1 = min(bx.z, sx0 + kSeg - 1);
-                int x1, x2;
-                span_at<EDGE>(*rr, y, x1, x2);
-                x1 = max(x1, sx0);
-                x2 = min(x2, sx1);
-                if (x1 > x2) continue;
-                BaryK k;
-                bary_consts(*rr, k);
-                const uint32_t rkey = s_key[j];
-                for (int x = x1; x <= x2; ++x) fragment(*rr, k, rkey, x, y);
+            *tot = total;
+            return woff + incl - v;
+        };
+        for (uint32_t c0 = r_begin; c0 < r_end; c0 += NT) {
+            const uint32_t i = c0 + threadIdx.x;
+            uint32_t rows = 0;
+            if (i < r_end) {
+                const uint32_t key = bp.bins[off + i];
+                const TriRecord* r = record_of(bp, key);
+                const DrawDesc& d = bp.draws[r->draw];
+                const int y0 = max(max(r->row0, Y0), (int)d.sc_y0);
+                const int y1 = min(min(r->row1, YE), (int)d.sc_y1 - 1);
+                const int xl = max(max(r->xmin, X0), (int)d.sc_x0);
+                const int xr = min(min(r->xmax, XE), (int)d.sc_x1 - 1);
+                if (y1 >= y0 && xr >= xl) {
+                    rows = (uint32_t)(y1 - y0 + 1);
+                    BaryK k;
+                    bary_consts(*r, k);
+                    s_b0[threadIdx.x] = make_float4(k.ax, k.ay, k.bx, k.by);
+                    s_b1[threadIdx.x] = make_float4(k.cx, k.cy, k.kc0, k.kc1);
+                    s_b2[threadIdx.x] = make_float4(k.kc2, k.rcp, k.area, r->fz[0]);
+                    s_b3[threadIdx.x] = make_float2(r->fz[1], r->fz[2]);
+                    const int fl = (k.area_ok ? 1 : 0) | (k.ident ? 2 : 0) | ((r->flags & (SPAN_DEGENERATE << 2)) ? 4 : 0);
+                    if (EDGE || !(fl & 4))
+                        s_sp0[threadIdx.x] = make_int4(r->sx[0], r->sy[0], r->sx[1], r->sy[1]);
+                    else
+                        s_sp0[threadIdx.x] = make_int4(r->xmin, r->xmax, 0, 0);
+                    s_sp1[threadIdx.x] = make_int4(r->sx[2], r->sy[2], fl, 0);
+                    s_box[threadIdx.x] = make_int4(y0, xl, xr, 0);
+                    s_rec[threadIdx.x] = r;
+                    s_key[threadIdx.x] = key;
+                }
             }
-            tile_sync<WARPS>();  // the shared record table is refilled by the next chunk
+            uint32_t total_rows;
+            s_excl[threadIdx.x] = block_scan(rows, &total_rows);
+            tile_sync<WARPS>();
+            for (uint32_t w0 = 0; w0 < total_rows; w0 += WAVE) {
+                // (a) spans of this thread's rows [q0, q0 + RPT) of the wave
+                const uint32_t q0 = w0 + (uint32_t)threadIdx.x * RPT;
+                uint32_t widths = 0;
+                uint32_t ent[RPT], wid[RPT];
+                int j = 0;
+                if (q0 < total_rows) {  // the record of row q0: the last entry whose prefix is <= q0
+#pragma unroll
+                    for (int step = NT / 2; step > 0; step >>= 1)
+                        if (s_excl[j + step] <= q0) j += step;
+                }
+                uint32_t jend = j + 1 < NT ? s_excl[j + 1] : total_rows;
+#pragma unroll
+                for (int k = 0; k < RPT; ++k) {
+                    const uint32_t q = q0 + k;
+                    ent[k] = 0;
+                    wid[k] = 0;
+                    if (q < total_rows) {
+                        while (q >= jend) {  // the next record with rows
+                            ++j;
+                            jend = j + 1 < NT ? s_excl[j + 1] : total_rows;
+                        }
+                        const int4 bx = s_box[j];
+                        const int y = bx.x + (int)(q - s_excl[j]);
+                        int x1, x2;
+                        if constexpr (EDGE) {
+                            span_at<EDGE>(*s_rec[j], y, x1, x2);
+                        } else {
+                            const int4 sp0 = s_sp0[j], sp1 = s_sp1[j];
+                            if (sp1.z & 4) {
+                                x1 = sp0.x;
+                                x2 = sp0.y;
+                            } else {
+                                span_rows(sp0.x, sp0.y, sp0.z, sp0.w, sp1.x, sp1.y, y, x1, x2);
+                            }
+                        }
+                        x1 = max(x1, bx.y);
+                        x2 = min(x2, bx.z);
+                        if (x1 <= x2) {
+                            wid[k] = (uint32_t)(x2 - x1 + 1);
+                            ent[k] = (uint32_t)j | ((uint32_t)(y - Y0) << 8) | ((uint32_t)(x1 - X0) << 16);
+                        }
+                    }
+                    widths += wid[k];
+                }
+                uint32_t total_px;
+                uint32_t pre = block_scan(widths, &total_px);
+#pragma unroll
+                for (int k = 0; k < RPT; ++k) {
+                    s_row[threadIdx.x * RPT + k] = ent[k];
+                    s_pre[threadIdx.x * RPT + k] = pre;
+                    pre += wid[k];
+                }
+                if (threadIdx.x == 0) s_pre[WAVE] = total_px;
+                tile_sync<WARPS>();
+                // (b) this thread's pixels [p, p_end) of the wave's total_px
+                const uint32_t per = (total_px + NT - 1) / NT;
+                uint32_t p = min(total_px, (uint32_t)threadIdx.x * per);
+                const uint32_t p_end = min(total_px, p + per);
+                if (p < p_end) {
+                    int q = 0;  // the row of pixel p: the last row whose prefix is <= p (and has pixels)
+#pragma unroll
+                    for (int step = WAVE / 2; step > 0; step >>= 1)
+                        if (s_pre[q + step] <= p) q += step;
+                    uint32_t qend = s_pre[q + 1];
+                    while (p < p_end) {
+                        while (p >= qend) qend = s_pre[++q + 1];
+                        const uint32_t e = s_row[q];
+                        const int jj = (int)(e & 0xFFu), y = Y0 + (int)((e >> 8) & 0xFFu);
+                        const int xb = X0 + (int)(e >> 16) - (int)s_pre[q];
+                        const float4 b0 = s_b0[jj], b1 = s_b1[jj], b2 = s_b2[jj];
+                        const float2 b3 = s_b3[jj];
+                        const int fl = s_sp1[jj].z;
+                        BaryK k;
+                        k.ax = b0.x; k.ay = b0.y; k.bx = b0.z; k.by = b0.w;
+                        k.cx = b1.x; k.cy = b1.y; k.kc0 = b1.z; k.kc1 = b1.w;
+                        k.kc2 = b2.x; k.rcp = b2.y; k.area = b2.z;
+                        k.area_ok = (fl & 1) != 0;
+                        k.ident = (fl & 2) != 0;
+                        const uint32_t rkey = s_key[jj];
+                        const TriRecord* rr = s_rec[jj];
+                        const uint32_t stop = min(p_end, qend);
+                        for (; p < stop; ++p) {
+                            const int x = xb + (int)p;
+                            float cmp[3];
+                            bary_at<EDGE>(*rr, k, x, y, cmp);
+                            ++frag_count;
+                            // fragment.z (raster.rs:345-346) from the staged vertex depths
+                            const float z = fadd(fadd(fmul(b2.w, cmp[0]), fmul(b3.x, cmp[1])), fmul(b3.y, cmp[2]));
+                            if (z != z) continue;
+                            atomicMin(&s_vis[(y - Y0) * T + (x - X0)], vis_key(cmpf, z, rkey));
+                        }
+                    }
+                }
+                tile_sync<WARPS>();  // the wave's rows are rewritten by the next wave
+            }
         }
         tile_sync<WARPS>();
         for (int o = 16; o > 0; o >>= 1) frag_count += __shfl_xor_sync(0xFFFFFFFFu, frag_count, o);
