@@ -49,7 +49,9 @@ def test_launch_modes_match_oracle(oracle_result, mode, order):
         out, n, st, _ = render_all(dev, **SMALL)
         assert_targets_same((out, n), oracle_result, f"mode {mode}")
         if mode == W.LaunchMode.BATCHED:
-            assert st.kernel_launches <= 6, st.kernel_launches  # one launch sequence for all draws
+            # one launch sequence for all draws: the setup stage is one launch per vertex-shader
+            # shape present in the batch, every other stage one launch
+            assert st.kernel_launches <= 8, st.kernel_launches
         if mode == W.LaunchMode.PER_DRAW:
             assert st.kernel_launches >= 4 * SMALL["n_draws"]
     finally:

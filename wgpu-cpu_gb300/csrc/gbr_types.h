@@ -275,7 +275,7 @@ struct BatchParams {
     unsigned long long* split_keys;  // [split_cap_items][T * T] survivor keys each chunk leaves
     uint32_t split_cap_heavy, split_cap_items;
     uint32_t split_chunk;        // records per chunk work item (> 0 when split_heavy is set)
-    uint32_t _pad_split;
+    uint32_t fvs_mask;           // bit f: a draw of the batch has FastVs shape f (0: unknown, one generic setup launch)
     const uint32_t* draw_base;   // [num_draws] prim_base of each draw, contiguous (null: read the descriptors)
 };
 

@@ -28,7 +28,7 @@ bool raster_config_supported(int tile, int warps);
 size_t raster_state_bytes();
 
 // Kernels launch_batch enqueues for a batch (its `launches` increment).
-uint32_t batch_kernel_launches(uint32_t total_prims, int tile, int warps, int kind);
+uint32_t batch_kernel_launches(uint32_t total_prims, int tile, int warps, int kind, uint32_t fvs_mask);
 
 // The FastVs shape of a resolved draw (FAST_VS_NONE when the fast setup path cannot run it).
 uint32_t fast_vs_kind(const DrawDesc& d);

@@ -101,7 +101,48 @@ inline bool vis_config_supported(int tile, int warps) {
     }
 }
 
+// One k_setup launch (all shapes when ONLY < 0), grid-stride over one wave of resident blocks.
+template <bool EDGE, int ONLY>
+cudaError_t launch_setup(const BatchParams& bp, int num_sms, cudaStream_t s) {
+    const size_t smem = setup_stage_bytes(bp.record_stride);
+    int resident = 1;  // k_setup blocks an SM holds at this stage size
+    static LaunchCache cache;
+    cudaError_t e = resident_blocks(cache, k_setup<EDGE, ONLY>, kSetupWarps * 32, smem, &resident);
+    if (e != cudaSuccess) return e;
+    const uint32_t cap = (uint32_t)num_sms * 16;
+    const uint32_t g = std::min((bp.total_prims + 127) / 128, std::min(cap, (uint32_t)(resident * num_sms)));
+    k_setup<EDGE, ONLY><<<g, kSetupWarps * 32, smem, s>>>(bp);
+    return cudaGetLastError();
+}
+
 }  // namespace launch_detail
+
+// The setup launches of a batch: one per FastVs shape its draws use (each kernel holds one
+// vertex-stage variant), or one generic launch when the shapes are not known.
+template <bool EDGE>
+cudaError_t launch_setups(const BatchParams& bp, int num_sms, cudaStream_t s, uint32_t* launches) {
+    using namespace launch_detail;
+    if (!bp.fvs_mask) {
+        ++*launches;
+        return launch_setup<EDGE, -1>(bp, num_sms, s);
+    }
+    for (int f = 0; f < 7; ++f) {
+        if (!((bp.fvs_mask >> f) & 1u)) continue;
+        cudaError_t e;
+        switch (f) {
+            case FAST_VS_NONE: e = launch_setup<EDGE, FAST_VS_NONE>(bp, num_sms, s); break;
+            case FAST_VS_MVP_COLOR: e = launch_setup<EDGE, FAST_VS_MVP_COLOR>(bp, num_sms, s); break;
+            case FAST_VS_MVP_TEX: e = launch_setup<EDGE, FAST_VS_MVP_TEX>(bp, num_sms, s); break;
+            case FAST_VS_QUAD: e = launch_setup<EDGE, FAST_VS_QUAD>(bp, num_sms, s); break;
+            case FAST_VS_CLIP: e = launch_setup<EDGE, FAST_VS_CLIP>(bp, num_sms, s); break;
+            case FAST_VS_TRIANGLE: e = launch_setup<EDGE, FAST_VS_TRIANGLE>(bp, num_sms, s); break;
+            default: e = launch_setup<EDGE, FAST_VS_QUAD_F16>(bp, num_sms, s); break;
+        }
+        if (e != cudaSuccess) return e;
+        ++*launches;
+    }
+    return cudaSuccess;
+}
 
 template <bool EDGE>
 cudaError_t launch_batch_t(const BatchParams& bp, int tile, int warps, int num_sms, cudaStream_t s,
@@ -119,14 +160,7 @@ cudaError_t launch_batch_t(const BatchParams& bp, int tile, int warps, int num_s
         ++*launches;
     }
     if (items) {
-        const size_t smem = setup_stage_bytes(bp.record_stride);
-        int resident = 1;  // k_setup blocks an SM holds at this stage size (grid-stride: one wave)
-        static LaunchCache setup_cache;
-        if ((e = resident_blocks(setup_cache, k_setup<EDGE>, kSetupWarps * 32, smem, &resident)) != cudaSuccess) return e;
-        const uint32_t g = std::min((items + 127) / 128, std::min(cap, (uint32_t)(resident * num_sms)));
-        k_setup<EDGE><<<g, kSetupWarps * 32, smem, s>>>(bp);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        ++*launches;
+        if ((e = launch_setups<EDGE>(bp, num_sms, s, launches)) != cudaSuccess) return e;
         k_setup_slow<EDGE><<<std::min((items + 127) / 128, (uint32_t)num_sms * 4), 128, 0, s>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         ++*launches;

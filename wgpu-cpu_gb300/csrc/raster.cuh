@@ -1116,7 +1116,12 @@ __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc&
 // primary records are built in shared memory and written out as one contiguous, coalesced
 // block (records of consecutive primitives are adjacent).  Primitives it cannot finish are
 // queued for k_setup_slow.
-template <bool EDGE>
+//
+// ONLY >= 0: this launch sets up only the 32-primitive groups it owns — the groups of one draw
+// whose FastVs shape is ONLY, and, when ONLY is the lowest shape of the batch (bp.fvs_mask), the
+// groups straddling draws — so its code holds one vertex-stage variant; the launch sequence runs
+// one such launch per shape present.  ONLY = -1 sets up every group (all variants inlined).
+template <bool EDGE, int ONLY = -1>
 __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
     extern __shared__ __align__(16) uint8_t s_stage_raw[];
     __shared__ DrawCache s_dc[kSetupWarps];
@@ -1144,6 +1149,10 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
         }
         const uint32_t di0 = __shfl_sync(0xFFFFFFFFu, di, 0);
         const bool uniform = __all_sync(0xFFFFFFFFu, !live || di == di0);
+        if constexpr (ONLY >= 0) {  // another launch's group: nothing to do here (warp-uniform)
+            const int owner = uniform ? (int)__ldg(&bp.draws[di0].fast_vs) : __ffs(bp.fvs_mask) - 1;
+            if (owner != ONLY) continue;
+        }
         if (uniform && dc.id != di0) {  // warp-uniform
             __syncwarp();
             const uint2* src = reinterpret_cast<const uint2*>(bp.draws + di0);
@@ -1159,6 +1168,9 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
         const TriRecord* coop = nullptr;
         bool done = false;
         if (live && uniform) {
+            if constexpr (ONLY > 0) {
+                done = fast_prim<ONLY, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop);
+            } else if constexpr (ONLY < 0) {
             switch (dc.d.fast_vs) {  // warp-uniform
                 case FAST_VS_MVP_COLOR: done = fast_prim<FAST_VS_MVP_COLOR, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
                 case FAST_VS_MVP_TEX: done = fast_prim<FAST_VS_MVP_TEX, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
@@ -1167,6 +1179,7 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
                 case FAST_VS_TRIANGLE: done = fast_prim<FAST_VS_TRIANGLE, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
                 case FAST_VS_QUAD_F16: done = fast_prim<FAST_VS_QUAD_F16, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
                 default: break;
+            }
             }
         }
         // tile counts of the finished records: one atomic per distinct tile of the warp's

@@ -594,6 +594,13 @@ class Planner {
     std::thread thread_;
 };
 
+// The FastVs shapes of a batch's draws (bit per shape): one setup launch each.
+uint32_t fvs_mask(const Batch& b) {
+    uint32_t m = 0;
+    for (const DrawDesc& d : b.draws) m |= 1u << d.fast_vs;
+    return m;
+}
+
 // Visibility raster (kind 3): every target has colour and depth, and every draw writes depth
 // with one batch-wide Less / LessEqual / Greater / GreaterEqual, does not blend and runs a
 // fragment stage that never discards.  Returns the compare function, or 0.
@@ -1688,6 +1695,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 bp.status = reinterpret_cast<BatchStatus*>(meta + off_status) + i;
                 bp.abort_flag = reinterpret_cast<uint32_t*>(meta);
                 bp.raster_rule = cfg.raster_rule;
+                bp.fvs_mask = b.jit ? 0u : fvs_mask(b);
                 if (kinds[i] == 3) {
                     bp.states = meta + states_off[i];
                     bp.vis_compare = visibility_compare(b);
@@ -1736,6 +1744,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 put(&batches[i].total_prims, sizeof(uint32_t));
                 put(&batches[i].total_tiles, sizeof(uint32_t));
                 put(&batches[i].nvar, sizeof(uint32_t));
+                const uint32_t fm = fvs_mask(batches[i]);
+                put(&fm, sizeof fm);
                 const void* jp = batches[i].jit.get();
                 put(&jp, sizeof jp);
                 const size_t nd = batches[i].draws.size(), nt = batches[i].targets.size();
@@ -1784,7 +1794,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                     run.launches += batches[i].lines ? 2u : (batches[i].strip_entries ? 1u : 0u) +
                                     (batches[i].jit ? 2u + (batches[i].total_prims ? 3u : 0u) + (kinds[i] == 3 ? 1u : 0u)
                                                     : batch_kernel_launches(batches[i].total_prims, btile[i], bwarps[i],
-                                                                            kinds[i]));
+                                                                            kinds[i], fvs_mask(batches[i])));
             }
             cuda_check(cudaGraphLaunch(graphs[key].exec, stream), "cudaGraphLaunch");
         } else {
