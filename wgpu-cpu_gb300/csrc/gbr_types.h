@@ -276,6 +276,12 @@ struct BatchParams {
     uint32_t split_cap_heavy, split_cap_items;
     uint32_t split_chunk;        // records per chunk work item (> 0 when split_heavy is set)
     uint32_t fvs_mask;           // bit f: a draw of the batch has FastVs shape f (0: unknown, one generic setup launch)
+    // draw-aligned setup groups per FastVs shape f: entries [sg_off[f], sg_off[f + 1]) of
+    // shape_groups are pairs (draw, first 32-primitive group of the draw, counted over the shape's
+    // draws in batch order), the last pair (~0, the shape's group count); none when no draw of the
+    // shape has primitives
+    const uint32_t* shape_groups;
+    uint32_t sg_off[8];
     const uint32_t* draw_base;   // [num_draws] prim_base of each draw, contiguous (null: read the descriptors)
 };
 

@@ -1117,53 +1117,42 @@ __device__ __forceinline__ bool fast_prim(const BatchParams& bp, const DrawDesc&
 // block (records of consecutive primitives are adjacent).  Primitives it cannot finish are
 // queued for k_setup_slow.
 //
-// ONLY >= 0: this launch sets up only the 32-primitive groups it owns — the groups of one draw
-// whose FastVs shape is ONLY, and, when ONLY is the lowest shape of the batch (bp.fvs_mask), the
-// groups straddling draws — so its code holds one vertex-stage variant; the launch sequence runs
-// one such launch per shape present.  ONLY = -1 sets up every group (all variants inlined).
+// ONLY >= 0: this launch sets up the draws whose FastVs shape is ONLY, so its code holds one
+// vertex-stage variant; the launch sequence runs one such launch per shape present.  Its work is
+// the shape's draws cut into 32-primitive groups aligned at each draw's first primitive
+// (bp.shape_groups lists them), so every group lies within one draw; a warp finds its group's
+// draw by a 32-way search of that list (two rounds for a thousand draws).
+// ONLY = -1 sets up every primitive of the batch in 32-primitive groups of the batch's primitive
+// order (all variants inlined); a group straddling draws goes to the generic kernel.
 template <bool EDGE, int ONLY = -1>
 __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
     extern __shared__ __align__(16) uint8_t s_stage_raw[];
     __shared__ DrawCache s_dc[kSetupWarps];
+    constexpr unsigned kFull = 0xFFFFFFFFu;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t rstride = bp.record_stride;
     uint8_t* stage = s_stage_raw + (size_t)warp * 32 * rstride;
     DrawCache& dc = s_dc[warp];
     if (lane == 0) dc.id = 0xFFFFFFFFu;
     __syncwarp();
-    // grid-stride over 32-primitive groups (measured faster than giving each warp a contiguous run
-    // of groups: 3.3 against 4.1 ms on the batched workload, whose expensive draws then pile up on
-    // a few warps)
     if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the grid
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < bp.total_prims; base += stride) {
+
+    // the draw's descriptor and matrix to the warp's cache (warp-uniform)
+    auto cache_draw = [&](uint32_t di) {
+        __syncwarp();
+        const uint2* src = reinterpret_cast<const uint2*>(bp.draws + di);
+        uint2* dst = reinterpret_cast<uint2*>(&dc.d);
+        for (uint32_t k = lane; k < sizeof(DrawDesc) / 8; k += 32) dst[k] = __ldg(src + k);
+        const uint8_t* u = bp.draws[di].uniform[0][0];
+        const bool has = u != nullptr && bp.draws[di].uniform_size[0][0] >= 64;
+        if (lane < 16) dc.mvp[lane] = has ? __ldg(reinterpret_cast<const float*>(u) + lane) : 0.0f;
+        if (lane == 0) dc.id = di;
+        __syncwarp();
+    };
+    // primitives [base, base + nrec) of the batch, lane -> base + lane (live: a primitive of the
+    // batch; uniform: the warp's live lanes share draw di, which is in the cache)
+    auto setup_group = [&](uint32_t base, uint32_t nrec, bool live, bool uniform, uint32_t di) {
         const uint32_t gp = base + lane;
-        const bool live = gp < bp.total_prims;
-        uint32_t di = 0;
-        if (live) {
-            if (dc.id != 0xFFFFFFFFu && gp >= dc.d.prim_base &&
-                gp - dc.d.prim_base < dc.d.prims_per_instance * dc.d.instance_count)
-                di = dc.id;
-            else
-                di = find_draw(bp, gp);
-        }
-        const uint32_t di0 = __shfl_sync(0xFFFFFFFFu, di, 0);
-        const bool uniform = __all_sync(0xFFFFFFFFu, !live || di == di0);
-        if constexpr (ONLY >= 0) {  // another launch's group: nothing to do here (warp-uniform)
-            const int owner = uniform ? (int)__ldg(&bp.draws[di0].fast_vs) : __ffs(bp.fvs_mask) - 1;
-            if (owner != ONLY) continue;
-        }
-        if (uniform && dc.id != di0) {  // warp-uniform
-            __syncwarp();
-            const uint2* src = reinterpret_cast<const uint2*>(bp.draws + di0);
-            uint2* dst = reinterpret_cast<uint2*>(&dc.d);
-            for (uint32_t k = lane; k < sizeof(DrawDesc) / 8; k += 32) dst[k] = __ldg(src + k);
-            const uint8_t* u = bp.draws[di0].uniform[0][0];
-            const bool has = u != nullptr && bp.draws[di0].uniform_size[0][0] >= 64;
-            if (lane < 16) dc.mvp[lane] = has ? __ldg(reinterpret_cast<const float*>(u) + lane) : 0.0f;
-            if (lane == 0) dc.id = di0;
-            __syncwarp();
-        }
         TriRecord* rec = reinterpret_cast<TriRecord*>(stage + (size_t)lane * rstride);
         const TriRecord* coop = nullptr;
         bool done = false;
@@ -1171,15 +1160,15 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
             if constexpr (ONLY > 0) {
                 done = fast_prim<ONLY, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop);
             } else if constexpr (ONLY < 0) {
-            switch (dc.d.fast_vs) {  // warp-uniform
-                case FAST_VS_MVP_COLOR: done = fast_prim<FAST_VS_MVP_COLOR, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                case FAST_VS_MVP_TEX: done = fast_prim<FAST_VS_MVP_TEX, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                case FAST_VS_QUAD: done = fast_prim<FAST_VS_QUAD, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                case FAST_VS_CLIP: done = fast_prim<FAST_VS_CLIP, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                case FAST_VS_TRIANGLE: done = fast_prim<FAST_VS_TRIANGLE, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                case FAST_VS_QUAD_F16: done = fast_prim<FAST_VS_QUAD_F16, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
-                default: break;
-            }
+                switch (dc.d.fast_vs) {  // warp-uniform
+                    case FAST_VS_MVP_COLOR: done = fast_prim<FAST_VS_MVP_COLOR, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                    case FAST_VS_MVP_TEX: done = fast_prim<FAST_VS_MVP_TEX, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                    case FAST_VS_QUAD: done = fast_prim<FAST_VS_QUAD, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                    case FAST_VS_CLIP: done = fast_prim<FAST_VS_CLIP, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                    case FAST_VS_TRIANGLE: done = fast_prim<FAST_VS_TRIANGLE, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                    case FAST_VS_QUAD_F16: done = fast_prim<FAST_VS_QUAD_F16, EDGE>(bp, dc.d, dc.mvp, gp, di, rec, coop); break;
+                    default: break;
+                }
             }
         }
         // tile counts of the finished records: one atomic per distinct tile of the warp's
@@ -1191,7 +1180,7 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
             if (bp.tile_hint) bp.tile_hint[gp] = hint;
         }
         const uint32_t single = hint < TILE_HINT_EMPTY ? hint : 0xFFFFFFFFu;
-        const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single);
+        const uint32_t peers = __match_any_sync(kFull, single);
         if (single != 0xFFFFFFFFu && (int)lane == __ffs(peers) - 1) atomicAdd(&bp.tile_count[single], (uint32_t)__popc(peers));
         if (hint == TILE_HINT_WALK && coop == nullptr) {
             const TargetDesc& t = bp.targets[dc.d.target];
@@ -1199,23 +1188,69 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
                                 [&](uint32_t lt) { atomicAdd(&bp.tile_count[t.tile_base + lt], 1u); });
         }
         // the rest to the generic kernel (its record is rewritten there)
-        const uint32_t m = __ballot_sync(0xFFFFFFFFu, live && !done);
+        const uint32_t m = __ballot_sync(kFull, live && !done);
         if (m) {
             const int leader = __ffs(m) - 1;
             uint32_t at = 0;
             if ((int)lane == leader) at = atomicAdd(&bp.status->slow_count, (uint32_t)__popc(m));
-            at = __shfl_sync(0xFFFFFFFFu, at, leader);
+            at = __shfl_sync(kFull, at, leader);
             if (live && !done) bp.slow_prims[at + __popc(m & ((1u << lane) - 1u))] = gp;
         }
         coop_tiles<EDGE>(bp, coop, lane, [&](uint32_t tile, uint32_t) { atomicAdd(&bp.tile_count[tile], 1u); });
         // the warp's records, staged above, out as one block
         __syncwarp();
-        const uint32_t nrec = min(32u, bp.total_prims - base);
         const uint32_t words = nrec * (rstride / 16);
         uint4* gdst = reinterpret_cast<uint4*>(bp.records + (size_t)base * rstride);
         const uint4* ssrc = reinterpret_cast<const uint4*>(stage);
         for (uint32_t k = lane; k < words; k += 32) gdst[k] = ssrc[k];
         __syncwarp();
+    };
+
+    if constexpr (ONLY >= 0) {
+        // grid-stride over the shape's draw-aligned groups
+        const uint32_t e0 = bp.sg_off[ONLY], e1 = bp.sg_off[ONLY + 1];
+        if (e1 == e0) return;
+        const uint2* tab = reinterpret_cast<const uint2*>(bp.shape_groups);
+        const uint32_t groups = __ldg(&tab[e1 - 1].y);
+        const uint32_t nwarps = gridDim.x * kSetupWarps;
+        for (uint32_t g = blockIdx.x * kSetupWarps + warp; g < groups; g += nwarps) {
+            // the last of the shape's draws whose first group is <= g; tab[lo].y <= g throughout
+            uint32_t lo = e0, cnt = e1 - 1 - e0;
+            while (cnt > 32) {
+                const uint32_t step = (cnt + 31) / 32;
+                const bool le = lane * step < cnt && __ldg(&tab[lo + lane * step].y) <= g;
+                const uint32_t at = 31 - __clz(__ballot_sync(kFull, le)) ;
+                lo += at * step;
+                cnt = min(step, cnt - at * step);
+            }
+            const bool le = lane < cnt && __ldg(&tab[lo + lane].y) <= g;
+            const uint2 ent = __ldg(&tab[lo + 31 - __clz(__ballot_sync(kFull, le))]);
+            if (dc.id != ent.x) cache_draw(ent.x);
+            const uint32_t first = dc.d.prim_base + (g - ent.y) * 32u;
+            const uint32_t end = dc.d.prim_base + dc.d.prims_per_instance * dc.d.instance_count;
+            setup_group(first, min(32u, end - first), first + lane < end, true, ent.x);
+        }
+    } else {
+        // grid-stride over 32-primitive groups (measured faster than giving each warp a contiguous
+        // run of groups: 3.3 against 4.1 ms on the batched workload, whose expensive draws then
+        // pile up on a few warps)
+        const uint32_t stride = gridDim.x * blockDim.x;
+        for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < bp.total_prims; base += stride) {
+            const uint32_t gp = base + lane;
+            const bool live = gp < bp.total_prims;
+            uint32_t di = 0;
+            if (live) {
+                if (dc.id != 0xFFFFFFFFu && gp >= dc.d.prim_base &&
+                    gp - dc.d.prim_base < dc.d.prims_per_instance * dc.d.instance_count)
+                    di = dc.id;
+                else
+                    di = find_draw(bp, gp);
+            }
+            const uint32_t di0 = __shfl_sync(kFull, di, 0);
+            const bool uniform = __all_sync(kFull, !live || di == di0);
+            if (uniform && dc.id != di0) cache_draw(di0);
+            setup_group(base, min(32u, bp.total_prims - base), live, uniform, di);
+        }
     }
 }
 

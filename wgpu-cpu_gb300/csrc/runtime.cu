@@ -601,6 +601,31 @@ uint32_t fvs_mask(const Batch& b) {
     return m;
 }
 
+// The setup kernels' work list per FastVs shape (BatchParams::shape_groups): for each shape f,
+// its draws with primitives as pairs (draw, first 32-primitive group), groups numbered over the
+// shape's draws in batch order and aligned at each draw's first primitive, then (~0, the shape's
+// group count); off[f] .. off[f + 1] are the shape's pairs.
+void shape_group_table(const Batch& b, std::vector<uint32_t>& table, uint32_t off[8]) {
+    table.clear();
+    for (uint32_t f = 0; f < 7; ++f) {
+        off[f] = (uint32_t)(table.size() / 2);
+        uint32_t groups = 0;
+        for (uint32_t k = 0; k < (uint32_t)b.draws.size(); ++k) {
+            const DrawDesc& d = b.draws[k];
+            const uint64_t n = (uint64_t)d.prims_per_instance * d.instance_count;
+            if (d.fast_vs != f || n == 0) continue;
+            table.push_back(k);
+            table.push_back(groups);
+            groups += (uint32_t)((n + 31) / 32);
+        }
+        if (table.size() / 2 > off[f]) {
+            table.push_back(~0u);
+            table.push_back(groups);
+        }
+    }
+    off[7] = (uint32_t)(table.size() / 2);
+}
+
 // Visibility raster (kind 3): every target has colour and depth, and every draw writes depth
 // with one batch-wide Less / LessEqual / Greater / GreaterEqual, does not blend and runs a
 // fragment stage that never discards.  Returns the compare function, or 0.
@@ -1562,13 +1587,23 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
     const size_t off_desc = align(off_counters + n_targets * kTargetCounters * sizeof(unsigned long long));
     std::vector<size_t> desc_off(nb, 0), states_off(nb, 0);
     std::vector<int> kinds(nb, 0);
+    std::vector<std::vector<uint32_t>> shape_tables(nb);
+    struct SgOff {
+        uint32_t v[8];
+    };
+    std::vector<SgOff> sg_offs(nb);
+    auto shape_table_at = [](const Batch& b) {  // offset of the shape table in the batch's descriptors
+        return (b.draws.size() * (sizeof(DrawDesc) + sizeof(uint32_t)) + b.targets.size() * sizeof(TargetDesc) + 7) &
+               ~size_t(7);
+    };
     size_t cur = off_desc;
     for (size_t i = from; i < nb; ++i) {
         kinds[i] = fragment_kind(batches[i], cfg.raster_order == GBR_RASTER_AUTO);
         desc_off[i] = cur;
-        // descriptors, targets, then the draws' first primitives as one contiguous table
-        cur = align(cur + batches[i].draws.size() * (sizeof(DrawDesc) + sizeof(uint32_t)) +
-                    batches[i].targets.size() * sizeof(TargetDesc));
+        // descriptors, targets, the draws' first primitives as one contiguous table, then the
+        // setup kernels' per-shape group table (8-byte aligned)
+        shape_group_table(batches[i], shape_tables[i], sg_offs[i].v);
+        cur = align(cur + shape_table_at(batches[i]) + shape_tables[i].size() * sizeof(uint32_t));
         if (kinds[i] == 3) {
             states_off[i] = cur;
             cur = align(cur + batches[i].draws.size() * raster_state_bytes());
@@ -1590,6 +1625,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         uint8_t* bases = p + batches[i].draws.size() * sizeof(DrawDesc) + batches[i].targets.size() * sizeof(TargetDesc);
         for (size_t k = 0; k < batches[i].draws.size(); ++k)
             std::memcpy(bases + k * sizeof(uint32_t), &batches[i].draws[k].prim_base, sizeof(uint32_t));
+        if (!shape_tables[i].empty())
+            std::memcpy(p + shape_table_at(batches[i]), shape_tables[i].data(), shape_tables[i].size() * sizeof(uint32_t));
     }
     cuda_check(cudaMemcpyAsync(meta, host_meta.data(), cur, cudaMemcpyHostToDevice, stream), "upload descriptors");
 
@@ -1696,6 +1733,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 bp.abort_flag = reinterpret_cast<uint32_t*>(meta);
                 bp.raster_rule = cfg.raster_rule;
                 bp.fvs_mask = b.jit ? 0u : fvs_mask(b);
+                bp.shape_groups = reinterpret_cast<const uint32_t*>(meta + desc_off[i] + shape_table_at(b));
+                std::memcpy(bp.sg_off, sg_offs[i].v, sizeof bp.sg_off);
                 if (kinds[i] == 3) {
                     bp.states = meta + states_off[i];
                     bp.vis_compare = visibility_compare(b);
@@ -1751,6 +1790,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
                 const size_t nd = batches[i].draws.size(), nt = batches[i].targets.size();
                 put(&nd, sizeof nd);
                 put(&nt, sizeof nt);
+                put(sg_offs[i].v, sizeof sg_offs[i].v);  // the setup launches' shape ranges
+                put(&desc_off[i], sizeof desc_off[i]);
             }
             const void* ptrs[9] = {records_buf.ptr, ovf_buf.ptr, tiles_buf.ptr, bins_buf.ptr, meta_buf.ptr, slow_buf.ptr,
                                    strip_buf.ptr, hint_buf.ptr, split_buf.ptr};
