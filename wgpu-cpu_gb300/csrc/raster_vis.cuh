@@ -150,18 +150,19 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchPara
     // phase 1: the record table of the chunk being rasterised (per thread: record, key, clipped box,
     // exclusive prefix of the row counts) and the warps' partial sums
     __shared__ const TriRecord* s_rec[NT];
-    __shared__ uint32_t s_key[NT], s_excl[NT];
+    // rows of the record: first row, pixel range clipped to tile and scissor, first row in the chunk
     __shared__ int4 s_box[NT];
     // per record of the chunk: barycentric terms (a, b, c, the three shoelace constants, 1/area,
-    // area), vertex depths, the span rule's sorted vertices (or the degenerate row's extent) and
-    // flags (bit 0 area in the fast-division range, bit 1 unclipped, bit 2 degenerate)
-    __shared__ float4 s_b0[NT], s_b1[NT], s_b2[NT];
-    __shared__ float2 s_b3[NT];
+    // area), vertex depths, flags (bit 0 area in the fast-division range, bit 1 unclipped, bit 2
+    // degenerate) and order key; the span rule's sorted vertices (or the degenerate row's extent)
+    __shared__ float4 s_b0[NT], s_b1[NT], s_b2[NT], s_b3[NT];
     __shared__ int4 s_sp0[NT], s_sp1[NT];
-    // a wave of the chunk's rows: (record | row << 8 | first pixel << 16) and the exclusive prefix
-    // of their covered widths (s_pre[WAVE] = the wave's pixels)
-    constexpr int WAVE = 2 * NT;
-    __shared__ uint32_t s_row[WAVE], s_pre[WAVE + 1];
+    // a wave of the chunk's rows: the record of each, (record | row << 8 | first pixel << 16) and
+    // the exclusive prefix of their covered widths; the row of each pixel of a block of PIXB
+    constexpr int WAVE = 2 * NT, PIXB = 8 * NT;
+    __shared__ uint8_t s_rrec[WAVE];
+    __shared__ uint32_t s_row[WAVE], s_pre[WAVE];
+    __shared__ uint16_t s_pix[PIXB];
     __shared__ uint32_t s_wsum[WARPS];
     __shared__ uint32_t s_tile, s_last;
     __shared__ uint2 s_runs;  // fragment-stage runs of the tile, and those that sample a texture
@@ -255,8 +256,8 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchPara
                     s_b0[threadIdx.x] = make_float4(k.ax, k.ay, k.bx, k.by);
                     s_b1[threadIdx.x] = make_float4(k.cx, k.cy, k.kc0, k.kc1);
                     s_b2[threadIdx.x] = make_float4(k.kc2, k.rcp, k.area, r->fz[0]);
-                    s_b3[threadIdx.x] = make_float2(r->fz[1], r->fz[2]);
                     const int fl = (k.area_ok ? 1 : 0) | (k.ident ? 2 : 0) | ((r->flags & (SPAN_DEGENERATE << 2)) ? 4 : 0);
+                    s_b3[threadIdx.x] = make_float4(r->fz[1], r->fz[2], __int_as_float(fl), __uint_as_float(key));
                     if (EDGE || !(fl & 4))
                         s_sp0[threadIdx.x] = make_int4(r->sx[0], r->sy[0], r->sx[1], r->sy[1]);
                     else
@@ -264,36 +265,30 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchPara
                     s_sp1[threadIdx.x] = make_int4(r->sx[2], r->sy[2], fl, 0);
                     s_box[threadIdx.x] = make_int4(y0, xl, xr, 0);
                     s_rec[threadIdx.x] = r;
-                    s_key[threadIdx.x] = key;
                 }
             }
             uint32_t total_rows;
-            s_excl[threadIdx.x] = block_scan(rows, &total_rows);
-            tile_sync<WARPS>();
+            const uint32_t excl = block_scan(rows, &total_rows);  // this record's first row in the chunk
+            if (rows) s_box[threadIdx.x].w = (int)excl;
             for (uint32_t w0 = 0; w0 < total_rows; w0 += WAVE) {
+                // (0) the record of each row of the wave
+                {
+                    const uint32_t q1 = min(excl + rows, w0 + WAVE);
+                    for (uint32_t q = max(excl, w0); q < q1; ++q) s_rrec[q - w0] = (uint8_t)threadIdx.x;
+                }
+                tile_sync<WARPS>();
                 // (a) spans of this thread's rows [q0, q0 + RPT) of the wave
-                const uint32_t q0 = w0 + (uint32_t)threadIdx.x * RPT;
+                const uint32_t q0 = (uint32_t)threadIdx.x * RPT;
                 uint32_t widths = 0;
                 uint32_t ent[RPT], wid[RPT];
-                int j = 0;
-                if (q0 < total_rows) {  // the record of row q0: the last entry whose prefix is <= q0
-#pragma unroll
-                    for (int step = NT / 2; step > 0; step >>= 1)
-                        if (s_excl[j + step] <= q0) j += step;
-                }
-                uint32_t jend = j + 1 < NT ? s_excl[j + 1] : total_rows;
 #pragma unroll
                 for (int k = 0; k < RPT; ++k) {
-                    const uint32_t q = q0 + k;
                     ent[k] = 0;
                     wid[k] = 0;
-                    if (q < total_rows) {
-                        while (q >= jend) {  // the next record with rows
-                            ++j;
-                            jend = j + 1 < NT ? s_excl[j + 1] : total_rows;
-                        }
+                    if (w0 + q0 + k < total_rows) {
+                        const int j = s_rrec[q0 + k];
                         const int4 bx = s_box[j];
-                        const int y = bx.x + (int)(q - s_excl[j]);
+                        const int y = bx.x + (int)(w0 + q0 + k - (uint32_t)bx.w);
                         int x1, x2;
                         if constexpr (EDGE) {
                             span_at<EDGE>(*s_rec[j], y, x1, x2);
@@ -317,54 +312,48 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchPara
                 }
                 uint32_t total_px;
                 uint32_t pre = block_scan(widths, &total_px);
+                uint32_t pre_k[RPT];
 #pragma unroll
                 for (int k = 0; k < RPT; ++k) {
-                    s_row[threadIdx.x * RPT + k] = ent[k];
-                    s_pre[threadIdx.x * RPT + k] = pre;
+                    pre_k[k] = pre;
+                    s_row[q0 + k] = ent[k];
+                    s_pre[q0 + k] = pre;
                     pre += wid[k];
                 }
-                if (threadIdx.x == 0) s_pre[WAVE] = total_px;
-                tile_sync<WARPS>();
-                // (b) this thread's pixels [p, p_end) of the wave's total_px
-                const uint32_t per = (total_px + NT - 1) / NT;
-                uint32_t p = min(total_px, (uint32_t)threadIdx.x * per);
-                const uint32_t p_end = min(total_px, p + per);
-                if (p < p_end) {
-                    int q = 0;  // the row of pixel p: the last row whose prefix is <= p (and has pixels)
+                // (b) the wave's covered pixels in blocks of PIXB: a table gives each pixel its row,
+                // and thread t takes pixels t, t + NT, ... of the block, so the lanes of a warp work
+                // on neighbouring pixels of the same few rows (shared constants, no divergence)
+                for (uint32_t b0 = 0; b0 < total_px; b0 += PIXB) {
 #pragma unroll
-                    for (int step = WAVE / 2; step > 0; step >>= 1)
-                        if (s_pre[q + step] <= p) q += step;
-                    uint32_t qend = s_pre[q + 1];
-                    while (p < p_end) {
-                        while (p >= qend) qend = s_pre[++q + 1];
+                    for (int k = 0; k < RPT; ++k) {
+                        const uint32_t u1 = min(pre_k[k] + wid[k], b0 + PIXB);
+                        for (uint32_t u = max(pre_k[k], b0); u < u1; ++u) s_pix[u - b0] = (uint16_t)(q0 + k);
+                    }
+                    tile_sync<WARPS>();
+                    const uint32_t nb = min((uint32_t)PIXB, total_px - b0);
+                    for (uint32_t i = threadIdx.x; i < nb; i += NT) {
+                        const uint32_t q = s_pix[i];
                         const uint32_t e = s_row[q];
                         const int jj = (int)(e & 0xFFu), y = Y0 + (int)((e >> 8) & 0xFFu);
-                        const int xb = X0 + (int)(e >> 16) - (int)s_pre[q];
-                        const float4 b0 = s_b0[jj], b1 = s_b1[jj], b2 = s_b2[jj];
-                        const float2 b3 = s_b3[jj];
-                        const int fl = s_sp1[jj].z;
+                        const int x = X0 + (int)(e >> 16) + (int)(b0 + i - s_pre[q]);
+                        const float4 b0v = s_b0[jj], b1 = s_b1[jj], b2 = s_b2[jj], b3 = s_b3[jj];
+                        const int fl = __float_as_int(b3.z);
                         BaryK k;
-                        k.ax = b0.x; k.ay = b0.y; k.bx = b0.z; k.by = b0.w;
+                        k.ax = b0v.x; k.ay = b0v.y; k.bx = b0v.z; k.by = b0v.w;
                         k.cx = b1.x; k.cy = b1.y; k.kc0 = b1.z; k.kc1 = b1.w;
                         k.kc2 = b2.x; k.rcp = b2.y; k.area = b2.z;
                         k.area_ok = (fl & 1) != 0;
                         k.ident = (fl & 2) != 0;
-                        const uint32_t rkey = s_key[jj];
-                        const TriRecord* rr = s_rec[jj];
-                        const uint32_t stop = min(p_end, qend);
-                        for (; p < stop; ++p) {
-                            const int x = xb + (int)p;
-                            float cmp[3];
-                            bary_at<EDGE>(*rr, k, x, y, cmp);
-                            ++frag_count;
-                            // fragment.z (raster.rs:345-346) from the staged vertex depths
-                            const float z = fadd(fadd(fmul(b2.w, cmp[0]), fmul(b3.x, cmp[1])), fmul(b3.y, cmp[2]));
-                            if (z != z) continue;
-                            atomicMin(&s_vis[(y - Y0) * T + (x - X0)], vis_key(cmpf, z, rkey));
-                        }
+                        float cmp[3];
+                        bary_at<EDGE>(*s_rec[jj], k, x, y, cmp);
+                        ++frag_count;
+                        // fragment.z (raster.rs:345-346) from the staged vertex depths
+                        const float z = fadd(fadd(fmul(b2.w, cmp[0]), fmul(b3.x, cmp[1])), fmul(b3.y, cmp[2]));
+                        if (z != z) continue;
+                        atomicMin(&s_vis[(y - Y0) * T + (x - X0)], vis_key(cmpf, z, __float_as_uint(b3.w)));
                     }
+                    tile_sync<WARPS>();  // the block's table (and after the last, the wave's rows) is rewritten
                 }
-                tile_sync<WARPS>();  // the wave's rows are rewritten by the next wave
             }
         }
         tile_sync<WARPS>();
