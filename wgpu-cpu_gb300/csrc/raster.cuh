@@ -470,10 +470,16 @@ __device__ __forceinline__ void build_record_frag(const BatchParams& bp, TriReco
             syv[i] = (int)py[i];
         }
     }
-    // bit 4: the clip barycentrics are exactly the unit vectors (an unclipped triangle)
-    if (v[0].b[0] == 1.0f && v[0].b[1] == 0.0f && v[0].b[2] == 0.0f && v[1].b[0] == 0.0f && v[1].b[1] == 1.0f &&
-        v[1].b[2] == 0.0f && v[2].b[0] == 0.0f && v[2].b[1] == 0.0f && v[2].b[2] == 1.0f)
-        flags |= 16u;
+    // bit 4: the clip barycentrics are exactly the unit vectors, bit for bit (+0, no -0: an
+    // unclipped triangle)
+    {
+        bool ident = true;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) ident = ident && __float_as_uint(v[i].b[j]) == (i == j ? 0x3F800000u : 0u);
+        if (ident) flags |= 16u;
+    }
     auto fb = [](float x) { return __float_as_uint(x); };
     auto ib = [](int x) { return (uint32_t)x; };
     uint4* h = reinterpret_cast<uint4*>(r);

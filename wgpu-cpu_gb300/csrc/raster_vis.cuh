@@ -58,9 +58,11 @@ __device__ __forceinline__ void bary_consts(const TriRecord& r, BaryK& k) {
 }
 
 // Barycentrics at the integer pixel corner (the edge-function rule: the pixel centre) composed
-// with the clip barycentrics (raster.rs:313-321, 334-343), as in k_raster.
-template <bool EDGE>
-__device__ __forceinline__ void bary_at(const TriRecord& r, const BaryK& k, int x, int y, float cmp[3]) {
+// with the clip barycentrics (raster.rs:313-321, 334-343), as in k_raster.  get_cb() returns the
+// record's clip barycentrics; it is called only for a clipped record (k.ident false), an
+// unclipped one composes with the unit vectors it holds.
+template <bool EDGE, class GetCb>
+__device__ __forceinline__ void bary_eval(const BaryK& k, int x, int y, float cmp[3], GetCb get_cb) {
     // an IEEE sum does not depend on operand order: x + a.x serves both terms containing it
     // The operations of the scalar formulas, sums and differences two lanes per packed f32x2
     // instruction (exact per lane; products scalar, see f2mul_rn); a - b is a + (-b).
@@ -91,16 +93,29 @@ __device__ __forceinline__ void bary_at(const TriRecord& r, const BaryK& k, int 
             cmp[2] = l02.y;
             return;
         }
+        const float* cb = get_cb();
 #pragma unroll
         for (int j = 0; j < 3; ++j)
-            cmp[j] = fadd(fadd(fmul(r.cb[j], l02.x), fmul(r.cb[3 + j], l1)), fmul(r.cb[6 + j], l02.y));
+            cmp[j] = fadd(fadd(fmul(cb[j], l02.x), fmul(cb[3 + j], l1)), fmul(cb[6 + j], l02.y));
         return;
     }
     const float l0 = div_by_recip(s02.x, k.area, k.rcp, k.area_ok);
     const float l1 = div_by_recip(s1, k.area, k.rcp, k.area_ok);
     const float l2 = div_by_recip(s02.y, k.area, k.rcp, k.area_ok);
+    if (k.ident) {  // the same operations with the unit vectors (a non-finite l makes 0 * l a NaN)
 #pragma unroll
-    for (int j = 0; j < 3; ++j) cmp[j] = fadd(fadd(fmul(r.cb[j], l0), fmul(r.cb[3 + j], l1)), fmul(r.cb[6 + j], l2));
+        for (int j = 0; j < 3; ++j)
+            cmp[j] = fadd(fadd(fmul(j == 0 ? 1.0f : 0.0f, l0), fmul(j == 1 ? 1.0f : 0.0f, l1)),
+                          fmul(j == 2 ? 1.0f : 0.0f, l2));
+        return;
+    }
+    const float* cb = get_cb();
+#pragma unroll
+    for (int j = 0; j < 3; ++j) cmp[j] = fadd(fadd(fmul(cb[j], l0), fmul(cb[3 + j], l1)), fmul(cb[6 + j], l2));
+}
+template <bool EDGE>
+__device__ __forceinline__ void bary_at(const TriRecord& r, const BaryK& k, int x, int y, float cmp[3]) {
+    bary_eval<EDGE>(k, x, y, cmp, [&] { return r.cb; });
 }
 
 __device__ __forceinline__ float frag_z(const TriRecord& r, const float cmp[3]) {  // raster.rs:345-346
@@ -149,14 +164,15 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchPara
     __shared__ float s_lut[256];
     // phase 1: the record table of the chunk being rasterised (per thread: record, key, clipped box,
     // exclusive prefix of the row counts) and the warps' partial sums
-    __shared__ const TriRecord* s_rec[NT];
     // rows of the record: first row, pixel range clipped to tile and scissor, first row in the chunk
     __shared__ int4 s_box[NT];
     // per record of the chunk: barycentric terms (a, b, c, the three shoelace constants, 1/area,
-    // area), vertex depths, flags (bit 0 area in the fast-division range, bit 1 unclipped, bit 2
-    // degenerate) and order key; the span rule's sorted vertices (or the degenerate row's extent)
+    // area), vertex depths, flags (bit 0 area in the fast-division range, bit 1 unclipped) and
+    // order key; the span rule's sorted vertices (the degenerate row's extent and -1 instead of
+    // the first two when all three lie on one row)
     __shared__ float4 s_b0[NT], s_b1[NT], s_b2[NT], s_b3[NT];
-    __shared__ int4 s_sp0[NT], s_sp1[NT];
+    __shared__ int4 s_sp0[NT];
+    __shared__ int2 s_sp1[NT];
     // a wave of the chunk's rows: the record of each, (record | row << 8 | first pixel << 16) and
     // the exclusive prefix of their covered widths; the row of each pixel of a block of PIXB
     constexpr int WAVE = 2 * NT, PIXB = 8 * NT;
@@ -256,15 +272,16 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchPara
                     s_b0[threadIdx.x] = make_float4(k.ax, k.ay, k.bx, k.by);
                     s_b1[threadIdx.x] = make_float4(k.cx, k.cy, k.kc0, k.kc1);
                     s_b2[threadIdx.x] = make_float4(k.kc2, k.rcp, k.area, r->fz[0]);
-                    const int fl = (k.area_ok ? 1 : 0) | (k.ident ? 2 : 0) | ((r->flags & (SPAN_DEGENERATE << 2)) ? 4 : 0);
+                    const int fl = (k.area_ok ? 1 : 0) | (k.ident ? 2 : 0);
                     s_b3[threadIdx.x] = make_float4(r->fz[1], r->fz[2], __int_as_float(fl), __uint_as_float(key));
-                    if (EDGE || !(fl & 4))
-                        s_sp0[threadIdx.x] = make_int4(r->sx[0], r->sy[0], r->sx[1], r->sy[1]);
-                    else
-                        s_sp0[threadIdx.x] = make_int4(r->xmin, r->xmax, 0, 0);
-                    s_sp1[threadIdx.x] = make_int4(r->sx[2], r->sy[2], fl, 0);
+                    if (!EDGE) {  // the span rule's rows (the framebuffer coordinates are >= 0)
+                        if (r->flags & (SPAN_DEGENERATE << 2))
+                            s_sp0[threadIdx.x] = make_int4(r->xmin, r->xmax, -1, -1);
+                        else
+                            s_sp0[threadIdx.x] = make_int4(r->sx[0], r->sy[0], r->sx[1], r->sy[1]);
+                        s_sp1[threadIdx.x] = make_int2(r->sx[2], r->sy[2]);
+                    }
                     s_box[threadIdx.x] = make_int4(y0, xl, xr, 0);
-                    s_rec[threadIdx.x] = r;
                 }
             }
             uint32_t total_rows;
@@ -291,13 +308,14 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchPara
                         const int y = bx.x + (int)(w0 + q0 + k - (uint32_t)bx.w);
                         int x1, x2;
                         if constexpr (EDGE) {
-                            span_at<EDGE>(*s_rec[j], y, x1, x2);
+                            span_at<EDGE>(*record_of(bp, __float_as_uint(s_b3[j].w)), y, x1, x2);
                         } else {
-                            const int4 sp0 = s_sp0[j], sp1 = s_sp1[j];
-                            if (sp1.z & 4) {
+                            const int4 sp0 = s_sp0[j];
+                            if (sp0.w < 0) {
                                 x1 = sp0.x;
                                 x2 = sp0.y;
                             } else {
+                                const int2 sp1 = s_sp1[j];
                                 span_rows(sp0.x, sp0.y, sp0.z, sp0.w, sp1.x, sp1.y, y, x1, x2);
                             }
                         }
@@ -345,12 +363,13 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchPara
                         k.area_ok = (fl & 1) != 0;
                         k.ident = (fl & 2) != 0;
                         float cmp[3];
-                        bary_at<EDGE>(*s_rec[jj], k, x, y, cmp);
+                        const uint32_t rkey = __float_as_uint(b3.w);
+                        bary_eval<EDGE>(k, x, y, cmp, [&] { return record_of(bp, rkey)->cb; });
                         ++frag_count;
                         // fragment.z (raster.rs:345-346) from the staged vertex depths
                         const float z = fadd(fadd(fmul(b2.w, cmp[0]), fmul(b3.x, cmp[1])), fmul(b3.y, cmp[2]));
                         if (z != z) continue;
-                        atomicMin(&s_vis[(y - Y0) * T + (x - X0)], vis_key(cmpf, z, __float_as_uint(b3.w)));
+                        atomicMin(&s_vis[(y - Y0) * T + (x - X0)], vis_key(cmpf, z, rkey));
                     }
                     tile_sync<WARPS>();  // the block's table (and after the last, the wave's rows) is rewritten
                 }
