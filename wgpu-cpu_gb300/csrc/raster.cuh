@@ -281,11 +281,25 @@ __device__ __forceinline__ void record_rows(const TriRecord& r, const DrawDesc& 
     hi = min(r.row1, min((int)d.sc_y1 - 1, (int)t.height - 1));
 }
 
+// Tiles of the record's unclipped bounding box (an upper bound of the tiles it emits into).
+__device__ __forceinline__ uint32_t bbox_tiles(const TriRecord& r, uint32_t shift) {
+    return (uint32_t)((r.row1 >> shift) - (r.row0 >> shift) + 1) * (uint32_t)((r.xmax >> shift) - (r.xmin >> shift) + 1);
+}
+
 // The tile columns [c0, c1] of tile row ty (within rows [lo, hi]) the record can emit into: the
 // spans at the row band's ends and around the middle vertex bound the band's pixels (c0 > c1: none).
+// A record whose bounding box spans at most four tiles takes the box's columns instead, without
+// evaluating spans: binning it into a tile it misses costs the raster one empty visit, and every
+// walker (counting and filling alike) goes through here, so the tile set stays the same.
 template <bool EDGE>
 __device__ __forceinline__ void tile_row_cols(const TriRecord& r, const DrawDesc& d, const TargetDesc& t, uint32_t shift,
                                               int lo, int hi, int ty, int& c0, int& c1) {
+    if (bbox_tiles(r, shift) <= 4u) {
+        const int mn = max(r.xmin, (int)d.sc_x0), mx = min(r.xmax, min((int)d.sc_x1 - 1, (int)t.width - 1));
+        c0 = mn > mx ? 1 : mn >> shift;
+        c1 = mn > mx ? 0 : mx >> shift;
+        return;
+    }
     const int T = 1 << shift;
     const int y0 = max(lo, ty << shift), y1 = min(hi, (ty << shift) + T - 1);
     int xa, xb, mn, mx;
@@ -383,6 +397,9 @@ static_assert(offsetof(TriRecord, row0) == 16 && offsetof(TriRecord, sx) == 32 &
                   offsetof(TriRecord, inv_w0) == 144 && offsetof(TriRecord, ovf) == 156 &&
                   offsetof(TriRecord, nsub) == 160 && offsetof(TriRecord, lod) == 164 && sizeof(TriRecord) == 176,
               "TriRecord layout assumed by build_record_frag");
+static_assert(offsetof(DrawDesc, sc_x0) % 8 == 0 && offsetof(DrawDesc, sc_y1) == offsetof(DrawDesc, sc_x0) + 12 &&
+                  sizeof(DrawDesc) % 16 == 0,
+              "DrawDesc scissor read as two 8-byte words by k_raster_vis");
 #endif
 
 // Writes a complete record (nsub = 1, ovf = 0; callers that emit more sub-triangles overwrite
@@ -563,11 +580,6 @@ __device__ __forceinline__ void count_tiles(const BatchParams& bp, const TriReco
 __device__ __forceinline__ bool tiles_are_many(const TriRecord& r, uint32_t shift) {
     return (r.row1 >> shift) - (r.row0 >> shift) >= 2;
 }
-// Tiles of the record's unclipped bounding box (an upper bound of the tiles it emits into).
-__device__ __forceinline__ uint32_t bbox_tiles(const TriRecord& r, uint32_t shift) {
-    return (uint32_t)((r.row1 >> shift) - (r.row0 >> shift) + 1) * (uint32_t)((r.xmax >> shift) - (r.xmin >> shift) + 1);
-}
-
 // Binning hint of a primary record, written by the fast setup so that k_fill need not read the
 // record back: the record covers nothing, exactly one tile (its global index), or anything else.
 enum : uint32_t { TILE_HINT_EMPTY = 0xFFFFFFFEu, TILE_HINT_WALK = 0xFFFFFFFFu };

@@ -57,6 +57,20 @@ __device__ __forceinline__ void bary_consts(const TriRecord& r, BaryK& k) {
     k.ident = (r.flags & 16u) != 0;
 }
 
+// bary_consts from the record's header words 0, 3, 4 and 5 (16-byte loads: flags, viewport
+// vertices, area).
+__device__ __forceinline__ void bary_consts_words(uint4 h0, uint4 h3, uint4 h4, uint4 h5, BaryK& k) {
+    k.ax = __uint_as_float(h3.z); k.bx = __uint_as_float(h3.w); k.cx = __uint_as_float(h4.x);
+    k.ay = __uint_as_float(h4.y); k.by = __uint_as_float(h4.z); k.cy = __uint_as_float(h4.w);
+    k.kc0 = fmul(fsub(k.cy, k.by), fadd(k.cx, k.bx));
+    k.kc1 = fmul(fsub(k.ay, k.cy), fadd(k.ax, k.cx));
+    k.kc2 = fmul(fsub(k.by, k.ay), fadd(k.bx, k.ax));
+    k.area = __uint_as_float(h5.x);
+    k.rcp = __frcp_rn(k.area);
+    k.area_ok = div_fast_ok(k.area);
+    k.ident = (h0.w & 16u) != 0;
+}
+
 // Barycentrics at the integer pixel corner (the edge-function rule: the pixel centre) composed
 // with the clip barycentrics (raster.rs:313-321, 334-343), as in k_raster.  get_cb() returns the
 // record's clip barycentrics; it is called only for a clipped record (k.ident false), an
@@ -259,27 +273,33 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchPara
             uint32_t rows = 0;
             if (i < r_end) {
                 const uint32_t key = bp.bins[off + i];
-                const TriRecord* r = record_of(bp, key);
-                const DrawDesc& d = bp.draws[r->draw];
-                const int y0 = max(max(r->row0, Y0), (int)d.sc_y0);
-                const int y1 = min(min(r->row1, YE), (int)d.sc_y1 - 1);
-                const int xl = max(max(r->xmin, X0), (int)d.sc_x0);
-                const int xr = min(min(r->xmax, XE), (int)d.sc_x1 - 1);
+                // the record's first 96 bytes (order, draw, flags, rows, sorted vertices, viewport
+                // vertices, area, vertex depths) as six 16-byte loads, the draw's scissor as two
+                const uint4* rv = reinterpret_cast<const uint4*>(record_of(bp, key));
+                const uint4 h0 = __ldg(rv), h1 = __ldg(rv + 1), h2 = __ldg(rv + 2), h3 = __ldg(rv + 3),
+                            h4 = __ldg(rv + 4), h5 = __ldg(rv + 5);
+                const uint2* sc = reinterpret_cast<const uint2*>(&bp.draws[h0.y].sc_x0);
+                const uint2 sc0 = __ldg(sc), sc1 = __ldg(sc + 1);  // (x0, y0), (x1, y1)
+                const int y0 = max(max((int)h1.x, Y0), (int)sc0.y);
+                const int y1 = min(min((int)h1.y, YE), (int)sc1.y - 1);
+                const int xl = max(max((int)h1.z, X0), (int)sc0.x);
+                const int xr = min(min((int)h1.w, XE), (int)sc1.x - 1);
                 if (y1 >= y0 && xr >= xl) {
                     rows = (uint32_t)(y1 - y0 + 1);
                     BaryK k;
-                    bary_consts(*r, k);
+                    bary_consts_words(h0, h3, h4, h5, k);
                     s_b0[threadIdx.x] = make_float4(k.ax, k.ay, k.bx, k.by);
                     s_b1[threadIdx.x] = make_float4(k.cx, k.cy, k.kc0, k.kc1);
-                    s_b2[threadIdx.x] = make_float4(k.kc2, k.rcp, k.area, r->fz[0]);
+                    s_b2[threadIdx.x] = make_float4(k.kc2, k.rcp, k.area, __uint_as_float(h5.y));
                     const int fl = (k.area_ok ? 1 : 0) | (k.ident ? 2 : 0);
-                    s_b3[threadIdx.x] = make_float4(r->fz[1], r->fz[2], __int_as_float(fl), __uint_as_float(key));
+                    s_b3[threadIdx.x] = make_float4(__uint_as_float(h5.z), __uint_as_float(h5.w), __int_as_float(fl),
+                                                    __uint_as_float(key));
                     if (!EDGE) {  // the span rule's rows (the framebuffer coordinates are >= 0)
-                        if (r->flags & (SPAN_DEGENERATE << 2))
-                            s_sp0[threadIdx.x] = make_int4(r->xmin, r->xmax, -1, -1);
+                        if (h0.w & (SPAN_DEGENERATE << 2))
+                            s_sp0[threadIdx.x] = make_int4((int)h1.z, (int)h1.w, -1, -1);
                         else
-                            s_sp0[threadIdx.x] = make_int4(r->sx[0], r->sy[0], r->sx[1], r->sy[1]);
-                        s_sp1[threadIdx.x] = make_int2(r->sx[2], r->sy[2]);
+                            s_sp0[threadIdx.x] = make_int4((int)h2.x, (int)h2.w, (int)h2.y, (int)h3.x);
+                        s_sp1[threadIdx.x] = make_int2((int)h2.z, (int)h3.y);
                     }
                     s_box[threadIdx.x] = make_int4(y0, xl, xr, 0);
                 }
@@ -433,13 +453,17 @@ __global__ void __launch_bounds__(WARPS * 32, 32 / WARPS) k_raster_vis(BatchPara
             bool write_depth = tg.depth_load == 1;
             if (key != kNone) {
                 const TriRecord& r = *record_of(bp, vis_order(cmpf, key));
+                const uint4* rv4 = reinterpret_cast<const uint4*>(&r);
+                const uint4 h0 = __ldg(rv4), h3 = __ldg(rv4 + 3), h4 = __ldg(rv4 + 4), h5 = __ldg(rv4 + 5);
                 BaryK k;
-                bary_consts(r, k);
+                bary_consts_words(h0, h3, h4, h5, k);
                 float cmp[3];
                 bary_at<EDGE>(r, k, x, y, cmp);
-                const float z = frag_z(r, cmp);
+                // fragment.z (raster.rs:345-346)
+                const float z = fadd(fadd(fmul(__uint_as_float(h5.y), cmp[0]), fmul(__uint_as_float(h5.z), cmp[1])),
+                                     fmul(__uint_as_float(h5.w), cmp[2]));
                 if (depth_compare(cmpf, z, depth)) {
-                    const RasterState& rs = states[r.draw];
+                    const RasterState& rs = states[h0.y];
                     const uint32_t nvar = rs.nvar;
                     const float* rv = rec_var(&r);
                     float var[MAX_VARYING_FLOATS];
