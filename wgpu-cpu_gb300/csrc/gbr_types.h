@@ -171,6 +171,11 @@ struct DrawDesc {
     uint32_t fast_vcount;    // fast setup: every vertex index below this fetches its FastVs attributes in range
     uint32_t flat_mask;      // bit k: inter-stage float k is @interpolate(flat) (vertex 0's value, bits kept)
     uint32_t early_depth;    // EarlyDepth of the fragment entry point
+    // fast setup of FAST_VS_MVP_COLOR / FAST_VS_MVP_TEX: 1 when the shape's attributes are one
+    // per-vertex buffer's whole vertex, packed from offset 0 (stride 24 / 32) in an 8- / 16-byte
+    // aligned buffer, so each vertex is read with 8- / 16-byte loads
+    uint32_t fast_packed;
+    uint32_t _pad_setup[3];
 };
 
 // Vertex stages the fast setup kernel specialises on: every input an f32 attribute of exactly

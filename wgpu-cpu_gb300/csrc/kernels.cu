@@ -182,6 +182,16 @@ uint32_t fast_vs_kind(const DrawDesc& d) {
     }
 }
 
+uint32_t fast_vs_packed(const DrawDesc& d) {
+    if (d.fast_vs != FAST_VS_MVP_COLOR && d.fast_vs != FAST_VS_MVP_TEX) return 0;
+    const bool tex = d.fast_vs == FAST_VS_MVP_TEX;
+    const int b = d.attr[0].buffer;
+    if (b < 0 || d.attr[0].offset != 0 || d.attr[1].buffer != b || d.attr[1].offset != 12) return 0;
+    if (tex && (d.attr[2].buffer != b || d.attr[2].offset != 24)) return 0;
+    if (d.vb_stride_vertex[b] != (tex ? 32u : 24u) || d.vb_stride_instance[b] != 0) return 0;
+    return reinterpret_cast<uintptr_t>(d.vb_data[b]) % (tex ? 16u : 8u) == 0 ? 1u : 0u;
+}
+
 uint32_t fast_vs_vcount(const DrawDesc& d) {
     // (location, bytes) of the attributes each FastVs shape fetches, as fast_vertex_in_range
     struct Use { int loc; uint32_t bytes; };
@@ -348,6 +358,7 @@ extern "C" GBR_API gbr_status gbr_render_triangles_noalloc(const float* clip_pos
     d.write_mask = 0xF;
     d.fast_vs = fast_vs_kind(d);
     d.fast_vcount = fast_vs_vcount(d);
+    d.fast_packed = fast_vs_packed(d);
     TargetDesc t;
     std::memset(&t, 0, sizeof t);
     t.color = color_target;

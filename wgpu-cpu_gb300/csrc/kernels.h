@@ -35,6 +35,8 @@ uint32_t fast_vs_kind(const DrawDesc& d);
 // Vertex indices below the result fetch every attribute of the draw's FastVs shape in range, for
 // every instance of the draw (0 when none does, or no shape applies).
 uint32_t fast_vs_vcount(const DrawDesc& d);
+// 1 when the fast setup can read each vertex of the draw with 8- or 16-byte loads (DrawDesc::fast_packed).
+uint32_t fast_vs_packed(const DrawDesc& d);
 
 // Places n coalesced writes: segment k copies desc[3k + 2] bytes from stage + desc[3k + 1] to the
 // device address desc[3k] (stage offsets are 16-byte aligned).

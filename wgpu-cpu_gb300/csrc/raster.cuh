@@ -288,13 +288,13 @@ __device__ __forceinline__ uint32_t bbox_tiles(const TriRecord& r, uint32_t shif
 
 // The tile columns [c0, c1] of tile row ty (within rows [lo, hi]) the record can emit into: the
 // spans at the row band's ends and around the middle vertex bound the band's pixels (c0 > c1: none).
-// A record whose bounding box spans at most four tiles takes the box's columns instead, without
+// A record whose bounding box spans at most eight tiles takes the box's columns instead, without
 // evaluating spans: binning it into a tile it misses costs the raster one empty visit, and every
 // walker (counting and filling alike) goes through here, so the tile set stays the same.
 template <bool EDGE>
 __device__ __forceinline__ void tile_row_cols(const TriRecord& r, const DrawDesc& d, const TargetDesc& t, uint32_t shift,
                                               int lo, int hi, int ty, int& c0, int& c1) {
-    if (bbox_tiles(r, shift) <= 4u) {
+    if (bbox_tiles(r, shift) <= 8u) {
         const int mn = max(r.xmin, (int)d.sc_x0), mx = min(r.xmax, min((int)d.sc_x1 - 1, (int)t.width - 1));
         c0 = mn > mx ? 1 : mn >> shift;
         c1 = mn > mx ? 0 : mx >> shift;
@@ -953,10 +953,25 @@ __device__ __forceinline__ void fast_vertex(const DrawDesc& d, const float* mvp,
                                             V4& pos, float* var) {
     float a0[4], a1[4], a2[2];
     if constexpr (FVS == FAST_VS_MVP_COLOR || FVS == FAST_VS_MVP_TEX) {
-        fetch_f32_unchecked<3>(d, 0, vertex, instance, a0);
-        fetch_f32_unchecked<3>(d, 1, vertex, instance, a1);
+        if (d.fast_packed) {  // the whole vertex: two 16-byte (textured) or three 8-byte loads
+            const uint8_t* vp = d.vb_data[d.attr[0].buffer] + (uint64_t)vertex * (FVS == FAST_VS_MVP_TEX ? 32u : 24u);
+            if constexpr (FVS == FAST_VS_MVP_TEX) {
+                const uint4 w0 = __ldg(reinterpret_cast<const uint4*>(vp)), w1 = __ldg(reinterpret_cast<const uint4*>(vp) + 1);
+                a0[0] = __uint_as_float(w0.x); a0[1] = __uint_as_float(w0.y); a0[2] = __uint_as_float(w0.z);
+                a1[0] = __uint_as_float(w0.w); a1[1] = __uint_as_float(w1.x); a1[2] = __uint_as_float(w1.y);
+                a2[0] = __uint_as_float(w1.z); a2[1] = __uint_as_float(w1.w);
+            } else {
+                const uint2* q = reinterpret_cast<const uint2*>(vp);
+                const uint2 w0 = __ldg(q), w1 = __ldg(q + 1), w2 = __ldg(q + 2);
+                a0[0] = __uint_as_float(w0.x); a0[1] = __uint_as_float(w0.y); a0[2] = __uint_as_float(w1.x);
+                a1[0] = __uint_as_float(w1.y); a1[1] = __uint_as_float(w2.x); a1[2] = __uint_as_float(w2.y);
+            }
+        } else {
+            fetch_f32_unchecked<3>(d, 0, vertex, instance, a0);
+            fetch_f32_unchecked<3>(d, 1, vertex, instance, a1);
+            if constexpr (FVS == FAST_VS_MVP_TEX) fetch_f32_unchecked<2>(d, 2, vertex, instance, a2);
+        }
         if constexpr (FVS == FAST_VS_MVP_TEX) {
-            fetch_f32_unchecked<2>(d, 2, vertex, instance, a2);
             var[3] = a2[0];
             var[4] = a2[1];
         }

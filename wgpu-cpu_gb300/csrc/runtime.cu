@@ -908,6 +908,7 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
     for (int k = 0; k < 4; ++k) d.blend_constant[k] = (float)dc.blend_constant[k];
     d.fast_vs = fast_vs_kind(d);
     d.fast_vcount = fast_vs_vcount(d);
+    d.fast_packed = fast_vs_packed(d);
     return d;
 }
 
