@@ -901,6 +901,24 @@ struct alignas(16) DrawCache {
 
 constexpr int kSetupWarps = 4;
 
+// Bulk copies shared -> global (the copy engine behind cp.async.bulk): both addresses 16-byte
+// aligned, the size a multiple of 16.  The issuing thread commits each copy as its own bulk group
+// and waits for its groups itself.
+__device__ __forceinline__ void bulk_store_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
+    const uint32_t s = (uint32_t)__cvta_generic_to_shared(ssrc);
+    asm volatile(
+        "cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;\n\t"
+        "cp.async.bulk.commit_group;" ::"l"(gdst),
+        "r"(s), "r"(bytes)
+        : "memory");
+}
+// the issuing thread's bulk copies have read their shared-memory source
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// the issuing thread's bulk copies are complete
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+// orders this thread's shared-memory writes before later bulk copies that read them
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
 // Shared memory of k_setup beyond its static part: each warp stages its 32 primary records.
 __host__ __device__ __forceinline__ size_t setup_stage_bytes(uint32_t record_stride) {
     return (size_t)kSetupWarps * 32 * record_stride;
@@ -1186,6 +1204,9 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
     // batch; uniform: the warp's live lanes share draw di, which is in the cache)
     auto setup_group = [&](uint32_t base, uint32_t nrec, bool live, bool uniform, uint32_t di) {
         const uint32_t gp = base + lane;
+        // the previous group's bulk copy has read the stage before its records are overwritten
+        if (lane == 0) bulk_wait_read();
+        __syncwarp();
         TriRecord* rec = reinterpret_cast<TriRecord*>(stage + (size_t)lane * rstride);
         const TriRecord* coop = nullptr;
         bool done = false;
@@ -1230,13 +1251,11 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
             if (live && !done) bp.slow_prims[at + __popc(m & ((1u << lane) - 1u))] = gp;
         }
         coop_tiles<EDGE>(bp, coop, lane, [&](uint32_t tile, uint32_t) { atomicAdd(&bp.tile_count[tile], 1u); });
-        // the warp's records, staged above, out as one block
+        // the warp's records, staged above, out as one block by the bulk-copy engine (16-byte
+        // aligned: the record stride is a multiple of 16)
+        fence_proxy_async_smem();
         __syncwarp();
-        const uint32_t words = nrec * (rstride / 16);
-        uint4* gdst = reinterpret_cast<uint4*>(bp.records + (size_t)base * rstride);
-        const uint4* ssrc = reinterpret_cast<const uint4*>(stage);
-        for (uint32_t k = lane; k < words; k += 32) gdst[k] = ssrc[k];
-        __syncwarp();
+        if (lane == 0) bulk_store_s2g(bp.records + (size_t)base * rstride, stage, nrec * rstride);
     };
 
     if constexpr (ONLY >= 0) {
@@ -1285,6 +1304,7 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
             setup_group(base, min(32u, bp.total_prims - base), live, uniform, di);
         }
     }
+    if (lane == 0) bulk_wait_all();  // the last copy is done before the CTA (and its stage) ends
 }
 
 // Single-CTA exclusive scan of tile counts -> tile_offset; zeroes tile_cursor.
