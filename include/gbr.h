@@ -552,6 +552,15 @@ GBR_API gbr_status gbr_texture_read(gbr_device device, gbr_texture texture, uint
  * destinations (cudaHostAlloc / cudaHostRegister) move at full DMA speed. */
 GBR_API gbr_status gbr_textures_read(gbr_device device, uint32_t count, const gbr_texture* textures,
                                      const uint32_t* mip_levels, void* const* dsts, const uint64_t* sizes);
+/* CommandEncoder::copy_texture_to_buffer + BufferSlice::map_async (buffer.rs:112-136) for
+ * `count` textures, without blocking: validates like gbr_textures_read, enqueues the readback
+ * behind every earlier queue operation and returns.  The readback takes the next submission
+ * index (*out_index): the destinations hold the bytes once gbr_device_poll(device, 1, 1,
+ * *out_index, ...) has returned GBR_OK, and the caller keeps them valid, and does not read them,
+ * until then.  A frame loop can so enqueue frame k + 1 while frame k's readback runs. */
+GBR_API gbr_status gbr_queue_read_textures(gbr_device device, uint32_t count, const gbr_texture* textures,
+                                           const uint32_t* mip_levels, void* const* dsts, const uint64_t* sizes,
+                                           uint64_t* out_index);
 
 /* DeviceInterface::create_sampler (device.rs:185-187 -> sampler.rs:4-29). */
 GBR_API gbr_status gbr_sampler_create(gbr_device device, const gbr_sampler_desc* desc, gbr_sampler* out_sampler);
@@ -635,8 +644,9 @@ GBR_API gbr_status gbr_device_flush_caches(gbr_device device);
  * raster kernels' division by a precomputed reciprocal (exact.cuh, div_by_recip) on the current
  * CUDA device and counts results whose bits differ from CUDA's __fdiv_rn.  The same samples go
  * through the packed f32x2 helpers (f2add, f2mul, f2fma, and a packed product feeding a packed
- * sum), which must give the bits of the scalar __fadd_rn / __fmul_rn / __fmaf_rn.
- * `first_mismatch` receives (a, b) of the first difference found, if any. */
+ * sum), which must give the bits of the scalar __fadd_rn / __fmul_rn / __fmaf_rn, and seeded
+ * integer pairs through the span rule's truncating division (div_trunc_span), which must equal
+ * exact integer division.  `first_mismatch` receives (a, b) of the first difference found, if any. */
 GBR_API gbr_status gbr_selftest_division(uint64_t samples, uint64_t seed, uint64_t* out_mismatches,
                                          float* first_mismatch);
 

@@ -314,7 +314,9 @@ def test_discard_program(gpu, orc):
 
 def test_division_by_reciprocal_matches_cuda(gpu):
     """The raster kernels divide by a per-record reciprocal with Markstein's correction steps;
-    every quotient must carry exactly the bits of CUDA's correctly rounded __fdiv_rn."""
+    every quotient must carry exactly the bits of CUDA's correctly rounded __fdiv_rn.  The same
+    samples check the packed f32x2 helpers and the span rule's binary32 integer division
+    (div_trunc_span) against exact integer division."""
     import ctypes
 
     fn = gpu.lib.cdll.gbr_selftest_division

@@ -72,6 +72,21 @@ __device__ __forceinline__ int64_t div_trunc(int64_t n, int64_t d) {
     return n / d;
 }
 
+// div_trunc with a binary32 fast path for |n|, d < 2^22 (every span of a target up to 2048
+// pixels a side): q0 = trunc(n * RN(1/d)) has relative error below 2^-22.4 against n / d, so
+// |q0 - trunc(n / d)| <= 1, and the exact remainder n - q0 d (|.| < 2^24) says which way to step.
+__device__ __forceinline__ int64_t div_trunc_span(int64_t n, int64_t d) {
+    if (n > -4194304ll && n < 4194304ll && d < 4194304ll) {
+        const int32_t ni = (int32_t)n, di = (int32_t)d;
+        int32_t q = __float2int_rz(__fmul_rn((float)ni, __frcp_rn((float)di)));
+        const int32_t r = ni - q * di;
+        if (ni >= 0) q += r < 0 ? -1 : (r >= di ? 1 : 0);
+        else q += r > 0 ? 1 : (r <= -di ? -1 : 0);
+        return q;
+    }
+    return div_trunc(n, d);
+}
+
 // a / b correctly rounded (round to nearest even), given y = RN(1/b) from __frcp_rn.
 //
 // Method: P. Markstein, "Computation of elementary functions on the IBM RISC System/6000

@@ -245,6 +245,9 @@ struct BatchStatus {
 // and the last chunk to finish merges them and shades the tile.
 constexpr uint32_t VIS_SPLIT_CHUNK = 2048;
 
+// Bits of the global tile index in a setup binning hint (BatchParams::tile_hint).
+constexpr uint32_t TILE_HINT_TILE_BITS = 26;
+
 struct BatchParams {
     const DrawDesc* draws;
     const TargetDesc* targets;

@@ -124,7 +124,15 @@ __global__ void k_selftest_division(uint64_t n, uint64_t seed, unsigned long lon
         auto bits_eq = [](float u, float v) { return __float_as_uint(u) == __float_as_uint(v) || (u != u && v != v); };
         const bool packed_same = bits_eq(pm.x, sm[0]) && bits_eq(pm.y, sm[1]) && bits_eq(ps.x, ss[0]) &&
                                  bits_eq(ps.y, ss[1]) && bits_eq(pf.x, sf[0]) && bits_eq(pf.y, sf[1]);
-        const bool same = bits_eq(q, ref) && bits_eq(y, one_over) && packed_same;
+        // the span rule's integer division: div_trunc_span against exact integer division, for
+        // |n|, d < 2^22 (its fast path) and beyond, with exact multiples of d and their neighbours
+        const int64_t dd = ((int64_t)((r1 >> 20) & 0x3FFFFF) >> ((r0 >> 59) % 22u)) + 1;
+        int64_t nn = (int64_t)((r0 >> 10) & 0x7FFFFF) - 0x3FFFFF;
+        if ((i & 7u) == 0) nn = (nn / dd) * dd + (int64_t)(r1 & 3u) - 1;
+        if ((i & 63u) == 1) nn *= 1 + (int64_t)(r1 & 1023u);  // past the fast path's range
+        const int64_t exact = nn >= INT32_MIN && nn <= INT32_MAX ? (int64_t)((int32_t)nn / (int32_t)dd) : nn / dd;
+        const bool int_same = div_trunc_span(nn, dd) == exact;
+        const bool same = bits_eq(q, ref) && bits_eq(y, one_over) && packed_same && int_same;
         if (!same && atomicAdd(mismatches, 1ull) == 0ull) {
             first[0] = a;
             first[1] = b;

@@ -253,10 +253,10 @@ __device__ __forceinline__ void span_edge(const TriRecord& r, int y, int& x1, in
 // The scanline rule's span of row y for the framebuffer vertices a, b, c sorted by y.
 __device__ __forceinline__ void span_rows(int ax, int ay, int bx, int by, int cx, int cy, int y, int& x1, int& x2) {
     int64_t i = y - ay;
-    int64_t a = ax + div_trunc((int64_t)(cx - ax) * i, (int64_t)(cy - ay));
+    int64_t a = ax + div_trunc_span((int64_t)(cx - ax) * i, (int64_t)(cy - ay));
     int64_t b;
-    if (y < by) b = ax + div_trunc((int64_t)(bx - ax) * i, (int64_t)(by - ay));
-    else b = bx + div_trunc((int64_t)(cx - bx) * (int64_t)(y - by), (int64_t)(cy - by));
+    if (y < by) b = ax + div_trunc_span((int64_t)(bx - ax) * i, (int64_t)(by - ay));
+    else b = bx + div_trunc_span((int64_t)(cx - bx) * (int64_t)(y - by), (int64_t)(cy - by));
     x1 = (int)(a < b ? a : b);
     x2 = (int)(a < b ? b : a);
 }

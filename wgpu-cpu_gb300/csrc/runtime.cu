@@ -302,6 +302,7 @@ struct Item {
     void* dst = nullptr;
     uint64_t size = 0;
     std::promise<Failure>* done = nullptr;  // reads: completion for the blocked caller
+    bool indexed = false;  // a read that took a submission index (completion recorded like a submission's)
     Clock::time_point t_submit;
     uint32_t merged = 0;  // submissions executed together with this one (serving mode)
 };
@@ -915,6 +916,7 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
 // ---------------------------------------------------------------- worker
 uint64_t submission_estimate(const Item& it);
 constexpr size_t kMaxGroup = 256;  // submissions merged into one launch at most
+constexpr size_t kLookaheadItems = 64;  // queue items the worker looks past for the next submission
 constexpr size_t kMaxCoalescedWrites = 4096;           // small buffer writes uploaded together at most
 constexpr uint64_t kMaxCoalescedBytes = 16ull << 20;  // and their bytes
 
@@ -989,16 +991,26 @@ void Device::worker_main() {
         }
         PlannedGroup cur = plan_group(std::move(group));
         for (;;) {
-            // look ahead: a submission group already queued is planned while this one runs
+            // look ahead: the next queued submission group is planned while this one runs, also
+            // past writes, reads and cache flushes queued before it (planning reads only host-side
+            // objects, which those do not change); they run, in queue order, after this group
             bool ahead = false;
+            std::vector<std::vector<Item>> between;
             {
                 std::lock_guard<std::mutex> lk(q_mu);
-                if (!queue.empty() && queue.front().kind == Item::SUBMIT) {
+                size_t k = 0;
+                while (k < queue.size() && k < kLookaheadItems && queue[k].kind != Item::SUBMIT) ++k;
+                if (k < queue.size() && queue[k].kind == Item::SUBMIT) {
+                    while (queue.front().kind != Item::SUBMIT) between.push_back(pop_group_locked());
                     planner.start(pop_group_locked());
                     ahead = true;
                 }
             }
             run_group(cur);
+            for (std::vector<Item>& g : between) {
+                if (g.size() > 1) execute_writes(g);
+                else execute(g[0]);
+            }
             if (!ahead) break;
             cur = planner.finish();
         }
@@ -1145,6 +1157,18 @@ void Device::execute(Item& it) {
         note_failure(f);
     }
     if (it.done) it.done->set_value(err);
+    if (it.indexed) {  // an asynchronous readback: its index completes (the copies were synchronised)
+        std::lock_guard<std::mutex> lk(q_mu);
+        SubmissionRecord rec;
+        rec.status = err.status;
+        rec.error = err.msg;
+        rec.stats.submission_index = it.index;
+        rec.stats.submit_to_fence_ms = ms_between(it.t_submit, Clock::now());
+        records[it.index] = rec;
+        completed_submissions = std::max(completed_submissions, it.index + 1);
+        while (records.size() > kKeptRecords) records.erase(records.begin());
+        done_cv.notify_all();
+    }
 }
 
 void Device::note_failure(const Failure& f) {
@@ -2520,6 +2544,36 @@ GBR_API gbr_status gbr_textures_read(gbr_device dh, uint32_t count, const gbr_te
         d->enqueue(std::move(it));
         Failure f = fut.get();
         if (f.status != GBR_OK) throw f;
+    })
+}
+
+GBR_API gbr_status gbr_queue_read_textures(gbr_device dh, uint32_t count, const gbr_texture* textures,
+                                           const uint32_t* mips, void* const* dsts, const uint64_t* sizes,
+                                           uint64_t* out_index) {
+    GBR_TRY({
+        auto d = get_device(dh);
+        if (count && (!textures || !mips || !dsts || !sizes)) fail(GBR_ERR_INVALID_ARGUMENT, "null argument");
+        Item it;
+        it.kind = Item::READ_TEXTURES;
+        it.t_submit = Clock::now();
+        for (uint32_t k = 0; k < count; ++k) {
+            auto t = d->get<Texture>(textures[k], "texture");
+            if (mips[k] >= t->mips_stored) fail(GBR_ERR_VALIDATION, "mip level not stored");
+            if (sizes[k] < t->mip_bytes(mips[k])) fail(GBR_ERR_VALIDATION, "destination too small");
+            if (!dsts[k]) fail(GBR_ERR_INVALID_ARGUMENT, "null destination");
+            it.textures.push_back(std::move(t));
+            it.mips.push_back(mips[k]);
+            it.dsts.push_back(dsts[k]);
+        }
+        it.indexed = true;
+        {
+            std::lock_guard<std::mutex> lk(d->q_mu);
+            if (d->lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", d->lost_msg.c_str());
+            it.index = d->next_submission++;
+            if (out_index) *out_index = it.index;
+            d->queue.push_back(std::move(it));
+            d->q_cv.notify_all();
+        }
     })
 }
 

@@ -499,6 +499,15 @@ unsafe extern "C" {
         dsts: *const *mut c_void,
         sizes: *const u64,
     ) -> gbr_status;
+    pub fn gbr_queue_read_textures(
+        device: gbr_device,
+        count: u32,
+        textures: *const gbr_texture,
+        mip_levels: *const u32,
+        dsts: *const *mut c_void,
+        sizes: *const u64,
+        out_index: *mut u64,
+    ) -> gbr_status;
     pub fn gbr_sampler_create(device: gbr_device, desc: *const gbr_sampler_desc, out_sampler: *mut gbr_sampler)
         -> gbr_status;
     pub fn gbr_sampler_destroy(device: gbr_device, sampler: gbr_sampler) -> gbr_status;

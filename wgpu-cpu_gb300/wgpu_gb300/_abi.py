@@ -267,6 +267,7 @@ OPTIONAL = {
     "wgsl_translate": (i32, [C.c_char_p, u64, C.c_char_p, C.c_char_p, C.c_char_p, u64, P(u64)]),
     "wgsl_compile_check": (i32, [C.c_char_p, u64, C.c_char_p, C.c_char_p, C.c_char_p, u64]),
     "textures_read": (i32, [u64, u32, P(u64), P(u32), P(C.c_void_p), P(u64)]),
+    "queue_read_textures": (i32, [u64, u32, P(u64), P(u32), P(C.c_void_p), P(u64), P(u64)]),
     "queue_write_buffers": (i32, [u64, u32, C.c_void_p]),
     "device_memory": (i32, [u64, P(u64), P(u64)]),
 }

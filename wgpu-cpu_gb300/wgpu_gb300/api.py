@@ -797,6 +797,26 @@ class Device:
         ns = (C.c_uint64 * k)(*[n for _, _, _, n in items])
         _check(self.lib, self.lib.textures_read(self.handle, k, hs, ms, ps, ns))
 
+    def read_textures_into_async(self, items):
+        """Enqueues the readback of several textures without waiting (gbr_queue_read_textures:
+        copy_texture_to_buffer + map_async): items as for read_textures_into.  Returns the
+        readback's submission index; the destinations hold the bytes once poll(True, index) has
+        returned.  A library without the call reads synchronously and returns None."""
+        items = list(items)
+        if not items:
+            return None
+        if self.lib.queue_read_textures is None:
+            self.read_textures_into(items)
+            return None
+        k = len(items)
+        hs = (C.c_uint64 * k)(*[t.handle for t, _, _, _ in items])
+        ms = (C.c_uint32 * k)(*[m for _, m, _, _ in items])
+        ps = (C.c_void_p * k)(*[p for _, _, p, _ in items])
+        ns = (C.c_uint64 * k)(*[n for _, _, _, n in items])
+        idx = C.c_uint64(0)
+        _check(self.lib, self.lib.queue_read_textures(self.handle, k, hs, ms, ps, ns, C.byref(idx)))
+        return idx.value
+
     def read_textures(self, textures: Sequence[Texture], mip_level: int = 0) -> List[np.ndarray]:
         outs = []
         for t in textures:
