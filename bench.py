@@ -115,7 +115,7 @@ def workloads():
             "blended quads: 10,000 quads (20,000 tris) sides U[16,1024], painter order, SrcAlpha/OneMinusSrcAlpha "
             "into 3840x2160 Rgba16Float, extension profile",
             {"triangles": 20000, "target": "3840x2160 rgba16float", "profile": "extension", "seed": 4},
-            tile=(32, 8), dtype="f32 (f16 storage)", texel_bytes=0, blend_bytes=8),
+            tile=(32, 4), dtype="f32 (f16 storage)", texel_bytes=0, blend_bytes=8),
         "colored": Workload(
             "colored", "colored UV sphere: 992 tris, 512x512 Rgba8Unorm, back-face cull, no depth",
             {"triangles": 992, "target": "512x512", "profile": "parity", "seed": 1}, tile=(16, 8)),
@@ -515,24 +515,29 @@ def run_ours(args, wk: Workload):
     out_bytes = sum(o.numel() for _, o in reads)
     buffer_writes = W.PreparedWrites([(obj, 0, host.numpy()) for obj, host in pinned if not isinstance(obj, W.Texture)])
     texture_writes = [(obj, host.numpy()) for obj, host in pinned if isinstance(obj, W.Texture)]
-    read_items = [(t, 0, o.data_ptr(), o.numel()) for t, o in reads]
+    # double-buffered targets, as a swapchain: frame k + 1 renders into the other set while frame
+    # k's targets come back (the same host destinations, written in frame order)
+    scene_b = wl.with_new_targets(scene)
+    cmds = [cmd, record(dev, scene_b)]
+    read_items = [[(t, 0, o.data_ptr(), o.numel()) for (t, _), (_, o) in zip(wl.scene_targets(sc), reads)]
+                  for sc in (scene, scene_b)]
 
-    def e2e_step():
+    def e2e_step(k):
         dev.queue.write_buffers(buffer_writes)
         for obj, host in texture_writes:
             dev.queue.write_texture(obj, host)
-        dev.queue.submit([cmd])
+        dev.queue.submit([cmds[k % 2]])
         # the readback, queue-ordered after the submission, without blocking: the next frame is
         # enqueued while this one's targets come back (copy_texture_to_buffer + map_async)
-        return dev.read_textures_into_async(read_items)
+        return dev.read_textures_into_async(read_items[k % 2])
 
-    for _ in range(max(1, min(args.warmup, 3))):
-        dev.poll(True, e2e_step())
-    e_steps = max(3, min(args.steps, 20))
+    for k in range(max(2, min(args.warmup, 4))):
+        dev.poll(True, e2e_step(k))
+    e_steps = max(4, min(args.steps, 20))
     barrier()
     t0 = time.perf_counter()
-    for _ in range(e_steps):
-        last_read = e2e_step()
+    for k in range(e_steps):
+        last_read = e2e_step(k)
     dev.poll(True, last_read)  # every frame's targets are back in host memory
     e2e_s = (time.perf_counter() - t0) / e_steps
     e2e_s, e2e_rate = replica_rate(frags_per_step, 1, e2e_s)
@@ -577,8 +582,9 @@ def run_ours(args, wk: Workload):
             "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": int(h2d) * world,
                     "d2h_bytes_per_step": int(out_bytes) * world, "ms_per_step": e2e_s * 1e3,
                     "note": "per frame: inputs uploaded from pinned host memory, frame submitted, every colour "
-                            "target read back to pinned host memory; frames pipelined (frame k+1 enqueued "
-                            "while frame k's readback runs), the clock stopped when the last readback landed"},
+                            "target read back to pinned host memory; frames pipelined over two target sets "
+                            "(double buffering: frame k+1 renders while frame k's targets are read back), the "
+                            "clock stopped when the last readback landed"},
             "gpu_launches": launches,
             "clocks": clocks.summary(),
             **extras,
@@ -642,7 +648,7 @@ def main():
     ap.add_argument("--no-extras", action="store_true",
                     help="batched workload: skip the per-draw, fill-bound and serving arms (profiling runs)")
     ap.add_argument("--fixed", action="store_true",
-                    help="batched workload: no CUDA graph and no autotuner (the workload's fixed tile shape)")
+                    help="no CUDA graph (and for the batched workload no autotuner: its fixed tile shape)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     if args.workload == "batched" and not args.fixed and not args.tile and args.impl == "ours":
@@ -653,6 +659,9 @@ def main():
         args.tile = args.warps = 0
     elif not args.tile and args.workload in workloads():
         args.tile, args.warps = workloads()[args.workload].tile
+        # the other workloads at their fixed tile shape, their launch sequence replayed from a
+        # CUDA graph as a frame loop would (--fixed: launched directly)
+        args.graphs = args.graphs or (args.impl == "ours" and not args.fixed)
     if args.workload == "serve":
         if args.impl == "reference":
             run_reference(args, workloads()["batched"])

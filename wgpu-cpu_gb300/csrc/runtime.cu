@@ -386,6 +386,36 @@ struct Device {
     cudaStream_t copy_stream = nullptr;
     cudaMemPool_t staging_pool = nullptr;
     std::mutex copy_mu;
+    // Asynchronous readbacks (gbr_queue_read_textures) run on rb_stream with the copy engines,
+    // after the queue work before them (an event), so the kernels of later submissions overlap
+    // them; a later writer of a texture that is being read first waits for that read's event.
+    // Completion is recorded in queue order (finish_reads).  All of it is the worker's.
+    cudaStream_t rb_stream = nullptr;
+    struct ReadFence {
+        cudaEvent_t ev = nullptr;
+        ReadFence() = default;
+        ReadFence(const ReadFence&) = delete;
+        ReadFence& operator=(const ReadFence&) = delete;
+        ~ReadFence() {
+            if (ev) cudaEventDestroy(ev);
+        }
+    };
+    struct PendingRead {
+        uint64_t index = 0;
+        std::shared_ptr<ReadFence> done;
+        std::vector<std::shared_ptr<Texture>> keep;
+        Clock::time_point t_submit;
+    };
+    std::map<const Texture*, std::shared_ptr<ReadFence>> read_fence;  // the last readback of each texture
+    std::deque<PendingRead> pending_reads;                            // in index order
+    void wait_reads_of(const Texture* t) {  // the queue's stream waits for t's readback in flight
+        auto f = read_fence.find(t);
+        if (f != read_fence.end()) cuda_check(cudaStreamWaitEvent(stream, f->second->ev, 0), "read fence");
+    }
+    void wait_all_reads() {
+        for (auto& f : read_fence) cuda_check(cudaStreamWaitEvent(stream, f.second->ev, 0), "read fence");
+    }
+    void finish_reads(uint64_t before);
 
     std::mutex obj_mu;
     uint64_t next_handle = 1;
@@ -980,6 +1010,11 @@ void Device::worker_main() {
         std::vector<Item> group;
         {
             std::unique_lock<std::mutex> lk(q_mu);
+            if (queue.empty() && !pending_reads.empty()) {  // idle: the readbacks in flight complete
+                lk.unlock();
+                finish_reads(UINT64_MAX);
+                continue;
+            }
             q_cv.wait(lk, [&] { return stopping || !queue.empty(); });
             if (queue.empty() && stopping) return;
             group = pop_group_locked();
@@ -1061,6 +1096,7 @@ void Device::execute_writes(std::vector<Item>& items) {
 
 void Device::execute(Item& it) {
     Failure err{GBR_OK, ""};
+    bool deferred = false;  // an asynchronous readback: completed later, by finish_reads
     try {
         if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
         switch (it.kind) {
@@ -1079,6 +1115,7 @@ void Device::execute(Item& it) {
                 break;
             case Item::WRITE_TEXTURE: {
                 Texture& t = *it.texture;
+                wait_reads_of(&t);
                 uint32_t w = t.mip_w(it.mip), h = t.mip_h(it.mip), layers = t.layers();
                 uint64_t row = (uint64_t)w * t.bpp;
                 const uint64_t src_size = it.staged ? it.staged_size : it.data.size();
@@ -1110,6 +1147,28 @@ void Device::execute(Item& it) {
                 cuda_check(cudaStreamSynchronize(stream), "texture_read sync");
                 break;
             case Item::READ_TEXTURES: {
+                if (it.indexed) {
+                    // asynchronous: the copy engines on rb_stream, after the queue work before it
+                    cudaEvent_t ready = nullptr;
+                    cuda_check(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "cudaEventCreate");
+                    cudaError_t e = cudaEventRecord(ready, stream);
+                    if (e == cudaSuccess) e = cudaStreamWaitEvent(rb_stream, ready, 0);
+                    cudaEventDestroy(ready);  // released once the wait is satisfied
+                    cuda_check(e, "readback ordering");
+                    for (size_t k = 0; k < it.textures.size(); ++k) {
+                        const Texture& t = *it.textures[k];
+                        cuda_check(cudaMemcpyAsync(it.dsts[k], t.ptr + t.mip_offset[it.mips[k]], t.mip_bytes(it.mips[k]),
+                                                   cudaMemcpyDeviceToHost, rb_stream),
+                                   "queue_read_textures");
+                    }
+                    auto done = std::make_shared<ReadFence>();
+                    cuda_check(cudaEventCreateWithFlags(&done->ev, cudaEventDisableTiming), "cudaEventCreate");
+                    cuda_check(cudaEventRecord(done->ev, rb_stream), "cudaEventRecord");
+                    for (const auto& t : it.textures) read_fence[t.get()] = done;
+                    pending_reads.push_back(PendingRead{it.index, done, it.textures, it.t_submit});
+                    deferred = true;
+                    break;
+                }
                 // Destinations the device can address (pinned host memory, as the attributes report
                 // it) are written by one copy kernel over all SMs, which moves the bytes over the
                 // CPU-GPU link faster than one copy-engine transfer per texture; any other
@@ -1157,7 +1216,7 @@ void Device::execute(Item& it) {
         note_failure(f);
     }
     if (it.done) it.done->set_value(err);
-    if (it.indexed) {  // an asynchronous readback: its index completes (the copies were synchronised)
+    if (it.indexed && !deferred) {  // an asynchronous readback that failed before its copies: done now
         std::lock_guard<std::mutex> lk(q_mu);
         SubmissionRecord rec;
         rec.status = err.status;
@@ -1166,6 +1225,31 @@ void Device::execute(Item& it) {
         rec.stats.submit_to_fence_ms = ms_between(it.t_submit, Clock::now());
         records[it.index] = rec;
         completed_submissions = std::max(completed_submissions, it.index + 1);
+        while (records.size() > kKeptRecords) records.erase(records.begin());
+        done_cv.notify_all();
+    }
+}
+
+// Completes the asynchronous readbacks with index < before, in order: waits for each one's
+// copies, records it like a submission and drops the fences that still point at it.
+void Device::finish_reads(uint64_t before) {
+    while (!pending_reads.empty() && pending_reads.front().index < before) {
+        PendingRead pr = std::move(pending_reads.front());
+        pending_reads.pop_front();
+        const cudaError_t e = cudaEventSynchronize(pr.done->ev);
+        for (const auto& t : pr.keep) {
+            auto f = read_fence.find(t.get());
+            if (f != read_fence.end() && f->second == pr.done) read_fence.erase(f);
+        }
+        if (e != cudaSuccess) note_failure(Failure{GBR_ERR_CUDA, cudaGetErrorString(e)});
+        std::lock_guard<std::mutex> lk(q_mu);
+        SubmissionRecord rec;
+        rec.status = e == cudaSuccess ? GBR_OK : GBR_ERR_CUDA;
+        if (e != cudaSuccess) rec.error = cudaGetErrorString(e);
+        rec.stats.submission_index = pr.index;
+        rec.stats.submit_to_fence_ms = ms_between(pr.t_submit, Clock::now());
+        records[pr.index] = rec;
+        completed_submissions = std::max(completed_submissions, pr.index + 1);
         while (records.size() > kKeptRecords) records.erase(records.begin());
         done_cv.notify_all();
     }
@@ -1257,6 +1341,12 @@ void Device::run_group(PlannedGroup& g) {
     try {
         if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
         if (g.failure.status != GBR_OK) throw g.failure;
+        // textures the group writes wait for their readbacks in flight (copies: all of them)
+        if (!read_fence.empty())
+            for (const Batch& b : batches) {
+                if (b.copy) wait_all_reads();
+                for (const Texture* t : b.writes) wait_reads_of(t);
+            }
         size_t from = 0;
         while (from < batches.size()) {
             const RunResult r = run_batches(batches, from, run);
@@ -1295,6 +1385,12 @@ void Device::run_group(PlannedGroup& g) {
         }
     float group_ms = 0.0f;
     if (run.ev && run.started) cudaEventElapsedTime(&group_ms, run.ev->start, run.ev->end);
+    // readbacks queued before these submissions complete first (completion is in queue order)
+    if (!pending_reads.empty()) {
+        uint64_t first = UINT64_MAX;
+        for (size_t i = 0; i < n; ++i) first = std::min(first, items[i].index);
+        finish_reads(first);
+    }
     std::lock_guard<std::mutex> lk(q_mu);
     for (size_t i = 0; i < n; ++i) {
         SubmissionRecord& rec = recs[i];
@@ -2260,6 +2356,7 @@ GBR_API gbr_status gbr_device_create(const gbr_device_config* cfg, gbr_device* o
             fail(GBR_ERR_INVALID_ARGUMENT, "the edge-function raster rule belongs to the extension profile");
         cuda_check(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking), "cudaStreamCreate");
         cuda_check(cudaStreamCreateWithFlags(&d->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        cuda_check(cudaStreamCreateWithFlags(&d->rb_stream, cudaStreamNonBlocking), "cudaStreamCreate");
         {
             cudaMemPoolProps props{};
             props.allocType = cudaMemAllocationTypePinned;
@@ -2322,8 +2419,12 @@ GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
             ps.ptr = nullptr;
             ps.done = nullptr;
         }
+        cudaStreamSynchronize(d->rb_stream);
+        d->read_fence.clear();
+        d->pending_reads.clear();
         cudaStreamDestroy(d->stream);
         cudaStreamDestroy(d->copy_stream);
+        cudaStreamDestroy(d->rb_stream);
         if (d->staging_pool) cudaMemPoolDestroy(d->staging_pool);
     })
 }

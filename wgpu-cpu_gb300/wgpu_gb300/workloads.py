@@ -586,6 +586,24 @@ def build_config(dev: W.Device, name: str, **over):
     return globals()[builder](dev, **{**kwargs, **over})
 
 
+def with_new_targets(scene):
+    """A copy of `scene` that renders the same draws into new targets of the same sizes and
+    formats: the second buffer of a double-buffered frame loop."""
+    import copy
+
+    dev = scene.device
+
+    def fresh(t):
+        return None if t is None else dev.create_texture(t.width, t.height, t.format)
+
+    s = copy.copy(scene)
+    if hasattr(scene, "passes"):
+        s.passes = [(fresh(p[0]), fresh(p[1]), *p[2:]) for p in scene.passes]
+    else:
+        s.color, s.depth = fresh(scene.color), fresh(scene.depth)
+    return s
+
+
 def scene_targets(scene) -> list:
     """(colour, depth or None) of every render pass of a Scene or MultiScene, in pass order."""
     if hasattr(scene, "passes"):
