@@ -408,11 +408,28 @@ struct Device {
     };
     std::map<const Texture*, std::shared_ptr<ReadFence>> read_fence;  // the last readback of each texture
     std::deque<PendingRead> pending_reads;                            // in index order
+    // Readbacks whose place in the queue's stream is marked (`ready`) but whose copies are not
+    // issued yet: the worker issues them while the next submission runs (issue_reads), or at once
+    // when a writer of one of their textures comes first.
+    struct DeferredRead {
+        Item item;
+        cudaEvent_t ready = nullptr;
+    };
+    std::deque<DeferredRead> deferred_reads;
+    void issue_reads();
     void wait_reads_of(const Texture* t) {  // the queue's stream waits for t's readback in flight
+        for (const DeferredRead& dr : deferred_reads)
+            for (const auto& u : dr.item.textures)
+                if (u.get() == t) {
+                    issue_reads();
+                    goto issued;
+                }
+    issued:
         auto f = read_fence.find(t);
         if (f != read_fence.end()) cuda_check(cudaStreamWaitEvent(stream, f->second->ev, 0), "read fence");
     }
     void wait_all_reads() {
+        issue_reads();
         for (auto& f : read_fence) cuda_check(cudaStreamWaitEvent(stream, f.second->ev, 0), "read fence");
     }
     void finish_reads(uint64_t before);
@@ -1010,7 +1027,7 @@ void Device::worker_main() {
         std::vector<Item> group;
         {
             std::unique_lock<std::mutex> lk(q_mu);
-            if (queue.empty() && !pending_reads.empty()) {  // idle: the readbacks in flight complete
+            if (queue.empty() && (!pending_reads.empty() || !deferred_reads.empty())) {  // idle: the readbacks complete
                 lk.unlock();
                 finish_reads(UINT64_MAX);
                 continue;
@@ -1148,24 +1165,20 @@ void Device::execute(Item& it) {
                 break;
             case Item::READ_TEXTURES: {
                 if (it.indexed) {
-                    // asynchronous: the copy engines on rb_stream, after the queue work before it
-                    cudaEvent_t ready = nullptr;
-                    cuda_check(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming), "cudaEventCreate");
-                    cudaError_t e = cudaEventRecord(ready, stream);
-                    if (e == cudaSuccess) e = cudaStreamWaitEvent(rb_stream, ready, 0);
-                    cudaEventDestroy(ready);  // released once the wait is satisfied
+                    // asynchronous: its place in the queue's stream marked now, its copies (copy
+                    // engines, rb_stream) issued by issue_reads
+                    DeferredRead dr;
+                    cuda_check(cudaEventCreateWithFlags(&dr.ready, cudaEventDisableTiming), "cudaEventCreate");
+                    const cudaError_t e = cudaEventRecord(dr.ready, stream);
+                    if (e != cudaSuccess) cudaEventDestroy(dr.ready);
                     cuda_check(e, "readback ordering");
-                    for (size_t k = 0; k < it.textures.size(); ++k) {
-                        const Texture& t = *it.textures[k];
-                        cuda_check(cudaMemcpyAsync(it.dsts[k], t.ptr + t.mip_offset[it.mips[k]], t.mip_bytes(it.mips[k]),
-                                                   cudaMemcpyDeviceToHost, rb_stream),
-                                   "queue_read_textures");
-                    }
-                    auto done = std::make_shared<ReadFence>();
-                    cuda_check(cudaEventCreateWithFlags(&done->ev, cudaEventDisableTiming), "cudaEventCreate");
-                    cuda_check(cudaEventRecord(done->ev, rb_stream), "cudaEventRecord");
-                    for (const auto& t : it.textures) read_fence[t.get()] = done;
-                    pending_reads.push_back(PendingRead{it.index, done, it.textures, it.t_submit});
+                    dr.item.kind = it.kind;
+                    dr.item.index = it.index;
+                    dr.item.t_submit = it.t_submit;
+                    dr.item.textures = std::move(it.textures);
+                    dr.item.mips = std::move(it.mips);
+                    dr.item.dsts = std::move(it.dsts);
+                    deferred_reads.push_back(std::move(dr));
                     deferred = true;
                     break;
                 }
@@ -1230,9 +1243,45 @@ void Device::execute(Item& it) {
     }
 }
 
+// Issues the copies of the deferred readbacks, in queue order: each on rb_stream after its
+// `ready` mark, then its `done` event, which becomes the fence of its textures.  A readback whose
+// copies cannot be issued completes at once with the error.
+void Device::issue_reads() {
+    while (!deferred_reads.empty()) {
+        DeferredRead dr = std::move(deferred_reads.front());
+        deferred_reads.pop_front();
+        Item& it = dr.item;
+        auto done = std::make_shared<ReadFence>();
+        cudaError_t e = cudaStreamWaitEvent(rb_stream, dr.ready, 0);
+        cudaEventDestroy(dr.ready);  // released once the wait is satisfied
+        for (size_t k = 0; e == cudaSuccess && k < it.textures.size(); ++k) {
+            const Texture& t = *it.textures[k];
+            e = cudaMemcpyAsync(it.dsts[k], t.ptr + t.mip_offset[it.mips[k]], t.mip_bytes(it.mips[k]),
+                                cudaMemcpyDeviceToHost, rb_stream);
+        }
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done->ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(done->ev, rb_stream);
+        if (e != cudaSuccess) {
+            note_failure(Failure{GBR_ERR_CUDA, cudaGetErrorString(e)});
+            std::lock_guard<std::mutex> lk(q_mu);
+            SubmissionRecord rec;
+            rec.status = GBR_ERR_CUDA;
+            rec.error = cudaGetErrorString(e);
+            rec.stats.submission_index = it.index;
+            records[it.index] = rec;
+            completed_submissions = std::max(completed_submissions, it.index + 1);
+            done_cv.notify_all();
+            continue;
+        }
+        for (const auto& t : it.textures) read_fence[t.get()] = done;
+        pending_reads.push_back(PendingRead{it.index, done, std::move(it.textures), it.t_submit});
+    }
+}
+
 // Completes the asynchronous readbacks with index < before, in order: waits for each one's
 // copies, records it like a submission and drops the fences that still point at it.
 void Device::finish_reads(uint64_t before) {
+    issue_reads();
     while (!pending_reads.empty() && pending_reads.front().index < before) {
         PendingRead pr = std::move(pending_reads.front());
         pending_reads.pop_front();
@@ -1342,7 +1391,7 @@ void Device::run_group(PlannedGroup& g) {
         if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
         if (g.failure.status != GBR_OK) throw g.failure;
         // textures the group writes wait for their readbacks in flight (copies: all of them)
-        if (!read_fence.empty())
+        if (!read_fence.empty() || !deferred_reads.empty())
             for (const Batch& b : batches) {
                 if (b.copy) wait_all_reads();
                 for (const Texture* t : b.writes) wait_reads_of(t);
@@ -1386,7 +1435,7 @@ void Device::run_group(PlannedGroup& g) {
     float group_ms = 0.0f;
     if (run.ev && run.started) cudaEventElapsedTime(&group_ms, run.ev->start, run.ev->end);
     // readbacks queued before these submissions complete first (completion is in queue order)
-    if (!pending_reads.empty()) {
+    if (!pending_reads.empty() || !deferred_reads.empty()) {
         uint64_t first = UINT64_MAX;
         for (size_t i = 0; i < n; ++i) first = std::min(first, items[i].index);
         finish_reads(first);
@@ -1962,6 +2011,9 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         } else {
             enqueue();
         }
+        // readbacks queued before this launch: their copies issued while it runs (ahead of this
+        // launch's own status readback, which waits for the launch)
+        issue_reads();
         cuda_check(cudaEventRecord(run.ev->end, stream), "event");
         cuda_check(cudaMemcpyAsync(st.data(), meta + off_status, nb * sizeof(BatchStatus), cudaMemcpyDeviceToHost,
                                    stream),
@@ -2422,6 +2474,8 @@ GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
         cudaStreamSynchronize(d->rb_stream);
         d->read_fence.clear();
         d->pending_reads.clear();
+        for (auto& dr : d->deferred_reads) cudaEventDestroy(dr.ready);
+        d->deferred_reads.clear();
         cudaStreamDestroy(d->stream);
         cudaStreamDestroy(d->copy_stream);
         cudaStreamDestroy(d->rb_stream);
