@@ -466,8 +466,8 @@ struct Device {
         uint8_t* ptr = nullptr;
         size_t size = 0;
         cudaEvent_t done = nullptr;
-    } pinned_stage[2];
-    int pinned_next = 0;
+    } pinned_stage[2], meta_stage[2];
+    int pinned_next = 0, meta_next = 0;
     uint32_t ovf_capacity = 4096;
     uint64_t bin_capacity = 1u << 22;
     // chunk work items the visibility raster may split heavy tiles into (0: 32 MiB of key arrays);
@@ -1782,9 +1782,24 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
     const uint64_t budget = cfg.hbm_budget_bytes ? cfg.hbm_budget_bytes : (80ull << 30);
     meta_buf.ensure(cur, &scratch_bytes);
     uint8_t* meta = static_cast<uint8_t*>(meta_buf.ptr);
-    std::vector<uint8_t> host_meta(cur, 0);
+    // the descriptors are built in pinned host memory (two buffers in turn, each reused once its
+    // upload has completed), so their upload is an asynchronous DMA
+    PinnedStage& hm = meta_stage[meta_next];
+    meta_next ^= 1;
+    if (hm.done) cuda_check(cudaEventSynchronize(hm.done), "descriptor staging reuse");
+    else cuda_check(cudaEventCreateWithFlags(&hm.done, cudaEventDisableTiming), "cudaEventCreate");
+    if (hm.size < cur) {
+        if (hm.ptr) cudaFreeHost(hm.ptr);
+        hm.ptr = nullptr;
+        hm.size = 0;
+        const size_t want = std::max<size_t>(cur, 1u << 20);
+        cuda_check(cudaHostAlloc(reinterpret_cast<void**>(&hm.ptr), want, cudaHostAllocDefault), "cudaHostAlloc");
+        hm.size = want;
+    }
+    uint8_t* const host_meta = hm.ptr;
+    std::memset(host_meta, 0, cur);
     for (size_t i = from; i < nb; ++i) {
-        uint8_t* p = host_meta.data() + desc_off[i];
+        uint8_t* p = host_meta + desc_off[i];
         std::memcpy(p, batches[i].draws.data(), batches[i].draws.size() * sizeof(DrawDesc));
         TargetDesc* tp = reinterpret_cast<TargetDesc*>(p + batches[i].draws.size() * sizeof(DrawDesc));
         for (size_t t = 0; t < batches[i].targets.size(); ++t) {
@@ -1798,7 +1813,8 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         if (!shape_tables[i].empty())
             std::memcpy(p + shape_table_at(batches[i]), shape_tables[i].data(), shape_tables[i].size() * sizeof(uint32_t));
     }
-    cuda_check(cudaMemcpyAsync(meta, host_meta.data(), cur, cudaMemcpyHostToDevice, stream), "upload descriptors");
+    cuda_check(cudaMemcpyAsync(meta, host_meta, cur, cudaMemcpyHostToDevice, stream), "upload descriptors");
+    cuda_check(cudaEventRecord(hm.done, stream), "cudaEventRecord");
 
     if (!run.ev) {
         run.ev = std::make_shared<EventPair>();
@@ -2465,12 +2481,14 @@ GBR_API gbr_status gbr_device_destroy(gbr_device dh) {
         d->flush_buf.release();
         cudaStreamSynchronize(d->stream);
         d->upload_buf.release();
-        for (auto& ps : d->pinned_stage) {
-            if (ps.ptr) cudaFreeHost(ps.ptr);
-            if (ps.done) cudaEventDestroy(ps.done);
-            ps.ptr = nullptr;
-            ps.done = nullptr;
-        }
+        for (auto* stages : {d->pinned_stage, d->meta_stage})
+            for (int k = 0; k < 2; ++k) {
+                auto& ps = stages[k];
+                if (ps.ptr) cudaFreeHost(ps.ptr);
+                if (ps.done) cudaEventDestroy(ps.done);
+                ps.ptr = nullptr;
+                ps.done = nullptr;
+            }
         cudaStreamSynchronize(d->rb_stream);
         d->read_fence.clear();
         d->pending_reads.clear();
