@@ -373,6 +373,7 @@ constexpr size_t kLazyWakeItems = 1024;  // queued writes that wake the worker b
 constexpr size_t kKeptRecords = 16384;   // finished submissions whose stats stay queryable
 
 struct PlannedGroup;
+class Planner;
 
 struct Device {
     gbr_device_config cfg{};
@@ -433,6 +434,12 @@ struct Device {
         for (auto& f : read_fence) cuda_check(cudaStreamWaitEvent(stream, f.second->ev, 0), "read fence");
     }
     void finish_reads(uint64_t before);
+    // worker lookahead (worker_main): the planner, whether it holds the next group, and the
+    // non-submission items queued before that group
+    Planner* la_planner = nullptr;
+    bool la_ahead = false;
+    std::vector<std::vector<Item>> la_between;
+    void lookahead();
 
     std::mutex obj_mu;
     uint64_t next_handle = 1;
@@ -963,7 +970,7 @@ DrawDesc make_draw(const DrawCmd& dc, uint32_t profile, bool has_depth_attachmen
 // ---------------------------------------------------------------- worker
 uint64_t submission_estimate(const Item& it);
 constexpr size_t kMaxGroup = 256;  // submissions merged into one launch at most
-constexpr size_t kLookaheadItems = 64;  // queue items the worker looks past for the next submission
+constexpr size_t kLookaheadItems = 8192;  // queue items the worker looks past for the next submission (a frame's writes can be hundreds)
 constexpr size_t kMaxCoalescedWrites = 4096;           // small buffer writes uploaded together at most
 constexpr uint64_t kMaxCoalescedBytes = 16ull << 20;  // and their bytes
 
@@ -1042,30 +1049,39 @@ void Device::worker_main() {
             continue;
         }
         PlannedGroup cur = plan_group(std::move(group));
+        la_planner = &planner;
         for (;;) {
             // look ahead: the next queued submission group is planned while this one runs, also
             // past writes, reads and cache flushes queued before it (planning reads only host-side
-            // objects, which those do not change); they run, in queue order, after this group
-            bool ahead = false;
-            std::vector<std::vector<Item>> between;
-            {
-                std::lock_guard<std::mutex> lk(q_mu);
-                size_t k = 0;
-                while (k < queue.size() && k < kLookaheadItems && queue[k].kind != Item::SUBMIT) ++k;
-                if (k < queue.size() && queue[k].kind == Item::SUBMIT) {
-                    while (queue.front().kind != Item::SUBMIT) between.push_back(pop_group_locked());
-                    planner.start(pop_group_locked());
-                    ahead = true;
-                }
-            }
+            // objects, which those do not change); they run, in queue order, after this group.
+            // The queue is looked at now and again just before the worker waits for the launch.
+            la_ahead = false;
+            la_between.clear();
+            lookahead();
             run_group(cur);
-            for (std::vector<Item>& g : between) {
+            for (std::vector<Item>& g : la_between) {
                 if (g.size() > 1) execute_writes(g);
                 else execute(g[0]);
             }
-            if (!ahead) break;
+            la_between.clear();
+            if (!la_ahead) break;
             cur = planner.finish();
         }
+        la_planner = nullptr;
+    }
+}
+
+// Hands the next queued submission group (and the writes, reads and flushes queued before it) to
+// the planner, once per group the worker runs (la_ahead).
+void Device::lookahead() {
+    if (!la_planner || la_ahead) return;
+    std::lock_guard<std::mutex> lk(q_mu);
+    size_t k = 0;
+    while (k < queue.size() && k < kLookaheadItems && queue[k].kind != Item::SUBMIT) ++k;
+    if (k < queue.size() && queue[k].kind == Item::SUBMIT) {
+        while (queue.front().kind != Item::SUBMIT) la_between.push_back(pop_group_locked());
+        la_planner->start(pop_group_locked());
+        la_ahead = true;
     }
 }
 
@@ -2030,6 +2046,7 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         // readbacks queued before this launch: their copies issued while it runs (ahead of this
         // launch's own status readback, which waits for the launch)
         issue_reads();
+        lookahead();  // a submission queued since this group started is planned while it runs
         cuda_check(cudaEventRecord(run.ev->end, stream), "event");
         cuda_check(cudaMemcpyAsync(st.data(), meta + off_status, nb * sizeof(BatchStatus), cudaMemcpyDeviceToHost,
                                    stream),
