@@ -1813,7 +1813,10 @@ RunResult Device::run_batches(std::vector<Batch>& batches, size_t from, GroupRun
         hm.size = want;
     }
     uint8_t* const host_meta = hm.ptr;
-    std::memset(host_meta, 0, cur);
+    // the abort flag, statuses, work counters and fragment counters start at zero; the descriptor
+    // regions below are written whole (the gaps between them are never read, and the raster
+    // states are built on the device)
+    std::memset(host_meta, 0, off_desc);
     for (size_t i = from; i < nb; ++i) {
         uint8_t* p = host_meta + desc_off[i];
         std::memcpy(p, batches[i].draws.data(), batches[i].draws.size() * sizeof(DrawDesc));
