@@ -78,3 +78,18 @@ def test_validation_errors(orc):
 def test_random_clip_scene_runs(orc):
     img, _, n = scenes.random_clip_triangles(orc, 200, 96, 64, seed=3)
     assert n > 0 and img.shape == (64, 96, 4)
+
+
+def test_second_target_set_renders_the_same_frame(orc):
+    """with_new_targets (the second buffer of a double-buffered frame loop) draws the same draws
+    into fresh targets of the same sizes and formats: both sets hold the same bytes."""
+    s = wl.scene_batched(orc, n_targets=3, n_draws=5, tri_lo=20, tri_hi=400, side_lo=32, side_hi=96, seed=9)
+    sb = wl.with_new_targets(s)
+    pairs = list(zip(wl.scene_targets(s), wl.scene_targets(sb)))
+    assert all(a[0] is not b[0] and a[1] is not b[1] for a, b in pairs)
+    for sc in (s, sb):
+        sc.render()
+    for (ca, da), (cb, db) in pairs:
+        assert (ca.width, ca.height, ca.format) == (cb.width, cb.height, cb.format)
+        assert np.array_equal(orc.read_texture(ca), orc.read_texture(cb))
+        assert np.array_equal(orc.read_texture(da), orc.read_texture(db))
