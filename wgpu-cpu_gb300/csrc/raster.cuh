@@ -583,9 +583,9 @@ __device__ __forceinline__ bool tiles_are_many(const TriRecord& r, uint32_t shif
 // Binning hint of a primary record, written by the fast setup so that k_fill need not read the
 // record back: the record covers nothing, exactly one tile (its global index), or anything else.
 enum : uint32_t { TILE_HINT_EMPTY = 0xFFFFFFFEu, TILE_HINT_WALK = 0xFFFFFFFFu };
-__device__ __forceinline__ uint32_t tile_hint_of(const BatchParams& bp, const TriRecord& r, const DrawDesc& d) {
+__device__ __forceinline__ uint32_t tile_hint_of(const BatchParams& bp, const TriRecord& r, const DrawDesc& d,
+                                                 const TargetDesc& t) {
     if (r.flags & 2u) return TILE_HINT_EMPTY;
-    const TargetDesc& t = bp.targets[d.target];
     uint32_t one;
     if (!tiles_are_many(r, bp.tile_shift) && single_tile(r, d, t, bp.tile_shift, one)) return t.tile_base + one;
     return TILE_HINT_WALK;
@@ -895,9 +895,12 @@ __global__ void __launch_bounds__(128) k_setup_slow(BatchParams bp) {
 struct alignas(16) DrawCache {
     DrawDesc d;
     float mvp[16];
-    uint32_t id;  // draw index, ~0 = empty
+    TargetDesc t;  // the draw's target
+    uint32_t id;   // draw index, ~0 = empty
     uint32_t _pad[3];
 };
+static_assert(sizeof(DrawDesc) % 16 == 0 && sizeof(TargetDesc) % 8 == 0 && sizeof(TargetDesc) / 8 <= 16,
+              "DrawCache is filled with 16-byte descriptor and 8-byte target loads");
 
 constexpr int kSetupWarps = 4;
 
@@ -1188,15 +1191,34 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
     __syncwarp();
     if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the grid
 
-    // the draw's descriptor and matrix to the warp's cache (warp-uniform)
+    // the draw's descriptor, matrix and target to the warp's cache (warp-uniform).  A warp's
+    // groups lie a grid apart, so nearly every group changes draws: every load of a round issues
+    // before any is used, and the copy costs two dependent loads (the descriptor with the matrix's
+    // address and the target's index, then the matrix and the target)
     auto cache_draw = [&](uint32_t di) {
-        __syncwarp();
-        const uint2* src = reinterpret_cast<const uint2*>(bp.draws + di);
-        uint2* dst = reinterpret_cast<uint2*>(&dc.d);
-        for (uint32_t k = lane; k < sizeof(DrawDesc) / 8; k += 32) dst[k] = __ldg(src + k);
+        constexpr uint32_t NQ = sizeof(DrawDesc) / 16, NR = (NQ + 31) / 32, NT = sizeof(TargetDesc) / 8;
+        const uint4* src = reinterpret_cast<const uint4*>(bp.draws + di);
+        uint4 q[NR];
+#pragma unroll
+        for (uint32_t r = 0; r < NR; ++r)
+            if (lane + 32 * r < NQ) q[r] = __ldg(src + lane + 32 * r);
         const uint8_t* u = bp.draws[di].uniform[0][0];
         const bool has = u != nullptr && bp.draws[di].uniform_size[0][0] >= 64;
-        if (lane < 16) dc.mvp[lane] = has ? __ldg(reinterpret_cast<const float*>(u) + lane) : 0.0f;
+        const uint32_t ti = bp.draws[di].target;
+        float m = 0.0f;
+        uint2 tw = make_uint2(0u, 0u);
+        if (lane < 16) {
+            if (has) m = __ldg(reinterpret_cast<const float*>(u) + lane);
+        } else if (lane < 16 + NT) {
+            tw = __ldg(reinterpret_cast<const uint2*>(bp.targets + ti) + (lane - 16));
+        }
+        __syncwarp();  // the warp is done with the previous draw's cache
+        uint4* dst = reinterpret_cast<uint4*>(&dc.d);
+#pragma unroll
+        for (uint32_t r = 0; r < NR; ++r)
+            if (lane + 32 * r < NQ) dst[lane + 32 * r] = q[r];
+        if (lane < 16) dc.mvp[lane] = m;
+        else if (lane < 16 + NT) reinterpret_cast<uint2*>(&dc.t)[lane - 16] = tw;
         if (lane == 0) dc.id = di;
         __syncwarp();
     };
@@ -1230,14 +1252,14 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
         // tiles for the other records but those handed to the warp as a whole (coop)
         uint32_t hint = TILE_HINT_EMPTY;
         if (live && done) {
-            hint = tile_hint_of(bp, *rec, dc.d);
+            hint = tile_hint_of(bp, *rec, dc.d, dc.t);
             if (bp.tile_hint) bp.tile_hint[gp] = hint;
         }
         const uint32_t single = hint < TILE_HINT_EMPTY ? hint : 0xFFFFFFFFu;
         const uint32_t peers = __match_any_sync(kFull, single);
         if (single != 0xFFFFFFFFu && (int)lane == __ffs(peers) - 1) atomicAdd(&bp.tile_count[single], (uint32_t)__popc(peers));
         if (hint == TILE_HINT_WALK && coop == nullptr) {
-            const TargetDesc& t = bp.targets[dc.d.target];
+            const TargetDesc& t = dc.t;
             for_each_tile<EDGE>(*rec, dc.d, t, bp.tile_shift,
                                 [&](uint32_t lt) { atomicAdd(&bp.tile_count[t.tile_base + lt], 1u); });
         }
