@@ -1497,11 +1497,12 @@ __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
         const uint32_t single = hint < TILE_HINT_EMPTY ? hint : 0xFFFFFFFFu;
         const uint32_t peers = __match_any_sync(0xFFFFFFFFu, single);
         if (single != 0xFFFFFFFFu) {
+            const uint32_t bin0 = bp.tile_offset[single];  // loaded while the cursor atomic is out
             const int leader = __ffs(peers) - 1;
             uint32_t pos = 0;
             if ((int)lane == leader) pos = atomicAdd(&bp.tile_cursor[single], (uint32_t)__popc(peers));
             pos = __shfl_sync(peers, pos, leader) + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-            bp.bins[bp.tile_offset[single] + pos] = i << SUBTRI_BITS;
+            bp.bins[bin0 + pos] = i << SUBTRI_BITS;
         } else if (i < total && hint == TILE_HINT_WALK) {
             const TriRecord* r = i < bp.total_prims ? rec_at(bp.records, bp.record_stride, i)
                                                     : rec_at(bp.ovf_records, bp.record_stride, i - bp.total_prims);
@@ -1512,9 +1513,43 @@ __global__ void __launch_bounds__(128) k_fill(BatchParams bp) {
                     const DrawDesc& d = bp.draws[r->draw];
                     const TargetDesc& t = bp.targets[d.target];
                     const uint32_t key = r->key;
-                    uint32_t one;
-                    if (single_tile(*r, d, t, bp.tile_shift, one)) put(t.tile_base + one, key);
-                    else for_each_tile<EDGE>(*r, d, t, bp.tile_shift, [&](uint32_t lt) { put(t.tile_base + lt, key); });
+                    // A box of at most eight tiles, to which tile_row_cols gives every tile row the
+                    // box's columns: for_each_tile's tiles are the rectangle of rows [lo, hi] and
+                    // columns [c0, c1].  Their cursor atomics and bin offsets go out together
+                    // (not one tile's round trip after another's), then the keys are stored.
+                    int lo, hi;
+                    record_rows(*r, d, t, lo, hi);
+                    if (lo <= hi) {
+                        const int ty0 = lo >> bp.tile_shift, ty1 = hi >> bp.tile_shift;
+                        int c0, c1;
+                        tile_row_cols<EDGE>(*r, d, t, bp.tile_shift, lo, hi, ty0, c0, c1);
+                        const int n = c1 >= c0 ? (ty1 - ty0 + 1) * (c1 - c0 + 1) : 0;
+                        if (n <= 8) {
+                            uint32_t slot[8];
+                            uint32_t lt = t.tile_base + (uint32_t)ty0 * t.tiles_x + (uint32_t)c0;
+                            const uint32_t row_step = t.tiles_x - (uint32_t)(c1 - c0);
+                            int tx = c0;
+#pragma unroll
+                            for (int k = 0; k < 8; ++k) {
+                                slot[k] = 0;
+                                if (k < n) {
+                                    slot[k] = bp.tile_offset[lt] + atomicAdd(&bp.tile_cursor[lt], 1u);
+                                    if (tx == c1) {
+                                        tx = c0;
+                                        lt += row_step;
+                                    } else {
+                                        ++tx;
+                                        ++lt;
+                                    }
+                                }
+                            }
+#pragma unroll
+                            for (int k = 0; k < 8; ++k)
+                                if (k < n) bp.bins[slot[k]] = key;
+                        } else {  // not reached (the box holds at most eight tiles); kept exact
+                            for_each_tile<EDGE>(*r, d, t, bp.tile_shift, [&](uint32_t lt) { put(t.tile_base + lt, key); });
+                        }
+                    }
                 }
             }
         }
