@@ -35,6 +35,15 @@ def test_library_exports_every_declared_symbol(libgbr):
     assert not missing, missing
 
 
+def test_rust_bindings_declare_every_entry_point():
+    """The shim crate's extern block (wgpu-cpu_gb300/rust/src/sys.rs, source only: no Rust
+    toolchain here) names every entry point the header declares, and nothing else."""
+    sys_rs = open(os.path.join(ROOT, "wgpu-cpu_gb300", "rust", "src", "sys.rs")).read()
+    bound = set(re.findall(r"pub fn (gbr_\w+)\s*\(", sys_rs))
+    declared = set(declared_symbols())
+    assert bound == declared, (sorted(declared - bound), sorted(bound - declared))
+
+
 def test_abi_version(libgbr):
     libgbr.gbr_abi_version.restype = ctypes.c_uint32
     from wgpu_gb300 import _abi as A

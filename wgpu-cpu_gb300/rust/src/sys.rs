@@ -459,7 +459,28 @@ pub struct gbr_buffer_write {
 }
 
 #[link(name = "gbr")]
-unsafe extern "C" {
+unsafe /// Render state of the allocation-free entry point (gbr_render_triangles_noalloc).
+#[repr(C)]
+#[derive(Clone, Copy, Default, Debug)]
+pub struct gbr_noalloc_state {
+    pub cull_mode: u32,
+    pub front_face: u32,
+    pub depth_compare: u32,
+    pub depth_write_enabled: u32,
+    pub color_load_op: u32,
+    pub depth_load_op: u32,
+    pub clear_color: [f32; 4],
+    pub clear_depth: f32,
+    pub _pad: u32,
+}
+
+pub const GBR_NOALLOC_SCRATCH_BYTES: u32 = 24 << 20;
+pub const GBR_NOALLOC_MAX_TRIANGLES: u32 = 32768;
+pub const GBR_NOALLOC_MAX_CLIPPED: u32 = 8192;
+pub const GBR_NOALLOC_MAX_DIM: u32 = 2048;
+pub const GBR_NOALLOC_MAX_BIN_ENTRIES: u32 = 3_800_000;
+
+extern "C" {
     pub fn gbr_last_error(buf: *mut c_char, buf_len: usize) -> usize;
     pub fn gbr_abi_version() -> u32;
     pub fn gbr_device_create(config: *const gbr_device_config, out_device: *mut gbr_device) -> gbr_status;
@@ -548,6 +569,60 @@ unsafe extern "C" {
         device: gbr_device,
         submission_index: u64,
         out_stats: *mut gbr_submission_stats,
+    ) -> gbr_status;
+
+    // extensions, diagnostics and the allocation-free entry point (not behind a wgpu trait)
+    pub fn gbr_shader_module_create_native(
+        device: gbr_device,
+        name: *const c_char,
+        out_module: *mut gbr_shader_module,
+    ) -> gbr_status;
+    pub fn gbr_render_pipeline_eval_vertices(
+        device: gbr_device,
+        pipeline: gbr_render_pipeline,
+        first_vertex: u32,
+        count: u32,
+        out: *mut f32,
+        errors: *mut u32,
+    ) -> gbr_status;
+    pub fn gbr_wgsl_translate(
+        wgsl: *const c_char,
+        wgsl_len: u64,
+        vertex_entry: *const c_char,
+        fragment_entry: *const c_char,
+        out: *mut c_char,
+        capacity: u64,
+        needed: *mut u64,
+    ) -> gbr_status;
+    pub fn gbr_wgsl_compile_check(
+        wgsl: *const c_char,
+        wgsl_len: u64,
+        vertex_entry: *const c_char,
+        fragment_entry: *const c_char,
+        log: *mut c_char,
+        capacity: u64,
+    ) -> gbr_status;
+    pub fn gbr_device_elapsed_ms(
+        device: gbr_device,
+        first_submission: u64,
+        last_submission: u64,
+        out_ms: *mut f64,
+    ) -> gbr_status;
+    pub fn gbr_device_memory(device: gbr_device, out_resident_bytes: *mut u64, out_transient_bytes: *mut u64)
+        -> gbr_status;
+    pub fn gbr_device_flush_caches(device: gbr_device) -> gbr_status;
+    pub fn gbr_selftest_division(samples: u64, seed: u64, out_mismatches: *mut u64, first_mismatch: *mut f32)
+        -> gbr_status;
+    pub fn gbr_render_triangles_noalloc(
+        clip_positions: *const f32,
+        colors: *const f32,
+        triangle_count: u32,
+        color_target: *mut u8,
+        depth_target: *mut f32,
+        width: u32,
+        height: u32,
+        state: *const gbr_noalloc_state,
+        stream: *mut c_void,
     ) -> gbr_status;
 }
 
