@@ -19,14 +19,14 @@ extern template cudaError_t launch_batch_t<true>(const BatchParams&, int, int, i
 
 size_t raster_state_bytes() { return sizeof(RasterState); }
 
-// One block per segment (grid-stride over segments): 16-byte copies where the destination and
-// size allow, else 4-byte, else bytes.
-__global__ void __launch_bounds__(256) k_scatter_writes(const uint8_t* stage, const uint64_t* desc, uint32_t n) {
+// One block per segment (grid-stride over segments): 16-byte copies where the destination, the
+// source and the size allow, else 4-byte, else bytes.
+__global__ void __launch_bounds__(256) k_scatter_writes(const uint64_t* desc, uint32_t n) {
     for (uint32_t seg = blockIdx.x; seg < n; seg += gridDim.x) {
         uint8_t* dst = reinterpret_cast<uint8_t*>(desc[3 * seg]);
-        const uint8_t* src = stage + desc[3 * seg + 1];
+        const uint8_t* src = reinterpret_cast<const uint8_t*>(desc[3 * seg + 1]);
         const uint64_t size = desc[3 * seg + 2];
-        const uintptr_t a = reinterpret_cast<uintptr_t>(dst);
+        const uintptr_t a = reinterpret_cast<uintptr_t>(dst) | reinterpret_cast<uintptr_t>(src);
         if ((a & 15) == 0 && (size & 15) == 0) {
             for (uint64_t k = threadIdx.x; k < size / 16; k += blockDim.x)
                 reinterpret_cast<uint4*>(dst)[k] = reinterpret_cast<const uint4*>(src)[k];
@@ -38,9 +38,9 @@ __global__ void __launch_bounds__(256) k_scatter_writes(const uint8_t* stage, co
         }
     }
 }
-cudaError_t launch_scatter_writes(const uint8_t* stage, const uint64_t* desc, uint32_t n, cudaStream_t s) {
+cudaError_t launch_scatter_writes(const uint64_t* desc, uint32_t n, cudaStream_t s) {
     if (!n) return cudaSuccess;
-    k_scatter_writes<<<n < 1024u ? n : 1024u, 256, 0, s>>>(stage, desc, n);
+    k_scatter_writes<<<n < 1024u ? n : 1024u, 256, 0, s>>>(desc, n);
     return cudaGetLastError();
 }
 

@@ -38,9 +38,9 @@ uint32_t fast_vs_vcount(const DrawDesc& d);
 // 1 when the fast setup can read each vertex of the draw with 8- or 16-byte loads (DrawDesc::fast_packed).
 uint32_t fast_vs_packed(const DrawDesc& d);
 
-// Places n coalesced writes: segment k copies desc[3k + 2] bytes from stage + desc[3k + 1] to the
-// device address desc[3k] (stage offsets are 16-byte aligned).
-cudaError_t launch_scatter_writes(const uint8_t* stage, const uint64_t* desc, uint32_t n, cudaStream_t s);
+// Places n coalesced write segments: segment k copies desc[3k + 2] bytes from the device address
+// desc[3k + 1] to the device address desc[3k]; the segments do not overlap.
+cudaError_t launch_scatter_writes(const uint64_t* desc, uint32_t n, cudaStream_t s);
 
 // Copies of device textures into host memory the device can address (pinned, mapped): up to
 // kCopyOutMax per launch, every source and destination 16-byte aligned.  All SMs take part in

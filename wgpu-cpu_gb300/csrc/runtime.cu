@@ -984,26 +984,28 @@ std::vector<Item> Device::pop_group_locked() {
             queue.pop_front();
             // continuous batching: the submissions queued behind this one join its launch while
             // their expected transient memory fits the HBM budget (the rest wait for the next)
-            // a run of small host-side buffer writes (per-draw uniforms and the like) goes up as
-            // one copy and one scatter kernel, still in queue order
+            // a run of buffer writes (per-draw uniforms, meshes and the like) is placed by one
+            // scatter kernel, still in queue order: the host-side bytes go up as one copy, the
+            // device-staged ones are copied from their staging
             // (a write overlapping an earlier one of the run ends it: the scatter kernel places
             // segments concurrently, and the later bytes must win)
-            if (group[0].kind == Item::WRITE_BUFFER && !group[0].staged) {
-                uint64_t bytes = group[0].data.size();
+            if (group[0].kind == Item::WRITE_BUFFER) {
+                auto host_bytes = [](const Item& it) { return it.staged ? uint64_t(0) : (uint64_t)it.data.size(); };
+                uint64_t bytes = host_bytes(group[0]);
                 std::map<uint64_t, uint64_t> spans;  // destination [begin, end) of the run's writes
                 auto span_of = [](const Item& it) {
                     const uint64_t b = reinterpret_cast<uint64_t>(it.buffer->ptr) + it.offset;
-                    return std::make_pair(b, b + it.data.size());
+                    return std::make_pair(b, b + (it.staged ? it.staged_size : (uint64_t)it.data.size()));
                 };
                 spans.insert(span_of(group[0]));
-                while (!queue.empty() && queue.front().kind == Item::WRITE_BUFFER && !queue.front().staged &&
-                       group.size() < kMaxCoalescedWrites && bytes + queue.front().data.size() <= kMaxCoalescedBytes) {
+                while (!queue.empty() && queue.front().kind == Item::WRITE_BUFFER &&
+                       group.size() < kMaxCoalescedWrites && bytes + host_bytes(queue.front()) <= kMaxCoalescedBytes) {
                     const auto sp = span_of(queue.front());
                     auto next = spans.lower_bound(sp.first);
                     if (next != spans.end() && next->first < sp.second) break;
                     if (next != spans.begin() && std::prev(next)->second > sp.first) break;
                     spans.insert(sp);
-                    bytes += queue.front().data.size();
+                    bytes += host_bytes(queue.front());
                     group.push_back(std::move(queue.front()));
                     queue.pop_front();
                 }
@@ -1085,15 +1087,22 @@ void Device::lookahead() {
     }
 }
 
-// Coalesced buffer writes: every segment copied into one pinned block (16-byte aligned offsets,
-// the segment table after them), one upload copy into device scratch, one scatter kernel.
+// Coalesced buffer writes: the host-side bytes copied into one pinned block (16-byte aligned
+// offsets, the segment table after them) and uploaded into device scratch with one copy; one
+// scatter kernel then places every write, from that scratch or from the write's device staging,
+// cut into pieces of kScatterPiece bytes so that many blocks share a large write.
+constexpr uint64_t kScatterPiece = 64u << 10;
 void Device::execute_writes(std::vector<Item>& items) {
     try {
         if (lost) fail(GBR_ERR_DEVICE_LOST, "device lost: %s", lost_msg.c_str());
-        const uint32_t n = (uint32_t)items.size();
-        uint64_t data_bytes = 0;
-        for (const Item& it : items) data_bytes += (it.data.size() + 15) & ~uint64_t(15);
-        const uint64_t total = data_bytes + (uint64_t)n * 3 * sizeof(uint64_t);
+        auto size_of = [](const Item& it) { return it.staged ? it.staged_size : (uint64_t)it.data.size(); };
+        uint64_t data_bytes = 0, nseg = 0;
+        for (const Item& it : items) {
+            if (!it.staged) data_bytes += (it.data.size() + 15) & ~uint64_t(15);
+            nseg += (size_of(it) + kScatterPiece - 1) / kScatterPiece;
+        }
+        if (nseg > UINT32_MAX) fail(GBR_ERR_UNSUPPORTED, "too many write segments");
+        const uint64_t total = data_bytes + nseg * 3 * sizeof(uint64_t);
         PinnedStage& ps = pinned_stage[pinned_next];
         pinned_next ^= 1;
         if (ps.done) cuda_check(cudaEventSynchronize(ps.done), "pinned staging reuse");
@@ -1107,21 +1116,33 @@ void Device::execute_writes(std::vector<Item>& items) {
             ps.size = want;
         }
         upload_buf.ensure(total, &scratch_bytes);
+        const uint64_t dev_stage = reinterpret_cast<uint64_t>(upload_buf.ptr);
         uint64_t* desc = reinterpret_cast<uint64_t*>(ps.ptr + data_bytes);
-        uint64_t off = 0;
-        for (uint32_t k = 0; k < n; ++k) {
-            const Item& it = items[k];
-            std::memcpy(ps.ptr + off, it.data.data(), it.data.size());
-            desc[3 * k] = reinterpret_cast<uint64_t>(it.buffer->ptr + it.offset);
-            desc[3 * k + 1] = off;
-            desc[3 * k + 2] = it.data.size();
-            off += (it.data.size() + 15) & ~uint64_t(15);
+        uint64_t off = 0, s = 0;
+        for (const Item& it : items) {
+            const uint64_t size = size_of(it);
+            uint64_t src = reinterpret_cast<uint64_t>(it.staged);
+            if (!it.staged) {
+                std::memcpy(ps.ptr + off, it.data.data(), size);
+                src = dev_stage + off;
+                off += (size + 15) & ~uint64_t(15);
+            }
+            const uint64_t dst = reinterpret_cast<uint64_t>(it.buffer->ptr + it.offset);
+            for (uint64_t p = 0; p < size; p += kScatterPiece, ++s) {
+                desc[3 * s] = dst + p;
+                desc[3 * s + 1] = src + p;
+                desc[3 * s + 2] = std::min(kScatterPiece, size - p);
+            }
         }
         cuda_check(cudaMemcpyAsync(upload_buf.ptr, ps.ptr, total, cudaMemcpyHostToDevice, stream), "coalesced writes");
         cuda_check(cudaEventRecord(ps.done, stream), "cudaEventRecord");
-        const uint8_t* stage = static_cast<const uint8_t*>(upload_buf.ptr);
-        cuda_check(launch_scatter_writes(stage, reinterpret_cast<const uint64_t*>(stage + data_bytes), n, stream),
+        cuda_check(launch_scatter_writes(reinterpret_cast<const uint64_t*>(dev_stage + data_bytes), (uint32_t)nseg, stream),
                    "scatter writes");
+        for (Item& it : items)  // stream-ordered after the kernel that reads them
+            if (it.staged) {
+                cuda_check(cudaFreeAsync(it.staged, stream), "write_buffer staging");
+                it.staged = nullptr;
+            }
     } catch (const Failure& f) {
         note_failure(f);
     }
