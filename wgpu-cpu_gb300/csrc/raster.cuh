@@ -1349,11 +1349,19 @@ __global__ void __launch_bounds__(1024) k_scan(BatchParams bp) {
         s_heavy = 0;
     }
     __syncthreads();
+    // the counts of a chunk are loaded while the chunk before it is scanned
+    uint32_t ahead[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+        const uint32_t i = tid + j * 1024;
+        ahead[j] = i < n ? bp.tile_count[i] : 0u;
+    }
     for (uint32_t base = 0; base < n; base += 4096) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
-            const uint32_t i = base + tid + j * 1024;
-            buf[tid + j * 1024] = i < n ? bp.tile_count[i] : 0u;
+            buf[tid + j * 1024] = ahead[j];
+            const uint32_t i = base + 4096 + tid + j * 1024;
+            ahead[j] = i < n ? bp.tile_count[i] : 0u;
         }
         __syncthreads();
         const uint32_t a0 = buf[4 * tid], a1 = buf[4 * tid + 1], a2 = buf[4 * tid + 2], a3 = buf[4 * tid + 3];
