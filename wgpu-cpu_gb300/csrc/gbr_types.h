@@ -291,6 +291,7 @@ struct BatchParams {
     const uint32_t* shape_groups;
     uint32_t sg_off[8];
     const uint32_t* draw_base;   // [num_draws] prim_base of each draw, contiguous (null: read the descriptors)
+    uint32_t slow_builds_states; // k_setup_slow also builds the visibility raster's per-draw states
 };
 
 }  // namespace gbr

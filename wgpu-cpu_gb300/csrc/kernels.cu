@@ -147,10 +147,10 @@ bool raster_config_supported(int tile, int warps) {
 uint32_t batch_kernel_launches(uint32_t total_prims, int tile, int warps, int kind, uint32_t fvs_mask) {
     if (kind == 3 && !launch_detail::vis_config_supported(tile, warps)) kind = 0;
     // scan + raster, one setup launch per FastVs shape (one when unknown) + generic setup + fill
-    // when there are primitives, the states of the visibility raster (the strip table is counted
-    // by the caller)
+    // when there are primitives, the states of the visibility raster when there are none (the
+    // generic setup builds them otherwise; the strip table is counted by the caller)
     const uint32_t setups = fvs_mask ? (uint32_t)__builtin_popcount(fvs_mask) : 1u;
-    return 2u + (total_prims ? setups + 2u : 0u) + (kind == 3 ? 1u : 0u);
+    return 2u + (total_prims ? setups + 2u : 0u) + (kind == 3 && !total_prims ? 1u : 0u);
 }
 
 uint32_t fast_vs_kind(const DrawDesc& d) {

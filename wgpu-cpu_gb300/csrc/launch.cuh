@@ -159,9 +159,13 @@ cudaError_t launch_batch_t(const BatchParams& bp, int tile, int warps, int num_s
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         ++*launches;
     }
+    // with primitives, the generic setup also builds the visibility raster's states
+    const bool slow_states = kind == 3 && items;
     if (items) {
         if ((e = launch_setups<EDGE>(bp, num_sms, s, launches)) != cudaSuccess) return e;
-        k_setup_slow<EDGE><<<std::min((items + 127) / 128, (uint32_t)num_sms * 4), 128, 0, s>>>(bp);
+        BatchParams sp = bp;
+        sp.slow_builds_states = slow_states ? 1u : 0u;
+        k_setup_slow<EDGE><<<std::min((items + 127) / 128, (uint32_t)num_sms * 4), 128, 0, s>>>(sp);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         ++*launches;
     }
@@ -182,7 +186,7 @@ cudaError_t launch_batch_t(const BatchParams& bp, int tile, int warps, int num_s
         if ((e = cudaStreamIsCapturing(s, &cs)) != cudaSuccess) return e;
         if (cs == cudaStreamCaptureStatusActive) ev_flags = cudaEventRecordExternal;
     }
-    if (kind == 3) {
+    if (kind == 3 && !slow_states) {
         k_build_states<><<<(bp.num_draws + 127) / 128, 128, 0, s>>>(bp);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
         ++*launches;

@@ -882,6 +882,13 @@ __global__ void __launch_bounds__(128) k_setup_slow(BatchParams bp) {
     const uint32_t n = bp.status->slow_count;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31;
+    if (bp.slow_builds_states) {
+        // the visibility raster's per-draw states (k_build_states' work), by the grid's last
+        // threads, which the queued primitives reach last if at all
+        RasterState* states = static_cast<RasterState*>(bp.states);
+        const uint32_t rt = stride - 1 - (blockIdx.x * blockDim.x + threadIdx.x);
+        for (uint32_t i = rt; i < bp.num_draws; i += stride) build_raster_state(bp.draws[i], i, states[i]);
+    }
     for (uint32_t base = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < n; base += stride) {
         if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the warp
         const TriRecord* coop = nullptr;
