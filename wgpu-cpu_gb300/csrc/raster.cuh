@@ -1199,9 +1199,9 @@ __global__ void __launch_bounds__(kSetupWarps * 32) k_setup(BatchParams bp) {
     if (*bp.abort_flag) return;  // written only by earlier kernels: uniform across the grid
 
     // the draw's descriptor, matrix and target to the warp's cache (warp-uniform).  A warp's
-    // groups lie a grid apart, so nearly every group changes draws: every load of a round issues
-    // before any is used, and the copy costs two dependent loads (the descriptor with the matrix's
-    // address and the target's index, then the matrix and the target)
+    // groups lie a grid apart, so nearly every group changes draws: the loads of each step issue
+    // together before any is used, so the copy costs two dependent loads (the descriptor with the
+    // matrix's address and the target's index, then the matrix and the target)
     auto cache_draw = [&](uint32_t di) {
         constexpr uint32_t NQ = sizeof(DrawDesc) / 16, NR = (NQ + 31) / 32, NT = sizeof(TargetDesc) / 8;
         const uint4* src = reinterpret_cast<const uint4*>(bp.draws + di);
