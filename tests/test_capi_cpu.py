@@ -44,6 +44,48 @@ def test_rust_bindings_declare_every_entry_point():
     assert bound == declared, (sorted(declared - bound), sorted(bound - declared))
 
 
+_C_SCALARS = {"char": "c_char", "void": "c_void", "uint8_t": "u8", "uint16_t": "u16", "uint32_t": "u32",
+              "uint64_t": "u64", "int32_t": "i32", "int64_t": "i64", "float": "f32", "double": "f64"}
+
+
+def _header_structs():
+    """{struct: [(field, Rust spelling of its C type)]} of every typedef struct in gbr.h."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"typedef struct (gbr_\w+)\s*\{(.*?)\}\s*\1\s*;", text, flags=re.S):
+        fields = []
+        for decl in (" ".join(d.split()) for d in m.group(2).split(";")):
+            if not decl:
+                continue
+            tm = re.match(r"^(const\s+)?(u?int\d+_t|float|double|char|void|gbr_\w+)\s*(.+)$", decl)
+            const, base, rest = tm.group(1), tm.group(2), tm.group(3)
+            for d in rest.split(","):
+                d = d.strip()
+                stars = len(d) - len(d.lstrip("*"))
+                dm = re.match(r"(\w+)\s*((?:\[[^\]]+\])*)$", d.lstrip("*").strip())
+                t = _C_SCALARS.get(base, base)
+                if stars:
+                    t = ("*const " if const else "*mut ") + t
+                for n in reversed(re.findall(r"\[([^\]]+)\]", dm.group(2))):
+                    t = f"[{t}; {n}]"
+                fields.append((dm.group(1), t.replace(" ", "")))
+        out[m.group(1)] = fields
+    return out
+
+
+def test_rust_structs_match_header():
+    """Every #[repr(C)] struct of the shim crate's sys.rs has the header struct's fields, in order,
+    with the same types (the crate cannot be compiled here, so its layout is checked as text)."""
+    text = re.sub(r"//[^\n]*", "", open(os.path.join(ROOT, "wgpu-cpu_gb300", "rust", "src", "sys.rs")).read())
+    rust = {}
+    for m in re.finditer(r"pub struct (gbr_\w+)\s*\{(.*?)\n\}", text, flags=re.S):
+        rust[m.group(1)] = [(f, t.replace(" ", "")) for f, t in re.findall(r"pub (\w+):\s*([^,\n]+),", m.group(2))]
+    header = _header_structs()
+    assert len(header) >= 30 and set(rust) == set(header), (sorted(set(header) ^ set(rust)))
+    bad = {k: (header[k], rust[k]) for k in header if header[k] != rust[k]}
+    assert not bad, bad
+
+
 def test_abi_version(libgbr):
     libgbr.gbr_abi_version.restype = ctypes.c_uint32
     from wgpu_gb300 import _abi as A
