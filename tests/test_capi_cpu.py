@@ -86,6 +86,32 @@ def test_rust_structs_match_header():
     assert not bad, bad
 
 
+def test_rust_enum_conversions_match_header():
+    """The shim crate's wgpu -> gbr enum conversions (literal codes in lib.rs) give each wgpu
+    variant the value of the header enumerator of the same name."""
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    values = {k: int(v) for k, v in re.findall(r"\b(GBR_\w+)\s*=\s*(-?\d+)\b", text)}
+    lib = open(os.path.join(ROOT, "wgpu-cpu_gb300", "rust", "src", "lib.rs")).read()
+    prefixes = {"texture_format": "GBR_TEXTURE_FORMAT_", "vertex_format": "GBR_VERTEX_FORMAT_",
+                "index_format": "GBR_INDEX_", "topology": "GBR_TOPOLOGY_", "compare": "GBR_COMPARE_",
+                "blend_factor": "GBR_BLEND_", "blend_component": "GBR_BLEND_OP_", "address_mode": "GBR_ADDRESS_",
+                "filter": "GBR_FILTER_", "mipmap_filter": "GBR_FILTER_"}
+    none_names = {"index_format": "GBR_INDEX_NONE", "compare": "GBR_COMPARE_UNDEFINED"}
+    snake = lambda v: re.sub(r"(?<=[a-z0-9])(?=[A-Z])", "_", v).upper()
+    checked, bad = 0, []
+    for fn, prefix in prefixes.items():
+        body = re.search(r"\nfn " + fn + r"\(.*?\n\}\n", lib, flags=re.S)
+        assert body, fn
+        arms = re.findall(r"(?:Some\()?(?:[\w:]*::)?(\w+)\)?\s*=>\s*(\d+),", body.group(0))
+        assert arms, fn
+        for variant, code in arms:
+            name = none_names[fn] if variant == "None" else prefix + snake(variant)
+            checked += 1
+            if values.get(name) != int(code):
+                bad.append((fn, variant, name, values.get(name), int(code)))
+    assert checked >= 60 and not bad, (checked, bad)
+
+
 def test_abi_version(libgbr):
     libgbr.gbr_abi_version.restype = ctypes.c_uint32
     from wgpu_gb300 import _abi as A
