@@ -112,6 +112,29 @@ def test_rust_enum_conversions_match_header():
     assert checked >= 60 and not bad, (checked, bad)
 
 
+def test_python_enums_match_header():
+    """The ctypes mirror's enum classes (wgpu_gb300.api) hold the header enumerators' values."""
+    from wgpu_gb300 import api as W
+
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    values = {k: int(v) for k, v in re.findall(r"\b(GBR_\w+)\s*=\s*(-?\d+)\b", text)}
+    prefixes = {W.TextureFormat: "GBR_TEXTURE_FORMAT_", W.VertexFormat: "GBR_VERTEX_FORMAT_",
+                W.VertexStepMode: "GBR_STEP_", W.IndexFormat: "GBR_INDEX_", W.PrimitiveTopology: "GBR_TOPOLOGY_",
+                W.FrontFace: "GBR_FRONT_FACE_", W.Face: "GBR_CULL_", W.CompareFunction: "GBR_COMPARE_",
+                W.BlendFactor: "GBR_BLEND_", W.BlendOperation: "GBR_BLEND_OP_", W.AddressMode: "GBR_ADDRESS_",
+                W.FilterMode: "GBR_FILTER_", W.LoadOp: "GBR_LOAD_OP_", W.Profile: "GBR_PROFILE_",
+                W.LaunchMode: "GBR_LAUNCH_", W.RasterOrder: "GBR_RASTER_", W.RasterRule: "GBR_RASTER_RULE_"}
+    checked, bad = 0, []
+    for cls, prefix in prefixes.items():
+        for name, v in vars(cls).items():
+            if name.startswith("_") or not isinstance(v, int):
+                continue
+            checked += 1
+            if values.get(prefix + name) != v:
+                bad.append((cls.__name__, name, prefix + name, values.get(prefix + name), v))
+    assert checked >= 70 and not bad, (checked, bad)
+
+
 def test_abi_version(libgbr):
     libgbr.gbr_abi_version.restype = ctypes.c_uint32
     from wgpu_gb300 import _abi as A
