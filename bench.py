@@ -577,7 +577,8 @@ def run_ours(args, wk: Workload):
                          "frac": achieved / peak if achieved else None,
                          "traffic": prof.get("dram_bytes_per_launch") if not over else None,
                          "peak_source": peak_src, "kernel": prof.get("kernel", "raster kernel (k_raster_vis or k_raster)"),
-                         "algorithmic_bytes_per_launch": ab["total"], "byte_model": ab, "kernel_ms": r_ms},
+                         "algorithmic_bytes_per_launch": ab["total"], "byte_model": ab, "kernel_ms": r_ms,
+                         **({"note": prof["note"]} if prof.get("note") and not over else {})},
             "cpu_baseline": base,
             "e2e": {"value": e2e_rate, "unit": UNIT, "h2d_bytes_per_step": int(h2d) * world,
                     "d2h_bytes_per_step": int(out_bytes) * world, "ms_per_step": e2e_s * 1e3,
